@@ -1,0 +1,417 @@
+/* cholmod_gb300.h -- GB300 (sm_103a) supernodal numeric Cholesky behind the
+ * CHOLMOD C API.
+ *
+ * Two groups of declarations:
+ *
+ * 1. The CHOLMOD objects this library reads and writes (cholmod_common,
+ *    cholmod_sparse, cholmod_factor, cholmod_dense) and the three CHOLMOD
+ *    entry points it replaces.  The struct layouts must be byte-identical to
+ *    CHOLMOD 5.3 built for int64 (cholmod_l_*) so that a program linked
+ *    against the reference CHOLMOD can pass its own objects to this library:
+ *    every member below has the type and position of the member of the same
+ *    name in CHOLMOD/Include/cholmod.h (cholmod_common :501-999,
+ *    cholmod_sparse :1168-1206, cholmod_factor :1539-1653, cholmod_dense
+ *    :1802-1813), and tests/test_abi.py checks every offset against that
+ *    header when the reference sources are present.  When this header and
+ *    cholmod.h are both visible in one translation unit, include cholmod.h
+ *    only (define CHOLMOD_GB300_USE_CHOLMOD_H before including this file).
+ *
+ * 2. gb300_* extensions: the host-side drivers a standalone program needs
+ *    (symbolic analysis from a given permutation, the factorize/solve
+ *    wrappers), the FP32-factor + FP64-refinement solver, and plain-pointer
+ *    entry points for foreign-function callers.
+ *
+ * All functions are extern "C", take plain pointers and sizes, and report
+ * errors the CHOLMOD way: TRUE/FALSE or NULL return, Common->status set,
+ * Common->error_handler called unless Common->try_catch.
+ */
+#ifndef CHOLMOD_GB300_H
+#define CHOLMOD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef CHOLMOD_GB300_USE_CHOLMOD_H
+
+/* ---- constants with the reference's values (cholmod.h) ---------------- */
+#define CHOLMOD_PATTERN 0
+#define CHOLMOD_REAL    1
+#define CHOLMOD_COMPLEX 2
+#define CHOLMOD_ZOMPLEX 3
+#define CHOLMOD_DOUBLE  0
+#define CHOLMOD_SINGLE  4
+#define CHOLMOD_INT     0
+#define CHOLMOD_LONG    2
+
+#define CHOLMOD_OK            (0)
+#define CHOLMOD_NOT_INSTALLED (-1)
+#define CHOLMOD_OUT_OF_MEMORY (-2)
+#define CHOLMOD_TOO_LARGE     (-3)
+#define CHOLMOD_INVALID       (-4)
+#define CHOLMOD_GPU_PROBLEM   (-5)
+#define CHOLMOD_NOT_POSDEF    (1)
+#define CHOLMOD_DSMALL        (2)
+
+#define CHOLMOD_SIMPLICIAL 0
+#define CHOLMOD_AUTO       1
+#define CHOLMOD_SUPERNODAL 2
+
+#define CHOLMOD_NATURAL     0
+#define CHOLMOD_GIVEN       1
+#define CHOLMOD_AMD         2
+#define CHOLMOD_METIS       3
+#define CHOLMOD_NESDIS      4
+#define CHOLMOD_COLAMD      5
+#define CHOLMOD_POSTORDERED 6
+#define CHOLMOD_MAXMETHODS  9
+
+#define CHOLMOD_A    0
+#define CHOLMOD_LDLt 1
+#define CHOLMOD_LD   2
+#define CHOLMOD_DLt  3
+#define CHOLMOD_L    4
+#define CHOLMOD_Lt   5
+#define CHOLMOD_D    6
+#define CHOLMOD_P    7
+#define CHOLMOD_Pt   8
+
+#define CHOLMOD_HOST_SUPERNODE_BUFFERS 8
+
+/* ---- cholmod_common: parameters, statistics, workspace ----------------- */
+typedef struct cholmod_common_struct
+{
+    double dbound ;
+    double grow0 ;
+    double grow1 ;
+    size_t grow2 ;
+    size_t maxrank ;
+    double supernodal_switch ;
+    int supernodal ;
+    int final_asis ;
+    int final_super ;
+    int final_ll ;
+    int final_pack ;
+    int final_monotonic ;
+    int final_resymbol ;
+    double zrelax [3] ;
+    size_t nrelax [3] ;
+    int prefer_zomplex ;
+    int prefer_upper ;
+    int quick_return_if_not_posdef ;
+    int prefer_binary ;
+    int print ;
+    int precise ;
+    int try_catch ;
+    void (*error_handler) (int status, const char *file, int line,
+        const char *message) ;
+    int nmethods ;
+    int current ;
+    int selected ;
+    struct cholmod_method_struct
+    {
+        double lnz ;
+        double fl ;
+        double prune_dense ;
+        double prune_dense2 ;
+        double nd_oksep ;
+        double other_1 [4] ;
+        size_t nd_small ;
+        double other_2 [4] ;
+        int aggressive ;
+        int order_for_lu ;
+        int nd_compress ;
+        int nd_camd ;
+        int nd_components ;
+        int ordering ;
+        size_t other_3 [4] ;
+    } method [CHOLMOD_MAXMETHODS + 1] ;
+    int postorder ;
+    int default_nesdis ;
+    double metis_memory ;
+    double metis_dswitch ;
+    size_t metis_nswitch ;
+    size_t nrow ;
+    int64_t mark ;
+    size_t iworksize ;
+    size_t xworkbytes ;
+    void *Flag ;
+    void *Head ;
+    void *Xwork ;
+    void *Iwork ;
+    int itype ;
+    int other_5 ;
+    int no_workspace_reallocate ;
+    int status ;
+    double fl ;
+    double lnz ;
+    double anz ;
+    double modfl ;
+    size_t malloc_count ;
+    size_t memory_usage ;
+    size_t memory_inuse ;
+    double nrealloc_col ;
+    double nrealloc_factor ;
+    double ndbounds_hit ;
+    double rowfacfl ;
+    double aatfl ;
+    int called_nd ;
+    int blas_ok ;
+    double SPQR_grain ;
+    double SPQR_small ;
+    int SPQR_shrink ;
+    int SPQR_nthreads ;
+    double SPQR_flopcount ;
+    double SPQR_analyze_time ;
+    double SPQR_factorize_time ;
+    double SPQR_solve_time ;
+    double SPQR_flopcount_bound ;
+    double SPQR_tol_used ;
+    double SPQR_norm_E_fro ;
+    int64_t SPQR_istat [8] ;
+    double nsbounds_hit ;
+    float sbound ;
+    float other_6 ;
+    int useGPU ;
+    size_t maxGpuMemBytes ;
+    double maxGpuMemFraction ;
+    size_t gpuMemorySize ;
+    double gpuKernelTime ;
+    int64_t gpuFlops ;
+    int gpuNumKernelLaunches ;
+    void *cublasHandle ;
+    void *gpuStream [CHOLMOD_HOST_SUPERNODE_BUFFERS] ;
+    void *cublasEventPotrf [3] ;
+    void *updateCKernelsComplete ;
+    void *updateCBuffersFree [CHOLMOD_HOST_SUPERNODE_BUFFERS] ;
+    void *dev_mempool ;
+    size_t dev_mempool_size ;
+    void *host_pinned_mempool ;
+    size_t host_pinned_mempool_size ;
+    size_t devBuffSize ;
+    int    ibuffer ;
+    double syrkStart ;
+    double cholmod_cpu_gemm_time ;
+    double cholmod_cpu_syrk_time ;
+    double cholmod_cpu_trsm_time ;
+    double cholmod_cpu_potrf_time ;
+    double cholmod_gpu_gemm_time ;
+    double cholmod_gpu_syrk_time ;
+    double cholmod_gpu_trsm_time ;
+    double cholmod_gpu_potrf_time ;
+    double cholmod_assemble_time ;
+    double cholmod_assemble_time2 ;
+    size_t cholmod_cpu_gemm_calls ;
+    size_t cholmod_cpu_syrk_calls ;
+    size_t cholmod_cpu_trsm_calls ;
+    size_t cholmod_cpu_potrf_calls ;
+    size_t cholmod_gpu_gemm_calls ;
+    size_t cholmod_gpu_syrk_calls ;
+    size_t cholmod_gpu_trsm_calls ;
+    size_t cholmod_gpu_potrf_calls ;
+    double chunk ;
+    int nthreads_max ;
+} cholmod_common ;
+
+/* ---- cholmod_sparse: compressed-column matrix -------------------------- */
+typedef struct cholmod_sparse_struct
+{
+    size_t nrow ;
+    size_t ncol ;
+    size_t nzmax ;
+    void *p ;       /* column pointers, size ncol+1 */
+    void *i ;       /* row indices, size nzmax */
+    void *nz ;      /* column counts if unpacked */
+    void *x ;       /* values */
+    void *z ;
+    int stype ;     /* 0 unsymmetric, >0 upper stored, <0 lower stored */
+    int itype ;
+    int xtype ;
+    int dtype ;
+    int sorted ;
+    int packed ;
+} cholmod_sparse ;
+
+/* ---- cholmod_factor: the supernodal layout consumed and produced ------- *
+ * super[nsuper+1]: first column of each supernode; pi[nsuper+1]: start of
+ * each supernode's row list in s; px[nsuper+1]: start of each supernode's
+ * values in x; s[ssize]: row indices (the first nscol rows of supernode s are
+ * its own columns super[s]..super[s+1]-1); x[xsize]: values, supernode s is
+ * an nsrow-by-nscol column-major block with leading dimension nsrow.       */
+typedef struct cholmod_factor_struct
+{
+    size_t n ;
+    size_t minor ;
+    void *Perm ;
+    void *ColCount ;
+    void *IPerm ;
+    size_t nzmax ;
+    void *p ;
+    void *i ;
+    void *x ;
+    void *z ;
+    void *nz ;
+    void *next ;
+    void *prev ;
+    size_t nsuper ;
+    size_t ssize ;
+    size_t xsize ;
+    size_t maxcsize ;
+    size_t maxesize ;
+    void *super ;
+    void *pi ;
+    void *px ;
+    void *s ;
+    int ordering ;
+    int is_ll ;
+    int is_super ;
+    int is_monotonic ;
+    int itype ;
+    int xtype ;
+    int dtype ;
+    int useGPU ;
+} cholmod_factor ;
+
+/* ---- cholmod_dense: column-major dense matrix --------------------------- */
+typedef struct cholmod_dense_struct
+{
+    size_t nrow ;
+    size_t ncol ;
+    size_t nzmax ;
+    size_t d ;
+    void *x ;
+    void *z ;
+    int xtype ;
+    int dtype ;
+} cholmod_dense ;
+
+#endif /* CHOLMOD_GB300_USE_CHOLMOD_H */
+
+/* ======================================================================== *
+ * 1. Drop-in boundary: the CHOLMOD entry points this library replaces.     *
+ * ======================================================================== */
+
+/* Supernodal numeric LL' of A+beta*I (A = tril(PAP'), stype < 0) on the GPU.
+ * Replaces CHOLMOD/Supernodal/cholmod_super_numeric.c:100-335 (declared at
+ * CHOLMOD/Include/cholmod.h:4016-4027); called by cholmod_l_factorize_p at
+ * CHOLMOD/Cholesky/cholmod_factorize.c:260.  Same contract: L symbolic or
+ * numeric supernodal on input, numeric on output with L->x filled (unless
+ * the factor is kept device-resident, see gb300_set_option), is_ll = TRUE,
+ * L->minor = n on success.  Not positive definite: returns TRUE with
+ * Common->status = CHOLMOD_NOT_POSDEF, L->minor = the failing column, that
+ * supernode factorized only up to the failing column and all later
+ * supernodes zero (quick_return_if_not_posdef: the failing supernode is
+ * left zero).  Real double and real single are supported; complex/zomplex
+ * input and the unsymmetric A*F form return FALSE with CHOLMOD_INVALID. */
+int cholmod_l_super_numeric (cholmod_sparse *A, cholmod_sparse *F,
+    double beta [2], cholmod_factor *L, cholmod_common *Common) ;
+
+/* Forward supernodal solve X = L\X on the GPU.  Replaces
+ * CHOLMOD/Supernodal/cholmod_super_solve.c:52-139 (cholmod.h:4037); called by
+ * cholmod_l_solve2 at CHOLMOD/Cholesky/cholmod_solve.c:698.  X is n-by-nrhs
+ * with leading dimension X->d; E must be at least nrhs*L->maxesize entries
+ * (checked as in the reference, not otherwise used). */
+int cholmod_l_super_lsolve (cholmod_factor *L, cholmod_dense *X,
+    cholmod_dense *E, cholmod_common *Common) ;
+
+/* Backward supernodal solve X = L'\X on the GPU.  Replaces
+ * CHOLMOD/Supernodal/cholmod_super_solve.c:153-240 (cholmod.h:4058); called
+ * by cholmod_l_solve2 at CHOLMOD/Cholesky/cholmod_solve.c:699. */
+int cholmod_l_super_ltsolve (cholmod_factor *L, cholmod_dense *X,
+    cholmod_dense *E, cholmod_common *Common) ;
+
+/* ======================================================================== *
+ * 2. gb300_* extensions.                                                    *
+ * ======================================================================== */
+
+/* Initialise a cholmod_common with CHOLMOD's default parameter values for
+ * the fields this library reads (cholmod_l_start / cholmod_l_defaults,
+ * CHOLMOD/Utility/t_cholmod_defaults.c:43-124).  For programs without the
+ * reference library.  gb300_finish releases this library's device state
+ * attached to Common. */
+int gb300_start (cholmod_common *Common) ;
+int gb300_finish (cholmod_common *Common) ;
+
+/* Options (defaults in brackets):
+ *  GB300_OPT_KEEP_ON_DEVICE [0]: 1 = do not copy L->x back to the host after
+ *      the factorization; the factor stays resident on the GPU for solves.
+ *  GB300_OPT_SMALL_COLS [64]: supernodes at most this wide are factorized by
+ *      one thread block each; wider ones by the blocked multi-block path. */
+#define GB300_OPT_KEEP_ON_DEVICE 1
+#define GB300_OPT_SMALL_COLS     2
+int gb300_set_option (cholmod_common *Common, int option, int64_t value) ;
+
+/* Supernodal symbolic analysis of A (stype < 0, lower) with a given final
+ * (already postordered) permutation Perm: elimination tree, column counts,
+ * fundamental supernodes, relaxed amalgamation and the row pattern L->s,
+ * following CHOLMOD/Supernodal/cholmod_super_symbolic.c:147-938 with the
+ * nrelax/zrelax parameters of Common.  Produces the factor cholmod_analyze
+ * returns when its selected ordering ends in Perm (the weighted postorder of
+ * cholmod_analyze.c:828-880 is already applied to Perm).  Sets Common->fl,
+ * Common->lnz, Common->anz as cholmod_rowcolcounts does.  NULL on error. */
+cholmod_factor *gb300_analyze_perm (cholmod_sparse *A, const int64_t *Perm,
+    cholmod_common *Common) ;
+
+/* S = tril(A(p,p)) then cholmod_l_super_numeric: the supernodal branch of
+ * cholmod_l_factorize_p (CHOLMOD/Cholesky/cholmod_factorize.c:172-283) for a
+ * symmetric-lower A.  beta may be NULL (zero). */
+int gb300_factorize (cholmod_sparse *A, double beta [2], cholmod_factor *L,
+    cholmod_common *Common) ;
+
+/* X = A\B through L: Y = P*B, cholmod_l_super_lsolve, cholmod_l_super_ltsolve,
+ * X = P'*Y (the supernodal branch of cholmod_l_solve2,
+ * CHOLMOD/Cholesky/cholmod_solve.c:656-724).  sys must be CHOLMOD_A.
+ * Returns a new dense X (free with gb300_free_dense) or NULL. */
+cholmod_dense *gb300_solve (int sys, cholmod_factor *L, cholmod_dense *B,
+    cholmod_common *Common) ;
+
+/* FP32 factor + FP64 iterative refinement.  gb300_factorize_mixed computes an
+ * FP32 supernodal factor of D*A*D (D = diag(A)^-1/2, symmetric diagonal
+ * scaling applied per supernode during assembly) and keeps it on the GPU;
+ * L->x is not written.  gb300_solve_refined solves A X = B in FP64 to the
+ * backward error tol (|b-Ax|_inf / (|A|_inf |x|_inf + |b|_inf) per column)
+ * with the residual SpMV and the update in FP64 on the GPU; when refinement
+ * stalls (no residual reduction in 2 steps, or a pivot <= eps*max diagonal
+ * in the FP32 factor) it refactors in FP64 and finishes with that factor.
+ * info (optional, 4 doubles): [0] iterations, [1] final backward error,
+ * [2] 1 if the FP64 fallback ran, [3] max backward error over columns. */
+int gb300_factorize_mixed (cholmod_sparse *A, cholmod_factor *L,
+    cholmod_common *Common) ;
+cholmod_dense *gb300_solve_refined (cholmod_sparse *A, cholmod_factor *L,
+    cholmod_dense *B, double tol, double *info, cholmod_common *Common) ;
+
+/* Release the GPU state attached to L (device factor, plans, graphs). */
+int gb300_release_factor (cholmod_factor *L, cholmod_common *Common) ;
+
+/* Object helpers for programs without the reference library.  Memory comes
+ * from malloc and is counted in Common->malloc_count / memory_inuse the way
+ * CHOLMOD counts it, so CHOLMOD's own cholmod_l_free_* can free it too. */
+cholmod_sparse *gb300_allocate_sparse (size_t nrow, size_t ncol, size_t nzmax,
+    int sorted, int packed, int stype, int xdtype, cholmod_common *Common) ;
+cholmod_dense *gb300_allocate_dense (size_t nrow, size_t ncol, size_t d,
+    int xdtype, cholmod_common *Common) ;
+int gb300_free_sparse (cholmod_sparse **A, cholmod_common *Common) ;
+int gb300_free_dense (cholmod_dense **X, cholmod_common *Common) ;
+int gb300_free_factor (cholmod_factor **L, cholmod_common *Common) ;
+
+/* Layout of the CHOLMOD objects as compiled into this library: object 0 =
+ * cholmod_common, 1 = cholmod_sparse, 2 = cholmod_factor, 3 = cholmod_dense.
+ * gb300_abi_offset returns offsetof(object, field) or -1 for an unknown
+ * field; gb300_abi_sizeof returns sizeof(object). */
+long gb300_abi_offset (int object, const char *field) ;
+long gb300_abi_sizeof (int object) ;
+
+/* Last device-side timings of this library for Common (milliseconds, CUDA
+ * events on the library's stream): [0] factor, [1] last solve sweep pair,
+ * [2] refined solve total, [3] assembly, [4] kernel launches of the last
+ * factorization (count). */
+int gb300_get_stats (cholmod_common *Common, double *out, int nout) ;
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CHOLMOD_GB300_H */

@@ -1,0 +1,257 @@
+"""ctypes bindings of libcholmod_gb300.so, mirroring the CHOLMOD calling style.
+
+The library is the product: a C ABI whose entry points are the CHOLMOD ones
+(``cholmod_l_super_numeric``, ``cholmod_l_super_lsolve``,
+``cholmod_l_super_ltsolve``) plus ``gb300_*`` drivers.  This module only
+marshals numpy arrays into CHOLMOD objects allocated by the library and calls
+through the C ABI; it does no numerical work itself.  Loading fails loudly if
+the shared library has not been built.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libcholmod_gb300.so")
+
+CHOLMOD_PATTERN, CHOLMOD_REAL = 0, 1
+CHOLMOD_DOUBLE, CHOLMOD_SINGLE = 0, 4
+CHOLMOD_OK, CHOLMOD_NOT_INSTALLED, CHOLMOD_OUT_OF_MEMORY = 0, -1, -2
+CHOLMOD_TOO_LARGE, CHOLMOD_INVALID, CHOLMOD_GPU_PROBLEM = -3, -4, -5
+CHOLMOD_NOT_POSDEF, CHOLMOD_DSMALL = 1, 2
+CHOLMOD_A = 0
+GB300_OPT_KEEP_ON_DEVICE, GB300_OPT_SMALL_COLS = 1, 2
+
+
+class cholmod_sparse(C.Structure):
+    _fields_ = [("nrow", C.c_size_t), ("ncol", C.c_size_t), ("nzmax", C.c_size_t),
+                ("p", C.c_void_p), ("i", C.c_void_p), ("nz", C.c_void_p),
+                ("x", C.c_void_p), ("z", C.c_void_p), ("stype", C.c_int),
+                ("itype", C.c_int), ("xtype", C.c_int), ("dtype", C.c_int),
+                ("sorted", C.c_int), ("packed", C.c_int)]
+
+
+class cholmod_factor(C.Structure):
+    _fields_ = [("n", C.c_size_t), ("minor", C.c_size_t), ("Perm", C.c_void_p),
+                ("ColCount", C.c_void_p), ("IPerm", C.c_void_p), ("nzmax", C.c_size_t),
+                ("p", C.c_void_p), ("i", C.c_void_p), ("x", C.c_void_p),
+                ("z", C.c_void_p), ("nz", C.c_void_p), ("next", C.c_void_p),
+                ("prev", C.c_void_p), ("nsuper", C.c_size_t), ("ssize", C.c_size_t),
+                ("xsize", C.c_size_t), ("maxcsize", C.c_size_t), ("maxesize", C.c_size_t),
+                ("super", C.c_void_p), ("pi", C.c_void_p), ("px", C.c_void_p),
+                ("s", C.c_void_p), ("ordering", C.c_int), ("is_ll", C.c_int),
+                ("is_super", C.c_int), ("is_monotonic", C.c_int), ("itype", C.c_int),
+                ("xtype", C.c_int), ("dtype", C.c_int), ("useGPU", C.c_int)]
+
+
+class cholmod_dense(C.Structure):
+    _fields_ = [("nrow", C.c_size_t), ("ncol", C.c_size_t), ("nzmax", C.c_size_t),
+                ("d", C.c_size_t), ("x", C.c_void_p), ("z", C.c_void_p),
+                ("xtype", C.c_int), ("dtype", C.c_int)]
+
+
+SP = C.POINTER(cholmod_sparse)
+FP = C.POINTER(cholmod_factor)
+DP = C.POINTER(cholmod_dense)
+
+_lib = None
+
+
+def lib():
+    """Load the C-ABI library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with "
+                           "python -c 'import __graft_entry__ as g; g.build()'")
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    sig = {
+        "gb300_start": (C.c_int, [vp]),
+        "gb300_finish": (C.c_int, [vp]),
+        "gb300_set_option": (C.c_int, [vp, C.c_int, C.c_int64]),
+        "gb300_get_stats": (C.c_int, [vp, C.POINTER(C.c_double), C.c_int]),
+        "gb300_abi_offset": (C.c_long, [C.c_int, C.c_char_p]),
+        "gb300_abi_sizeof": (C.c_long, [C.c_int]),
+        "gb300_allocate_sparse": (SP, [C.c_size_t, C.c_size_t, C.c_size_t, C.c_int,
+                                       C.c_int, C.c_int, C.c_int, vp]),
+        "gb300_allocate_dense": (DP, [C.c_size_t, C.c_size_t, C.c_size_t, C.c_int, vp]),
+        "gb300_free_sparse": (C.c_int, [C.POINTER(SP), vp]),
+        "gb300_free_dense": (C.c_int, [C.POINTER(DP), vp]),
+        "gb300_free_factor": (C.c_int, [C.POINTER(FP), vp]),
+        "gb300_analyze_perm": (FP, [SP, C.POINTER(C.c_int64), vp]),
+        "gb300_factorize": (C.c_int, [SP, C.POINTER(C.c_double), FP, vp]),
+        "gb300_solve": (DP, [C.c_int, FP, DP, vp]),
+        "gb300_factorize_mixed": (C.c_int, [SP, FP, vp]),
+        "gb300_solve_refined": (DP, [SP, FP, DP, C.c_double, C.POINTER(C.c_double), vp]),
+        "gb300_release_factor": (C.c_int, [FP, vp]),
+        "cholmod_l_super_numeric": (C.c_int, [SP, SP, C.POINTER(C.c_double), FP, vp]),
+        "cholmod_l_super_lsolve": (C.c_int, [FP, DP, DP, vp]),
+        "cholmod_l_super_ltsolve": (C.c_int, [FP, DP, DP, vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+_COMMON_FIELDS = {
+    "status": C.c_int, "print": C.c_int, "try_catch": C.c_int,
+    "quick_return_if_not_posdef": C.c_int, "fl": C.c_double, "lnz": C.c_double,
+    "anz": C.c_double, "malloc_count": C.c_size_t, "memory_inuse": C.c_size_t,
+    "supernodal": C.c_int, "useGPU": C.c_int,
+}
+
+
+class Common:
+    """A cholmod_common owned by Python, initialised with gb300_start."""
+
+    def __init__(self, print_level=0):
+        L = lib()
+        self._buf = C.create_string_buffer(L.gb300_abi_sizeof(0))
+        self.ptr = C.cast(self._buf, C.c_void_p)
+        L.gb300_start(self.ptr)
+        self["print"] = print_level
+
+    def _field(self, name):
+        off = lib().gb300_abi_offset(0, name.encode())
+        if off < 0:
+            raise KeyError(name)
+        return _COMMON_FIELDS[name].from_address(self.ptr.value + off)
+
+    def __getitem__(self, name):
+        return self._field(name).value
+
+    def __setitem__(self, name, value):
+        self._field(name).value = value
+
+    @property
+    def status(self):
+        return self["status"]
+
+    def set_option(self, option, value):
+        return lib().gb300_set_option(self.ptr, option, int(value))
+
+    def stats(self):
+        out = (C.c_double * 8)()
+        lib().gb300_get_stats(self.ptr, out, 8)
+        return list(out)
+
+    def finish(self):
+        if self.ptr:
+            lib().gb300_finish(self.ptr)
+
+    def __del__(self):
+        try:
+            self.finish()
+        except Exception:
+            pass
+
+
+def _arr(ptr, dtype, count):
+    if not ptr or count == 0:
+        return np.zeros(0, dtype=dtype)
+    ct = {np.int64: C.c_int64, np.float64: C.c_double, np.float32: C.c_float}[dtype]
+    return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ct)), shape=(count,))
+
+
+def sparse(n, Ap, Ai, Ax, common, stype=-1, dtype="d", ncol=None):
+    """Allocate a cholmod_sparse in the library and copy the CSC arrays in."""
+    ncol = n if ncol is None else ncol
+    nz = int(Ap[-1])
+    dt = CHOLMOD_SINGLE if dtype == "s" else CHOLMOD_DOUBLE
+    A = lib().gb300_allocate_sparse(n, ncol, nz, 1, 1, stype, CHOLMOD_REAL + dt, common.ptr)
+    if not A:
+        raise RuntimeError(f"allocate_sparse failed, status {common.status}")
+    a = A.contents
+    _arr(a.p, np.int64, ncol + 1)[:] = Ap
+    _arr(a.i, np.int64, max(nz, 1))[:nz] = Ai
+    _arr(a.x, np.float32 if dtype == "s" else np.float64, max(nz, 1))[:nz] = Ax
+    return A
+
+
+def free_sparse(A, common):
+    lib().gb300_free_sparse(C.byref(A), common.ptr)
+
+
+def dense(X, common, dtype="d"):
+    X = np.asarray(X)
+    if X.ndim == 1:
+        X = X[:, None]
+    n, k = X.shape
+    dt = CHOLMOD_SINGLE if dtype == "s" else CHOLMOD_DOUBLE
+    D = lib().gb300_allocate_dense(n, k, n, CHOLMOD_REAL + dt, common.ptr)
+    if not D:
+        raise RuntimeError(f"allocate_dense failed, status {common.status}")
+    _arr(D.contents.x, np.float32 if dtype == "s" else np.float64, max(n * k, 1))[:n * k] = \
+        X.T.ravel()
+    return D
+
+
+def dense_array(D):
+    d = D.contents
+    dt = np.float32 if d.dtype == CHOLMOD_SINGLE else np.float64
+    a = _arr(d.x, dt, d.d * d.ncol).reshape(d.ncol, d.d)[:, :d.nrow].T.copy()
+    return a
+
+
+def free_dense(D, common):
+    lib().gb300_free_dense(C.byref(D), common.ptr)
+
+
+def analyze_perm(A, perm, common):
+    perm = np.ascontiguousarray(perm, dtype=np.int64)
+    L = lib().gb300_analyze_perm(A, perm.ctypes.data_as(C.POINTER(C.c_int64)), common.ptr)
+    if not L:
+        raise RuntimeError(f"analyze failed, status {common.status}")
+    return L
+
+
+def factor_arrays(L, with_x=True):
+    """numpy copies of the supernodal fields of a cholmod_factor."""
+    f = L.contents
+    ns = f.nsuper
+    out = {
+        "n": f.n, "minor": f.minor, "nsuper": ns, "ssize": f.ssize, "xsize": f.xsize,
+        "maxcsize": f.maxcsize, "maxesize": f.maxesize, "is_super": f.is_super,
+        "xtype": f.xtype, "dtype": f.dtype,
+        "Perm": _arr(f.Perm, np.int64, f.n).copy(),
+        "ColCount": _arr(f.ColCount, np.int64, f.n).copy(),
+        "Super": _arr(f.super, np.int64, ns + 1).copy(),
+        "Pi": _arr(f.pi, np.int64, ns + 1).copy(),
+        "Px": _arr(f.px, np.int64, ns + 1).copy(),
+        "Ls": _arr(f.s, np.int64, f.ssize).copy(),
+    }
+    if with_x and f.x:
+        dt = np.float32 if f.dtype == CHOLMOD_SINGLE else np.float64
+        out["Lx"] = _arr(f.x, dt, f.xsize).copy()
+    return out
+
+
+def free_factor(L, common):
+    lib().gb300_free_factor(C.byref(L), common.ptr)
+
+
+def super_numeric(S, L, common, beta=0.0):
+    b = (C.c_double * 2)(beta, 0.0)
+    return lib().cholmod_l_super_numeric(S, None, b, L, common.ptr)
+
+
+def factorize(A, L, common, beta=0.0):
+    b = (C.c_double * 2)(beta, 0.0)
+    return lib().gb300_factorize(A, b, L, common.ptr)
+
+
+def solve(L, B, common, dtype="d"):
+    Bd = dense(B, common, dtype)
+    X = lib().gb300_solve(CHOLMOD_A, L, Bd, common.ptr)
+    free_dense(Bd, common)
+    if not X:
+        raise RuntimeError(f"solve failed, status {common.status}")
+    out = dense_array(X)
+    free_dense(X, common)
+    return out

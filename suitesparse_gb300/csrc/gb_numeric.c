@@ -1,0 +1,593 @@
+/* gb_numeric.c -- host drivers of the GPU factorization and sweeps, and the
+ * CHOLMOD entry points cholmod_l_super_numeric / _lsolve / _ltsolve.
+ *
+ * Device state is attached to a factor through a side table keyed by the
+ * cholmod_factor pointer and validated by a fingerprint of its supernodal
+ * pattern (cholmod_factor is ABI and cannot grow).  The plan of a pattern
+ * (gb_plan.c) is built and uploaded once; every factorization then uploads
+ * only the values of A, replays the level sequence on one stream, checks one
+ * word for a failed pivot, and copies L->x back unless the caller keeps the
+ * factor on the device.  There is no CPU fallback: any CUDA failure returns
+ * FALSE with Common->status = CHOLMOD_GPU_PROBLEM.
+ */
+#include "gb_plan.h"
+#include <cuda_runtime.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+struct gb_ctx {
+    cudaStream_t stream;
+    int device;
+    int64_t opt_keep, opt_small;
+    double stats[8];
+    cudaEvent_t ev0, ev1;
+};
+
+gb_ctx *gb_ctx_new(void)
+{
+    gb_ctx *c = calloc(1, sizeof(gb_ctx));
+    if (!c) return NULL;
+    c->opt_keep = 0;
+    c->opt_small = GB_SMALL_MAX;
+    c->device = -1;
+    return c;
+}
+
+void gb_ctx_delete(gb_ctx *c)
+{
+    if (!c) return;
+    if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    free(c);
+}
+
+static int ctx_ready(gb_ctx *c)
+{
+    if (c->stream) return TRUE;
+    if (cudaGetDevice(&c->device) != cudaSuccess) return FALSE;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return FALSE;
+    if (cudaEventCreate(&c->ev0) != cudaSuccess) return FALSE;
+    if (cudaEventCreate(&c->ev1) != cudaSuccess) return FALSE;
+    return TRUE;
+}
+
+int64_t gb_option(cholmod_common *Common, int option)
+{
+    gb_ctx *c = gb_ctx_get(Common, 0);
+    if (option == GB300_OPT_KEEP_ON_DEVICE) return c ? c->opt_keep : 0;
+    if (option == GB300_OPT_SMALL_COLS) return c ? c->opt_small : GB_SMALL_MAX;
+    return 0;
+}
+
+int gb300_set_option(cholmod_common *Common, int option, int64_t value)
+{
+    if (!Common) return FALSE;
+    gb_ctx *c = gb_ctx_get(Common, 1);
+    if (!c) { GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "out of memory"); return FALSE; }
+    if (option == GB300_OPT_KEEP_ON_DEVICE) c->opt_keep = value ? 1 : 0;
+    else if (option == GB300_OPT_SMALL_COLS) c->opt_small = GB_MAX(1, GB_MIN(GB_SMALL_MAX, value));
+    else { GB_ERROR(CHOLMOD_INVALID, "unknown option"); return FALSE; }
+    return TRUE;
+}
+
+int gb300_get_stats(cholmod_common *Common, double *out, int nout)
+{
+    gb_ctx *c = gb_ctx_get(Common, 0);
+    if (!c || !out) return FALSE;
+    for (int i = 0; i < nout && i < 8; i++) out[i] = c->stats[i];
+    return TRUE;
+}
+
+/* ---- factor side table --------------------------------------------------- */
+
+static gb_plan *plan_head = NULL;
+static pthread_mutex_t plan_lock = PTHREAD_MUTEX_INITIALIZER;
+
+static int plan_matches(const gb_plan *P, const cholmod_factor *L)
+{
+    return P->L == L && P->super_ptr == L->super && P->s_ptr == L->s && P->pi_ptr == L->pi
+           && P->n == (Int)L->n && P->nsuper == (Int)L->nsuper
+           && P->ssize == (Int)L->ssize && P->xsize == (Int)L->xsize;
+}
+
+static void plan_unlink(gb_plan *P)
+{
+    for (gb_plan **pp = &plan_head; *pp; pp = &(*pp)->next)
+        if (*pp == P) { *pp = P->next; break; }
+}
+
+int gb_release_factor_state(cholmod_factor *L)
+{
+    pthread_mutex_lock(&plan_lock);
+    gb_plan *found = NULL;
+    for (gb_plan *P = plan_head; P; P = P->next)
+        if (P->L == L) { found = P; break; }
+    if (found) plan_unlink(found);
+    pthread_mutex_unlock(&plan_lock);
+    if (found) {
+        cudaDeviceSynchronize();
+        gb_plan_free(found);
+    }
+    return TRUE;
+}
+
+int gb300_release_factor(cholmod_factor *L, cholmod_common *Common)
+{
+    (void)Common;
+    if (!L) return FALSE;
+    return gb_release_factor_state(L);
+}
+
+/* Find (or build and upload) the plan of L.  A stale entry for the same
+ * pointer with a different pattern is dropped. */
+static gb_plan *plan_get(cholmod_factor *L, cholmod_common *Common, gb_ctx *ctx, int create)
+{
+    pthread_mutex_lock(&plan_lock);
+    gb_plan *P = NULL;
+    for (gb_plan *q = plan_head; q; q = q->next)
+        if (q->L == L) { P = q; break; }
+    if (P && (!plan_matches(P, L) || P->hash != gb_pattern_hash(L))) {
+        plan_unlink(P);
+        pthread_mutex_unlock(&plan_lock);
+        cudaStreamSynchronize(ctx->stream);
+        gb_plan_free(P);
+        pthread_mutex_lock(&plan_lock);
+        P = NULL;
+    }
+    pthread_mutex_unlock(&plan_lock);
+    if (P || !create) return P;
+    P = gb_plan_build(L, ctx->opt_small);
+    if (!P) { GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "plan construction failed"); return NULL; }
+    if (!gb_plan_upload(P)) {
+        gb_plan_free(P);
+        GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation of the plan failed");
+        return NULL;
+    }
+    pthread_mutex_lock(&plan_lock);
+    P->next = plan_head;
+    plan_head = P;
+    pthread_mutex_unlock(&plan_lock);
+    return P;
+}
+
+static int dev_grow(void **p, size_t *cap, size_t bytes)
+{
+    if (bytes <= *cap && *p) return TRUE;
+    if (*p) cudaFree(*p);
+    *p = NULL;
+    *cap = 0;
+    if (cudaMalloc(p, bytes ? bytes : 16) != cudaSuccess) { *p = NULL; return FALSE; }
+    *cap = bytes;
+    return TRUE;
+}
+
+static int dt_index(int dtype) { return dtype == CHOLMOD_SINGLE ? 1 : 0; }
+static size_t dt_size(int dtype) { return dtype == CHOLMOD_SINGLE ? sizeof(float) : sizeof(double); }
+
+/* device factor and update-block buffers of one precision */
+static int ensure_numeric(gb_plan *P, int dtype)
+{
+    int d = dt_index(dtype);
+    size_t e = dt_size(dtype);
+    if (!P->d_Lx[d] && cudaMalloc(&P->d_Lx[d], e * GB_MAX(P->xsize, 1)) != cudaSuccess) {
+        P->d_Lx[d] = NULL;
+        return FALSE;
+    }
+    if (!P->d_CB[d] && cudaMalloc(&P->d_CB[d], e * GB_MAX(P->cb_total, 1)) != cudaSuccess) {
+        P->d_CB[d] = NULL;
+        return FALSE;
+    }
+    return TRUE;
+}
+
+#define CU(call) do { if ((call) != cudaSuccess) goto cuda_fail; } while (0)
+#define LK(call) do { if ((call) != 0) goto cuda_fail; } while (0)
+
+/* Replay the factorization sequence.  Sx has dtype a_dtype; the factor is
+ * computed in l_dtype; scale (device, optional) applies D A D. */
+static int run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dtype,
+                      const double *scale, double beta)
+{
+    cudaStream_t st = ctx->stream;
+    int d = dt_index(l_dtype);
+    int ldt = l_dtype == CHOLMOD_SINGLE ? 4 : 0;
+    int adt = a_dtype == CHOLMOD_SINGLE ? 4 : 0;
+    void *Lx = P->d_Lx[d], *CB = P->d_CB[d];
+    const gb_launch_rec *seq = P->fact_seq.p;
+    int launches = 0;
+    CU(cudaMemsetAsync(P->d_fail, 0xFF, sizeof(int32_t) * (P->nsuper + 1), st));
+    CU(cudaMemsetAsync(P->d_anyfail, 0, sizeof(int32_t), st));
+    for (size_t i = 0; i < P->fact_seq.n; i++) {
+        const gb_launch_rec *r = &seq[i];
+        switch (r->kind) {
+        case GB_K_ASM:
+            LK(gb_launch_assemble(&P->ptrs, P->d_asm + r->off, r->count, P->d_Sp, P->d_Si,
+                                  Sx, adt, scale, beta, Lx, CB, ldt, st));
+            break;
+        case GB_K_SMALL:
+            LK(gb_launch_factor_small(&P->ptrs, P->d_node + r->off, r->count, Lx, ldt, st));
+            break;
+        case GB_K_POTRF:
+            LK(gb_launch_potrf_diag(&P->ptrs, P->d_potrf + r->off, r->count, Lx, ldt, st));
+            break;
+        case GB_K_TRSM:
+            LK(gb_launch_trsm_rows(&P->ptrs, P->d_trsm + r->off, r->count, Lx, ldt, st));
+            break;
+        case GB_K_GEMM:
+            LK(gb_launch_gemm(&P->ptrs, P->d_gemm + r->off, P->d_gemm_owner + r->off,
+                              r->count, Lx, CB, ldt, st));
+            break;
+        }
+        launches++;
+    }
+    ctx->stats[4] = launches;
+    return TRUE;
+cuda_fail:
+    return FALSE;
+}
+
+/* Replay one sweep on Y (device, n x nrhs, ld n) with the device factor. */
+static int run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int forward)
+{
+    cudaStream_t st = ctx->stream;
+    int d = dt_index(l_dtype);
+    int ldt = l_dtype == CHOLMOD_SINGLE ? 4 : 0;
+    size_t e = dt_size(l_dtype);
+    if (!dev_grow(&P->d_U, &P->u_cap, e * GB_MAX(P->cbv_total, 1) * nrhs)) return FALSE;
+    const void *Lx = P->d_Lx[d];
+    gb_vec *seqv = forward ? &P->fwd_seq : &P->bwd_seq;
+    const gb_launch_rec *seq = seqv->p;
+    for (size_t i = 0; i < seqv->n; i++) {
+        const gb_launch_rec *r = &seq[i];
+        int rc = 0;
+        switch (r->kind) {
+        case GB_K_FWD_SMALL: rc = gb_launch_sweep_node(0, &P->ptrs, P->d_node + r->off, r->count, Lx, ldt, nrhs, Y, P->n, P->d_U, st); break;
+        case GB_K_FWD_GATHER: rc = gb_launch_sweep_node(1, &P->ptrs, P->d_node + r->off, r->count, Lx, ldt, nrhs, Y, P->n, P->d_U, st); break;
+        case GB_K_BWD_SMALL: rc = gb_launch_sweep_node(2, &P->ptrs, P->d_node + r->off, r->count, Lx, ldt, nrhs, Y, P->n, P->d_U, st); break;
+        case GB_K_FWD_DIAG: rc = gb_launch_sweep_step(0, &P->ptrs, P->d_sweep + r->off, r->count, Lx, ldt, nrhs, Y, P->n, P->d_U, st); break;
+        case GB_K_FWD_PANEL: rc = gb_launch_sweep_step(1, &P->ptrs, P->d_sweep + r->off, r->count, Lx, ldt, nrhs, Y, P->n, P->d_U, st); break;
+        case GB_K_BWD_OFFDIAG: rc = gb_launch_sweep_step(2, &P->ptrs, P->d_sweep + r->off, r->count, Lx, ldt, nrhs, Y, P->n, P->d_U, st); break;
+        case GB_K_BWD_DIAG: rc = gb_launch_sweep_step(3, &P->ptrs, P->d_sweep + r->off, r->count, Lx, ldt, nrhs, Y, P->n, P->d_U, st); break;
+        case GB_K_BWD_PANEL: rc = gb_launch_sweep_step(4, &P->ptrs, P->d_sweep + r->off, r->count, Lx, ldt, nrhs, Y, P->n, P->d_U, st); break;
+        }
+        if (rc) return FALSE;
+    }
+    return TRUE;
+}
+
+/* After a factorization with a failed pivot: reproduce the reference's
+ * state (CHOLMOD/Supernodal/t_cholmod_super_numeric_worker.c:1084-1146):
+ * s0 = first failing supernode in index order, L->minor = its first column
+ * + failing local column; columns from the failing one (or all of s0 when
+ * the first column failed or quick_return_if_not_posdef) and every later
+ * supernode are zero.  Supernodes before s0 are neither descendants of a
+ * failing supernode nor affected by one, so their values are final. */
+static int fix_not_posdef(gb_plan *P, gb_ctx *ctx, cholmod_factor *L, int l_dtype,
+                          cholmod_common *Common)
+{
+    int32_t *fail = malloc(sizeof(int32_t) * (P->nsuper + 1));
+    if (!fail) { GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "out of memory"); return FALSE; }
+    if (cudaMemcpyAsync(fail, P->d_fail, sizeof(int32_t) * P->nsuper, cudaMemcpyDeviceToHost,
+                        ctx->stream) != cudaSuccess
+        || cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        free(fail);
+        GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error");
+        return FALSE;
+    }
+    Int s0 = -1;
+    for (Int s = 0; s < P->nsuper; s++) if (fail[s] >= 0) { s0 = s; break; }
+    if (s0 < 0) { free(fail); return TRUE; }
+    const Int *Super = L->super, *Pi = L->pi, *Px = L->px;
+    Int info = fail[s0] + 1;                         /* LAPACK-style, 1-based */
+    free(fail);
+    Int nsrow = Pi[s0 + 1] - Pi[s0];
+    Int keep = (info == 1 || Common->quick_return_if_not_posdef) ? 0 : info - 1;
+    int d = dt_index(l_dtype);
+    if (gb_launch_zero_range(P->d_Lx[d], l_dtype == CHOLMOD_SINGLE ? 4 : 0,
+                             Px[s0] + keep * nsrow, P->xsize, ctx->stream) != 0) {
+        GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error");
+        return FALSE;
+    }
+    L->minor = (size_t)(Super[s0] + info - 1);
+    if (Common->status == CHOLMOD_OK) GB_ERROR(CHOLMOD_NOT_POSDEF, "matrix not positive definite");
+    return TRUE;
+}
+
+/* Upload S = A (lower, packed, sorted or not) values and pattern. */
+static int upload_input(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, int a_dtype)
+{
+    Int n = (Int)A->ncol;
+    const Int *Ap = A->p;
+    Int nz = Ap[n];
+    size_t e = dt_size(a_dtype);
+    if (!dev_grow((void **)&P->d_Sp, &P->sp_cap, sizeof(int64_t) * (n + 1))) return FALSE;
+    if (!dev_grow((void **)&P->d_Si, &P->si_cap, sizeof(int64_t) * GB_MAX(nz, 1))) return FALSE;
+    if (!dev_grow(&P->d_Sx, &P->sx_cap, e * GB_MAX(nz, 1))) return FALSE;
+    cudaStream_t st = ctx->stream;
+    if (cudaMemcpyAsync(P->d_Sp, A->p, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st) != cudaSuccess) return FALSE;
+    if (nz && cudaMemcpyAsync(P->d_Si, A->i, sizeof(int64_t) * nz, cudaMemcpyHostToDevice, st) != cudaSuccess) return FALSE;
+    if (nz && cudaMemcpyAsync(P->d_Sx, A->x, e * nz, cudaMemcpyHostToDevice, st) != cudaSuccess) return FALSE;
+    return TRUE;
+}
+
+/* ======================================================================== */
+
+int cholmod_l_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2],
+                            cholmod_factor *L, cholmod_common *Common)
+{
+    if (!Common) return FALSE;
+    if (!L || !A) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return FALSE; }
+    if (A->xtype < CHOLMOD_REAL || A->xtype > CHOLMOD_ZOMPLEX || !A->x) {
+        GB_ERROR(CHOLMOD_INVALID, "invalid xtype");
+        return FALSE;
+    }
+    if (L->xtype < CHOLMOD_PATTERN || L->xtype > CHOLMOD_COMPLEX) {
+        GB_ERROR(CHOLMOD_INVALID, "invalid xtype");
+        return FALSE;
+    }
+    if (A->stype < 0) {
+        if (A->nrow != A->ncol || A->nrow != L->n) {
+            GB_ERROR(CHOLMOD_INVALID, "invalid dimensions");
+            return FALSE;
+        }
+    } else if (A->stype == 0) {
+        if (A->nrow != L->n) { GB_ERROR(CHOLMOD_INVALID, "invalid dimensions"); return FALSE; }
+        (void)F;
+        GB_ERROR(CHOLMOD_INVALID, "unsymmetric A*F' form not supported on the GPU path");
+        return FALSE;
+    } else {
+        GB_ERROR(CHOLMOD_INVALID, "symmetric upper case not supported");
+        return FALSE;
+    }
+    if (!L->is_super) { GB_ERROR(CHOLMOD_INVALID, "L not supernodal"); return FALSE; }
+    if (L->xtype != CHOLMOD_PATTERN) {
+        if (!(A->xtype == CHOLMOD_REAL && L->xtype == CHOLMOD_REAL)
+            && !(A->xtype >= CHOLMOD_COMPLEX && L->xtype == CHOLMOD_COMPLEX)) {
+            GB_ERROR(CHOLMOD_INVALID, "complex type mismatch");
+            return FALSE;
+        }
+        if (A->dtype != L->dtype) {
+            GB_ERROR(CHOLMOD_INVALID, "A and L must have the same dtype");
+            return FALSE;
+        }
+    }
+    if (A->xtype != CHOLMOD_REAL) {
+        GB_ERROR(CHOLMOD_INVALID, "complex factorization not supported on the GPU path");
+        return FALSE;
+    }
+    if (A->itype != CHOLMOD_LONG || L->itype != CHOLMOD_LONG) {
+        GB_ERROR(CHOLMOD_INVALID, "int64 (cholmod_l_) objects required");
+        return FALSE;
+    }
+    Common->status = CHOLMOD_OK;
+    int dtype = A->dtype;
+    cholmod_sparse *Apk = A;
+    if (!A->packed) {
+        /* pack the columns (unpacked input) on the host */
+        Int n = (Int)A->ncol, nz = 0;
+        const Int *Ap = A->p, *Anz = A->nz;
+        for (Int j = 0; j < n; j++) nz += Anz[j];
+        Apk = gb300_allocate_sparse(A->nrow, n, nz, A->sorted, TRUE, A->stype,
+                                    CHOLMOD_REAL + dtype, Common);
+        if (!Apk) return FALSE;
+        Int *Bp = Apk->p, *Bi = Apk->i;
+        size_t e = dt_size(dtype);
+        Int q = 0;
+        for (Int j = 0; j < n; j++) {
+            Bp[j] = q;
+            memcpy(Bi + q, (Int *)A->i + Ap[j], sizeof(Int) * Anz[j]);
+            memcpy((char *)Apk->x + q * e, (char *)A->x + Ap[j] * e, e * Anz[j]);
+            q += Anz[j];
+        }
+        Bp[n] = q;
+    }
+
+    gb_ctx *ctx = gb_ctx_get(Common, 1);
+    if (!ctx || !ctx_ready(ctx)) {
+        if (Apk != A) gb300_free_sparse(&Apk, Common);
+        GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device");
+        return FALSE;
+    }
+    int symbolic = (L->xtype == CHOLMOD_PATTERN);
+    gb_plan *P = plan_get(L, Common, ctx, 1);
+    if (!P) { if (Apk != A) gb300_free_sparse(&Apk, Common); return FALSE; }
+    if (!ensure_numeric(P, dtype) || !upload_input(P, ctx, Apk, dtype)) {
+        if (Apk != A) gb300_free_sparse(&Apk, Common);
+        GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed");
+        return FALSE;
+    }
+    if (symbolic) {
+        /* supernodal symbolic -> numeric: allocate L->x (change_factor) */
+        L->dtype = dtype;
+        L->x = gb_malloc(L->xsize, dt_size(dtype), Common);
+        if (!L->x) { if (Apk != A) gb300_free_sparse(&Apk, Common); return FALSE; }
+        memset(L->x, 0, GB_MIN(2 * sizeof(double), L->xsize * dt_size(dtype)));
+        L->xtype = CHOLMOD_REAL;
+    }
+    L->is_ll = TRUE;
+
+    int ok = TRUE;
+    cudaEventRecord(ctx->ev0, ctx->stream);
+    ok = run_factor(P, ctx, P->d_Sx, dtype, dtype, NULL, beta ? beta[0] : 0.0);
+    cudaEventRecord(ctx->ev1, ctx->stream);
+    int32_t anyfail = 0;
+    if (ok) ok = cudaMemcpyAsync(&anyfail, P->d_anyfail, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess
+                 && cudaStreamSynchronize(ctx->stream) == cudaSuccess;
+    if (!ok) {
+        if (Apk != A) gb300_free_sparse(&Apk, Common);
+        GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the factorization");
+        return FALSE;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats[0] = ms;
+    L->minor = L->n;
+    if (anyfail && !fix_not_posdef(P, ctx, L, dtype, Common)) {
+        if (Apk != A) gb300_free_sparse(&Apk, Common);
+        return FALSE;
+    }
+    int d = dt_index(dtype);
+    P->dev_valid[d] = 1;
+    P->dev_valid[1 - d] = 0;
+    P->host_x[d] = L->x;
+    if (!ctx->opt_keep) {
+        if (cudaMemcpyAsync(L->x, P->d_Lx[d], dt_size(dtype) * L->xsize, cudaMemcpyDeviceToHost,
+                            ctx->stream) != cudaSuccess
+            || cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+            if (Apk != A) gb300_free_sparse(&Apk, Common);
+            GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error copying L");
+            return FALSE;
+        }
+    } else {
+        cudaStreamSynchronize(ctx->stream);
+    }
+    if (Apk != A) gb300_free_sparse(&Apk, Common);
+    return Common->status >= CHOLMOD_OK;
+}
+
+/* device factor of L in dtype, uploading L->x when this library did not
+ * produce the current values */
+static gb_plan *factor_on_device(cholmod_factor *L, gb_ctx *ctx, cholmod_common *Common)
+{
+    gb_plan *P = plan_get(L, Common, ctx, 1);
+    if (!P) return NULL;
+    int d = dt_index(L->dtype);
+    if (P->dev_valid[d] && P->host_x[d] == L->x) return P;
+    if (!L->x) { GB_ERROR(CHOLMOD_INVALID, "L has no numerical values"); return NULL; }
+    if (!ensure_numeric(P, L->dtype)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed"); return NULL; }
+    if (cudaMemcpyAsync(P->d_Lx[d], L->x, dt_size(L->dtype) * L->xsize, cudaMemcpyHostToDevice,
+                        ctx->stream) != cudaSuccess) {
+        GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error");
+        return NULL;
+    }
+    P->dev_valid[d] = 1;
+    P->host_x[d] = L->x;
+    return P;
+}
+
+static int super_solve(cholmod_factor *L, cholmod_dense *X, cholmod_dense *E,
+                       cholmod_common *Common, int forward)
+{
+    if (!Common) return FALSE;
+    if (!L || !X || !E) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return FALSE; }
+    if (L->xtype != CHOLMOD_REAL || X->xtype != CHOLMOD_REAL || E->xtype != CHOLMOD_REAL) {
+        GB_ERROR(CHOLMOD_INVALID, "real factor and matrices required");
+        return FALSE;
+    }
+    if (L->dtype != X->dtype || L->dtype != E->dtype) {
+        GB_ERROR(CHOLMOD_INVALID, "all xtypes and dtypes must match");
+        return FALSE;
+    }
+    if (!L->is_ll) { GB_ERROR(CHOLMOD_INVALID, "L must be LL', not LDL'"); return FALSE; }
+    if (!L->is_super) { GB_ERROR(CHOLMOD_INVALID, "L must be supernodal"); return FALSE; }
+    if (X->nrow != L->n) { GB_ERROR(CHOLMOD_INVALID, "X and L dimensions must match"); return FALSE; }
+    if (E->nzmax < X->ncol * L->maxesize) {
+        GB_ERROR(CHOLMOD_INVALID, "workspace E not large enough");
+        return FALSE;
+    }
+    Common->status = CHOLMOD_OK;
+    if (L->n == 0 || X->ncol == 0) return TRUE;
+    gb_ctx *ctx = gb_ctx_get(Common, 1);
+    if (!ctx || !ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return FALSE; }
+    gb_plan *P = factor_on_device(L, ctx, Common);
+    if (!P) return FALSE;
+    int nrhs = (int)X->ncol;
+    size_t e = dt_size(L->dtype);
+    Int n = P->n;
+    if (!dev_grow(&P->d_Y, &P->y_cap, e * n * nrhs)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed"); return FALSE; }
+    cudaStream_t st = ctx->stream;
+    int ok = cudaMemcpy2DAsync(P->d_Y, e * n, X->x, e * X->d, e * n, nrhs,
+                               cudaMemcpyHostToDevice, st) == cudaSuccess;
+    cudaEventRecord(ctx->ev0, st);
+    ok = ok && run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, forward);
+    cudaEventRecord(ctx->ev1, st);
+    ok = ok && cudaMemcpy2DAsync(X->x, e * X->d, P->d_Y, e * n, e * n, nrhs,
+                                 cudaMemcpyDeviceToHost, st) == cudaSuccess;
+    ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
+    if (!ok) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the solve"); return FALSE; }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats[1] = ms;
+    return TRUE;
+}
+
+int cholmod_l_super_lsolve(cholmod_factor *L, cholmod_dense *X, cholmod_dense *E,
+                           cholmod_common *Common)
+{
+    return super_solve(L, X, E, Common, 1);
+}
+
+int cholmod_l_super_ltsolve(cholmod_factor *L, cholmod_dense *X, cholmod_dense *E,
+                            cholmod_common *Common)
+{
+    return super_solve(L, X, E, Common, 0);
+}
+
+/* ---- gb300_factorize / gb300_solve ---------------------------------------- */
+
+int gb300_factorize(cholmod_sparse *A, double beta[2], cholmod_factor *L,
+                    cholmod_common *Common)
+{
+    if (!Common) return FALSE;
+    if (!A || !L) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return FALSE; }
+    if (A->stype >= 0 || A->nrow != A->ncol || A->nrow != L->n || !L->Perm) {
+        GB_ERROR(CHOLMOD_INVALID, "A must be symmetric-lower and match L");
+        return FALSE;
+    }
+    cholmod_sparse *S = gb_permute_lower(A, L->Perm, Common);
+    if (!S) return FALSE;
+    double zero[2] = {0, 0};
+    int ok = cholmod_l_super_numeric(S, NULL, beta ? beta : zero, L, Common);
+    gb300_free_sparse(&S, Common);
+    return ok;
+}
+
+cholmod_dense *gb300_solve(int sys, cholmod_factor *L, cholmod_dense *B,
+                           cholmod_common *Common)
+{
+    if (!Common) return NULL;
+    if (!L || !B) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return NULL; }
+    if (sys != CHOLMOD_A) { GB_ERROR(CHOLMOD_INVALID, "only sys = CHOLMOD_A is supported"); return NULL; }
+    if (L->xtype != CHOLMOD_REAL || !L->is_super || B->xtype != CHOLMOD_REAL
+        || B->nrow != L->n || B->dtype != L->dtype) {
+        GB_ERROR(CHOLMOD_INVALID, "invalid L or B");
+        return NULL;
+    }
+    Common->status = CHOLMOD_OK;
+    gb_ctx *ctx = gb_ctx_get(Common, 1);
+    if (!ctx || !ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return NULL; }
+    gb_plan *P = factor_on_device(L, ctx, Common);
+    if (!P) return NULL;
+    int nrhs = (int)B->ncol;
+    Int n = P->n;
+    size_t e = dt_size(L->dtype);
+    int dt = L->dtype == CHOLMOD_SINGLE ? 4 : 0;
+    cholmod_dense *X = gb300_allocate_dense(n, nrhs, n, CHOLMOD_REAL + L->dtype, Common);
+    if (!X) return NULL;
+    if (n == 0 || nrhs == 0) return X;
+    cudaStream_t st = ctx->stream;
+    int ok = dev_grow(&P->d_Y, &P->y_cap, e * n * nrhs) && dev_grow(&P->d_B, &P->b_cap, e * n * nrhs);
+    ok = ok && cudaMemcpy2DAsync(P->d_B, e * n, B->x, e * B->d, e * n, nrhs,
+                                 cudaMemcpyHostToDevice, st) == cudaSuccess;
+    cudaEventRecord(ctx->ev0, st);
+    ok = ok && gb_launch_perm_in(n, nrhs, P->d_Perm, NULL, P->d_B, dt, n, P->d_Y, dt, n, st) == 0;
+    ok = ok && run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, 1);
+    ok = ok && run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, 0);
+    ok = ok && gb_launch_perm_out(n, nrhs, P->d_Perm, NULL, P->d_Y, dt, n, P->d_B, dt, n, 0, st) == 0;
+    cudaEventRecord(ctx->ev1, st);
+    ok = ok && cudaMemcpyAsync(X->x, P->d_B, e * n * nrhs, cudaMemcpyDeviceToHost, st) == cudaSuccess;
+    ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
+    if (!ok) {
+        gb300_free_dense(&X, Common);
+        GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the solve");
+        return NULL;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats[1] = ms;
+    return X;
+}

@@ -1,0 +1,142 @@
+/* gb_plan.h -- per-pattern GPU plan of the supernodal factorization/sweeps.
+ *
+ * Everything here depends only on the supernodal pattern (L->super, L->pi,
+ * L->px, L->s) and is built once per pattern on the host, uploaded once, and
+ * reused by every refactorization and solve with that pattern:
+ *   - the supernodal etree (parent, children in increasing order, levels);
+ *   - the relative map of each supernode's off-diagonal rows into its
+ *     parent's row list (the scatter target of the extend-add);
+ *   - offsets of every update block (m^2 entries) and update vector;
+ *   - the task lists and the launch sequence of the factorization and of
+ *     the two sweeps, level by level.
+ */
+#ifndef GB_PLAN_H
+#define GB_PLAN_H
+
+#include "gb_internal.h"
+#include "gb_kernels.cuh"
+#include <cuda_runtime.h>
+
+typedef struct {
+    const int64_t *Super, *Pi, *Px, *cboff, *cbvoff;
+    const int32_t *Ls, *relmap, *child_ptr, *child_list;
+    int32_t *fail, *anyfail;
+} gb_pattern_ptrs;
+
+enum {
+    GB_K_ASM = 1, GB_K_SMALL, GB_K_POTRF, GB_K_TRSM, GB_K_GEMM,
+    GB_K_FWD_SMALL, GB_K_FWD_GATHER, GB_K_FWD_DIAG, GB_K_FWD_PANEL,
+    GB_K_BWD_SMALL, GB_K_BWD_OFFDIAG, GB_K_BWD_DIAG, GB_K_BWD_PANEL
+};
+
+typedef struct { int32_t kind, count; int64_t off; } gb_launch_rec;
+
+/* growable host array */
+typedef struct { void *p; size_t n, cap, esz; } gb_vec;
+
+typedef struct gb_plan {
+    /* identity of the pattern this plan was built for */
+    const cholmod_factor *L;
+    const void *super_ptr, *s_ptr, *pi_ptr;
+    Int n, nsuper, ssize, xsize;
+    uint64_t hash;
+
+    /* host arrays derived from the pattern (kept for the plan's lifetime) */
+    int32_t *h_child_ptr, *h_child_list, *h_relmap;
+    int64_t *h_cboff, *h_cbvoff;
+
+    int nlevels;
+    int64_t cb_total, cbv_total;      /* entries of all update blocks/vectors */
+    int64_t fl_gemm;                  /* FMA-pairs*2 of the update products  */
+
+    /* host task arrays and launch sequences */
+    gb_vec asm_t, node_t, potrf_t, trsm_t, gemm_t, gemm_owner, sweep_t;
+    gb_vec fact_seq, fwd_seq, bwd_seq;
+
+    /* device copies */
+    int64_t *d_Super, *d_Pi, *d_Px, *d_cboff, *d_cbvoff, *d_Perm;
+    int32_t *d_Ls, *d_relmap, *d_child_ptr, *d_child_list, *d_fail, *d_anyfail;
+    gb_asm_task *d_asm;
+    gb_node_task *d_node;
+    gb_potrf_task *d_potrf;
+    gb_trsm_task *d_trsm;
+    gb_gemm_task *d_gemm;
+    int32_t *d_gemm_owner;
+    gb_sweep_task *d_sweep;
+    gb_pattern_ptrs ptrs;
+
+    /* numeric buffers, [0] double, [1] single */
+    void *d_Lx[2], *d_CB[2];
+    int dev_valid[2];                 /* device factor holds the last result */
+    const void *host_x[2];            /* L->x that the device factor mirrors */
+
+    /* inputs and sweep workspace */
+    int64_t *d_Sp, *d_Si;
+    void *d_Sx;
+    size_t sx_cap, si_cap, sp_cap;
+    void *d_Y, *d_U, *d_B;
+    size_t y_cap, u_cap, b_cap;
+
+    /* full (both triangles) FP64 copy of A for residuals, plus scaling */
+    int64_t *d_Rp;
+    int32_t *d_Rj;
+    double *d_Rx, *d_scale, *d_X, *d_R, *d_bx, *d_red;
+    size_t r_cap, rx_cap, x_cap;
+    uint64_t a_hash;
+
+    struct gb_plan *next;             /* side-table chaining */
+} gb_plan;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int gb_vec_push(gb_vec *v, const void *e);
+void gb_vec_free(gb_vec *v);
+
+/* Build the plan (host side) for a supernodal symbolic factor. */
+gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols);
+/* Upload the pattern, task arrays and launch sequences. */
+int gb_plan_upload(gb_plan *P);
+void gb_plan_free(gb_plan *P);
+uint64_t gb_pattern_hash(const cholmod_factor *L);
+
+/* kernel launchers (gb_kernels.cu); dtype 0 = double, 4 = single; each
+ * enqueues on st and returns the cudaError_t of the launch as int */
+int gb_launch_assemble(const gb_pattern_ptrs *pp, const gb_asm_task *tasks, int ntasks,
+                       const int64_t *Sp, const int64_t *Si, const void *Sx, int a_dtype,
+                       const double *scale, double beta, void *Lx, void *CB, int l_dtype,
+                       cudaStream_t st);
+int gb_launch_factor_small(const gb_pattern_ptrs *pp, const gb_node_task *tasks, int ntasks,
+                           void *Lx, int dtype, cudaStream_t st);
+int gb_launch_potrf_diag(const gb_pattern_ptrs *pp, const gb_potrf_task *tasks, int ntasks,
+                         void *Lx, int dtype, cudaStream_t st);
+int gb_launch_trsm_rows(const gb_pattern_ptrs *pp, const gb_trsm_task *tasks, int ntasks,
+                        void *Lx, int dtype, cudaStream_t st);
+int gb_launch_gemm(const gb_pattern_ptrs *pp, const gb_gemm_task *tasks, const int32_t *owner,
+                   int ntasks, void *Lx, void *CB, int dtype, cudaStream_t st);
+int gb_launch_sweep_node(int kind, const gb_pattern_ptrs *pp, const gb_node_task *tasks,
+                         int ntasks, const void *Lx, int dtype, int nrhs, void *Y,
+                         int64_t ldy, void *U, cudaStream_t st);
+int gb_launch_sweep_step(int kind, const gb_pattern_ptrs *pp, const gb_sweep_task *tasks,
+                         int ntasks, const void *Lx, int dtype, int nrhs, void *Y,
+                         int64_t ldy, void *U, cudaStream_t st);
+int gb_launch_perm_in(int64_t n, int nrhs, const int64_t *perm, const double *scale,
+                      const void *B, int b_dtype, int64_t ldb, void *Y, int y_dtype,
+                      int64_t ldy, cudaStream_t st);
+int gb_launch_perm_out(int64_t n, int nrhs, const int64_t *perm, const double *scale,
+                       const void *Y, int y_dtype, int64_t ldy, void *X, int x_dtype,
+                       int64_t ldx, int add, cudaStream_t st);
+int gb_launch_residual(int64_t n, int nrhs, const int64_t *Rp, const int32_t *Rj,
+                       const double *Rx, const double *X, int64_t ldx, const double *B,
+                       int64_t ldb, double *R, int64_t ldr, cudaStream_t st);
+int gb_launch_colmax3(int64_t n, int nrhs, const double *R, int64_t ldr, const double *X,
+                      int64_t ldx, const double *B, int64_t ldb, double *out, cudaStream_t st);
+int gb_launch_anorm(int64_t n, const int64_t *Rp, const double *Rx, double *out, cudaStream_t st);
+int gb_launch_zero_range(void *x, int dtype, int64_t from, int64_t to, cudaStream_t st);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,268 @@
+"""Seeded synthetic SPD matrices for the supernodal Cholesky workloads.
+
+Every generator is deterministic across machines (x86_64 and aarch64): values
+are built only from IEEE-754 +, -, *, / and sqrt (each correctly rounded in
+numpy's elementwise ufuncs) and a counter-based splitmix64 stream, never from
+libm transcendental functions whose last bit can differ between platforms.
+Log-uniform samples use :func:`det_exp`, an exp written here from its
+definition (Cody-Waite range reduction + Taylor polynomial).
+
+Matrices are returned as the lower triangle in compressed-column form with
+sorted row indices (CHOLMOD's ``stype = -1`` symmetric-lower convention,
+cholmod.h:1168-1206): ``(n, Ap int64[n+1], Ai int64[nnz], Ax float64[nnz])``.
+
+Workloads (each a stand-in with the reference benchmark's shapes, sizes and
+value distributions; no public matrix collection is read):
+  * ``laplace2d(nx, ny, ...)`` 5-point Dirichlet Laplacian, constant or
+    log-uniform edge coefficients, optional diagonal shift.
+  * ``laplace3d(nx, ny, nz, ...)`` 7-point Dirichlet Laplacian.
+  * ``elastic27(m, seed)`` 27-point stencil with 3 unknowns per grid node.
+"""
+import numpy as np
+
+_GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed, count, offset=0):
+    """``count`` outputs of the splitmix64 stream of ``seed`` (uint64)."""
+    with np.errstate(over="ignore"):
+        k = np.arange(offset + 1, offset + count + 1, dtype=np.uint64)
+        z = np.uint64(seed) + k * _GOLDEN
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform01(seed, count, offset=0):
+    """Uniform doubles in [0, 1) with 53 random bits."""
+    z = splitmix64(seed, count, offset) >> np.uint64(11)
+    return z.astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+_LN2_HI = 6.93147180369123816490e-01   # ln 2 split so that k*_LN2_HI is exact
+_LN2_LO = 1.90821492927058770002e-10
+
+
+def det_exp(x):
+    """exp(x) from +,-,* only: x = k ln2 + r, |r| <= ln2/2, Taylor to r^17."""
+    x = np.asarray(x, dtype=np.float64)
+    k = np.rint(x * (1.0 / 0.6931471805599453))
+    r = (x - k * _LN2_HI) - k * _LN2_LO
+    p = np.ones_like(r)
+    for j in range(17, 0, -1):          # Horner: 1 + r/1 (1 + r/2 (1 + ...))
+        p = 1.0 + (r / float(j)) * p
+    return np.ldexp(p, k.astype(np.int64))
+
+
+def log_uniform(lo, hi, u):
+    """Map uniform u in [0,1) to log-uniform values in [lo, hi]."""
+    a = float(np.log(lo))   # constants: identical on any IEEE platform
+    b = float(np.log(hi))
+    return det_exp(a + u * (b - a))
+
+
+def _csc_lower(n, rows, cols, vals):
+    """Sum duplicates of (rows >= cols) triplets into sorted lower CSC."""
+    keep = rows >= cols
+    rows, cols, vals = rows[keep], cols[keep], vals[keep]
+    order = np.lexsort((rows, cols))
+    rows, cols, vals = rows[order], cols[order], vals[order]
+    key = cols * np.int64(n) + rows
+    uniq, start = np.unique(key, return_index=True)
+    sums = np.add.reduceat(vals, start) if len(vals) else vals
+    Ai = (uniq % n).astype(np.int64)
+    Aj = (uniq // n).astype(np.int64)
+    Ap = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(Ap, Aj + 1, 1)
+    Ap = np.cumsum(Ap).astype(np.int64)
+    return n, Ap, Ai, np.ascontiguousarray(sums, dtype=np.float64)
+
+
+def _grid_laplacian(dims, coef, shift):
+    """Dirichlet graph Laplacian on a box grid; ``coef[d]`` are the edge
+    conductivities of direction d, shape dims with dims[d] + 1 along axis d
+    (edges to the ghost layer on both faces included)."""
+    dims = tuple(int(v) for v in dims)
+    n = int(np.prod(dims))
+    idx = np.arange(n, dtype=np.int64).reshape(dims[::-1]).transpose()  # x fastest
+    diag = np.full(dims, float(shift))
+    rows, cols, vals = [], [], []
+    for d, c in enumerate(coef):
+        lo = [slice(None)] * len(dims)
+        hi = [slice(None)] * len(dims)
+        lo[d] = slice(0, dims[d])       # edge before node
+        hi[d] = slice(1, dims[d] + 1)   # edge after node
+        diag = diag + c[tuple(lo)] + c[tuple(hi)]
+        a = [slice(None)] * len(dims)
+        b = [slice(None)] * len(dims)
+        a[d] = slice(0, dims[d] - 1)
+        b[d] = slice(1, dims[d])
+        inner = [slice(None)] * len(dims)
+        inner[d] = slice(1, dims[d])
+        i = idx[tuple(b)].ravel(order="F")
+        j = idx[tuple(a)].ravel(order="F")
+        v = -c[tuple(inner)].ravel(order="F")
+        rows.append(i)
+        cols.append(j)
+        vals.append(v)
+    rows.append(idx.ravel(order="F"))
+    cols.append(idx.ravel(order="F"))
+    vals.append(diag.ravel(order="F"))
+    return _csc_lower(n, np.concatenate(rows), np.concatenate(cols),
+                      np.concatenate(vals))
+
+
+def _edge_coefs(dims, seed, lo, hi):
+    coef = []
+    offset = 0
+    for d in range(len(dims)):
+        shp = list(dims)
+        shp[d] += 1
+        cnt = int(np.prod(shp))
+        u = uniform01(seed, cnt, offset)
+        offset += cnt
+        coef.append(log_uniform(lo, hi, u).reshape(shp[::-1]).transpose())
+    return coef
+
+
+def laplace2d(nx, ny=None, seed=None, lo=1e-2, hi=1e2, shift=0.0):
+    """2D 5-point Laplacian; constant unit coefficients when seed is None."""
+    ny = nx if ny is None else ny
+    dims = (nx, ny)
+    if seed is None:
+        coef = [np.ones((nx + 1, ny)), np.ones((nx, ny + 1))]
+    else:
+        coef = _edge_coefs(dims, seed, lo, hi)
+    return _grid_laplacian(dims, coef, shift)
+
+
+def laplace3d(nx, ny=None, nz=None, seed=None, lo=1e-2, hi=1e2, shift=0.0):
+    """3D 7-point Laplacian; constant unit coefficients when seed is None."""
+    ny = nx if ny is None else ny
+    nz = nx if nz is None else nz
+    dims = (nx, ny, nz)
+    if seed is None:
+        coef = [np.ones((nx + 1, ny, nz)), np.ones((nx, ny + 1, nz)),
+                np.ones((nx, ny, nz + 1))]
+    else:
+        coef = _edge_coefs(dims, seed, lo, hi)
+    return _grid_laplacian(dims, coef, shift)
+
+
+def _rotations(u):
+    """Rotation matrices from unit quaternions built from 4 uniforms each."""
+    q = 2.0 * u.reshape(-1, 4) - 1.0
+    nrm = np.sqrt((q * q).sum(axis=1))
+    nrm[nrm == 0] = 1.0
+    w, x, y, z = (q / nrm[:, None]).T
+    R = np.empty((len(w), 3, 3))
+    R[:, 0, 0] = 1 - 2 * (y * y + z * z)
+    R[:, 0, 1] = 2 * (x * y - z * w)
+    R[:, 0, 2] = 2 * (x * z + y * w)
+    R[:, 1, 0] = 2 * (x * y + z * w)
+    R[:, 1, 1] = 1 - 2 * (x * x + z * z)
+    R[:, 1, 2] = 2 * (y * z - x * w)
+    R[:, 2, 0] = 2 * (x * z - y * w)
+    R[:, 2, 1] = 2 * (y * z + x * w)
+    R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return R
+
+
+def _spd_blocks(seed, count, offset, lo=0.1, hi=10.0):
+    """``count`` random 3x3 SPD blocks Q diag(lam) Q', lam log-uniform."""
+    u = uniform01(seed, 7 * count, offset)
+    lam = log_uniform(lo, hi, u[:3 * count]).reshape(count, 3)
+    Q = _rotations(u[3 * count:])
+    B = np.einsum("kij,kj,klj->kil", Q, lam, Q)
+    return 0.5 * (B + B.transpose(0, 2, 1))
+
+
+def elastic27(m, seed=2, dof=3, margin=1e-6):
+    """27-point stencil on an m^3 grid with 3 unknowns per node.
+
+    Each coupling between two neighbouring nodes is minus a random 3x3 SPD
+    block (eigenvalues log-uniform in [0.1, 10]); each node's own block is a
+    random SPD block whose diagonal is then raised, where needed, so that
+    every row is strictly diagonally dominant by ``margin``.
+    """
+    assert dof == 3
+    nn = m ** 3
+    n = nn * 3
+    node = np.arange(nn, dtype=np.int64).reshape(m, m, m).transpose()  # x fastest
+    offs = [(dx, dy, dz) for dz in (-1, 0, 1) for dy in (-1, 0, 1)
+            for dx in (-1, 0, 1) if (dx, dy, dz) > (0, 0, 0)]
+    # forward neighbour pairs (13 directions), lexicographically positive
+    pi, pj = [], []
+    for (dx, dy, dz) in offs:
+        xs = slice(max(0, -dx), m - max(0, dx))
+        ys = slice(max(0, -dy), m - max(0, dy))
+        zs = slice(max(0, -dz), m - max(0, dz))
+        a = node[xs, ys, zs]
+        b = node[slice(xs.start + dx, xs.stop + dx), slice(ys.start + dy, ys.stop + dy),
+                 slice(zs.start + dz, zs.stop + dz)]
+        pi.append(a.ravel(order="F"))
+        pj.append(b.ravel(order="F"))
+    pi = np.concatenate(pi)
+    pj = np.concatenate(pj)
+    npair = len(pi)
+    Boff = -_spd_blocks(seed, npair, 0)
+    Bdiag = _spd_blocks(seed, nn, 7 * npair)
+    # row sums of |off-diagonal| for diagonal dominance
+    absoff = np.zeros((nn, 3))
+    np.add.at(absoff, pi, np.abs(Boff).sum(axis=2))
+    np.add.at(absoff, pj, np.abs(Boff).sum(axis=1))
+    own = np.abs(Bdiag).sum(axis=2) - np.abs(np.einsum("kii->ki", Bdiag))
+    need = absoff + own + margin
+    d = np.einsum("kii->ki", Bdiag)
+    newd = np.where(d >= need, d, need)
+    Bdiag = Bdiag.copy()
+    for r in range(3):
+        Bdiag[:, r, r] = newd[:, r]
+    # assemble triplets: node block (I,J) -> rows 3I+r, cols 3J+c
+    r3 = np.arange(3)
+    rows, cols, vals = [], [], []
+    # off-diagonal blocks, both (i,j) and (j,i) = block^T (symmetric blocks)
+    for (I, J, B) in ((pi, pj, Boff), (pj, pi, Boff.transpose(0, 2, 1))):
+        rows.append((3 * I[:, None, None] + r3[None, :, None]).repeat(3, axis=2).ravel())
+        cols.append((3 * J[:, None, None] + r3[None, None, :]).repeat(3, axis=1).ravel())
+        vals.append(B.ravel())
+    I = np.arange(nn, dtype=np.int64)
+    rows.append((3 * I[:, None, None] + r3[None, :, None]).repeat(3, axis=2).ravel())
+    cols.append((3 * I[:, None, None] + r3[None, None, :]).repeat(3, axis=1).ravel())
+    vals.append(Bdiag.ravel())
+    return _csc_lower(n, np.concatenate(rows).astype(np.int64),
+                      np.concatenate(cols).astype(np.int64), np.concatenate(vals))
+
+
+def rhs(n, nrhs, seed):
+    """Right-hand sides with entries i.i.d. uniform in [-1, 1], column-major."""
+    return (2.0 * uniform01(seed, n * nrhs) - 1.0).reshape(nrhs, n).T.copy(order="F")
+
+
+def full_from_lower(n, Ap, Ai, Ax):
+    """Both triangles (CSC) of a symmetric matrix stored as its lower part."""
+    cols = np.repeat(np.arange(n, dtype=np.int64), np.diff(Ap))
+    off = Ai != cols
+    r = np.concatenate([Ai, cols[off]])
+    c = np.concatenate([cols, Ai[off]])
+    v = np.concatenate([Ax, Ax[off]])
+    order = np.lexsort((r, c))
+    r, c, v = r[order], c[order], v[order]
+    Fp = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(Fp, c + 1, 1)
+    return np.cumsum(Fp).astype(np.int64), r.astype(np.int64), v
+
+
+def digest(*arrays):
+    """SHA-256 over the raw bytes of the given arrays (fixture fingerprints)."""
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        a = np.ascontiguousarray(a)
+        h.update(str(a.dtype).encode())
+        h.update(str(a.shape).encode())
+        h.update(a.tobytes())
+    return h.hexdigest()
