@@ -1,0 +1,378 @@
+"""Benchmark: supernodal Cholesky factor + solve of the 64^3 variable-coefficient
+7-point Laplacian (n = 262,144, METIS ordering) on one GB300.
+
+Metric (one JSON line on stdout): factor TFLOP/s (flop count = the symbolic
+analysis' Common->fl, each multiply and each add counted once) of the FP32
+factor + FP64 iterative-refinement form, with solves/s to backward error
+<= 1e-12, the plain FP64 form beside it, and p50/p99 step latency.
+
+A step is one factorization of the matrix (numeric values re-assembled from
+A) followed by one refined solve to 1e-12 with one right-hand side.
+  value       = fl / device time of the factorization, inputs resident on the
+                GPU (CUDA events on the library's stream)
+  e2e         = the same through the C ABI from host buffers
+                (gb300_factorize_mixed + gb300_solve_refined, pinned B/X,
+                host permutation, host->device copies and the read of X inside
+                the timed region)
+  --impl reference  times the CPU oracle (the reference's left-looking
+                supernodal algorithm over OpenBLAS, all host cores) on the same
+                matrix in FP64, the form the reference CPU path computes.
+
+Data: synthetic (seeded generator), the ordering is the reference's METIS
+permutation stored with the golden fixtures.  The factor (0.57 GB FP32,
+1.1 GB FP64) and update blocks (1-4 GB) are far larger than L2, so no L2
+flush is needed between steps.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "factor TFLOP/s + solves/s at 1e-12 backward err, FP32+IR vs FP64; p50/p99"
+WORKLOAD = "c2: 3D 7-point variable-coefficient Laplacian 64^3 (n=262144), METIS"
+
+
+def load_case(name="c2"):
+    from suitesparse_gb300 import matrices as M
+    gold = json.load(open(os.path.join(ROOT, "tests", "golden", "golden.json")))[name]
+    arrays = np.load(os.path.join(ROOT, "tests", "golden", "golden_arrays.npz"))
+    n, Ap, Ai, Ax = M.config_matrix(name)
+    perm = arrays[name + "_Perm"].astype(np.int64)
+    return gold, (n, Ap, Ai, Ax), perm
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            time.sleep(0.3)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cudart():
+    for p in ("/usr/local/cuda/lib64/libcudart.so", "libcudart.so"):
+        try:
+            return ctypes.CDLL(p)
+        except OSError:
+            continue
+    return None
+
+
+def pin(rt, arr):
+    """Page-lock a numpy array's memory (host->device copies from pinned memory)."""
+    if rt is not None and arr.nbytes:
+        rt.cudaHostRegister(ctypes.c_void_p(arr.ctypes.data), ctypes.c_size_t(arr.nbytes), 0)
+
+
+def pin_ptr(rt, ptr, nbytes):
+    if rt is not None and ptr and nbytes:
+        rt.cudaHostRegister(ctypes.c_void_p(ptr), ctypes.c_size_t(nbytes), 0)
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0"))
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return ws, rank, dist
+    return 1, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_oracle_run(mat, perm, fl, steps=1, threads=None):
+    """FP64 factor + solve with the CPU oracle over OpenBLAS; seconds per step."""
+    from oracle import oracle as O
+    from suitesparse_gb300 import cholmod as CH
+    from suitesparse_gb300 import matrices as M
+    n, Ap, Ai, Ax = mat
+    O.build()
+    O.lib(use_blas=True)
+    threads = threads or os.cpu_count() or 1
+    O.blas_threads(threads)
+    c = CH.Common()
+    A = CH.sparse(n, Ap, Ai, Ax, c)
+    L = CH.analyze_perm(A, perm, c)
+    f = CH.factor_arrays(L, with_x=False)
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+    sym = {k: f[k] for k in ("Super", "Pi", "Px", "Ls")}
+    sym["n"] = n
+    Sp, Si, Sx = O.permute_lower(n, Ap, Ai, Ax, perm)
+    B = M.rhs(n, 1, 1)
+    tf, ts, be = [], [], None
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        st, minor, Lx = O.factor(sym, Sp, Si, Sx, use_blas=True)
+        t1 = time.perf_counter()
+        X = O.solve(sym, Lx, perm, B, use_blas=True)
+        t2 = time.perf_counter()
+        tf.append(t1 - t0)
+        ts.append(t2 - t1)
+        be = float(O.backward_error(n, Ap, Ai, Ax, X, B).max())
+    return tf, ts, be, threads
+
+
+def run_reference(args):
+    ws, rank, dist = dist_setup()
+    if rank != 0:
+        return 0
+    gold, mat, perm = load_case()
+    fl = gold["fl"]
+    tf, ts, be, threads = cpu_oracle_run(mat, perm, fl, steps=args.warmup + args.steps)
+    tf, ts = tf[args.warmup:], ts[args.warmup:]
+    t_step = [a + b for a, b in zip(tf, ts)]
+    value = fl / statistics.mean(tf) / 1e12
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.mean(t_step), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": "FP64 supernodal LL' + solve (CPU)",
+                   "l2": "inputs larger than L2"},
+        "solves_per_s": 1.0 / statistics.mean(t_step),
+        "p50_ms": 1e3 * statistics.median(t_step),
+        "p99_ms": 1e3 * float(np.percentile(t_step, 99)),
+        "backward_error": be,
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+                         "sample": "full c2 FP64 factorization + 1-RHS solve per step"},
+        "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    ws, rank, dist = dist_setup()
+    from suitesparse_gb300 import cholmod as CH
+    from suitesparse_gb300 import matrices as M
+    from oracle import oracle as O
+    gold, mat, perm = load_case()
+    n, Ap, Ai, Ax = mat
+    fl = gold["fl"]
+    rt = cudart()
+    c = CH.Common()
+    A = CH.sparse(n, Ap, Ai, Ax, c)
+    a = A.contents
+    pin_ptr(rt, a.p, 8 * (n + 1))
+    pin_ptr(rt, a.i, 8 * int(Ap[-1]))
+    pin_ptr(rt, a.x, 8 * int(Ap[-1]))
+    L = CH.analyze_perm(A, perm, c)
+    assert c["fl"] == fl
+    B = M.rhs(n, 1, 1)
+    info = CH.factor_info(L, c)
+
+    def step_mixed():
+        t0 = time.perf_counter()
+        ok = CH.factorize_mixed(A, L, c)
+        st = c.stats()
+        X, rinfo = CH.solve_refined(A, L, B, c, tol=1e-12)
+        t1 = time.perf_counter()
+        st2 = c.stats()
+        assert ok, c.status
+        return st[0], st2[2], t1 - t0, X, rinfo
+
+    for _ in range(args.warmup):
+        step_mixed()
+    barrier(dist)
+    l0 = c.stats()[5]
+    fac_ms, sol_ms, e2e_s, infos = [], [], [], []
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0")) if ws == 1 else 0) as clk:
+        t_all = time.perf_counter()
+        for _ in range(args.steps):
+            f_ms, s_ms, w_s, X, rinfo = step_mixed()
+            fac_ms.append(f_ms)
+            sol_ms.append(s_ms)
+            e2e_s.append(w_s)
+            infos.append(rinfo)
+        t_all = time.perf_counter() - t_all
+    launches = int(c.stats()[5] - l0)
+    barrier(dist)
+    t_fac = max_over_ranks(dist, statistics.mean(fac_ms))
+    t_step = [a + b for a, b in zip(fac_ms, sol_ms)]
+    be = float(O.backward_error(n, Ap, Ai, Ax, X, B).max())
+
+    # plain FP64 form (drop-in path: cholmod_l_super_numeric + supernodal sweeps)
+    fp64_fac, fp64_sol = [], []
+    for i in range(args.fp64_steps + 1):
+        ok = CH.factorize(A, L, c)
+        f64 = c.stats()[0]
+        X64 = CH.solve(L, B, c)
+        s64 = c.stats()[1]
+        if i > 0:
+            fp64_fac.append(f64)
+            fp64_sol.append(s64)
+    be64 = float(O.backward_error(n, Ap, Ai, Ax, X64, B).max())
+
+    # resident-factor solve throughput at 1, 8, 64 right-hand sides
+    CH.factorize_mixed(A, L, c)
+    solves = {}
+    for k in (1, 8, 64):
+        Bk = M.rhs(n, k, 10 + k)
+        CH.solve_refined(A, L, Bk, c)
+        ts = []
+        for _ in range(3):
+            Xk, rk = CH.solve_refined(A, L, Bk, c)
+            ts.append(c.stats()[2])
+        solves[str(k)] = {"solves_per_s": k / (statistics.mean(ts) * 1e-3),
+                          "iterations": rk["iterations"], "berr": rk["berr"]}
+
+    # roofline of the dominant kernel (tile update) from a profiled factorization
+    c.set_option(CH.GB300_OPT_PROFILE, 1)
+    CH.factorize_mixed(A, L, c)
+    prof = c.profile()
+    c.set_option(CH.GB300_OPT_PROFILE, 0)
+    peak32 = CH.fma_peak("s")
+    peak64 = CH.fma_peak("d")
+    g_ms, g_n = prof.get("gemm_tile", (0.0, 0))
+    achieved = info["fl_gemm"] / (g_ms * 1e-3) / 1e12 if g_ms else None
+    prof_total = sum(v[0] for v in prof.values()) or 1.0
+
+    value = fl / (t_fac * 1e-3) / 1e12 * ws
+    e2e_val = fl / statistics.mean(e2e_s) / 1e12 * ws
+    nnz = int(Ap[-1])
+    # bytes moved per e2e step: S (p, i, x) and both triangles of A (p, j, x),
+    # the scaling vectors, B in; X out
+    h2d = 8 * (n + 1) + 16 * nnz + 8 * (n + 1) + 12 * (2 * nnz - n) + 16 * n + 8 * n
+    d2h = 8 * n
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": statistics.mean(t_step), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 factor + f64 refinement",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": "FP32 supernodal LL' (diagonal scaling) + "
+                   "FP64 iterative refinement to 1e-12", "nrhs": 1,
+                   "l2": "inputs larger than L2 (factor + update blocks > 1.5 GB)",
+                   "parallelism": "replicas" if ws > 1 else "1 GPU"},
+        "solves_per_s": 1e3 / statistics.mean(t_step) * ws,
+        "p50_ms": statistics.median(t_step),
+        "p99_ms": float(np.percentile(t_step, 99)),
+        "backward_error": be,
+        "refine_iterations": [r["iterations"] for r in infos][-1],
+        "fp64_fallback": any(r["fp64_fallback"] for r in infos),
+        "fp64": {"factor_tflops": fl / (statistics.mean(fp64_fac) * 1e-3) / 1e12,
+                 "factor_ms": statistics.mean(fp64_fac), "solve_ms": statistics.mean(fp64_sol),
+                 "solves_per_s": 1e3 / (statistics.mean(fp64_fac) + statistics.mean(fp64_sol)),
+                 "backward_error": be64},
+        "speedup_solves_vs_fp64": (1e3 / statistics.mean(t_step)) /
+                                  (1e3 / (statistics.mean(fp64_fac) + statistics.mean(fp64_sol))),
+        "resident_factor_solves": solves,
+        "e2e": {"value": e2e_val, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "solves_per_s": 1.0 / statistics.mean(e2e_s) * ws},
+        "roofline": {"kernel": "k_gemm_nt<float> (update-block / trailing tile update)",
+                     "bound": "compute (FP32 FMA pipe, SIMT)", "achieved": achieved,
+                     "peak": peak32, "unit": "TFLOP/s",
+                     "frac": (achieved / peak32) if (achieved and peak32) else None,
+                     "peak_source": "measured: FMA-chain probe gb300_fma_peak in this run",
+                     "traffic": None, "share_of_factor_time": g_ms / prof_total,
+                     "fp64_fma_peak": peak64},
+        "kernel_profile_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
+        "plan": info,
+        "gpu_launches": launches,
+        "wall_s_timed_region": t_all,
+        "clocks": clk.summary(),
+    }
+    if args.cpu_baseline and rank == 0:
+        tf, ts, bec, threads = cpu_oracle_run(mat, perm, fl, steps=1)
+        line["cpu_baseline"] = {"value": fl / tf[0] / 1e12, "unit": "TFLOP/s", "cores": threads,
+                                "kind": "port",
+                                "sample": "one full c2 FP64 factorization (oracle over "
+                                          "OpenBLAS, the reference's left-looking algorithm)",
+                                "solve_s": ts[0]}
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+    c.finish()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

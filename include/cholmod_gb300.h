@@ -339,9 +339,13 @@ int gb300_finish (cholmod_common *Common) ;
  *  GB300_OPT_KEEP_ON_DEVICE [0]: 1 = do not copy L->x back to the host after
  *      the factorization; the factor stays resident on the GPU for solves.
  *  GB300_OPT_SMALL_COLS [64]: supernodes at most this wide are factorized by
- *      one thread block each; wider ones by the blocked multi-block path. */
+ *      one thread block each; wider ones by the blocked multi-block path.
+ *  GB300_OPT_PROFILE [0]: 1 = time every kernel launch of the factorization
+ *      with CUDA events (summed per kernel kind, see gb300_get_profile); also
+ *      clears the accumulated profile. */
 #define GB300_OPT_KEEP_ON_DEVICE 1
 #define GB300_OPT_SMALL_COLS     2
+#define GB300_OPT_PROFILE        3
 int gb300_set_option (cholmod_common *Common, int option, int64_t value) ;
 
 /* Supernodal symbolic analysis of A (stype < 0, lower) with a given final
@@ -404,10 +408,26 @@ int gb300_free_factor (cholmod_factor **L, cholmod_common *Common) ;
 long gb300_abi_offset (int object, const char *field) ;
 long gb300_abi_sizeof (int object) ;
 
+/* Per-kernel-kind totals of the profiled factorizations: ms[k] and count[k]
+ * for kind k = 1 assembly, 2 small-supernode factor, 3 diagonal-block LL',
+ * 4 panel triangular solve, 5 tile update (C -= A B'). */
+int gb300_get_profile (cholmod_common *Common, double *ms, double *count, int nkinds) ;
+
+/* Facts of the GPU plan of L (built if needed): [0] algorithmic flops of the
+ * tile updates, [1] etree levels, [2] launches per factorization, [3]
+ * update-block entries, [4] tile-update tasks, [5] supernodes, [6] launches
+ * per forward sweep, [7] per backward sweep, [8] update-vector entries,
+ * [9] mixed state (0 none, 1 FP32 factor, 2 FP64 factor). */
+int gb300_factor_info (cholmod_factor *L, cholmod_common *Common, double *out, int nout) ;
+
+/* Measured multiply-add throughput of the current GPU's FP64 (dtype 0) or
+ * FP32 (dtype 4) pipes, TFLOP/s (a register-resident FMA-chain probe). */
+int gb300_fma_peak (int dtype, double *tflops) ;
+
 /* Last device-side timings of this library for Common (milliseconds, CUDA
  * events on the library's stream): [0] factor, [1] last solve sweep pair,
  * [2] refined solve total, [3] assembly, [4] kernel launches of the last
- * factorization (count). */
+ * factorization (count), [5] kernel launches issued through Common so far. */
 int gb300_get_stats (cholmod_common *Common, double *out, int nout) ;
 
 #ifdef __cplusplus

@@ -1,0 +1,181 @@
+"""Python side of the CPU oracle (oracle/oracle.c).
+
+TEST INFRASTRUCTURE: the checker for tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py.  Never imported by the product.
+
+``build()`` compiles oracle.c with gcc into oracle/liboracle.so.  When the
+OpenBLAS bundled with scipy is present (both here and on the GPU host), its
+Fortran-ABI routines are installed as the oracle's dense kernels, as the
+reference CHOLMOD uses an external BLAS; otherwise the oracle's own loops run.
+"""
+import ctypes as C
+import glob
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+_lib = None
+_blas = None
+
+
+def build():
+    src = [os.path.join(HERE, "oracle.c")]
+    hdr = os.path.join(HERE, "oracle_body.h")
+    newest = max(os.path.getmtime(p) for p in src + [hdr])
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-o", LIB + ".tmp"] + src + ["-lm"],
+                   check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def openblas():
+    """ctypes handle of scipy's bundled OpenBLAS, or None."""
+    global _blas
+    if _blas is not None:
+        return _blas or None
+    try:
+        import scipy
+        d = os.path.join(os.path.dirname(scipy.__file__), "..", "scipy.libs")
+        libs = sorted(glob.glob(os.path.join(d, "libscipy_openblas*.so")))
+        _blas = C.CDLL(libs[0]) if libs else False
+    except Exception:
+        _blas = False
+    return _blas or None
+
+
+def lib(use_blas=True):
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = C.CDLL(LIB)
+        _lib.oracle_super_numeric.restype = C.c_int
+        _lib.oracle_super_solve.restype = C.c_int
+        _lib.oracle_has_blas.restype = C.c_int
+    set_blas(use_blas)
+    return _lib
+
+
+def set_blas(on=True):
+    L = _lib
+    b = openblas() if on else None
+    if b is None:
+        L.oracle_set_blas(*([None] * 8))
+        return False
+    names = ["scipy_dgemm_", "scipy_dsyrk_", "scipy_dtrsm_", "scipy_dpotrf_",
+             "scipy_sgemm_", "scipy_ssyrk_", "scipy_strsm_", "scipy_spotrf_"]
+    ptrs = [C.cast(getattr(b, nm), C.c_void_p) for nm in names]
+    L.oracle_set_blas(*ptrs)
+    return True
+
+
+def blas_threads(n):
+    """Set the OpenBLAS thread count (returns False without OpenBLAS)."""
+    b = openblas()
+    if b is None:
+        return False
+    for nm in ("scipy_openblas_set_num_threads", "openblas_set_num_threads"):
+        if hasattr(b, nm):
+            getattr(b, nm)(int(n))
+            return True
+    return False
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def factor(sym, Sp, Si, Sx, beta=0.0, dtype="d", quick_return=False, use_blas=True):
+    """Supernodal LL' of S = tril(PAP') (sorted lower CSC) on the pattern
+    ``sym`` (dict with n, Super, Pi, Px, Ls).  Returns (status, minor, Lx)."""
+    L = lib(use_blas)
+    Super, Pi, Px, Ls = (np.ascontiguousarray(sym[k], np.int64) for k in ("Super", "Pi", "Px", "Ls"))
+    n, nsuper = int(sym["n"]), len(Super) - 1
+    rt = np.float32 if dtype == "s" else np.float64
+    Sp = np.ascontiguousarray(Sp, np.int64)
+    Si = np.ascontiguousarray(Si, np.int64)
+    Sx = np.ascontiguousarray(Sx, rt)
+    Lx = np.zeros(max(int(Px[-1]), 1), rt)
+    minor = C.c_int64(0)
+    st = L.oracle_super_numeric(4 if dtype == "s" else 0, C.c_int64(n), C.c_int64(nsuper),
+                                _p(Super, C.c_int64), _p(Pi, C.c_int64), _p(Px, C.c_int64),
+                                _p(Ls, C.c_int64), _p(Sp, C.c_int64), _p(Si, C.c_int64),
+                                Sx.ctypes.data_as(C.c_void_p), C.c_double(beta),
+                                C.c_int(1 if quick_return else 0),
+                                Lx.ctypes.data_as(C.c_void_p), C.byref(minor))
+    return st, minor.value, Lx[:int(Px[-1])]
+
+
+def sweep(sym, Lx, X, lower, dtype="d", use_blas=True):
+    """Forward (lower=True: X = L\\X) or backward (X = L'\\X) sweep, in place
+    on a copy of X (n x nrhs, permuted order); returns the result."""
+    L = lib(use_blas)
+    Super, Pi, Px, Ls = (np.ascontiguousarray(sym[k], np.int64) for k in ("Super", "Pi", "Px", "Ls"))
+    rt = np.float32 if dtype == "s" else np.float64
+    X = np.array(X, dtype=rt, order="F", copy=True)
+    if X.ndim == 1:
+        X = X[:, None].copy(order="F")
+    n, nrhs = X.shape
+    Lx = np.ascontiguousarray(Lx, rt)
+    st = L.oracle_super_solve(4 if dtype == "s" else 0, C.c_int(1 if lower else 0),
+                              C.c_int64(n), C.c_int64(len(Super) - 1), _p(Super, C.c_int64),
+                              _p(Pi, C.c_int64), _p(Px, C.c_int64), _p(Ls, C.c_int64),
+                              Lx.ctypes.data_as(C.c_void_p), C.c_int64(nrhs),
+                              X.ctypes.data_as(C.c_void_p), C.c_int64(n))
+    if st != 0:
+        raise RuntimeError("oracle sweep failed")
+    return X
+
+
+def permute_lower(n, Ap, Ai, Ax, perm):
+    """S = tril(A(p,p)) in sorted CSC (numpy), A given by its lower part."""
+    pinv = np.empty(n, np.int64)
+    pinv[np.asarray(perm, np.int64)] = np.arange(n, dtype=np.int64)
+    cols = np.repeat(np.arange(n, dtype=np.int64), np.diff(Ap))
+    keep = Ai >= cols
+    i, j, x = pinv[Ai[keep]], pinv[cols[keep]], Ax[keep]
+    r, c = np.maximum(i, j), np.minimum(i, j)
+    order = np.lexsort((r, c))
+    r, c, x = r[order], c[order], x[order]
+    Sp = np.zeros(n + 1, np.int64)
+    np.add.at(Sp, c + 1, 1)
+    return np.cumsum(Sp).astype(np.int64), r.astype(np.int64), x
+
+
+def solve(sym, Lx, perm, B, dtype="d", use_blas=True):
+    """X = A\\B through the oracle factor: P, forward, backward, P'."""
+    B = np.asarray(B)
+    if B.ndim == 1:
+        B = B[:, None]
+    perm = np.asarray(perm, np.int64)
+    Y = B[perm, :]
+    Y = sweep(sym, Lx, Y, True, dtype, use_blas)
+    Y = sweep(sym, Lx, Y, False, dtype, use_blas)
+    X = np.empty_like(Y)
+    X[perm, :] = Y
+    return X
+
+
+def backward_error(n, Ap, Ai, Ax, X, B):
+    """|b - A x|_inf / (|A|_inf |x|_inf + |b|_inf) per column (A lower-stored
+    symmetric), the measure of CHOLMOD/Demo/cholmod_di_demo.c:614-617."""
+    X = np.asarray(X, np.float64)
+    B = np.asarray(B, np.float64)
+    if X.ndim == 1:
+        X, B = X[:, None], B[:, None]
+    cols = np.repeat(np.arange(n, dtype=np.int64), np.diff(Ap))
+    off = Ai != cols
+    AX = np.zeros_like(X)
+    np.add.at(AX, Ai, Ax[:, None] * X[cols])
+    np.add.at(AX, cols[off], Ax[off][:, None] * X[Ai[off]])
+    rowsum = np.zeros(n)
+    np.add.at(rowsum, Ai, np.abs(Ax))
+    np.add.at(rowsum, cols[off], np.abs(Ax[off]))
+    anorm = rowsum.max() if n else 0.0
+    R = B - AX
+    return np.abs(R).max(axis=0) / (anorm * np.abs(X).max(axis=0) + np.abs(B).max(axis=0))

@@ -21,7 +21,8 @@ CHOLMOD_OK, CHOLMOD_NOT_INSTALLED, CHOLMOD_OUT_OF_MEMORY = 0, -1, -2
 CHOLMOD_TOO_LARGE, CHOLMOD_INVALID, CHOLMOD_GPU_PROBLEM = -3, -4, -5
 CHOLMOD_NOT_POSDEF, CHOLMOD_DSMALL = 1, 2
 CHOLMOD_A = 0
-GB300_OPT_KEEP_ON_DEVICE, GB300_OPT_SMALL_COLS = 1, 2
+GB300_OPT_KEEP_ON_DEVICE, GB300_OPT_SMALL_COLS, GB300_OPT_PROFILE = 1, 2, 3
+KIND_NAMES = {1: "assemble", 2: "factor_small", 3: "potrf_diag", 4: "trsm_rows", 5: "gemm_tile"}
 
 
 class cholmod_sparse(C.Structure):
@@ -87,6 +88,9 @@ def lib():
         "gb300_factorize_mixed": (C.c_int, [SP, FP, vp]),
         "gb300_solve_refined": (DP, [SP, FP, DP, C.c_double, C.POINTER(C.c_double), vp]),
         "gb300_release_factor": (C.c_int, [FP, vp]),
+        "gb300_get_profile": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]),
+        "gb300_factor_info": (C.c_int, [FP, vp, C.POINTER(C.c_double), C.c_int]),
+        "gb300_fma_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
         "cholmod_l_super_numeric": (C.c_int, [SP, SP, C.POINTER(C.c_double), FP, vp]),
         "cholmod_l_super_lsolve": (C.c_int, [FP, DP, DP, vp]),
         "cholmod_l_super_ltsolve": (C.c_int, [FP, DP, DP, vp]),
@@ -140,6 +144,12 @@ class Common:
         out = (C.c_double * 8)()
         lib().gb300_get_stats(self.ptr, out, 8)
         return list(out)
+
+    def profile(self):
+        ms = (C.c_double * 16)()
+        cnt = (C.c_double * 16)()
+        lib().gb300_get_profile(self.ptr, ms, cnt, 16)
+        return {KIND_NAMES.get(k, str(k)): (ms[k], cnt[k]) for k in range(16) if cnt[k]}
 
     def finish(self):
         if self.ptr:
@@ -255,3 +265,34 @@ def solve(L, B, common, dtype="d"):
     out = dense_array(X)
     free_dense(X, common)
     return out
+
+
+def factor_info(L, common):
+    out = (C.c_double * 10)()
+    if not lib().gb300_factor_info(L, common.ptr, out, 10):
+        raise RuntimeError(f"factor_info failed, status {common.status}")
+    keys = ["fl_gemm", "nlevels", "launches_factor", "cb_entries", "gemm_tasks", "nsuper",
+            "launches_fwd", "launches_bwd", "cbv_entries", "mixed"]
+    return dict(zip(keys, list(out)))
+
+
+def fma_peak(dtype="d"):
+    out = C.c_double(0)
+    ok = lib().gb300_fma_peak(4 if dtype == "s" else 0, C.byref(out))
+    return out.value if ok else None
+
+
+def factorize_mixed(A, L, common):
+    return lib().gb300_factorize_mixed(A, L, common.ptr)
+
+
+def solve_refined(A, L, B, common, tol=1e-12):
+    Bd = dense(B, common)
+    info = (C.c_double * 4)()
+    X = lib().gb300_solve_refined(A, L, Bd, tol, info, common.ptr)
+    free_dense(Bd, common)
+    if not X:
+        raise RuntimeError(f"refined solve failed, status {common.status}")
+    out = dense_array(X)
+    free_dense(X, common)
+    return out, {"iterations": int(info[0]), "berr": info[1], "fp64_fallback": bool(info[2])}

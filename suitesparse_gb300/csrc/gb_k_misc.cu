@@ -1,0 +1,265 @@
+// gb_k_misc.cu -- permutation with scaling, FP64 residual r = b - A x,
+// norms for the backward error, diagonal extremes of the factor, clearing.
+#include "gb_k_common.cuh"
+
+// ---------------------------------------------------------------------------
+// permutations, scaling, residual (FP64) and norms
+// ---------------------------------------------------------------------------
+
+// Y(k, r) = scale(k-th permuted) * B(perm[k], r), converting type
+template <typename TB, typename TY>
+__global__ void k_perm_in(int64_t n, int nrhs, const int64_t *__restrict__ perm,
+                          const double *__restrict__ scale, const TB *__restrict__ B,
+                          int64_t ldb, TY *Y, int64_t ldy)
+{
+    const int64_t total = n * nrhs;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = idx % n, r = idx / n;
+        const int64_t i = perm ? perm[k] : k;
+        double v = (double)B[i + r * ldb];
+        if (scale) v *= scale[i];
+        Y[k + r * ldy] = (TY)v;
+    }
+}
+
+// X(perm[k], r) = scale(perm[k]) * Y(k, r)  [op 0: assign, op 1: add]
+template <typename TY, typename TX>
+__global__ void k_perm_out(int64_t n, int nrhs, const int64_t *__restrict__ perm,
+                           const double *__restrict__ scale, const TY *__restrict__ Y,
+                           int64_t ldy, TX *X, int64_t ldx, int add)
+{
+    const int64_t total = n * nrhs;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = idx % n, r = idx / n;
+        const int64_t i = perm ? perm[k] : k;
+        double v = (double)Y[k + r * ldy];
+        if (scale) v *= scale[i];
+        if (add) X[i + r * ldx] += (TX)v;
+        else X[i + r * ldx] = (TX)v;
+    }
+}
+
+// R = B - A X with A in full compressed-row form (both triangles), FP64,
+// one thread per (row, column of X), sequential sum: fixed order.
+__global__ void k_residual(int64_t n, int nrhs, const int64_t *__restrict__ Rp,
+                           const int32_t *__restrict__ Rj, const double *__restrict__ Rx,
+                           const double *__restrict__ X, int64_t ldx,
+                           const double *__restrict__ B, int64_t ldb,
+                           double *R, int64_t ldr)
+{
+    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < n * nrhs;
+         w += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = w % n, r = w / n;
+        const double *x = X + r * ldx;
+        double acc = 0.0;
+        for (int64_t p = Rp[i]; p < Rp[i + 1]; p++) acc += Rx[p] * x[Rj[p]];
+        R[i + r * ldr] = B[i + r * ldb] - acc;
+    }
+}
+
+// out[0] = min over the diagonal of L of L(k,k)^2, out[1] = max (one block)
+template <typename T>
+__global__ void k_diag_minmax(int nsuper, const int64_t *__restrict__ Super,
+                              const int64_t *__restrict__ Pi, const int64_t *__restrict__ Px,
+                              const T *__restrict__ Lx, double *out)
+{
+    __shared__ double smin[1024], smax[1024];
+    double lo = 1e308, hi = 0.0;
+    for (int s = threadIdx.x; s < nsuper; s += blockDim.x) {
+        const int nscol = (int)(Super[s + 1] - Super[s]);
+        const int64_t nsrow = Pi[s + 1] - Pi[s];
+        const T *panel = Lx + Px[s];
+        for (int j = 0; j < nscol; j++) {
+            const double d = (double)panel[j + j * nsrow];
+            lo = fmin(lo, d * d);
+            hi = fmax(hi, d * d);
+        }
+    }
+    smin[threadIdx.x] = lo;
+    smax[threadIdx.x] = hi;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + o]);
+            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { out[0] = smin[0]; out[1] = smax[0]; }
+}
+
+// per column r: out[3r] = max|R|, out[3r+1] = max|X|, out[3r+2] = max|B|;
+// one block per column, fixed reduction tree.
+__global__ void k_colmax3(int64_t n, const double *__restrict__ R, int64_t ldr,
+                          const double *__restrict__ X, int64_t ldx,
+                          const double *__restrict__ B, int64_t ldb, double *out)
+{
+    __shared__ double sm[3][256];
+    const int r = blockIdx.x;
+    double a = 0, b = 0, c = 0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        a = fmax(a, fabs(R[i + r * ldr]));
+        b = fmax(b, fabs(X[i + r * ldx]));
+        c = fmax(c, fabs(B[i + r * ldb]));
+    }
+    sm[0][threadIdx.x] = a;
+    sm[1][threadIdx.x] = b;
+    sm[2][threadIdx.x] = c;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int q = 0; q < 3; q++)
+                sm[q][threadIdx.x] = fmax(sm[q][threadIdx.x], sm[q][threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 3; q++) out[3 * r + q] = sm[q][0];
+}
+
+// max over rows of sum |A(i,:)| (for the backward error denominator)
+__global__ void k_anorm_inf(int64_t n, const int64_t *__restrict__ Rp,
+                            const double *__restrict__ Rx, double *out)
+{
+    __shared__ double sm[256];
+    double best = 0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        double acc = 0;
+        for (int64_t p = Rp[i]; p < Rp[i + 1]; p++) acc += fabs(Rx[p]);
+        best = fmax(best, acc);
+    }
+    sm[threadIdx.x] = best;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sm[0];
+}
+
+// zero factor entries [from, to) (not-positive-definite clean-up)
+template <typename T>
+__global__ void k_zero_range(T *x, int64_t from, int64_t to)
+{
+    for (int64_t i = from + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < to;
+         i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = (T)0;
+}
+
+
+// FMA throughput probe: 8 independent multiply-add chains per thread.
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_peak(int iters, T seed, T *out)
+{
+    T a[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) a[c] = seed + (T)(threadIdx.x + c);
+    const T m = (T)0.999999, b = (T)1e-7;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int c = 0; c < 8; c++) a[c] = a[c] * m + b;
+    }
+    T s = 0;
+#pragma unroll
+    for (int c = 0; c < 8; c++) s += a[c];
+    if (s == (T)-12345.0) out[0] = s;     // keeps the chains live
+}
+
+extern "C" {
+
+int gb_launch_fma_peak(int dtype, int iters, int blocks, float *ms, cudaStream_t st)
+{
+    cudaEvent_t e0, e1;
+    void *out = NULL;
+    if (cudaMalloc(&out, 16) != cudaSuccess) return 1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    if (dtype == 0) k_fma_peak<double><<<blocks, 256, 0, st>>>(iters, 1.0, (double *)out);
+    else k_fma_peak<float><<<blocks, 256, 0, st>>>(iters, 1.0f, (float *)out);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    return (int)cudaGetLastError();
+}
+
+
+// b_dtype/y_dtype: 0 double, 4 single
+int gb_launch_perm_in(int64_t n, int nrhs, const int64_t *perm, const double *scale,
+                      const void *B, int b_dtype, int64_t ldb, void *Y, int y_dtype,
+                      int64_t ldy, cudaStream_t st)
+{
+    int g = gb_grid_for(n * nrhs);
+    if (b_dtype == 0 && y_dtype == 0)
+        k_perm_in<double, double><<<g, 256, 0, st>>>(n, nrhs, perm, scale, (const double *)B, ldb, (double *)Y, ldy);
+    else if (b_dtype == 0 && y_dtype == 4)
+        k_perm_in<double, float><<<g, 256, 0, st>>>(n, nrhs, perm, scale, (const double *)B, ldb, (float *)Y, ldy);
+    else if (b_dtype == 4 && y_dtype == 4)
+        k_perm_in<float, float><<<g, 256, 0, st>>>(n, nrhs, perm, scale, (const float *)B, ldb, (float *)Y, ldy);
+    else
+        k_perm_in<float, double><<<g, 256, 0, st>>>(n, nrhs, perm, scale, (const float *)B, ldb, (double *)Y, ldy);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_perm_out(int64_t n, int nrhs, const int64_t *perm, const double *scale,
+                       const void *Y, int y_dtype, int64_t ldy, void *X, int x_dtype,
+                       int64_t ldx, int add, cudaStream_t st)
+{
+    int g = gb_grid_for(n * nrhs);
+    if (y_dtype == 0 && x_dtype == 0)
+        k_perm_out<double, double><<<g, 256, 0, st>>>(n, nrhs, perm, scale, (const double *)Y, ldy, (double *)X, ldx, add);
+    else if (y_dtype == 4 && x_dtype == 0)
+        k_perm_out<float, double><<<g, 256, 0, st>>>(n, nrhs, perm, scale, (const float *)Y, ldy, (double *)X, ldx, add);
+    else if (y_dtype == 4 && x_dtype == 4)
+        k_perm_out<float, float><<<g, 256, 0, st>>>(n, nrhs, perm, scale, (const float *)Y, ldy, (float *)X, ldx, add);
+    else
+        k_perm_out<double, float><<<g, 256, 0, st>>>(n, nrhs, perm, scale, (const double *)Y, ldy, (float *)X, ldx, add);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_residual(int64_t n, int nrhs, const int64_t *Rp, const int32_t *Rj,
+                       const double *Rx, const double *X, int64_t ldx, const double *B,
+                       int64_t ldb, double *R, int64_t ldr, cudaStream_t st)
+{
+    int g = gb_grid_for(n * nrhs);
+    k_residual<<<g, 256, 0, st>>>(n, nrhs, Rp, Rj, Rx, X, ldx, B, ldb, R, ldr);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_diag_minmax(int nsuper, const int64_t *Super, const int64_t *Pi,
+                          const int64_t *Px, const void *Lx, int dtype, double *out,
+                          cudaStream_t st)
+{
+    if (dtype == 0) k_diag_minmax<double><<<1, 1024, 0, st>>>(nsuper, Super, Pi, Px, (const double *)Lx, out);
+    else k_diag_minmax<float><<<1, 1024, 0, st>>>(nsuper, Super, Pi, Px, (const float *)Lx, out);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_colmax3(int64_t n, int nrhs, const double *R, int64_t ldr, const double *X,
+                      int64_t ldx, const double *B, int64_t ldb, double *out, cudaStream_t st)
+{
+    k_colmax3<<<nrhs, 256, 0, st>>>(n, R, ldr, X, ldx, B, ldb, out);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_anorm(int64_t n, const int64_t *Rp, const double *Rx, double *out, cudaStream_t st)
+{
+    k_anorm_inf<<<1, 256, 0, st>>>(n, Rp, Rx, out);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_zero_range(void *x, int dtype, int64_t from, int64_t to, cudaStream_t st)
+{
+    if (to <= from) return 0;
+    int g = gb_grid_for(to - from);
+    if (dtype == 0) k_zero_range<double><<<g, 256, 0, st>>>((double *)x, from, to);
+    else k_zero_range<float><<<g, 256, 0, st>>>((float *)x, from, to);
+    return (int)cudaGetLastError();
+}
+
+
+}  // extern "C"

@@ -1,19 +1,273 @@
-/* gb_mixed.c -- FP32 factor + FP64 iterative refinement (filled in below). */
+/* gb_mixed.c -- FP32 supernodal factor + FP64 iterative refinement.
+ *
+ * gb300_factorize_mixed: S = tril(PAP') is uploaded in FP64; the assembly
+ * kernel applies the symmetric diagonal scaling D A D (D = diag(A)^-1/2, so
+ * every diagonal entry of the scaled matrix is 1) per supernode while it
+ * rounds the values to FP32, and the FP32 factor stays on the GPU.  A pivot
+ * L(k,k)^2 <= eps_single (relative to the unit diagonal of the scaled
+ * matrix), or a failed FP32 factorization, switches to the FP64 factor.
+ *
+ * gb300_solve_refined: x_0 = 0, r_0 = b; repeat  d = D P' L^-T L^-1 P D r
+ * (sweeps in FP32), x += d, r = b - A x (FP64 SpMV on the GPU, both
+ * triangles of A resident), until every column's backward error
+ * |r|_inf / (|A|_inf |x|_inf + |b|_inf) <= tol.  When the backward error has
+ * not decreased for 2 consecutive steps, the matrix is refactored in FP64
+ * and refinement continues with that factor.  The refinement scheme is the
+ * one the reference's demo applies once (CHOLMOD/Demo/cholmod_di_demo.c
+ * :627-663: r = b - A x with cholmod_sdmult, solve, x += dx), iterated here
+ * with the stopping and fallback rules above.
+ */
 #include "gb_plan.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define GB_EPS_SINGLE 1.1920928955078125e-07
+#define GB_MAX_REFINE 30
+
+enum { GB_REASON_NONE = 0, GB_REASON_FP32_FAILED = 1, GB_REASON_SMALL_PIVOT = 2,
+       GB_REASON_STALLED = 3 };
+
+/* Full (both triangles) compressed-row copy of the lower-stored A: row i of
+ * the result is column i of the full symmetric matrix. */
+static int upload_full_A(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, cholmod_common *Common)
+{
+    Int n = (Int)A->nrow;
+    const Int *Ap = A->p, *Ai = A->i, *Anz = A->nz;
+    const double *Ax = A->x;
+    Int *cnt = calloc(n + 1, sizeof(Int));
+    if (!cnt) { GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "out of memory"); return FALSE; }
+    Int nz = 0;
+    for (Int j = 0; j < n; j++) {
+        Int p = Ap[j], pend = A->packed ? Ap[j + 1] : p + Anz[j];
+        for (; p < pend; p++) {
+            Int i = Ai[p];
+            if (i < j) continue;
+            cnt[i]++;
+            nz++;
+            if (i != j) { cnt[j]++; nz++; }
+        }
+    }
+    int64_t *Rp = malloc(sizeof(int64_t) * (n + 1));
+    int32_t *Rj = malloc(sizeof(int32_t) * (nz + 1));
+    double *Rx = malloc(sizeof(double) * (nz + 1));
+    double *dorig = malloc(sizeof(double) * (n + 1));
+    double *dperm = malloc(sizeof(double) * (n + 1));
+    int ok = Rp && Rj && Rx && dorig && dperm;
+    if (ok) {
+        Rp[0] = 0;
+        for (Int i = 0; i < n; i++) Rp[i + 1] = Rp[i] + cnt[i];
+        for (Int i = 0; i < n; i++) { cnt[i] = Rp[i]; dorig[i] = 0; }
+        double anorm = 0;
+        for (Int j = 0; j < n; j++) {
+            Int p = Ap[j], pend = A->packed ? Ap[j + 1] : p + Anz[j];
+            for (; p < pend; p++) {
+                Int i = Ai[p];
+                if (i < j) continue;
+                Rj[cnt[i]] = (int32_t)j;
+                Rx[cnt[i]++] = Ax[p];
+                if (i != j) {
+                    Rj[cnt[j]] = (int32_t)i;
+                    Rx[cnt[j]++] = Ax[p];
+                } else {
+                    dorig[i] = Ax[p];
+                }
+            }
+        }
+        (void)anorm;
+        const Int *Perm = P->L->Perm;
+        for (Int i = 0; i < n; i++) dorig[i] = dorig[i] > 0 ? 1.0 / sqrt(dorig[i]) : 1.0;
+        for (Int k = 0; k < n; k++) dperm[k] = dorig[Perm[k]];
+        cudaStream_t st = ctx->stream;
+        ok = gb_dev_grow((void **)&P->d_Rp, &P->rp_cap, sizeof(int64_t) * (n + 1))
+             && gb_dev_grow((void **)&P->d_Rj, &P->rj_cap, sizeof(int32_t) * (nz + 1))
+             && gb_dev_grow((void **)&P->d_Rx, &P->rx_cap, sizeof(double) * (nz + 1));
+        size_t cap = 0;
+        if (ok && !P->d_scale) ok = gb_dev_grow((void **)&P->d_scale, &cap, sizeof(double) * (n + 1));
+        cap = 0;
+        if (ok && !P->d_scale_perm) ok = gb_dev_grow((void **)&P->d_scale_perm, &cap, sizeof(double) * (n + 1));
+        if (ok && !P->d_red) { cap = 0; ok = gb_dev_grow((void **)&P->d_red, &cap, sizeof(double) * 64); }
+        ok = ok && cudaMemcpyAsync(P->d_Rp, Rp, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st) == cudaSuccess
+             && cudaMemcpyAsync(P->d_Rj, Rj, sizeof(int32_t) * nz, cudaMemcpyHostToDevice, st) == cudaSuccess
+             && cudaMemcpyAsync(P->d_Rx, Rx, sizeof(double) * nz, cudaMemcpyHostToDevice, st) == cudaSuccess
+             && cudaMemcpyAsync(P->d_scale, dorig, sizeof(double) * n, cudaMemcpyHostToDevice, st) == cudaSuccess
+             && cudaMemcpyAsync(P->d_scale_perm, dperm, sizeof(double) * n, cudaMemcpyHostToDevice, st) == cudaSuccess
+             && gb_launch_anorm(n, P->d_Rp, P->d_Rx, P->d_red + 63, st) == 0
+             && cudaMemcpyAsync(&P->anorm, P->d_red + 63, sizeof(double), cudaMemcpyDeviceToHost, st) == cudaSuccess
+             && cudaStreamSynchronize(st) == cudaSuccess;
+        if (!ok) GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error uploading A");
+    } else {
+        GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "out of memory");
+    }
+    free(cnt); free(Rp); free(Rj); free(Rx); free(dorig); free(dperm);
+    return ok;
+}
+
+static int factor_fp64(gb_plan *P, gb_ctx *ctx, int reason, cholmod_common *Common)
+{
+    if (!gb_ensure_numeric(P, CHOLMOD_DOUBLE)) {
+        GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed");
+        return FALSE;
+    }
+    int32_t anyfail = 0;
+    int ok = gb_run_factor(P, ctx, P->d_Sx, CHOLMOD_DOUBLE, CHOLMOD_DOUBLE, NULL, 0.0)
+             && cudaMemcpyAsync(&anyfail, P->d_anyfail, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                ctx->stream) == cudaSuccess
+             && cudaStreamSynchronize(ctx->stream) == cudaSuccess;
+    if (!ok) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the FP64 factorization"); return FALSE; }
+    P->mixed = 2;
+    P->mixed_reason = reason;
+    P->dev_valid[0] = 0;                 /* not L->x's values */
+    if (anyfail) {
+        gb_fix_not_posdef(P, ctx, (cholmod_factor *)P->L, CHOLMOD_DOUBLE, Common);
+        return TRUE;
+    }
+    return TRUE;
+}
 
 int gb300_factorize_mixed(cholmod_sparse *A, cholmod_factor *L, cholmod_common *Common)
 {
-    (void)A; (void)L;
     if (!Common) return FALSE;
-    GB_ERROR(CHOLMOD_NOT_INSTALLED, "mixed precision path not built");
-    return FALSE;
+    if (!A || !L) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return FALSE; }
+    if (A->stype >= 0 || A->nrow != A->ncol || A->nrow != L->n || !L->Perm || !L->is_super
+        || A->xtype != CHOLMOD_REAL || A->dtype != CHOLMOD_DOUBLE || A->itype != CHOLMOD_LONG) {
+        GB_ERROR(CHOLMOD_INVALID, "A must be real double symmetric-lower matching supernodal L");
+        return FALSE;
+    }
+    Common->status = CHOLMOD_OK;
+    gb_ctx *ctx = gb_ctx_get(Common, 1);
+    if (!ctx || !gb_ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return FALSE; }
+    gb_plan *P = gb_plan_get(L, Common, ctx, 1);
+    if (!P) return FALSE;
+    cholmod_sparse *S = gb_permute_lower(A, L->Perm, Common);
+    if (!S) return FALSE;
+    int ok = gb_upload_input(P, ctx, S, CHOLMOD_DOUBLE) && upload_full_A(P, ctx, A, Common)
+             && gb_ensure_numeric(P, CHOLMOD_SINGLE);
+    gb300_free_sparse(&S, Common);
+    if (!ok) {
+        if (Common->status == CHOLMOD_OK) GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed");
+        return FALSE;
+    }
+    L->minor = L->n;
+    int32_t anyfail = 0;
+    double mm[2] = {0, 0};
+    cudaStream_t st = ctx->stream;
+    cudaEventRecord(ctx->ev0, st);
+    ok = gb_run_factor(P, ctx, P->d_Sx, CHOLMOD_DOUBLE, CHOLMOD_SINGLE, P->d_scale_perm, 0.0)
+         && gb_launch_diag_minmax((int)P->nsuper, P->d_Super, P->d_Pi, P->d_Px, P->d_Lx[1], 4,
+                                  P->d_red, st) == 0;
+    cudaEventRecord(ctx->ev1, st);
+    ok = ok && cudaMemcpyAsync(&anyfail, P->d_anyfail, sizeof(int32_t), cudaMemcpyDeviceToHost, st) == cudaSuccess
+         && cudaMemcpyAsync(mm, P->d_red, 2 * sizeof(double), cudaMemcpyDeviceToHost, st) == cudaSuccess
+         && cudaStreamSynchronize(st) == cudaSuccess;
+    if (!ok) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the FP32 factorization"); return FALSE; }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats[0] = ms;
+    P->mixed = 1;
+    P->mixed_reason = GB_REASON_NONE;
+    P->dev_valid[1] = 0;                 /* the FP32 factor is of D A D, not of L->x */
+    if (anyfail) return factor_fp64(P, ctx, GB_REASON_FP32_FAILED, Common);
+    if (mm[0] <= GB_EPS_SINGLE * mm[1]) return factor_fp64(P, ctx, GB_REASON_SMALL_PIVOT, Common);
+    return TRUE;
 }
 
 cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod_dense *B,
                                    double tol, double *info, cholmod_common *Common)
 {
-    (void)A; (void)L; (void)B; (void)tol; (void)info;
     if (!Common) return NULL;
-    GB_ERROR(CHOLMOD_NOT_INSTALLED, "mixed precision path not built");
-    return NULL;
+    if (!A || !L || !B) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return NULL; }
+    if (B->nrow != L->n || B->xtype != CHOLMOD_REAL || B->dtype != CHOLMOD_DOUBLE
+        || A->nrow != L->n) {
+        GB_ERROR(CHOLMOD_INVALID, "B must be real double with n rows");
+        return NULL;
+    }
+    Common->status = CHOLMOD_OK;
+    gb_ctx *ctx = gb_ctx_get(Common, 1);
+    if (!ctx || !gb_ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return NULL; }
+    gb_plan *P = gb_plan_get(L, Common, ctx, 0);
+    if (!P || !P->mixed) {
+        GB_ERROR(CHOLMOD_INVALID, "no mixed-precision factor: call gb300_factorize_mixed first");
+        return NULL;
+    }
+    Int n = P->n;
+    int nrhs = (int)B->ncol;
+    cholmod_dense *X = gb300_allocate_dense(n, nrhs, n, CHOLMOD_REAL + CHOLMOD_DOUBLE, Common);
+    if (!X) return NULL;
+    if (info) { info[0] = 0; info[1] = 0; info[2] = P->mixed == 2; info[3] = 0; }
+    if (n == 0 || nrhs == 0) return X;
+    cudaStream_t st = ctx->stream;
+    size_t nb = sizeof(double) * n * nrhs;
+    double *hred = malloc(sizeof(double) * 3 * nrhs);
+    double *best = malloc(sizeof(double) * nrhs);
+    int ok = hred && best && gb_dev_grow((void **)&P->d_X, &P->x_cap, nb)
+             && gb_dev_grow((void **)&P->d_R, &P->r_cap, nb)
+             && gb_dev_grow((void **)&P->d_bx, &P->bx_cap, nb)
+             && gb_dev_grow(&P->d_Y, &P->y_cap, nb);
+    if (ok && nrhs * 3 > 60) {
+        size_t cap = 0;
+        cudaFree(P->d_red);
+        P->d_red = NULL;
+        ok = gb_dev_grow((void **)&P->d_red, &cap, sizeof(double) * (3 * nrhs + 64));
+    }
+    ok = ok && cudaMemcpy2DAsync(P->d_bx, sizeof(double) * n, B->x, sizeof(double) * B->d,
+                                 sizeof(double) * n, nrhs, cudaMemcpyHostToDevice, st) == cudaSuccess
+         && cudaMemsetAsync(P->d_X, 0, nb, st) == cudaSuccess
+         && cudaMemcpyAsync(P->d_R, P->d_bx, nb, cudaMemcpyDeviceToDevice, st) == cudaSuccess;
+    cudaEventRecord(ctx->ev0, st);
+    int it = 0, stall = 0;
+    double bmax_all = 0, berr_max = INFINITY;
+    for (int r = 0; r < nrhs && best; r++) best[r] = INFINITY;
+    while (ok && it < GB_MAX_REFINE) {
+        /* correction with the current factor: x += D P' L^-T L^-1 P D r */
+        int single = (P->mixed == 1);
+        int ydt = single ? 4 : 0;
+        const double *scale = single ? P->d_scale : NULL;
+        ok = gb_launch_perm_in(n, nrhs, P->d_Perm, scale, P->d_R, 0, n, P->d_Y, ydt, n, st) == 0
+             && gb_run_sweep(P, ctx, single ? CHOLMOD_SINGLE : CHOLMOD_DOUBLE, nrhs, P->d_Y, 1)
+             && gb_run_sweep(P, ctx, single ? CHOLMOD_SINGLE : CHOLMOD_DOUBLE, nrhs, P->d_Y, 0)
+             && gb_launch_perm_out(n, nrhs, P->d_Perm, scale, P->d_Y, ydt, n, P->d_X, 0, n, 1, st) == 0
+             && gb_launch_residual(n, nrhs, P->d_Rp, P->d_Rj, P->d_Rx, P->d_X, n, P->d_bx, n,
+                                   P->d_R, n, st) == 0
+             && gb_launch_colmax3(n, nrhs, P->d_R, n, P->d_X, n, P->d_bx, n, P->d_red, st) == 0
+             && cudaMemcpyAsync(hred, P->d_red, sizeof(double) * 3 * nrhs, cudaMemcpyDeviceToHost, st) == cudaSuccess
+             && cudaStreamSynchronize(st) == cudaSuccess;
+        ctx->launches += 5;
+        if (!ok) break;
+        it++;
+        berr_max = 0;
+        int improved = 0;
+        for (int r = 0; r < nrhs; r++) {
+            double den = P->anorm * hred[3 * r + 1] + hred[3 * r + 2];
+            double be = den > 0 ? hred[3 * r] / den : 0;
+            if (be < best[r]) { if (be < 0.5 * best[r]) improved = 1; best[r] = be; }
+            berr_max = fmax(berr_max, be);
+            bmax_all = fmax(bmax_all, hred[3 * r + 2]);
+        }
+        if (berr_max <= tol) break;
+        stall = improved ? 0 : stall + 1;
+        if (stall >= 2) {
+            if (P->mixed == 2) break;           /* FP64 factor cannot do better */
+            ok = factor_fp64(P, ctx, GB_REASON_STALLED, Common);
+            stall = 0;
+            if (info) info[2] = 1;
+        }
+    }
+    cudaEventRecord(ctx->ev1, st);
+    ok = ok && cudaMemcpy2DAsync(X->x, sizeof(double) * X->d, P->d_X, sizeof(double) * n,
+                                 sizeof(double) * n, nrhs, cudaMemcpyDeviceToHost, st) == cudaSuccess
+         && cudaStreamSynchronize(st) == cudaSuccess;
+    free(hred);
+    free(best);
+    if (!ok) {
+        gb300_free_dense(&X, Common);
+        if (Common->status == CHOLMOD_OK) GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in refinement");
+        return NULL;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats[2] = ms;
+    if (info) { info[0] = it; info[1] = berr_max; info[3] = berr_max; info[2] = P->mixed == 2; }
+    if (berr_max > tol) GB_ERROR(CHOLMOD_DSMALL, "refinement did not reach the requested tolerance");
+    return X;
 }

@@ -18,14 +18,6 @@
 #include <stdlib.h>
 #include <string.h>
 
-struct gb_ctx {
-    cudaStream_t stream;
-    int device;
-    int64_t opt_keep, opt_small;
-    double stats[8];
-    cudaEvent_t ev0, ev1;
-};
-
 gb_ctx *gb_ctx_new(void)
 {
     gb_ctx *c = calloc(1, sizeof(gb_ctx));
@@ -42,10 +34,12 @@ void gb_ctx_delete(gb_ctx *c)
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    for (int i = 0; i < c->npev; i++) cudaEventDestroy(c->pev[i]);
+    free(c->pev);
     free(c);
 }
 
-static int ctx_ready(gb_ctx *c)
+int gb_ctx_ready(gb_ctx *c)
 {
     if (c->stream) return TRUE;
     if (cudaGetDevice(&c->device) != cudaSuccess) return FALSE;
@@ -69,6 +63,10 @@ int gb300_set_option(cholmod_common *Common, int option, int64_t value)
     gb_ctx *c = gb_ctx_get(Common, 1);
     if (!c) { GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "out of memory"); return FALSE; }
     if (option == GB300_OPT_KEEP_ON_DEVICE) c->opt_keep = value ? 1 : 0;
+    else if (option == GB300_OPT_PROFILE) {
+        c->prof = value ? 1 : 0;
+        for (int k = 0; k < 16; k++) c->kind_ms[k] = c->kind_n[k] = 0;
+    }
     else if (option == GB300_OPT_SMALL_COLS) c->opt_small = GB_MAX(1, GB_MIN(GB_SMALL_MAX, value));
     else { GB_ERROR(CHOLMOD_INVALID, "unknown option"); return FALSE; }
     return TRUE;
@@ -79,6 +77,36 @@ int gb300_get_stats(cholmod_common *Common, double *out, int nout)
     gb_ctx *c = gb_ctx_get(Common, 0);
     if (!c || !out) return FALSE;
     for (int i = 0; i < nout && i < 8; i++) out[i] = c->stats[i];
+    if (nout > 5) out[5] = (double)c->launches;
+    return TRUE;
+}
+
+int gb300_get_profile(cholmod_common *Common, double *ms, double *count, int nkinds)
+{
+    gb_ctx *c = gb_ctx_get(Common, 0);
+    if (!c) return FALSE;
+    for (int k = 0; k < nkinds && k < 16; k++) {
+        if (ms) ms[k] = c->kind_ms[k];
+        if (count) count[k] = c->kind_n[k];
+    }
+    return TRUE;
+}
+
+int gb300_fma_peak(int dtype, double *tflops)
+{
+    cudaStream_t st;
+    if (!tflops || cudaStreamCreate(&st) != cudaSuccess) return FALSE;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int iters = dtype == 4 ? 4096 : 512, blocks = sms * 8;
+    float ms = 0;
+    int ok = gb_launch_fma_peak(dtype, iters, blocks, &ms, st) == 0      /* warm-up */
+             && gb_launch_fma_peak(dtype, iters, blocks, &ms, st) == 0;
+    cudaStreamDestroy(st);
+    if (!ok || ms <= 0) return FALSE;
+    /* 256 threads x 8 chains x iters x 2 flops per block */
+    *tflops = 2.0 * 8.0 * iters * 256.0 * blocks / (ms * 1e-3) / 1e12;
     return TRUE;
 }
 
@@ -115,6 +143,20 @@ int gb_release_factor_state(cholmod_factor *L)
     return TRUE;
 }
 
+int gb300_factor_info(cholmod_factor *L, cholmod_common *Common, double *out, int nout)
+{
+    if (!Common || !L || !out) return FALSE;
+    gb_ctx *ctx = gb_ctx_get(Common, 1);
+    if (!ctx || !gb_ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return FALSE; }
+    gb_plan *P = gb_plan_get(L, Common, ctx, 1);
+    if (!P) return FALSE;
+    double v[10] = {P->fl_gemm, (double)P->nlevels, (double)P->fact_seq.n, (double)P->cb_total,
+                    (double)P->gemm_t.n, (double)P->nsuper, (double)P->fwd_seq.n,
+                    (double)P->bwd_seq.n, (double)P->cbv_total, (double)P->mixed};
+    for (int i = 0; i < nout && i < 10; i++) out[i] = v[i];
+    return TRUE;
+}
+
 int gb300_release_factor(cholmod_factor *L, cholmod_common *Common)
 {
     (void)Common;
@@ -124,7 +166,7 @@ int gb300_release_factor(cholmod_factor *L, cholmod_common *Common)
 
 /* Find (or build and upload) the plan of L.  A stale entry for the same
  * pointer with a different pattern is dropped. */
-static gb_plan *plan_get(cholmod_factor *L, cholmod_common *Common, gb_ctx *ctx, int create)
+gb_plan *gb_plan_get(cholmod_factor *L, cholmod_common *Common, gb_ctx *ctx, int create)
 {
     pthread_mutex_lock(&plan_lock);
     gb_plan *P = NULL;
@@ -154,7 +196,7 @@ static gb_plan *plan_get(cholmod_factor *L, cholmod_common *Common, gb_ctx *ctx,
     return P;
 }
 
-static int dev_grow(void **p, size_t *cap, size_t bytes)
+int gb_dev_grow(void **p, size_t *cap, size_t bytes)
 {
     if (bytes <= *cap && *p) return TRUE;
     if (*p) cudaFree(*p);
@@ -169,7 +211,7 @@ static int dt_index(int dtype) { return dtype == CHOLMOD_SINGLE ? 1 : 0; }
 static size_t dt_size(int dtype) { return dtype == CHOLMOD_SINGLE ? sizeof(float) : sizeof(double); }
 
 /* device factor and update-block buffers of one precision */
-static int ensure_numeric(gb_plan *P, int dtype)
+int gb_ensure_numeric(gb_plan *P, int dtype)
 {
     int d = dt_index(dtype);
     size_t e = dt_size(dtype);
@@ -189,8 +231,8 @@ static int ensure_numeric(gb_plan *P, int dtype)
 
 /* Replay the factorization sequence.  Sx has dtype a_dtype; the factor is
  * computed in l_dtype; scale (device, optional) applies D A D. */
-static int run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dtype,
-                      const double *scale, double beta)
+int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dtype,
+                  const double *scale, double beta)
 {
     cudaStream_t st = ctx->stream;
     int d = dt_index(l_dtype);
@@ -199,10 +241,22 @@ static int run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int 
     void *Lx = P->d_Lx[d], *CB = P->d_CB[d];
     const gb_launch_rec *seq = P->fact_seq.p;
     int launches = 0;
+    int prof = ctx->prof;
+    if (prof && ctx->npev < (int)(2 * P->fact_seq.n)) {
+        int need = (int)(2 * P->fact_seq.n);
+        cudaEvent_t *ev = realloc(ctx->pev, sizeof(cudaEvent_t) * need);
+        if (!ev) prof = 0;
+        else {
+            ctx->pev = ev;
+            for (int i = ctx->npev; i < need; i++) CU(cudaEventCreate(&ctx->pev[i]));
+            ctx->npev = need;
+        }
+    }
     CU(cudaMemsetAsync(P->d_fail, 0xFF, sizeof(int32_t) * (P->nsuper + 1), st));
     CU(cudaMemsetAsync(P->d_anyfail, 0, sizeof(int32_t), st));
     for (size_t i = 0; i < P->fact_seq.n; i++) {
         const gb_launch_rec *r = &seq[i];
+        if (prof) CU(cudaEventRecord(ctx->pev[2 * i], st));
         switch (r->kind) {
         case GB_K_ASM:
             LK(gb_launch_assemble(&P->ptrs, P->d_asm + r->off, r->count, P->d_Sp, P->d_Si,
@@ -222,22 +276,34 @@ static int run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int 
                               r->count, Lx, CB, ldt, st));
             break;
         }
+        if (prof) CU(cudaEventRecord(ctx->pev[2 * i + 1], st));
         launches++;
     }
+    if (prof) {
+        CU(cudaStreamSynchronize(st));
+        for (size_t i = 0; i < P->fact_seq.n; i++) {
+            float ms = 0;
+            CU(cudaEventElapsedTime(&ms, ctx->pev[2 * i], ctx->pev[2 * i + 1]));
+            int k = seq[i].kind & 15;
+            ctx->kind_ms[k] += ms;
+            ctx->kind_n[k] += 1;
+        }
+    }
     ctx->stats[4] = launches;
+    ctx->launches += launches;
     return TRUE;
 cuda_fail:
     return FALSE;
 }
 
 /* Replay one sweep on Y (device, n x nrhs, ld n) with the device factor. */
-static int run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int forward)
+int gb_run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int forward)
 {
     cudaStream_t st = ctx->stream;
     int d = dt_index(l_dtype);
     int ldt = l_dtype == CHOLMOD_SINGLE ? 4 : 0;
     size_t e = dt_size(l_dtype);
-    if (!dev_grow(&P->d_U, &P->u_cap, e * GB_MAX(P->cbv_total, 1) * nrhs)) return FALSE;
+    if (!gb_dev_grow(&P->d_U, &P->u_cap, e * GB_MAX(P->cbv_total, 1) * nrhs)) return FALSE;
     const void *Lx = P->d_Lx[d];
     gb_vec *seqv = forward ? &P->fwd_seq : &P->bwd_seq;
     const gb_launch_rec *seq = seqv->p;
@@ -256,6 +322,7 @@ static int run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, in
         }
         if (rc) return FALSE;
     }
+    ctx->launches += (int64_t)seqv->n;
     return TRUE;
 }
 
@@ -266,7 +333,7 @@ static int run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, in
  * the first column failed or quick_return_if_not_posdef) and every later
  * supernode are zero.  Supernodes before s0 are neither descendants of a
  * failing supernode nor affected by one, so their values are final. */
-static int fix_not_posdef(gb_plan *P, gb_ctx *ctx, cholmod_factor *L, int l_dtype,
+int gb_fix_not_posdef(gb_plan *P, gb_ctx *ctx, cholmod_factor *L, int l_dtype,
                           cholmod_common *Common)
 {
     int32_t *fail = malloc(sizeof(int32_t) * (P->nsuper + 1));
@@ -298,15 +365,15 @@ static int fix_not_posdef(gb_plan *P, gb_ctx *ctx, cholmod_factor *L, int l_dtyp
 }
 
 /* Upload S = A (lower, packed, sorted or not) values and pattern. */
-static int upload_input(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, int a_dtype)
+int gb_upload_input(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, int a_dtype)
 {
     Int n = (Int)A->ncol;
     const Int *Ap = A->p;
     Int nz = Ap[n];
     size_t e = dt_size(a_dtype);
-    if (!dev_grow((void **)&P->d_Sp, &P->sp_cap, sizeof(int64_t) * (n + 1))) return FALSE;
-    if (!dev_grow((void **)&P->d_Si, &P->si_cap, sizeof(int64_t) * GB_MAX(nz, 1))) return FALSE;
-    if (!dev_grow(&P->d_Sx, &P->sx_cap, e * GB_MAX(nz, 1))) return FALSE;
+    if (!gb_dev_grow((void **)&P->d_Sp, &P->sp_cap, sizeof(int64_t) * (n + 1))) return FALSE;
+    if (!gb_dev_grow((void **)&P->d_Si, &P->si_cap, sizeof(int64_t) * GB_MAX(nz, 1))) return FALSE;
+    if (!gb_dev_grow(&P->d_Sx, &P->sx_cap, e * GB_MAX(nz, 1))) return FALSE;
     cudaStream_t st = ctx->stream;
     if (cudaMemcpyAsync(P->d_Sp, A->p, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st) != cudaSuccess) return FALSE;
     if (nz && cudaMemcpyAsync(P->d_Si, A->i, sizeof(int64_t) * nz, cudaMemcpyHostToDevice, st) != cudaSuccess) return FALSE;
@@ -387,15 +454,15 @@ int cholmod_l_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2]
     }
 
     gb_ctx *ctx = gb_ctx_get(Common, 1);
-    if (!ctx || !ctx_ready(ctx)) {
+    if (!ctx || !gb_ctx_ready(ctx)) {
         if (Apk != A) gb300_free_sparse(&Apk, Common);
         GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device");
         return FALSE;
     }
     int symbolic = (L->xtype == CHOLMOD_PATTERN);
-    gb_plan *P = plan_get(L, Common, ctx, 1);
+    gb_plan *P = gb_plan_get(L, Common, ctx, 1);
     if (!P) { if (Apk != A) gb300_free_sparse(&Apk, Common); return FALSE; }
-    if (!ensure_numeric(P, dtype) || !upload_input(P, ctx, Apk, dtype)) {
+    if (!gb_ensure_numeric(P, dtype) || !gb_upload_input(P, ctx, Apk, dtype)) {
         if (Apk != A) gb300_free_sparse(&Apk, Common);
         GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed");
         return FALSE;
@@ -412,7 +479,7 @@ int cholmod_l_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2]
 
     int ok = TRUE;
     cudaEventRecord(ctx->ev0, ctx->stream);
-    ok = run_factor(P, ctx, P->d_Sx, dtype, dtype, NULL, beta ? beta[0] : 0.0);
+    ok = gb_run_factor(P, ctx, P->d_Sx, dtype, dtype, NULL, beta ? beta[0] : 0.0);
     cudaEventRecord(ctx->ev1, ctx->stream);
     int32_t anyfail = 0;
     if (ok) ok = cudaMemcpyAsync(&anyfail, P->d_anyfail, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess
@@ -426,7 +493,7 @@ int cholmod_l_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2]
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     ctx->stats[0] = ms;
     L->minor = L->n;
-    if (anyfail && !fix_not_posdef(P, ctx, L, dtype, Common)) {
+    if (anyfail && !gb_fix_not_posdef(P, ctx, L, dtype, Common)) {
         if (Apk != A) gb300_free_sparse(&Apk, Common);
         return FALSE;
     }
@@ -453,12 +520,12 @@ int cholmod_l_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2]
  * produce the current values */
 static gb_plan *factor_on_device(cholmod_factor *L, gb_ctx *ctx, cholmod_common *Common)
 {
-    gb_plan *P = plan_get(L, Common, ctx, 1);
+    gb_plan *P = gb_plan_get(L, Common, ctx, 1);
     if (!P) return NULL;
     int d = dt_index(L->dtype);
     if (P->dev_valid[d] && P->host_x[d] == L->x) return P;
     if (!L->x) { GB_ERROR(CHOLMOD_INVALID, "L has no numerical values"); return NULL; }
-    if (!ensure_numeric(P, L->dtype)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed"); return NULL; }
+    if (!gb_ensure_numeric(P, L->dtype)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed"); return NULL; }
     if (cudaMemcpyAsync(P->d_Lx[d], L->x, dt_size(L->dtype) * L->xsize, cudaMemcpyHostToDevice,
                         ctx->stream) != cudaSuccess) {
         GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error");
@@ -492,18 +559,18 @@ static int super_solve(cholmod_factor *L, cholmod_dense *X, cholmod_dense *E,
     Common->status = CHOLMOD_OK;
     if (L->n == 0 || X->ncol == 0) return TRUE;
     gb_ctx *ctx = gb_ctx_get(Common, 1);
-    if (!ctx || !ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return FALSE; }
+    if (!ctx || !gb_ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return FALSE; }
     gb_plan *P = factor_on_device(L, ctx, Common);
     if (!P) return FALSE;
     int nrhs = (int)X->ncol;
     size_t e = dt_size(L->dtype);
     Int n = P->n;
-    if (!dev_grow(&P->d_Y, &P->y_cap, e * n * nrhs)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed"); return FALSE; }
+    if (!gb_dev_grow(&P->d_Y, &P->y_cap, e * n * nrhs)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed"); return FALSE; }
     cudaStream_t st = ctx->stream;
     int ok = cudaMemcpy2DAsync(P->d_Y, e * n, X->x, e * X->d, e * n, nrhs,
                                cudaMemcpyHostToDevice, st) == cudaSuccess;
     cudaEventRecord(ctx->ev0, st);
-    ok = ok && run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, forward);
+    ok = ok && gb_run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, forward);
     cudaEventRecord(ctx->ev1, st);
     ok = ok && cudaMemcpy2DAsync(X->x, e * X->d, P->d_Y, e * n, e * n, nrhs,
                                  cudaMemcpyDeviceToHost, st) == cudaSuccess;
@@ -559,7 +626,7 @@ cholmod_dense *gb300_solve(int sys, cholmod_factor *L, cholmod_dense *B,
     }
     Common->status = CHOLMOD_OK;
     gb_ctx *ctx = gb_ctx_get(Common, 1);
-    if (!ctx || !ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return NULL; }
+    if (!ctx || !gb_ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return NULL; }
     gb_plan *P = factor_on_device(L, ctx, Common);
     if (!P) return NULL;
     int nrhs = (int)B->ncol;
@@ -570,13 +637,13 @@ cholmod_dense *gb300_solve(int sys, cholmod_factor *L, cholmod_dense *B,
     if (!X) return NULL;
     if (n == 0 || nrhs == 0) return X;
     cudaStream_t st = ctx->stream;
-    int ok = dev_grow(&P->d_Y, &P->y_cap, e * n * nrhs) && dev_grow(&P->d_B, &P->b_cap, e * n * nrhs);
+    int ok = gb_dev_grow(&P->d_Y, &P->y_cap, e * n * nrhs) && gb_dev_grow(&P->d_B, &P->b_cap, e * n * nrhs);
     ok = ok && cudaMemcpy2DAsync(P->d_B, e * n, B->x, e * B->d, e * n, nrhs,
                                  cudaMemcpyHostToDevice, st) == cudaSuccess;
     cudaEventRecord(ctx->ev0, st);
     ok = ok && gb_launch_perm_in(n, nrhs, P->d_Perm, NULL, P->d_B, dt, n, P->d_Y, dt, n, st) == 0;
-    ok = ok && run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, 1);
-    ok = ok && run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, 0);
+    ok = ok && gb_run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, 1);
+    ok = ok && gb_run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, 0);
     ok = ok && gb_launch_perm_out(n, nrhs, P->d_Perm, NULL, P->d_Y, dt, n, P->d_B, dt, n, 0, st) == 0;
     cudaEventRecord(ctx->ev1, st);
     ok = ok && cudaMemcpyAsync(X->x, P->d_B, e * n * nrhs, cudaMemcpyDeviceToHost, st) == cudaSuccess;

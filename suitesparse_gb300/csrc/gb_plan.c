@@ -59,6 +59,22 @@ uint64_t gb_pattern_hash(const cholmod_factor *L)
     return h;
 }
 
+/* flops of a tile update that land in stored entries (2 per multiply-add) */
+static double gemm_flops(const gb_gemm_task *g)
+{
+    double cnt = 0;
+    if (g->flags & GB_GEMM_LOWER) {
+        for (int c = 0; c < g->n; c++) {
+            int r0 = c + g->diag_off;          /* first stored row of column c */
+            if (r0 < 0) r0 = 0;
+            if (r0 < g->m) cnt += g->m - r0;
+        }
+    } else {
+        cnt = (double)g->m * g->n;
+    }
+    return 2.0 * cnt * g->k;
+}
+
 static int push_launch(gb_vec *seq, int kind, size_t count, size_t off)
 {
     if (count == 0) return TRUE;
@@ -253,6 +269,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
                         int32_t own = (int32_t)s;
                         ok &= gb_vec_push(&P->gemm_t, &g);
                         ok &= gb_vec_push(&P->gemm_owner, &own);
+                        P->fl_gemm += gemm_flops(&g);
                     }
                 }
             }
@@ -281,7 +298,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
                     int32_t own = (int32_t)s;
                     ok &= gb_vec_push(&P->gemm_t, &g);
                     ok &= gb_vec_push(&P->gemm_owner, &own);
-                    P->fl_gemm += 2 * (int64_t)g.m * g.n * g.k;
+                    P->fl_gemm += gemm_flops(&g);
                 }
             }
         }
@@ -484,8 +501,8 @@ void gb_plan_free(gb_plan *P)
                    P->d_anyfail, P->d_asm, P->d_node, P->d_potrf, P->d_trsm, P->d_gemm,
                    P->d_gemm_owner, P->d_sweep, P->d_Lx[0], P->d_Lx[1], P->d_CB[0],
                    P->d_CB[1], P->d_Sp, P->d_Si, P->d_Sx, P->d_Y, P->d_U, P->d_B,
-                   P->d_Rp, P->d_Rj, P->d_Rx, P->d_scale, P->d_X, P->d_R, P->d_bx,
-                   P->d_red};
+                   P->d_Rp, P->d_Rj, P->d_Rx, P->d_scale, P->d_scale_perm, P->d_X, P->d_R,
+                   P->d_bx, P->d_red};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++)
         if (dev[i]) cudaFree(dev[i]);
     gb_vec_free(&P->asm_t); gb_vec_free(&P->node_t); gb_vec_free(&P->potrf_t);

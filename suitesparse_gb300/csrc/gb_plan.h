@@ -47,7 +47,7 @@ typedef struct gb_plan {
 
     int nlevels;
     int64_t cb_total, cbv_total;      /* entries of all update blocks/vectors */
-    int64_t fl_gemm;                  /* FMA-pairs*2 of the update products  */
+    double fl_gemm;                   /* algorithmic flops of the tile updates */
 
     /* host task arrays and launch sequences */
     gb_vec asm_t, node_t, potrf_t, trsm_t, gemm_t, gemm_owner, sweep_t;
@@ -80,9 +80,12 @@ typedef struct gb_plan {
     /* full (both triangles) FP64 copy of A for residuals, plus scaling */
     int64_t *d_Rp;
     int32_t *d_Rj;
-    double *d_Rx, *d_scale, *d_X, *d_R, *d_bx, *d_red;
-    size_t r_cap, rx_cap, x_cap;
+    double *d_Rx, *d_scale, *d_scale_perm, *d_X, *d_R, *d_bx, *d_red;
+    size_t rp_cap, rj_cap, rx_cap, x_cap, r_cap, bx_cap;
     uint64_t a_hash;
+    int mixed;                        /* 0 none, 1 FP32 factor, 2 FP64 factor */
+    int mixed_reason;                 /* why the FP64 factor was used */
+    double anorm;                     /* |A|_inf of the refined system */
 
     struct gb_plan *next;             /* side-table chaining */
 } gb_plan;
@@ -90,6 +93,23 @@ typedef struct gb_plan {
 #ifdef __cplusplus
 extern "C" {
 #endif
+
+/* per-Common library state (defined here for the drivers in gb_numeric.c
+ * and gb_mixed.c) */
+struct gb_ctx {
+    cudaStream_t stream;
+    int device;
+    int64_t opt_keep, opt_small;
+    double stats[8];
+    int64_t launches;            /* kernel launches issued since creation */
+    cudaEvent_t ev0, ev1;
+    /* optional per-launch timing of the factorization (gb300_set_option
+     * GB300_OPT_PROFILE): events around every launch, summed per kind */
+    int prof;
+    cudaEvent_t *pev;
+    int npev;
+    double kind_ms[16], kind_n[16];
+};
 
 int gb_vec_push(gb_vec *v, const void *e);
 void gb_vec_free(gb_vec *v);
@@ -100,6 +120,18 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols);
 int gb_plan_upload(gb_plan *P);
 void gb_plan_free(gb_plan *P);
 uint64_t gb_pattern_hash(const cholmod_factor *L);
+
+/* drivers shared by gb_numeric.c and gb_mixed.c */
+int gb_ctx_ready(gb_ctx *c);
+gb_plan *gb_plan_get(cholmod_factor *L, cholmod_common *Common, gb_ctx *ctx, int create);
+int gb_dev_grow(void **p, size_t *cap, size_t bytes);
+int gb_ensure_numeric(gb_plan *P, int dtype);
+int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dtype,
+                  const double *scale, double beta);
+int gb_run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int forward);
+int gb_fix_not_posdef(gb_plan *P, gb_ctx *ctx, cholmod_factor *L, int l_dtype,
+                      cholmod_common *Common);
+int gb_upload_input(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, int a_dtype);
 
 /* kernel launchers (gb_kernels.cu); dtype 0 = double, 4 = single; each
  * enqueues on st and returns the cudaError_t of the launch as int */
@@ -133,6 +165,10 @@ int gb_launch_residual(int64_t n, int nrhs, const int64_t *Rp, const int32_t *Rj
 int gb_launch_colmax3(int64_t n, int nrhs, const double *R, int64_t ldr, const double *X,
                       int64_t ldx, const double *B, int64_t ldb, double *out, cudaStream_t st);
 int gb_launch_anorm(int64_t n, const int64_t *Rp, const double *Rx, double *out, cudaStream_t st);
+int gb_launch_diag_minmax(int nsuper, const int64_t *Super, const int64_t *Pi,
+                          const int64_t *Px, const void *Lx, int dtype, double *out,
+                          cudaStream_t st);
+int gb_launch_fma_peak(int dtype, int iters, int blocks, float *ms, cudaStream_t st);
 int gb_launch_zero_range(void *x, int dtype, int64_t from, int64_t to, cudaStream_t st);
 
 #ifdef __cplusplus

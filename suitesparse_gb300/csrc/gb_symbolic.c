@@ -154,7 +154,7 @@ cholmod_factor *gb_analyze_perm(cholmod_sparse *A, const Int *Perm,
     Int *Up = NULL, *Ui = NULL;
     Int *Parent = gb_malloc(n, sizeof(Int), Common);
     Int *ColCount = gb_calloc(n, sizeof(Int), Common);
-    Int *W = gb_malloc(GB_MAX(6 * n, 1), sizeof(Int), Common);
+    Int *W = gb_malloc(6 * (n + 1), sizeof(Int), Common);
     if (!Parent || !ColCount || !W || !upper_pattern(n, Sp, Si, &Up, &Ui, Common))
         goto fail;
 
@@ -205,8 +205,8 @@ cholmod_factor *gb_analyze_perm(cholmod_sparse *A, const Int *Perm,
 
     /* fundamental supernodes: j joins j-1 when j is j-1's parent, its only
      * child, and column j-1's pattern is column j's plus the diagonal */
-    Int *Wi = W, *Super = W + n, *SuperMap = W + 2 * n, *Sparent = W + 3 * n,
-        *Snz = W + 4 * n, *Merged = W + 5 * n;
+    Int *Wi = W, *Super = W + (n + 1), *SuperMap = W + 2 * (n + 1),
+        *Sparent = W + 3 * (n + 1), *Snz = W + 4 * (n + 1), *Merged = W + 5 * (n + 1);
     for (Int j = 0; j < n; j++) Wi[j] = 0;
     for (Int j = 0; j < n; j++)
         if (Parent[j] != EMPTY) Wi[Parent[j]]++;
@@ -373,7 +373,7 @@ cholmod_factor *gb_analyze_perm(cholmod_sparse *A, const Int *Perm,
         L->maxesize = maxesize;
     }
 
-    gb_free(6 * n, sizeof(Int), W, Common);
+    gb_free(6 * (n + 1), sizeof(Int), W, Common);
     gb_free(n, sizeof(Int), Parent, Common);
     gb_free(n, sizeof(Int), ColCount, Common);
     gb_free(n + 1, sizeof(Int), Up, Common);
@@ -384,7 +384,7 @@ cholmod_factor *gb_analyze_perm(cholmod_sparse *A, const Int *Perm,
 
 fail:
     if (L) gb300_free_factor(&L, Common);
-    gb_free(6 * n, sizeof(Int), W, Common);
+    gb_free(6 * (n + 1), sizeof(Int), W, Common);
     gb_free(n, sizeof(Int), Parent, Common);
     gb_free(n, sizeof(Int), ColCount, Common);
     if (Up) gb_free(n + 1, sizeof(Int), Up, Common);

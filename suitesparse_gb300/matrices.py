@@ -57,10 +57,24 @@ def det_exp(x):
     return np.ldexp(p, k.astype(np.int64))
 
 
+def det_log(x):
+    """ln(x) of a positive scalar from +,-,*,/ only: x = m 2^e with m in
+    [sqrt(1/2), sqrt(2)), ln m = 2 atanh((m-1)/(m+1)) summed to convergence."""
+    m, e = np.frexp(np.float64(x))
+    if m < 0.7071067811865476:
+        m, e = m * 2.0, e - 1
+    t = (m - 1.0) / (m + 1.0)
+    t2, term, acc = t * t, t, 0.0
+    for j in range(1, 80, 2):
+        acc = acc + term / j
+        term = term * t2
+    return float(2.0 * acc + e * _LN2_HI + e * _LN2_LO)
+
+
 def log_uniform(lo, hi, u):
     """Map uniform u in [0,1) to log-uniform values in [lo, hi]."""
-    a = float(np.log(lo))   # constants: identical on any IEEE platform
-    b = float(np.log(hi))
+    a = det_log(lo)
+    b = det_log(hi)
     return det_exp(a + u * (b - a))
 
 
@@ -155,7 +169,8 @@ def laplace3d(nx, ny=None, nz=None, seed=None, lo=1e-2, hi=1e2, shift=0.0):
 def _rotations(u):
     """Rotation matrices from unit quaternions built from 4 uniforms each."""
     q = 2.0 * u.reshape(-1, 4) - 1.0
-    nrm = np.sqrt((q * q).sum(axis=1))
+    nrm = np.sqrt(((q[:, 0] * q[:, 0] + q[:, 1] * q[:, 1]) + q[:, 2] * q[:, 2])
+                  + q[:, 3] * q[:, 3])
     nrm[nrm == 0] = 1.0
     w, x, y, z = (q / nrm[:, None]).T
     R = np.empty((len(w), 3, 3))
@@ -176,7 +191,13 @@ def _spd_blocks(seed, count, offset, lo=0.1, hi=10.0):
     u = uniform01(seed, 7 * count, offset)
     lam = log_uniform(lo, hi, u[:3 * count]).reshape(count, 3)
     Q = _rotations(u[3 * count:])
-    B = np.einsum("kij,kj,klj->kil", Q, lam, Q)
+    B = np.zeros((count, 3, 3))
+    for i in range(3):              # explicit sums: fixed order on any platform
+        for l in range(3):
+            acc = Q[:, i, 0] * lam[:, 0] * Q[:, l, 0]
+            acc = acc + Q[:, i, 1] * lam[:, 1] * Q[:, l, 1]
+            acc = acc + Q[:, i, 2] * lam[:, 2] * Q[:, l, 2]
+            B[:, i, l] = acc
     return 0.5 * (B + B.transpose(0, 2, 1))
 
 
@@ -211,12 +232,17 @@ def elastic27(m, seed=2, dof=3, margin=1e-6):
     Boff = -_spd_blocks(seed, npair, 0)
     Bdiag = _spd_blocks(seed, nn, 7 * npair)
     # row sums of |off-diagonal| for diagonal dominance
+    aB = np.abs(Boff)
+    rows_abs = (aB[:, :, 0] + aB[:, :, 1]) + aB[:, :, 2]     # row sums of |B|
+    cols_abs = (aB[:, 0, :] + aB[:, 1, :]) + aB[:, 2, :]     # row sums of |B'|
     absoff = np.zeros((nn, 3))
-    np.add.at(absoff, pi, np.abs(Boff).sum(axis=2))
-    np.add.at(absoff, pj, np.abs(Boff).sum(axis=1))
-    own = np.abs(Bdiag).sum(axis=2) - np.abs(np.einsum("kii->ki", Bdiag))
+    np.add.at(absoff, pi, rows_abs)
+    np.add.at(absoff, pj, cols_abs)
+    aD = np.abs(Bdiag)
+    own = np.stack([aD[:, 0, 1] + aD[:, 0, 2], aD[:, 1, 0] + aD[:, 1, 2],
+                    aD[:, 2, 0] + aD[:, 2, 1]], axis=1)
     need = absoff + own + margin
-    d = np.einsum("kii->ki", Bdiag)
+    d = np.stack([Bdiag[:, 0, 0], Bdiag[:, 1, 1], Bdiag[:, 2, 2]], axis=1)
     newd = np.where(d >= need, d, need)
     Bdiag = Bdiag.copy()
     for r in range(3):
@@ -266,3 +292,42 @@ def digest(*arrays):
         h.update(str(a.shape).encode())
         h.update(a.tobytes())
     return h.hexdigest()
+
+
+def batch_sides(seed=3, count=8, lo=16, hi=96):
+    """``count`` distinct grid sides drawn uniformly from [lo, hi] (splitmix64
+    stream of ``seed``, first draws kept, repeats skipped)."""
+    sides, off = [], 0
+    while len(sides) < count:
+        u = uniform01(seed, 64, off)
+        off += 64
+        for v in u:
+            s = lo + int(v * (hi - lo + 1))
+            if s not in sides:
+                sides.append(s)
+                if len(sides) == count:
+                    break
+    return sides
+
+
+def batch_system(index, side, seed=3, lo=0.1, hi=10.0):
+    """System ``index`` of the batched workload: 2D 5-point Laplacian on a
+    side x side grid with log-uniform edge coefficients in [lo, hi]."""
+    return laplace2d(side, side, seed=(seed << 32) + index + 1, lo=lo, hi=hi)
+
+
+# Named workloads (the benchmark configurations; parity-test cases)
+CONFIGS = {
+    "c1": dict(kind="laplace2d", args=dict(nx=100, shift=1e-3), ordering="amd",
+               rhs_seed=0, nrhs=1),
+    "c2": dict(kind="laplace3d", args=dict(nx=64, seed=1, lo=1e-2, hi=1e2),
+               ordering="metis", rhs_seed=1, nrhs=1),
+    "c3": dict(kind="elastic27", args=dict(m=40, seed=2), ordering="metis",
+               rhs_seed=2, nrhs=1),
+}
+
+
+def config_matrix(name):
+    c = CONFIGS[name]
+    gen = {"laplace2d": laplace2d, "laplace3d": laplace3d, "elastic27": elastic27}[c["kind"]]
+    return gen(**c["args"])

@@ -1,0 +1,198 @@
+"""GPU supernodal factorization and sweeps through the C ABI, checked against
+the CPU oracle (same inputs) and the reference's golden outputs."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import make_case
+from suitesparse_gb300 import cholmod as CH
+from suitesparse_gb300 import matrices as M
+
+pytestmark = pytest.mark.gpu
+
+SMALL = ["g2c", "g2v", "g3", "g3a", "e27", "c1"]
+L_TOL = 1e-10          # ||L_gpu - L_ref||_F / ||L_ref||_F, FP64
+L_TOL_SINGLE = 1e-4    # FP32 factors from different summation orders
+
+
+def setup(meta, arrays, name, common, dtype="d"):
+    n, Ap, Ai, Ax = make_case(meta, name)
+    A = CH.sparse(n, Ap, Ai, Ax if dtype == "d" else Ax.astype(np.float32), common, dtype=dtype)
+    perm = arrays[name + "_Perm"].astype(np.int64)
+    L = CH.analyze_perm(A, perm, common)
+    return (n, Ap, Ai, Ax), A, L, perm
+
+
+def oracle_factor(oracle_mod, mat, perm, f, dtype="d", beta=0.0, quick=False):
+    n, Ap, Ai, Ax = mat
+    sym = {k: f[k] for k in ("Super", "Pi", "Px", "Ls")}
+    sym["n"] = n
+    Sp, Si, Sx = oracle_mod.permute_lower(n, Ap, Ai, Ax, perm)
+    if dtype == "s":
+        Sx = Sx.astype(np.float32)
+    st, minor, Lx = oracle_mod.factor(sym, Sp, Si, Sx, beta=beta, dtype=dtype, quick_return=quick)
+    return sym, st, minor, Lx
+
+
+def relerr(a, b):
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("name", SMALL)
+def test_factor_double(golden, lib, oracle_mod, name):
+    meta, arrays = golden
+    c = CH.Common()
+    mat, A, L, perm = setup(meta, arrays, name, c)
+    assert CH.factorize(A, L, c) == 1 and c.status == CH.CHOLMOD_OK
+    f = CH.factor_arrays(L)
+    assert f["minor"] == mat[0] and f["xtype"] == CH.CHOLMOD_REAL
+    sym, st, minor, Lx = oracle_factor(oracle_mod, mat, perm, f)
+    assert relerr(f["Lx"], Lx) < L_TOL
+    if name + "_Lx" in arrays:
+        assert relerr(f["Lx"], arrays[name + "_Lx"]) < L_TOL
+    assert abs(np.linalg.norm(f["Lx"]) - meta[name]["L_fro"]) <= 1e-12 * meta[name]["L_fro"]
+    # strictly upper part of every diagonal block stays zero, as in CHOLMOD
+    for s in range(f["nsuper"]):
+        nscol = f["Super"][s + 1] - f["Super"][s]
+        nsrow = f["Pi"][s + 1] - f["Pi"][s]
+        blk = f["Lx"][f["Px"][s]:f["Px"][s] + nsrow * nscol].reshape(nscol, nsrow).T
+        assert np.all(np.triu(blk[:nscol, :nscol], 1) == 0)
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+
+
+@pytest.mark.parametrize("name", ["g2v", "g3", "e27", "c1"])
+def test_factor_single(golden, lib, oracle_mod, name):
+    meta, arrays = golden
+    c = CH.Common()
+    mat, A, L, perm = setup(meta, arrays, name, c, dtype="s")
+    assert CH.factorize(A, L, c) == 1 and c.status == CH.CHOLMOD_OK
+    f = CH.factor_arrays(L)
+    assert f["dtype"] == CH.CHOLMOD_SINGLE
+    sym, st, minor, Lx = oracle_factor(oracle_mod, mat, perm, f, dtype="s")
+    assert relerr(f["Lx"], Lx) < L_TOL_SINGLE
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+
+
+@pytest.mark.parametrize("name", ["g2v", "g3", "e27", "c1"])
+@pytest.mark.parametrize("nrhs", [1, 8, 64])
+def test_solve_backward_error(golden, lib, oracle_mod, name, nrhs):
+    meta, arrays = golden
+    c = CH.Common()
+    mat, A, L, perm = setup(meta, arrays, name, c)
+    assert CH.factorize(A, L, c) == 1
+    B = M.rhs(mat[0], nrhs, 7 + nrhs)
+    X = CH.solve(L, B, c)
+    be = oracle_mod.backward_error(*mat, X, B)
+    assert be.max() <= 1e-14
+    f = CH.factor_arrays(L)
+    sym = {k: f[k] for k in ("Super", "Pi", "Px", "Ls")}
+    sym["n"] = mat[0]
+    Xo = oracle_mod.solve(sym, f["Lx"], perm, B)
+    assert np.abs(X - Xo).max() <= 1e-12 * np.abs(Xo).max()
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+
+
+@pytest.mark.parametrize("nrhs", [1, 3, 40])
+def test_super_lsolve_ltsolve_boundary(golden, lib, oracle_mod, nrhs):
+    """cholmod_l_super_lsolve / _ltsolve through the C ABI vs the oracle."""
+    meta, arrays = golden
+    c = CH.Common()
+    mat, A, L, perm = setup(meta, arrays, "g3", c)
+    assert CH.factorize(A, L, c) == 1
+    f = CH.factor_arrays(L)
+    sym = {k: f[k] for k in ("Super", "Pi", "Px", "Ls")}
+    sym["n"] = mat[0]
+    Y = M.rhs(mat[0], nrhs, 3)
+    for lower, fn in ((True, lib.cholmod_l_super_lsolve), (False, lib.cholmod_l_super_ltsolve)):
+        X = CH.dense(Y, c)
+        E = CH.dense(np.zeros((f["maxesize"] * nrhs, 1)), c)
+        assert fn(L, X, E, c.ptr) == 1 and c.status == CH.CHOLMOD_OK
+        got = CH.dense_array(X)
+        want = oracle_mod.sweep(sym, f["Lx"], Y, lower)
+        assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+        CH.free_dense(X, c)
+        CH.free_dense(E, c)
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+
+
+def test_super_numeric_boundary_with_beta(golden, lib, oracle_mod):
+    """cholmod_l_super_numeric called directly on S = tril(PAP'), beta != 0."""
+    meta, arrays = golden
+    c = CH.Common()
+    mat, A, L, perm = setup(meta, arrays, "g2v", c)
+    n, Ap, Ai, Ax = mat
+    from oracle import oracle as O
+    Sp, Si, Sx = O.permute_lower(n, Ap, Ai, Ax, perm)
+    S = CH.sparse(n, Sp, Si, Sx, c)
+    beta = 0.25
+    assert CH.super_numeric(S, L, c, beta=beta) == 1 and c.status == CH.CHOLMOD_OK
+    f = CH.factor_arrays(L)
+    sym, st, minor, Lx = oracle_factor(oracle_mod, mat, perm, f, beta=beta)
+    assert relerr(f["Lx"], Lx) < L_TOL
+    # refactorization of the same pattern with new values reuses the plan
+    S2 = CH.sparse(n, Sp, Si, 2.0 * Sx, c)
+    assert CH.super_numeric(S2, L, c, beta=2 * beta) == 1
+    f2 = CH.factor_arrays(L)
+    assert relerr(f2["Lx"], np.sqrt(2.0) * Lx) < L_TOL
+    for X in (S, S2, A):
+        CH.free_sparse(X, c)
+    CH.free_factor(L, c)
+
+
+@pytest.mark.parametrize("quick", [False, True])
+def test_not_positive_definite(golden, lib, oracle_mod, quick):
+    meta, arrays = golden
+    rec = meta["npd"]
+    c = CH.Common()
+    c["quick_return_if_not_posdef"] = 1 if quick else 0
+    mat, A, L, perm = setup(meta, arrays, "npd", c)
+    assert CH.factorize(A, L, c) == 1
+    assert c.status == CH.CHOLMOD_NOT_POSDEF
+    f = CH.factor_arrays(L)
+    assert f["minor"] == rec["minor"]
+    sym, st, minor, Lx = oracle_factor(oracle_mod, mat, perm, f, quick=quick)
+    assert st == 1 and minor == rec["minor"]
+    assert np.array_equal(f["Lx"] == 0, Lx == 0)
+    assert relerr(f["Lx"], Lx) < L_TOL
+    if not quick:
+        assert relerr(f["Lx"], arrays["npd_Lx"]) < L_TOL
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+
+
+def test_keep_factor_on_device(golden, lib):
+    meta, arrays = golden
+    c = CH.Common()
+    c.set_option(CH.GB300_OPT_KEEP_ON_DEVICE, 1)
+    mat, A, L, perm = setup(meta, arrays, "g3", c)
+    assert CH.factorize(A, L, c) == 1
+    B = M.rhs(mat[0], 2, 1)
+    X = CH.solve(L, B, c)
+    from oracle import oracle as O
+    assert O.backward_error(*mat, X, B).max() < 1e-14
+    assert lib.gb300_release_factor(L, c.ptr) == 1
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+
+
+def test_c2_full_size_fp64(golden, lib, oracle_mod):
+    """64^3 variable-coefficient Laplacian at full size: L norm against the
+    reference's and the solve's backward error (size-independent checks)."""
+    meta, arrays = golden
+    rec = meta["c2"]
+    c = CH.Common()
+    mat, A, L, perm = setup(meta, arrays, "c2", c)
+    assert CH.factorize(A, L, c) == 1 and c.status == CH.CHOLMOD_OK
+    f = CH.factor_arrays(L)
+    assert abs(np.linalg.norm(f["Lx"]) - rec["L_fro"]) <= 1e-10 * rec["L_fro"]
+    B = M.rhs(mat[0], 1, rec["rhs_seed"])
+    X = CH.solve(L, B, c)
+    assert oracle_mod.backward_error(*mat, X, B).max() <= 1e-12
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)

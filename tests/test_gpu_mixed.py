@@ -1,0 +1,75 @@
+"""FP32 factor + FP64 iterative refinement reaches the FP64 accuracy target."""
+import numpy as np
+import pytest
+
+from conftest import make_case
+from suitesparse_gb300 import cholmod as CH
+from suitesparse_gb300 import matrices as M
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12     # backward error |b-Ax|_inf / (|A|_inf |x|_inf + |b|_inf)
+
+
+def setup(meta, arrays, name, c):
+    n, Ap, Ai, Ax = make_case(meta, name)
+    A = CH.sparse(n, Ap, Ai, Ax, c)
+    L = CH.analyze_perm(A, arrays[name + "_Perm"].astype(np.int64), c)
+    return (n, Ap, Ai, Ax), A, L
+
+
+@pytest.mark.parametrize("name", ["g2v", "g3", "e27", "c1"])
+@pytest.mark.parametrize("nrhs", [1, 8])
+def test_refined_reaches_tolerance(golden, lib, oracle_mod, name, nrhs):
+    meta, arrays = golden
+    c = CH.Common()
+    mat, A, L = setup(meta, arrays, name, c)
+    assert CH.factorize_mixed(A, L, c) == 1 and c.status == CH.CHOLMOD_OK
+    B = M.rhs(mat[0], nrhs, 21)
+    X, info = CH.solve_refined(A, L, B, c, tol=TOL)
+    be = oracle_mod.backward_error(*mat, X, B)
+    assert be.max() <= TOL, (be, info)
+    assert info["berr"] <= TOL and info["iterations"] >= 1
+    # the FP32 factor is not written to L->x
+    assert L.contents.xtype == CH.CHOLMOD_PATTERN
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+
+
+def test_refined_c2_full_size(golden, lib, oracle_mod):
+    """64^3 variable-coefficient Laplacian (condition ~1e8) at full size."""
+    meta, arrays = golden
+    c = CH.Common()
+    mat, A, L = setup(meta, arrays, "c2", c)
+    assert CH.factorize_mixed(A, L, c) == 1
+    for nrhs in (1, 8, 64):
+        B = M.rhs(mat[0], nrhs, 5 + nrhs)
+        X, info = CH.solve_refined(A, L, B, c, tol=TOL)
+        be = oracle_mod.backward_error(*mat, X, B)
+        assert be.max() <= TOL, (nrhs, be.max(), info)
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+
+
+def test_mixed_matches_fp64_solution(golden, lib, oracle_mod):
+    meta, arrays = golden
+    c = CH.Common()
+    mat, A, L = setup(meta, arrays, "g3", c)
+    B = M.rhs(mat[0], 3, 2)
+    assert CH.factorize(A, L, c) == 1
+    X64 = CH.solve(L, B, c)
+    assert CH.factorize_mixed(A, L, c) == 1
+    X, info = CH.solve_refined(A, L, B, c, tol=1e-14)
+    assert np.abs(X - X64).max() <= 1e-11 * np.abs(X64).max()
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+
+
+def test_mixed_not_positive_definite(golden, lib):
+    meta, arrays = golden
+    c = CH.Common()
+    mat, A, L = setup(meta, arrays, "npd", c)
+    assert CH.factorize_mixed(A, L, c) == 1
+    assert c.status == CH.CHOLMOD_NOT_POSDEF
+    assert L.contents.minor == meta["npd"]["minor"]
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
