@@ -38,11 +38,13 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+CASE = "c2"
 METRIC = "factor TFLOP/s + solves/s at 1e-12 backward err, FP32+IR vs FP64; p50/p99"
 WORKLOAD = "c2: 3D 7-point variable-coefficient Laplacian 64^3 (n=262144), METIS"
 
 
-def load_case(name="c2"):
+def load_case(name=None):
+    name = name or CASE
     from suitesparse_gb300 import matrices as M
     gold = json.load(open(os.path.join(ROOT, "tests", "golden", "golden.json")))[name]
     arrays = np.load(os.path.join(ROOT, "tests", "golden", "golden_arrays.npz"))
@@ -230,6 +232,8 @@ def run_gpu(args):
     assert c["fl"] == fl
     B = M.rhs(n, 1, 1)
     info = CH.factor_info(L, c)
+    if gold.get("fl") is None:
+        fl = c["fl"]
 
     def step_mixed():
         t0 = time.perf_counter()
@@ -261,6 +265,12 @@ def run_gpu(args):
     t_step = [a + b for a, b in zip(fac_ms, sol_ms)]
     be = float(O.backward_error(n, Ap, Ai, Ax, X, B).max())
 
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"case": CASE, "factor_ms": statistics.mean(fac_ms),
+                              "solve_ms": statistics.mean(sol_ms), "backward_error": be,
+                              "gpu_launches": launches}), flush=True)
+        return 0
     # plain FP64 form (drop-in path: cholmod_l_super_numeric + supernodal sweeps)
     fp64_fac, fp64_sol = [], []
     for i in range(args.fp64_steps + 1):
@@ -366,7 +376,15 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--case", default="c2", choices=["c1", "c2", "c3"],
+                    help="workload (c2 is the benchmark configuration; c1/c3 for profiling)")
+    ap.add_argument("--quick", action="store_true",
+                    help="mixed-form steps only (no FP64 form, solve sweep, roofline, CPU leg)")
     args = ap.parse_args()
+    global CASE, WORKLOAD
+    CASE = args.case
+    if CASE != "c2":
+        WORKLOAD = f"{CASE} (profiling case, not the benchmark configuration)"
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

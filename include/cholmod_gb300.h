@@ -342,10 +342,18 @@ int gb300_finish (cholmod_common *Common) ;
  *      one thread block each; wider ones by the blocked multi-block path.
  *  GB300_OPT_PROFILE [0]: 1 = time every kernel launch of the factorization
  *      with CUDA events (summed per kernel kind, see gb300_get_profile); also
- *      clears the accumulated profile. */
+ *      clears the accumulated profile.
+ *  GB300_OPT_SWEEP [1]: 1 = each sweep is one dependency-driven launch over
+ *      all supernodes (diagonal blocks applied through their inverses);
+ *      0 = one launch per etree level and block step.
+ *  GB300_OPT_TRACE [0]: 1 = the single-launch sweeps record, per task, the
+ *      global-timer values when it started, when its dependencies were met
+ *      and when it finished (gb300_get_trace). */
 #define GB300_OPT_KEEP_ON_DEVICE 1
 #define GB300_OPT_SMALL_COLS     2
 #define GB300_OPT_PROFILE        3
+#define GB300_OPT_SWEEP          4
+#define GB300_OPT_TRACE          5
 int gb300_set_option (cholmod_common *Common, int option, int64_t value) ;
 
 /* Supernodal symbolic analysis of A (stype < 0, lower) with a given final
@@ -412,6 +420,21 @@ long gb300_abi_sizeof (int object) ;
  * for kind k = 1 assembly, 2 small-supernode factor, 3 diagonal-block LL',
  * 4 panel triangular solve, 5 tile update (C -= A B'). */
 int gb300_get_profile (cholmod_common *Common, double *ms, double *count, int nkinds) ;
+
+/* Per-task times (ns, device global timer) of the last traced forward
+ * (forward = 1) or backward sweep: out[3t..3t+2] = start, dependencies met,
+ * end of task t, tasks in ticket order.  Returns the number of tasks. */
+int gb300_get_trace (cholmod_common *Common, int forward, unsigned long long *out,
+    int64_t nmax) ;
+
+/* Per-task trace of the last traced factorization's task graphs (all
+ * levels, plan order): out[3t..3t+2] = claimed, finished (ns), block. */
+int gb300_get_factor_trace (cholmod_common *Common, unsigned long long *out,
+    int64_t nmax) ;
+
+/* The factorization task graph of L's plan, 8 int32 per task: type, s, b,
+ * r, c, priority, level, 0 (task types as in the trace).  Returns the count. */
+int gb300_plan_tasks (cholmod_factor *L, cholmod_common *Common, int32_t *out, int64_t nmax) ;
 
 /* Facts of the GPU plan of L (built if needed): [0] algorithmic flops of the
  * tile updates, [1] etree levels, [2] launches per factorization, [3]

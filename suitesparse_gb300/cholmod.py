@@ -21,7 +21,8 @@ CHOLMOD_OK, CHOLMOD_NOT_INSTALLED, CHOLMOD_OUT_OF_MEMORY = 0, -1, -2
 CHOLMOD_TOO_LARGE, CHOLMOD_INVALID, CHOLMOD_GPU_PROBLEM = -3, -4, -5
 CHOLMOD_NOT_POSDEF, CHOLMOD_DSMALL = 1, 2
 CHOLMOD_A = 0
-GB300_OPT_KEEP_ON_DEVICE, GB300_OPT_SMALL_COLS, GB300_OPT_PROFILE = 1, 2, 3
+GB300_OPT_KEEP_ON_DEVICE, GB300_OPT_SMALL_COLS, GB300_OPT_PROFILE, GB300_OPT_SWEEP = 1, 2, 3, 4
+GB300_OPT_TRACE = 5
 KIND_NAMES = {1: "assemble", 2: "factor_small", 3: "potrf_diag", 4: "trsm_rows", 5: "gemm_tile"}
 
 
@@ -91,6 +92,9 @@ def lib():
         "gb300_get_profile": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]),
         "gb300_factor_info": (C.c_int, [FP, vp, C.POINTER(C.c_double), C.c_int]),
         "gb300_fma_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+        "gb300_get_trace": (C.c_int, [vp, C.c_int, C.POINTER(C.c_ulonglong), C.c_int64]),
+        "gb300_get_factor_trace": (C.c_int, [vp, C.POINTER(C.c_ulonglong), C.c_int64]),
+        "gb300_plan_tasks": (C.c_int, [FP, vp, C.POINTER(C.c_int32), C.c_int64]),
         "cholmod_l_super_numeric": (C.c_int, [SP, SP, C.POINTER(C.c_double), FP, vp]),
         "cholmod_l_super_lsolve": (C.c_int, [FP, DP, DP, vp]),
         "cholmod_l_super_ltsolve": (C.c_int, [FP, DP, DP, vp]),
@@ -150,6 +154,20 @@ class Common:
         cnt = (C.c_double * 16)()
         lib().gb300_get_profile(self.ptr, ms, cnt, 16)
         return {KIND_NAMES.get(k, str(k)): (ms[k], cnt[k]) for k in range(16) if cnt[k]}
+
+    def trace(self, forward, nmax=1 << 22):
+        out = (C.c_ulonglong * (3 * nmax))()
+        nt = lib().gb300_get_trace(self.ptr, 1 if forward else 0, out, nmax)
+        if nt < 0:
+            return None
+        return np.frombuffer(out, dtype=np.uint64, count=3 * nt).reshape(nt, 3).copy()
+
+    def factor_trace(self, nmax=1 << 22):
+        out = (C.c_ulonglong * (3 * nmax))()
+        nt = lib().gb300_get_factor_trace(self.ptr, out, nmax)
+        if nt < 0:
+            return None
+        return np.frombuffer(out, dtype=np.uint64, count=3 * nt).reshape(nt, 3).copy()
 
     def finish(self):
         if self.ptr:

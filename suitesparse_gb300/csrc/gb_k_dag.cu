@@ -1,0 +1,250 @@
+// gb_k_dag.cu -- device task-graph executor for the wide supernodes of one
+// etree level (and the update blocks of every supernode of the level).
+//
+// The task graph is static per symbolic pattern (built on the host,
+// gb_plan.c): 64-grid tile tasks of a right-looking blocked LL' of each wide
+// panel (diagonal LL' + inverse, panel solve, trailing update) and the
+// update-block products.  One persistent launch executes it: thread 0 of a
+// block pops a ready task (critical-path queue first), the block runs it,
+// then thread 0 decrements the dependency counters of its successors and
+// pushes each one that reaches zero onto the queue of its priority.  Blocks
+// never wait for an unfinished task: a task is popped only when ready, so
+// the executor cannot deadlock.  Popping from empty queues spins with a
+// bound (GB_DAG_SPIN), after which the error word is set and every block
+// returns.
+//
+// Reference (the same arithmetic, per supernode, on the CPU):
+// CHOLMOD/Supernodal/t_cholmod_super_numeric_worker.c dpotrf :1004-1058,
+// dtrsm :1152-1218, the dsyrk/dgemm update matrices :768-883.
+
+#include "gb_k_common.cuh"
+
+#define GB_DAG_SPIN (1 << 24)
+
+struct gb_dag_dev {
+    const gb_dtask *tasks;
+    int ntasks;
+    const int32_t *succ_ptr, *succ;
+    int32_t *cnt;            // live dependency counters
+    int32_t *q0, *q1;        // ready queues: slot = task id, -1 not yet written
+    int32_t *ctrl;           // [0] head0 [1] tail0 [2] head1 [3] tail1 [4] roles [5] err
+                             // [6] tasks of the critical queue [7] of the bulk queue
+    int32_t *err;            // error word kept across levels
+    unsigned long long *trace; // optional: per task [claimed, finished, block] (ns)
+};
+
+__device__ __forceinline__ unsigned long long dag_timer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ int dag_ld_acquire(const int32_t *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void dag_st_release(int32_t *p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ int dag_add_acq_rel(int32_t *p, int v)
+{
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+#define GB_DAG_POLLERS 16   // blocks that serve only the critical-path queue
+
+// thread 0: claim slot h of a queue (the pusher reserved it with tail and
+// writes it right away, or will once the task is ready)
+__device__ int dag_take(const gb_dag_dev &D, const int32_t *slots, int h)
+{
+    for (int k = 0; k < GB_DAG_SPIN; k++) {
+        const int v = dag_ld_acquire(slots + h);
+        if (v >= 0) return v;
+        if (dag_ld_acquire(D.ctrl + 5)) return -2;
+        __nanosleep(k < 64 ? 32 : 256);
+    }
+    atomicExch(D.ctrl + 5, 1);
+    atomicExch(D.err, 1);
+    return -2;
+}
+
+// Thread 0: the next task id, -1 when its queue is exhausted, -2 on error.
+// The first GB_DAG_POLLERS blocks to start serve the critical-path queue:
+// they claim a slot only when it is already reserved (compare-and-swap on
+// the head, no waiting for future tasks).  All other blocks claim bulk-queue
+// slots in order with atomicAdd and wait for their slot to be filled.
+// Deadlock-free: slots are reserved in order, so a block waiting on a bulk
+// slot waits either for a slot being written or for a task not yet ready,
+// and every ready task is either in a claimed slot (its block runs it) or
+// is a critical task a poller can claim; pollers never wait.
+__device__ int dag_pop(const gb_dag_dev &D, int poller)
+{
+    int32_t *ctrl = D.ctrl;
+    const int total0 = ctrl[6], total1 = ctrl[7];
+    if (!poller) {
+        const int h = atomicAdd(ctrl + 2, 1);
+        if (h >= total1) return -1;
+        return dag_take(D, D.q1, h);
+    }
+    for (int it = 0; it < GB_DAG_SPIN; it++) {
+        if (dag_ld_acquire(ctrl + 5)) return -2;
+        int h0 = dag_ld_acquire(ctrl + 0);
+        if (h0 < total0 && h0 < dag_ld_acquire(ctrl + 1)) {
+            if (atomicCAS(ctrl + 0, h0, h0 + 1) == h0) return dag_take(D, D.q0, h0);
+            continue;
+        }
+        if (h0 >= total0) return -1;
+        __nanosleep(64);
+    }
+    atomicExch(ctrl + 5, 1);
+    atomicExch(D.err, 1);
+    return -2;
+}
+
+// thread 0, after the block finished task id
+__device__ void dag_complete(const gb_dag_dev &D, int id)
+{
+    __threadfence();
+    for (int e = D.succ_ptr[id]; e < D.succ_ptr[id + 1]; e++) {
+        const int v = D.succ[e];
+        if (dag_add_acq_rel(D.cnt + v, -1) == 1) {
+            const int q = D.tasks[v].prio ? 1 : 0;
+            const int slot = atomicAdd(D.ctrl + 2 * q + 1, 1);
+            dag_st_release((q ? D.q1 : D.q0) + slot, v);
+        }
+    }
+}
+
+template <typename T>
+__host__ __device__ constexpr size_t dag_smem()
+{
+    // diagonal block (64 x 65) + two operand tiles (64 x 65) for the panel
+    // solve; the tile update uses 2 x 16 x 68 of the same space
+    return sizeof(T) * (3 * 64 * 65);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T (*A)[65] = (T (*)[65])smem_raw;
+    T *S1 = (T *)smem_raw + 64 * 65, *S2 = S1 + 64 * 65;
+    __shared__ int sid, sfail, spoll;
+    if (threadIdx.x == 0) spoll = atomicAdd(D.ctrl + 4, 1) < GB_DAG_POLLERS;
+    __syncthreads();
+    const int poller = spoll;
+    for (;;) {
+        if (threadIdx.x == 0) sid = dag_pop(D, poller);
+        __syncthreads();
+        const int id = sid;
+        if (id < 0) return;
+        if (D.trace && threadIdx.x == 0) {
+            D.trace[3 * (size_t)id] = dag_timer();
+            D.trace[3 * (size_t)id + 2] = blockIdx.x;
+        }
+        const gb_dtask tk = D.tasks[id];
+        const int s = tk.s;
+        const int nscol = (int)(P.Super[s + 1] - P.Super[s]);
+        const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
+        T *panel = Lx + P.Px[s];
+        const int f = P.fail[s];
+        if (tk.type == GB_DT_POTRF) {
+            const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
+            if (f < 0) {
+                T *blk = panel + c0 + (int64_t)c0 * nsrow;
+                for (int idx = threadIdx.x; idx < 64 * 64; idx += blockDim.x) {
+                    const int i = idx & 63, j = idx >> 6;
+                    A[i][j] = (i < nb && j < nb && i >= j) ? blk[i + (int64_t)j * nsrow] : (T)0;
+                }
+                __syncthreads();
+                const int fl = potrf64<T>(A, nb, &sfail);
+                __syncthreads();
+                for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+                    const int i = idx % nb, j = idx / nb;
+                    if (i >= j) blk[i + (int64_t)j * nsrow] = A[i][j];
+                }
+                if (fl >= 0 && threadIdx.x == 0) {
+                    P.fail[s] = c0 + fl;
+                    atomicExch(P.anyfail, 1);
+                }
+                tri_inverse64<T>(A, nb, S1, Linv + P.linvoff[P.blkoff[s] + tk.b]);
+            }
+        } else if (tk.type == GB_DT_TRSM) {
+            const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
+            if (!(f >= 0 && f < c0)) {
+                const int ncols = (f >= 0) ? f - c0 : nb;
+                const int r0 = max(64 * tk.r, c0 + nb), r1 = min(64 * tk.r + 64, nsrow);
+                const int nr = r1 - r0;
+                const T *li = Linv + P.linvoff[P.blkoff[s] + tk.b];
+                for (int idx = threadIdx.x; idx < 64 * 64; idx += blockDim.x) {
+                    const int cc = idx & 63, k = idx >> 6;
+                    S2[k * 65 + cc] = (cc < nb && k < nb) ? li[cc + (int64_t)k * nb] : (T)0;
+                    S1[k * 65 + cc] = (cc < nr && k < nb) ? panel[r0 + cc + (int64_t)(c0 + k) * nsrow] : (T)0;
+                }
+                __syncthreads();
+                trsm_tile<T>(S1, S2, 65, nr, nb, ncols, panel + r0 + (int64_t)c0 * nsrow, nsrow);
+            }
+        } else if (tk.type == GB_DT_UPD) {
+            if (f < 0) {
+                const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
+                const int cs = 64 * tk.c, ce = min(cs + 64, nscol);
+                const int rs = max(64 * tk.r, cs), re = min(64 * tk.r + 64, nsrow);
+                gemm_tile_k64<T>(panel + rs + (int64_t)c0 * nsrow, nsrow,
+                                 panel + cs + (int64_t)c0 * nsrow, nsrow,
+                                 panel + rs + (int64_t)cs * nsrow, nsrow,
+                                 re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, S1, S2);
+            }
+        } else {  // GB_DT_CB
+            if (f < 0) {
+                const int m = nsrow - nscol;
+                const int I = 64 * tk.r, J = 64 * tk.c;
+                gemm_tile_nt<T>(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
+                                CB + P.cboff[s] + I + (int64_t)J * m, m,
+                                min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
+                                S1, S2);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (D.trace) D.trace[3 * (size_t)id + 1] = dag_timer();
+            dag_complete(D, id);
+        }
+    }
+}
+
+extern "C" {
+
+int gb_launch_dag(const gb_pattern_ptrs *pp, const gb_dag_args *a, void *Lx, void *CB,
+                  void *Linv, int dtype, int grid, cudaStream_t st)
+{
+    if (a->ntasks <= 0) return 0;
+    gb_dev_pattern P = gb_to_dev(pp);
+    gb_dag_dev D;
+    D.tasks = a->tasks; D.ntasks = a->ntasks; D.succ_ptr = a->succ_ptr; D.succ = a->succ;
+    D.cnt = a->cnt; D.q0 = a->q0; D.q1 = a->q1; D.ctrl = a->ctrl; D.err = a->err;
+    D.trace = a->trace;
+    static int configured = 0;
+    if (!configured) {
+        cudaFuncSetAttribute(k_dag<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<double>());
+        cudaFuncSetAttribute(k_dag<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<float>());
+        configured = 1;
+    }
+    /* the first GB_DAG_POLLERS blocks serve only the critical queue: keep
+     * at least one bulk block, and no more bulk blocks than tasks */
+    if (grid > a->ntasks + GB_DAG_POLLERS) grid = a->ntasks + GB_DAG_POLLERS;
+    if (grid < GB_DAG_POLLERS + 1) grid = GB_DAG_POLLERS + 1;
+    if (dtype == 0) k_dag<double><<<grid, 256, dag_smem<double>(), st>>>(P, D, (double *)Lx, (double *)CB, (double *)Linv);
+    else k_dag<float><<<grid, 256, dag_smem<float>(), st>>>(P, D, (float *)Lx, (float *)CB, (float *)Linv);
+    return (int)cudaGetLastError();
+}
+
+}  // extern "C"

@@ -59,15 +59,23 @@ __global__ void k_residual(int64_t n, int nrhs, const int64_t *__restrict__ Rp,
     }
 }
 
-// out[0] = min over the diagonal of L of L(k,k)^2, out[1] = max (one block)
+// out[0] = min over the diagonal of L of L(k,k)^2, out[1] = max.  Grid-wide:
+// per-block reduction, then 64-bit atomics on the bit patterns (the values
+// are >= 0, for which IEEE order equals unsigned integer order).
+__global__ void k_minmax_init(double *out)
+{
+    out[0] = __longlong_as_double(0x7FF0000000000000LL);   // +inf
+    out[1] = 0.0;
+}
+
 template <typename T>
 __global__ void k_diag_minmax(int nsuper, const int64_t *__restrict__ Super,
                               const int64_t *__restrict__ Pi, const int64_t *__restrict__ Px,
                               const T *__restrict__ Lx, double *out)
 {
-    __shared__ double smin[1024], smax[1024];
-    double lo = 1e308, hi = 0.0;
-    for (int s = threadIdx.x; s < nsuper; s += blockDim.x) {
+    __shared__ double smin[256], smax[256];
+    double lo = __longlong_as_double(0x7FF0000000000000LL), hi = 0.0;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsuper; s += gridDim.x * blockDim.x) {
         const int nscol = (int)(Super[s + 1] - Super[s]);
         const int64_t nsrow = Pi[s + 1] - Pi[s];
         const T *panel = Lx + Px[s];
@@ -87,7 +95,10 @@ __global__ void k_diag_minmax(int nsuper, const int64_t *__restrict__ Super,
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) { out[0] = smin[0]; out[1] = smax[0]; }
+    if (threadIdx.x == 0) {
+        atomicMin((unsigned long long *)&out[0], (unsigned long long)__double_as_longlong(smin[0]));
+        atomicMax((unsigned long long *)&out[1], (unsigned long long)__double_as_longlong(smax[0]));
+    }
 }
 
 // per column r: out[3r] = max|R|, out[3r+1] = max|X|, out[3r+2] = max|B|;
@@ -124,7 +135,8 @@ __global__ void k_anorm_inf(int64_t n, const int64_t *__restrict__ Rp,
 {
     __shared__ double sm[256];
     double best = 0;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
         double acc = 0;
         for (int64_t p = Rp[i]; p < Rp[i + 1]; p++) acc += fabs(Rx[p]);
         best = fmax(best, acc);
@@ -135,7 +147,8 @@ __global__ void k_anorm_inf(int64_t n, const int64_t *__restrict__ Rp,
         if (threadIdx.x < o) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + o]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) *out = sm[0];
+    if (threadIdx.x == 0)
+        atomicMax((unsigned long long *)out, (unsigned long long)__double_as_longlong(sm[0]));
 }
 
 // zero factor entries [from, to) (not-positive-definite clean-up)
@@ -234,8 +247,10 @@ int gb_launch_diag_minmax(int nsuper, const int64_t *Super, const int64_t *Pi,
                           const int64_t *Px, const void *Lx, int dtype, double *out,
                           cudaStream_t st)
 {
-    if (dtype == 0) k_diag_minmax<double><<<1, 1024, 0, st>>>(nsuper, Super, Pi, Px, (const double *)Lx, out);
-    else k_diag_minmax<float><<<1, 1024, 0, st>>>(nsuper, Super, Pi, Px, (const float *)Lx, out);
+    k_minmax_init<<<1, 1, 0, st>>>(out);
+    const int g = gb_grid_for(nsuper);
+    if (dtype == 0) k_diag_minmax<double><<<g, 256, 0, st>>>(nsuper, Super, Pi, Px, (const double *)Lx, out);
+    else k_diag_minmax<float><<<g, 256, 0, st>>>(nsuper, Super, Pi, Px, (const float *)Lx, out);
     return (int)cudaGetLastError();
 }
 
@@ -248,7 +263,8 @@ int gb_launch_colmax3(int64_t n, int nrhs, const double *R, int64_t ldr, const d
 
 int gb_launch_anorm(int64_t n, const int64_t *Rp, const double *Rx, double *out, cudaStream_t st)
 {
-    k_anorm_inf<<<1, 256, 0, st>>>(n, Rp, Rx, out);
+    if (cudaMemsetAsync(out, 0, sizeof(double), st) != cudaSuccess) return 1;
+    k_anorm_inf<<<gb_grid_for(n), 256, 0, st>>>(n, Rp, Rx, out);
     return (int)cudaGetLastError();
 }
 

@@ -1,0 +1,476 @@
+// gb_k_sweep1.cu -- single-launch supernodal sweeps.
+//
+// Each sweep (forward L y = b, backward L' x = y) is one kernel launch whose
+// thread blocks take tasks in a fixed topological order through an atomic
+// ticket and wait, with bounded spins, for the tasks they depend on.  Tasks
+// are ordered by etree level (ascending for the forward sweep, descending
+// for the backward sweep), so that independent branches interleave:
+//
+//   forward  per supernode s: its 64-row diagonal blocks in order, then its
+//            off-diagonal row blocks.  A diagonal block waits for s's
+//            children (their update vectors) and, one at a time, for the
+//            earlier diagonal blocks of s:  x_i = Linv_ii (b_i - children -
+//            sum_{j<i} L_ij x_j).  An off-diagonal row block waits for all
+//            diagonal blocks of s and writes its rows of the update vector
+//            u_s = (children's contributions) + L21 x1, which s's parent
+//            gathers (owner-computes, children in a fixed order).
+//   backward per supernode s, diagonal blocks last to first: wait for the
+//            parent supernode (whose completion implies all ancestors'),
+//            x_i = Linv_ii' (y_i - L21(:,i)' x(rows of s) - sum_{j>i} L_ji' x_j).
+//
+// Latency: the 64x64 tile of L needed after a wait is loaded into registers
+// before the wait and parked in shared memory after it, so a dependency step
+// costs one flag round trip plus shared-memory arithmetic.  Products reduce
+// over 4 lanes with shuffles (no padded right-hand sides: the FP64 pipe of
+// this GPU issues under 2 multiply-adds per clock per SM).
+//
+// A task only waits for tasks with smaller tickets, which were taken by
+// blocks already running, so the sweep cannot deadlock.  Every wait gives up
+// after GB_SPIN_LIMIT polls, sets the error word and returns; every other
+// waiter then returns at once.  Linv holds the inverse of every diagonal
+// block (k_diag_inverse, after the factorization).
+//
+// Correspondence with the reference: CHOLMOD/Supernodal/
+// t_cholmod_super_solve_worker.c (dtrsv/dtrsm + dgemv/dgemm per supernode,
+// forward :63-301, backward :358-578).
+
+#include "gb_k_common.cuh"
+
+#define SR 64          // rows of a diagonal block / row block
+#define TLD 65         // padded leading dimension of a shared tile
+#define RCH 16         // right-hand-side columns per pass
+#define GB_SPIN_LIMIT (1 << 22)
+
+__device__ __forceinline__ int ld_acquire(const int32_t *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(int32_t *p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long gtimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// thread 0 only: wait until *flag >= target; false on timeout / abort
+__device__ bool wait_ge(const int32_t *flag, int target, int32_t *err)
+{
+    if (ld_acquire(flag) >= target) return true;
+    for (int it = 0; it < GB_SPIN_LIMIT; it++) {
+        __nanosleep(64);
+        if (ld_acquire(flag) >= target) return true;
+        if (ld_acquire(err)) return false;
+    }
+    atomicExch(err, 1);
+    return false;
+}
+
+// ---- 64x64 tiles: registers -> shared memory ------------------------------
+
+// element (rr, cc) of the nr x nc region at base (leading dimension ld);
+// thread t holds elements t + 256 q, q = 0..15 (coalesced along rr)
+template <typename T>
+__device__ __forceinline__ void tile_fetch(T (&reg)[16], const T *base, int64_t ld, int nr, int nc)
+{
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const int idx = threadIdx.x + q * 256;
+        const int rr = idx & 63, cc = idx >> 6;
+        reg[q] = (rr < nr && cc < nc) ? base[rr + (int64_t)cc * ld] : (T)0;
+    }
+}
+
+// tile[cc * TLD + rr] = element (rr, cc)
+template <typename T>
+__device__ __forceinline__ void tile_park(T *tile, const T (&reg)[16])
+{
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const int idx = threadIdx.x + q * 256;
+        tile[(idx >> 6) * TLD + (idx & 63)] = reg[q];
+    }
+}
+
+// ys[r][k] += sign * sum_c op(tile)(r, c) xs[c][k],  op = identity (trans=0:
+// element (r, c) = tile[c*TLD + r]) or transpose (trans=1: tile[r*TLD + c]).
+// Thread layout: row r = 8*warp + lane/4, lanes lane%4 split c; 2 shuffles.
+template <typename T, int NK>
+__device__ __forceinline__ void tile_gemv_k(const T *tile, int trans, int nr, int nc,
+                                            const T *xs, T *ys, int nk, T sign)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = warp * 8 + (lane >> 2), q = lane & 3;
+    for (int k0 = 0; k0 < nk; k0 += NK) {
+        T acc[NK];
+#pragma unroll
+        for (int kk = 0; kk < NK; kk++) acc[kk] = (T)0;
+        if (r < nr) {
+            for (int c = q; c < nc; c += 4) {
+                const T l = trans ? tile[r * TLD + c] : tile[c * TLD + r];
+#pragma unroll
+                for (int kk = 0; kk < NK; kk++) acc[kk] += l * xs[c * RCH + k0 + kk];
+            }
+        }
+#pragma unroll
+        for (int kk = 0; kk < NK; kk++) {
+            T v = acc[kk];
+            v += __shfl_xor_sync(0xffffffffu, v, 1);
+            v += __shfl_xor_sync(0xffffffffu, v, 2);
+            if (q == 0 && r < nr && k0 + kk < nk) ys[r * RCH + k0 + kk] += sign * v;
+        }
+    }
+}
+
+template <typename T>
+__device__ void tile_gemv(const T *tile, int trans, int nr, int nc, const T *xs, T *ys,
+                          int nk, T sign)
+{
+    if (nk == 1) tile_gemv_k<T, 1>(tile, trans, nr, nc, xs, ys, nk, sign);
+    else if (nk <= 2) tile_gemv_k<T, 2>(tile, trans, nr, nc, xs, ys, nk, sign);
+    else if (nk <= 4) tile_gemv_k<T, 4>(tile, trans, nr, nc, xs, ys, nk, sign);
+    else tile_gemv_k<T, 8>(tile, trans, nr, nc, xs, ys, nk, sign);
+    __syncthreads();
+}
+
+struct gb_sweep_state {
+    const gb_stask *tasks;
+    int ntasks;
+    const int32_t *blkoff;     // first global diagonal-block id of s
+    const int64_t *linvoff;    // offset of each diagonal block's inverse
+    const int32_t *ntask_s;    // tasks of supernode s in this sweep
+    const int32_t *parent;     // supernodal etree parent (-1 root)
+    int32_t *xready, *done, *ticket, *err;
+    unsigned long long *trace; // optional: per task [start, dependencies met, end] (ns)
+};
+
+// dynamic shared memory: tile A, tile B (64 x TLD each), xs, ys (64 x RCH)
+template <typename T>
+__host__ __device__ constexpr size_t sweep_smem() { return sizeof(T) * (2 * SR * TLD + 2 * SR * RCH); }
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_fwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int nrhs,
+            T *Y, int64_t ldy, T *U)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *tA = (T *)smem_raw, *tB = tA + SR * TLD, *xs = tB + SR * TLD, *ys = xs + SR * RCH;
+    __shared__ int st, abort_;
+    T reg[16];
+    for (;;) {
+        if (threadIdx.x == 0) { st = atomicAdd(S.ticket, 1); abort_ = 0; }
+        __syncthreads();
+        const int t = st;
+        if (t >= S.ntasks) return;
+        const gb_stask tk = S.tasks[t];
+        if (S.trace && threadIdx.x == 0) S.trace[3 * (size_t)t] = gtimer();
+        const int s = tk.s;
+        const int64_t k1 = P.Super[s];
+        const int nscol = (int)(P.Super[s + 1] - k1);
+        const int64_t psi = P.Pi[s];
+        const int nsrow = (int)(P.Pi[s + 1] - psi);
+        const int m = nsrow - nscol;
+        const T *panel = Lx + P.Px[s];
+        T *us = U + P.cbvoff[s] * nrhs;
+        const int r0 = tk.r0, nr = tk.nr;
+        const int nblk = (nscol + SR - 1) / SR;
+        // first L tile this task needs, fetched before any wait
+        if (tk.kind == 0 && tk.idx > 0) tile_fetch(reg, panel + r0, nsrow, nr, SR);
+        else if (tk.kind == 1) tile_fetch(reg, panel + r0, nsrow, nr, min(SR, nscol));
+        if (threadIdx.x == 0) {
+            for (int ci = P.child_ptr[s]; ci < P.child_ptr[s + 1] && !abort_; ci++) {
+                const int c = P.child_list[ci];
+                if (!wait_ge(S.done + c, S.ntask_s[c], S.err)) abort_ = 1;
+            }
+        }
+        __syncthreads();
+        if (abort_) return;
+        if (S.trace && threadIdx.x == 0) S.trace[3 * (size_t)t + 1] = gtimer();
+        for (int k0 = 0; k0 < nrhs; k0 += RCH) {
+            const int nk = min(RCH, nrhs - k0);
+            if (k0 > 0) {
+                if (tk.kind == 0 && tk.idx > 0) tile_fetch(reg, panel + r0, nsrow, nr, SR);
+                else if (tk.kind == 1) tile_fetch(reg, panel + r0, nsrow, nr, min(SR, nscol));
+            }
+            // start value: b (diagonal rows) or 0 (update-vector rows)
+            for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
+                const int r = idx / RCH, k = idx % RCH;
+                T v = (T)0;
+                if (tk.kind == 0 && r < nr && k < nk) v = Y[k1 + r0 + r + (int64_t)(k0 + k) * ldy];
+                ys[idx] = v;
+            }
+            __syncthreads();
+            // gather the children's update vectors at rows [r0, r0+nr)
+            const T gsign = tk.kind == 0 ? (T)-1 : (T)1;
+            for (int ci = P.child_ptr[s]; ci < P.child_ptr[s + 1]; ci++) {
+                const int c = P.child_list[ci];
+                const int ncc = (int)(P.Super[c + 1] - P.Super[c]);
+                const int64_t pic = P.Pi[c];
+                const int mc = (int)(P.Pi[c + 1] - pic) - ncc;
+                const int32_t *rm = P.relmap + pic + ncc;
+                const int a = lower_bound_i32(rm, 0, mc, r0);
+                const int b = lower_bound_i32(rm, a, mc, r0 + nr);
+                const T *uc = U + P.cbvoff[c] * nrhs;
+                for (int idx = threadIdx.x; idx < (b - a) * nk; idx += blockDim.x) {
+                    const int i = a + idx % (b - a), k = idx / (b - a);
+                    ys[(rm[i] - r0) * RCH + k] += gsign * uc[i + (int64_t)(k0 + k) * mc];
+                }
+                __syncthreads();
+            }
+            if (tk.kind == 0) {
+                const int i = tk.idx;
+                for (int j = 0; j < i; j++) {
+                    if (k0 == 0 && threadIdx.x == 0) {
+                        if (!wait_ge(S.xready + S.blkoff[s] + j, 1, S.err)) abort_ = 1;
+                    }
+                    tile_park(tA, reg);
+                    __syncthreads();
+                    if (abort_) return;
+                    for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
+                        const int c = idx / RCH, k = idx % RCH;
+                        const int nc = min(SR, nscol - j * SR);
+                        xs[idx] = (c < nc && k < nk) ? Y[k1 + j * SR + c + (int64_t)(k0 + k) * ldy] : (T)0;
+                    }
+                    __syncthreads();
+                    if (j + 1 < i) tile_fetch(reg, panel + r0 + (int64_t)((j + 1) * SR) * nsrow, nsrow, nr, SR);
+                    tile_gemv<T>(tA, 0, nr, min(SR, nscol - j * SR), xs, ys, nk, (T)-1);
+                }
+                // x_i = Linv_ii ys
+                tile_fetch(reg, Linv + S.linvoff[S.blkoff[s] + i], nr, nr, nr);
+                tile_park(tB, reg);
+                for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
+                    xs[idx] = ys[idx];
+                    ys[idx] = (T)0;
+                }
+                __syncthreads();
+                tile_gemv<T>(tB, 0, nr, nr, xs, ys, nk, (T)1);
+                for (int idx = threadIdx.x; idx < nr * nk; idx += blockDim.x) {
+                    const int r = idx % nr, k = idx / nr;
+                    Y[k1 + r0 + r + (int64_t)(k0 + k) * ldy] = ys[r * RCH + k];
+                }
+                __syncthreads();
+            } else {
+                // update-vector rows: ys += L(rows, 0:nscol) x1, x1 final
+                if (k0 == 0 && threadIdx.x == 0) {
+                    if (!wait_ge(S.xready + S.blkoff[s] + nblk - 1, 1, S.err)) abort_ = 1;
+                }
+                __syncthreads();
+                if (abort_) return;
+                for (int j = 0; j < nblk; j++) {
+                    const int nc = min(SR, nscol - j * SR);
+                    tile_park(tA, reg);
+                    for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
+                        const int c = idx / RCH, k = idx % RCH;
+                        xs[idx] = (c < nc && k < nk) ? Y[k1 + j * SR + c + (int64_t)(k0 + k) * ldy] : (T)0;
+                    }
+                    __syncthreads();
+                    if (j + 1 < nblk)
+                        tile_fetch(reg, panel + r0 + (int64_t)((j + 1) * SR) * nsrow, nsrow, nr,
+                                   min(SR, nscol - (j + 1) * SR));
+                    tile_gemv<T>(tA, 0, nr, nc, xs, ys, nk, (T)1);
+                }
+                for (int idx = threadIdx.x; idx < nr * nk; idx += blockDim.x) {
+                    const int r = idx % nr, k = idx / nr;
+                    us[(r0 - nscol) + r + (int64_t)(k0 + k) * m] = ys[r * RCH + k];
+                }
+                __syncthreads();
+            }
+        }
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (tk.kind == 0) st_release(S.xready + S.blkoff[s] + tk.idx, 1);
+            atomicAdd(S.done + s, 1);
+            if (S.trace) S.trace[3 * (size_t)t + 2] = gtimer();
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_bwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int nrhs,
+            T *Y, int64_t ldy)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *tA = (T *)smem_raw, *tB = tA + SR * TLD, *xs = tB + SR * TLD, *ys = xs + SR * RCH;
+    __shared__ int st, abort_;
+    T reg[16];
+    for (;;) {
+        if (threadIdx.x == 0) { st = atomicAdd(S.ticket, 1); abort_ = 0; }
+        __syncthreads();
+        const int t = st;
+        if (t >= S.ntasks) return;
+        const gb_stask tk = S.tasks[t];
+        if (S.trace && threadIdx.x == 0) S.trace[3 * (size_t)t] = gtimer();
+        const int s = tk.s;
+        const int64_t k1 = P.Super[s];
+        const int nscol = (int)(P.Super[s + 1] - k1);
+        const int64_t psi = P.Pi[s];
+        const int nsrow = (int)(P.Pi[s + 1] - psi);
+        const int m = nsrow - nscol;
+        const T *panel = Lx + P.Px[s];
+        const int32_t *rows = P.Ls + psi + nscol;
+        const int par = S.parent[s];
+        const int i = tk.idx, r0 = tk.r0, nr = tk.nr;
+        const int nblk = (nscol + SR - 1) / SR;
+        // first L21 tile: rows nscol.., columns of block i
+        if (m > 0) tile_fetch(reg, panel + nscol + (int64_t)r0 * nsrow, nsrow, min(SR, m), nr);
+        if (threadIdx.x == 0 && par >= 0) {
+            if (!wait_ge(S.done + par, S.ntask_s[par], S.err)) abort_ = 1;
+        }
+        __syncthreads();
+        if (abort_) return;
+        if (S.trace && threadIdx.x == 0) S.trace[3 * (size_t)t + 1] = gtimer();
+        for (int k0 = 0; k0 < nrhs; k0 += RCH) {
+            const int nk = min(RCH, nrhs - k0);
+            if (k0 > 0 && m > 0) tile_fetch(reg, panel + nscol + (int64_t)r0 * nsrow, nsrow, min(SR, m), nr);
+            for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
+                const int r = idx / RCH, k = idx % RCH;
+                ys[idx] = (r < nr && k < nk) ? Y[k1 + r0 + r + (int64_t)(k0 + k) * ldy] : (T)0;
+            }
+            // ys -= L21(:, blk i)' x(rows of s), 64 rows at a time
+            for (int q0 = 0; q0 < m; q0 += SR) {
+                const int nq = min(SR, m - q0);
+                tile_park(tA, reg);
+                for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
+                    const int c = idx / RCH, k = idx % RCH;
+                    xs[idx] = (c < nq && k < nk) ? Y[rows[q0 + c] + (int64_t)(k0 + k) * ldy] : (T)0;
+                }
+                __syncthreads();
+                if (q0 + SR < m)
+                    tile_fetch(reg, panel + nscol + q0 + SR + (int64_t)r0 * nsrow, nsrow,
+                               min(SR, m - q0 - SR), nr);
+                tile_gemv<T>(tA, 1, nr, nq, xs, ys, nk, (T)-1);
+            }
+            // later diagonal blocks of s: ys -= L(blk j, blk i)' x_j
+            if (nblk - 1 > i)
+                tile_fetch(reg, panel + (nblk - 1) * SR + (int64_t)r0 * nsrow, nsrow,
+                           min(SR, nscol - (nblk - 1) * SR), nr);
+            __syncthreads();
+            for (int j = nblk - 1; j > i; j--) {
+                const int nc = min(SR, nscol - j * SR);
+                if (k0 == 0 && threadIdx.x == 0) {
+                    if (!wait_ge(S.xready + S.blkoff[s] + j, 1, S.err)) abort_ = 1;
+                }
+                tile_park(tA, reg);
+                __syncthreads();
+                if (abort_) return;
+                for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
+                    const int c = idx / RCH, k = idx % RCH;
+                    xs[idx] = (c < nc && k < nk) ? Y[k1 + j * SR + c + (int64_t)(k0 + k) * ldy] : (T)0;
+                }
+                __syncthreads();
+                if (j - 1 > i)
+                    tile_fetch(reg, panel + (j - 1) * SR + (int64_t)r0 * nsrow, nsrow, SR, nr);
+                tile_gemv<T>(tA, 1, nr, nc, xs, ys, nk, (T)-1);
+            }
+            // x_i = Linv_ii' ys
+            tile_fetch(reg, Linv + S.linvoff[S.blkoff[s] + i], nr, nr, nr);
+            tile_park(tB, reg);
+            for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
+                xs[idx] = ys[idx];
+                ys[idx] = (T)0;
+            }
+            __syncthreads();
+            tile_gemv<T>(tB, 1, nr, nr, xs, ys, nk, (T)1);
+            for (int idx = threadIdx.x; idx < nr * nk; idx += blockDim.x) {
+                const int r = idx % nr, k = idx / nr;
+                Y[k1 + r0 + r + (int64_t)(k0 + k) * ldy] = ys[r * RCH + k];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            __threadfence();
+            st_release(S.xready + S.blkoff[s] + i, 1);
+            atomicAdd(S.done + s, 1);
+            if (S.trace) S.trace[3 * (size_t)t + 2] = gtimer();
+        }
+        __syncthreads();
+    }
+}
+
+// inverse of every diagonal block (lower triangular, nb <= 64), one block
+// each: thread j computes column j of X = L^-1 by forward substitution,
+// writing it straight to the output (its own earlier entries are re-read).
+template <typename T>
+__global__ void __launch_bounds__(SR)
+k_diag_inverse(gb_dev_pattern P, const gb_stask *__restrict__ dtasks, const int32_t *blkoff,
+               const int64_t *linvoff, const T *Lx, T *Linv)
+{
+    __shared__ T A[SR][SR + 1];
+    const gb_stask tk = dtasks[blockIdx.x];
+    const int s = tk.s;
+    const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
+    const int nb = tk.nr, r0 = tk.r0;
+    const T *blk = Lx + P.Px[s] + r0 + (int64_t)r0 * nsrow;
+    for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+        const int i = idx % nb, j = idx / nb;
+        A[i][j] = (i >= j) ? blk[i + (int64_t)j * nsrow] : (T)0;
+    }
+    __syncthreads();
+    T *out = Linv + linvoff[blkoff[s] + tk.idx];
+    const int j = threadIdx.x;
+    if (j < nb) {
+        T *x = out + (int64_t)j * nb;
+        for (int i = 0; i < j; i++) x[i] = (T)0;
+        x[j] = (T)1 / A[j][j];
+        for (int i = j + 1; i < nb; i++) {
+            T acc = (T)0;
+            for (int k = j; k < i; k++) acc += A[i][k] * x[k];
+            x[i] = -acc / A[i][i];
+        }
+    }
+}
+
+extern "C" {
+
+int gb_launch_sweep1(int forward, const gb_pattern_ptrs *pp, const gb_sweep1_args *a,
+                     const void *Lx, const void *Linv, int dtype, int nrhs, void *Y,
+                     int64_t ldy, void *U, int grid, cudaStream_t st)
+{
+    if (a->ntasks <= 0) return 0;
+    gb_dev_pattern P = gb_to_dev(pp);
+    gb_sweep_state S;
+    S.tasks = a->tasks; S.ntasks = a->ntasks; S.blkoff = a->blkoff; S.linvoff = a->linvoff;
+    S.ntask_s = a->ntask_s; S.parent = a->parent; S.xready = a->xready; S.done = a->done;
+    S.ticket = a->ticket; S.err = a->err; S.trace = a->trace;
+    if (grid > a->ntasks) grid = a->ntasks;
+    static int configured = 0;
+    if (!configured) {
+        cudaFuncSetAttribute(k_fwd_sweep<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double>());
+        cudaFuncSetAttribute(k_bwd_sweep<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double>());
+        cudaFuncSetAttribute(k_fwd_sweep<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<float>());
+        cudaFuncSetAttribute(k_bwd_sweep<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<float>());
+        configured = 1;
+    }
+    if (dtype == 0) {
+        const size_t sm = sweep_smem<double>();
+        if (forward) k_fwd_sweep<double><<<grid, 256, sm, st>>>(P, S, (const double *)Lx, (const double *)Linv, nrhs, (double *)Y, ldy, (double *)U);
+        else k_bwd_sweep<double><<<grid, 256, sm, st>>>(P, S, (const double *)Lx, (const double *)Linv, nrhs, (double *)Y, ldy);
+    } else {
+        const size_t sm = sweep_smem<float>();
+        if (forward) k_fwd_sweep<float><<<grid, 256, sm, st>>>(P, S, (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy, (float *)U);
+        else k_bwd_sweep<float><<<grid, 256, sm, st>>>(P, S, (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy);
+    }
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_diag_inverse(const gb_pattern_ptrs *pp, const gb_stask *dtasks, int ndiag,
+                           const int32_t *blkoff, const int64_t *linvoff, const void *Lx,
+                           void *Linv, int dtype, cudaStream_t st)
+{
+    if (ndiag <= 0) return 0;
+    gb_dev_pattern P = gb_to_dev(pp);
+    if (dtype == 0) k_diag_inverse<double><<<ndiag, SR, 0, st>>>(P, dtasks, blkoff, linvoff, (const double *)Lx, (double *)Linv);
+    else k_diag_inverse<float><<<ndiag, SR, 0, st>>>(P, dtasks, blkoff, linvoff, (const float *)Lx, (float *)Linv);
+    return (int)cudaGetLastError();
+}
+
+}  // extern "C"

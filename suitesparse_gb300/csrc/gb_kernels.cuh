@@ -38,9 +38,29 @@ typedef struct { int32_t s, pad; } gb_node_task;
 /* Blocked triangular solve step of a wide supernode: block [c0, c0+nb). */
 typedef struct { int32_t s, c0, nb, r0, nr, pad0, pad1, pad2; } gb_sweep_task;
 
+/* Task of the single-launch sweeps: kind 0 = diagonal block idx of s (rows
+ * r0..r0+nr of the supernode, r0 = 64*idx), kind 1 = off-diagonal rows
+ * [r0, r0+nr) (r0 >= nscol) producing the update vector. */
+typedef struct { int32_t s, kind, idx, r0, nr, pad0, pad1, pad2; } gb_stask;
+
+/* Task of the per-level device task graph of the wide supernodes (64-grid
+ * tiles of the panel of s; c0 = 64 b):
+ *   POTRF (s, b)       LL' + inverse of the diagonal block of column block b
+ *   TRSM  (s, b, r)    panel rows of row tile r below that block
+ *   UPD   (s, b, r, c) tile (r, c) of the panel -= L(r, blk b) L(c, blk b)'
+ *   CB    (s, r, c)    update-block tile (r, c) -= L21(r) L21(c)', k = nscol
+ * prio 0 = the tasks near the diagonal that the next steps wait on
+ * (POTRF; TRSM of row tiles <= b+3; UPD of tiles r <= b+3, c <= b+2),
+ * 1 = bulk. */
+typedef struct { int32_t type, s, b, r, c, prio, pad0, pad1; } gb_dtask;
+#define GB_DT_POTRF 1
+#define GB_DT_TRSM  2
+#define GB_DT_UPD   3
+#define GB_DT_CB    4
+
 #define GB_NB 64            /* block size of the blocked paths */
 #define GB_TILE 64          /* output tile edge of the update kernel */
-#define GB_TRSM_ROWS 128    /* rows per triangular-solve task */
+#define GB_TRSM_ROWS 64     /* rows per triangular-solve task */
 #define GB_SMALL_MAX 64     /* widest supernode factored by one block */
 
 #endif

@@ -110,10 +110,13 @@ static int factor_fp64(gb_plan *P, gb_ctx *ctx, int reason, cholmod_common *Comm
         return FALSE;
     }
     int32_t anyfail = 0;
+    int32_t dagerr = 0;
     int ok = gb_run_factor(P, ctx, P->d_Sx, CHOLMOD_DOUBLE, CHOLMOD_DOUBLE, NULL, 0.0)
              && cudaMemcpyAsync(&anyfail, P->d_anyfail, sizeof(int32_t), cudaMemcpyDeviceToHost,
                                 ctx->stream) == cudaSuccess
-             && cudaStreamSynchronize(ctx->stream) == cudaSuccess;
+             && cudaMemcpyAsync(&dagerr, P->d_ticket + 3, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                ctx->stream) == cudaSuccess
+             && cudaStreamSynchronize(ctx->stream) == cudaSuccess && !dagerr;
     if (!ok) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the FP64 factorization"); return FALSE; }
     P->mixed = 2;
     P->mixed_reason = reason;
@@ -157,9 +160,11 @@ int gb300_factorize_mixed(cholmod_sparse *A, cholmod_factor *L, cholmod_common *
          && gb_launch_diag_minmax((int)P->nsuper, P->d_Super, P->d_Pi, P->d_Px, P->d_Lx[1], 4,
                                   P->d_red, st) == 0;
     cudaEventRecord(ctx->ev1, st);
+    int32_t dagerr = 0;
     ok = ok && cudaMemcpyAsync(&anyfail, P->d_anyfail, sizeof(int32_t), cudaMemcpyDeviceToHost, st) == cudaSuccess
          && cudaMemcpyAsync(mm, P->d_red, 2 * sizeof(double), cudaMemcpyDeviceToHost, st) == cudaSuccess
-         && cudaStreamSynchronize(st) == cudaSuccess;
+         && cudaMemcpyAsync(&dagerr, P->d_ticket + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, st) == cudaSuccess
+         && cudaStreamSynchronize(st) == cudaSuccess && !dagerr;
     if (!ok) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the FP32 factorization"); return FALSE; }
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
@@ -216,6 +221,7 @@ cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod
          && cudaMemcpyAsync(P->d_R, P->d_bx, nb, cudaMemcpyDeviceToDevice, st) == cudaSuccess;
     cudaEventRecord(ctx->ev0, st);
     int it = 0, stall = 0;
+    int32_t serr = 0;
     double bmax_all = 0, berr_max = INFINITY;
     for (int r = 0; r < nrhs && best; r++) best[r] = INFINITY;
     while (ok && it < GB_MAX_REFINE) {
@@ -231,7 +237,8 @@ cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod
                                    P->d_R, n, st) == 0
              && gb_launch_colmax3(n, nrhs, P->d_R, n, P->d_X, n, P->d_bx, n, P->d_red, st) == 0
              && cudaMemcpyAsync(hred, P->d_red, sizeof(double) * 3 * nrhs, cudaMemcpyDeviceToHost, st) == cudaSuccess
-             && cudaStreamSynchronize(st) == cudaSuccess;
+             && cudaMemcpyAsync(&serr, P->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, st) == cudaSuccess
+             && cudaStreamSynchronize(st) == cudaSuccess && !(ctx->sweep_mode == 1 && serr);
         ctx->launches += 5;
         if (!ok) break;
         it++;

@@ -25,6 +25,7 @@ gb_ctx *gb_ctx_new(void)
     c->opt_keep = 0;
     c->opt_small = GB_SMALL_MAX;
     c->device = -1;
+    c->sweep_mode = 1;
     return c;
 }
 
@@ -35,6 +36,8 @@ void gb_ctx_delete(gb_ctx *c)
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (int i = 0; i < c->npev; i++) cudaEventDestroy(c->pev[i]);
+    if (c->d_trace) cudaFree(c->d_trace);
+    if (c->d_ftrace) cudaFree(c->d_ftrace);
     free(c->pev);
     free(c);
 }
@@ -43,6 +46,8 @@ int gb_ctx_ready(gb_ctx *c)
 {
     if (c->stream) return TRUE;
     if (cudaGetDevice(&c->device) != cudaSuccess) return FALSE;
+    if (cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess)
+        return FALSE;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return FALSE;
     if (cudaEventCreate(&c->ev0) != cudaSuccess) return FALSE;
     if (cudaEventCreate(&c->ev1) != cudaSuccess) return FALSE;
@@ -63,6 +68,8 @@ int gb300_set_option(cholmod_common *Common, int option, int64_t value)
     gb_ctx *c = gb_ctx_get(Common, 1);
     if (!c) { GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "out of memory"); return FALSE; }
     if (option == GB300_OPT_KEEP_ON_DEVICE) c->opt_keep = value ? 1 : 0;
+    else if (option == GB300_OPT_SWEEP) c->sweep_mode = value ? 1 : 0;
+    else if (option == GB300_OPT_TRACE) c->trace_on = value ? 1 : 0;
     else if (option == GB300_OPT_PROFILE) {
         c->prof = value ? 1 : 0;
         for (int k = 0; k < 16; k++) c->kind_ms[k] = c->kind_n[k] = 0;
@@ -90,6 +97,29 @@ int gb300_get_profile(cholmod_common *Common, double *ms, double *count, int nki
         if (count) count[k] = c->kind_n[k];
     }
     return TRUE;
+}
+
+int gb300_get_trace(cholmod_common *Common, int forward, unsigned long long *out, int64_t nmax)
+{
+    gb_ctx *c = gb_ctx_get(Common, 0);
+    if (!c || !c->d_trace || !out) return -1;
+    int64_t nt = c->trace_n[forward ? 0 : 1];
+    if (nt > nmax) nt = nmax;
+    if (cudaMemcpy(out, c->d_trace + c->trace_off[forward ? 0 : 1],
+                   3 * nt * sizeof(unsigned long long), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return -1;
+    return (int)nt;
+}
+
+int gb300_get_factor_trace(cholmod_common *Common, unsigned long long *out, int64_t nmax)
+{
+    gb_ctx *c = gb_ctx_get(Common, 0);
+    if (!c || !c->d_ftrace || !out) return -1;
+    int64_t nt = c->ftrace_n < nmax ? c->ftrace_n : nmax;
+    if (cudaMemcpy(out, c->d_ftrace, 3 * nt * sizeof(unsigned long long),
+                   cudaMemcpyDeviceToHost) != cudaSuccess)
+        return -1;
+    return (int)nt;
 }
 
 int gb300_fma_peak(int dtype, double *tflops)
@@ -241,6 +271,12 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
     void *Lx = P->d_Lx[d], *CB = P->d_CB[d];
     const gb_launch_rec *seq = P->fact_seq.p;
     int launches = 0;
+    if (!P->d_Linv[d] && cudaMalloc(&P->d_Linv[d], dt_size(l_dtype) * GB_MAX(P->linv_total, 1))
+                             != cudaSuccess) {
+        P->d_Linv[d] = NULL;
+        return FALSE;
+    }
+    void *Linv = P->d_Linv[d];
     int prof = ctx->prof;
     if (prof && ctx->npev < (int)(2 * P->fact_seq.n)) {
         int need = (int)(2 * P->fact_seq.n);
@@ -254,6 +290,7 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
     }
     CU(cudaMemsetAsync(P->d_fail, 0xFF, sizeof(int32_t) * (P->nsuper + 1), st));
     CU(cudaMemsetAsync(P->d_anyfail, 0, sizeof(int32_t), st));
+    CU(cudaMemsetAsync(P->d_ticket + 3, 0, sizeof(int32_t), st));
     for (size_t i = 0; i < P->fact_seq.n; i++) {
         const gb_launch_rec *r = &seq[i];
         if (prof) CU(cudaEventRecord(ctx->pev[2 * i], st));
@@ -263,18 +300,55 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
                                   Sx, adt, scale, beta, Lx, CB, ldt, st));
             break;
         case GB_K_SMALL:
-            LK(gb_launch_factor_small(&P->ptrs, P->d_node + r->off, r->count, Lx, ldt, st));
+            LK(gb_launch_factor_small(&P->ptrs, P->d_node + r->off, r->count, Lx, Linv, ldt, st));
             break;
         case GB_K_POTRF:
-            LK(gb_launch_potrf_diag(&P->ptrs, P->d_potrf + r->off, r->count, Lx, ldt, st));
+            LK(gb_launch_potrf_diag(&P->ptrs, P->d_potrf + r->off, r->count, Lx, Linv, ldt, st));
             break;
         case GB_K_TRSM:
-            LK(gb_launch_trsm_rows(&P->ptrs, P->d_trsm + r->off, r->count, Lx, ldt, st));
+            LK(gb_launch_trsm_rows(&P->ptrs, P->d_trsm + r->off, r->count, Lx, Linv, ldt, st));
             break;
         case GB_K_GEMM:
             LK(gb_launch_gemm(&P->ptrs, P->d_gemm + r->off, P->d_gemm_owner + r->off,
                               r->count, Lx, CB, ldt, st));
             break;
+        case GB_K_DAG: {
+            const gb_dag_level *lv = (const gb_dag_level *)P->dag_lv.p + r->off;
+            size_t nt = (size_t)lv->ntasks;
+            CU(cudaMemcpyAsync(P->d_dag_cnt, P->d_dag_nd + lv->task_off, sizeof(int32_t) * nt,
+                               cudaMemcpyDeviceToDevice, st));
+            CU(cudaMemsetAsync(P->d_dag_q, 0xFF, sizeof(int32_t) * 2 * nt, st));
+            if (lv->n0)
+                CU(cudaMemcpyAsync(P->d_dag_q, P->d_dag_q0i + lv->q0_off, sizeof(int32_t) * lv->n0,
+                                   cudaMemcpyDeviceToDevice, st));
+            if (lv->n1)
+                CU(cudaMemcpyAsync(P->d_dag_q + nt, P->d_dag_q1i + lv->q1_off,
+                                   sizeof(int32_t) * lv->n1, cudaMemcpyDeviceToDevice, st));
+            CU(cudaMemcpyAsync(P->d_dag_ctrl, P->d_dag_ctrl0 + 8 * r->off, sizeof(int32_t) * 8,
+                               cudaMemcpyDeviceToDevice, st));
+            gb_dag_args a;
+            a.tasks = P->d_dag_t + lv->task_off;
+            a.ntasks = (int)nt;
+            a.succ_ptr = P->d_dag_sp + lv->sp_off;
+            a.succ = P->d_dag_succ + lv->succ_off;
+            a.cnt = P->d_dag_cnt;
+            a.q0 = P->d_dag_q;
+            a.q1 = P->d_dag_q + nt;
+            a.ctrl = P->d_dag_ctrl;
+            a.err = P->d_ticket + 3;
+            a.trace = NULL;
+            if (ctx->trace_on) {
+                /* factorization trace: all levels' tasks, 3 words each */
+                size_t need = 3 * (P->dag_t.n + 1) * sizeof(unsigned long long);
+                if (gb_dev_grow((void **)&ctx->d_ftrace, &ctx->ftrace_cap, need)) {
+                    a.trace = ctx->d_ftrace + 3 * lv->task_off;
+                    ctx->ftrace_n = (int64_t)P->dag_t.n;
+                }
+            }
+            int grid = GB_MAX(1, ctx->sms) * (ldt == 4 ? 4 : 2);
+            LK(gb_launch_dag(&P->ptrs, &a, Lx, CB, Linv, ldt, grid, st));
+            break;
+        }
         }
         if (prof) CU(cudaEventRecord(ctx->pev[2 * i + 1], st));
         launches++;
@@ -291,9 +365,37 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
     }
     ctx->stats[4] = launches;
     ctx->launches += launches;
+    /* every diagonal block's inverse was formed with its factorization */
+    P->linv_valid[d] = 1;
     return TRUE;
 cuda_fail:
     return FALSE;
+}
+
+/* inverses of the diagonal blocks of the device factor (for the sweeps) */
+int gb_run_inverse(gb_plan *P, gb_ctx *ctx, int l_dtype)
+{
+    int d = dt_index(l_dtype);
+    if (!P->d_Linv[d] && cudaMalloc(&P->d_Linv[d], dt_size(l_dtype) * GB_MAX(P->linv_total, 1))
+                             != cudaSuccess) {
+        P->d_Linv[d] = NULL;
+        return FALSE;
+    }
+    if (gb_launch_diag_inverse(&P->ptrs, P->d_sd, (int)P->sd_t.n, P->d_blkoff, P->d_linvoff,
+                               P->d_Lx[d], P->d_Linv[d], l_dtype == CHOLMOD_SINGLE ? 4 : 0,
+                               ctx->stream) != 0)
+        return FALSE;
+    ctx->launches += 1;
+    P->linv_valid[d] = 1;
+    return TRUE;
+}
+
+/* error word of the single-launch sweeps (call after a synchronization) */
+static int sweep_failed(gb_plan *P)
+{
+    int32_t e = 0;
+    if (cudaMemcpy(&e, P->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) return TRUE;
+    return e != 0;
 }
 
 /* Replay one sweep on Y (device, n x nrhs, ld n) with the device factor. */
@@ -305,6 +407,40 @@ int gb_run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int fo
     size_t e = dt_size(l_dtype);
     if (!gb_dev_grow(&P->d_U, &P->u_cap, e * GB_MAX(P->cbv_total, 1) * nrhs)) return FALSE;
     const void *Lx = P->d_Lx[d];
+    if (ctx->sweep_mode == 1) {
+        if (!P->linv_valid[d] && !gb_run_inverse(P, ctx, l_dtype)) return FALSE;
+        gb_sweep1_args a;
+        a.tasks = forward ? P->d_sf : P->d_sb;
+        a.ntasks = (int)(forward ? P->sf_t.n : P->sb_t.n);
+        a.blkoff = P->d_blkoff;
+        a.linvoff = P->d_linvoff;
+        a.ntask_s = forward ? P->d_ntask_f : P->d_ntask_b;
+        a.parent = P->d_parent;
+        a.xready = P->d_xready;
+        a.done = P->d_done;
+        a.ticket = P->d_ticket;
+        a.err = P->d_err;
+        a.trace = NULL;
+        if (ctx->trace_on) {
+            size_t need = 3 * (size_t)(P->sf_t.n + P->sb_t.n + 2) * sizeof(unsigned long long);
+            if (gb_dev_grow((void **)&ctx->d_trace, &ctx->trace_cap, need)) {
+                int64_t off = forward ? 0 : 3 * (int64_t)(P->sf_t.n + 1);
+                a.trace = ctx->d_trace + off;
+                ctx->trace_off[forward ? 0 : 1] = off;
+                ctx->trace_n[forward ? 0 : 1] = a.ntasks;
+            }
+        }
+        if (cudaMemsetAsync(P->d_xready, 0, sizeof(int32_t) * (P->nblk_total + 1), st) != cudaSuccess
+            || cudaMemsetAsync(P->d_done, 0, sizeof(int32_t) * (P->nsuper + 1), st) != cudaSuccess
+            || cudaMemsetAsync(P->d_ticket, 0, sizeof(int32_t) * 4, st) != cudaSuccess)
+            return FALSE;
+        int grid = GB_MAX(1, ctx->sms) * 4;
+        if (gb_launch_sweep1(forward, &P->ptrs, &a, Lx, P->d_Linv[d], ldt, nrhs, Y, P->n,
+                             P->d_U, grid, st) != 0)
+            return FALSE;
+        ctx->launches += 1;
+        return TRUE;
+    }
     gb_vec *seqv = forward ? &P->fwd_seq : &P->bwd_seq;
     const gb_launch_rec *seq = seqv->p;
     for (size_t i = 0; i < seqv->n; i++) {
@@ -360,6 +496,7 @@ int gb_fix_not_posdef(gb_plan *P, gb_ctx *ctx, cholmod_factor *L, int l_dtype,
         return FALSE;
     }
     L->minor = (size_t)(Super[s0] + info - 1);
+    P->linv_valid[d] = 0;
     if (Common->status == CHOLMOD_OK) GB_ERROR(CHOLMOD_NOT_POSDEF, "matrix not positive definite");
     return TRUE;
 }
@@ -481,9 +618,10 @@ int cholmod_l_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2]
     cudaEventRecord(ctx->ev0, ctx->stream);
     ok = gb_run_factor(P, ctx, P->d_Sx, dtype, dtype, NULL, beta ? beta[0] : 0.0);
     cudaEventRecord(ctx->ev1, ctx->stream);
-    int32_t anyfail = 0;
+    int32_t anyfail = 0, dagerr = 0;
     if (ok) ok = cudaMemcpyAsync(&anyfail, P->d_anyfail, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess
-                 && cudaStreamSynchronize(ctx->stream) == cudaSuccess;
+                 && cudaMemcpyAsync(&dagerr, P->d_ticket + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess
+                 && cudaStreamSynchronize(ctx->stream) == cudaSuccess && !dagerr;
     if (!ok) {
         if (Apk != A) gb300_free_sparse(&Apk, Common);
         GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the factorization");
@@ -533,6 +671,7 @@ static gb_plan *factor_on_device(cholmod_factor *L, gb_ctx *ctx, cholmod_common 
     }
     P->dev_valid[d] = 1;
     P->host_x[d] = L->x;
+    P->linv_valid[d] = 0;
     return P;
 }
 
@@ -575,6 +714,7 @@ static int super_solve(cholmod_factor *L, cholmod_dense *X, cholmod_dense *E,
     ok = ok && cudaMemcpy2DAsync(X->x, e * X->d, P->d_Y, e * n, e * n, nrhs,
                                  cudaMemcpyDeviceToHost, st) == cudaSuccess;
     ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
+    ok = ok && !(ctx->sweep_mode == 1 && sweep_failed(P));
     if (!ok) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the solve"); return FALSE; }
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
@@ -648,6 +788,7 @@ cholmod_dense *gb300_solve(int sys, cholmod_factor *L, cholmod_dense *B,
     cudaEventRecord(ctx->ev1, st);
     ok = ok && cudaMemcpyAsync(X->x, P->d_B, e * n * nrhs, cudaMemcpyDeviceToHost, st) == cudaSuccess;
     ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
+    ok = ok && !(ctx->sweep_mode == 1 && sweep_failed(P));
     if (!ok) {
         gb300_free_dense(&X, Common);
         GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the solve");
@@ -657,4 +798,31 @@ cholmod_dense *gb300_solve(int sys, cholmod_factor *L, cholmod_dense *B,
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     ctx->stats[1] = ms;
     return X;
+}
+
+/* The factorization task graph of L's plan, 8 int32 per task (type, s, b,
+ * r, c, priority, level, 0), for inspecting a factorization trace.  Returns
+ * the number of tasks. */
+int gb300_plan_tasks(cholmod_factor *L, cholmod_common *Common, int32_t *out, int64_t nmax)
+{
+    if (!Common || !L) return -1;
+    gb_ctx *ctx = gb_ctx_get(Common, 1);
+    if (!ctx || !gb_ctx_ready(ctx)) return -1;
+    gb_plan *P = gb_plan_get(L, Common, ctx, 1);
+    if (!P) return -1;
+    const gb_dtask *t = P->dag_t.p;
+    const gb_dag_level *lv = P->dag_lv.p;
+    int64_t n = (int64_t)P->dag_t.n;
+    if (out) {
+        for (size_t l = 0; l < P->dag_lv.n; l++) {
+            for (int32_t q = 0; q < lv[l].ntasks; q++) {
+                int64_t i = lv[l].task_off + q;
+                if (i >= nmax) break;
+                out[8 * i + 0] = t[i].type; out[8 * i + 1] = t[i].s; out[8 * i + 2] = t[i].b;
+                out[8 * i + 3] = t[i].r; out[8 * i + 4] = t[i].c; out[8 * i + 5] = t[i].prio;
+                out[8 * i + 6] = (int32_t)l; out[8 * i + 7] = 0;
+            }
+        }
+    }
+    return (int)n;
 }

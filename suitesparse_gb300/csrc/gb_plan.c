@@ -111,7 +111,17 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
     vec_init(&P->gemm_t, sizeof(gb_gemm_task));
     vec_init(&P->gemm_owner, sizeof(int32_t));
     vec_init(&P->sweep_t, sizeof(gb_sweep_task));
+    vec_init(&P->sf_t, sizeof(gb_stask));
+    vec_init(&P->sb_t, sizeof(gb_stask));
+    vec_init(&P->sd_t, sizeof(gb_stask));
     vec_init(&P->fact_seq, sizeof(gb_launch_rec));
+    vec_init(&P->dag_t, sizeof(gb_dtask));
+    vec_init(&P->dag_sp, sizeof(int32_t));
+    vec_init(&P->dag_succ, sizeof(int32_t));
+    vec_init(&P->dag_nd, sizeof(int32_t));
+    vec_init(&P->dag_q0, sizeof(int32_t));
+    vec_init(&P->dag_q1, sizeof(int32_t));
+    vec_init(&P->dag_lv, sizeof(gb_dag_level));
     vec_init(&P->fwd_seq, sizeof(gb_launch_rec));
     vec_init(&P->bwd_seq, sizeof(gb_launch_rec));
 
@@ -195,11 +205,12 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
     P->cb_total = cbt;
     P->cbv_total = cbvt;
 
-    /* ---- factorization sequence ---- */
-    const int T = GB_TILE, NB = GB_NB;
+    /* ---- factorization sequence: per level ASM, SMALL, DAG ---- */
+    const int NB = GB_NB;
+    gb_vec edges;
+    vec_init(&edges, 2 * sizeof(int32_t));
     for (int l = 0; l < nlevels && ok; l++) {
         size_t a0 = P->asm_t.n;
-        int maxsteps = 0;
         for (Int q = lev_ptr[l]; q < lev_ptr[l + 1]; q++) {
             Int s = lev_list[q];
             Int nsrow = Pi[s + 1] - Pi[s];
@@ -208,8 +219,6 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
                 gb_asm_task a = {(int32_t)s, (int32_t)t0, (int32_t)GB_MIN(t0 + 64, nsrow), 0};
                 ok &= gb_vec_push(&P->asm_t, &a);
             }
-            Int nscol = Super[s + 1] - Super[s];
-            if (nscol > small_cols) maxsteps = (int)GB_MAX(maxsteps, (nscol + NB - 1) / NB);
         }
         ok &= push_launch(&P->fact_seq, GB_K_ASM, P->asm_t.n - a0, a0);
         size_t n0 = P->node_t.n;
@@ -221,89 +230,153 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
             }
         }
         ok &= push_launch(&P->fact_seq, GB_K_SMALL, P->node_t.n - n0, n0);
-        for (int b = 0; b < maxsteps && ok; b++) {
-            size_t p0 = P->potrf_t.n, r0 = P->trsm_t.n, g0 = P->gemm_t.n;
-            for (Int q = lev_ptr[l]; q < lev_ptr[l + 1]; q++) {
-                Int s = lev_list[q];
-                Int nscol = Super[s + 1] - Super[s], nsrow = Pi[s + 1] - Pi[s];
-                if (nscol <= small_cols) continue;
-                Int c0 = (Int)b * NB;
-                if (c0 >= nscol) continue;
-                Int nb = GB_MIN(NB, nscol - c0);
-                gb_potrf_task pt = {(int32_t)s, (int32_t)c0, (int32_t)nb, 0};
-                ok &= gb_vec_push(&P->potrf_t, &pt);
-                for (Int r = c0 + nb; r < nsrow; r += GB_TRSM_ROWS) {
-                    gb_trsm_task tt = {(int32_t)s, (int32_t)c0, (int32_t)nb, (int32_t)r,
-                                       (int32_t)GB_MIN(GB_TRSM_ROWS, nsrow - r), 0, 0, 0};
-                    ok &= gb_vec_push(&P->trsm_t, &tt);
-                }
-            }
-            ok &= push_launch(&P->fact_seq, GB_K_POTRF, P->potrf_t.n - p0, p0);
-            ok &= push_launch(&P->fact_seq, GB_K_TRSM, P->trsm_t.n - r0, r0);
-            for (Int q = lev_ptr[l]; q < lev_ptr[l + 1]; q++) {
-                Int s = lev_list[q];
-                Int nscol = Super[s + 1] - Super[s], nsrow = Pi[s + 1] - Pi[s];
-                if (nscol <= small_cols) continue;
-                Int c0 = (Int)b * NB;
-                if (c0 >= nscol) continue;
-                Int nb = GB_MIN(NB, nscol - c0);
-                Int t0 = c0 + nb;   /* trailing columns [t0, nscol), rows [t0, nsrow) */
-                for (Int cs = t0; cs < nscol; cs += T) {
-                    Int nc = GB_MIN(T, nscol - cs);
-                    for (Int rs = cs; rs < nsrow; rs += T) {
-                        /* rows of this tile that can be >= its columns */
-                        Int nr = GB_MIN(T, nsrow - rs);
-                        gb_gemm_task g;
-                        memset(&g, 0, sizeof g);
-                        g.a = Px[s] + rs + c0 * nsrow;
-                        g.b = Px[s] + cs + c0 * nsrow;
-                        g.c = Px[s] + rs + cs * nsrow;
-                        g.lda = g.ldb = g.ldc = (int32_t)nsrow;
-                        g.m = (int32_t)nr;
-                        g.n = (int32_t)nc;
-                        g.k = (int32_t)nb;
-                        if (rs < cs + nc - 1) {        /* crosses the diagonal */
-                            g.flags = GB_GEMM_LOWER;
-                            g.diag_off = (int32_t)(cs - rs);
-                        }
-                        int32_t own = (int32_t)s;
-                        ok &= gb_vec_push(&P->gemm_t, &g);
-                        ok &= gb_vec_push(&P->gemm_owner, &own);
-                        P->fl_gemm += gemm_flops(&g);
-                    }
-                }
-            }
-            ok &= push_launch(&P->fact_seq, GB_K_GEMM, P->gemm_t.n - g0, g0);
-        }
-        /* update blocks of the level */
-        size_t g0 = P->gemm_t.n;
-        for (Int q = lev_ptr[l]; q < lev_ptr[l + 1]; q++) {
+
+        /* task graph of the level: tiles of the wide panels + update blocks */
+        int32_t base = 0;
+        size_t t0g = P->dag_t.n;
+        edges.n = 0;
+        for (Int q = lev_ptr[l]; q < lev_ptr[l + 1] && ok; q++) {
             Int s = lev_list[q];
             Int nscol = Super[s + 1] - Super[s], nsrow = Pi[s + 1] - Pi[s];
             Int m = nsrow - nscol;
-            for (Int J = 0; J < m; J += T) {
-                for (Int I = J; I < m; I += T) {
-                    gb_gemm_task g;
-                    memset(&g, 0, sizeof g);
-                    g.a = Px[s] + nscol + I;
-                    g.b = Px[s] + nscol + J;
-                    g.c = cboff[s] + I + J * m;
-                    g.lda = g.ldb = (int32_t)nsrow;
-                    g.ldc = (int32_t)m;
-                    g.m = (int32_t)GB_MIN(T, m - I);
-                    g.n = (int32_t)GB_MIN(T, m - J);
-                    g.k = (int32_t)nscol;
-                    g.flags = GB_GEMM_C_IN_CB | (I == J ? GB_GEMM_LOWER : 0);
-                    g.diag_off = 0;
-                    int32_t own = (int32_t)s;
-                    ok &= gb_vec_push(&P->gemm_t, &g);
-                    ok &= gb_vec_push(&P->gemm_owner, &own);
-                    P->fl_gemm += gemm_flops(&g);
+            Int Cp = (nscol + NB - 1) / NB, R = (nsrow + NB - 1) / NB;
+            int32_t *Pid = NULL, *Tid = NULL, *Uid = NULL;
+            if (nscol > small_cols) {
+                Pid = malloc(sizeof(int32_t) * Cp);
+                Tid = malloc(sizeof(int32_t) * Cp * R);
+                Uid = malloc(sizeof(int32_t) * Cp * R * Cp);
+                if (!Pid || !Tid || !Uid) { free(Pid); free(Tid); free(Uid); ok = 0; break; }
+                for (Int b = 0; b < Cp; b++) {
+                    Int c0 = b * NB, nb = GB_MIN(NB, nscol - c0);
+                    gb_dtask pt = {GB_DT_POTRF, (int32_t)s, (int32_t)b, 0, 0, 0, 0, 0};
+                    Pid[b] = base + (int32_t)(P->dag_t.n - t0g);
+                    ok &= gb_vec_push(&P->dag_t, &pt);
+                    for (Int r = 0; r < R; r++) {
+                        Tid[b * R + r] = -1;
+                        if (r < b) continue;
+                        Int r0 = GB_MAX(NB * r, c0 + nb), r1 = GB_MIN(NB * r + NB, nsrow);
+                        if (r1 <= r0) continue;
+                        gb_dtask tt = {GB_DT_TRSM, (int32_t)s, (int32_t)b, (int32_t)r, 0,
+                                       r <= b + 3 ? 0 : 1, 0, 0};
+                        Tid[b * R + r] = base + (int32_t)(P->dag_t.n - t0g);
+                        ok &= gb_vec_push(&P->dag_t, &tt);
+                    }
+                    for (Int cc = 0; cc < Cp; cc++) {
+                        for (Int r = 0; r < R; r++) {
+                            Uid[(b * R + r) * Cp + cc] = -1;
+                            if (cc <= b || r < cc) continue;
+                            gb_dtask ut = {GB_DT_UPD, (int32_t)s, (int32_t)b, (int32_t)r, (int32_t)cc,
+                                           (cc <= b + 2 && r <= b + 3) ? 0 : 1, 0, 0};
+                            Uid[(b * R + r) * Cp + cc] = base + (int32_t)(P->dag_t.n - t0g);
+                            ok &= gb_vec_push(&P->dag_t, &ut);
+                        }
+                    }
+                }
+                /* edges of the blocked right-looking factorization */
+                for (Int b = 0; b < Cp && ok; b++) {
+                    int32_t e[2];
+                    if (b > 0) {
+                        e[0] = Uid[((b - 1) * R + b) * Cp + b]; e[1] = Pid[b];
+                        ok &= gb_vec_push(&edges, e);
+                    }
+                    for (Int r = b; r < R; r++) {
+                        int32_t t = Tid[b * R + r];
+                        if (t < 0) continue;
+                        e[0] = Pid[b]; e[1] = t;
+                        ok &= gb_vec_push(&edges, e);
+                        if (b > 0) {
+                            e[0] = Uid[((b - 1) * R + r) * Cp + b]; e[1] = t;
+                            ok &= gb_vec_push(&edges, e);
+                        }
+                    }
+                    for (Int cc = b + 1; cc < Cp; cc++) {
+                        for (Int r = cc; r < R; r++) {
+                            int32_t u = Uid[(b * R + r) * Cp + cc];
+                            e[1] = u;
+                            e[0] = Tid[b * R + r]; ok &= gb_vec_push(&edges, e);
+                            if (r != cc) { e[0] = Tid[b * R + cc]; ok &= gb_vec_push(&edges, e); }
+                            if (b > 0) {
+                                e[0] = Uid[((b - 1) * R + r) * Cp + cc];
+                                ok &= gb_vec_push(&edges, e);
+                            }
+                        }
+                    }
                 }
             }
+            /* update-block tiles (k = nscol) */
+            for (Int J = 0; J < m && ok; J += NB) {
+                for (Int I = J; I < m; I += NB) {
+                    gb_dtask ct = {GB_DT_CB, (int32_t)s, 0, (int32_t)(I / NB), (int32_t)(J / NB), 1, 0, 0};
+                    int32_t cid = base + (int32_t)(P->dag_t.n - t0g);
+                    ok &= gb_vec_push(&P->dag_t, &ct);
+                    if (Pid) {
+                        /* rows of L21 tiles I and J final: last panel solves */
+                        Int lastb = Cp - 1;
+                        Int rows[2] = {nscol + I, nscol + J};
+                        int32_t prev = -1;
+                        for (int w = 0; w < 2; w++) {
+                            Int rlo = rows[w] / NB, rhi = GB_MIN(rows[w] + NB, nsrow) - 1;
+                            rhi /= NB;
+                            for (Int r = rlo; r <= rhi; r++) {
+                                int32_t t = Tid[lastb * R + r];
+                                if (t < 0 || t == prev) continue;
+                                int32_t e[2] = {t, cid};
+                                ok &= gb_vec_push(&edges, e);
+                                prev = t;
+                            }
+                        }
+                    }
+                }
+            }
+            free(Pid); free(Tid); free(Uid);
         }
-        ok &= push_launch(&P->fact_seq, GB_K_GEMM, P->gemm_t.n - g0, g0);
+        if (!ok) break;
+        /* CSR of successors, dependency counts, initial ready lists */
+        int32_t ntl = (int32_t)(P->dag_t.n - t0g);
+        gb_dag_level lv;
+        memset(&lv, 0, sizeof lv);
+        lv.task_off = (int64_t)t0g;
+        lv.ntasks = ntl;
+        lv.sp_off = (int64_t)P->dag_sp.n;
+        lv.succ_off = (int64_t)P->dag_succ.n;
+        lv.q0_off = (int64_t)P->dag_q0.n;
+        lv.q1_off = (int64_t)P->dag_q1.n;
+        if (ntl > 0) {
+            int32_t *deg = calloc(ntl + 1, sizeof(int32_t));
+            int32_t *nd = calloc(ntl + 1, sizeof(int32_t));
+            int32_t *pos = malloc(sizeof(int32_t) * (ntl + 1));
+            int32_t *succ = malloc(sizeof(int32_t) * (edges.n + 1));
+            if (!deg || !nd || !pos || !succ) ok = 0;
+            const int32_t *E = edges.p;
+            for (size_t q2 = 0; ok && q2 < edges.n; q2++) { deg[E[2 * q2] + 1]++; nd[E[2 * q2 + 1]]++; }
+            for (int32_t t = 0; ok && t < ntl; t++) deg[t + 1] += deg[t];
+            if (ok) memcpy(pos, deg, sizeof(int32_t) * (ntl + 1));
+            for (size_t q2 = 0; ok && q2 < edges.n; q2++) succ[pos[E[2 * q2]]++] = E[2 * q2 + 1];
+            for (int32_t t = 0; ok && t <= ntl; t++) ok &= gb_vec_push(&P->dag_sp, &deg[t]);
+            for (size_t q2 = 0; ok && q2 < edges.n; q2++) ok &= gb_vec_push(&P->dag_succ, &succ[q2]);
+            const gb_dtask *dt = (const gb_dtask *)P->dag_t.p + t0g;
+            for (int32_t t = 0; ok && t < ntl; t++) {
+                if (dt[t].prio == 0) lv.total0++; else lv.total1++;
+                ok &= gb_vec_push(&P->dag_nd, &nd[t]);
+                if (nd[t] == 0) {
+                    if (dt[t].prio == 0) { ok &= gb_vec_push(&P->dag_q0, &t); lv.n0++; }
+                    else { ok &= gb_vec_push(&P->dag_q1, &t); lv.n1++; }
+                }
+            }
+            free(deg); free(nd); free(pos); free(succ);
+            P->dag_max = GB_MAX(P->dag_max, ntl);
+        }
+        int32_t li = (int32_t)P->dag_lv.n;
+        ok &= gb_vec_push(&P->dag_lv, &lv);
+        if (ntl > 0) {
+            gb_launch_rec r;
+            r.kind = GB_K_DAG;
+            r.count = ntl;
+            r.off = li;
+            ok &= gb_vec_push(&P->fact_seq, &r);
+        }
     }
+    gb_vec_free(&edges);
 
     /* ---- forward sweep sequence ---- */
     for (int l = 0; l < nlevels && ok; l++) {
@@ -416,6 +489,70 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
             ok &= push_launch(&P->bwd_seq, GB_K_BWD_PANEL, P->sweep_t.n - d0, d0);
         }
     }
+    /* ---- single-launch sweep tasks (postorder = topological order) ---- */
+    P->h_blkoff = malloc(sizeof(int32_t) * (nsuper + 1));
+    P->h_ntask_f = malloc(sizeof(int32_t) * (nsuper + 1));
+    P->h_ntask_b = malloc(sizeof(int32_t) * (nsuper + 1));
+    P->h_parent = malloc(sizeof(int32_t) * (nsuper + 1));
+    if (!P->h_blkoff || !P->h_ntask_f || !P->h_ntask_b || !P->h_parent) ok = 0;
+    int64_t nblk_total = 0;
+    for (Int s = 0; s < nsuper && ok; s++) {
+        Int nscol = Super[s + 1] - Super[s], nsrow = Pi[s + 1] - Pi[s];
+        Int nblk = (nscol + 63) / 64, m = nsrow - nscol;
+        P->h_blkoff[s] = (int32_t)nblk_total;
+        P->h_parent[s] = (int32_t)parent[s];
+        nblk_total += nblk;
+        P->h_ntask_b[s] = (int32_t)nblk;
+        P->h_ntask_f[s] = (int32_t)(nblk + (m + 63) / 64);
+        for (Int i = 0; i < nblk; i++) {     /* diagonal blocks in global block order */
+            gb_stask t = {(int32_t)s, 0, (int32_t)i, (int32_t)(i * 64),
+                          (int32_t)GB_MIN(64, nscol - i * 64), 0, 0, 0};
+            ok &= gb_vec_push(&P->sd_t, &t);
+        }
+    }
+    /* forward: levels ascending; backward: levels descending, so that a task
+     * only depends on tasks listed before it and branches interleave */
+    for (int l = 0; l < nlevels && ok; l++) {
+        for (Int q = lev_ptr[l]; q < lev_ptr[l + 1]; q++) {
+            Int s = lev_list[q];
+            Int nscol = Super[s + 1] - Super[s], nsrow = Pi[s + 1] - Pi[s];
+            Int nblk = (nscol + 63) / 64;
+            for (Int i = 0; i < nblk; i++) {
+                gb_stask t = {(int32_t)s, 0, (int32_t)i, (int32_t)(i * 64),
+                              (int32_t)GB_MIN(64, nscol - i * 64), 0, 0, 0};
+                ok &= gb_vec_push(&P->sf_t, &t);
+            }
+            for (Int r = nscol; r < nsrow; r += 64) {
+                gb_stask t = {(int32_t)s, 1, 0, (int32_t)r, (int32_t)GB_MIN(64, nsrow - r), 0, 0, 0};
+                ok &= gb_vec_push(&P->sf_t, &t);
+            }
+        }
+    }
+    for (int l = nlevels - 1; l >= 0 && ok; l--) {
+        for (Int q = lev_ptr[l + 1] - 1; q >= lev_ptr[l]; q--) {
+            Int s = lev_list[q];
+            Int nscol = Super[s + 1] - Super[s];
+            Int nblk = (nscol + 63) / 64;
+            for (Int i = nblk - 1; i >= 0; i--) {
+                gb_stask t = {(int32_t)s, 0, (int32_t)i, (int32_t)(i * 64),
+                              (int32_t)GB_MIN(64, nscol - i * 64), 0, 0, 0};
+                ok &= gb_vec_push(&P->sb_t, &t);
+            }
+        }
+    }
+    P->nblk_total = nblk_total;
+    P->h_linvoff = malloc(sizeof(int64_t) * (nblk_total + 1));
+    if (!P->h_linvoff) ok = 0;
+    if (ok) {
+        int64_t off = 0;
+        const gb_stask *sd = P->sd_t.p;
+        for (size_t q = 0; q < P->sd_t.n; q++) {
+            P->h_linvoff[q] = off;               /* sd_t is in global block order */
+            off += (int64_t)sd[q].nr * sd[q].nr;
+        }
+        P->h_linvoff[nblk_total] = off;
+        P->linv_total = off;
+    }
     if (!ok) goto fail;
 
     P->h_child_ptr = child_ptr;
@@ -474,6 +611,46 @@ int gb_plan_upload(gb_plan *P)
     UP(P->d_gemm, P->gemm_t.p, P->gemm_t.n * P->gemm_t.esz);
     UP(P->d_gemm_owner, P->gemm_owner.p, P->gemm_owner.n * P->gemm_owner.esz);
     UP(P->d_sweep, P->sweep_t.p, P->sweep_t.n * P->sweep_t.esz);
+    UP(P->d_dag_t, P->dag_t.p, P->dag_t.n * P->dag_t.esz);
+    UP(P->d_dag_sp, P->dag_sp.p, P->dag_sp.n * P->dag_sp.esz);
+    UP(P->d_dag_succ, P->dag_succ.p, P->dag_succ.n * P->dag_succ.esz);
+    UP(P->d_dag_nd, P->dag_nd.p, P->dag_nd.n * P->dag_nd.esz);
+    UP(P->d_dag_q0i, P->dag_q0.p, P->dag_q0.n * P->dag_q0.esz);
+    UP(P->d_dag_q1i, P->dag_q1.p, P->dag_q1.n * P->dag_q1.esz);
+    {
+        size_t nl = P->dag_lv.n;
+        int32_t *ctrl0 = calloc(8 * (nl + 1), sizeof(int32_t));
+        if (!ctrl0) goto fail;
+        const gb_dag_level *lv = P->dag_lv.p;
+        for (size_t i = 0; i < nl; i++) {
+            ctrl0[8 * i + 1] = lv[i].n0;
+            ctrl0[8 * i + 3] = lv[i].n1;
+            ctrl0[8 * i + 6] = lv[i].total0;
+            ctrl0[8 * i + 7] = lv[i].total1;
+        }
+        int okc = cudaMalloc((void **)&P->d_dag_ctrl0, sizeof(int32_t) * 8 * (nl + 1)) == cudaSuccess
+                  && cudaMemcpy(P->d_dag_ctrl0, ctrl0, sizeof(int32_t) * 8 * (nl + 1), cudaMemcpyHostToDevice) == cudaSuccess;
+        free(ctrl0);
+        if (!okc) goto fail;
+    }
+    {
+        size_t mx = (size_t)GB_MAX(P->dag_max, 1);
+        if (cudaMalloc((void **)&P->d_dag_cnt, sizeof(int32_t) * mx) != cudaSuccess) goto fail;
+        if (cudaMalloc((void **)&P->d_dag_q, sizeof(int32_t) * 2 * mx) != cudaSuccess) goto fail;
+        if (cudaMalloc((void **)&P->d_dag_ctrl, sizeof(int32_t) * 8) != cudaSuccess) goto fail;
+    }
+    UP(P->d_sf, P->sf_t.p, P->sf_t.n * P->sf_t.esz);
+    UP(P->d_sb, P->sb_t.p, P->sb_t.n * P->sb_t.esz);
+    UP(P->d_sd, P->sd_t.p, P->sd_t.n * P->sd_t.esz);
+    UP(P->d_blkoff, P->h_blkoff, sizeof(int32_t) * (ns + 1));
+    UP(P->d_ntask_f, P->h_ntask_f, sizeof(int32_t) * (ns + 1));
+    UP(P->d_ntask_b, P->h_ntask_b, sizeof(int32_t) * (ns + 1));
+    UP(P->d_parent, P->h_parent, sizeof(int32_t) * (ns + 1));
+    UP(P->d_linvoff, P->h_linvoff, sizeof(int64_t) * (P->nblk_total + 1));
+    if (cudaMalloc((void **)&P->d_xready, sizeof(int32_t) * (P->nblk_total + 1)) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&P->d_done, sizeof(int32_t) * (ns + 1)) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&P->d_ticket, sizeof(int32_t) * 4) != cudaSuccess) goto fail;
+    P->d_err = P->d_ticket + 2;
     P->ptrs.Super = P->d_Super;
     P->ptrs.Pi = P->d_Pi;
     P->ptrs.Px = P->d_Px;
@@ -485,6 +662,8 @@ int gb_plan_upload(gb_plan *P)
     P->ptrs.child_list = P->d_child_list;
     P->ptrs.fail = P->d_fail;
     P->ptrs.anyfail = P->d_anyfail;
+    P->ptrs.blkoff = P->d_blkoff;
+    P->ptrs.linvoff = P->d_linvoff;
     ok = TRUE;
 fail:
     free(Ls32);
@@ -496,13 +675,23 @@ void gb_plan_free(gb_plan *P)
     if (!P) return;
     free(P->h_child_ptr); free(P->h_child_list); free(P->h_relmap);
     free(P->h_cboff); free(P->h_cbvoff);
+    free(P->h_blkoff); free(P->h_ntask_f); free(P->h_ntask_b); free(P->h_parent);
+    free(P->h_linvoff);
+    gb_vec_free(&P->sf_t); gb_vec_free(&P->sb_t); gb_vec_free(&P->sd_t);
+    gb_vec_free(&P->dag_t); gb_vec_free(&P->dag_sp); gb_vec_free(&P->dag_succ);
+    gb_vec_free(&P->dag_nd); gb_vec_free(&P->dag_q0); gb_vec_free(&P->dag_q1);
+    gb_vec_free(&P->dag_lv);
     void *dev[] = {P->d_Super, P->d_Pi, P->d_Px, P->d_cboff, P->d_cbvoff, P->d_Perm,
                    P->d_Ls, P->d_relmap, P->d_child_ptr, P->d_child_list, P->d_fail,
                    P->d_anyfail, P->d_asm, P->d_node, P->d_potrf, P->d_trsm, P->d_gemm,
                    P->d_gemm_owner, P->d_sweep, P->d_Lx[0], P->d_Lx[1], P->d_CB[0],
                    P->d_CB[1], P->d_Sp, P->d_Si, P->d_Sx, P->d_Y, P->d_U, P->d_B,
                    P->d_Rp, P->d_Rj, P->d_Rx, P->d_scale, P->d_scale_perm, P->d_X, P->d_R,
-                   P->d_bx, P->d_red};
+                   P->d_bx, P->d_red, P->d_sf, P->d_sb, P->d_sd, P->d_blkoff, P->d_ntask_f,
+                   P->d_ntask_b, P->d_parent, P->d_linvoff, P->d_xready, P->d_done,
+                   P->d_ticket, P->d_Linv[0], P->d_Linv[1], P->d_dag_t, P->d_dag_sp,
+                   P->d_dag_succ, P->d_dag_nd, P->d_dag_q0i, P->d_dag_q1i, P->d_dag_ctrl0,
+                   P->d_dag_cnt, P->d_dag_q, P->d_dag_ctrl};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++)
         if (dev[i]) cudaFree(dev[i]);
     gb_vec_free(&P->asm_t); gb_vec_free(&P->node_t); gb_vec_free(&P->potrf_t);

@@ -21,15 +21,45 @@ typedef struct {
     const int64_t *Super, *Pi, *Px, *cboff, *cbvoff;
     const int32_t *Ls, *relmap, *child_ptr, *child_list;
     int32_t *fail, *anyfail;
+    const int32_t *blkoff;
+    const int64_t *linvoff;
 } gb_pattern_ptrs;
 
 enum {
-    GB_K_ASM = 1, GB_K_SMALL, GB_K_POTRF, GB_K_TRSM, GB_K_GEMM,
+    GB_K_ASM = 1, GB_K_SMALL, GB_K_POTRF, GB_K_TRSM, GB_K_GEMM, GB_K_DAG,
     GB_K_FWD_SMALL, GB_K_FWD_GATHER, GB_K_FWD_DIAG, GB_K_FWD_PANEL,
     GB_K_BWD_SMALL, GB_K_BWD_OFFDIAG, GB_K_BWD_DIAG, GB_K_BWD_PANEL
 };
 
 typedef struct { int32_t kind, count; int64_t off; } gb_launch_rec;
+
+/* one level's task graph inside the plan's concatenated arrays */
+typedef struct {
+    int64_t task_off, sp_off, succ_off, q0_off, q1_off;
+    int32_t ntasks, n0, n1, total0, total1, pad;
+} gb_dag_level;
+
+/* arguments of the task-graph executor (device pointers of one level) */
+typedef struct {
+    const gb_dtask *tasks;
+    int ntasks;
+    const int32_t *succ_ptr, *succ;
+    int32_t *cnt, *q0, *q1, *ctrl;
+    int32_t *err;            /* persistent error word of the factorization */
+    unsigned long long *trace;
+} gb_dag_args;
+
+/* arguments of the single-launch sweeps (device pointers) */
+typedef struct {
+    const gb_stask *tasks;
+    int ntasks;
+    const int32_t *blkoff;
+    const int64_t *linvoff;
+    const int32_t *ntask_s;
+    const int32_t *parent;
+    int32_t *xready, *done, *ticket, *err;
+    unsigned long long *trace;
+} gb_sweep1_args;
 
 /* growable host array */
 typedef struct { void *p; size_t n, cap, esz; } gb_vec;
@@ -64,6 +94,25 @@ typedef struct gb_plan {
     int32_t *d_gemm_owner;
     gb_sweep_task *d_sweep;
     gb_pattern_ptrs ptrs;
+
+    /* per-level task graphs of the factorization */
+    gb_vec dag_t, dag_sp, dag_succ, dag_nd, dag_q0, dag_q1, dag_lv;
+    int32_t dag_max;
+    gb_dtask *d_dag_t;
+    int32_t *d_dag_sp, *d_dag_succ, *d_dag_nd, *d_dag_q0i, *d_dag_q1i, *d_dag_ctrl0;
+    int32_t *d_dag_cnt, *d_dag_q, *d_dag_ctrl;
+
+    /* single-launch sweeps: tasks, diagonal-block inverses, flags */
+    gb_vec sf_t, sb_t, sd_t;          /* forward, backward, diagonal-block tasks */
+    int64_t nblk_total, linv_total;
+    gb_stask *d_sf, *d_sb, *d_sd;
+    int32_t *d_blkoff, *d_ntask_f, *d_ntask_b, *d_parent;
+    int64_t *d_linvoff;
+    int32_t *d_xready, *d_done, *d_ticket, *d_err;
+    int32_t *h_blkoff, *h_ntask_f, *h_ntask_b, *h_parent;
+    int64_t *h_linvoff;
+    void *d_Linv[2];
+    int linv_valid[2];
 
     /* numeric buffers, [0] double, [1] single */
     void *d_Lx[2], *d_CB[2];
@@ -106,6 +155,16 @@ struct gb_ctx {
     /* optional per-launch timing of the factorization (gb300_set_option
      * GB300_OPT_PROFILE): events around every launch, summed per kind */
     int prof;
+    int sweep_mode;              /* 1 = single-launch sweeps (default), 0 = per level */
+    int trace_on;                /* record per-task times of the sweeps */
+    unsigned long long *d_trace; /* device trace buffer (3 x tasks) */
+    size_t trace_cap;
+    int64_t trace_n[2];          /* tasks traced by the last forward/backward sweep */
+    int64_t trace_off[2];
+    unsigned long long *d_ftrace;  /* factorization task trace */
+    size_t ftrace_cap;
+    int64_t ftrace_n;
+    int sms;
     cudaEvent_t *pev;
     int npev;
     double kind_ms[16], kind_n[16];
@@ -129,6 +188,7 @@ int gb_ensure_numeric(gb_plan *P, int dtype);
 int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dtype,
                   const double *scale, double beta);
 int gb_run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int forward);
+int gb_run_inverse(gb_plan *P, gb_ctx *ctx, int l_dtype);
 int gb_fix_not_posdef(gb_plan *P, gb_ctx *ctx, cholmod_factor *L, int l_dtype,
                       cholmod_common *Common);
 int gb_upload_input(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, int a_dtype);
@@ -140,11 +200,11 @@ int gb_launch_assemble(const gb_pattern_ptrs *pp, const gb_asm_task *tasks, int 
                        const double *scale, double beta, void *Lx, void *CB, int l_dtype,
                        cudaStream_t st);
 int gb_launch_factor_small(const gb_pattern_ptrs *pp, const gb_node_task *tasks, int ntasks,
-                           void *Lx, int dtype, cudaStream_t st);
+                           void *Lx, void *Linv, int dtype, cudaStream_t st);
 int gb_launch_potrf_diag(const gb_pattern_ptrs *pp, const gb_potrf_task *tasks, int ntasks,
-                         void *Lx, int dtype, cudaStream_t st);
+                         void *Lx, void *Linv, int dtype, cudaStream_t st);
 int gb_launch_trsm_rows(const gb_pattern_ptrs *pp, const gb_trsm_task *tasks, int ntasks,
-                        void *Lx, int dtype, cudaStream_t st);
+                        void *Lx, const void *Linv, int dtype, cudaStream_t st);
 int gb_launch_gemm(const gb_pattern_ptrs *pp, const gb_gemm_task *tasks, const int32_t *owner,
                    int ntasks, void *Lx, void *CB, int dtype, cudaStream_t st);
 int gb_launch_sweep_node(int kind, const gb_pattern_ptrs *pp, const gb_node_task *tasks,
@@ -169,6 +229,14 @@ int gb_launch_diag_minmax(int nsuper, const int64_t *Super, const int64_t *Pi,
                           const int64_t *Px, const void *Lx, int dtype, double *out,
                           cudaStream_t st);
 int gb_launch_fma_peak(int dtype, int iters, int blocks, float *ms, cudaStream_t st);
+int gb_launch_dag(const gb_pattern_ptrs *pp, const gb_dag_args *a, void *Lx, void *CB,
+                  void *Linv, int dtype, int grid, cudaStream_t st);
+int gb_launch_sweep1(int forward, const gb_pattern_ptrs *pp, const gb_sweep1_args *a,
+                     const void *Lx, const void *Linv, int dtype, int nrhs, void *Y,
+                     int64_t ldy, void *U, int grid, cudaStream_t st);
+int gb_launch_diag_inverse(const gb_pattern_ptrs *pp, const gb_stask *dtasks, int ndiag,
+                           const int32_t *blkoff, const int64_t *linvoff, const void *Lx,
+                           void *Linv, int dtype, cudaStream_t st);
 int gb_launch_zero_range(void *x, int dtype, int64_t from, int64_t to, cudaStream_t st);
 
 #ifdef __cplusplus
