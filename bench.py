@@ -303,8 +303,8 @@ def run_gpu(args):
     c.set_option(CH.GB300_OPT_PROFILE, 0)
     peak32 = CH.fma_peak("s")
     peak64 = CH.fma_peak("d")
-    g_ms, g_n = prof.get("gemm_tile", (0.0, 0))
-    achieved = info["fl_gemm"] / (g_ms * 1e-3) / 1e12 if g_ms else None
+    g_ms, g_n = prof.get("task_graph", (0.0, 0))
+    achieved = info["fl_taskgraph"] / (g_ms * 1e-3) / 1e12 if g_ms else None
     prof_total = sum(v[0] for v in prof.values()) or 1.0
 
     value = fl / (t_fac * 1e-3) / 1e12 * ws
@@ -340,7 +340,8 @@ def run_gpu(args):
         "e2e": {"value": e2e_val, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "solves_per_s": 1.0 / statistics.mean(e2e_s) * ws},
-        "roofline": {"kernel": "k_gemm_nt<float> (update-block / trailing tile update)",
+        "roofline": {"kernel": "k_dag<float> (per-level task graph: tile LL', panel solves, "
+                               "tile and update-block products)",
                      "bound": "compute (FP32 FMA pipe, SIMT)", "achieved": achieved,
                      "peak": peak32, "unit": "TFLOP/s",
                      "frac": (achieved / peak32) if (achieved and peak32) else None,

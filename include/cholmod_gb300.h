@@ -417,8 +417,8 @@ long gb300_abi_offset (int object, const char *field) ;
 long gb300_abi_sizeof (int object) ;
 
 /* Per-kernel-kind totals of the profiled factorizations: ms[k] and count[k]
- * for kind k = 1 assembly, 2 small-supernode factor, 3 diagonal-block LL',
- * 4 panel triangular solve, 5 tile update (C -= A B'). */
+ * for kind k = 1 assembly, 2 small-supernode factor, 6 task graph of the
+ * level (wide panels and update blocks). */
 int gb300_get_profile (cholmod_common *Common, double *ms, double *count, int nkinds) ;
 
 /* Per-task times (ns, device global timer) of the last traced forward
@@ -437,7 +437,7 @@ int gb300_get_factor_trace (cholmod_common *Common, unsigned long long *out,
 int gb300_plan_tasks (cholmod_factor *L, cholmod_common *Common, int32_t *out, int64_t nmax) ;
 
 /* Facts of the GPU plan of L (built if needed): [0] algorithmic flops of the
- * tile updates, [1] etree levels, [2] launches per factorization, [3]
+ * task graphs (wide panels' LL', solves and updates, and every update block), [1] etree levels, [2] launches per factorization, [3]
  * update-block entries, [4] tile-update tasks, [5] supernodes, [6] launches
  * per forward sweep, [7] per backward sweep, [8] update-vector entries,
  * [9] mixed state (0 none, 1 FP32 factor, 2 FP64 factor). */

@@ -23,7 +23,8 @@ CHOLMOD_NOT_POSDEF, CHOLMOD_DSMALL = 1, 2
 CHOLMOD_A = 0
 GB300_OPT_KEEP_ON_DEVICE, GB300_OPT_SMALL_COLS, GB300_OPT_PROFILE, GB300_OPT_SWEEP = 1, 2, 3, 4
 GB300_OPT_TRACE = 5
-KIND_NAMES = {1: "assemble", 2: "factor_small", 3: "potrf_diag", 4: "trsm_rows", 5: "gemm_tile"}
+KIND_NAMES = {1: "assemble", 2: "factor_small", 3: "potrf_diag", 4: "trsm_rows", 5: "gemm_tile",
+              6: "task_graph"}
 
 
 class cholmod_sparse(C.Structure):
@@ -289,7 +290,7 @@ def factor_info(L, common):
     out = (C.c_double * 10)()
     if not lib().gb300_factor_info(L, common.ptr, out, 10):
         raise RuntimeError(f"factor_info failed, status {common.status}")
-    keys = ["fl_gemm", "nlevels", "launches_factor", "cb_entries", "gemm_tasks", "nsuper",
+    keys = ["fl_taskgraph", "nlevels", "launches_factor", "cb_entries", "gemm_tasks", "nsuper",
             "launches_fwd", "launches_bwd", "cbv_entries", "mixed"]
     return dict(zip(keys, list(out)))
 

@@ -75,11 +75,14 @@ __global__ void k_diag_minmax(int nsuper, const int64_t *__restrict__ Super,
 {
     __shared__ double smin[256], smax[256];
     double lo = __longlong_as_double(0x7FF0000000000000LL), hi = 0.0;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsuper; s += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int s = warp; s < nsuper; s += nwarps) {          // one warp per supernode
         const int nscol = (int)(Super[s + 1] - Super[s]);
         const int64_t nsrow = Pi[s + 1] - Pi[s];
         const T *panel = Lx + Px[s];
-        for (int j = 0; j < nscol; j++) {
+        for (int j = lane; j < nscol; j += 32) {
             const double d = (double)panel[j + j * nsrow];
             lo = fmin(lo, d * d);
             hi = fmax(hi, d * d);
@@ -101,16 +104,18 @@ __global__ void k_diag_minmax(int nsuper, const int64_t *__restrict__ Super,
     }
 }
 
-// per column r: out[3r] = max|R|, out[3r+1] = max|X|, out[3r+2] = max|B|;
-// one block per column, fixed reduction tree.
+// per column r: out[3r] = max|R|, out[3r+1] = max|X|, out[3r+2] = max|B|
+// (out zeroed first); grid-wide, 64-bit atomics on the bit patterns of the
+// nonnegative maxima.
 __global__ void k_colmax3(int64_t n, const double *__restrict__ R, int64_t ldr,
                           const double *__restrict__ X, int64_t ldx,
                           const double *__restrict__ B, int64_t ldb, double *out)
 {
     __shared__ double sm[3][256];
-    const int r = blockIdx.x;
+    const int r = blockIdx.y;
     double a = 0, b = 0, c = 0;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
         a = fmax(a, fabs(R[i + r * ldr]));
         b = fmax(b, fabs(X[i + r * ldx]));
         c = fmax(c, fabs(B[i + r * ldb]));
@@ -126,7 +131,9 @@ __global__ void k_colmax3(int64_t n, const double *__restrict__ R, int64_t ldr,
         __syncthreads();
     }
     if (threadIdx.x == 0)
-        for (int q = 0; q < 3; q++) out[3 * r + q] = sm[q][0];
+        for (int q = 0; q < 3; q++)
+            atomicMax((unsigned long long *)&out[3 * r + q],
+                      (unsigned long long)__double_as_longlong(sm[q][0]));
 }
 
 // max over rows of sum |A(i,:)| (for the backward error denominator)
@@ -257,7 +264,12 @@ int gb_launch_diag_minmax(int nsuper, const int64_t *Super, const int64_t *Pi,
 int gb_launch_colmax3(int64_t n, int nrhs, const double *R, int64_t ldr, const double *X,
                       int64_t ldx, const double *B, int64_t ldb, double *out, cudaStream_t st)
 {
-    k_colmax3<<<nrhs, 256, 0, st>>>(n, R, ldr, X, ldx, B, ldb, out);
+    if (cudaMemsetAsync(out, 0, sizeof(double) * 3 * nrhs, st) != cudaSuccess) return 1;
+    int gx = (int)((n + 255) / 256);
+    if (gx > 304) gx = 304;
+    if (gx < 1) gx = 1;
+    dim3 grid(gx, nrhs);
+    k_colmax3<<<grid, 256, 0, st>>>(n, R, ldr, X, ldx, B, ldb, out);
     return (int)cudaGetLastError();
 }
 

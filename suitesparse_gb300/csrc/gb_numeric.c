@@ -180,7 +180,7 @@ int gb300_factor_info(cholmod_factor *L, cholmod_common *Common, double *out, in
     if (!ctx || !gb_ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return FALSE; }
     gb_plan *P = gb_plan_get(L, Common, ctx, 1);
     if (!P) return FALSE;
-    double v[10] = {P->fl_gemm, (double)P->nlevels, (double)P->fact_seq.n, (double)P->cb_total,
+    double v[10] = {P->fl_dag, (double)P->nlevels, (double)P->fact_seq.n, (double)P->cb_total,
                     (double)P->gemm_t.n, (double)P->nsuper, (double)P->fwd_seq.n,
                     (double)P->bwd_seq.n, (double)P->cbv_total, (double)P->mixed};
     for (int i = 0; i < nout && i < 10; i++) out[i] = v[i];

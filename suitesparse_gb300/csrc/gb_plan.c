@@ -303,6 +303,21 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
                     }
                 }
             }
+            if (Pid) {
+                /* algorithmic flops of the panel tasks (2 per multiply-add) */
+                for (Int b = 0; b < Cp; b++) {
+                    double nb = (double)GB_MIN(NB, nscol - b * NB);
+                    P->fl_dag += nb * nb * nb / 3.0;                         /* LL' */
+                    P->fl_dag += (double)(nsrow - b * NB - nb) * nb * nb;    /* solve */
+                    double w = (double)(nscol - b * NB - nb);                /* trailing cols */
+                    double h = (double)(nsrow - b * NB - nb);                /* trailing rows */
+                    P->fl_dag += (w * h - w * (w - 1) / 2.0) * 2.0 * nb;     /* lower update */
+                }
+            }
+            {
+                double mm = (double)m;
+                P->fl_dag += mm * (mm + 1) / 2.0 * 2.0 * (double)nscol;     /* update block */
+            }
             /* update-block tiles (k = nscol) */
             for (Int J = 0; J < m && ok; J += NB) {
                 for (Int I = J; I < m; I += NB) {

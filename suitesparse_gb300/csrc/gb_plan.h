@@ -78,6 +78,7 @@ typedef struct gb_plan {
     int nlevels;
     int64_t cb_total, cbv_total;      /* entries of all update blocks/vectors */
     double fl_gemm;                   /* algorithmic flops of the tile updates */
+    double fl_dag;                    /* algorithmic flops of the task graphs */
 
     /* host task arrays and launch sequences */
     gb_vec asm_t, node_t, potrf_t, trsm_t, gemm_t, gemm_owner, sweep_t;
