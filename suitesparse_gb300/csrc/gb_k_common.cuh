@@ -281,6 +281,146 @@ __device__ void gemm_tile_k64(const T *A, int64_t lda, const T *B, int64_t ldb, 
     }
 }
 
+// LL' and inverse of a 64 x 64 (nb <= 64) lower block in shared memory with
+// 256 threads.  A (leading dimension 65) is overwritten by L; X receives
+// L^-1 (X[c*65 + r] = Linv(r, c), zeros above the diagonal); T is scratch
+// of 3*256 entries.  Per 16-column panel: warp 0 factors the 16 x 16
+// diagonal block in registers (lane = row, shuffles) and inverts it (lane =
+// column); the rows below become B * inv(D)' (independent dot products);
+// the trailing lower part takes the rank-16 update.  Afterwards the
+// off-diagonal 16 x 16 blocks of the inverse are formed in three waves,
+// X_ij = -X_ii sum_{k=j}^{i-1} L_ik X_kj.  Returns the first column whose
+// pivot is not positive (earlier columns of L are final), or -1.
+template <typename T>
+__device__ int potrf_inv64(T (*A)[65], T *X, T *Tm, int nb, int *sfail)
+{
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < 64 * 65; idx += blockDim.x) X[idx] = (T)0;
+    if (tid == 0) *sfail = -1;
+    __syncthreads();
+    int failed = -1;
+    for (int p0 = 0; p0 < nb; p0 += 16) {
+        const int pw = min(16, nb - p0);
+        if (tid < 32) {
+            const int i = tid;
+            T row[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) row[k] = (i < pw && k <= i) ? A[p0 + i][p0 + k] : (T)0;
+            int bad = -1;
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                if (j < pw && bad < 0) {
+                    const T d = __shfl_sync(0xffffffffu, row[j], j);
+                    if (!(d > (T)0)) {
+                        bad = j;
+                    } else {
+                        const T sd = gb_sqrt<T>(d), rsd = (T)1 / sd;
+                        if (i == j) row[j] = sd;
+                        else if (i > j) row[j] *= rsd;
+#pragma unroll
+                        for (int k = j + 1; k < 16; k++) {
+                            const T lkj = __shfl_sync(0xffffffffu, row[j], k);
+                            if (i >= k && k < pw) row[k] -= row[j] * lkj;
+                        }
+                    }
+                }
+            }
+            if (i < pw) {
+#pragma unroll
+                for (int k = 0; k < 16; k++)
+                    if (k <= i) A[p0 + i][p0 + k] = row[k];
+            }
+            if (bad >= 0) {
+                if (i == 0) *sfail = p0 + bad;
+            } else {
+                __syncwarp();
+                // lane j: column j of inv(D), x_i = -(sum_{k=j}^{i-1} D_ik x_k) / D_ii
+                const int j = i;
+                T x[16];
+#pragma unroll
+                for (int r = 0; r < 16; r++) {
+                    T v = (T)0;
+                    if (r == j) v = (T)1;
+#pragma unroll
+                    for (int k = 0; k < r; k++)
+                        if (k >= j) v -= A[p0 + r][p0 + k] * x[k];
+                    x[r] = (j < pw && r < pw && r >= j) ? v / A[p0 + r][p0 + r] : (T)0;
+                }
+                if (j < pw) {
+#pragma unroll
+                    for (int r = 0; r < 16; r++) X[(p0 + j) * 65 + p0 + r] = x[r];
+                }
+            }
+        }
+        __syncthreads();
+        if (*sfail >= 0) { failed = *sfail; break; }
+        // rows below: L(r, panel) = A(r, panel) inv(D)'  (3 outputs per thread)
+        {
+            const int nrb = nb - p0 - pw;
+            T out[3];
+            int cnt = 0;
+            for (int e = tid; e < nrb * 16 && cnt < 3; e += blockDim.x, cnt++) {
+                const int r = p0 + pw + e / 16, cc = e % 16;
+                T acc = (T)0;
+#pragma unroll
+                for (int q = 0; q < 16; q++) acc += A[r][p0 + q] * X[(p0 + q) * 65 + p0 + cc];
+                out[cnt] = acc;
+            }
+            __syncthreads();
+            cnt = 0;
+            for (int e = tid; e < nrb * 16 && cnt < 3; e += blockDim.x, cnt++) {
+                const int r = p0 + pw + e / 16, cc = e % 16;
+                if (cc < pw) A[r][p0 + cc] = out[cnt];
+            }
+        }
+        __syncthreads();
+        // trailing lower part: rank-pw update, one (row, 8-column group) each
+        const int t0 = p0 + pw, nt = nb - t0;
+        const int ngroups = (nt + 7) / 8;
+        for (int w = tid; w < nt * ngroups; w += blockDim.x) {
+            const int r = t0 + w / ngroups, cb = t0 + 8 * (w % ngroups);
+            if (cb > r) continue;
+            T a[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) a[k] = (k < pw) ? A[r][p0 + k] : (T)0;
+            for (int cc = cb; cc < cb + 8 && cc <= r; cc++) {
+                T acc = A[r][cc];
+#pragma unroll
+                for (int k = 0; k < 16; k++) acc -= a[k] * A[cc][p0 + k];
+                A[r][cc] = acc;
+            }
+        }
+        __syncthreads();
+    }
+    if (failed >= 0) return failed;
+    // off-diagonal 16 x 16 blocks of the inverse, by distance d = i - j
+    const int nbk = (nb + 15) / 16;
+    for (int d = 1; d < nbk; d++) {
+        const int nblk = nbk - d;          // blocks (j + d, j), j = 0..nblk-1
+        for (int e = tid; e < nblk * 256; e += blockDim.x) {
+            const int j = e / 256, rc = e % 256, r = rc / 16, cc = rc % 16, i = j + d;
+            T acc = (T)0;
+            for (int k = j; k < i; k++) {
+#pragma unroll
+                for (int q = 0; q < 16; q++)
+                    acc += A[16 * i + r][16 * k + q] * X[(16 * j + cc) * 65 + 16 * k + q];
+            }
+            Tm[e] = acc;
+        }
+        __syncthreads();
+        for (int e = tid; e < nblk * 256; e += blockDim.x) {
+            const int j = e / 256, rc = e % 256, r = rc / 16, cc = rc % 16, i = j + d;
+            T acc = (T)0;
+#pragma unroll
+            for (int q = 0; q < 16; q++)
+                acc += X[(16 * i + q) * 65 + 16 * i + r] * Tm[j * 256 + q * 16 + cc];
+            X[(16 * j + cc) * 65 + 16 * i + r] = -acc;
+        }
+        __syncthreads();
+    }
+    return -1;
+}
+
 // One 64 x 64 output tile of C -= A B' (SIMT): A is m x k (lda), B is n x k
 // (ldb), both column-major; 16-deep k slices staged in As/Bs (each
 // 16 x (64+4)); store only r - c >= diag_off when lower.  256 threads, 4x4.
@@ -327,6 +467,88 @@ __device__ void gemm_tile_nt(const T *A, int64_t lda, const T *B, int64_t ldb, T
             if (c >= n) continue;
             if (lower && r - c < diag_off) continue;
             C[r + (int64_t)c * ldc] -= acc[i][j];
+        }
+    }
+}
+
+// FP32 tile update C[0:m, 0:n] -= A[0:m, 0:k] B[0:n, 0:k]' (m, n <= 64;
+// column-major operands; lower: update only entries with row - col >=
+// diag_off) with 256 threads.  Thread (tx, ty) = (tid % 16, tid / 16) owns
+// rows 4tx..4tx+3 and columns 4ty..4ty+3; its C entries are read into
+// registers before the k loop so their latency overlaps the first operand
+// loads, and the products are summed from zero and subtracted once at the
+// end (subtracting each product from C in turn loses accuracy in the
+// Schur complement).  Operands move through shared memory in k chunks of 32
+// (k-major, 68-float rows so a thread reads its 4 rows or columns as one
+// float4), two stages: the next chunk is loaded into registers while the
+// current one is multiplied.  S needs 2 x 2 x 32 x 68 floats.
+__device__ __forceinline__ void gemm_tile_f32(const float *A, int64_t lda, const float *B, int64_t ldb,
+                                              float *C, int64_t ldc, int m, int n, int k, bool lower,
+                                              int diag_off, float *S)
+{
+    constexpr int BK = 32, LDS = 68, STAGE = 2 * BK * LDS;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    float acc[4][4], cv[4][4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int cc = 4 * ty + j;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int r = 4 * tx + i;
+            cv[i][j] = (r < m && cc < n) ? C[r + (int64_t)cc * ldc] : 0.0f;
+            acc[i][j] = 0.0f;
+        }
+    }
+    // loader mapping: element q of this thread is row (tid & 63), k offset
+    // (tid >> 6) + 4q of the chunk
+    const int li = tid & 63, lk = tid >> 6;
+    float ra[8], rb[8];
+    auto load = [&](int k0) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int kg = k0 + lk + 4 * q;
+            ra[q] = (li < m && kg < k) ? A[li + (int64_t)kg * lda] : 0.0f;
+            rb[q] = (li < n && kg < k) ? B[li + (int64_t)kg * ldb] : 0.0f;
+        }
+    };
+    auto store = [&](int st) {
+        float *As = S + st * STAGE, *Bs = As + BK * LDS;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            As[(lk + 4 * q) * LDS + li] = ra[q];
+            Bs[(lk + 4 * q) * LDS + li] = rb[q];
+        }
+    };
+    const int nch = (k + BK - 1) / BK;
+    if (nch > 0) {
+        load(0);
+        store(0);
+    }
+    __syncthreads();
+    for (int ch = 0; ch < nch; ch++) {
+        const int st = ch & 1;
+        if (ch + 1 < nch) load((ch + 1) * BK);
+        const float *As = S + st * STAGE, *Bs = As + BK * LDS;
+#pragma unroll 8
+        for (int kk = 0; kk < BK; kk++) {
+            const float4 a = *reinterpret_cast<const float4 *>(As + kk * LDS + 4 * tx);
+            const float4 b = *reinterpret_cast<const float4 *>(Bs + kk * LDS + 4 * ty);
+            const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        }
+        if (ch + 1 < nch) store(st ^ 1);
+        __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int cc = 4 * ty + j;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int r = 4 * tx + i;
+            if (r < m && cc < n && !(lower && r - cc < diag_off)) C[r + (int64_t)cc * ldc] = cv[i][j] - acc[i][j];
         }
     }
 }

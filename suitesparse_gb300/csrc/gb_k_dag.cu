@@ -132,7 +132,7 @@ __host__ __device__ constexpr size_t dag_smem()
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2)
 k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -166,7 +166,7 @@ k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
                     A[i][j] = (i < nb && j < nb && i >= j) ? blk[i + (int64_t)j * nsrow] : (T)0;
                 }
                 __syncthreads();
-                const int fl = potrf64<T>(A, nb, &sfail);
+                const int fl = potrf_inv64<T>(A, S1, S2, nb, &sfail);
                 __syncthreads();
                 for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
                     const int i = idx % nb, j = idx / nb;
@@ -176,7 +176,11 @@ k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
                     P.fail[s] = c0 + fl;
                     atomicExch(P.anyfail, 1);
                 }
-                tri_inverse64<T>(A, nb, S1, Linv + P.linvoff[P.blkoff[s] + tk.b]);
+                T *li = Linv + P.linvoff[P.blkoff[s] + tk.b];
+                for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+                    const int i = idx % nb, j = idx / nb;
+                    li[i + (int64_t)j * nb] = S1[j * 65 + i];
+                }
             }
         } else if (tk.type == GB_DT_TRSM) {
             const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
@@ -198,19 +202,31 @@ k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
                 const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
                 const int cs = 64 * tk.c, ce = min(cs + 64, nscol);
                 const int rs = max(64 * tk.r, cs), re = min(64 * tk.r + 64, nsrow);
-                gemm_tile_k64<T>(panel + rs + (int64_t)c0 * nsrow, nsrow,
-                                 panel + cs + (int64_t)c0 * nsrow, nsrow,
-                                 panel + rs + (int64_t)cs * nsrow, nsrow,
-                                 re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, S1, S2);
+                if constexpr (sizeof(T) == 4)
+                    gemm_tile_f32(panel + rs + (int64_t)c0 * nsrow, nsrow,
+                                  panel + cs + (int64_t)c0 * nsrow, nsrow,
+                                  panel + rs + (int64_t)cs * nsrow, nsrow,
+                                  re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, (float *)smem_raw);
+                else
+                    gemm_tile_k64<T>(panel + rs + (int64_t)c0 * nsrow, nsrow,
+                                     panel + cs + (int64_t)c0 * nsrow, nsrow,
+                                     panel + rs + (int64_t)cs * nsrow, nsrow,
+                                     re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, S1, S2);
             }
         } else {  // GB_DT_CB
             if (f < 0) {
                 const int m = nsrow - nscol;
                 const int I = 64 * tk.r, J = 64 * tk.c;
-                gemm_tile_nt<T>(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
-                                CB + P.cboff[s] + I + (int64_t)J * m, m,
-                                min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
-                                S1, S2);
+                if constexpr (sizeof(T) == 4)
+                    gemm_tile_f32(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
+                                  CB + P.cboff[s] + I + (int64_t)J * m, m,
+                                  min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
+                                  (float *)smem_raw);
+                else
+                    gemm_tile_nt<T>(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
+                                    CB + P.cboff[s] + I + (int64_t)J * m, m,
+                                    min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
+                                    S1, S2);
             }
         }
         __syncthreads();

@@ -345,7 +345,7 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
                     ctx->ftrace_n = (int64_t)P->dag_t.n;
                 }
             }
-            int grid = GB_MAX(1, ctx->sms) * (ldt == 4 ? 4 : 2);
+            int grid = GB_MAX(1, ctx->sms) * (ldt == 4 ? 3 : 2);  /* resident blocks per SM */
             LK(gb_launch_dag(&P->ptrs, &a, Lx, CB, Linv, ldt, grid, st));
             break;
         }
