@@ -281,120 +281,172 @@ __device__ void gemm_tile_k64(const T *A, int64_t lda, const T *B, int64_t ldb, 
     }
 }
 
+template <typename T> __device__ __forceinline__ T gb_rsqrt(T x);
+template <> __device__ __forceinline__ double gb_rsqrt<double>(double x) { return rsqrt(x); }
+template <> __device__ __forceinline__ float gb_rsqrt<float>(float x) { return rsqrtf(x); }
+
+// One warp, lane i = row i of a 16 x 16 lower block held in registers
+// (row[k] = A(i, k), k <= i; rows >= pw are zero): LL' in place, pivots by
+// reciprocal square root (L(j,j) = d rsqrt(d), column j scaled by rsqrt(d)).
+// rinv receives 1 / L(i,i) in lane i.  Returns the first column whose pivot
+// is not positive (the same in every lane), or -1.
+template <typename T>
+__device__ __forceinline__ int warp_potrf16(T (&row)[16], T &rinv, int pw)
+{
+    const int i = threadIdx.x & 31;
+    int bad = -1;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        if (j < pw && bad < 0) {
+            const T d = __shfl_sync(0xffffffffu, row[j], j);
+            if (!(d > (T)0)) {
+                bad = j;
+            } else {
+                const T r = gb_rsqrt<T>(d);
+                if (i == j) { row[j] = d * r; rinv = r; }
+                else if (i > j) row[j] *= r;
+#pragma unroll
+                for (int k = j + 1; k < 16; k++) {
+                    const T lkj = __shfl_sync(0xffffffffu, row[j], k);
+                    if (i >= k && k < pw) row[k] -= row[j] * lkj;
+                }
+            }
+        }
+    }
+    return bad;
+}
+
+// One warp: lane c (< pv) forms column c of the inverse of the 16 x 16
+// lower factor stored in A[p1.., p1..] (leading pv x pv block; zero
+// elsewhere): x[r] = -(1 / L(r,r)) sum_{k<r} L(r, k) x[k] for r > c, with
+// the factor read from shared memory (the same address in every lane) and
+// 1 / L(r,r) taken from lane r's rinv.
+template <typename T>
+__device__ __forceinline__ void warp_trinv16(T (*A)[65], int p1, T rinv, T (&x)[16], int pv)
+{
+    const int c = threadIdx.x & 31;
+    T rv[16];
+#pragma unroll
+    for (int r = 0; r < 16; r++) rv[r] = __shfl_sync(0xffffffffu, rinv, r);
+#pragma unroll
+    for (int r = 0; r < 16; r++) {
+        T v = (T)0;
+#pragma unroll
+        for (int k = 0; k < r; k++) v += A[p1 + r][p1 + k] * x[k];
+        x[r] = (r < pv && r >= c) ? ((r == c) ? rv[r] : -rv[r] * v) : (T)0;
+    }
+}
+
+// Warp 0: diagonal 16 x 16 block of panel p1 (width pw1): take the rank-pwp
+// update from the previous panel p0 (if p0 >= 0), factor, invert, store L
+// into A and the inverse into X; on a non-positive pivot write its column
+// to *sfail.
+template <typename T>
+__device__ __forceinline__ void diag_block16(T (*A)[65], T *X, int p1, int pw1, int p0, int pwp, int *sfail)
+{
+    const int i = threadIdx.x & 31;
+    T row[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) row[k] = (i < pw1 && k <= i) ? A[p1 + i][p1 + k] : (T)0;
+    if (p0 >= 0) {
+        T a[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) a[q] = (i < pw1 && q < pwp) ? A[p1 + i][p0 + q] : (T)0;
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            if (k < pw1) {
+                T s = (T)0;
+#pragma unroll
+                for (int q = 0; q < 16; q++) s += a[q] * A[p1 + k][p0 + q];
+                if (k <= i) row[k] -= s;
+            }
+        }
+    }
+    T rinv = (T)0, x[16];
+    const int bad = warp_potrf16<T>(row, rinv, pw1);
+    const int pv = bad >= 0 ? bad : pw1;
+    if (i < pw1) {
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            if (k <= i) A[p1 + i][p1 + k] = row[k];
+    }
+    __syncwarp();
+    warp_trinv16<T>(A, p1, rinv, x, pv);
+    if (i < pv) {
+#pragma unroll
+        for (int r = 0; r < 16; r++)
+            if (r >= i) X[(p1 + i) * 65 + p1 + r] = x[r];
+    }
+    if (bad >= 0 && i == 0) *sfail = p1 + bad;
+}
+
 // LL' and inverse of a 64 x 64 (nb <= 64) lower block in shared memory with
 // 256 threads.  A (leading dimension 65) is overwritten by L; X receives
-// L^-1 (X[c*65 + r] = Linv(r, c), zeros above the diagonal); T is scratch
-// of 3*256 entries.  Per 16-column panel: warp 0 factors the 16 x 16
-// diagonal block in registers (lane = row, shuffles) and inverts it (lane =
-// column); the rows below become B * inv(D)' (independent dot products);
-// the trailing lower part takes the rank-16 update.  Afterwards the
-// off-diagonal 16 x 16 blocks of the inverse are formed in three waves,
-// X_ij = -X_ii sum_{k=j}^{i-1} L_ik X_kj.  Returns the first column whose
-// pivot is not positive (earlier columns of L are final), or -1.
+// L^-1 (X[c*65 + r] = Linv(r, c), zeros above the diagonal); Tm is scratch
+// of 3*256 entries.  In 16-column panels: warp 0 factors and inverts the
+// panel's diagonal block in registers; the rows below become A * inv(D)'
+// (a half warp per row, operands by shuffle); then warp 0 applies the
+// panel's update to the next diagonal block and factors it while the other
+// warps update the rest of the trailing lower part.  The off-diagonal
+// 16 x 16 blocks of the inverse follow in three waves, X_ij = -X_ii
+// sum_{k=j}^{i-1} L_ik X_kj.  Returns the first column whose pivot is not
+// positive, or -1; on failure the columns before it (of L and of the
+// inverse) are final.
 template <typename T>
 __device__ int potrf_inv64(T (*A)[65], T *X, T *Tm, int nb, int *sfail)
 {
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, warp = tid >> 5;
     for (int idx = tid; idx < 64 * 65; idx += blockDim.x) X[idx] = (T)0;
     if (tid == 0) *sfail = -1;
     __syncthreads();
-    int failed = -1;
+    if (warp == 0) diag_block16<T>(A, X, 0, min(16, nb), -1, 0, sfail);
+    __syncthreads();
+    int nv = nb;
     for (int p0 = 0; p0 < nb; p0 += 16) {
         const int pw = min(16, nb - p0);
-        if (tid < 32) {
-            const int i = tid;
-            T row[16];
+        const int f = *sfail;
+        const int pv = (f >= 0) ? f - p0 : pw;
+        // rows below the diagonal block: L(r, panel) = A(r, panel) inv(D)'
+        const int rb = p0 + pw, nrows = nb - rb;
+        for (int base = 0; base < nrows; base += 16) {
+            const int rr = base + (tid >> 4), cc = tid & 15;
+            const bool ok = rr < nrows;
+            const T a = (ok && cc < pw) ? A[rb + rr][p0 + cc] : (T)0;
+            T acc = (T)0;
 #pragma unroll
-            for (int k = 0; k < 16; k++) row[k] = (i < pw && k <= i) ? A[p0 + i][p0 + k] : (T)0;
-            int bad = -1;
+            for (int q = 0; q < 16; q++) acc += __shfl_sync(0xffffffffu, a, q, 16) * X[(p0 + q) * 65 + p0 + cc];
+            if (ok && cc < pv) A[rb + rr][p0 + cc] = acc;
+        }
+        if (f >= 0) { nv = f; break; }
+        __syncthreads();
+        if (rb < nb) {
+            const int pw1 = min(16, nb - rb);
+            if (warp == 0) {
+                diag_block16<T>(A, X, rb, pw1, p0, pw, sfail);
+            } else {
+                // rows below the next diagonal block, columns rb..r
+                const int t0 = rb + pw1, nt = nb - t0, ng = (nb - rb + 7) / 8;
+                for (int w = tid - 32; w < nt * ng; w += blockDim.x - 32) {
+                    const int r = t0 + w / ng, cb = rb + 8 * (w % ng);
+                    if (cb > r) continue;
+                    T a[16];
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-                if (j < pw && bad < 0) {
-                    const T d = __shfl_sync(0xffffffffu, row[j], j);
-                    if (!(d > (T)0)) {
-                        bad = j;
-                    } else {
-                        const T sd = gb_sqrt<T>(d), rsd = (T)1 / sd;
-                        if (i == j) row[j] = sd;
-                        else if (i > j) row[j] *= rsd;
+                    for (int q = 0; q < 16; q++) a[q] = (q < pw) ? A[r][p0 + q] : (T)0;
+                    const int ce = min(cb + 8, r + 1);
+                    for (int cc = cb; cc < ce; cc++) {
+                        T s = (T)0;
 #pragma unroll
-                        for (int k = j + 1; k < 16; k++) {
-                            const T lkj = __shfl_sync(0xffffffffu, row[j], k);
-                            if (i >= k && k < pw) row[k] -= row[j] * lkj;
-                        }
+                        for (int q = 0; q < 16; q++) s += a[q] * A[cc][p0 + q];
+                        A[r][cc] -= s;
                     }
                 }
-            }
-            if (i < pw) {
-#pragma unroll
-                for (int k = 0; k < 16; k++)
-                    if (k <= i) A[p0 + i][p0 + k] = row[k];
-            }
-            if (bad >= 0) {
-                if (i == 0) *sfail = p0 + bad;
-            } else {
-                __syncwarp();
-                // lane j: column j of inv(D), x_i = -(sum_{k=j}^{i-1} D_ik x_k) / D_ii
-                const int j = i;
-                T x[16];
-#pragma unroll
-                for (int r = 0; r < 16; r++) {
-                    T v = (T)0;
-                    if (r == j) v = (T)1;
-#pragma unroll
-                    for (int k = 0; k < r; k++)
-                        if (k >= j) v -= A[p0 + r][p0 + k] * x[k];
-                    x[r] = (j < pw && r < pw && r >= j) ? v / A[p0 + r][p0 + r] : (T)0;
-                }
-                if (j < pw) {
-#pragma unroll
-                    for (int r = 0; r < 16; r++) X[(p0 + j) * 65 + p0 + r] = x[r];
-                }
-            }
-        }
-        __syncthreads();
-        if (*sfail >= 0) { failed = *sfail; break; }
-        // rows below: L(r, panel) = A(r, panel) inv(D)'  (3 outputs per thread)
-        {
-            const int nrb = nb - p0 - pw;
-            T out[3];
-            int cnt = 0;
-            for (int e = tid; e < nrb * 16 && cnt < 3; e += blockDim.x, cnt++) {
-                const int r = p0 + pw + e / 16, cc = e % 16;
-                T acc = (T)0;
-#pragma unroll
-                for (int q = 0; q < 16; q++) acc += A[r][p0 + q] * X[(p0 + q) * 65 + p0 + cc];
-                out[cnt] = acc;
-            }
-            __syncthreads();
-            cnt = 0;
-            for (int e = tid; e < nrb * 16 && cnt < 3; e += blockDim.x, cnt++) {
-                const int r = p0 + pw + e / 16, cc = e % 16;
-                if (cc < pw) A[r][p0 + cc] = out[cnt];
-            }
-        }
-        __syncthreads();
-        // trailing lower part: rank-pw update, one (row, 8-column group) each
-        const int t0 = p0 + pw, nt = nb - t0;
-        const int ngroups = (nt + 7) / 8;
-        for (int w = tid; w < nt * ngroups; w += blockDim.x) {
-            const int r = t0 + w / ngroups, cb = t0 + 8 * (w % ngroups);
-            if (cb > r) continue;
-            T a[16];
-#pragma unroll
-            for (int k = 0; k < 16; k++) a[k] = (k < pw) ? A[r][p0 + k] : (T)0;
-            for (int cc = cb; cc < cb + 8 && cc <= r; cc++) {
-                T acc = A[r][cc];
-#pragma unroll
-                for (int k = 0; k < 16; k++) acc -= a[k] * A[cc][p0 + k];
-                A[r][cc] = acc;
             }
         }
         __syncthreads();
     }
-    if (failed >= 0) return failed;
+    __syncthreads();
     // off-diagonal 16 x 16 blocks of the inverse, by distance d = i - j
-    const int nbk = (nb + 15) / 16;
+    const int nbk = (nv + 15) / 16;
     for (int d = 1; d < nbk; d++) {
         const int nblk = nbk - d;          // blocks (j + d, j), j = 0..nblk-1
         for (int e = tid; e < nblk * 256; e += blockDim.x) {
@@ -418,7 +470,7 @@ __device__ int potrf_inv64(T (*A)[65], T *X, T *Tm, int nb, int *sfail)
         }
         __syncthreads();
     }
-    return -1;
+    return nv < nb ? nv : -1;
 }
 
 // One 64 x 64 output tile of C -= A B' (SIMT): A is m x k (lda), B is n x k

@@ -27,10 +27,11 @@ struct gb_dag_dev {
     const int32_t *succ_ptr, *succ;
     int32_t *cnt;            // live dependency counters
     int32_t *q0, *q1;        // ready queues: slot = task id, -1 not yet written
-    int32_t *ctrl;           // [0] head0 [1] tail0 [2] head1 [3] tail1 [4] roles [5] err
-                             // [6] tasks of the critical queue [7] of the bulk queue
+    int32_t *ctrl;           // GB_DAG_NCTRL control words (gb_kernels.cuh)
     int32_t *err;            // error word kept across levels
     unsigned long long *trace; // optional: per task [claimed, finished, block] (ns)
+    int32_t *smflag;         // per SM: epoch of the launch whose poller runs there
+    int32_t epoch;
 };
 
 __device__ __forceinline__ unsigned long long dag_timer()
@@ -109,11 +110,15 @@ __device__ int dag_pop(const gb_dag_dev &D, int poller)
     return -2;
 }
 
-// thread 0, after the block finished task id
+// warp 0, after the block finished task id (and a block barrier): release
+// the block's writes, then decrement the successors' dependency counters,
+// one successor per lane (critical successors come first in the list), and
+// queue those that became ready
 __device__ void dag_complete(const gb_dag_dev &D, int id)
 {
     __threadfence();
-    for (int e = D.succ_ptr[id]; e < D.succ_ptr[id + 1]; e++) {
+    const int e0 = D.succ_ptr[id], e1 = D.succ_ptr[id + 1];
+    for (int e = e0 + (int)(threadIdx.x & 31); e < e1; e += 32) {
         const int v = D.succ[e];
         if (dag_add_acq_rel(D.cnt + v, -1) == 1) {
             const int q = D.tasks[v].prio ? 1 : 0;
@@ -132,15 +137,33 @@ __host__ __device__ constexpr size_t dag_smem()
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2)
+__global__ void __launch_bounds__(256, 2)
 k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T (*A)[65] = (T (*)[65])smem_raw;
     T *S1 = (T *)smem_raw + 64 * 65, *S2 = S1 + 64 * 65;
     __shared__ int sid, sfail, spoll;
-    if (threadIdx.x == 0) spoll = atomicAdd(D.ctrl + 4, 1) < GB_DAG_POLLERS;
+    if (threadIdx.x == 0) {
+        // The first GB_DAG_POLLERS blocks to start serve the critical queue
+        // and mark their SM.  The critical path is a chain of latency-bound
+        // tasks, so a bulk block that finds itself on a marked SM leaves
+        // (at most 2 GB_DAG_POLLERS of them, and only in a large grid, so
+        // that plenty of bulk blocks remain).
+        int role = atomicAdd(D.ctrl + 4, 1) < GB_DAG_POLLERS;
+        unsigned smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        smid %= GB_DAG_NSMF;
+        if (role) {
+            atomicExch(D.smflag + smid, D.epoch);
+        } else if (gridDim.x >= 4 * GB_DAG_POLLERS && dag_ld_acquire(D.smflag + smid) == D.epoch
+                   && atomicAdd(D.ctrl + 8, 1) < 2 * GB_DAG_POLLERS) {
+            role = 2;
+        }
+        spoll = role;
+    }
     __syncthreads();
+    if (spoll == 2) return;
     const int poller = spoll;
     for (;;) {
         if (threadIdx.x == 0) sid = dag_pop(D, poller);
@@ -230,8 +253,8 @@ k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
             }
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            if (D.trace) D.trace[3 * (size_t)id + 1] = dag_timer();
+        if (threadIdx.x < 32) {
+            if (D.trace && threadIdx.x == 0) D.trace[3 * (size_t)id + 1] = dag_timer();
             dag_complete(D, id);
         }
     }
@@ -248,6 +271,7 @@ int gb_launch_dag(const gb_pattern_ptrs *pp, const gb_dag_args *a, void *Lx, voi
     D.tasks = a->tasks; D.ntasks = a->ntasks; D.succ_ptr = a->succ_ptr; D.succ = a->succ;
     D.cnt = a->cnt; D.q0 = a->q0; D.q1 = a->q1; D.ctrl = a->ctrl; D.err = a->err;
     D.trace = a->trace;
+    D.smflag = a->smflag; D.epoch = a->epoch;
     static int configured = 0;
     if (!configured) {
         cudaFuncSetAttribute(k_dag<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<double>());

@@ -58,6 +58,12 @@ typedef struct { int32_t type, s, b, r, c, prio, pad0, pad1; } gb_dtask;
 #define GB_DT_UPD   3
 #define GB_DT_CB    4
 
+/* control words of one task-graph launch: [0] head0 [1] tail0 [2] head1
+ * [3] tail1 [4] blocks started [5] error [6] total0 [7] total1 [8] blocks
+ * that left a poller's SM */
+#define GB_DAG_NCTRL 16
+#define GB_DAG_NSMF 1024    /* per-SM poller marks (indexed by %smid) */
+
 #define GB_NB 64            /* block size of the blocked paths */
 #define GB_TILE 64          /* output tile edge of the update kernel */
 #define GB_TRSM_ROWS 64     /* rows per triangular-solve task */

@@ -324,8 +324,8 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
             if (lv->n1)
                 CU(cudaMemcpyAsync(P->d_dag_q + nt, P->d_dag_q1i + lv->q1_off,
                                    sizeof(int32_t) * lv->n1, cudaMemcpyDeviceToDevice, st));
-            CU(cudaMemcpyAsync(P->d_dag_ctrl, P->d_dag_ctrl0 + 8 * r->off, sizeof(int32_t) * 8,
-                               cudaMemcpyDeviceToDevice, st));
+            CU(cudaMemcpyAsync(P->d_dag_ctrl, P->d_dag_ctrl0 + GB_DAG_NCTRL * r->off,
+                               sizeof(int32_t) * GB_DAG_NCTRL, cudaMemcpyDeviceToDevice, st));
             gb_dag_args a;
             a.tasks = P->d_dag_t + lv->task_off;
             a.ntasks = (int)nt;
@@ -337,6 +337,9 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
             a.ctrl = P->d_dag_ctrl;
             a.err = P->d_ticket + 3;
             a.trace = NULL;
+            a.smflag = P->d_dag_smf;
+            if (++P->dag_epoch <= 0) P->dag_epoch = 1;
+            a.epoch = P->dag_epoch;
             if (ctx->trace_on) {
                 /* factorization trace: all levels' tasks, 3 words each */
                 size_t need = 3 * (P->dag_t.n + 1) * sizeof(unsigned long long);
@@ -345,7 +348,7 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
                     ctx->ftrace_n = (int64_t)P->dag_t.n;
                 }
             }
-            int grid = GB_MAX(1, ctx->sms) * (ldt == 4 ? 3 : 2);  /* resident blocks per SM */
+            int grid = GB_MAX(1, ctx->sms) * 2;  /* resident blocks per SM */
             LK(gb_launch_dag(&P->ptrs, &a, Lx, CB, Linv, ldt, grid, st));
             break;
         }

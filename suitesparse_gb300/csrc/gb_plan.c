@@ -367,9 +367,21 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
             for (int32_t t = 0; ok && t < ntl; t++) deg[t + 1] += deg[t];
             if (ok) memcpy(pos, deg, sizeof(int32_t) * (ntl + 1));
             for (size_t q2 = 0; ok && q2 < edges.n; q2++) succ[pos[E[2 * q2]]++] = E[2 * q2 + 1];
+            const gb_dtask *dt = (const gb_dtask *)P->dag_t.p + t0g;
+            /* critical successors first: a finished task notifies its
+             * successors 32 at a time, in list order */
+            int32_t *tmp = ok ? malloc(sizeof(int32_t) * (edges.n + 1)) : NULL;
+            if (!tmp) ok = 0;
+            for (int32_t t = 0; ok && t < ntl; t++) {
+                int32_t w = deg[t];
+                for (int pass = 0; pass < 2; pass++)
+                    for (int32_t e = deg[t]; e < deg[t + 1]; e++)
+                        if ((dt[succ[e]].prio == 0) == (pass == 0)) tmp[w++] = succ[e];
+                memcpy(succ + deg[t], tmp + deg[t], sizeof(int32_t) * (deg[t + 1] - deg[t]));
+            }
+            free(tmp);
             for (int32_t t = 0; ok && t <= ntl; t++) ok &= gb_vec_push(&P->dag_sp, &deg[t]);
             for (size_t q2 = 0; ok && q2 < edges.n; q2++) ok &= gb_vec_push(&P->dag_succ, &succ[q2]);
-            const gb_dtask *dt = (const gb_dtask *)P->dag_t.p + t0g;
             for (int32_t t = 0; ok && t < ntl; t++) {
                 if (dt[t].prio == 0) lv.total0++; else lv.total1++;
                 ok &= gb_vec_push(&P->dag_nd, &nd[t]);
@@ -634,17 +646,17 @@ int gb_plan_upload(gb_plan *P)
     UP(P->d_dag_q1i, P->dag_q1.p, P->dag_q1.n * P->dag_q1.esz);
     {
         size_t nl = P->dag_lv.n;
-        int32_t *ctrl0 = calloc(8 * (nl + 1), sizeof(int32_t));
+        int32_t *ctrl0 = calloc(GB_DAG_NCTRL * (nl + 1), sizeof(int32_t));
         if (!ctrl0) goto fail;
         const gb_dag_level *lv = P->dag_lv.p;
         for (size_t i = 0; i < nl; i++) {
-            ctrl0[8 * i + 1] = lv[i].n0;
-            ctrl0[8 * i + 3] = lv[i].n1;
-            ctrl0[8 * i + 6] = lv[i].total0;
-            ctrl0[8 * i + 7] = lv[i].total1;
+            ctrl0[GB_DAG_NCTRL * i + 1] = lv[i].n0;
+            ctrl0[GB_DAG_NCTRL * i + 3] = lv[i].n1;
+            ctrl0[GB_DAG_NCTRL * i + 6] = lv[i].total0;
+            ctrl0[GB_DAG_NCTRL * i + 7] = lv[i].total1;
         }
-        int okc = cudaMalloc((void **)&P->d_dag_ctrl0, sizeof(int32_t) * 8 * (nl + 1)) == cudaSuccess
-                  && cudaMemcpy(P->d_dag_ctrl0, ctrl0, sizeof(int32_t) * 8 * (nl + 1), cudaMemcpyHostToDevice) == cudaSuccess;
+        int okc = cudaMalloc((void **)&P->d_dag_ctrl0, sizeof(int32_t) * GB_DAG_NCTRL * (nl + 1)) == cudaSuccess
+                  && cudaMemcpy(P->d_dag_ctrl0, ctrl0, sizeof(int32_t) * GB_DAG_NCTRL * (nl + 1), cudaMemcpyHostToDevice) == cudaSuccess;
         free(ctrl0);
         if (!okc) goto fail;
     }
@@ -652,7 +664,9 @@ int gb_plan_upload(gb_plan *P)
         size_t mx = (size_t)GB_MAX(P->dag_max, 1);
         if (cudaMalloc((void **)&P->d_dag_cnt, sizeof(int32_t) * mx) != cudaSuccess) goto fail;
         if (cudaMalloc((void **)&P->d_dag_q, sizeof(int32_t) * 2 * mx) != cudaSuccess) goto fail;
-        if (cudaMalloc((void **)&P->d_dag_ctrl, sizeof(int32_t) * 8) != cudaSuccess) goto fail;
+        if (cudaMalloc((void **)&P->d_dag_ctrl, sizeof(int32_t) * GB_DAG_NCTRL) != cudaSuccess) goto fail;
+        if (cudaMalloc((void **)&P->d_dag_smf, sizeof(int32_t) * GB_DAG_NSMF) != cudaSuccess) goto fail;
+        if (cudaMemset(P->d_dag_smf, 0, sizeof(int32_t) * GB_DAG_NSMF) != cudaSuccess) goto fail;
     }
     UP(P->d_sf, P->sf_t.p, P->sf_t.n * P->sf_t.esz);
     UP(P->d_sb, P->sb_t.p, P->sb_t.n * P->sb_t.esz);
@@ -706,7 +720,7 @@ void gb_plan_free(gb_plan *P)
                    P->d_ntask_b, P->d_parent, P->d_linvoff, P->d_xready, P->d_done,
                    P->d_ticket, P->d_Linv[0], P->d_Linv[1], P->d_dag_t, P->d_dag_sp,
                    P->d_dag_succ, P->d_dag_nd, P->d_dag_q0i, P->d_dag_q1i, P->d_dag_ctrl0,
-                   P->d_dag_cnt, P->d_dag_q, P->d_dag_ctrl};
+                   P->d_dag_cnt, P->d_dag_q, P->d_dag_ctrl, P->d_dag_smf};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++)
         if (dev[i]) cudaFree(dev[i]);
     gb_vec_free(&P->asm_t); gb_vec_free(&P->node_t); gb_vec_free(&P->potrf_t);

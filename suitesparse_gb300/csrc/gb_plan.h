@@ -47,6 +47,8 @@ typedef struct {
     int32_t *cnt, *q0, *q1, *ctrl;
     int32_t *err;            /* persistent error word of the factorization */
     unsigned long long *trace;
+    int32_t *smflag;         /* [GB_DAG_NSMF] launch epoch of the SM's poller */
+    int32_t epoch;           /* distinct per launch, nonzero */
 } gb_dag_args;
 
 /* arguments of the single-launch sweeps (device pointers) */
@@ -101,7 +103,8 @@ typedef struct gb_plan {
     int32_t dag_max;
     gb_dtask *d_dag_t;
     int32_t *d_dag_sp, *d_dag_succ, *d_dag_nd, *d_dag_q0i, *d_dag_q1i, *d_dag_ctrl0;
-    int32_t *d_dag_cnt, *d_dag_q, *d_dag_ctrl;
+    int32_t *d_dag_cnt, *d_dag_q, *d_dag_ctrl, *d_dag_smf;
+    int32_t dag_epoch;
 
     /* single-launch sweeps: tasks, diagonal-block inverses, flags */
     gb_vec sf_t, sb_t, sd_t;          /* forward, backward, diagonal-block tasks */
