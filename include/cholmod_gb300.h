@@ -453,6 +453,38 @@ int gb300_fma_peak (int dtype, double *tflops) ;
  * factorization (count), [5] kernel launches issued through Common so far. */
 int gb300_get_stats (cholmod_common *Common, double *out, int nout) ;
 
+/* Backward error of solutions that are already in device memory, with no
+ * allocation of any kind (no counterpart in the reference library).  For
+ * callers that must not allocate while they run: a serving loop with a
+ * fixed memory footprint that cannot afford the implicit synchronization of
+ * cudaMalloc/cudaFree, or an application that hands this library memory it
+ * has already reserved.  Everything is caller-owned device memory:
+ *   A:    n x n symmetric, BOTH triangles in compressed-column form
+ *         (Ap [n+1], Ai [nnz] int64, Ax [nnz] double); by symmetry column i
+ *         serves as row i of the residual;
+ *   X, B: n x nrhs, column-major, leading dimensions ldx, ldb >= n;
+ *   berr: nrhs doubles, receives |b - A x|_inf / (|A|_inf |x|_inf + |b|_inf)
+ *         per column -- the measure gb300_solve_refined reports in info.
+ * The work is queued on stream (a cudaStream_t, NULL for the default
+ * stream) and the call returns without waiting.  The reduction scratch is a
+ * fixed device array inside this library, sized for GB300_BERR_MAX_RHS
+ * columns; it must be all zero when a call starts, which holds because it is
+ * zero at load and every call zeroes it before it finishes.  Consequently
+ * calls on one device must not overlap: issue them on one stream (or
+ * otherwise order them); two calls in flight at once on the same device race
+ * on the scratch.  The first call on each device looks up the scratch
+ * address (cudaGetSymbolAddress, with that device current); make that first
+ * call before any stream capture.  Returns 0, or GB300_NOALLOC_INVALID (bad
+ * pointer, size or leading dimension), GB300_NOALLOC_TOO_LARGE (nrhs >
+ * GB300_BERR_MAX_RHS; nothing is queued), GB300_NOALLOC_CUDA (CUDA error). */
+#define GB300_BERR_MAX_RHS 64
+#define GB300_NOALLOC_INVALID   (-1)
+#define GB300_NOALLOC_TOO_LARGE (-2)
+#define GB300_NOALLOC_CUDA      (-3)
+int gb300_backward_error_noalloc (int64_t n, const int64_t *Ap, const int64_t *Ai,
+    const double *Ax, int nrhs, const double *X, int64_t ldx, const double *B,
+    int64_t ldb, double *berr, void *stream) ;
+
 #ifdef __cplusplus
 }
 #endif
