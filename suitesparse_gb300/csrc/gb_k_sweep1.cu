@@ -10,10 +10,11 @@
 //            off-diagonal row blocks.  A diagonal block waits for s's
 //            children (their update vectors) and, one at a time, for the
 //            earlier diagonal blocks of s:  x_i = Linv_ii (b_i - children -
-//            sum_{j<i} L_ij x_j).  An off-diagonal row block waits for all
-//            diagonal blocks of s and writes its rows of the update vector
-//            u_s = (children's contributions) + L21 x1, which s's parent
-//            gathers (owner-computes, children in a fixed order).
+//            sum_{j<i} L_ij x_j).  An off-diagonal row block takes the
+//            diagonal blocks of s one at a time as they become final and
+//            writes its rows of the update vector u_s = (children's
+//            contributions) + L21 x1, which s's parent gathers
+//            (owner-computes, children in a fixed order).
 //   backward per supernode s, diagonal blocks last to first: wait for the
 //            parent supernode (whose completion implies all ancestors'),
 //            x_i = Linv_ii' (y_i - L21(:,i)' x(rows of s) - sum_{j>i} L_ji' x_j).
@@ -257,15 +258,16 @@ k_fwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
                 }
                 __syncthreads();
             } else {
-                // update-vector rows: ys += L(rows, 0:nscol) x1, x1 final
-                if (k0 == 0 && threadIdx.x == 0) {
-                    if (!wait_ge(S.xready + S.blkoff[s] + nblk - 1, 1, S.err)) abort_ = 1;
-                }
-                __syncthreads();
-                if (abort_) return;
+                // update-vector rows: ys += L(rows, 0:nscol) x1, taking each
+                // 64-column block of x1 as soon as it is final
                 for (int j = 0; j < nblk; j++) {
                     const int nc = min(SR, nscol - j * SR);
+                    if (k0 == 0 && threadIdx.x == 0) {
+                        if (!wait_ge(S.xready + S.blkoff[s] + j, 1, S.err)) abort_ = 1;
+                    }
                     tile_park(tA, reg);
+                    __syncthreads();
+                    if (abort_) return;
                     for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
                         const int c = idx / RCH, k = idx % RCH;
                         xs[idx] = (c < nc && k < nk) ? Y[k1 + j * SR + c + (int64_t)(k0 + k) * ldy] : (T)0;
