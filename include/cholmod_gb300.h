@@ -348,12 +348,18 @@ int gb300_finish (cholmod_common *Common) ;
  *      0 = one launch per etree level and block step.
  *  GB300_OPT_TRACE [0]: 1 = the single-launch sweeps record, per task, the
  *      global-timer values when it started, when its dependencies were met
- *      and when it finished (gb300_get_trace). */
+ *      and when it finished (gb300_get_trace).
+ *  GB300_OPT_FACTOR [1]: 1 = the numeric factorization is one persistent
+ *      launch over a task graph of the whole etree (assembly chunks, small
+ *      supernodes, tiles of the wide supernodes, update blocks; a supernode
+ *      starts when its children's update blocks are done); 0 = one launch
+ *      of each kind per etree level, levels in sequence. */
 #define GB300_OPT_KEEP_ON_DEVICE 1
 #define GB300_OPT_SMALL_COLS     2
 #define GB300_OPT_PROFILE        3
 #define GB300_OPT_SWEEP          4
 #define GB300_OPT_TRACE          5
+#define GB300_OPT_FACTOR         6
 int gb300_set_option (cholmod_common *Common, int option, int64_t value) ;
 
 /* Supernodal symbolic analysis of A (stype < 0, lower) with a given final

@@ -605,7 +605,7 @@ __device__ __forceinline__ void gemm_tile_f32(const float *A, int64_t lda, const
     }
 }
 
-static inline gb_dev_pattern gb_to_dev(const gb_pattern_ptrs *p)
+static inline __host__ __device__ gb_dev_pattern gb_to_dev(const gb_pattern_ptrs *p)
 {
     gb_dev_pattern d;
     d.Super = p->Super; d.Pi = p->Pi; d.Px = p->Px; d.cboff = p->cboff;

@@ -17,21 +17,26 @@
 // CHOLMOD/Supernodal/t_cholmod_super_numeric_worker.c dpotrf :1004-1058,
 // dtrsm :1152-1218, the dsyrk/dgemm update matrices :768-883.
 
-#include "gb_k_common.cuh"
+#include "gb_k_bodies.cuh"
 
 #define GB_DAG_SPIN (1 << 24)
 
+// ready queues and control words of one executor launch
+struct gb_dq {
+    int32_t *q0, *q1;        // ready queues: slot = task id, -1 not yet written
+    int32_t *ctrl;           // GB_DAG_NCTRL control words (gb_kernels.cuh)
+    int32_t *err;            // error word kept across launches
+    int32_t *smflag;         // per SM: epoch of the launch whose poller runs there
+    int32_t epoch;
+};
+
 struct gb_dag_dev {
+    gb_dq Q;
     const gb_dtask *tasks;
     int ntasks;
     const int32_t *succ_ptr, *succ;
     int32_t *cnt;            // live dependency counters
-    int32_t *q0, *q1;        // ready queues: slot = task id, -1 not yet written
-    int32_t *ctrl;           // GB_DAG_NCTRL control words (gb_kernels.cuh)
-    int32_t *err;            // error word kept across levels
     unsigned long long *trace; // optional: per task [claimed, finished, block] (ns)
-    int32_t *smflag;         // per SM: epoch of the launch whose poller runs there
-    int32_t epoch;
 };
 
 __device__ __forceinline__ unsigned long long dag_timer()
@@ -64,7 +69,7 @@ __device__ __forceinline__ int dag_add_acq_rel(int32_t *p, int v)
 
 // thread 0: claim slot h of a queue (the pusher reserved it with tail and
 // writes it right away, or will once the task is ready)
-__device__ int dag_take(const gb_dag_dev &D, const int32_t *slots, int h)
+__device__ int dag_take(const gb_dq &D, const int32_t *slots, int h)
 {
     for (int k = 0; k < GB_DAG_SPIN; k++) {
         const int v = dag_ld_acquire(slots + h);
@@ -86,7 +91,7 @@ __device__ int dag_take(const gb_dag_dev &D, const int32_t *slots, int h)
 // slot waits either for a slot being written or for a task not yet ready,
 // and every ready task is either in a claimed slot (its block runs it) or
 // is a critical task a poller can claim; pollers never wait.
-__device__ int dag_pop(const gb_dag_dev &D, int poller)
+__device__ int dag_pop(const gb_dq &D, int poller)
 {
     int32_t *ctrl = D.ctrl;
     const int total0 = ctrl[6], total1 = ctrl[7];
@@ -110,6 +115,15 @@ __device__ int dag_pop(const gb_dag_dev &D, int poller)
     return -2;
 }
 
+// warp 0: queue task v (its last dependency just finished) on the queue of
+// its priority
+__device__ __forceinline__ void dag_push(const gb_dq &D, int v, int prio)
+{
+    const int q = prio ? 1 : 0;
+    const int slot = atomicAdd(D.ctrl + 2 * q + 1, 1);
+    dag_st_release((q ? D.q1 : D.q0) + slot, v);
+}
+
 // warp 0, after the block finished task id (and a block barrier): release
 // the block's writes, then decrement the successors' dependency counters,
 // one successor per lane (critical successors come first in the list), and
@@ -120,12 +134,29 @@ __device__ void dag_complete(const gb_dag_dev &D, int id)
     const int e0 = D.succ_ptr[id], e1 = D.succ_ptr[id + 1];
     for (int e = e0 + (int)(threadIdx.x & 31); e < e1; e += 32) {
         const int v = D.succ[e];
-        if (dag_add_acq_rel(D.cnt + v, -1) == 1) {
-            const int q = D.tasks[v].prio ? 1 : 0;
-            const int slot = atomicAdd(D.ctrl + 2 * q + 1, 1);
-            dag_st_release((q ? D.q1 : D.q0) + slot, v);
-        }
+        if (dag_add_acq_rel(D.cnt + v, -1) == 1) dag_push(D.Q, v, D.tasks[v].prio);
     }
+}
+
+// thread 0 at the start of an executor block: 1 = poller, 0 = bulk block,
+// 2 = leave.  The first GB_DAG_POLLERS blocks to start serve the critical
+// queue and mark their SM.  The critical path is a chain of latency-bound
+// tasks, so a bulk block that finds itself on a marked SM leaves (at most
+// 2 GB_DAG_POLLERS of them, and only in a large grid, so that plenty of bulk
+// blocks remain).
+__device__ int dag_role(const gb_dq &D)
+{
+    int role = atomicAdd(D.ctrl + 4, 1) < GB_DAG_POLLERS;
+    unsigned smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    smid %= GB_DAG_NSMF;
+    if (role) {
+        atomicExch(D.smflag + smid, D.epoch);
+    } else if (gridDim.x >= 4 * GB_DAG_POLLERS && dag_ld_acquire(D.smflag + smid) == D.epoch
+               && atomicAdd(D.ctrl + 8, 1) < 2 * GB_DAG_POLLERS) {
+        role = 2;
+    }
+    return role;
 }
 
 template <typename T>
@@ -136,37 +167,105 @@ __host__ __device__ constexpr size_t dag_smem()
     return sizeof(T) * (3 * 64 * 65);
 }
 
+// The work of one tile task (POTRF, TRSM, UPD or CB) of supernode tk.s.
+// smem_raw: dag_smem<T>() bytes.
+template <typename T>
+__device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx, T *CB, T *Linv,
+                              unsigned char *smem_raw, int &sfail)
+{
+    T (*A)[65] = (T (*)[65])smem_raw;
+    T *S1 = (T *)smem_raw + 64 * 65, *S2 = S1 + 64 * 65;
+    const int s = tk.s;
+    const int nscol = (int)(P.Super[s + 1] - P.Super[s]);
+    const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
+    T *panel = Lx + P.Px[s];
+    const int f = P.fail[s];
+    if (tk.type == GB_DT_POTRF) {
+        const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
+        if (f < 0) {
+            T *blk = panel + c0 + (int64_t)c0 * nsrow;
+            for (int idx = threadIdx.x; idx < 64 * 64; idx += blockDim.x) {
+                const int i = idx & 63, j = idx >> 6;
+                A[i][j] = (i < nb && j < nb && i >= j) ? blk[i + (int64_t)j * nsrow] : (T)0;
+            }
+            __syncthreads();
+            const int fl = potrf_inv64<T>(A, S1, S2, nb, &sfail);
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+                const int i = idx % nb, j = idx / nb;
+                if (i >= j) blk[i + (int64_t)j * nsrow] = A[i][j];
+            }
+            if (fl >= 0 && threadIdx.x == 0) {
+                P.fail[s] = c0 + fl;
+                atomicExch(P.anyfail, 1);
+            }
+            T *li = Linv + P.linvoff[P.blkoff[s] + tk.b];
+            for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+                const int i = idx % nb, j = idx / nb;
+                li[i + (int64_t)j * nb] = S1[j * 65 + i];
+            }
+        }
+    } else if (tk.type == GB_DT_TRSM) {
+        const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
+        if (!(f >= 0 && f < c0)) {
+            const int ncols = (f >= 0) ? f - c0 : nb;
+            const int r0 = max(64 * tk.r, c0 + nb), r1 = min(64 * tk.r + 64, nsrow);
+            const int nr = r1 - r0;
+            const T *li = Linv + P.linvoff[P.blkoff[s] + tk.b];
+            for (int idx = threadIdx.x; idx < 64 * 64; idx += blockDim.x) {
+                const int cc = idx & 63, k = idx >> 6;
+                S2[k * 65 + cc] = (cc < nb && k < nb) ? li[cc + (int64_t)k * nb] : (T)0;
+                S1[k * 65 + cc] = (cc < nr && k < nb) ? panel[r0 + cc + (int64_t)(c0 + k) * nsrow] : (T)0;
+            }
+            __syncthreads();
+            trsm_tile<T>(S1, S2, 65, nr, nb, ncols, panel + r0 + (int64_t)c0 * nsrow, nsrow);
+        }
+    } else if (tk.type == GB_DT_UPD) {
+        if (f < 0) {
+            const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
+            const int cs = 64 * tk.c, ce = min(cs + 64, nscol);
+            const int rs = max(64 * tk.r, cs), re = min(64 * tk.r + 64, nsrow);
+            if constexpr (sizeof(T) == 4)
+                gemm_tile_f32(panel + rs + (int64_t)c0 * nsrow, nsrow,
+                              panel + cs + (int64_t)c0 * nsrow, nsrow,
+                              panel + rs + (int64_t)cs * nsrow, nsrow,
+                              re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, (float *)smem_raw);
+            else
+                gemm_tile_k64<T>(panel + rs + (int64_t)c0 * nsrow, nsrow,
+                                 panel + cs + (int64_t)c0 * nsrow, nsrow,
+                                 panel + rs + (int64_t)cs * nsrow, nsrow,
+                                 re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, S1, S2);
+        }
+    } else {  // GB_DT_CB
+        if (f < 0) {
+            const int m = nsrow - nscol;
+            const int I = 64 * tk.r, J = 64 * tk.c;
+            if constexpr (sizeof(T) == 4)
+                gemm_tile_f32(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
+                              CB + P.cboff[s] + I + (int64_t)J * m, m,
+                              min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
+                              (float *)smem_raw);
+            else
+                gemm_tile_nt<T>(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
+                                CB + P.cboff[s] + I + (int64_t)J * m, m,
+                                min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
+                                S1, S2);
+        }
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256, 2)
 k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T (*A)[65] = (T (*)[65])smem_raw;
-    T *S1 = (T *)smem_raw + 64 * 65, *S2 = S1 + 64 * 65;
     __shared__ int sid, sfail, spoll;
-    if (threadIdx.x == 0) {
-        // The first GB_DAG_POLLERS blocks to start serve the critical queue
-        // and mark their SM.  The critical path is a chain of latency-bound
-        // tasks, so a bulk block that finds itself on a marked SM leaves
-        // (at most 2 GB_DAG_POLLERS of them, and only in a large grid, so
-        // that plenty of bulk blocks remain).
-        int role = atomicAdd(D.ctrl + 4, 1) < GB_DAG_POLLERS;
-        unsigned smid;
-        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-        smid %= GB_DAG_NSMF;
-        if (role) {
-            atomicExch(D.smflag + smid, D.epoch);
-        } else if (gridDim.x >= 4 * GB_DAG_POLLERS && dag_ld_acquire(D.smflag + smid) == D.epoch
-                   && atomicAdd(D.ctrl + 8, 1) < 2 * GB_DAG_POLLERS) {
-            role = 2;
-        }
-        spoll = role;
-    }
+    if (threadIdx.x == 0) spoll = dag_role(D.Q);
     __syncthreads();
     if (spoll == 2) return;
     const int poller = spoll;
     for (;;) {
-        if (threadIdx.x == 0) sid = dag_pop(D, poller);
+        if (threadIdx.x == 0) sid = dag_pop(D.Q, poller);
         __syncthreads();
         const int id = sid;
         if (id < 0) return;
@@ -175,83 +274,7 @@ k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
             D.trace[3 * (size_t)id + 2] = blockIdx.x;
         }
         const gb_dtask tk = D.tasks[id];
-        const int s = tk.s;
-        const int nscol = (int)(P.Super[s + 1] - P.Super[s]);
-        const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
-        T *panel = Lx + P.Px[s];
-        const int f = P.fail[s];
-        if (tk.type == GB_DT_POTRF) {
-            const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
-            if (f < 0) {
-                T *blk = panel + c0 + (int64_t)c0 * nsrow;
-                for (int idx = threadIdx.x; idx < 64 * 64; idx += blockDim.x) {
-                    const int i = idx & 63, j = idx >> 6;
-                    A[i][j] = (i < nb && j < nb && i >= j) ? blk[i + (int64_t)j * nsrow] : (T)0;
-                }
-                __syncthreads();
-                const int fl = potrf_inv64<T>(A, S1, S2, nb, &sfail);
-                __syncthreads();
-                for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
-                    const int i = idx % nb, j = idx / nb;
-                    if (i >= j) blk[i + (int64_t)j * nsrow] = A[i][j];
-                }
-                if (fl >= 0 && threadIdx.x == 0) {
-                    P.fail[s] = c0 + fl;
-                    atomicExch(P.anyfail, 1);
-                }
-                T *li = Linv + P.linvoff[P.blkoff[s] + tk.b];
-                for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
-                    const int i = idx % nb, j = idx / nb;
-                    li[i + (int64_t)j * nb] = S1[j * 65 + i];
-                }
-            }
-        } else if (tk.type == GB_DT_TRSM) {
-            const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
-            if (!(f >= 0 && f < c0)) {
-                const int ncols = (f >= 0) ? f - c0 : nb;
-                const int r0 = max(64 * tk.r, c0 + nb), r1 = min(64 * tk.r + 64, nsrow);
-                const int nr = r1 - r0;
-                const T *li = Linv + P.linvoff[P.blkoff[s] + tk.b];
-                for (int idx = threadIdx.x; idx < 64 * 64; idx += blockDim.x) {
-                    const int cc = idx & 63, k = idx >> 6;
-                    S2[k * 65 + cc] = (cc < nb && k < nb) ? li[cc + (int64_t)k * nb] : (T)0;
-                    S1[k * 65 + cc] = (cc < nr && k < nb) ? panel[r0 + cc + (int64_t)(c0 + k) * nsrow] : (T)0;
-                }
-                __syncthreads();
-                trsm_tile<T>(S1, S2, 65, nr, nb, ncols, panel + r0 + (int64_t)c0 * nsrow, nsrow);
-            }
-        } else if (tk.type == GB_DT_UPD) {
-            if (f < 0) {
-                const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
-                const int cs = 64 * tk.c, ce = min(cs + 64, nscol);
-                const int rs = max(64 * tk.r, cs), re = min(64 * tk.r + 64, nsrow);
-                if constexpr (sizeof(T) == 4)
-                    gemm_tile_f32(panel + rs + (int64_t)c0 * nsrow, nsrow,
-                                  panel + cs + (int64_t)c0 * nsrow, nsrow,
-                                  panel + rs + (int64_t)cs * nsrow, nsrow,
-                                  re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, (float *)smem_raw);
-                else
-                    gemm_tile_k64<T>(panel + rs + (int64_t)c0 * nsrow, nsrow,
-                                     panel + cs + (int64_t)c0 * nsrow, nsrow,
-                                     panel + rs + (int64_t)cs * nsrow, nsrow,
-                                     re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, S1, S2);
-            }
-        } else {  // GB_DT_CB
-            if (f < 0) {
-                const int m = nsrow - nscol;
-                const int I = 64 * tk.r, J = 64 * tk.c;
-                if constexpr (sizeof(T) == 4)
-                    gemm_tile_f32(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
-                                  CB + P.cboff[s] + I + (int64_t)J * m, m,
-                                  min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
-                                  (float *)smem_raw);
-                else
-                    gemm_tile_nt<T>(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
-                                    CB + P.cboff[s] + I + (int64_t)J * m, m,
-                                    min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
-                                    S1, S2);
-            }
-        }
+        dag_tile_task<T>(P, tk, Lx, CB, Linv, smem_raw, sfail);
         __syncthreads();
         if (threadIdx.x < 32) {
             if (D.trace && threadIdx.x == 0) D.trace[3 * (size_t)id + 1] = dag_timer();
@@ -260,7 +283,155 @@ k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
     }
 }
 
+// ---------------------------------------------------------------------------
+// whole-factorization executor: every level's tile tasks, the assembly
+// chunks and the small supernodes of one or more instances of a pattern in
+// one persistent launch (graph built by gb_plan.c: fdag_build)
+// ---------------------------------------------------------------------------
+
+struct gb_fdag_dev {
+    gb_dq Q;
+    const gb_fpat *pats;
+    const gb_finst *inst;
+    const int64_t *ibase;
+    int ninst;
+    int32_t *cnt;
+    unsigned long long *trace;
+    const void *Sx;
+    int a_dtype;
+    const double *scale;
+    double beta;
+};
+
+// thread 0: the instance that owns global task id (ibase ascending)
+__device__ __forceinline__ int fdag_instance(const gb_fdag_dev &D, int id)
+{
+    int lo = 0, hi = D.ninst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (D.ibase[mid] <= id) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256, 2)
+k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int sid, sinst, sfail, spoll;
+    if (threadIdx.x == 0) spoll = dag_role(D.Q);
+    __syncthreads();
+    if (spoll == 2) return;
+    const int poller = spoll;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            sid = dag_pop(D.Q, poller);
+            if (sid >= 0) sinst = fdag_instance(D, sid);
+        }
+        __syncthreads();
+        const int id = sid;
+        if (id < 0) return;
+        if (D.trace && threadIdx.x == 0) {
+            D.trace[3 * (size_t)id] = dag_timer();
+            D.trace[3 * (size_t)id + 2] = blockIdx.x;
+        }
+        const gb_finst I = D.inst[sinst];
+        const gb_fpat &PP = D.pats[I.pat];
+        const int local = (int)(id - I.base);
+        const gb_dtask tk = PP.tasks[local];
+        gb_dev_pattern P = gb_to_dev(&PP.pp);
+        P.fail = I.fail;
+        P.anyfail = I.anyfail;
+        T *Lx = LxB + I.lx, *CB = CBB + I.cb, *Linv = LinvB + I.linv;
+        if (tk.type == GB_DT_ASM) {
+            const gb_asm_task a = {tk.s, tk.b, tk.r, 0};
+            const double *scale = D.scale ? D.scale + I.scale : nullptr;
+            if (D.a_dtype == 0)
+                assemble_body<double, T>(P, a, PP.Sp, PP.Si, (const double *)D.Sx + I.sx, scale,
+                                         D.beta, Lx, CB);
+            else
+                assemble_body<float, T>(P, a, PP.Sp, PP.Si, (const float *)D.Sx + I.sx, scale,
+                                        D.beta, Lx, CB);
+        } else if (tk.type == GB_DT_SMALL) {
+            factor_small_body<T>(P, tk.s, Lx, Linv, smem_raw, &sfail);
+        } else if (tk.type == GB_DT_NODE) {
+            // assembly chunk by chunk, LL', then every update-block tile
+            const int s = tk.s;
+            const int nscol = (int)(P.Super[s + 1] - P.Super[s]);
+            const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
+            const int m = nsrow - nscol;
+            const double *scale = D.scale ? D.scale + I.scale : nullptr;
+            for (int t0 = 0; t0 < nsrow; t0 += 64) {
+                const gb_asm_task a = {s, t0, min(t0 + 64, nsrow), 0};
+                if (D.a_dtype == 0)
+                    assemble_body<double, T>(P, a, PP.Sp, PP.Si, (const double *)D.Sx + I.sx,
+                                             scale, D.beta, Lx, CB);
+                else
+                    assemble_body<float, T>(P, a, PP.Sp, PP.Si, (const float *)D.Sx + I.sx,
+                                            scale, D.beta, Lx, CB);
+                __syncthreads();
+            }
+            factor_small_body<T>(P, s, Lx, Linv, smem_raw, &sfail);
+            __syncthreads();
+            for (int J = 0; J < m; J += 64)
+                for (int I0 = J; I0 < m; I0 += 64) {
+                    const gb_dtask ct = {GB_DT_CB, s, 0, I0 / 64, J / 64, 1, 0, 0};
+                    dag_tile_task<T>(P, ct, Lx, CB, Linv, smem_raw, sfail);
+                    __syncthreads();
+                }
+        } else {
+            dag_tile_task<T>(P, tk, Lx, CB, Linv, smem_raw, sfail);
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            if (D.trace && threadIdx.x == 0) D.trace[3 * (size_t)id + 1] = dag_timer();
+            __threadfence();
+            const int e0 = PP.succ_ptr[local], e1 = PP.succ_ptr[local + 1];
+            for (int e = e0 + (int)threadIdx.x; e < e1; e += 32) {
+                const int v = PP.succ[e];
+                const int g = (int)(I.base + v);
+                if (dag_add_acq_rel(D.cnt + g, -1) != 1) continue;
+                if (PP.tasks[v].type != GB_DT_JOIN) {
+                    dag_push(D.Q, g, PP.tasks[v].prio);
+                    continue;
+                }
+                // a join (no work, never queued): release its successors here;
+                // they are never joins themselves
+                for (int f = PP.succ_ptr[v]; f < PP.succ_ptr[v + 1]; f++) {
+                    const int w = PP.succ[f];
+                    const int gw = (int)(I.base + w);
+                    if (dag_add_acq_rel(D.cnt + gw, -1) == 1) dag_push(D.Q, gw, PP.tasks[w].prio);
+                }
+            }
+        }
+    }
+}
+
 extern "C" {
+
+int gb_launch_fdag(const gb_fdag_args *a, void *Lx, void *CB, void *Linv, int dtype, int grid,
+                   cudaStream_t st)
+{
+    if (a->ntotal <= 0) return 0;
+    gb_fdag_dev D;
+    D.Q.q0 = a->q0; D.Q.q1 = a->q1; D.Q.ctrl = a->ctrl; D.Q.err = a->err;
+    D.Q.smflag = a->smflag; D.Q.epoch = a->epoch;
+    D.pats = a->pats; D.inst = a->inst; D.ibase = a->inst_base; D.ninst = a->ninst;
+    D.cnt = a->cnt; D.trace = a->trace;
+    D.Sx = a->Sx; D.a_dtype = a->a_dtype; D.scale = a->scale; D.beta = a->beta;
+    static int configured = 0;
+    if (!configured) {
+        cudaFuncSetAttribute(k_fdag<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<double>());
+        cudaFuncSetAttribute(k_fdag<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<float>());
+        configured = 1;
+    }
+    if (grid > a->ntotal + GB_DAG_POLLERS) grid = (int)(a->ntotal + GB_DAG_POLLERS);
+    if (grid < GB_DAG_POLLERS + 1) grid = GB_DAG_POLLERS + 1;
+    if (dtype == 0) k_fdag<double><<<grid, 256, dag_smem<double>(), st>>>(D, (double *)Lx, (double *)CB, (double *)Linv);
+    else k_fdag<float><<<grid, 256, dag_smem<float>(), st>>>(D, (float *)Lx, (float *)CB, (float *)Linv);
+    return (int)cudaGetLastError();
+}
 
 int gb_launch_dag(const gb_pattern_ptrs *pp, const gb_dag_args *a, void *Lx, void *CB,
                   void *Linv, int dtype, int grid, cudaStream_t st)
@@ -269,9 +440,9 @@ int gb_launch_dag(const gb_pattern_ptrs *pp, const gb_dag_args *a, void *Lx, voi
     gb_dev_pattern P = gb_to_dev(pp);
     gb_dag_dev D;
     D.tasks = a->tasks; D.ntasks = a->ntasks; D.succ_ptr = a->succ_ptr; D.succ = a->succ;
-    D.cnt = a->cnt; D.q0 = a->q0; D.q1 = a->q1; D.ctrl = a->ctrl; D.err = a->err;
-    D.trace = a->trace;
-    D.smflag = a->smflag; D.epoch = a->epoch;
+    D.cnt = a->cnt; D.trace = a->trace;
+    D.Q.q0 = a->q0; D.Q.q1 = a->q1; D.Q.ctrl = a->ctrl; D.Q.err = a->err;
+    D.Q.smflag = a->smflag; D.Q.epoch = a->epoch;
     static int configured = 0;
     if (!configured) {
         cudaFuncSetAttribute(k_dag<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<double>());

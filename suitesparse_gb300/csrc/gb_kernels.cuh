@@ -57,6 +57,19 @@ typedef struct { int32_t type, s, b, r, c, prio, pad0, pad1; } gb_dtask;
 #define GB_DT_TRSM  2
 #define GB_DT_UPD   3
 #define GB_DT_CB    4
+/* tasks of the whole-factorization graph (gb_plan.c):
+ *   ASM   (s, b = t0, r = t1)  assembly of front columns [t0, t1) of s
+ *   SMALL (s)                  whole supernode at most GB_SMALL_MAX wide
+ *   JOIN  (s)                  no work: fan-in of a supernode's assembly
+ *                              chunks, or of its children's update blocks
+ *                              (also marks tasks folded into a NODE task) */
+#define GB_DT_ASM   5
+#define GB_DT_SMALL 6
+#define GB_DT_JOIN  7
+/*   NODE  (s)                  a small supernode whole: assembly, LL' and
+ *                              every update-block tile, in one task */
+#define GB_DT_NODE  8
+#define GB_NODE_MAX_ROWS 256        /* small supernodes fused into NODE tasks */
 
 /* control words of one task-graph launch: [0] head0 [1] tail0 [2] head1
  * [3] tail1 [4] blocks started [5] error [6] total0 [7] total1 [8] blocks

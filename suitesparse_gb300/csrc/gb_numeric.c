@@ -26,6 +26,7 @@ gb_ctx *gb_ctx_new(void)
     c->opt_small = GB_SMALL_MAX;
     c->device = -1;
     c->sweep_mode = 1;
+    c->factor_mode = 1;
     return c;
 }
 
@@ -69,6 +70,7 @@ int gb300_set_option(cholmod_common *Common, int option, int64_t value)
     if (!c) { GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "out of memory"); return FALSE; }
     if (option == GB300_OPT_KEEP_ON_DEVICE) c->opt_keep = value ? 1 : 0;
     else if (option == GB300_OPT_SWEEP) c->sweep_mode = value ? 1 : 0;
+    else if (option == GB300_OPT_FACTOR) c->factor_mode = value ? 1 : 0;
     else if (option == GB300_OPT_TRACE) c->trace_on = value ? 1 : 0;
     else if (option == GB300_OPT_PROFILE) {
         c->prof = value ? 1 : 0;
@@ -291,6 +293,65 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
     CU(cudaMemsetAsync(P->d_fail, 0xFF, sizeof(int32_t) * (P->nsuper + 1), st));
     CU(cudaMemsetAsync(P->d_anyfail, 0, sizeof(int32_t), st));
     CU(cudaMemsetAsync(P->d_ticket + 3, 0, sizeof(int32_t), st));
+    if (ctx->factor_mode == 1) {
+        /* one persistent launch over the whole-factorization task graph */
+        size_t N = P->fd_t.n, n0 = P->fd_q0.n, n1 = P->fd_q1.n;
+        gb_fpat *hp = &P->h_fd_pat;
+        hp->pp = P->ptrs;
+        hp->tasks = P->d_fd_t;
+        hp->succ_ptr = P->d_fd_sp;
+        hp->succ = P->d_fd_succ;
+        hp->Sp = P->d_Sp;
+        hp->Si = P->d_Si;
+        hp->ntasks = (int32_t)N;
+        if (prof) CU(cudaEventRecord(ctx->pev[0], st));
+        CU(cudaMemcpyAsync(P->d_fd_pat, hp, sizeof *hp, cudaMemcpyHostToDevice, st));
+        CU(cudaMemcpyAsync(P->d_fd_cnt, P->d_fd_nd, sizeof(int32_t) * N, cudaMemcpyDeviceToDevice, st));
+        CU(cudaMemsetAsync(P->d_fd_q, 0xFF, sizeof(int32_t) * 2 * N, st));
+        if (n0) CU(cudaMemcpyAsync(P->d_fd_q, P->d_fd_qi, sizeof(int32_t) * n0, cudaMemcpyDeviceToDevice, st));
+        if (n1) CU(cudaMemcpyAsync(P->d_fd_q + N, P->d_fd_qi + n0, sizeof(int32_t) * n1, cudaMemcpyDeviceToDevice, st));
+        CU(cudaMemcpyAsync(P->d_dag_ctrl, P->d_fd_ctrl0, sizeof(int32_t) * GB_DAG_NCTRL, cudaMemcpyDeviceToDevice, st));
+        gb_fdag_args a;
+        memset(&a, 0, sizeof a);
+        a.pats = P->d_fd_pat;
+        a.inst = P->d_fd_inst;
+        a.inst_base = P->d_fd_ibase;
+        a.ninst = 1;
+        a.ntotal = (int64_t)N;
+        a.cnt = P->d_fd_cnt;
+        a.q0 = P->d_fd_q;
+        a.q1 = P->d_fd_q + N;
+        a.ctrl = P->d_dag_ctrl;
+        a.err = P->d_ticket + 3;
+        a.smflag = P->d_dag_smf;
+        if (++P->dag_epoch <= 0) P->dag_epoch = 1;
+        a.epoch = P->dag_epoch;
+        a.Sx = Sx;
+        a.a_dtype = adt;
+        a.scale = scale;
+        a.beta = beta;
+        if (ctx->trace_on) {
+            size_t need = 3 * (N + 1) * sizeof(unsigned long long);
+            if (gb_dev_grow((void **)&ctx->d_ftrace, &ctx->ftrace_cap, need)) {
+                a.trace = ctx->d_ftrace;
+                ctx->ftrace_n = (int64_t)N;
+            }
+        }
+        int grid = GB_MAX(1, ctx->sms) * 2;   /* resident blocks per SM */
+        LK(gb_launch_fdag(&a, Lx, CB, Linv, ldt, grid, st));
+        if (prof) {
+            CU(cudaEventRecord(ctx->pev[1], st));
+            CU(cudaStreamSynchronize(st));
+            float ms = 0;
+            CU(cudaEventElapsedTime(&ms, ctx->pev[0], ctx->pev[1]));
+            ctx->kind_ms[GB_K_FDAG] += ms;
+            ctx->kind_n[GB_K_FDAG] += 1;
+        }
+        ctx->stats[4] = 1;
+        ctx->launches += 1;
+        P->linv_valid[d] = 1;
+        return TRUE;
+    }
     for (size_t i = 0; i < P->fact_seq.n; i++) {
         const gb_launch_rec *r = &seq[i];
         if (prof) CU(cudaEventRecord(ctx->pev[2 * i], st));

@@ -85,6 +85,181 @@ static int push_launch(gb_vec *seq, int kind, size_t count, size_t off)
     return gb_vec_push(seq, &r);
 }
 
+/* Whole-factorization task graph from the per-level graphs: local ids
+ * [0, ndag) are the level-graph tasks (same order), then the assembly
+ * chunks, the small supernodes, JA(s) (s assembled) and JK(s) (the update
+ * blocks of all children of s are complete).  Edges: the level graphs' own;
+ * ASM(s, *) -> JA(s) -> SMALL(s) or POTRF(s, block 0); SMALL(s) -> CB(s, *);
+ * CB(c, *) -> JK(parent c) -> ASM(parent c, *) (a leaf's JK has no edges).
+ * Joins carry no work and are never queued.  Every task of s follows
+ * JA(s), so the front is assembled before any tile task touches it, and the
+ * parent's assembly follows every update-block tile of every child. */
+static int fdag_build(gb_plan *P)
+{
+    const int64_t ns = P->nsuper;
+    const size_t ndag = P->dag_t.n, nasm = P->asm_t.n;
+    const gb_dtask *dt = P->dag_t.p;
+    const gb_asm_task *at = P->asm_t.p;
+    const gb_node_task *nt = P->node_t.p;
+    const gb_launch_rec *seq = P->fact_seq.p;
+    size_t nsmall = 0;
+    for (size_t i = 0; i < P->fact_seq.n; i++)
+        if (seq[i].kind == GB_K_SMALL) nsmall += (size_t)seq[i].count;
+    const size_t A0 = ndag, S0 = A0 + nasm, JA0 = S0 + nsmall, JK0 = JA0 + (size_t)ns;
+    const size_t N = JK0 + (size_t)ns;
+    if (N >= (size_t)1 << 30) return 0;
+    int ok = 1;
+    int32_t *potrf0 = malloc(sizeof(int32_t) * (ns + 1));
+    int32_t *small_id = malloc(sizeof(int32_t) * (ns + 1));
+    int32_t *cbp = calloc(ns + 2, sizeof(int32_t));
+    int32_t *cbl = malloc(sizeof(int32_t) * (ndag + 1));
+    int32_t *deg = NULL, *nd = NULL, *pos = NULL, *succ = NULL, *tmp = NULL;
+    gb_vec E;
+    vec_init(&E, 2 * sizeof(int32_t));
+    if (!potrf0 || !small_id || !cbp || !cbl) ok = 0;
+    for (int64_t s = 0; ok && s < ns; s++) potrf0[s] = small_id[s] = -1;
+    /* small supernodes with few rows run whole as one NODE task: their
+     * assembly chunks and update-block tiles stay in the list as inert
+     * joins without edges */
+    const int64_t *Pi = P->L->pi, *Sup = P->L->super;
+#define FUSED(s) (Sup[(s) + 1] - Sup[s] <= P->small_cols && Pi[(s) + 1] - Pi[s] <= GB_NODE_MAX_ROWS)
+    /* tasks */
+    for (size_t i = 0; ok && i < ndag; i++) {
+        gb_dtask t = dt[i];
+        if (t.type == GB_DT_POTRF && t.b == 0) potrf0[t.s] = (int32_t)i;
+        if (t.type == GB_DT_CB) {
+            if (FUSED(t.s)) t.type = GB_DT_JOIN;
+            else cbp[t.s + 2]++;
+        }
+        ok &= gb_vec_push(&P->fd_t, &t);
+    }
+    for (size_t i = 0; ok && i < nasm; i++) {
+        gb_dtask t = {FUSED(at[i].s) ? GB_DT_JOIN : GB_DT_ASM, at[i].s, at[i].t0, at[i].t1, 0, 1, 0, 0};
+        ok &= gb_vec_push(&P->fd_t, &t);
+    }
+    {
+        size_t k = 0;
+        for (size_t i = 0; ok && i < P->fact_seq.n; i++) {
+            if (seq[i].kind != GB_K_SMALL) continue;
+            for (int32_t q = 0; ok && q < seq[i].count; q++) {
+                int32_t s = nt[seq[i].off + q].s;
+                gb_dtask t = {FUSED(s) ? GB_DT_NODE : GB_DT_SMALL, s, 0, 0, 0, 1, 0, 0};
+                small_id[s] = (int32_t)(S0 + k++);
+                ok &= gb_vec_push(&P->fd_t, &t);
+            }
+        }
+    }
+    for (int w = 0; w < 2 && ok; w++)
+        for (int64_t s = 0; ok && s < ns; s++) {
+            gb_dtask t = {GB_DT_JOIN, (int32_t)s, w, 0, 0, 0, 0, 0};
+            ok &= gb_vec_push(&P->fd_t, &t);
+        }
+    /* update-block tiles of each supernode (CSR by supernode) */
+    for (int64_t s = 0; ok && s < ns; s++) cbp[s + 2] += cbp[s + 1];
+    for (size_t i = 0; ok && i < ndag; i++)
+        if (dt[i].type == GB_DT_CB && !FUSED(dt[i].s)) cbl[cbp[dt[i].s + 1]++] = (int32_t)i;
+    /* edges */
+    const gb_dag_level *lv = P->dag_lv.p;
+    const int32_t *lsp = P->dag_sp.p, *lsucc = P->dag_succ.p;
+    for (size_t l = 0; ok && l < P->dag_lv.n; l++) {
+        for (int32_t t = 0; ok && t < lv[l].ntasks; t++) {
+            int32_t e0 = lsp[lv[l].sp_off + t], e1 = lsp[lv[l].sp_off + t + 1];
+            for (int32_t e = e0; ok && e < e1; e++) {
+                int32_t ed[2] = {(int32_t)(lv[l].task_off + t),
+                                 (int32_t)(lv[l].task_off + lsucc[lv[l].succ_off + e])};
+                ok &= gb_vec_push(&E, ed);
+            }
+        }
+    }
+    for (size_t i = 0; ok && i < nasm; i++) {
+        int32_t a = (int32_t)(A0 + i), s = at[i].s;
+        if (FUSED(s)) continue;
+        int32_t e1[2] = {a, (int32_t)(JA0 + s)}, e2[2] = {(int32_t)(JK0 + s), a};
+        ok &= gb_vec_push(&E, e1);
+        if (P->h_child_ptr[s + 1] > P->h_child_ptr[s]) ok &= gb_vec_push(&E, e2);
+    }
+    for (int64_t s = 0; ok && s < ns; s++) {
+        int32_t ja = (int32_t)(JA0 + s);
+        if (FUSED(s)) {
+            /* JK(s) -> NODE(s) -> JK(parent) */
+            if (small_id[s] < 0) { ok = 0; break; }
+            if (P->h_child_ptr[s + 1] > P->h_child_ptr[s]) {
+                int32_t e[2] = {(int32_t)(JK0 + s), small_id[s]};
+                ok &= gb_vec_push(&E, e);
+            }
+            int32_t par = P->h_parent[s];
+            if (par >= 0) {
+                int32_t e[2] = {small_id[s], (int32_t)(JK0 + par)};
+                ok &= gb_vec_push(&E, e);
+            }
+            continue;
+        }
+        if (small_id[s] >= 0) {
+            int32_t e[2] = {ja, small_id[s]};
+            ok &= gb_vec_push(&E, e);
+            for (int32_t q = cbp[s]; ok && q < cbp[s + 1]; q++) {
+                int32_t e2[2] = {small_id[s], cbl[q]};
+                ok &= gb_vec_push(&E, e2);
+            }
+        } else if (potrf0[s] >= 0) {
+            int32_t e[2] = {ja, potrf0[s]};
+            ok &= gb_vec_push(&E, e);
+        } else {
+            ok = 0;                       /* every supernode has one of them */
+        }
+        int32_t par = P->h_parent[s];
+        if (par >= 0)
+            for (int32_t q = cbp[s]; ok && q < cbp[s + 1]; q++) {
+                int32_t e[2] = {cbl[q], (int32_t)(JK0 + par)};
+                ok &= gb_vec_push(&E, e);
+            }
+    }
+    /* CSR, critical successors first; in-degrees; initial ready lists */
+    if (ok) {
+        deg = calloc(N + 1, sizeof(int32_t));
+        nd = calloc(N + 1, sizeof(int32_t));
+        pos = malloc(sizeof(int32_t) * (N + 1));
+        succ = malloc(sizeof(int32_t) * (E.n + 1));
+        tmp = malloc(sizeof(int32_t) * (E.n + 1));
+        if (!deg || !nd || !pos || !succ || !tmp) ok = 0;
+    }
+    if (ok) {
+        const int32_t *ed = E.p;
+        const gb_dtask *ft = P->fd_t.p;
+        for (size_t q = 0; q < E.n; q++) { deg[ed[2 * q] + 1]++; nd[ed[2 * q + 1]]++; }
+        for (size_t t = 0; t < N; t++) deg[t + 1] += deg[t];
+        memcpy(pos, deg, sizeof(int32_t) * (N + 1));
+        for (size_t q = 0; q < E.n; q++) succ[pos[ed[2 * q]]++] = ed[2 * q + 1];
+        for (size_t t = 0; t < N; t++) {
+            int32_t w = deg[t];
+            for (int pass = 0; pass < 2; pass++)
+                for (int32_t e = deg[t]; e < deg[t + 1]; e++)
+                    if ((ft[succ[e]].prio == 0) == (pass == 0)) tmp[w++] = succ[e];
+            memcpy(succ + deg[t], tmp + deg[t], sizeof(int32_t) * (deg[t + 1] - deg[t]));
+        }
+        for (size_t t = 0; ok && t <= N; t++) ok &= gb_vec_push(&P->fd_sp, &deg[t]);
+        for (size_t q = 0; ok && q < E.n; q++) ok &= gb_vec_push(&P->fd_succ, &succ[q]);
+        /* joins are never queued: the block that finishes a join's last
+         * predecessor releases its successors itself */
+        P->fd_total0 = P->fd_total1 = 0;
+        for (size_t t = 0; ok && t < N; t++) {
+            int32_t id = (int32_t)t;
+            ok &= gb_vec_push(&P->fd_nd, &nd[t]);
+            if (ft[t].type == GB_DT_JOIN) {
+                if (nd[t] == 0 && deg[t + 1] > deg[t]) ok = 0;   /* never released */
+                continue;
+            }
+            if (ft[t].prio == 0) P->fd_total0++; else P->fd_total1++;
+            if (nd[t] == 0) ok &= gb_vec_push(ft[t].prio == 0 ? &P->fd_q0 : &P->fd_q1, &id);
+        }
+    }
+#undef FUSED
+    free(potrf0); free(small_id); free(cbp); free(cbl);
+    free(deg); free(nd); free(pos); free(succ); free(tmp);
+    gb_vec_free(&E);
+    return ok;
+}
+
 gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
 {
     if (small_cols < 1) small_cols = 1;
@@ -96,6 +271,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
     gb_plan *P = calloc(1, sizeof(gb_plan));
     if (!P) return NULL;
     P->L = L;
+    P->small_cols = small_cols;
     P->super_ptr = L->super;
     P->s_ptr = L->s;
     P->pi_ptr = L->pi;
@@ -122,6 +298,12 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
     vec_init(&P->dag_q0, sizeof(int32_t));
     vec_init(&P->dag_q1, sizeof(int32_t));
     vec_init(&P->dag_lv, sizeof(gb_dag_level));
+    vec_init(&P->fd_t, sizeof(gb_dtask));
+    vec_init(&P->fd_sp, sizeof(int32_t));
+    vec_init(&P->fd_succ, sizeof(int32_t));
+    vec_init(&P->fd_nd, sizeof(int32_t));
+    vec_init(&P->fd_q0, sizeof(int32_t));
+    vec_init(&P->fd_q1, sizeof(int32_t));
     vec_init(&P->fwd_seq, sizeof(gb_launch_rec));
     vec_init(&P->bwd_seq, sizeof(gb_launch_rec));
 
@@ -588,6 +770,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
     P->h_cboff = cboff;
     P->h_cbvoff = cbvoff;
     free(SuperMap); free(parent); free(level); free(Map); free(lev_ptr); free(lev_list);
+    if (!fdag_build(P)) { gb_plan_free(P); return NULL; }
     return P;
 
 fail:
@@ -693,6 +876,40 @@ int gb_plan_upload(gb_plan *P)
     P->ptrs.anyfail = P->d_anyfail;
     P->ptrs.blkoff = P->d_blkoff;
     P->ptrs.linvoff = P->d_linvoff;
+    /* whole-factorization task graph, one instance */
+    UP(P->d_fd_t, P->fd_t.p, P->fd_t.n * P->fd_t.esz);
+    UP(P->d_fd_sp, P->fd_sp.p, P->fd_sp.n * P->fd_sp.esz);
+    UP(P->d_fd_succ, P->fd_succ.p, P->fd_succ.n * P->fd_succ.esz);
+    UP(P->d_fd_nd, P->fd_nd.p, P->fd_nd.n * P->fd_nd.esz);
+    {
+        size_t n0 = P->fd_q0.n, n1 = P->fd_q1.n, N = P->fd_t.n;
+        int32_t *qi = malloc(sizeof(int32_t) * (n0 + n1 + 1));
+        if (!qi) goto fail;
+        if (n0) memcpy(qi, P->fd_q0.p, sizeof(int32_t) * n0);
+        if (n1) memcpy(qi + n0, P->fd_q1.p, sizeof(int32_t) * n1);
+        int okq = cudaMalloc((void **)&P->d_fd_qi, sizeof(int32_t) * (n0 + n1 + 1)) == cudaSuccess
+                  && cudaMemcpy(P->d_fd_qi, qi, sizeof(int32_t) * (n0 + n1), cudaMemcpyHostToDevice) == cudaSuccess;
+        free(qi);
+        if (!okq) goto fail;
+        int32_t ctrl0[GB_DAG_NCTRL];
+        memset(ctrl0, 0, sizeof ctrl0);
+        ctrl0[1] = (int32_t)n0;
+        ctrl0[3] = (int32_t)n1;
+        ctrl0[6] = P->fd_total0;
+        ctrl0[7] = P->fd_total1;
+        UP(P->d_fd_ctrl0, ctrl0, sizeof ctrl0);
+        if (cudaMalloc((void **)&P->d_fd_cnt, sizeof(int32_t) * (N + 1)) != cudaSuccess) goto fail;
+        if (cudaMalloc((void **)&P->d_fd_q, sizeof(int32_t) * 2 * (N + 1)) != cudaSuccess) goto fail;
+        gb_finst inst;
+        memset(&inst, 0, sizeof inst);
+        inst.fail = P->d_fail;
+        inst.anyfail = P->d_anyfail;
+        UP(P->d_fd_inst, &inst, sizeof inst);
+        int64_t ib = 0;
+        UP(P->d_fd_ibase, &ib, sizeof ib);
+        if (cudaMalloc((void **)&P->d_fd_pat, sizeof(gb_fpat)) != cudaSuccess) goto fail;
+        memset(&P->h_fd_pat, 0, sizeof P->h_fd_pat);
+    }
     ok = TRUE;
 fail:
     free(Ls32);
@@ -710,6 +927,8 @@ void gb_plan_free(gb_plan *P)
     gb_vec_free(&P->dag_t); gb_vec_free(&P->dag_sp); gb_vec_free(&P->dag_succ);
     gb_vec_free(&P->dag_nd); gb_vec_free(&P->dag_q0); gb_vec_free(&P->dag_q1);
     gb_vec_free(&P->dag_lv);
+    gb_vec_free(&P->fd_t); gb_vec_free(&P->fd_sp); gb_vec_free(&P->fd_succ);
+    gb_vec_free(&P->fd_nd); gb_vec_free(&P->fd_q0); gb_vec_free(&P->fd_q1);
     void *dev[] = {P->d_Super, P->d_Pi, P->d_Px, P->d_cboff, P->d_cbvoff, P->d_Perm,
                    P->d_Ls, P->d_relmap, P->d_child_ptr, P->d_child_list, P->d_fail,
                    P->d_anyfail, P->d_asm, P->d_node, P->d_potrf, P->d_trsm, P->d_gemm,
@@ -720,7 +939,9 @@ void gb_plan_free(gb_plan *P)
                    P->d_ntask_b, P->d_parent, P->d_linvoff, P->d_xready, P->d_done,
                    P->d_ticket, P->d_Linv[0], P->d_Linv[1], P->d_dag_t, P->d_dag_sp,
                    P->d_dag_succ, P->d_dag_nd, P->d_dag_q0i, P->d_dag_q1i, P->d_dag_ctrl0,
-                   P->d_dag_cnt, P->d_dag_q, P->d_dag_ctrl, P->d_dag_smf};
+                   P->d_dag_cnt, P->d_dag_q, P->d_dag_ctrl, P->d_dag_smf, P->d_fd_t,
+                   P->d_fd_sp, P->d_fd_succ, P->d_fd_nd, P->d_fd_qi, P->d_fd_ctrl0,
+                   P->d_fd_cnt, P->d_fd_q, P->d_fd_pat, P->d_fd_inst, P->d_fd_ibase};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++)
         if (dev[i]) cudaFree(dev[i]);
     gb_vec_free(&P->asm_t); gb_vec_free(&P->node_t); gb_vec_free(&P->potrf_t);

@@ -28,7 +28,7 @@ typedef struct {
 enum {
     GB_K_ASM = 1, GB_K_SMALL, GB_K_POTRF, GB_K_TRSM, GB_K_GEMM, GB_K_DAG,
     GB_K_FWD_SMALL, GB_K_FWD_GATHER, GB_K_FWD_DIAG, GB_K_FWD_PANEL,
-    GB_K_BWD_SMALL, GB_K_BWD_OFFDIAG, GB_K_BWD_DIAG, GB_K_BWD_PANEL
+    GB_K_BWD_SMALL, GB_K_BWD_OFFDIAG, GB_K_BWD_DIAG, GB_K_BWD_PANEL, GB_K_FDAG
 };
 
 typedef struct { int32_t kind, count; int64_t off; } gb_launch_rec;
@@ -51,6 +51,40 @@ typedef struct {
     int32_t epoch;           /* distinct per launch, nonzero */
 } gb_dag_args;
 
+/* Whole-factorization task graph (one persistent launch for every level):
+ * a pattern's local task list and successor CSR, and instances of it (one
+ * per independent system of a batch; a single matrix is one instance), each
+ * with its own value offsets, failure flags and global task-id base. */
+typedef struct {
+    gb_pattern_ptrs pp;              /* device pattern arrays */
+    const gb_dtask *tasks;           /* local tasks */
+    const int32_t *succ_ptr, *succ;  /* local successor CSR */
+    const int64_t *Sp, *Si;          /* S = tril(PAP') column pointers/indices */
+    int32_t ntasks, pad;
+} gb_fpat;
+
+typedef struct {
+    int32_t pat, pad;
+    int64_t base;                    /* global id of local task 0 */
+    int64_t lx, cb, linv, sx, scale; /* element offsets into the value buffers */
+    int32_t *fail, *anyfail;         /* [nsuper], [1] of this instance */
+} gb_finst;
+
+typedef struct {
+    const gb_fpat *pats;             /* device */
+    const gb_finst *inst;            /* device */
+    const int64_t *inst_base;        /* device [ninst], ascending */
+    int32_t ninst;
+    int64_t ntotal;                  /* tasks over all instances */
+    int32_t *cnt, *q0, *q1, *ctrl, *err, *smflag;
+    int32_t epoch;
+    unsigned long long *trace;
+    const void *Sx;                  /* values of S (dtype a_dtype) */
+    int a_dtype;                     /* 0 double, 4 single */
+    const double *scale;             /* optional D A D scaling */
+    double beta;
+} gb_fdag_args;
+
 /* arguments of the single-launch sweeps (device pointers) */
 typedef struct {
     const gb_stask *tasks;
@@ -71,6 +105,7 @@ typedef struct gb_plan {
     const cholmod_factor *L;
     const void *super_ptr, *s_ptr, *pi_ptr;
     Int n, nsuper, ssize, xsize;
+    Int small_cols;                   /* widest supernode factored whole by one block */
     uint64_t hash;
 
     /* host arrays derived from the pattern (kept for the plan's lifetime) */
@@ -105,6 +140,18 @@ typedef struct gb_plan {
     int32_t *d_dag_sp, *d_dag_succ, *d_dag_nd, *d_dag_q0i, *d_dag_q1i, *d_dag_ctrl0;
     int32_t *d_dag_cnt, *d_dag_q, *d_dag_ctrl, *d_dag_smf;
     int32_t dag_epoch;
+
+    /* whole-factorization task graph (local ids: level-graph tasks, then
+     * assembly chunks, small supernodes, and two joins per supernode) */
+    gb_vec fd_t, fd_sp, fd_succ, fd_nd, fd_q0, fd_q1;
+    int32_t fd_total0, fd_total1;
+    gb_dtask *d_fd_t;
+    int32_t *d_fd_sp, *d_fd_succ, *d_fd_nd, *d_fd_qi, *d_fd_ctrl0;
+    int32_t *d_fd_cnt, *d_fd_q;
+    gb_fpat h_fd_pat;                 /* host copy, refreshed per factorization */
+    gb_fpat *d_fd_pat;
+    gb_finst *d_fd_inst;
+    int64_t *d_fd_ibase;
 
     /* single-launch sweeps: tasks, diagonal-block inverses, flags */
     gb_vec sf_t, sb_t, sd_t;          /* forward, backward, diagonal-block tasks */
@@ -160,6 +207,7 @@ struct gb_ctx {
      * GB300_OPT_PROFILE): events around every launch, summed per kind */
     int prof;
     int sweep_mode;              /* 1 = single-launch sweeps (default), 0 = per level */
+    int factor_mode;             /* 1 = one whole-factorization launch (default), 0 = per level */
     int trace_on;                /* record per-task times of the sweeps */
     unsigned long long *d_trace; /* device trace buffer (3 x tasks) */
     size_t trace_cap;
@@ -233,6 +281,8 @@ int gb_launch_diag_minmax(int nsuper, const int64_t *Super, const int64_t *Pi,
                           const int64_t *Px, const void *Lx, int dtype, double *out,
                           cudaStream_t st);
 int gb_launch_fma_peak(int dtype, int iters, int blocks, float *ms, cudaStream_t st);
+int gb_launch_fdag(const gb_fdag_args *a, void *Lx, void *CB, void *Linv, int dtype, int grid,
+                   cudaStream_t st);
 int gb_launch_dag(const gb_pattern_ptrs *pp, const gb_dag_args *a, void *Lx, void *CB,
                   void *Linv, int dtype, int grid, cudaStream_t st);
 int gb_launch_sweep1(int forward, const gb_pattern_ptrs *pp, const gb_sweep1_args *a,
