@@ -459,6 +459,20 @@ int gb300_fma_peak (int dtype, double *tflops) ;
  * factorization (count), [5] kernel launches issued through Common so far. */
 int gb300_get_stats (cholmod_common *Common, double *out, int nout) ;
 
+/* Batches of independent systems (no counterpart in the reference, which
+ * factors one matrix per call).  gb300_batch_analyze returns the supernodal
+ * symbolic factor of the block-diagonal matrix diag(A_0, ..., A_{nsys-1}),
+ * system i having the pattern whose symbolic factor is Lpat[sys_pat[i]]; it
+ * equals gb300_analyze_perm of that block-diagonal matrix with the
+ * block-diagonal permutation, built by concatenation (no analysis is
+ * repeated).  Factorize and solve the batch through the ordinary entry points
+ * with the block-diagonal A (the systems' lower triangles placed on the
+ * diagonal): the factorization is one persistent launch over the whole
+ * forest, and gb300_solve_refined measures the backward error of each system
+ * separately.  Free the result with gb300_free_factor. */
+cholmod_factor *gb300_batch_analyze (int npat, cholmod_factor *const *Lpat,
+    int64_t nsys, const int32_t *sys_pat, cholmod_common *Common) ;
+
 /* Backward error of solutions that are already in device memory, with no
  * allocation of any kind (no counterpart in the reference library).  For
  * callers that must not allocate while they run: a serving loop with a

@@ -96,6 +96,7 @@ def lib():
         "gb300_get_trace": (C.c_int, [vp, C.c_int, C.POINTER(C.c_ulonglong), C.c_int64]),
         "gb300_get_factor_trace": (C.c_int, [vp, C.POINTER(C.c_ulonglong), C.c_int64]),
         "gb300_plan_tasks": (C.c_int, [FP, vp, C.POINTER(C.c_int32), C.c_int64]),
+        "gb300_batch_analyze": (FP, [C.c_int, C.POINTER(FP), C.c_int64, C.POINTER(C.c_int32), vp]),
         "cholmod_l_super_numeric": (C.c_int, [SP, SP, C.POINTER(C.c_double), FP, vp]),
         "cholmod_l_super_lsolve": (C.c_int, [FP, DP, DP, vp]),
         "cholmod_l_super_ltsolve": (C.c_int, [FP, DP, DP, vp]),
@@ -299,6 +300,18 @@ def fma_peak(dtype="d"):
     out = C.c_double(0)
     ok = lib().gb300_fma_peak(4 if dtype == "s" else 0, C.byref(out))
     return out.value if ok else None
+
+
+def batch_analyze(Lpats, sys_pat, common):
+    """Symbolic factor of the block-diagonal batch whose system i has the
+    pattern Lpats[sys_pat[i]] (gb300_batch_analyze)."""
+    arr = (FP * len(Lpats))(*Lpats)
+    sp = np.ascontiguousarray(sys_pat, dtype=np.int32)
+    L = lib().gb300_batch_analyze(len(Lpats), arr, len(sp),
+                                   sp.ctypes.data_as(C.POINTER(C.c_int32)), common.ptr)
+    if not L:
+        raise RuntimeError(f"batch analyze failed, status {common.status}")
+    return L
 
 
 def factorize_mixed(A, L, common):

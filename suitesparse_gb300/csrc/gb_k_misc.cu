@@ -158,6 +158,61 @@ __global__ void k_anorm_inf(int64_t n, const int64_t *__restrict__ Rp,
         atomicMax((unsigned long long *)out, (unsigned long long)__double_as_longlong(sm[0]));
 }
 
+// Segmented forms (one segment per independent block of A): block
+// (chunk, r) reduces rows [lo, hi) of one segment, then 64-bit atomic max
+// into that segment's slot (out zeroed first).  colmax: out[3 (seg nrhs + r)
+// + q] for q = max|R|, max|X|, max|B|; anorm: out[seg] = max row sum |A|.
+__global__ void k_colmax3_seg(const gb_seg_chunk *__restrict__ chunks, int nrhs,
+                              const double *__restrict__ R, int64_t ldr,
+                              const double *__restrict__ X, int64_t ldx,
+                              const double *__restrict__ B, int64_t ldb, double *out)
+{
+    __shared__ double sm[3][256];
+    const gb_seg_chunk ch = chunks[blockIdx.x];
+    const int r = blockIdx.y;
+    double a = 0, b = 0, c = 0;
+    for (int64_t i = ch.lo + threadIdx.x; i < ch.hi; i += blockDim.x) {
+        a = fmax(a, fabs(R[i + r * ldr]));
+        b = fmax(b, fabs(X[i + r * ldx]));
+        c = fmax(c, fabs(B[i + r * ldb]));
+    }
+    sm[0][threadIdx.x] = a;
+    sm[1][threadIdx.x] = b;
+    sm[2][threadIdx.x] = c;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int q = 0; q < 3; q++)
+                sm[q][threadIdx.x] = fmax(sm[q][threadIdx.x], sm[q][threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 3; q++)
+            atomicMax((unsigned long long *)&out[3 * ((int64_t)ch.seg * nrhs + r) + q],
+                      (unsigned long long)__double_as_longlong(sm[q][0]));
+}
+
+__global__ void k_anorm_seg(const gb_seg_chunk *__restrict__ chunks, const int64_t *__restrict__ Rp,
+                            const double *__restrict__ Rx, double *out)
+{
+    __shared__ double sm[256];
+    const gb_seg_chunk ch = chunks[blockIdx.x];
+    double best = 0;
+    for (int64_t i = ch.lo + threadIdx.x; i < ch.hi; i += blockDim.x) {
+        double acc = 0;
+        for (int64_t p = Rp[i]; p < Rp[i + 1]; p++) acc += fabs(Rx[p]);
+        best = fmax(best, acc);
+    }
+    sm[threadIdx.x] = best;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        atomicMax((unsigned long long *)&out[ch.seg], (unsigned long long)__double_as_longlong(sm[0]));
+}
+
 // zero factor entries [from, to) (not-positive-definite clean-up)
 template <typename T>
 __global__ void k_zero_range(T *x, int64_t from, int64_t to)
@@ -277,6 +332,26 @@ int gb_launch_anorm(int64_t n, const int64_t *Rp, const double *Rx, double *out,
 {
     if (cudaMemsetAsync(out, 0, sizeof(double), st) != cudaSuccess) return 1;
     k_anorm_inf<<<gb_grid_for(n), 256, 0, st>>>(n, Rp, Rx, out);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_colmax3_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t nseg, int nrhs,
+                          const double *R, int64_t ldr, const double *X, int64_t ldx,
+                          const double *B, int64_t ldb, double *out, cudaStream_t st)
+{
+    if (cudaMemsetAsync(out, 0, sizeof(double) * 3 * nseg * nrhs, st) != cudaSuccess) return 1;
+    if (nchunk <= 0 || nrhs <= 0) return 0;
+    dim3 grid((unsigned)nchunk, (unsigned)nrhs);
+    k_colmax3_seg<<<grid, 256, 0, st>>>(chunks, nrhs, R, ldr, X, ldx, B, ldb, out);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_anorm_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t nseg, const int64_t *Rp,
+                        const double *Rx, double *out, cudaStream_t st)
+{
+    if (cudaMemsetAsync(out, 0, sizeof(double) * nseg, st) != cudaSuccess) return 1;
+    if (nchunk <= 0) return 0;
+    k_anorm_seg<<<(unsigned)nchunk, 256, 0, st>>>(chunks, Rp, Rx, out);
     return (int)cudaGetLastError();
 }
 

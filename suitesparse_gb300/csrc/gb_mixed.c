@@ -92,9 +92,12 @@ static int upload_full_A(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, cholmod_com
              && cudaMemcpyAsync(P->d_Rx, Rx, sizeof(double) * nz, cudaMemcpyHostToDevice, st) == cudaSuccess
              && cudaMemcpyAsync(P->d_scale, dorig, sizeof(double) * n, cudaMemcpyHostToDevice, st) == cudaSuccess
              && cudaMemcpyAsync(P->d_scale_perm, dperm, sizeof(double) * n, cudaMemcpyHostToDevice, st) == cudaSuccess
-             && gb_launch_anorm(n, P->d_Rp, P->d_Rx, P->d_red + 63, st) == 0
-             && cudaMemcpyAsync(&P->anorm, P->d_red + 63, sizeof(double), cudaMemcpyDeviceToHost, st) == cudaSuccess
+             && gb_launch_anorm_seg(P->nchunk, P->d_chunk, P->nseg, P->d_Rp, P->d_Rx, P->d_anorm_seg, st) == 0
+             && cudaMemcpyAsync(P->h_anorm_seg, P->d_anorm_seg, sizeof(double) * P->nseg,
+                                cudaMemcpyDeviceToHost, st) == cudaSuccess
              && cudaStreamSynchronize(st) == cudaSuccess;
+        P->anorm = 0;
+        for (int64_t g = 0; ok && g < P->nseg; g++) P->anorm = fmax(P->anorm, P->h_anorm_seg[g]);
         if (!ok) GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error uploading A");
     } else {
         GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "out of memory");
@@ -203,18 +206,15 @@ cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod
     if (n == 0 || nrhs == 0) return X;
     cudaStream_t st = ctx->stream;
     size_t nb = sizeof(double) * n * nrhs;
-    double *hred = malloc(sizeof(double) * 3 * nrhs);
-    double *best = malloc(sizeof(double) * nrhs);
+    /* backward error per independent block (segment) and column */
+    const int64_t nsg = P->nseg, nred = 3 * nsg * nrhs;
+    double *hred = malloc(sizeof(double) * nred);
+    double *best = malloc(sizeof(double) * nsg * nrhs);
     int ok = hred && best && gb_dev_grow((void **)&P->d_X, &P->x_cap, nb)
              && gb_dev_grow((void **)&P->d_R, &P->r_cap, nb)
              && gb_dev_grow((void **)&P->d_bx, &P->bx_cap, nb)
-             && gb_dev_grow(&P->d_Y, &P->y_cap, nb);
-    if (ok && nrhs * 3 > 60) {
-        size_t cap = 0;
-        cudaFree(P->d_red);
-        P->d_red = NULL;
-        ok = gb_dev_grow((void **)&P->d_red, &cap, sizeof(double) * (3 * nrhs + 64));
-    }
+             && gb_dev_grow(&P->d_Y, &P->y_cap, nb)
+             && gb_dev_grow((void **)&P->d_bred, &P->bred_cap, sizeof(double) * nred);
     ok = ok && cudaMemcpy2DAsync(P->d_bx, sizeof(double) * n, B->x, sizeof(double) * B->d,
                                  sizeof(double) * n, nrhs, cudaMemcpyHostToDevice, st) == cudaSuccess
          && cudaMemsetAsync(P->d_X, 0, nb, st) == cudaSuccess
@@ -223,7 +223,7 @@ cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod
     int it = 0, stall = 0;
     int32_t serr = 0;
     double bmax_all = 0, berr_max = INFINITY;
-    for (int r = 0; r < nrhs && best; r++) best[r] = INFINITY;
+    for (int64_t r = 0; r < nsg * nrhs && best; r++) best[r] = INFINITY;
     while (ok && it < GB_MAX_REFINE) {
         /* correction with the current factor: x += D P' L^-T L^-1 P D r */
         int single = (P->mixed == 1);
@@ -235,8 +235,9 @@ cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod
              && gb_launch_perm_out(n, nrhs, P->d_Perm, scale, P->d_Y, ydt, n, P->d_X, 0, n, 1, st) == 0
              && gb_launch_residual(n, nrhs, P->d_Rp, P->d_Rj, P->d_Rx, P->d_X, n, P->d_bx, n,
                                    P->d_R, n, st) == 0
-             && gb_launch_colmax3(n, nrhs, P->d_R, n, P->d_X, n, P->d_bx, n, P->d_red, st) == 0
-             && cudaMemcpyAsync(hred, P->d_red, sizeof(double) * 3 * nrhs, cudaMemcpyDeviceToHost, st) == cudaSuccess
+             && gb_launch_colmax3_seg(P->nchunk, P->d_chunk, nsg, nrhs, P->d_R, n, P->d_X, n,
+                                      P->d_bx, n, P->d_bred, st) == 0
+             && cudaMemcpyAsync(hred, P->d_bred, sizeof(double) * nred, cudaMemcpyDeviceToHost, st) == cudaSuccess
              && cudaMemcpyAsync(&serr, P->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, st) == cudaSuccess
              && cudaStreamSynchronize(st) == cudaSuccess && !(ctx->sweep_mode == 1 && serr);
         ctx->launches += 5;
@@ -244,12 +245,13 @@ cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod
         it++;
         berr_max = 0;
         int improved = 0;
-        for (int r = 0; r < nrhs; r++) {
-            double den = P->anorm * hred[3 * r + 1] + hred[3 * r + 2];
-            double be = den > 0 ? hred[3 * r] / den : 0;
-            if (be < best[r]) { if (be < 0.5 * best[r]) improved = 1; best[r] = be; }
+        for (int64_t q = 0; q < nsg * nrhs; q++) {
+            const double *h = hred + 3 * q;
+            double den = P->h_anorm_seg[q / nrhs] * h[1] + h[2];
+            double be = den > 0 ? h[0] / den : 0;
+            if (be < best[q]) { if (be < 0.5 * best[q]) improved = 1; best[q] = be; }
             berr_max = fmax(berr_max, be);
-            bmax_all = fmax(bmax_all, hred[3 * r + 2]);
+            bmax_all = fmax(bmax_all, h[2]);
         }
         if (berr_max <= tol) break;
         stall = improved ? 0 : stall + 1;

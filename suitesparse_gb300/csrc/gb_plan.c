@@ -260,6 +260,66 @@ static int fdag_build(gb_plan *P)
     return ok;
 }
 
+/* Independent blocks: the trees of the supernodal etree.  With Perm, the
+ * rows of each tree in the original order; if every tree is one contiguous
+ * range of original rows (a batch of systems placed on the diagonal, or an
+ * irreducible matrix), those ranges are the segments, else one segment. */
+static int segments_build(gb_plan *P)
+{
+    const Int n = P->n, ns = P->nsuper;
+    const Int *Super = P->L->super, *Perm = P->L->Perm;
+    int32_t *root = malloc(sizeof(int32_t) * (ns + 1));
+    int32_t *comp = malloc(sizeof(int32_t) * (n + 1));
+    int ok = root && comp;
+    /* parents come after children in supernode order */
+    for (Int s = ns - 1; ok && s >= 0; s--) {
+        int32_t par = P->h_parent[s];
+        root[s] = par < 0 ? (int32_t)s : root[par];
+    }
+    for (Int s = 0; ok && s < ns; s++)
+        for (Int k = Super[s]; k < Super[s + 1]; k++) comp[Perm ? Perm[k] : k] = root[s];
+    Int runs = 0, ntrees = 0;
+    for (Int s = 0; ok && s < ns; s++) ntrees += P->h_parent[s] < 0;
+    for (Int i = 0; ok && i < n; i++) runs += (i == 0 || comp[i] != comp[i - 1]);
+    int contiguous = ok && runs == ntrees;
+    P->nseg = contiguous ? GB_MAX(runs, 1) : 1;
+    P->h_seg = malloc(sizeof(int64_t) * (P->nseg + 1));
+    if (!P->h_seg) ok = 0;
+    if (ok) {
+        if (contiguous && n > 0) {
+            Int q = 0;
+            for (Int i = 0; i < n; i++)
+                if (i == 0 || comp[i] != comp[i - 1]) P->h_seg[q++] = i;
+        } else {
+            P->h_seg[0] = 0;
+        }
+        P->h_seg[P->nseg] = n;
+        P->nchunk = 0;
+        for (int64_t g = 0; g < P->nseg; g++) {
+            int64_t len = P->h_seg[g + 1] - P->h_seg[g];
+            P->nchunk += GB_MAX(1, (len + GB_SEG_CHUNK - 1) / GB_SEG_CHUNK);
+        }
+        P->h_chunk = malloc(sizeof(gb_seg_chunk) * P->nchunk);
+        if (!P->h_chunk) ok = 0;
+    }
+    if (ok) {
+        int64_t q = 0;
+        for (int64_t g = 0; g < P->nseg; g++) {
+            int64_t lo = P->h_seg[g], hi = P->h_seg[g + 1];
+            do {
+                gb_seg_chunk ch = {lo, GB_MIN(hi, lo + GB_SEG_CHUNK), (int32_t)g, 0};
+                P->h_chunk[q++] = ch;
+                lo += GB_SEG_CHUNK;
+            } while (lo < hi);
+        }
+        P->h_anorm_seg = calloc(P->nseg, sizeof(double));
+        if (!P->h_anorm_seg) ok = 0;
+    }
+    free(root);
+    free(comp);
+    return ok;
+}
+
 gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
 {
     if (small_cols < 1) small_cols = 1;
@@ -770,7 +830,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
     P->h_cboff = cboff;
     P->h_cbvoff = cbvoff;
     free(SuperMap); free(parent); free(level); free(Map); free(lev_ptr); free(lev_list);
-    if (!fdag_build(P)) { gb_plan_free(P); return NULL; }
+    if (!fdag_build(P) || !segments_build(P)) { gb_plan_free(P); return NULL; }
     return P;
 
 fail:
@@ -876,6 +936,8 @@ int gb_plan_upload(gb_plan *P)
     P->ptrs.anyfail = P->d_anyfail;
     P->ptrs.blkoff = P->d_blkoff;
     P->ptrs.linvoff = P->d_linvoff;
+    UP(P->d_chunk, P->h_chunk, sizeof(gb_seg_chunk) * P->nchunk);
+    if (cudaMalloc((void **)&P->d_anorm_seg, sizeof(double) * (P->nseg + 1)) != cudaSuccess) goto fail;
     /* whole-factorization task graph, one instance */
     UP(P->d_fd_t, P->fd_t.p, P->fd_t.n * P->fd_t.esz);
     UP(P->d_fd_sp, P->fd_sp.p, P->fd_sp.n * P->fd_sp.esz);
@@ -927,6 +989,7 @@ void gb_plan_free(gb_plan *P)
     gb_vec_free(&P->dag_t); gb_vec_free(&P->dag_sp); gb_vec_free(&P->dag_succ);
     gb_vec_free(&P->dag_nd); gb_vec_free(&P->dag_q0); gb_vec_free(&P->dag_q1);
     gb_vec_free(&P->dag_lv);
+    free(P->h_seg); free(P->h_chunk); free(P->h_anorm_seg);
     gb_vec_free(&P->fd_t); gb_vec_free(&P->fd_sp); gb_vec_free(&P->fd_succ);
     gb_vec_free(&P->fd_nd); gb_vec_free(&P->fd_q0); gb_vec_free(&P->fd_q1);
     void *dev[] = {P->d_Super, P->d_Pi, P->d_Px, P->d_cboff, P->d_cbvoff, P->d_Perm,
@@ -941,7 +1004,8 @@ void gb_plan_free(gb_plan *P)
                    P->d_dag_succ, P->d_dag_nd, P->d_dag_q0i, P->d_dag_q1i, P->d_dag_ctrl0,
                    P->d_dag_cnt, P->d_dag_q, P->d_dag_ctrl, P->d_dag_smf, P->d_fd_t,
                    P->d_fd_sp, P->d_fd_succ, P->d_fd_nd, P->d_fd_qi, P->d_fd_ctrl0,
-                   P->d_fd_cnt, P->d_fd_q, P->d_fd_pat, P->d_fd_inst, P->d_fd_ibase};
+                   P->d_fd_cnt, P->d_fd_q, P->d_fd_pat, P->d_fd_inst, P->d_fd_ibase,
+                   P->d_chunk, P->d_anorm_seg, P->d_bred};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++)
         if (dev[i]) cudaFree(dev[i]);
     gb_vec_free(&P->asm_t); gb_vec_free(&P->node_t); gb_vec_free(&P->potrf_t);

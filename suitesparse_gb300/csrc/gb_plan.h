@@ -85,6 +85,10 @@ typedef struct {
     double beta;
 } gb_fdag_args;
 
+/* a chunk of rows of one segment, for segmented reductions */
+typedef struct { int64_t lo, hi; int32_t seg, pad; } gb_seg_chunk;
+#define GB_SEG_CHUNK 4096
+
 /* arguments of the single-launch sweeps (device pointers) */
 typedef struct {
     const gb_stask *tasks;
@@ -186,6 +190,15 @@ typedef struct gb_plan {
     int mixed;                        /* 0 none, 1 FP32 factor, 2 FP64 factor */
     int mixed_reason;                 /* why the FP64 factor was used */
     double anorm;                     /* |A|_inf of the refined system */
+    /* independent blocks of A (trees of the supernodal etree) when each is a
+     * contiguous range of original rows; else one segment of all rows.  The
+     * refinement measures the backward error per segment and column. */
+    int64_t nseg, nchunk;
+    int64_t *h_seg;                   /* [nseg+1] row ranges */
+    gb_seg_chunk *h_chunk;            /* row chunks of at most GB_SEG_CHUNK rows */
+    gb_seg_chunk *d_chunk;
+    double *h_anorm_seg, *d_anorm_seg, *d_bred;
+    size_t bred_cap;
 
     struct gb_plan *next;             /* side-table chaining */
 } gb_plan;
@@ -277,6 +290,11 @@ int gb_launch_residual(int64_t n, int nrhs, const int64_t *Rp, const int32_t *Rj
 int gb_launch_colmax3(int64_t n, int nrhs, const double *R, int64_t ldr, const double *X,
                       int64_t ldx, const double *B, int64_t ldb, double *out, cudaStream_t st);
 int gb_launch_anorm(int64_t n, const int64_t *Rp, const double *Rx, double *out, cudaStream_t st);
+int gb_launch_anorm_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t nseg, const int64_t *Rp,
+                        const double *Rx, double *out, cudaStream_t st);
+int gb_launch_colmax3_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t nseg, int nrhs,
+                          const double *R, int64_t ldr, const double *X, int64_t ldx,
+                          const double *B, int64_t ldb, double *out, cudaStream_t st);
 int gb_launch_diag_minmax(int nsuper, const int64_t *Super, const int64_t *Pi,
                           const int64_t *Px, const void *Lx, int dtype, double *out,
                           cudaStream_t st);

@@ -420,3 +420,100 @@ cholmod_factor *gb300_analyze_perm(cholmod_sparse *A, const int64_t *Perm,
     }
     return gb_analyze_perm(A, Perm, Common);
 }
+
+/* Symbolic factor of a batch of independent systems: the block-diagonal
+ * matrix diag(A_0, A_1, ...) where system i has the pattern of Lpat[sys_pat[i]]
+ * (each a supernodal symbolic factor from gb300_analyze_perm or
+ * cholmod_analyze).  Supernodes never span two blocks (the etree of a
+ * block-diagonal matrix is a forest and relaxed amalgamation only merges a
+ * supernode with its parent), so the result is the concatenation of the
+ * blocks' factors with their column, row-index and value offsets, and it
+ * equals gb300_analyze_perm of the block-diagonal matrix with the
+ * block-diagonal permutation.  No counterpart in the reference, which
+ * factors one matrix per call. */
+cholmod_factor *gb300_batch_analyze(int npat, cholmod_factor *const *Lpat, int64_t nsys,
+                                    const int32_t *sys_pat, cholmod_common *Common)
+{
+    if (!Common) return NULL;
+    Common->status = CHOLMOD_OK;
+    if (npat < 1 || !Lpat || nsys < 1 || !sys_pat) {
+        GB_ERROR(CHOLMOD_INVALID, "invalid batch description");
+        return NULL;
+    }
+    for (int p = 0; p < npat; p++) {
+        const cholmod_factor *F = Lpat[p];
+        if (!F || !F->is_super || F->itype != CHOLMOD_LONG || !F->super || !F->pi || !F->px
+            || !F->s || !F->Perm || !F->ColCount) {
+            GB_ERROR(CHOLMOD_INVALID, "each pattern must be a supernodal symbolic factor");
+            return NULL;
+        }
+    }
+    Int n = 0, nsuper = 0, ssz = 0, xsz = 0, maxc = 1, maxe = 1;
+    for (int64_t i = 0; i < nsys; i++) {
+        if (sys_pat[i] < 0 || sys_pat[i] >= npat) {
+            GB_ERROR(CHOLMOD_INVALID, "system pattern index out of range");
+            return NULL;
+        }
+        const cholmod_factor *F = Lpat[sys_pat[i]];
+        const Int *Fpi = F->pi, *Fpx = F->px;
+        n += (Int)F->n;
+        nsuper += (Int)F->nsuper;
+        ssz += Fpi[F->nsuper];
+        xsz += Fpx[F->nsuper];
+        maxc = GB_MAX(maxc, (Int)F->maxcsize);
+        maxe = GB_MAX(maxe, (Int)F->maxesize);
+    }
+    cholmod_factor *L = gb_calloc(1, sizeof(cholmod_factor), Common);
+    if (!L) return NULL;
+    L->n = n;
+    L->minor = n;
+    L->nsuper = nsuper;
+    L->ssize = GB_MAX(ssz, 1);
+    L->xsize = GB_MAX(xsz, 1);
+    L->maxcsize = maxc;
+    L->maxesize = maxe;
+    L->ordering = CHOLMOD_GIVEN;
+    L->is_ll = TRUE;
+    L->is_super = TRUE;
+    L->is_monotonic = TRUE;
+    L->itype = CHOLMOD_LONG;
+    L->xtype = CHOLMOD_PATTERN;
+    L->dtype = CHOLMOD_DOUBLE;
+    L->Perm = gb_malloc(GB_MAX(n, 1), sizeof(Int), Common);
+    L->ColCount = gb_malloc(GB_MAX(n, 1), sizeof(Int), Common);
+    L->super = gb_malloc(nsuper + 1, sizeof(Int), Common);
+    L->pi = gb_malloc(nsuper + 1, sizeof(Int), Common);
+    L->px = gb_malloc(nsuper + 1, sizeof(Int), Common);
+    L->s = gb_malloc(L->ssize, sizeof(Int), Common);
+    if (!L->Perm || !L->ColCount || !L->super || !L->pi || !L->px || !L->s) {
+        gb300_free_factor(&L, Common);
+        return NULL;
+    }
+    Int *Perm = L->Perm, *CC = L->ColCount, *Sup = L->super, *Pi = L->pi, *Px = L->px, *Ls = L->s;
+    Int c0 = 0, s0 = 0, p0 = 0, x0 = 0;
+    for (int64_t i = 0; i < nsys; i++) {
+        const cholmod_factor *F = Lpat[sys_pat[i]];
+        const Int fn = (Int)F->n, fns = (Int)F->nsuper;
+        const Int *FPerm = F->Perm, *FCC = F->ColCount, *FSup = F->super, *FPi = F->pi,
+                  *FPx = F->px, *FLs = F->s;
+        for (Int k = 0; k < fn; k++) {
+            Perm[c0 + k] = c0 + FPerm[k];
+            CC[c0 + k] = FCC[k];
+        }
+        for (Int s = 0; s < fns; s++) {
+            Sup[s0 + s] = c0 + FSup[s];
+            Pi[s0 + s] = p0 + FPi[s];
+            Px[s0 + s] = x0 + FPx[s];
+        }
+        for (Int q = 0; q < FPi[fns]; q++) Ls[p0 + q] = c0 + FLs[q];
+        c0 += fn;
+        s0 += fns;
+        p0 += FPi[fns];
+        x0 += FPx[fns];
+    }
+    Sup[nsuper] = n;
+    Pi[nsuper] = p0;
+    Px[nsuper] = x0;
+    if (ssz == 0) Ls[0] = 0;
+    return L;
+}

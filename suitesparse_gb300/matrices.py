@@ -316,6 +316,34 @@ def batch_system(index, side, seed=3, lo=0.1, hi=10.0):
     return laplace2d(side, side, seed=(seed << 32) + index + 1, lo=lo, hi=hi)
 
 
+def batch_layout(nsys=4096, seed=3, npat=8, lo=16, hi=96):
+    """The batched workload's systems: ``npat`` distinct grid sides
+    (batch_sides) and, for each of ``nsys`` systems, the index of its side
+    (uniform over the sides, splitmix64 stream of ``seed`` + 1)."""
+    sides = batch_sides(seed, npat, lo, hi)
+    u = uniform01(seed + 1, nsys, 0)
+    pat = np.minimum((u * npat).astype(np.int32), npat - 1)
+    return sides, pat
+
+
+def block_diag_lower(mats):
+    """Lower-triangular CSC of diag(A_0, A_1, ...) from (n, Ap, Ai, Ax) tuples."""
+    n = sum(m[0] for m in mats)
+    nnz = sum(int(m[1][-1]) for m in mats)
+    Ap = np.zeros(n + 1, dtype=np.int64)
+    Ai = np.empty(nnz, dtype=np.int64)
+    Ax = np.empty(nnz, dtype=np.float64)
+    c0 = p0 = 0
+    for (ni, p, i, x) in mats:
+        k = int(p[-1])
+        Ap[c0 + 1:c0 + ni + 1] = p0 + p[1:]
+        Ai[p0:p0 + k] = c0 + i
+        Ax[p0:p0 + k] = x
+        c0 += ni
+        p0 += k
+    return n, Ap, Ai, Ax
+
+
 # Named workloads (the benchmark configurations; parity-test cases)
 CONFIGS = {
     "c1": dict(kind="laplace2d", args=dict(nx=100, shift=1e-3), ordering="amd",
