@@ -473,6 +473,38 @@ int gb300_get_stats (cholmod_common *Common, double *out, int nout) ;
 cholmod_factor *gb300_batch_analyze (int npat, cholmod_factor *const *Lpat,
     int64_t nsys, const int32_t *sys_pat, cholmod_common *Common) ;
 
+/* Request server (no counterpart in the reference, a per-call library).
+ * nslots worker threads, each with its own cholmod_common and CUDA stream,
+ * take factor and solve requests as they arrive; requests that are admitted
+ * together run on the GPU at the same time.  Symbolic analyses are cached by
+ * the caller's pattern id (analysed once, with perm, on first sight);
+ * factors stay resident on the device keyed by the caller's factor id (a
+ * factor request for a resident factor refactorizes it in place); a factor
+ * request is admitted when its device-memory estimate (from nnz(L)) fits
+ * under budget_bytes, evicting idle factors least recently used first;
+ * requests of one factor run in order, and queued solves of one factor are
+ * coalesced into one refined solve of up to max_rhs columns.  Every solve is
+ * the FP32 factor + FP64 refinement to backward error 1e-12.  A, perm and B
+ * are copied at submission.  arrival is a gb300_server_now() time stamp.
+ * gb300_server_wait blocks until request req is done, copies a solve's X
+ * (n x nrhs, leading dimension ldx) and fills out[7]: arrival, start,
+ * finish (seconds, gb300_server_now clock), backward error, refinement
+ * iterations, status, columns of the coalesced solve.  Returns the
+ * request's CHOLMOD status.  gb300_server_stats: [0] resident bytes, [1]
+ * budget, [2] resident factors, [3] cached patterns, [4] evictions, [5]
+ * solves merged into another, [6] requests served. */
+typedef struct gb300_server gb300_server ;
+gb300_server *gb300_server_create (int nslots, int64_t budget_bytes, int max_rhs) ;
+int gb300_server_factor (gb300_server *S, int64_t req, int64_t factor_id,
+    int64_t pattern_id, int64_t n, const int64_t *Ap, const int64_t *Ai,
+    const double *Ax, const int64_t *perm, double arrival) ;
+int gb300_server_solve (gb300_server *S, int64_t req, int64_t factor_id, int64_t n,
+    int nrhs, const double *B, double arrival) ;
+int gb300_server_wait (gb300_server *S, int64_t req, double *X, int64_t ldx, double *out) ;
+int gb300_server_stats (gb300_server *S, double *out, int nout) ;
+int gb300_server_destroy (gb300_server *S) ;
+double gb300_server_now (void) ;
+
 /* Backward error of solutions that are already in device memory, with no
  * allocation of any kind (no counterpart in the reference library).  For
  * callers that must not allocate while they run: a serving loop with a

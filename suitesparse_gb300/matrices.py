@@ -316,6 +316,41 @@ def batch_system(index, side, seed=3, lo=0.1, hi=10.0):
     return laplace2d(side, side, seed=(seed << 32) + index + 1, lo=lo, hi=hi)
 
 
+def grid_nd_perm(dims, leaf=16):
+    """Geometric nested-dissection ordering of a box grid (x fastest, as the
+    grid generators number nodes): recursive bisection across the longest
+    side, each separator plane ordered after both halves.  Returns Perm with
+    Perm[k] = original index of the k-th pivot."""
+    dims = tuple(int(v) for v in dims)
+    strides = np.cumprod((1,) + dims[:-1]).astype(np.int64)
+    out = []
+    stack = [(tuple(0 for _ in dims), dims)]
+    # explicit post-order: (box, state) with state 0 = expand, 1 = emit separator
+    work = [("box", (0,) * len(dims), dims)]
+    while work:
+        kind, lo, sz = work.pop()
+        if kind == "sep" or int(np.prod(sz)) <= leaf or max(sz) <= 2:
+            grids = np.meshgrid(*[np.arange(l, l + s) for l, s in zip(lo, sz)], indexing="ij")
+            ids = sum(g.astype(np.int64) * st for g, st in zip(grids, strides))
+            out.append(ids.ravel(order="F"))
+            continue
+        d = int(np.argmax(sz))
+        m = sz[d] // 2
+        left_sz = list(sz); left_sz[d] = m
+        right_lo = list(lo); right_lo[d] = lo[d] + m + 1
+        right_sz = list(sz); right_sz[d] = sz[d] - m - 1
+        sep_lo = list(lo); sep_lo[d] = lo[d] + m
+        sep_sz = list(sz); sep_sz[d] = 1
+        # pushed in reverse: left, right, then the separator last
+        work.append(("sep", tuple(sep_lo), tuple(sep_sz)))
+        if right_sz[d] > 0:
+            work.append(("box", tuple(right_lo), tuple(right_sz)))
+        if m > 0:
+            work.append(("box", lo, tuple(left_sz)))
+    del stack
+    return np.concatenate(out).astype(np.int64)
+
+
 def batch_layout(nsys=4096, seed=3, npat=8, lo=16, hi=96):
     """The batched workload's systems: ``npat`` distinct grid sides
     (batch_sides) and, for each of ``nsys`` systems, the index of its side

@@ -1,0 +1,201 @@
+"""Serving: a stream of factor and solve requests through the library's
+request server (gb300_server_* in include/cholmod_gb300.h).
+
+The stream restates the serving workload: requests arrive as a Poisson
+process; matrices are 2D 5-point and 3D 7-point grid Laplacians with
+log-uniform coefficients; a share of the factor requests reuses one of a
+few cached patterns with new values (the server reuses the symbolic analysis
+and, for a resident factor id, the device factor), a share are solve-only
+requests against a resident factor with 1-32 right-hand sides, the rest are
+factor requests of new patterns.  Orderings are geometric nested dissection
+of the grids (matrices.grid_nd_perm) given with a pattern's first request.
+"""
+import ctypes as C
+import threading
+import time
+
+import numpy as np
+
+from . import cholmod as CH
+from . import matrices as M
+
+
+def _lib():
+    L = CH.lib()
+    if not getattr(L, "_serve_sig", False):
+        vp, i64, dp = C.c_void_p, C.c_int64, C.POINTER(C.c_double)
+        ip = C.POINTER(C.c_int64)
+        sig = {
+            "gb300_server_create": (vp, [C.c_int, i64, C.c_int]),
+            "gb300_server_factor": (C.c_int, [vp, i64, i64, i64, i64, ip, ip, dp, ip, C.c_double]),
+            "gb300_server_solve": (C.c_int, [vp, i64, i64, i64, C.c_int, dp, C.c_double]),
+            "gb300_server_wait": (C.c_int, [vp, i64, dp, i64, dp]),
+            "gb300_server_stats": (C.c_int, [vp, dp, C.c_int]),
+            "gb300_server_destroy": (C.c_int, [vp]),
+            "gb300_server_now": (C.c_double, []),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        L._serve_sig = True
+    return L
+
+
+def _i64(a):
+    return np.ascontiguousarray(a, dtype=np.int64)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Server:
+    """Python handle of a gb300_server."""
+
+    def __init__(self, nslots=4, budget_bytes=150 << 30, max_rhs=64):
+        self.L = _lib()
+        self.h = self.L.gb300_server_create(nslots, int(budget_bytes), max_rhs)
+        if not self.h:
+            raise RuntimeError("gb300_server_create failed")
+        self.n = {}
+
+    def now(self):
+        return self.L.gb300_server_now()
+
+    def factor(self, req, factor_id, pattern_id, mat, perm=None, arrival=None):
+        n, Ap, Ai, Ax = mat
+        Ap, Ai, Ax = _i64(Ap), _i64(Ai), _f64(Ax)
+        pp = _i64(perm).ctypes.data_as(C.POINTER(C.c_int64)) if perm is not None else None
+        st = self.L.gb300_server_factor(
+            self.h, req, factor_id, pattern_id, n, Ap.ctypes.data_as(C.POINTER(C.c_int64)),
+            Ai.ctypes.data_as(C.POINTER(C.c_int64)), Ax.ctypes.data_as(C.POINTER(C.c_double)),
+            pp, self.now() if arrival is None else arrival)
+        if st != 0:
+            raise RuntimeError(f"factor request {req} rejected: status {st}")
+        self.n[req] = (n, 0)
+
+    def solve(self, req, factor_id, B, arrival=None):
+        B = np.asfortranarray(_f64(B if B.ndim == 2 else B[:, None]))
+        n, k = B.shape
+        st = self.L.gb300_server_solve(self.h, req, factor_id, n, k,
+                                       B.ctypes.data_as(C.POINTER(C.c_double)),
+                                       self.now() if arrival is None else arrival)
+        if st != 0:
+            raise RuntimeError(f"solve request {req} rejected: status {st}")
+        self.n[req] = (n, k)
+
+    def wait(self, req):
+        """(status, X or None, dict of times / backward error)"""
+        n, k = self.n.pop(req)
+        X = np.zeros((n, k), dtype=np.float64, order="F") if k else None
+        out = (C.c_double * 7)()
+        st = self.L.gb300_server_wait(
+            self.h, req, X.ctypes.data_as(C.POINTER(C.c_double)) if k else None, n, out)
+        info = dict(arrival=out[0], start=out[1], finish=out[2], berr=out[3],
+                    iterations=int(out[4]), status=int(out[5]), batch_cols=int(out[6]))
+        return st, X, info
+
+    def stats(self):
+        out = (C.c_double * 7)()
+        self.L.gb300_server_stats(self.h, out, 7)
+        keys = ("resident_bytes", "budget_bytes", "resident_factors", "cached_patterns",
+                "evictions", "coalesced", "served")
+        return dict(zip(keys, list(out)))
+
+    def close(self):
+        if self.h:
+            self.L.gb300_server_destroy(self.h)
+            self.h = None
+
+
+def make_stream(nreq=200, seed=5, rate=200.0, sides2d=(32, 160), sides3d=(16, 40),
+                ncached=16, p_reuse=0.6, p_solve=0.2, max_rhs=32):
+    """A request stream: list of dicts with kind, arrival offset (s), ids and
+    inputs.  Patterns are grids; pattern ids 0..ncached-1 are the cached set,
+    new patterns get fresh ids."""
+    rng = np.random.default_rng(seed)
+
+    def new_pattern(pid):
+        if rng.random() < 0.5:
+            s = int(np.exp(rng.uniform(np.log(sides2d[0]), np.log(sides2d[1]))))
+            return dict(pid=pid, dims=(s, s))
+        s = int(np.exp(rng.uniform(np.log(sides3d[0]), np.log(sides3d[1]))))
+        return dict(pid=pid, dims=(s, s, s))
+
+    cached = [new_pattern(p) for p in range(ncached)]
+    next_pid, next_fid = ncached, 0
+    resident = []                        # factor ids known to be factored, with their pattern
+    t = 0.0
+    out = []
+    for r in range(nreq):
+        t += rng.exponential(1.0 / rate)
+        u = rng.random()
+        if u < p_solve and resident:
+            fid, pat = resident[int(rng.integers(len(resident)))]
+            out.append(dict(kind="solve", req=r, t=t, fid=fid, pat=pat,
+                            nrhs=int(rng.integers(1, max_rhs + 1)), seed=int(rng.integers(1 << 30))))
+            continue
+        if u < p_solve + p_reuse:
+            pat = cached[int(rng.integers(ncached))]
+        else:
+            pat = new_pattern(next_pid)
+            next_pid += 1
+        fid = next_fid
+        next_fid += 1
+        out.append(dict(kind="factor", req=r, t=t, fid=fid, pat=pat,
+                        seed=int(rng.integers(1 << 30))))
+        resident.append((fid, pat))
+    return out
+
+
+def request_inputs(rq, _cache={}):
+    """Matrix (and ordering) of a factor request, or B of a solve request."""
+    pat = rq["pat"]
+    dims = pat["dims"]
+    if rq["kind"] == "factor":
+        gen = M.laplace2d if len(dims) == 2 else M.laplace3d
+        mat = gen(*dims, seed=rq["seed"], lo=1e-2, hi=1e2)
+        key = dims
+        if key not in _cache:
+            _cache[key] = M.grid_nd_perm(dims)
+        return mat, _cache[key]
+    n = int(np.prod(dims))
+    return M.rhs(n, rq["nrhs"], rq["seed"] % 1000003)
+
+
+def run_stream(server, stream, realtime=True):
+    """Submit the stream (at its arrival times when realtime) from one
+    thread, collect every request's result in another.  Returns the
+    per-request records and the wall time."""
+    inputs = {rq["req"]: request_inputs(rq) for rq in stream}
+    seen = set()
+    t0 = server.now()
+    records = {}
+
+    def submitter():
+        for rq in stream:
+            if realtime:
+                delay = t0 + rq["t"] - server.now()
+                if delay > 0:
+                    time.sleep(delay)
+            arr = server.now()
+            if rq["kind"] == "factor":
+                mat, perm = inputs[rq["req"]]
+                pid = rq["pat"]["pid"]
+                server.factor(rq["req"], rq["fid"], pid, mat, perm if pid not in seen else None,
+                              arrival=arr)
+                seen.add(pid)
+            else:
+                server.solve(rq["req"], rq["fid"], inputs[rq["req"]], arrival=arr)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    for rq in stream:
+        while rq["req"] not in server.n:
+            time.sleep(1e-4)
+        st, X, info = server.wait(rq["req"])
+        info["status"] = st
+        records[rq["req"]] = dict(kind=rq["kind"], X=X, **info)
+    th.join()
+    return records, server.now() - t0
