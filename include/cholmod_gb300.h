@@ -353,13 +353,18 @@ int gb300_finish (cholmod_common *Common) ;
  *      launch over a task graph of the whole etree (assembly chunks, small
  *      supernodes, tiles of the wide supernodes, update blocks; a supernode
  *      starts when its children's update blocks are done); 0 = one launch
- *      of each kind per etree level, levels in sequence. */
+ *      of each kind per etree level, levels in sequence.
+ *  GB300_OPT_TENSOR [0]: 1 = in the FP32 factorization the tile and
+ *      update-block products run on the tensor cores (tcgen05, operands
+ *      split into two TF32 parts, three products, FP32 accumulation);
+ *      0 = FP32 multiply-adds on the CUDA cores. */
 #define GB300_OPT_KEEP_ON_DEVICE 1
 #define GB300_OPT_SMALL_COLS     2
 #define GB300_OPT_PROFILE        3
 #define GB300_OPT_SWEEP          4
 #define GB300_OPT_TRACE          5
 #define GB300_OPT_FACTOR         6
+#define GB300_OPT_TENSOR         7
 int gb300_set_option (cholmod_common *Common, int option, int64_t value) ;
 
 /* Supernodal symbolic analysis of A (stype < 0, lower) with a given final

@@ -22,7 +22,7 @@ CHOLMOD_TOO_LARGE, CHOLMOD_INVALID, CHOLMOD_GPU_PROBLEM = -3, -4, -5
 CHOLMOD_NOT_POSDEF, CHOLMOD_DSMALL = 1, 2
 CHOLMOD_A = 0
 GB300_OPT_KEEP_ON_DEVICE, GB300_OPT_SMALL_COLS, GB300_OPT_PROFILE, GB300_OPT_SWEEP = 1, 2, 3, 4
-GB300_OPT_TRACE, GB300_OPT_FACTOR = 5, 6
+GB300_OPT_TRACE, GB300_OPT_FACTOR, GB300_OPT_TENSOR = 5, 6, 7
 KIND_NAMES = {1: "assemble", 2: "factor_small", 3: "potrf_diag", 4: "trsm_rows", 5: "gemm_tile",
               6: "task_graph", 15: "whole_graph"}
 

@@ -605,6 +605,170 @@ __device__ __forceinline__ void gemm_tile_f32(const float *A, int64_t lda, const
     }
 }
 
+// ---------------------------------------------------------------------------
+// tensor-core tile update (tcgen05, kind::tf32, accumulator in TMEM)
+// ---------------------------------------------------------------------------
+
+#define GB_TC_SPIN (1 << 22)
+
+// per block: TMEM accumulator (64 columns), the mbarrier the MMAs commit to,
+// and its phase; ok = 0 after a wait gave up
+struct gb_tc_ctx {
+    uint32_t taddr, mbar, phase;
+    int ok;
+};
+
+__device__ __forceinline__ uint32_t gb_su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: K-major, no swizzle; core matrices of 8
+// rows x 16 bytes, lbo = byte distance of core matrices adjacent along K,
+// sbo = along M/N; bit 46 = descriptor version of tcgen05
+__device__ __forceinline__ uint64_t gb_tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16)
+           | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ float gb_tf32_rna(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// element (m, k) of a K-major tile with a K chunk of 32 (4-byte elements):
+// lbo = 128 bytes, sbo = 1024 bytes
+__device__ __forceinline__ uint32_t gb_tc_off(int m, int k)
+{
+    return (uint32_t)((m >> 3) * 1024 + (k >> 2) * 128 + (m & 7) * 16 + (k & 3) * 4);
+}
+
+__device__ __forceinline__ bool gb_mbar_wait(uint32_t mbar, uint32_t phase)
+{
+    for (int it = 0; it < GB_TC_SPIN; it++) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}" : "=r"(done) : "r"(mbar), "r"(phase) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void gb_tc_mma(uint32_t taddr, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t accumulate)
+{
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                 " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}"
+                 :: "r"(taddr), "l"(a), "l"(b), "r"(idesc), "r"(accumulate) : "memory");
+}
+
+// C[0:m, 0:n] -= A[0:m, 0:k] B[0:n, 0:k]' (m, n <= 64, column-major; lower:
+// only entries with row - col >= diag_off) on the tensor cores with 256
+// threads.  FP32 operands are split x = hi + lo with hi = x rounded to TF32
+// and the product is hi*hi + hi*lo + lo*hi (3 MMAs of kind::tf32 per K step
+// of 8, FP32 accumulation in TMEM), which keeps the error near that of an
+// FP32 sum.  The MMA is M = 128 x N = 64 with A's rows 64..127 zero, so row
+// i of the accumulator is TMEM lane i.  Per K chunk of 32 the operands are
+// split and stored in the canonical K-major layout (smem: 48 KB), thread 0
+// issues the 12 MMAs and commits them to the mbarrier, and the next chunk's
+// global loads run while the tensor cores work.  Returns false when a wait
+// gave up (tc.ok = 0).
+static __device__ __noinline__ bool gemm_tile_tc(const float *A, int64_t lda, const float *B, int64_t ldb, float *C,
+                             int64_t ldc, int m, int n, int k, bool lower, int diag_off,
+                             unsigned char *smem, gb_tc_ctx &tc)
+{
+    if (k <= 0) return true;
+    unsigned char *Ahi = smem, *Alo = smem + 16384, *Bhi = smem + 32768, *Blo = smem + 40960;
+    const int tid = threadIdx.x;
+    // rows 64..127 of the A tiles are zero
+    for (int i = tid; i < 2048; i += blockDim.x) {
+        ((float *)(Ahi + 8192))[i] = 0.0f;
+        ((float *)(Alo + 8192))[i] = 0.0f;
+    }
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(64 >> 3) << 17)
+                           | ((uint32_t)(128 >> 4) << 24);
+    // loader: element q of this thread is row (tid & 63), k offset (tid >> 6) + 4q
+    const int li = tid & 63, lk = tid >> 6;
+    float ra[8], rb[8];
+    auto load = [&](int k0) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int kg = k0 + lk + 4 * q;
+            ra[q] = (li < m && kg < k) ? A[li + (int64_t)kg * lda] : 0.0f;
+            rb[q] = (li < n && kg < k) ? B[li + (int64_t)kg * ldb] : 0.0f;
+        }
+    };
+    load(0);
+    bool ok = true;
+    for (int k0 = 0; k0 < k; k0 += 32) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const uint32_t off = gb_tc_off(li, lk + 4 * q);
+            const float ah = gb_tf32_rna(ra[q]), bh = gb_tf32_rna(rb[q]);
+            *(float *)(Ahi + off) = ah;
+            *(float *)(Alo + off) = ra[q] - ah;
+            *(float *)(Bhi + off) = bh;
+            *(float *)(Blo + off) = rb[q] - bh;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const uint64_t dah = gb_tc_desc(gb_su32(Ahi) + j * 256, 128, 1024);
+                const uint64_t dal = gb_tc_desc(gb_su32(Alo) + j * 256, 128, 1024);
+                const uint64_t dbh = gb_tc_desc(gb_su32(Bhi) + j * 256, 128, 1024);
+                const uint64_t dbl = gb_tc_desc(gb_su32(Blo) + j * 256, 128, 1024);
+                gb_tc_mma(tc.taddr, dah, dbh, idesc, (k0 > 0 || j > 0) ? 1u : 0u);
+                gb_tc_mma(tc.taddr, dah, dbl, idesc, 1u);
+                gb_tc_mma(tc.taddr, dal, dbh, idesc, 1u);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         :: "r"(tc.mbar) : "memory");
+        }
+        if (k0 + 32 < k) load(k0 + 32);
+        // the MMAs read this chunk's operands: wait before they are replaced
+        if (!gb_mbar_wait(tc.mbar, tc.phase)) ok = false;
+        tc.phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        __syncthreads();
+        if (!ok) break;
+    }
+    if (!ok) {
+        tc.ok = 0;
+        return false;
+    }
+    // epilogue: lanes 0..63 of the accumulator, read by warps 0 and 1
+    const int warp = tid >> 5;
+    if (warp < 2) {
+        const int row = tid;
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+            uint32_t r[16];
+            const uint32_t a = tc.taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                           "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+                           "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                         : "r"(a) : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 16; q++) {
+                const int col = c0 + q;
+                if (row < m && col < n && !(lower && row - col < diag_off))
+                    C[row + (int64_t)col * ldc] -= __uint_as_float(r[q]);
+            }
+        }
+    }
+    // the next task's MMAs overwrite the accumulator: reads done first
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    return true;
+}
+
 static inline __host__ __device__ gb_dev_pattern gb_to_dev(const gb_pattern_ptrs *p)
 {
     gb_dev_pattern d;

@@ -171,7 +171,7 @@ __host__ __device__ constexpr size_t dag_smem()
 // smem_raw: dag_smem<T>() bytes.
 template <typename T>
 __device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx, T *CB, T *Linv,
-                              unsigned char *smem_raw, int &sfail)
+                              unsigned char *smem_raw, int &sfail, gb_tc_ctx *tc = nullptr)
 {
     T (*A)[65] = (T (*)[65])smem_raw;
     T *S1 = (T *)smem_raw + 64 * 65, *S2 = S1 + 64 * 65;
@@ -225,11 +225,18 @@ __device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx
             const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
             const int cs = 64 * tk.c, ce = min(cs + 64, nscol);
             const int rs = max(64 * tk.r, cs), re = min(64 * tk.r + 64, nsrow);
-            if constexpr (sizeof(T) == 4)
-                gemm_tile_f32(panel + rs + (int64_t)c0 * nsrow, nsrow,
-                              panel + cs + (int64_t)c0 * nsrow, nsrow,
-                              panel + rs + (int64_t)cs * nsrow, nsrow,
-                              re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, (float *)smem_raw);
+            if constexpr (sizeof(T) == 4) {
+                if (tc)
+                    gemm_tile_tc(panel + rs + (int64_t)c0 * nsrow, nsrow,
+                                 panel + cs + (int64_t)c0 * nsrow, nsrow,
+                                 panel + rs + (int64_t)cs * nsrow, nsrow,
+                                 re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, smem_raw, *tc);
+                else
+                    gemm_tile_f32(panel + rs + (int64_t)c0 * nsrow, nsrow,
+                                  panel + cs + (int64_t)c0 * nsrow, nsrow,
+                                  panel + rs + (int64_t)cs * nsrow, nsrow,
+                                  re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, (float *)smem_raw);
+            }
             else
                 gemm_tile_k64<T>(panel + rs + (int64_t)c0 * nsrow, nsrow,
                                  panel + cs + (int64_t)c0 * nsrow, nsrow,
@@ -240,11 +247,18 @@ __device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx
         if (f < 0) {
             const int m = nsrow - nscol;
             const int I = 64 * tk.r, J = 64 * tk.c;
-            if constexpr (sizeof(T) == 4)
-                gemm_tile_f32(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
-                              CB + P.cboff[s] + I + (int64_t)J * m, m,
-                              min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
-                              (float *)smem_raw);
+            if constexpr (sizeof(T) == 4) {
+                if (tc)
+                    gemm_tile_tc(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
+                                 CB + P.cboff[s] + I + (int64_t)J * m, m,
+                                 min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
+                                 smem_raw, *tc);
+                else
+                    gemm_tile_f32(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
+                                  CB + P.cboff[s] + I + (int64_t)J * m, m,
+                                  min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
+                                  (float *)smem_raw);
+            }
             else
                 gemm_tile_nt<T>(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
                                 CB + P.cboff[s] + I + (int64_t)J * m, m,
@@ -291,6 +305,7 @@ k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
 
 struct gb_fdag_dev {
     gb_dq Q;
+    int use_tc;              // FP32 tile products on the tensor cores
     const gb_fpat *pats;
     const gb_finst *inst;
     const int64_t *ibase;
@@ -314,16 +329,41 @@ __device__ __forceinline__ int fdag_instance(const gb_fdag_dev &D, int id)
     return lo;
 }
 
-template <typename T>
+template <typename T, bool TC>
 __global__ void __launch_bounds__(256, 2)
 k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ int sid, sinst, sfail, spoll;
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
     if (threadIdx.x == 0) spoll = dag_role(D.Q);
     __syncthreads();
     if (spoll == 2) return;
     const int poller = spoll;
+    // FP32: tile products on the tensor cores; a TMEM accumulator of 64
+    // columns for the block's lifetime (at most 2 blocks per SM: 128 of 512)
+    gb_tc_ctx tcx = {0u, 0u, 0u, 1};
+    gb_tc_ctx *tc = nullptr;
+    if constexpr (TC && sizeof(T) == 4) {
+        {
+            if (threadIdx.x == 0) {
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(gb_su32(&mbar)), "r"(1));
+                asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            }
+            if (threadIdx.x < 32) {
+                asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                             :: "r"(gb_su32(&tmem_base)), "r"(64));
+                asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            tcx.taddr = tmem_base;
+            tcx.mbar = gb_su32(&mbar);
+            tc = &tcx;
+        }
+    }
     for (;;) {
         if (threadIdx.x == 0) {
             sid = dag_pop(D.Q, poller);
@@ -331,7 +371,7 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
         }
         __syncthreads();
         const int id = sid;
-        if (id < 0) return;
+        if (id < 0) break;
         if (D.trace && threadIdx.x == 0) {
             D.trace[3 * (size_t)id] = dag_timer();
             D.trace[3 * (size_t)id + 2] = blockIdx.x;
@@ -381,7 +421,16 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                     __syncthreads();
                 }
         } else {
-            dag_tile_task<T>(P, tk, Lx, CB, Linv, smem_raw, sfail);
+            dag_tile_task<T>(P, tk, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr);
+            if (TC && tc && !tcx.ok) {
+                // a tensor-core wait gave up: stop the executor (every block
+                // returns on the error word)
+                if (threadIdx.x == 0) {
+                    atomicExch(D.Q.ctrl + 5, 1);
+                    atomicExch(D.Q.err, 1);
+                }
+                break;
+            }
         }
         __syncthreads();
         if (threadIdx.x < 32) {
@@ -406,6 +455,17 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
             }
         }
     }
+    if (TC && tc) {
+        if (!tcx.ok) {
+            // MMAs may still be in flight: wait once more (bounded) before
+            // the accumulator is released
+            gb_mbar_wait(tcx.mbar, tcx.phase);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x < 32)
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tcx.taddr), "r"(64));
+    }
 }
 
 extern "C" {
@@ -420,16 +480,22 @@ int gb_launch_fdag(const gb_fdag_args *a, void *Lx, void *CB, void *Linv, int dt
     D.pats = a->pats; D.inst = a->inst; D.ibase = a->inst_base; D.ninst = a->ninst;
     D.cnt = a->cnt; D.trace = a->trace;
     D.Sx = a->Sx; D.a_dtype = a->a_dtype; D.scale = a->scale; D.beta = a->beta;
+    D.use_tc = a->use_tc;
     static int configured = 0;
     if (!configured) {
-        cudaFuncSetAttribute(k_fdag<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<double>());
-        cudaFuncSetAttribute(k_fdag<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<float>());
+        cudaFuncSetAttribute(k_fdag<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<double>());
+        cudaFuncSetAttribute(k_fdag<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<float>());
+        cudaFuncSetAttribute(k_fdag<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<float>());
         configured = 1;
     }
     if (grid > a->ntotal + GB_DAG_POLLERS) grid = (int)(a->ntotal + GB_DAG_POLLERS);
     if (grid < GB_DAG_POLLERS + 1) grid = GB_DAG_POLLERS + 1;
-    if (dtype == 0) k_fdag<double><<<grid, 256, dag_smem<double>(), st>>>(D, (double *)Lx, (double *)CB, (double *)Linv);
-    else k_fdag<float><<<grid, 256, dag_smem<float>(), st>>>(D, (float *)Lx, (float *)CB, (float *)Linv);
+    if (dtype == 0)
+        k_fdag<double, false><<<grid, 256, dag_smem<double>(), st>>>(D, (double *)Lx, (double *)CB, (double *)Linv);
+    else if (D.use_tc)
+        k_fdag<float, true><<<grid, 256, dag_smem<float>(), st>>>(D, (float *)Lx, (float *)CB, (float *)Linv);
+    else
+        k_fdag<float, false><<<grid, 256, dag_smem<float>(), st>>>(D, (float *)Lx, (float *)CB, (float *)Linv);
     return (int)cudaGetLastError();
 }
 

@@ -27,6 +27,7 @@ gb_ctx *gb_ctx_new(void)
     c->device = -1;
     c->sweep_mode = 1;
     c->factor_mode = 1;
+    c->tc_mode = 0;
     return c;
 }
 
@@ -71,6 +72,7 @@ int gb300_set_option(cholmod_common *Common, int option, int64_t value)
     if (option == GB300_OPT_KEEP_ON_DEVICE) c->opt_keep = value ? 1 : 0;
     else if (option == GB300_OPT_SWEEP) c->sweep_mode = value ? 1 : 0;
     else if (option == GB300_OPT_FACTOR) c->factor_mode = value ? 1 : 0;
+    else if (option == GB300_OPT_TENSOR) c->tc_mode = value ? 1 : 0;
     else if (option == GB300_OPT_TRACE) c->trace_on = value ? 1 : 0;
     else if (option == GB300_OPT_PROFILE) {
         c->prof = value ? 1 : 0;
@@ -330,6 +332,7 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
         a.a_dtype = adt;
         a.scale = scale;
         a.beta = beta;
+        a.use_tc = ctx->tc_mode;
         if (ctx->trace_on) {
             size_t need = 3 * (N + 1) * sizeof(unsigned long long);
             if (gb_dev_grow((void **)&ctx->d_ftrace, &ctx->ftrace_cap, need)) {
@@ -469,8 +472,17 @@ int gb_run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int fo
     int d = dt_index(l_dtype);
     int ldt = l_dtype == CHOLMOD_SINGLE ? 4 : 0;
     size_t e = dt_size(l_dtype);
-    if (!gb_dev_grow(&P->d_U, &P->u_cap, e * GB_MAX(P->cbv_total, 1) * nrhs)) return FALSE;
     const void *Lx = P->d_Lx[d];
+    if (ctx->sweep_mode == 1 && nrhs > GB_SWEEP_COLS) {
+        /* passes of GB_SWEEP_COLS columns: each pass's update vectors
+         * (cbv_total x GB_SWEEP_COLS entries) stay resident in L2 */
+        for (int k0 = 0; k0 < nrhs; k0 += GB_SWEEP_COLS)
+            if (!gb_run_sweep(P, ctx, l_dtype, GB_MIN(GB_SWEEP_COLS, nrhs - k0),
+                              (char *)Y + e * (size_t)k0 * (size_t)P->n, forward))
+                return FALSE;
+        return TRUE;
+    }
+    if (!gb_dev_grow(&P->d_U, &P->u_cap, e * GB_MAX(P->cbv_total, 1) * nrhs)) return FALSE;
     if (ctx->sweep_mode == 1) {
         if (!P->linv_valid[d] && !gb_run_inverse(P, ctx, l_dtype)) return FALSE;
         gb_sweep1_args a;

@@ -83,7 +83,11 @@ typedef struct {
     int a_dtype;                     /* 0 double, 4 single */
     const double *scale;             /* optional D A D scaling */
     double beta;
+    int use_tc;                      /* FP32 tile products on the tensor cores */
 } gb_fdag_args;
+
+/* right-hand-side columns per single-launch sweep pass */
+#define GB_SWEEP_COLS 16
 
 /* a chunk of rows of one segment, for segmented reductions */
 typedef struct { int64_t lo, hi; int32_t seg, pad; } gb_seg_chunk;
@@ -221,6 +225,7 @@ struct gb_ctx {
     int prof;
     int sweep_mode;              /* 1 = single-launch sweeps (default), 0 = per level */
     int factor_mode;             /* 1 = one whole-factorization launch (default), 0 = per level */
+    int tc_mode;                 /* 1 = FP32 tile products on the tensor cores (default 0) */
     int trace_on;                /* record per-task times of the sweeps */
     unsigned long long *d_trace; /* device trace buffer (3 x tasks) */
     size_t trace_cap;

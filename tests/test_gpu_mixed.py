@@ -73,3 +73,20 @@ def test_mixed_not_positive_definite(golden, lib):
     assert L.contents.minor == meta["npd"]["minor"]
     CH.free_factor(L, c)
     CH.free_sparse(A, c)
+
+
+def test_refined_tensor_core_tiles(golden, lib, oracle_mod):
+    """The FP32 factorization with its tile products on the tensor cores
+    (GB300_OPT_TENSOR: tcgen05, 3xTF32) still refines to the FP64 target."""
+    meta, arrays = golden
+    for name in ("g3", "c1"):
+        c = CH.Common()
+        c.set_option(CH.GB300_OPT_TENSOR, 1)
+        mat, A, L = setup(meta, arrays, name, c)
+        assert CH.factorize_mixed(A, L, c) == 1
+        B = M.rhs(mat[0], 4, 31)
+        X, info = CH.solve_refined(A, L, B, c, tol=TOL)
+        be = oracle_mod.backward_error(*mat, X, B)
+        assert be.max() <= TOL and not info["fp64_fallback"], (name, be.max(), info)
+        CH.free_factor(L, c)
+        CH.free_sparse(A, c)
