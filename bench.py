@@ -11,9 +11,9 @@ A) followed by one refined solve to 1e-12 with one right-hand side.
   value       = fl / device time of the factorization, inputs resident on the
                 GPU (CUDA events on the library's stream)
   e2e         = the same through the C ABI from host buffers
-                (gb300_factorize_mixed + gb300_solve_refined, pinned B/X,
-                host permutation, host->device copies and the read of X inside
-                the timed region)
+                (gb300_factorize_mixed + gb300_solve_refined: the copy of A's
+                values, their permutation on the GPU, the copy of B and the
+                read of X inside the timed region)
   --impl reference  times the CPU oracle (the reference's left-looking
                 supernodal algorithm over OpenBLAS, all host cores) on the same
                 matrix in FP64, the form the reference CPU path computes.
@@ -315,9 +315,9 @@ def run_gpu(args):
     value = fl / (t_fac * 1e-3) / 1e12 * ws
     e2e_val = fl / statistics.mean(e2e_s) / 1e12 * ws
     nnz = int(Ap[-1])
-    # bytes moved per e2e step: S (p, i, x) and both triangles of A (p, j, x),
-    # the scaling vectors, B in; X out
-    h2d = 8 * (n + 1) + 16 * nnz + 8 * (n + 1) + 12 * (2 * nnz - n) + 16 * n + 8 * n
+    # bytes moved per e2e step: A's values (the pattern's device maps form S,
+    # the rows of A and the scaling on the GPU) and B in; X out
+    h2d = 8 * nnz + 8 * n
     d2h = 8 * n
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws,

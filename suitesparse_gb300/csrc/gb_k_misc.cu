@@ -213,6 +213,35 @@ __global__ void k_anorm_seg(const gb_seg_chunk *__restrict__ chunks, const int64
         atomicMax((unsigned long long *)&out[ch.seg], (unsigned long long)__double_as_longlong(sm[0]));
 }
 
+// dst[q] = src[map[q]] (device-side value permutation)
+__global__ void k_gather(int64_t n, const int64_t *__restrict__ map, const double *__restrict__ src,
+                         double *__restrict__ dst)
+{
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x)
+        dst[q] = src[map[q]];
+}
+
+// scale[i] = A(i,i)^-1/2 (1 when not positive or absent), scale_perm[k] =
+// scale[Perm[k]]: the diagonal scaling D of the mixed factorization
+__global__ void k_diag_scale(int64_t n, const int64_t *__restrict__ dmap, const double *__restrict__ Ax,
+                             double *__restrict__ scale)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double d = dmap[i] >= 0 ? Ax[dmap[i]] : 0.0;
+        scale[i] = d > 0 ? 1.0 / sqrt(d) : 1.0;
+    }
+}
+
+__global__ void k_permute_vec(int64_t n, const int64_t *__restrict__ Perm, const double *__restrict__ v,
+                              double *__restrict__ out)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        out[k] = v[Perm[k]];
+}
+
 // zero factor entries [from, to) (not-positive-definite clean-up)
 template <typename T>
 __global__ void k_zero_range(T *x, int64_t from, int64_t to)
@@ -309,6 +338,7 @@ int gb_launch_diag_minmax(int nsuper, const int64_t *Super, const int64_t *Pi,
                           const int64_t *Px, const void *Lx, int dtype, double *out,
                           cudaStream_t st)
 {
+    if (!out || !Lx) return (int)cudaErrorInvalidValue;
     k_minmax_init<<<1, 1, 0, st>>>(out);
     const int g = gb_grid_for(nsuper);
     if (dtype == 0) k_diag_minmax<double><<<g, 256, 0, st>>>(nsuper, Super, Pi, Px, (const double *)Lx, out);
@@ -319,6 +349,7 @@ int gb_launch_diag_minmax(int nsuper, const int64_t *Super, const int64_t *Pi,
 int gb_launch_colmax3(int64_t n, int nrhs, const double *R, int64_t ldr, const double *X,
                       int64_t ldx, const double *B, int64_t ldb, double *out, cudaStream_t st)
 {
+    if (!out || !R || !X || !B) return (int)cudaErrorInvalidValue;
     if (cudaMemsetAsync(out, 0, sizeof(double) * 3 * nrhs, st) != cudaSuccess) return 1;
     int gx = (int)((n + 255) / 256);
     if (gx > 304) gx = 304;
@@ -339,6 +370,7 @@ int gb_launch_colmax3_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t ns
                           const double *R, int64_t ldr, const double *X, int64_t ldx,
                           const double *B, int64_t ldb, double *out, cudaStream_t st)
 {
+    if (!out || !chunks || !R || !X || !B) return (int)cudaErrorInvalidValue;
     if (cudaMemsetAsync(out, 0, sizeof(double) * 3 * nseg * nrhs, st) != cudaSuccess) return 1;
     if (nchunk <= 0 || nrhs <= 0) return 0;
     dim3 grid((unsigned)nchunk, (unsigned)nrhs);
@@ -349,9 +381,28 @@ int gb_launch_colmax3_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t ns
 int gb_launch_anorm_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t nseg, const int64_t *Rp,
                         const double *Rx, double *out, cudaStream_t st)
 {
+    if (!out || !chunks || !Rp || !Rx) return (int)cudaErrorInvalidValue;
     if (cudaMemsetAsync(out, 0, sizeof(double) * nseg, st) != cudaSuccess) return 1;
     if (nchunk <= 0) return 0;
     k_anorm_seg<<<(unsigned)nchunk, 256, 0, st>>>(chunks, Rp, Rx, out);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_gather(int64_t n, const int64_t *map, const double *src, double *dst, cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    if (!map || !src || !dst) return (int)cudaErrorInvalidValue;
+    k_gather<<<gb_grid_for(n), 256, 0, st>>>(n, map, src, dst);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_diag_scale(int64_t n, const int64_t *dmap, const double *Ax, const int64_t *Perm,
+                         double *scale, double *scale_perm, cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    if (!dmap || !Ax || !Perm || !scale || !scale_perm) return (int)cudaErrorInvalidValue;
+    k_diag_scale<<<gb_grid_for(n), 256, 0, st>>>(n, dmap, Ax, scale);
+    k_permute_vec<<<gb_grid_for(n), 256, 0, st>>>(n, Perm, scale, scale_perm);
     return (int)cudaGetLastError();
 }
 

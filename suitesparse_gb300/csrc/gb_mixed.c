@@ -145,11 +145,26 @@ int gb300_factorize_mixed(cholmod_sparse *A, cholmod_factor *L, cholmod_common *
     if (!ctx || !gb_ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return FALSE; }
     gb_plan *P = gb_plan_get(L, Common, ctx, 1);
     if (!P) return FALSE;
-    cholmod_sparse *S = gb_permute_lower(A, L->Perm, Common);
-    if (!S) return FALSE;
-    int ok = gb_upload_input(P, ctx, S, CHOLMOD_DOUBLE) && upload_full_A(P, ctx, A, Common)
+    /* values of S = tril(PAP'), rows of A and the scaling: gathered on the
+     * device through per-pattern maps, or formed on the host */
+    int ok = TRUE;
+    if (!P->d_red) {                     /* pivot check and reduction words */
+        size_t cap = 0;
+        ok = gb_dev_grow((void **)&P->d_red, &cap, sizeof(double) * 64);
+    }
+    if (!ok) {
+        GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "device allocation failed");
+        return FALSE;
+    }
+    if (gb_valmap_apply(P, ctx, A, Common)) {
+        ok = gb_ensure_numeric(P, CHOLMOD_SINGLE);
+    } else {
+        cholmod_sparse *S = gb_permute_lower(A, L->Perm, Common);
+        if (!S) return FALSE;
+        ok = gb_upload_input(P, ctx, S, CHOLMOD_DOUBLE) && upload_full_A(P, ctx, A, Common)
              && gb_ensure_numeric(P, CHOLMOD_SINGLE);
-    gb300_free_sparse(&S, Common);
+        gb300_free_sparse(&S, Common);
+    }
     if (!ok) {
         if (Common->status == CHOLMOD_OK) GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed");
         return FALSE;

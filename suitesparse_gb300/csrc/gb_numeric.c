@@ -584,6 +584,7 @@ int gb_upload_input(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, int a_dtype)
     const Int *Ap = A->p;
     Int nz = Ap[n];
     size_t e = dt_size(a_dtype);
+    P->s_from_vm = 0;           /* d_Sp/d_Si now hold this S's pattern */
     if (!gb_dev_grow((void **)&P->d_Sp, &P->sp_cap, sizeof(int64_t) * (n + 1))) return FALSE;
     if (!gb_dev_grow((void **)&P->d_Si, &P->si_cap, sizeof(int64_t) * GB_MAX(nz, 1))) return FALSE;
     if (!gb_dev_grow(&P->d_Sx, &P->sx_cap, e * GB_MAX(nz, 1))) return FALSE;

@@ -188,6 +188,13 @@ typedef struct gb_plan {
     /* full (both triangles) FP64 copy of A for residuals, plus scaling */
     int64_t *d_Rp;
     int32_t *d_Rj;
+    /* value maps of the caller's A (gb_valmap.c) */
+    int vm_valid, vm_packed, s_from_vm;
+    int64_t vm_n, vm_xlen, vm_snz, vm_rnz;
+    int64_t *h_vm_Ap, *h_vm_Ai, *h_vm_Anz, *h_vm_Sp, *h_vm_Si;
+    int64_t *d_smap, *d_rmap, *d_dmap;
+    double *d_Ax;
+    size_t ax_cap;
     double *d_Rx, *d_scale, *d_scale_perm, *d_X, *d_R, *d_bx, *d_red;
     size_t rp_cap, rj_cap, rx_cap, x_cap, r_cap, bx_cap;
     uint64_t a_hash;
@@ -244,6 +251,8 @@ int gb_vec_push(gb_vec *v, const void *e);
 void gb_vec_free(gb_vec *v);
 
 /* Build the plan (host side) for a supernodal symbolic factor. */
+int gb_valmap_apply(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, cholmod_common *Common);
+void gb_valmap_free(gb_plan *P);
 gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols);
 /* Upload the pattern, task arrays and launch sequences. */
 int gb_plan_upload(gb_plan *P);
@@ -295,6 +304,9 @@ int gb_launch_residual(int64_t n, int nrhs, const int64_t *Rp, const int32_t *Rj
 int gb_launch_colmax3(int64_t n, int nrhs, const double *R, int64_t ldr, const double *X,
                       int64_t ldx, const double *B, int64_t ldb, double *out, cudaStream_t st);
 int gb_launch_anorm(int64_t n, const int64_t *Rp, const double *Rx, double *out, cudaStream_t st);
+int gb_launch_gather(int64_t n, const int64_t *map, const double *src, double *dst, cudaStream_t st);
+int gb_launch_diag_scale(int64_t n, const int64_t *dmap, const double *Ax, const int64_t *Perm,
+                         double *scale, double *scale_perm, cudaStream_t st);
 int gb_launch_anorm_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t nseg, const int64_t *Rp,
                         const double *Rx, double *out, cudaStream_t st);
 int gb_launch_colmax3_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t nseg, int nrhs,
