@@ -25,8 +25,11 @@
 // over 4 lanes with shuffles (no padded right-hand sides: the FP64 pipe of
 // this GPU issues under 2 multiply-adds per clock per SM).
 //
-// A task only waits for tasks with smaller tickets, which were taken by
-// blocks already running, so the sweep cannot deadlock.  Every wait gives up
+// A ticket names a group of consecutive tasks (runs of leaf-level tasks, 8
+// per ticket; other tasks alone), run in order by the block that took it.  A
+// task only waits for tasks listed before it, which belong to its own group
+// (already done) or to groups taken by blocks already running, so the sweep
+// cannot deadlock.  Every wait gives up
 // after GB_SPIN_LIMIT polls, sets the error word and returns; every other
 // waiter then returns at once.  Linv holds the inverse of every diagonal
 // block (k_diag_inverse, after the factorization).
@@ -144,6 +147,8 @@ __device__ void tile_gemv(const T *tile, int trans, int nr, int nc, const T *xs,
 struct gb_sweep_state {
     const gb_stask *tasks;
     int ntasks;
+    const int32_t *gptr;       // tickets name groups: tasks [gptr[g], gptr[g+1])
+    int ngroups;
     const int32_t *blkoff;     // first global diagonal-block id of s
     const int64_t *linvoff;    // offset of each diagonal block's inverse
     const int32_t *ntask_s;    // tasks of supernode s in this sweep
@@ -157,19 +162,21 @@ template <typename T>
 __host__ __device__ constexpr size_t sweep_smem() { return sizeof(T) * (2 * SR * TLD + 2 * SR * RCH); }
 
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 k_fwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int nrhs,
             T *Y, int64_t ldy, T *U)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *tA = (T *)smem_raw, *tB = tA + SR * TLD, *xs = tB + SR * TLD, *ys = xs + SR * RCH;
-    __shared__ int st, abort_;
+    __shared__ int sg, abort_;
     T reg[16];
     for (;;) {
-        if (threadIdx.x == 0) { st = atomicAdd(S.ticket, 1); abort_ = 0; }
+        if (threadIdx.x == 0) { sg = atomicAdd(S.ticket, 1); abort_ = 0; }
         __syncthreads();
-        const int t = st;
-        if (t >= S.ntasks) return;
+        const int g = sg;
+        if (g >= S.ngroups) return;
+        const int tend = S.gptr[g + 1];
+        for (int t = S.gptr[g]; t < tend; t++) {
         const gb_stask tk = S.tasks[t];
         if (S.trace && threadIdx.x == 0) S.trace[3 * (size_t)t] = gtimer();
         const int s = tk.s;
@@ -182,6 +189,12 @@ k_fwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
         T *us = U + P.cbvoff[s] * nrhs;
         const int r0 = tk.r0, nr = tk.nr;
         const int nblk = (nscol + SR - 1) / SR;
+        // the diagonal block's inverse depends on nothing: parked in tB
+        // before any wait, off the dependency chain
+        if (tk.kind == 0) {
+            tile_fetch(reg, Linv + S.linvoff[S.blkoff[s] + tk.idx], nr, nr, nr);
+            tile_park(tB, reg);
+        }
         // first L tile this task needs, fetched before any wait
         if (tk.kind == 0 && tk.idx > 0) tile_fetch(reg, panel + r0, nsrow, nr, SR);
         else if (tk.kind == 1) tile_fetch(reg, panel + r0, nsrow, nr, min(SR, nscol));
@@ -243,9 +256,7 @@ k_fwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
                     if (j + 1 < i) tile_fetch(reg, panel + r0 + (int64_t)((j + 1) * SR) * nsrow, nsrow, nr, SR);
                     tile_gemv<T>(tA, 0, nr, min(SR, nscol - j * SR), xs, ys, nk, (T)-1);
                 }
-                // x_i = Linv_ii ys
-                tile_fetch(reg, Linv + S.linvoff[S.blkoff[s] + i], nr, nr, nr);
-                tile_park(tB, reg);
+                // x_i = Linv_ii ys (Linv_ii parked in tB at the start)
                 for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
                     xs[idx] = ys[idx];
                     ys[idx] = (T)0;
@@ -292,23 +303,26 @@ k_fwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
             if (S.trace) S.trace[3 * (size_t)t + 2] = gtimer();
         }
         __syncthreads();
+        }
     }
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 k_bwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int nrhs,
             T *Y, int64_t ldy)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *tA = (T *)smem_raw, *tB = tA + SR * TLD, *xs = tB + SR * TLD, *ys = xs + SR * RCH;
-    __shared__ int st, abort_;
+    __shared__ int sg, abort_;
     T reg[16];
     for (;;) {
-        if (threadIdx.x == 0) { st = atomicAdd(S.ticket, 1); abort_ = 0; }
+        if (threadIdx.x == 0) { sg = atomicAdd(S.ticket, 1); abort_ = 0; }
         __syncthreads();
-        const int t = st;
-        if (t >= S.ntasks) return;
+        const int g = sg;
+        if (g >= S.ngroups) return;
+        const int tend = S.gptr[g + 1];
+        for (int t = S.gptr[g]; t < tend; t++) {
         const gb_stask tk = S.tasks[t];
         if (S.trace && threadIdx.x == 0) S.trace[3 * (size_t)t] = gtimer();
         const int s = tk.s;
@@ -322,6 +336,9 @@ k_bwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
         const int par = S.parent[s];
         const int i = tk.idx, r0 = tk.r0, nr = tk.nr;
         const int nblk = (nscol + SR - 1) / SR;
+        // the diagonal block's inverse, parked in tB before any wait
+        tile_fetch(reg, Linv + S.linvoff[S.blkoff[s] + i], nr, nr, nr);
+        tile_park(tB, reg);
         // first L21 tile: rows nscol.., columns of block i
         if (m > 0) tile_fetch(reg, panel + nscol + (int64_t)r0 * nsrow, nsrow, min(SR, m), nr);
         if (threadIdx.x == 0 && par >= 0) {
@@ -373,9 +390,7 @@ k_bwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
                     tile_fetch(reg, panel + (j - 1) * SR + (int64_t)r0 * nsrow, nsrow, SR, nr);
                 tile_gemv<T>(tA, 1, nr, nc, xs, ys, nk, (T)-1);
             }
-            // x_i = Linv_ii' ys
-            tile_fetch(reg, Linv + S.linvoff[S.blkoff[s] + i], nr, nr, nr);
-            tile_park(tB, reg);
+            // x_i = Linv_ii' ys (Linv_ii parked in tB at the start)
             for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
                 xs[idx] = ys[idx];
                 ys[idx] = (T)0;
@@ -395,6 +410,7 @@ k_bwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
             if (S.trace) S.trace[3 * (size_t)t + 2] = gtimer();
         }
         __syncthreads();
+        }
     }
 }
 
@@ -443,7 +459,8 @@ int gb_launch_sweep1(int forward, const gb_pattern_ptrs *pp, const gb_sweep1_arg
     S.tasks = a->tasks; S.ntasks = a->ntasks; S.blkoff = a->blkoff; S.linvoff = a->linvoff;
     S.ntask_s = a->ntask_s; S.parent = a->parent; S.xready = a->xready; S.done = a->done;
     S.ticket = a->ticket; S.err = a->err; S.trace = a->trace;
-    if (grid > a->ntasks) grid = a->ntasks;
+    S.gptr = a->gptr; S.ngroups = a->ngroups;
+    if (grid > a->ngroups) grid = a->ngroups;
     static int configured = 0;
     if (!configured) {
         cudaFuncSetAttribute(k_fwd_sweep<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double>());

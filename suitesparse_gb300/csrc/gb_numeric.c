@@ -488,6 +488,8 @@ int gb_run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int fo
         gb_sweep1_args a;
         a.tasks = forward ? P->d_sf : P->d_sb;
         a.ntasks = (int)(forward ? P->sf_t.n : P->sb_t.n);
+        a.gptr = forward ? P->d_gf : P->d_gb;
+        a.ngroups = (int)(forward ? P->gf.n : P->gb.n) - 1;
         a.blkoff = P->d_blkoff;
         a.linvoff = P->d_linvoff;
         a.ntask_s = forward ? P->d_ntask_f : P->d_ntask_b;

@@ -348,6 +348,8 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
     vec_init(&P->gemm_owner, sizeof(int32_t));
     vec_init(&P->sweep_t, sizeof(gb_sweep_task));
     vec_init(&P->sf_t, sizeof(gb_stask));
+    vec_init(&P->gf, sizeof(int32_t));
+    vec_init(&P->gb, sizeof(int32_t));
     vec_init(&P->sb_t, sizeof(gb_stask));
     vec_init(&P->sd_t, sizeof(gb_stask));
     vec_init(&P->fact_seq, sizeof(gb_launch_rec));
@@ -809,6 +811,32 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
             }
         }
     }
+    /* ticket groups: runs of tasks of leaf-level supernodes (levels 0-1, at
+     * most 64 columns and 64 rows), 8 per ticket, so that the tens of
+     * thousands of tiny tasks do not serialise on the ticket counter; every
+     * other task is a group of its own.  A block runs its group in order, and
+     * a task still depends only on tasks listed before it. */
+    for (int w = 0; w < 2 && ok; w++) {
+        gb_vec *tv = w ? &P->sb_t : &P->sf_t, *gv = w ? &P->gb : &P->gf;
+        const gb_stask *tt = tv->p;
+        int32_t start = 0;
+        ok &= gb_vec_push(gv, &start);
+        size_t q = 0;
+        while (ok && q < tv->n) {
+            size_t e = q + 1;
+            Int s = tt[q].s;
+            int small = level[s] <= 1 && Super[s + 1] - Super[s] <= 64 && Pi[s + 1] - Pi[s] <= 64;
+            if (small)
+                while (e < tv->n && e - q < 8) {
+                    Int s2 = tt[e].s;
+                    if (!(level[s2] <= 1 && Super[s2 + 1] - Super[s2] <= 64 && Pi[s2 + 1] - Pi[s2] <= 64)) break;
+                    e++;
+                }
+            int32_t end = (int32_t)e;
+            ok &= gb_vec_push(gv, &end);
+            q = e;
+        }
+    }
     P->nblk_total = nblk_total;
     P->h_linvoff = malloc(sizeof(int64_t) * (nblk_total + 1));
     if (!P->h_linvoff) ok = 0;
@@ -912,6 +940,8 @@ int gb_plan_upload(gb_plan *P)
         if (cudaMemset(P->d_dag_smf, 0, sizeof(int32_t) * GB_DAG_NSMF) != cudaSuccess) goto fail;
     }
     UP(P->d_sf, P->sf_t.p, P->sf_t.n * P->sf_t.esz);
+    UP(P->d_gf, P->gf.p, P->gf.n * P->gf.esz);
+    UP(P->d_gb, P->gb.p, P->gb.n * P->gb.esz);
     UP(P->d_sb, P->sb_t.p, P->sb_t.n * P->sb_t.esz);
     UP(P->d_sd, P->sd_t.p, P->sd_t.n * P->sd_t.esz);
     UP(P->d_blkoff, P->h_blkoff, sizeof(int32_t) * (ns + 1));
@@ -986,6 +1016,7 @@ void gb_plan_free(gb_plan *P)
     free(P->h_blkoff); free(P->h_ntask_f); free(P->h_ntask_b); free(P->h_parent);
     free(P->h_linvoff);
     gb_vec_free(&P->sf_t); gb_vec_free(&P->sb_t); gb_vec_free(&P->sd_t);
+    gb_vec_free(&P->gf); gb_vec_free(&P->gb);
     gb_vec_free(&P->dag_t); gb_vec_free(&P->dag_sp); gb_vec_free(&P->dag_succ);
     gb_vec_free(&P->dag_nd); gb_vec_free(&P->dag_q0); gb_vec_free(&P->dag_q1);
     gb_vec_free(&P->dag_lv);
@@ -1006,7 +1037,7 @@ void gb_plan_free(gb_plan *P)
                    P->d_dag_cnt, P->d_dag_q, P->d_dag_ctrl, P->d_dag_smf, P->d_fd_t,
                    P->d_fd_sp, P->d_fd_succ, P->d_fd_nd, P->d_fd_qi, P->d_fd_ctrl0,
                    P->d_fd_cnt, P->d_fd_q, P->d_fd_pat, P->d_fd_inst, P->d_fd_ibase,
-                   P->d_chunk, P->d_anorm_seg, P->d_bred};
+                   P->d_chunk, P->d_anorm_seg, P->d_bred, P->d_gf, P->d_gb};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++)
         if (dev[i]) cudaFree(dev[i]);
     gb_vec_free(&P->asm_t); gb_vec_free(&P->node_t); gb_vec_free(&P->potrf_t);

@@ -97,6 +97,8 @@ typedef struct { int64_t lo, hi; int32_t seg, pad; } gb_seg_chunk;
 typedef struct {
     const gb_stask *tasks;
     int ntasks;
+    const int32_t *gptr;        /* [ngroups+1]: tickets name groups of consecutive tasks */
+    int ngroups;
     const int32_t *blkoff;
     const int64_t *linvoff;
     const int32_t *ntask_s;
@@ -165,6 +167,8 @@ typedef struct gb_plan {
     gb_vec sf_t, sb_t, sd_t;          /* forward, backward, diagonal-block tasks */
     int64_t nblk_total, linv_total;
     gb_stask *d_sf, *d_sb, *d_sd;
+    gb_vec gf, gb;                    /* sweep task groups (forward, backward) */
+    int32_t *d_gf, *d_gb;
     int32_t *d_blkoff, *d_ntask_f, *d_ntask_b, *d_parent;
     int64_t *d_linvoff;
     int32_t *d_xready, *d_done, *d_ticket, *d_err;
