@@ -510,6 +510,14 @@ int gb300_server_stats (gb300_server *S, double *out, int nout) ;
 int gb300_server_destroy (gb300_server *S) ;
 double gb300_server_now (void) ;
 
+/* Failure-detection check (no counterpart in the reference): runs the
+ * library's bounded device-side wait on a flag that nothing sets, giving up
+ * after polls polls (each about 100 ns), the way every wait of the sweeps
+ * and task graphs gives up.  out[0] = 1 if the wait succeeded (it cannot),
+ * out[1] = the error word it set.  Returns TRUE when the kernel ran and the
+ * CUDA context is still usable afterwards. */
+int gb300_wait_probe (int64_t polls, int32_t *out) ;
+
 /* Backward error of solutions that are already in device memory, with no
  * allocation of any kind (no counterpart in the reference library).  For
  * callers that must not allocate while they run: a serving loop with a

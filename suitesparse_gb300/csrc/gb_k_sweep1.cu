@@ -65,16 +65,33 @@ __device__ __forceinline__ unsigned long long gtimer()
 }
 
 // thread 0 only: wait until *flag >= target; false on timeout / abort
-__device__ bool wait_ge(const int32_t *flag, int target, int32_t *err)
+__device__ bool wait_ge_n(const int32_t *flag, int target, int32_t *err, long long limit)
 {
     if (ld_acquire(flag) >= target) return true;
-    for (int it = 0; it < GB_SPIN_LIMIT; it++) {
+    for (long long it = 0; it < limit; it++) {
         __nanosleep(64);
         if (ld_acquire(flag) >= target) return true;
         if (ld_acquire(err)) return false;
     }
     atomicExch(err, 1);
     return false;
+}
+
+__device__ bool wait_ge(const int32_t *flag, int target, int32_t *err)
+{
+    return wait_ge_n(flag, target, err, GB_SPIN_LIMIT);
+}
+
+// the bounded wait on a flag that nothing sets: it gives up after limit
+// polls, sets the error word and returns (out[0] = whether the wait
+// succeeded, out[1] = the error word)
+__global__ void k_wait_probe(const int32_t *flag, int32_t *err, long long limit, int32_t *out)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const bool ok = wait_ge_n(flag, 1, err, limit);
+        out[0] = ok ? 1 : 0;
+        out[1] = ld_acquire(err);
+    }
 }
 
 // ---- 64x64 tiles: registers -> shared memory ------------------------------
@@ -479,6 +496,21 @@ int gb_launch_sweep1(int forward, const gb_pattern_ptrs *pp, const gb_sweep1_arg
         else k_bwd_sweep<float><<<grid, 256, sm, st>>>(P, S, (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy);
     }
     return (int)cudaGetLastError();
+}
+
+int gb300_wait_probe(int64_t polls, int32_t *out)
+{
+    if (!out || polls < 0 || polls > (1ll << 30)) return 0;
+    int32_t *d = NULL;
+    if (cudaMalloc((void **)&d, 4 * sizeof(int32_t)) != cudaSuccess) return 0;
+    int ok = cudaMemset(d, 0, 4 * sizeof(int32_t)) == cudaSuccess;
+    if (ok) {
+        k_wait_probe<<<1, 32>>>(d, d + 1, (long long)polls, d + 2);
+        ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess
+             && cudaMemcpy(out, d + 2, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost) == cudaSuccess;
+    }
+    cudaFree(d);
+    return ok;
 }
 
 int gb_launch_diag_inverse(const gb_pattern_ptrs *pp, const gb_stask *dtasks, int ndiag,
