@@ -236,9 +236,16 @@ def run_gpu(args):
     L = CH.analyze_perm(A, perm, c)
     assert fl is None or c["fl"] == fl
     B = M.rhs(n, 1, 1)
-    info = CH.factor_info(L, c)
     if gold.get("fl") is None:
         fl = c["fl"]
+    # schedule parameters (small/large cutoff, subtree size) by the autotuner
+    tuned = None
+    if not args.quick:
+        from suitesparse_gb300 import autotune as AT
+        best, table = AT.autotune(A, L, c, reps=2, mixed=True)
+        tuned = {"small_cols": best[0], "subtree_work": best[1],
+                 "table_ms": {f"{k[0]}/{k[1]}": v for k, v in table.items()}}
+    info = CH.factor_info(L, c)
 
     def step_mixed():
         t0 = time.perf_counter()
@@ -361,6 +368,7 @@ def run_gpu(args):
                      "fp64_fma_peak": peak64},
         "kernel_profile_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
         "plan": info,
+        "autotune": tuned,
         "gpu_launches": launches,
         "wall_s_timed_region": t_all,
         "clocks": clk.summary(),
@@ -396,6 +404,12 @@ def run_batch(args):
     c = CH.Common()
     b = BT.Batch(c, sides, pat, perms, mats)
     B = M.rhs(b.n, nrhs, 3)
+    from suitesparse_gb300 import autotune as AT
+    best, table = AT.autotune(b.A, b.L, c, reps=1, mixed=True,
+                              candidates=((64, 4_000_000), (64, 16_000_000), (64, 64_000_000),
+                                          (32, 16_000_000)))
+    tuned = {"small_cols": best[0], "subtree_work": best[1],
+             "table_ms": {f"{k[0]}/{k[1]}": v for k, v in table.items()}}
 
     def step():
         t0 = time.perf_counter()
@@ -455,7 +469,7 @@ def run_batch(args):
         "e2e": {"value": fl / statistics.mean(wall) / 1e12, "unit": "TFLOP/s",
                 "h2d_bytes_per_step": int(8 * (b.n + 1) + 16 * int(b.A.contents.nzmax) + 8 * b.n * nrhs),
                 "d2h_bytes_per_step": int(8 * b.n * nrhs)},
-        "plan": info_plan, "gpu_launches": launches, "clocks": clk.summary(),
+        "plan": info_plan, "autotune": tuned, "gpu_launches": launches, "clocks": clk.summary(),
     }
     b.free()
     c.finish()

@@ -340,6 +340,12 @@ int gb300_finish (cholmod_common *Common) ;
  *      the factorization; the factor stays resident on the GPU for solves.
  *  GB300_OPT_SMALL_COLS [64]: supernodes at most this wide are factorized by
  *      one thread block each; wider ones by the blocked multi-block path.
+ *      A change applies from the next factorization (the plan is rebuilt).
+ *  GB300_OPT_SUBTREE_WORK [4000000]: a subtree whose supernodes are all at
+ *      most GB300_OPT_SMALL_COLS wide and whose estimated work (sum of
+ *      nscol nsrow^2 + 1e4 per supernode) is at most this many flops is
+ *      factorized whole by one thread block; 0 = never.  A change applies
+ *      from the next factorization (the plan is rebuilt).
  *  GB300_OPT_PROFILE [0]: 1 = time every kernel launch of the factorization
  *      with CUDA events (summed per kernel kind, see gb300_get_profile); also
  *      clears the accumulated profile.
@@ -365,6 +371,7 @@ int gb300_finish (cholmod_common *Common) ;
 #define GB300_OPT_TRACE          5
 #define GB300_OPT_FACTOR         6
 #define GB300_OPT_TENSOR         7
+#define GB300_OPT_SUBTREE_WORK   8
 int gb300_set_option (cholmod_common *Common, int option, int64_t value) ;
 
 /* Supernodal symbolic analysis of A (stype < 0, lower) with a given final

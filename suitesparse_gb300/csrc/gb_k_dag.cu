@@ -395,31 +395,37 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                                         D.beta, Lx, CB);
         } else if (tk.type == GB_DT_SMALL) {
             factor_small_body<T>(P, tk.s, Lx, Linv, smem_raw, &sfail);
-        } else if (tk.type == GB_DT_NODE) {
-            // assembly chunk by chunk, LL', then every update-block tile
-            const int s = tk.s;
-            const int nscol = (int)(P.Super[s + 1] - P.Super[s]);
-            const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
-            const int m = nsrow - nscol;
+        } else if (tk.type == GB_DT_NODE || tk.type == GB_DT_SUBTREE) {
+            // a small supernode whole (NODE), or every supernode of a subtree
+            // in order, children first (SUBTREE): assembly chunk by chunk,
+            // LL', then every update-block tile.  A parent reads its
+            // children's update blocks written by this block before a barrier.
+            const int cnt = tk.type == GB_DT_NODE ? 1 : tk.r;
             const double *scale = D.scale ? D.scale + I.scale : nullptr;
-            for (int t0 = 0; t0 < nsrow; t0 += 64) {
-                const gb_asm_task a = {s, t0, min(t0 + 64, nsrow), 0};
-                if (D.a_dtype == 0)
-                    assemble_body<double, T>(P, a, PP.Sp, PP.Si, (const double *)D.Sx + I.sx,
-                                             scale, D.beta, Lx, CB);
-                else
-                    assemble_body<float, T>(P, a, PP.Sp, PP.Si, (const float *)D.Sx + I.sx,
-                                            scale, D.beta, Lx, CB);
-                __syncthreads();
-            }
-            factor_small_body<T>(P, s, Lx, Linv, smem_raw, &sfail);
-            __syncthreads();
-            for (int J = 0; J < m; J += 64)
-                for (int I0 = J; I0 < m; I0 += 64) {
-                    const gb_dtask ct = {GB_DT_CB, s, 0, I0 / 64, J / 64, 1, 0, 0};
-                    dag_tile_task<T>(P, ct, Lx, CB, Linv, smem_raw, sfail);
+            for (int q = 0; q < cnt; q++) {
+                const int s = tk.type == GB_DT_NODE ? tk.s : PP.sub_list[tk.b + q];
+                const int nscol = (int)(P.Super[s + 1] - P.Super[s]);
+                const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
+                const int m = nsrow - nscol;
+                for (int t0 = 0; t0 < nsrow; t0 += 64) {
+                    const gb_asm_task a = {s, t0, min(t0 + 64, nsrow), 0};
+                    if (D.a_dtype == 0)
+                        assemble_body<double, T>(P, a, PP.Sp, PP.Si, (const double *)D.Sx + I.sx,
+                                                 scale, D.beta, Lx, CB);
+                    else
+                        assemble_body<float, T>(P, a, PP.Sp, PP.Si, (const float *)D.Sx + I.sx,
+                                                scale, D.beta, Lx, CB);
                     __syncthreads();
                 }
+                factor_small_body<T>(P, s, Lx, Linv, smem_raw, &sfail);
+                __syncthreads();
+                for (int J = 0; J < m; J += 64)
+                    for (int I0 = J; I0 < m; I0 += 64) {
+                        const gb_dtask ct = {GB_DT_CB, s, 0, I0 / 64, J / 64, 1, 0, 0};
+                        dag_tile_task<T>(P, ct, Lx, CB, Linv, smem_raw, sfail);
+                        __syncthreads();
+                    }
+            }
         } else {
             dag_tile_task<T>(P, tk, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr);
             if (TC && tc && !tcx.ok) {

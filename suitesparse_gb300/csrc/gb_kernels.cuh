@@ -69,6 +69,12 @@ typedef struct { int32_t type, s, b, r, c, prio, pad0, pad1; } gb_dtask;
 /*   NODE  (s)                  a small supernode whole: assembly, LL' and
  *                              every update-block tile, in one task */
 #define GB_DT_NODE  8
+/*   SUBTREE (s, b = offset, r = count)  a whole subtree of small supernodes
+ *                              (list entries [b, b + r) of the pattern's
+ *                              subtree list, children first), each as NODE,
+ *                              in one task: no queue traffic inside it */
+#define GB_DT_SUBTREE 9
+#define GB_SUBTREE_WORK 4.0e6       /* work estimate per subtree task (flops) */
 #define GB_NODE_MAX_ROWS 256        /* small supernodes fused into NODE tasks */
 
 /* control words of one task-graph launch: [0] head0 [1] tail0 [2] head1

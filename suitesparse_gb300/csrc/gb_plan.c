@@ -106,9 +106,56 @@ static int fdag_build(gb_plan *P)
     for (size_t i = 0; i < P->fact_seq.n; i++)
         if (seq[i].kind == GB_K_SMALL) nsmall += (size_t)seq[i].count;
     const size_t A0 = ndag, S0 = A0 + nasm, JA0 = S0 + nsmall, JK0 = JA0 + (size_t)ns;
-    const size_t N = JK0 + (size_t)ns;
-    if (N >= (size_t)1 << 30) return 0;
+    const size_t SB0 = JK0 + (size_t)ns;
+    const int64_t *Pi = P->L->pi, *Sup = P->L->super;
     int ok = 1;
+    /* Subtrees of small supernodes run whole as one SUBTREE task: every
+     * supernode of the subtree at most small_cols wide and the estimated
+     * work (nscol nsrow^2 per supernode plus a fixed cost) at most
+     * GB_SUBTREE_WORK; the largest such subtrees are taken.  Their members'
+     * own tasks stay in the list as inert joins without edges. */
+    int32_t *sub_root = malloc(sizeof(int32_t) * (ns + 1));
+    double *work = calloc(ns + 1, sizeof(double));
+    char *elig = malloc(ns + 1);
+    size_t nsub = 0;
+    if (!sub_root || !work || !elig) ok = 0;
+    for (int64_t s = 0; ok && s < ns; s++) elig[s] = 1;
+    for (int64_t s = 0; ok && s < ns; s++) {          /* children before parents */
+        double nscol = (double)(Sup[s + 1] - Sup[s]), nsrow = (double)(Pi[s + 1] - Pi[s]);
+        work[s] += nscol * nsrow * nsrow + 1.0e4;
+        if (Sup[s + 1] - Sup[s] > P->small_cols) elig[s] = 0;
+        int32_t par = P->h_parent[s];
+        if (par >= 0) {
+            work[par] += work[s];
+            if (!elig[s]) elig[par] = 0;
+        }
+    }
+#define SUB_OK(s) (elig[s] && work[s] <= P->sub_work)
+    for (int64_t s = ns - 1; ok && s >= 0; s--) {      /* parents before children */
+        int32_t par = P->h_parent[s];
+        if (SUB_OK(s) && !(par >= 0 && SUB_OK(par))) { sub_root[s] = (int32_t)s; nsub++; }
+        else sub_root[s] = (par >= 0 && SUB_OK(s)) ? sub_root[par] : -1;
+    }
+#undef SUB_OK
+    int32_t *sub_off = ok ? calloc(ns + 2, sizeof(int32_t)) : NULL;
+    if (!sub_off) ok = 0;
+    for (int64_t s = 0; ok && s < ns; s++)
+        if (sub_root[s] >= 0) sub_off[sub_root[s] + 1]++;
+    for (int64_t s = 0; ok && s < ns; s++) sub_off[s + 1] += sub_off[s];
+    if (ok) {
+        /* members in ascending order: children before parents */
+        int32_t *fill = malloc(sizeof(int32_t) * (ns + 1)), *lst = malloc(sizeof(int32_t) * (ns + 1));
+        if (!fill || !lst) ok = 0;
+        for (int64_t s = 0; ok && s < ns; s++) fill[s] = sub_off[s];
+        for (int64_t s = 0; ok && s < ns; s++)
+            if (sub_root[s] >= 0) lst[fill[sub_root[s]]++] = (int32_t)s;
+        for (int64_t q = 0; ok && q < sub_off[ns]; q++) ok &= gb_vec_push(&P->fd_sub, &lst[q]);
+        free(fill);
+        free(lst);
+    }
+#define MEMBER(s) (sub_root[s] >= 0)
+    const size_t N = SB0 + nsub;
+    if (N >= (size_t)1 << 30) ok = 0;
     int32_t *potrf0 = malloc(sizeof(int32_t) * (ns + 1));
     int32_t *small_id = malloc(sizeof(int32_t) * (ns + 1));
     int32_t *cbp = calloc(ns + 2, sizeof(int32_t));
@@ -121,8 +168,7 @@ static int fdag_build(gb_plan *P)
     /* small supernodes with few rows run whole as one NODE task: their
      * assembly chunks and update-block tiles stay in the list as inert
      * joins without edges */
-    const int64_t *Pi = P->L->pi, *Sup = P->L->super;
-#define FUSED(s) (Sup[(s) + 1] - Sup[s] <= P->small_cols && Pi[(s) + 1] - Pi[s] <= GB_NODE_MAX_ROWS)
+#define FUSED(s) (MEMBER(s) || (Sup[(s) + 1] - Sup[s] <= P->small_cols && Pi[(s) + 1] - Pi[s] <= GB_NODE_MAX_ROWS))
     /* tasks */
     for (size_t i = 0; ok && i < ndag; i++) {
         gb_dtask t = dt[i];
@@ -143,7 +189,7 @@ static int fdag_build(gb_plan *P)
             if (seq[i].kind != GB_K_SMALL) continue;
             for (int32_t q = 0; ok && q < seq[i].count; q++) {
                 int32_t s = nt[seq[i].off + q].s;
-                gb_dtask t = {FUSED(s) ? GB_DT_NODE : GB_DT_SMALL, s, 0, 0, 0, 1, 0, 0};
+                gb_dtask t = {MEMBER(s) ? GB_DT_JOIN : FUSED(s) ? GB_DT_NODE : GB_DT_SMALL, s, 0, 0, 0, 1, 0, 0};
                 small_id[s] = (int32_t)(S0 + k++);
                 ok &= gb_vec_push(&P->fd_t, &t);
             }
@@ -154,6 +200,15 @@ static int fdag_build(gb_plan *P)
             gb_dtask t = {GB_DT_JOIN, (int32_t)s, w, 0, 0, 0, 0, 0};
             ok &= gb_vec_push(&P->fd_t, &t);
         }
+    int32_t *sub_id = ok ? malloc(sizeof(int32_t) * (ns + 1)) : NULL;
+    if (!sub_id) ok = 0;
+    for (int64_t s = 0, k = 0; ok && s < ns; s++) {
+        sub_id[s] = -1;
+        if (sub_root[s] != s) continue;
+        gb_dtask t = {GB_DT_SUBTREE, (int32_t)s, sub_off[s], sub_off[s + 1] - sub_off[s], 0, 1, 0, 0};
+        sub_id[s] = (int32_t)(SB0 + k++);
+        ok &= gb_vec_push(&P->fd_t, &t);
+    }
     /* update-block tiles of each supernode (CSR by supernode) */
     for (int64_t s = 0; ok && s < ns; s++) cbp[s + 2] += cbp[s + 1];
     for (size_t i = 0; ok && i < ndag; i++)
@@ -180,6 +235,15 @@ static int fdag_build(gb_plan *P)
     }
     for (int64_t s = 0; ok && s < ns; s++) {
         int32_t ja = (int32_t)(JA0 + s);
+        if (MEMBER(s)) {
+            /* SUBTREE(root) -> JK(parent of the root) */
+            int32_t par = P->h_parent[s];
+            if (sub_root[s] == s && par >= 0) {
+                int32_t e[2] = {sub_id[s], (int32_t)(JK0 + par)};
+                ok &= gb_vec_push(&E, e);
+            }
+            continue;
+        }
         if (FUSED(s)) {
             /* JK(s) -> NODE(s) -> JK(parent) */
             if (small_id[s] < 0) { ok = 0; break; }
@@ -254,6 +318,8 @@ static int fdag_build(gb_plan *P)
         }
     }
 #undef FUSED
+#undef MEMBER
+    free(sub_root); free(work); free(elig); free(sub_off); free(sub_id);
     free(potrf0); free(small_id); free(cbp); free(cbl);
     free(deg); free(nd); free(pos); free(succ); free(tmp);
     gb_vec_free(&E);
@@ -320,7 +386,7 @@ static int segments_build(gb_plan *P)
     return ok;
 }
 
-gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
+gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_work)
 {
     if (small_cols < 1) small_cols = 1;
     if (small_cols > GB_SMALL_MAX) small_cols = GB_SMALL_MAX;
@@ -332,6 +398,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
     if (!P) return NULL;
     P->L = L;
     P->small_cols = small_cols;
+    P->sub_work = sub_work;
     P->super_ptr = L->super;
     P->s_ptr = L->s;
     P->pi_ptr = L->pi;
@@ -366,6 +433,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols)
     vec_init(&P->fd_nd, sizeof(int32_t));
     vec_init(&P->fd_q0, sizeof(int32_t));
     vec_init(&P->fd_q1, sizeof(int32_t));
+    vec_init(&P->fd_sub, sizeof(int32_t));
     vec_init(&P->fwd_seq, sizeof(gb_launch_rec));
     vec_init(&P->bwd_seq, sizeof(gb_launch_rec));
 
@@ -973,6 +1041,7 @@ int gb_plan_upload(gb_plan *P)
     UP(P->d_fd_sp, P->fd_sp.p, P->fd_sp.n * P->fd_sp.esz);
     UP(P->d_fd_succ, P->fd_succ.p, P->fd_succ.n * P->fd_succ.esz);
     UP(P->d_fd_nd, P->fd_nd.p, P->fd_nd.n * P->fd_nd.esz);
+    UP(P->d_fd_sub, P->fd_sub.p, P->fd_sub.n * P->fd_sub.esz);
     {
         size_t n0 = P->fd_q0.n, n1 = P->fd_q1.n, N = P->fd_t.n;
         int32_t *qi = malloc(sizeof(int32_t) * (n0 + n1 + 1));
@@ -1024,6 +1093,7 @@ void gb_plan_free(gb_plan *P)
     free(P->h_seg); free(P->h_chunk); free(P->h_anorm_seg);
     gb_vec_free(&P->fd_t); gb_vec_free(&P->fd_sp); gb_vec_free(&P->fd_succ);
     gb_vec_free(&P->fd_nd); gb_vec_free(&P->fd_q0); gb_vec_free(&P->fd_q1);
+    gb_vec_free(&P->fd_sub);
     void *dev[] = {P->d_Super, P->d_Pi, P->d_Px, P->d_cboff, P->d_cbvoff, P->d_Perm,
                    P->d_Ls, P->d_relmap, P->d_child_ptr, P->d_child_list, P->d_fail,
                    P->d_anyfail, P->d_asm, P->d_node, P->d_potrf, P->d_trsm, P->d_gemm,
@@ -1036,7 +1106,7 @@ void gb_plan_free(gb_plan *P)
                    P->d_dag_succ, P->d_dag_nd, P->d_dag_q0i, P->d_dag_q1i, P->d_dag_ctrl0,
                    P->d_dag_cnt, P->d_dag_q, P->d_dag_ctrl, P->d_dag_smf, P->d_fd_t,
                    P->d_fd_sp, P->d_fd_succ, P->d_fd_nd, P->d_fd_qi, P->d_fd_ctrl0,
-                   P->d_fd_cnt, P->d_fd_q, P->d_fd_pat, P->d_fd_inst, P->d_fd_ibase,
+                   P->d_fd_cnt, P->d_fd_q, P->d_fd_pat, P->d_fd_inst, P->d_fd_ibase, P->d_fd_sub,
                    P->d_chunk, P->d_anorm_seg, P->d_bred, P->d_gf, P->d_gb};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++)
         if (dev[i]) cudaFree(dev[i]);

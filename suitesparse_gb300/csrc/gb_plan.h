@@ -60,6 +60,7 @@ typedef struct {
     const gb_dtask *tasks;           /* local tasks */
     const int32_t *succ_ptr, *succ;  /* local successor CSR */
     const int64_t *Sp, *Si;          /* S = tril(PAP') column pointers/indices */
+    const int32_t *sub_list;         /* supernodes of the SUBTREE tasks */
     int32_t ntasks, pad;
 } gb_fpat;
 
@@ -116,6 +117,7 @@ typedef struct gb_plan {
     const void *super_ptr, *s_ptr, *pi_ptr;
     Int n, nsuper, ssize, xsize;
     Int small_cols;                   /* widest supernode factored whole by one block */
+    double sub_work;                  /* work limit of a SUBTREE task (0: none) */
     uint64_t hash;
 
     /* host arrays derived from the pattern (kept for the plan's lifetime) */
@@ -153,11 +155,11 @@ typedef struct gb_plan {
 
     /* whole-factorization task graph (local ids: level-graph tasks, then
      * assembly chunks, small supernodes, and two joins per supernode) */
-    gb_vec fd_t, fd_sp, fd_succ, fd_nd, fd_q0, fd_q1;
+    gb_vec fd_t, fd_sp, fd_succ, fd_nd, fd_q0, fd_q1, fd_sub;
     int32_t fd_total0, fd_total1;
     gb_dtask *d_fd_t;
     int32_t *d_fd_sp, *d_fd_succ, *d_fd_nd, *d_fd_qi, *d_fd_ctrl0;
-    int32_t *d_fd_cnt, *d_fd_q;
+    int32_t *d_fd_cnt, *d_fd_q, *d_fd_sub;
     gb_fpat h_fd_pat;                 /* host copy, refreshed per factorization */
     gb_fpat *d_fd_pat;
     gb_finst *d_fd_inst;
@@ -228,6 +230,7 @@ struct gb_ctx {
     cudaStream_t stream;
     int device;
     int64_t opt_keep, opt_small;
+    double opt_subwork;                /* SUBTREE task work limit for new plans */
     double stats[8];
     int64_t launches;            /* kernel launches issued since creation */
     cudaEvent_t ev0, ev1;
@@ -257,7 +260,7 @@ void gb_vec_free(gb_vec *v);
 /* Build the plan (host side) for a supernodal symbolic factor. */
 int gb_valmap_apply(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, cholmod_common *Common);
 void gb_valmap_free(gb_plan *P);
-gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols);
+gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_work);
 /* Upload the pattern, task arrays and launch sequences. */
 int gb_plan_upload(gb_plan *P);
 void gb_plan_free(gb_plan *P);
