@@ -346,6 +346,14 @@ int gb300_finish (cholmod_common *Common) ;
  *      nscol nsrow^2 + 1e4 per supernode) is at most this many flops is
  *      factorized whole by one thread block; 0 = never.  A change applies
  *      from the next factorization (the plan is rebuilt).
+ *  GB300_OPT_WARP_ROWS [32]: in the one-launch factorization, a supernode
+ *      factorized whole (a subtree member, or a small supernode on its own)
+ *      whose front has at most this many rows (0-32) is assembled and
+ *      factorized by one warp instead of a whole thread block; the subtree
+ *      members run wave by wave (a wave: supernodes of equal height in the
+ *      subtree), several one-warp fronts at once.  The factor is the same
+ *      bit for bit with every value.  0 = never.  A change applies from the
+ *      next factorization (the plan is rebuilt).
  *  GB300_OPT_PROFILE [0]: 1 = time every kernel launch of the factorization
  *      with CUDA events (summed per kernel kind, see gb300_get_profile); also
  *      clears the accumulated profile.
@@ -372,6 +380,7 @@ int gb300_finish (cholmod_common *Common) ;
 #define GB300_OPT_FACTOR         6
 #define GB300_OPT_TENSOR         7
 #define GB300_OPT_SUBTREE_WORK   8
+#define GB300_OPT_WARP_ROWS      9
 int gb300_set_option (cholmod_common *Common, int option, int64_t value) ;
 
 /* Supernodal symbolic analysis of A (stype < 0, lower) with a given final

@@ -179,4 +179,195 @@ __device__ void factor_small_body(const gb_dev_pattern &P, int s, T *Lx, T *Linv
 #undef NB
 #undef LDT
 
+// ---------------------------------------------------------------------------
+// a front of at most 32 rows, whole, on one warp (lane = front row): its
+// assembly, LL' of the diagonal block, the block's inverse (kept for the
+// sweeps), the panel rows below as products with that inverse, and the
+// update block.  The front stays in the warp's shared region; nothing waits
+// on another warp.  Every value is formed by the same operations in the same
+// order as the block path (assemble_body, factor_small_body and the update-
+// block tile), so the factor is the same bit for bit on either path:
+//  * the diagonal block is factorized right-looking, which subtracts the
+//    products L(i,k) L(j,k) from A(i,j) in the order k = 0, 1, ... exactly as
+//    the block path's left-looking loop does;
+//  * the inverse is the block path's column-by-column substitution;
+//  * L21(r,c) = sum_k A21(r,k) Linv(c,k) summed from zero in k order;
+//  * the update block is C - (sum_k L21(i,k) L21(j,k)), summed from zero.
+// The reference forms the same quantities with dpotrf / dtrsm / dsyrk
+// (t_cholmod_super_numeric_worker.c :1004-1058, :1152-1218, :640-720).
+// ---------------------------------------------------------------------------
+
+#define GB_WF_LD 33
+
+// bytes of one warp's shared region
+template <typename T>
+__host__ __device__ constexpr size_t warp_front_smem()
+{
+    return sizeof(T) * (32 * GB_WF_LD + 32) + sizeof(int) * 66;
+}
+
+template <typename TA, typename T>
+__device__ __noinline__ void warp_front(const gb_dev_pattern &P, int s, const int64_t *__restrict__ Sp,
+                           const int64_t *__restrict__ Si, const TA *__restrict__ Sx,
+                           const double *__restrict__ scale, double beta, T *Lx, T *CB, T *Linv,
+                           unsigned char *wsm)
+{
+    constexpr int LD = GB_WF_LD;
+    constexpr unsigned FULL = 0xffffffffu;
+    T *F = (T *)wsm;                       // front, column-major: F[j*LD + i]
+    T *xd = F + 32 * LD;                   // diagonal of the block inverse
+    int *rows = (int *)(xd + 32);          // front row -> row of L
+    int *spc = rows + 32;                  // A's column starts, relative to Sp[k1]
+    const int lane = threadIdx.x & 31;
+    const int64_t k1 = P.Super[s];
+    const int nscol = (int)(P.Super[s + 1] - k1);
+    const int64_t psi = P.Pi[s];
+    const int nsrow = (int)(P.Pi[s + 1] - psi);
+    const int m = nsrow - nscol;
+    T *panel = Lx + P.Px[s];
+
+    // 1. zero the front; row indices; A's column starts
+    for (int j = 0; j < nsrow; j++) F[j * LD + lane] = (T)0;
+    rows[lane] = lane < nsrow ? P.Ls[psi + lane] : 0x7fffffff;
+    const int64_t p0 = Sp[k1];
+    for (int t = lane; t <= nscol; t += 32) spc[t] = (int)(Sp[k1 + t] - p0);
+    __syncwarp();
+
+    // 2. entries of A in the panel columns (rows at or below the diagonal)
+    const int ne = spc[nscol];
+    for (int q = lane; q < ne; q += 32) {
+        int lo = 0, hi = nscol - 1;            // column: last t with spc[t] <= q
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (spc[mid] <= q) lo = mid; else hi = mid - 1;
+        }
+        const int t = lo;
+        const int64_t k = k1 + t;
+        const int64_t i = Si[p0 + q];
+        if (i < k) continue;
+        int a = t, b = nsrow;                  // front row of i
+        while (a < b) {
+            const int mid = (a + b) >> 1;
+            if ((int64_t)rows[mid] < i) a = mid + 1; else b = mid;
+        }
+        if (a < nsrow && (int64_t)rows[a] == i) {
+            double v = (double)Sx[p0 + q];
+            if (i == k) v += beta;
+            if (scale) v = v * (scale[i] * scale[k]);
+            F[t * LD + a] = (T)v;
+        }
+    }
+    __syncwarp();
+    if (beta != 0.0) {                         // beta on diagonals A does not store
+        for (int t = lane; t < nscol; t += 32) {
+            const int64_t k = k1 + t;
+            bool has = false;
+            for (int q = spc[t]; q < spc[t + 1]; q++)
+                if (Si[p0 + q] == k) { has = true; break; }
+            if (!has) {
+                double v = beta;
+                if (scale) v *= scale[k] * scale[k];
+                F[t * LD + t] += (T)v;
+            }
+        }
+        __syncwarp();
+    }
+
+    // 3. extend-add of each child's update block, children in a fixed order
+    // (loads of 8 columns issued before their adds)
+    for (int ci = P.child_ptr[s]; ci < P.child_ptr[s + 1]; ci++) {
+        const int c = P.child_list[ci];
+        const int ncc = (int)(P.Super[c + 1] - P.Super[c]);
+        const int64_t pic = P.Pi[c];
+        const int mc = (int)(P.Pi[c + 1] - pic) - ncc;
+        const int32_t *rm = P.relmap + pic + ncc;
+        const T *cbc = CB + P.cboff[c];
+        const int ri = lane < mc ? rm[lane] : 0;
+        for (int j0 = 0; j0 < mc; j0 += 8) {
+            T v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int j = j0 + u;
+                v[u] = (j < mc && lane >= j && lane < mc) ? cbc[lane + (int64_t)j * mc] : (T)0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int j = j0 + u;
+                const int rj = __shfl_sync(FULL, ri, j & 31);
+                if (j < mc && lane >= j && lane < mc) F[rj * LD + ri] += v[u];
+            }
+        }
+        __syncwarp();
+    }
+
+    // 4. LL' of the diagonal block (rows and columns below nscol)
+    int fail = -1;
+    for (int k = 0; k < nscol; k++) {
+        const T d = F[k * LD + k];
+        if (!(d > (T)0)) { fail = k; break; }
+        const T lkk = gb_sqrt<T>(d);
+        __syncwarp();
+        if (lane == k) F[k * LD + k] = lkk;
+        else if (lane > k && lane < nscol) F[k * LD + lane] = F[k * LD + lane] / lkk;
+        __syncwarp();
+        if (lane > k && lane < nscol) {
+            const T lik = F[k * LD + lane];
+            for (int j = k + 1; j <= lane; j++) F[j * LD + lane] -= lik * F[k * LD + j];
+        }
+        __syncwarp();
+    }
+
+    // 5. X = inverse of the diagonal block, lane j forms column j: X(j,j)
+    // in xd[j], X(i,j) for i > j in the block's upper triangle at F[i*LD + j]
+    if (lane < nscol) {
+        const int j = lane;
+        const T xjj = (T)1 / F[j * LD + j];
+        xd[j] = xjj;
+        for (int i = j + 1; i < nscol; i++) {
+            T acc = (T)0;
+            for (int k = j; k < i; k++) acc += F[k * LD + i] * (k == j ? xjj : F[k * LD + j]);
+            F[i * LD + j] = -acc / F[i * LD + i];
+        }
+    }
+    __syncwarp();
+    {
+        T *out = Linv + P.linvoff[P.blkoff[s]];   // column-major, ld nscol
+        for (int j = 0; j < nscol; j++)
+            if (lane < nscol)
+                out[lane + (int64_t)j * nscol] =
+                    lane < j ? (T)0 : (lane == j ? xd[j] : F[lane * LD + j]);
+    }
+
+    // 6. panel rows below: L21(r,c) = sum_{k<=c} A21(r,k) X(c,k), in place
+    // from the last column (A21(r,k), k <= c, is still unchanged)
+    const int ncols = fail >= 0 ? fail : nscol;
+    if (lane >= nscol && lane < nsrow) {
+        for (int c = ncols - 1; c >= 0; c--) {
+            T acc = (T)0;
+            for (int k = 0; k <= c; k++) acc += F[k * LD + lane] * (k == c ? xd[c] : F[c * LD + k]);
+            F[c * LD + lane] = acc;
+        }
+    }
+    __syncwarp();
+
+    // 7. the panel (zero above the diagonal) and the update block
+    for (int t = 0; t < nscol; t++)
+        if (lane < nsrow) panel[lane + (int64_t)t * nsrow] = lane < t ? (T)0 : F[t * LD + lane];
+    T *cb = CB + P.cboff[s];
+    for (int j = nscol; j < nsrow; j++) {
+        if (lane >= j && lane < nsrow) {
+            T acc = (T)0;
+            if (fail < 0)
+                for (int k = 0; k < nscol; k++) acc += F[k * LD + lane] * F[k * LD + j];
+            cb[(lane - nscol) + (int64_t)(j - nscol) * m] = F[j * LD + lane] - acc;
+        }
+    }
+    if (fail >= 0 && lane == 0) {
+        P.fail[s] = fail;
+        atomicExch(P.anyfail, 1);
+    }
+}
+
+#undef GB_WF_LD
+
 #endif

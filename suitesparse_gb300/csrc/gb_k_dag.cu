@@ -329,6 +329,9 @@ __device__ __forceinline__ int fdag_instance(const gb_fdag_dev &D, int id)
     return lo;
 }
 
+static_assert(8 * warp_front_smem<float>() <= dag_smem<float>(), "one-warp fronts: shared memory");
+static_assert(8 * warp_front_smem<double>() <= dag_smem<double>(), "one-warp fronts: shared memory");
+
 template <typename T, bool TC>
 __global__ void __launch_bounds__(256, 2)
 k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
@@ -397,34 +400,65 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
             factor_small_body<T>(P, tk.s, Lx, Linv, smem_raw, &sfail);
         } else if (tk.type == GB_DT_NODE || tk.type == GB_DT_SUBTREE) {
             // a small supernode whole (NODE), or every supernode of a subtree
-            // in order, children first (SUBTREE): assembly chunk by chunk,
-            // LL', then every update-block tile.  A parent reads its
-            // children's update blocks written by this block before a barrier.
-            const int cnt = tk.type == GB_DT_NODE ? 1 : tk.r;
+            // wave by wave, children in earlier waves (SUBTREE).  A front of
+            // at most warp_rows rows runs on one warp (a wave's such fronts
+            // side by side, a warp each); any other runs on the whole block:
+            // assembly chunk by chunk, LL', then every update-block tile.  A
+            // parent reads its children's update blocks, written by this
+            // block, after a barrier.
             const double *scale = D.scale ? D.scale + I.scale : nullptr;
-            for (int q = 0; q < cnt; q++) {
-                const int s = tk.type == GB_DT_NODE ? tk.s : PP.sub_list[tk.b + q];
-                const int nscol = (int)(P.Super[s + 1] - P.Super[s]);
-                const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
-                const int m = nsrow - nscol;
-                for (int t0 = 0; t0 < nsrow; t0 += 64) {
-                    const gb_asm_task a = {s, t0, min(t0 + 64, nsrow), 0};
-                    if (D.a_dtype == 0)
-                        assemble_body<double, T>(P, a, PP.Sp, PP.Si, (const double *)D.Sx + I.sx,
-                                                 scale, D.beta, Lx, CB);
-                    else
-                        assemble_body<float, T>(P, a, PP.Sp, PP.Si, (const float *)D.Sx + I.sx,
-                                                scale, D.beta, Lx, CB);
-                    __syncthreads();
+            const int warp = threadIdx.x >> 5;
+            const bool node = tk.type == GB_DT_NODE;
+            int q = 0, w1 = 0, w2 = 1;
+            if (node) {
+                w1 = (int)(P.Pi[tk.s + 1] - P.Pi[tk.s]) <= PP.warp_rows ? 1 : 0;
+            }
+            while (q < (node ? 1 : tk.r)) {
+                if (!node) {
+                    // wave [q, w2): one-warp fronts [q, w1), then the others
+                    w1 = PP.sub_meta[2 * (tk.b + q)];
+                    w2 = PP.sub_meta[2 * (tk.b + q) + 1];
+                    if (w2 <= q || w2 > tk.r || w1 < q || w1 > w2) {
+                        if (threadIdx.x == 0) atomicExch(D.Q.err, 1);
+                        break;
+                    }
                 }
-                factor_small_body<T>(P, s, Lx, Linv, smem_raw, &sfail);
-                __syncthreads();
-                for (int J = 0; J < m; J += 64)
-                    for (int I0 = J; I0 < m; I0 += 64) {
-                        const gb_dtask ct = {GB_DT_CB, s, 0, I0 / 64, J / 64, 1, 0, 0};
-                        dag_tile_task<T>(P, ct, Lx, CB, Linv, smem_raw, sfail);
+                for (int i = q + warp; i < w1; i += 8) {
+                    const int s = node ? tk.s : PP.sub_list[tk.b + i];
+                    unsigned char *wsm = smem_raw + (size_t)warp * warp_front_smem<T>();
+                    if (D.a_dtype == 0)
+                        warp_front<double, T>(P, s, PP.Sp, PP.Si, (const double *)D.Sx + I.sx, scale,
+                                              D.beta, Lx, CB, Linv, wsm);
+                    else
+                        warp_front<float, T>(P, s, PP.Sp, PP.Si, (const float *)D.Sx + I.sx, scale,
+                                             D.beta, Lx, CB, Linv, wsm);
+                }
+                if (w1 > q) __syncthreads();
+                for (int i = w1; i < w2; i++) {
+                    const int s = node ? tk.s : PP.sub_list[tk.b + i];
+                    const int nscol = (int)(P.Super[s + 1] - P.Super[s]);
+                    const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
+                    const int m = nsrow - nscol;
+                    for (int t0 = 0; t0 < nsrow; t0 += 64) {
+                        const gb_asm_task a = {s, t0, min(t0 + 64, nsrow), 0};
+                        if (D.a_dtype == 0)
+                            assemble_body<double, T>(P, a, PP.Sp, PP.Si, (const double *)D.Sx + I.sx,
+                                                     scale, D.beta, Lx, CB);
+                        else
+                            assemble_body<float, T>(P, a, PP.Sp, PP.Si, (const float *)D.Sx + I.sx,
+                                                    scale, D.beta, Lx, CB);
                         __syncthreads();
                     }
+                    factor_small_body<T>(P, s, Lx, Linv, smem_raw, &sfail);
+                    __syncthreads();
+                    for (int J = 0; J < m; J += 64)
+                        for (int I0 = J; I0 < m; I0 += 64) {
+                            const gb_dtask ct = {GB_DT_CB, s, 0, I0 / 64, J / 64, 1, 0, 0};
+                            dag_tile_task<T>(P, ct, Lx, CB, Linv, smem_raw, sfail);
+                            __syncthreads();
+                        }
+                }
+                q = w2;
             }
         } else {
             dag_tile_task<T>(P, tk, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr);

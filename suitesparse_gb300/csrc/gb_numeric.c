@@ -25,6 +25,7 @@ gb_ctx *gb_ctx_new(void)
     c->opt_keep = 0;
     c->opt_small = GB_SMALL_MAX;
     c->opt_subwork = GB_SUBTREE_WORK;
+    c->opt_warprows = GB_WARP_ROWS;
     c->device = -1;
     c->sweep_mode = 1;
     c->factor_mode = 1;
@@ -63,6 +64,7 @@ int64_t gb_option(cholmod_common *Common, int option)
     if (option == GB300_OPT_KEEP_ON_DEVICE) return c ? c->opt_keep : 0;
     if (option == GB300_OPT_SMALL_COLS) return c ? c->opt_small : GB_SMALL_MAX;
     if (option == GB300_OPT_SUBTREE_WORK) return c ? (int64_t)c->opt_subwork : (int64_t)GB_SUBTREE_WORK;
+    if (option == GB300_OPT_WARP_ROWS) return c ? c->opt_warprows : GB_WARP_ROWS;
     return 0;
 }
 
@@ -82,6 +84,7 @@ int gb300_set_option(cholmod_common *Common, int option, int64_t value)
     }
     else if (option == GB300_OPT_SMALL_COLS) c->opt_small = GB_MAX(1, GB_MIN(GB_SMALL_MAX, value));
     else if (option == GB300_OPT_SUBTREE_WORK) c->opt_subwork = value < 0 ? 0.0 : (double)value;
+    else if (option == GB300_OPT_WARP_ROWS) c->opt_warprows = GB_MAX(0, GB_MIN(GB_WARP_ROWS, value));
     else { GB_ERROR(CHOLMOD_INVALID, "unknown option"); return FALSE; }
     return TRUE;
 }
@@ -210,7 +213,8 @@ gb_plan *gb_plan_get(cholmod_factor *L, cholmod_common *Common, gb_ctx *ctx, int
     for (gb_plan *q = plan_head; q; q = q->next)
         if (q->L == L) { P = q; break; }
     if (P && (!plan_matches(P, L) || P->hash != gb_pattern_hash(L)
-              || (create && (P->small_cols != ctx->opt_small || P->sub_work != ctx->opt_subwork)))) {
+              || (create && (P->small_cols != ctx->opt_small || P->sub_work != ctx->opt_subwork
+                             || P->warp_rows != ctx->opt_warprows)))) {
         plan_unlink(P);
         pthread_mutex_unlock(&plan_lock);
         cudaStreamSynchronize(ctx->stream);
@@ -220,7 +224,7 @@ gb_plan *gb_plan_get(cholmod_factor *L, cholmod_common *Common, gb_ctx *ctx, int
     }
     pthread_mutex_unlock(&plan_lock);
     if (P || !create) return P;
-    P = gb_plan_build(L, ctx->opt_small, ctx->opt_subwork);
+    P = gb_plan_build(L, ctx->opt_small, ctx->opt_subwork, ctx->opt_warprows);
     if (!P) { GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "plan construction failed"); return NULL; }
     if (!gb_plan_upload(P)) {
         gb_plan_free(P);
@@ -310,6 +314,8 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
         hp->Sp = P->d_Sp;
         hp->Si = P->d_Si;
         hp->sub_list = P->d_fd_sub;
+        hp->sub_meta = P->d_fd_smeta;
+        hp->warp_rows = (int32_t)P->warp_rows;
         hp->ntasks = (int32_t)N;
         if (prof) CU(cudaEventRecord(ctx->pev[0], st));
         CU(cudaMemcpyAsync(P->d_fd_pat, hp, sizeof *hp, cudaMemcpyHostToDevice, st));

@@ -143,15 +143,67 @@ static int fdag_build(gb_plan *P)
         if (sub_root[s] >= 0) sub_off[sub_root[s] + 1]++;
     for (int64_t s = 0; ok && s < ns; s++) sub_off[s + 1] += sub_off[s];
     if (ok) {
-        /* members in ascending order: children before parents */
+        /* members wave by wave: wave h holds the members of height h in the
+         * subtree (leaves 0), so every member's children are in earlier
+         * waves; within a wave the fronts of at most warp_rows rows come
+         * first (one warp each), then the others (the whole block each),
+         * each group in ascending order.  key = 2 height + (not one-warp). */
         int32_t *fill = malloc(sizeof(int32_t) * (ns + 1)), *lst = malloc(sizeof(int32_t) * (ns + 1));
-        if (!fill || !lst) ok = 0;
-        for (int64_t s = 0; ok && s < ns; s++) fill[s] = sub_off[s];
+        int32_t *key = malloc(sizeof(int32_t) * (ns + 1)), *meta = calloc(2 * (size_t)ns + 2, sizeof(int32_t));
+        if (!fill || !lst || !key || !meta) ok = 0;
+        for (int64_t s = 0; ok && s < ns; s++) key[s] = 0;
+        for (int64_t s = 0; ok && s < ns; s++) {       /* children before parents */
+            if (sub_root[s] < 0) continue;
+            int32_t par = P->h_parent[s];
+            if (par >= 0 && sub_root[par] == sub_root[s] && key[par] < key[s] + 2)
+                key[par] = key[s] + 2;
+        }
         for (int64_t s = 0; ok && s < ns; s++)
-            if (sub_root[s] >= 0) lst[fill[sub_root[s]]++] = (int32_t)s;
-        for (int64_t q = 0; ok && q < sub_off[ns]; q++) ok &= gb_vec_push(&P->fd_sub, &lst[q]);
+            if (sub_root[s] >= 0 && Pi[s + 1] - Pi[s] > P->warp_rows) key[s] |= 1;
+        /* counting sort of each subtree's members by key (stable) */
+        int32_t maxkey = 0;
+        for (int64_t s = 0; ok && s < ns; s++)
+            if (sub_root[s] >= 0 && key[s] > maxkey) maxkey = key[s];
+        int32_t *kcnt = ok ? calloc((size_t)maxkey + 2, sizeof(int32_t)) : NULL;
+        if (!kcnt) ok = 0;
+        for (int64_t s = 0; ok && s < ns; s++) fill[s] = 0;
+        for (int64_t s = 0; ok && s < ns; s++)          /* members in ascending order */
+            if (sub_root[s] >= 0) lst[sub_off[sub_root[s]] + fill[sub_root[s]]++] = (int32_t)s;
+        for (int64_t r = 0; ok && r < ns; r++) {
+            if (sub_root[r] != r) continue;
+            const int32_t b = sub_off[r], e = sub_off[r + 1];
+            int32_t kmax = 0;
+            for (int32_t q = b; q < e; q++) if (key[lst[q]] > kmax) kmax = key[lst[q]];
+            for (int32_t k = 0; k <= kmax + 1; k++) kcnt[k] = 0;
+            for (int32_t q = b; q < e; q++) kcnt[key[lst[q]] + 1]++;
+            for (int32_t k = 0; k <= kmax; k++) kcnt[k + 1] += kcnt[k];
+            /* wave starts: per wave (key pair 2h, 2h+1) the end of the
+             * one-warp group and the end of the wave, relative to b */
+            for (int32_t h = 0; 2 * h <= kmax; h++) {
+                const int32_t w0 = kcnt[2 * h], w1 = kcnt[2 * h + 1];
+                const int32_t w2 = 2 * h + 2 <= kmax + 1 ? kcnt[2 * h + 2] : e - b;
+                if (w2 > w0) {
+                    meta[2 * (size_t)(b + w0)] = w1;
+                    meta[2 * (size_t)(b + w0) + 1] = w2;
+                }
+            }
+            for (int32_t q = b; q < e; q++) {
+                const int32_t s = lst[q];
+                fill[s] = b + kcnt[key[s]]++;
+            }
+        }
+        for (int64_t s = 0; ok && s < ns; s++)
+            if (sub_root[s] >= 0) key[fill[s]] = (int32_t)s;
+        for (int64_t q = 0; ok && q < sub_off[ns]; q++) {
+            ok &= gb_vec_push(&P->fd_sub, &key[q]);
+            ok &= gb_vec_push(&P->fd_smeta, &meta[2 * q]);
+            ok &= gb_vec_push(&P->fd_smeta, &meta[2 * q + 1]);
+        }
+        free(kcnt);
         free(fill);
         free(lst);
+        free(key);
+        free(meta);
     }
 #define MEMBER(s) (sub_root[s] >= 0)
     const size_t N = SB0 + nsub;
@@ -386,7 +438,8 @@ static int segments_build(gb_plan *P)
     return ok;
 }
 
-gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_work)
+gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_work,
+                       int64_t warp_rows)
 {
     if (small_cols < 1) small_cols = 1;
     if (small_cols > GB_SMALL_MAX) small_cols = GB_SMALL_MAX;
@@ -399,6 +452,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
     P->L = L;
     P->small_cols = small_cols;
     P->sub_work = sub_work;
+    P->warp_rows = warp_rows < 0 ? 0 : (warp_rows > GB_WARP_ROWS ? GB_WARP_ROWS : warp_rows);
     P->super_ptr = L->super;
     P->s_ptr = L->s;
     P->pi_ptr = L->pi;
@@ -434,6 +488,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
     vec_init(&P->fd_q0, sizeof(int32_t));
     vec_init(&P->fd_q1, sizeof(int32_t));
     vec_init(&P->fd_sub, sizeof(int32_t));
+    vec_init(&P->fd_smeta, sizeof(int32_t));
     vec_init(&P->fwd_seq, sizeof(gb_launch_rec));
     vec_init(&P->bwd_seq, sizeof(gb_launch_rec));
 
@@ -1042,6 +1097,7 @@ int gb_plan_upload(gb_plan *P)
     UP(P->d_fd_succ, P->fd_succ.p, P->fd_succ.n * P->fd_succ.esz);
     UP(P->d_fd_nd, P->fd_nd.p, P->fd_nd.n * P->fd_nd.esz);
     UP(P->d_fd_sub, P->fd_sub.p, P->fd_sub.n * P->fd_sub.esz);
+    UP(P->d_fd_smeta, P->fd_smeta.p, P->fd_smeta.n * P->fd_smeta.esz);
     {
         size_t n0 = P->fd_q0.n, n1 = P->fd_q1.n, N = P->fd_t.n;
         int32_t *qi = malloc(sizeof(int32_t) * (n0 + n1 + 1));
@@ -1094,6 +1150,7 @@ void gb_plan_free(gb_plan *P)
     gb_vec_free(&P->fd_t); gb_vec_free(&P->fd_sp); gb_vec_free(&P->fd_succ);
     gb_vec_free(&P->fd_nd); gb_vec_free(&P->fd_q0); gb_vec_free(&P->fd_q1);
     gb_vec_free(&P->fd_sub);
+    gb_vec_free(&P->fd_smeta);
     void *dev[] = {P->d_Super, P->d_Pi, P->d_Px, P->d_cboff, P->d_cbvoff, P->d_Perm,
                    P->d_Ls, P->d_relmap, P->d_child_ptr, P->d_child_list, P->d_fail,
                    P->d_anyfail, P->d_asm, P->d_node, P->d_potrf, P->d_trsm, P->d_gemm,
@@ -1107,6 +1164,7 @@ void gb_plan_free(gb_plan *P)
                    P->d_dag_cnt, P->d_dag_q, P->d_dag_ctrl, P->d_dag_smf, P->d_fd_t,
                    P->d_fd_sp, P->d_fd_succ, P->d_fd_nd, P->d_fd_qi, P->d_fd_ctrl0,
                    P->d_fd_cnt, P->d_fd_q, P->d_fd_pat, P->d_fd_inst, P->d_fd_ibase, P->d_fd_sub,
+                   P->d_fd_smeta,
                    P->d_chunk, P->d_anorm_seg, P->d_bred, P->d_gf, P->d_gb};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++)
         if (dev[i]) cudaFree(dev[i]);

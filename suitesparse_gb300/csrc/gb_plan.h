@@ -60,8 +60,11 @@ typedef struct {
     const gb_dtask *tasks;           /* local tasks */
     const int32_t *succ_ptr, *succ;  /* local successor CSR */
     const int64_t *Sp, *Si;          /* S = tril(PAP') column pointers/indices */
-    const int32_t *sub_list;         /* supernodes of the SUBTREE tasks */
-    int32_t ntasks, pad;
+    const int32_t *sub_list;         /* supernodes of the SUBTREE tasks, wave by wave */
+    const int32_t *sub_meta;         /* [2 per sub_list entry] at a wave's first entry:
+                                      * end of its one-warp fronts, end of the wave
+                                      * (both relative to the task's first entry) */
+    int32_t ntasks, warp_rows;       /* fronts with at most warp_rows rows: one warp */
 } gb_fpat;
 
 typedef struct {
@@ -118,6 +121,7 @@ typedef struct gb_plan {
     Int n, nsuper, ssize, xsize;
     Int small_cols;                   /* widest supernode factored whole by one block */
     double sub_work;                  /* work limit of a SUBTREE task (0: none) */
+    Int warp_rows;                    /* fronts this tall or less run on one warp (0: none) */
     uint64_t hash;
 
     /* host arrays derived from the pattern (kept for the plan's lifetime) */
@@ -155,11 +159,11 @@ typedef struct gb_plan {
 
     /* whole-factorization task graph (local ids: level-graph tasks, then
      * assembly chunks, small supernodes, and two joins per supernode) */
-    gb_vec fd_t, fd_sp, fd_succ, fd_nd, fd_q0, fd_q1, fd_sub;
+    gb_vec fd_t, fd_sp, fd_succ, fd_nd, fd_q0, fd_q1, fd_sub, fd_smeta;
     int32_t fd_total0, fd_total1;
     gb_dtask *d_fd_t;
     int32_t *d_fd_sp, *d_fd_succ, *d_fd_nd, *d_fd_qi, *d_fd_ctrl0;
-    int32_t *d_fd_cnt, *d_fd_q, *d_fd_sub;
+    int32_t *d_fd_cnt, *d_fd_q, *d_fd_sub, *d_fd_smeta;
     gb_fpat h_fd_pat;                 /* host copy, refreshed per factorization */
     gb_fpat *d_fd_pat;
     gb_finst *d_fd_inst;
@@ -231,6 +235,7 @@ struct gb_ctx {
     int device;
     int64_t opt_keep, opt_small;
     double opt_subwork;                /* SUBTREE task work limit for new plans */
+    int64_t opt_warprows;              /* one-warp front height limit for new plans */
     double stats[8];
     int64_t launches;            /* kernel launches issued since creation */
     cudaEvent_t ev0, ev1;
@@ -260,7 +265,8 @@ void gb_vec_free(gb_vec *v);
 /* Build the plan (host side) for a supernodal symbolic factor. */
 int gb_valmap_apply(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, cholmod_common *Common);
 void gb_valmap_free(gb_plan *P);
-gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_work);
+gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_work,
+                       int64_t warp_rows);
 /* Upload the pattern, task arrays and launch sequences. */
 int gb_plan_upload(gb_plan *P);
 void gb_plan_free(gb_plan *P);

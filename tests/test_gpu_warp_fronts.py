@@ -1,0 +1,86 @@
+"""One-warp fronts (GB300_OPT_WARP_ROWS): a front of at most that many rows
+assembled and factorized by one warp gives the same factor, bit for bit, as
+the same front on a whole thread block, whatever the subtree grouping
+(GB300_OPT_SUBTREE_WORK) -- in FP64, in FP32, through the mixed form's
+refined solution, and for a matrix that is not positive definite."""
+import numpy as np
+import pytest
+
+from conftest import make_case
+from suitesparse_gb300 import cholmod as CH
+from suitesparse_gb300 import matrices as M
+
+pytestmark = pytest.mark.gpu
+
+SETTINGS = [(0, 0), (32, 0), (0, 4_000_000), (16, 4_000_000), (32, 4_000_000), (32, 10**9)]
+
+
+def _factor(meta, arrays, name, warp_rows, sub_work, dtype="d"):
+    c = CH.Common()
+    c.set_option(CH.GB300_OPT_WARP_ROWS, warp_rows)
+    c.set_option(CH.GB300_OPT_SUBTREE_WORK, sub_work)
+    n, Ap, Ai, Ax = make_case(meta, name)
+    A = CH.sparse(n, Ap, Ai, Ax if dtype == "d" else Ax.astype(np.float32), c, dtype=dtype)
+    L = CH.analyze_perm(A, arrays[name + "_Perm"].astype(np.int64), c)
+    assert CH.factorize(A, L, c) == 1
+    f = CH.factor_arrays(L)
+    out = (c.status, f["minor"], np.array(f["Lx"], copy=True))
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+    return out
+
+
+def _tiny_share(meta, arrays, name):
+    c = CH.Common()
+    n, Ap, Ai, Ax = make_case(meta, name)
+    A = CH.sparse(n, Ap, Ai, Ax, c)
+    L = CH.analyze_perm(A, arrays[name + "_Perm"].astype(np.int64), c)
+    f = CH.factor_arrays(L)
+    share = float(np.mean(np.diff(f["Pi"]) <= 32))
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
+    return share
+
+
+@pytest.mark.parametrize("dtype", ["d", "s"])
+@pytest.mark.parametrize("name", ["g2v", "g3", "e27", "c1"])
+def test_same_factor_bit_for_bit(golden, lib, name, dtype):
+    meta, arrays = golden
+    assert _tiny_share(meta, arrays, name) > 0.05     # the case exercises the warp path
+    ref = _factor(meta, arrays, name, 0, 0, dtype)
+    assert ref[0] == CH.CHOLMOD_OK
+    for wr, sw in SETTINGS[1:]:
+        st, minor, Lx = _factor(meta, arrays, name, wr, sw, dtype)
+        assert st == ref[0] and minor == ref[1]
+        assert np.array_equal(Lx, ref[2]), (wr, sw)
+
+
+def test_not_positive_definite_same_state(golden, lib):
+    meta, arrays = golden
+    ref = _factor(meta, arrays, "npd", 0, 0)
+    assert ref[0] == CH.CHOLMOD_NOT_POSDEF and ref[1] == meta["npd"]["minor"]
+    for wr, sw in SETTINGS[1:]:
+        st, minor, Lx = _factor(meta, arrays, "npd", wr, sw)
+        assert st == ref[0] and minor == ref[1]
+        assert np.array_equal(Lx, ref[2]), (wr, sw)
+
+
+def test_mixed_refined_solution_same(golden, lib, oracle_mod):
+    meta, arrays = golden
+    n, Ap, Ai, Ax = make_case(meta, "c1")
+    B = M.rhs(n, 3, 4)
+    sols = []
+    for wr, sw in ((0, 0), (32, 4_000_000)):
+        c = CH.Common()
+        c.set_option(CH.GB300_OPT_WARP_ROWS, wr)
+        c.set_option(CH.GB300_OPT_SUBTREE_WORK, sw)
+        A = CH.sparse(n, Ap, Ai, Ax, c)
+        L = CH.analyze_perm(A, arrays["c1_Perm"].astype(np.int64), c)
+        assert CH.factorize_mixed(A, L, c) == 1
+        X, info = CH.solve_refined(A, L, B, c, tol=1e-12)
+        assert oracle_mod.backward_error(n, Ap, Ai, Ax, X, B).max() <= 1e-12
+        sols.append((np.array(X, copy=True), info["iterations"]))
+        CH.free_factor(L, c)
+        CH.free_sparse(A, c)
+    assert sols[0][1] == sols[1][1]
+    assert np.array_equal(sols[0][0], sols[1][0])
