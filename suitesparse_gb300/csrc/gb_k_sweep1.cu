@@ -431,6 +431,167 @@ k_bwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
     }
 }
 
+// ---- leaf subtrees: one warp each ------------------------------------------
+// A leaf subtree (supernodes s0..root, contiguous in postorder, every front
+// at most 32 rows) is swept by one warp, lane = row of the front, with no
+// waits: the forward sweep runs these before its other tasks (they depend on
+// nothing), the backward sweep after them (they depend only on their
+// ancestors' x, final by then).  Per supernode, forward:
+//   y1 = b1 - (children's update-vector rows in the diagonal block),
+//   x1 = Linv y1,  u = (children's rows below the diagonal block) + L21 x1;
+// backward: y1 = x1 - L21' x(rows below), x1 = Linv' y1.  Children's update
+// vectors are gathered in a fixed order (owner-computes).  A warp takes its
+// next subtree from a ticket.
+
+#define LF_LD 17                 // staging rows of 16 right-hand sides (+1)
+#define LF_WARPS 4               // warps per block
+
+__device__ __forceinline__ int leaf_next(int32_t *ticket)
+{
+    int L = 0;
+    if ((threadIdx.x & 31) == 0) L = atomicAdd(ticket, 1);
+    return __shfl_sync(0xffffffffu, L, 0);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * LF_WARPS)
+k_fwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
+           const int32_t *__restrict__ blkoff, const int64_t *__restrict__ linvoff,
+           const int32_t *__restrict__ ntask_f, int32_t *done, int32_t *ticket, const T *Lx,
+           const T *Linv, int nrhs, T *Y, int64_t ldy, T *U)
+{
+    __shared__ T stage[LF_WARPS][2][32 * LF_LD];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T *ys = stage[warp][0], *xs = stage[warp][1];
+    for (int L = leaf_next(ticket); L < nleaf; L = leaf_next(ticket)) {
+        const int s0 = leaf[2 * L], root = leaf[2 * L + 1];
+        for (int s = s0; s <= root; s++) {
+            const int64_t k1 = P.Super[s];
+            const int nscol = (int)(P.Super[s + 1] - k1);
+            const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
+            const int m = nsrow - nscol;
+            const T *panel = Lx + P.Px[s];
+            const T *li = Linv + linvoff[blkoff[s]];
+            T *us = U + P.cbvoff[s] * nrhs;
+            for (int k0 = 0; k0 < nrhs; k0 += 16) {
+                const int nk = min(16, nrhs - k0);
+                for (int k = 0; k < nk; k++)
+                    ys[lane * LF_LD + k] = lane < nscol ? Y[k1 + lane + (int64_t)(k0 + k) * ldy] : (T)0;
+                __syncwarp();
+                for (int ci = P.child_ptr[s]; ci < P.child_ptr[s + 1]; ci++) {
+                    const int c = P.child_list[ci];
+                    const int ncc = (int)(P.Super[c + 1] - P.Super[c]);
+                    const int64_t pic = P.Pi[c];
+                    const int mc = (int)(P.Pi[c + 1] - pic) - ncc;
+                    if (lane < mc) {
+                        const int t = P.relmap[pic + ncc + lane];
+                        const T *uc = U + P.cbvoff[c] * nrhs;
+                        const T sg = t < nscol ? (T)-1 : (T)1;
+                        for (int k = 0; k < nk; k++)
+                            ys[t * LF_LD + k] += sg * uc[lane + (int64_t)(k0 + k) * mc];
+                    }
+                    __syncwarp();
+                }
+                T x[16];
+#pragma unroll
+                for (int k = 0; k < 16; k++) x[k] = (T)0;
+                if (lane < nscol) {
+                    for (int c = 0; c <= lane; c++) {
+                        const T l = li[lane + c * nscol];
+#pragma unroll
+                        for (int k = 0; k < 16; k++)
+                            if (k < nk) x[k] += l * ys[c * LF_LD + k];
+                    }
+#pragma unroll
+                    for (int k = 0; k < 16; k++)
+                        if (k < nk) {
+                            Y[k1 + lane + (int64_t)(k0 + k) * ldy] = x[k];
+                            xs[lane * LF_LD + k] = x[k];
+                        }
+                }
+                __syncwarp();
+                if (lane >= nscol && lane < nsrow) {
+                    T u[16];
+#pragma unroll
+                    for (int k = 0; k < 16; k++) u[k] = k < nk ? ys[lane * LF_LD + k] : (T)0;
+                    for (int c = 0; c < nscol; c++) {
+                        const T l = panel[lane + c * nsrow];
+#pragma unroll
+                        for (int k = 0; k < 16; k++)
+                            if (k < nk) u[k] += l * xs[c * LF_LD + k];
+                    }
+#pragma unroll
+                    for (int k = 0; k < 16; k++)
+                        if (k < nk) us[(lane - nscol) + (int64_t)(k0 + k) * m] = u[k];
+                }
+                __syncwarp();
+            }
+        }
+        if (lane == 0) done[root] = ntask_f[root];
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * LF_WARPS)
+k_bwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
+           const int32_t *__restrict__ blkoff, const int64_t *__restrict__ linvoff,
+           int32_t *ticket, const T *Lx, const T *Linv, int nrhs, T *Y, int64_t ldy)
+{
+    __shared__ T stage[LF_WARPS][2][32 * LF_LD];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T *ys = stage[warp][0], *xs = stage[warp][1];
+    for (int L = leaf_next(ticket); L < nleaf; L = leaf_next(ticket)) {
+        const int s0 = leaf[2 * L], root = leaf[2 * L + 1];
+        for (int s = root; s >= s0; s--) {
+            const int64_t k1 = P.Super[s];
+            const int nscol = (int)(P.Super[s + 1] - k1);
+            const int64_t psi = P.Pi[s];
+            const int nsrow = (int)(P.Pi[s + 1] - psi);
+            const int m = nsrow - nscol;
+            const T *panel = Lx + P.Px[s];
+            const T *li = Linv + linvoff[blkoff[s]];
+            for (int k0 = 0; k0 < nrhs; k0 += 16) {
+                const int nk = min(16, nrhs - k0);
+                if (lane < m) {
+                    const int64_t g = P.Ls[psi + nscol + lane];
+                    for (int k = 0; k < nk; k++) xs[lane * LF_LD + k] = Y[g + (int64_t)(k0 + k) * ldy];
+                }
+                __syncwarp();
+                if (lane < nscol) {
+                    T y[16];
+#pragma unroll
+                    for (int k = 0; k < 16; k++) y[k] = k < nk ? Y[k1 + lane + (int64_t)(k0 + k) * ldy] : (T)0;
+                    for (int q = 0; q < m; q++) {
+                        const T l = panel[nscol + q + (int64_t)lane * nsrow];
+#pragma unroll
+                        for (int k = 0; k < 16; k++)
+                            if (k < nk) y[k] -= l * xs[q * LF_LD + k];
+                    }
+#pragma unroll
+                    for (int k = 0; k < 16; k++)
+                        if (k < nk) ys[lane * LF_LD + k] = y[k];
+                }
+                __syncwarp();
+                if (lane < nscol) {
+                    T x[16];
+#pragma unroll
+                    for (int k = 0; k < 16; k++) x[k] = (T)0;
+                    for (int c = lane; c < nscol; c++) {
+                        const T l = li[c + lane * nscol];
+#pragma unroll
+                        for (int k = 0; k < 16; k++)
+                            if (k < nk) x[k] += l * ys[c * LF_LD + k];
+                    }
+#pragma unroll
+                    for (int k = 0; k < 16; k++)
+                        if (k < nk) Y[k1 + lane + (int64_t)(k0 + k) * ldy] = x[k];
+                }
+                __syncwarp();
+            }
+        }
+    }
+}
+
 // inverse of every diagonal block (lower triangular, nb <= 64), one block
 // each: thread j computes column j of X = L^-1 by forward substitution,
 // writing it straight to the output (its own earlier entries are re-read).
@@ -494,6 +655,38 @@ int gb_launch_sweep1(int forward, const gb_pattern_ptrs *pp, const gb_sweep1_arg
         const size_t sm = sweep_smem<float>();
         if (forward) k_fwd_sweep<float><<<grid, 256, sm, st>>>(P, S, (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy, (float *)U);
         else k_bwd_sweep<float><<<grid, 256, sm, st>>>(P, S, (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy);
+    }
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_sweep_leaf(int forward, const gb_pattern_ptrs *pp, const int32_t *leaf, int nleaf,
+                         const int32_t *blkoff, const int64_t *linvoff, const int32_t *ntask_f,
+                         int32_t *done, int32_t *ticket, const void *Lx, const void *Linv,
+                         int dtype, int nrhs, void *Y, int64_t ldy, void *U, int grid,
+                         cudaStream_t st)
+{
+    if (nleaf <= 0) return 0;
+    if (!leaf || !blkoff || !linvoff || !done || !ticket || !Lx || !Linv || !Y
+        || (forward && (!ntask_f || !U)))
+        return (int)cudaErrorInvalidValue;
+    gb_dev_pattern P = gb_to_dev(pp);
+    const int need = (nleaf + LF_WARPS - 1) / LF_WARPS;
+    if (grid > need) grid = need;
+    if (grid < 1) grid = 1;
+    if (dtype == 0) {
+        if (forward)
+            k_fwd_leaf<double><<<grid, 32 * LF_WARPS, 0, st>>>(P, leaf, nleaf, blkoff, linvoff, ntask_f, done, ticket,
+                                                               (const double *)Lx, (const double *)Linv, nrhs, (double *)Y, ldy, (double *)U);
+        else
+            k_bwd_leaf<double><<<grid, 32 * LF_WARPS, 0, st>>>(P, leaf, nleaf, blkoff, linvoff, ticket,
+                                                               (const double *)Lx, (const double *)Linv, nrhs, (double *)Y, ldy);
+    } else {
+        if (forward)
+            k_fwd_leaf<float><<<grid, 32 * LF_WARPS, 0, st>>>(P, leaf, nleaf, blkoff, linvoff, ntask_f, done, ticket,
+                                                              (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy, (float *)U);
+        else
+            k_bwd_leaf<float><<<grid, 32 * LF_WARPS, 0, st>>>(P, leaf, nleaf, blkoff, linvoff, ticket,
+                                                              (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy);
     }
     return (int)cudaGetLastError();
 }

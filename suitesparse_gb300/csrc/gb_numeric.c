@@ -524,10 +524,30 @@ int gb_run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int fo
             || cudaMemsetAsync(P->d_ticket, 0, sizeof(int32_t) * 4, st) != cudaSuccess)
             return FALSE;
         int grid = GB_MAX(1, ctx->sms) * 4;
-        if (gb_launch_sweep1(forward, &P->ptrs, &a, Lx, P->d_Linv[d], ldt, nrhs, Y, P->n,
-                             P->d_U, grid, st) != 0)
-            return FALSE;
-        ctx->launches += 1;
+        /* leaf subtrees (one warp each): before the other tasks forward,
+         * after them backward */
+        const int nleaf = (int)P->lf_t.n;
+        const int lgrid = GB_MAX(1, ctx->sms) * 16;
+        if (forward && nleaf > 0) {
+            if (gb_launch_sweep_leaf(1, &P->ptrs, P->d_lf, nleaf, P->d_blkoff, P->d_linvoff,
+                                     P->d_ntask_f, P->d_done, P->d_ticket + 1, Lx, P->d_Linv[d],
+                                     ldt, nrhs, Y, P->n, P->d_U, lgrid, st) != 0)
+                return FALSE;
+            ctx->launches += 1;
+        }
+        if (a.ntasks > 0) {
+            if (gb_launch_sweep1(forward, &P->ptrs, &a, Lx, P->d_Linv[d], ldt, nrhs, Y, P->n,
+                                 P->d_U, grid, st) != 0)
+                return FALSE;
+            ctx->launches += 1;
+        }
+        if (!forward && nleaf > 0) {
+            if (gb_launch_sweep_leaf(0, &P->ptrs, P->d_lf, nleaf, P->d_blkoff, P->d_linvoff,
+                                     P->d_ntask_b, P->d_done, P->d_ticket + 1, Lx, P->d_Linv[d],
+                                     ldt, nrhs, Y, P->n, P->d_U, lgrid, st) != 0)
+                return FALSE;
+            ctx->launches += 1;
+        }
         return TRUE;
     }
     gb_vec *seqv = forward ? &P->fwd_seq : &P->bwd_seq;

@@ -473,6 +473,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
     vec_init(&P->gb, sizeof(int32_t));
     vec_init(&P->sb_t, sizeof(gb_stask));
     vec_init(&P->sd_t, sizeof(gb_stask));
+    vec_init(&P->lf_t, 2 * sizeof(int32_t));
     vec_init(&P->fact_seq, sizeof(gb_launch_rec));
     vec_init(&P->dag_t, sizeof(gb_dtask));
     vec_init(&P->dag_sp, sizeof(int32_t));
@@ -904,11 +905,43 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
             ok &= gb_vec_push(&P->sd_t, &t);
         }
     }
+    /* leaf subtrees of the sweeps: maximal subtrees whose fronts all have at
+     * most warp_rows rows, at most GB_LEAF_MEMBERS supernodes each.  One warp
+     * sweeps a whole one (children first forward, parents first backward) in
+     * a launch of its own, before the forward sweep's other tasks (a leaf
+     * subtree depends on nothing) and after the backward sweep's (it depends
+     * only on its ancestors).  In postorder a subtree is the index range
+     * [root - size + 1, root]; its supernodes have no tasks in the lists. */
+    int32_t *lcnt = calloc(nsuper + 1, sizeof(int32_t));
+    char *lel = malloc(nsuper + 1), *lmem = calloc(nsuper + 1, 1);
+    if (!lcnt || !lel || !lmem) ok = 0;
+    for (Int s = 0; s < nsuper && ok; s++) lel[s] = Pi[s + 1] - Pi[s] <= P->warp_rows;
+    for (Int s = 0; s < nsuper && ok; s++) {          /* children before parents */
+        lcnt[s] += 1;
+        if (parent[s] != EMPTY) {
+            lcnt[parent[s]] += lcnt[s];
+            if (!lel[s]) lel[parent[s]] = 0;
+        }
+    }
+#define LEAF_OK(s) (lel[s] && lcnt[s] <= GB_LEAF_MEMBERS)
+    for (Int s = 0; s < nsuper && ok; s++) {
+        if (!LEAF_OK(s) || (parent[s] != EMPTY && LEAF_OK(parent[s]))) continue;
+        Int s0 = s - lcnt[s] + 1;
+        int contiguous = s0 >= 0;
+        for (Int q = s0; contiguous && q < s; q++)
+            contiguous = parent[q] > q && parent[q] <= s;
+        if (!contiguous) continue;
+        int32_t pr[2] = {(int32_t)s0, (int32_t)s};
+        ok &= gb_vec_push(&P->lf_t, pr);
+        for (Int q = s0; q <= s; q++) lmem[q] = 1;
+    }
+#undef LEAF_OK
     /* forward: levels ascending; backward: levels descending, so that a task
      * only depends on tasks listed before it and branches interleave */
     for (int l = 0; l < nlevels && ok; l++) {
         for (Int q = lev_ptr[l]; q < lev_ptr[l + 1]; q++) {
             Int s = lev_list[q];
+            if (lmem[s]) continue;
             Int nscol = Super[s + 1] - Super[s], nsrow = Pi[s + 1] - Pi[s];
             Int nblk = (nscol + 63) / 64;
             for (Int i = 0; i < nblk; i++) {
@@ -925,6 +958,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
     for (int l = nlevels - 1; l >= 0 && ok; l--) {
         for (Int q = lev_ptr[l + 1] - 1; q >= lev_ptr[l]; q--) {
             Int s = lev_list[q];
+            if (lmem[s]) continue;
             Int nscol = Super[s + 1] - Super[s];
             Int nblk = (nscol + 63) / 64;
             for (Int i = nblk - 1; i >= 0; i--) {
@@ -960,6 +994,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
             q = e;
         }
     }
+    free(lcnt); free(lel); free(lmem);
     P->nblk_total = nblk_total;
     P->h_linvoff = malloc(sizeof(int64_t) * (nblk_total + 1));
     if (!P->h_linvoff) ok = 0;
@@ -1066,6 +1101,7 @@ int gb_plan_upload(gb_plan *P)
     UP(P->d_gf, P->gf.p, P->gf.n * P->gf.esz);
     UP(P->d_gb, P->gb.p, P->gb.n * P->gb.esz);
     UP(P->d_sb, P->sb_t.p, P->sb_t.n * P->sb_t.esz);
+    UP(P->d_lf, P->lf_t.p, P->lf_t.n * P->lf_t.esz);
     UP(P->d_sd, P->sd_t.p, P->sd_t.n * P->sd_t.esz);
     UP(P->d_blkoff, P->h_blkoff, sizeof(int32_t) * (ns + 1));
     UP(P->d_ntask_f, P->h_ntask_f, sizeof(int32_t) * (ns + 1));
@@ -1141,6 +1177,7 @@ void gb_plan_free(gb_plan *P)
     free(P->h_blkoff); free(P->h_ntask_f); free(P->h_ntask_b); free(P->h_parent);
     free(P->h_linvoff);
     gb_vec_free(&P->sf_t); gb_vec_free(&P->sb_t); gb_vec_free(&P->sd_t);
+    gb_vec_free(&P->lf_t);
     gb_vec_free(&P->gf); gb_vec_free(&P->gb);
     gb_vec_free(&P->dag_t); gb_vec_free(&P->dag_sp); gb_vec_free(&P->dag_succ);
     gb_vec_free(&P->dag_nd); gb_vec_free(&P->dag_q0); gb_vec_free(&P->dag_q1);
@@ -1157,7 +1194,7 @@ void gb_plan_free(gb_plan *P)
                    P->d_gemm_owner, P->d_sweep, P->d_Lx[0], P->d_Lx[1], P->d_CB[0],
                    P->d_CB[1], P->d_Sp, P->d_Si, P->d_Sx, P->d_Y, P->d_U, P->d_B,
                    P->d_Rp, P->d_Rj, P->d_Rx, P->d_scale, P->d_scale_perm, P->d_X, P->d_R,
-                   P->d_bx, P->d_red, P->d_sf, P->d_sb, P->d_sd, P->d_blkoff, P->d_ntask_f,
+                   P->d_bx, P->d_red, P->d_sf, P->d_sb, P->d_sd, P->d_lf, P->d_blkoff, P->d_ntask_f,
                    P->d_ntask_b, P->d_parent, P->d_linvoff, P->d_xready, P->d_done,
                    P->d_ticket, P->d_Linv[0], P->d_Linv[1], P->d_dag_t, P->d_dag_sp,
                    P->d_dag_succ, P->d_dag_nd, P->d_dag_q0i, P->d_dag_q1i, P->d_dag_ctrl0,

@@ -92,6 +92,7 @@ typedef struct {
 
 /* right-hand-side columns per single-launch sweep pass */
 #define GB_SWEEP_COLS 16
+#define GB_LEAF_MEMBERS 64         /* supernodes of a sweep leaf subtree */
 
 /* a chunk of rows of one segment, for segmented reductions */
 typedef struct { int64_t lo, hi; int32_t seg, pad; } gb_seg_chunk;
@@ -171,6 +172,8 @@ typedef struct gb_plan {
 
     /* single-launch sweeps: tasks, diagonal-block inverses, flags */
     gb_vec sf_t, sb_t, sd_t;          /* forward, backward, diagonal-block tasks */
+    gb_vec lf_t;                      /* leaf subtrees of the sweeps: (first, root) */
+    int32_t *d_lf;
     int64_t nblk_total, linv_total;
     gb_stask *d_sf, *d_sb, *d_sd;
     gb_vec gf, gb;                    /* sweep task groups (forward, backward) */
@@ -336,6 +339,11 @@ int gb_launch_dag(const gb_pattern_ptrs *pp, const gb_dag_args *a, void *Lx, voi
 int gb_launch_sweep1(int forward, const gb_pattern_ptrs *pp, const gb_sweep1_args *a,
                      const void *Lx, const void *Linv, int dtype, int nrhs, void *Y,
                      int64_t ldy, void *U, int grid, cudaStream_t st);
+int gb_launch_sweep_leaf(int forward, const gb_pattern_ptrs *pp, const int32_t *leaf, int nleaf,
+                         const int32_t *blkoff, const int64_t *linvoff, const int32_t *ntask_f,
+                         int32_t *done, int32_t *ticket, const void *Lx, const void *Linv,
+                         int dtype, int nrhs, void *Y, int64_t ldy, void *U, int grid,
+                         cudaStream_t st);
 int gb_launch_diag_inverse(const gb_pattern_ptrs *pp, const gb_stask *dtasks, int ndiag,
                            const int32_t *blkoff, const int64_t *linvoff, const void *Lx,
                            void *Linv, int dtype, cudaStream_t st);
