@@ -433,17 +433,19 @@ k_bwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
 
 // ---- leaf subtrees: one warp each ------------------------------------------
 // A leaf subtree (supernodes s0..root, contiguous in postorder, every front
-// at most 32 rows) is swept by one warp, lane = row of the front, with no
+// at most 64 rows) is swept by one warp, rows r = lane and lane + 32, with no
 // waits: the forward sweep runs these before its other tasks (they depend on
 // nothing), the backward sweep after them (they depend only on their
 // ancestors' x, final by then).  Per supernode, forward:
 //   y1 = b1 - (children's update-vector rows in the diagonal block),
 //   x1 = Linv y1,  u = (children's rows below the diagonal block) + L21 x1;
 // backward: y1 = x1 - L21' x(rows below), x1 = Linv' y1.  Children's update
-// vectors are gathered in a fixed order (owner-computes).  A warp takes its
-// next subtree from a ticket.
+// vectors are gathered in a fixed order (owner-computes); their offsets are
+// fetched by the lanes together, one child per lane.  A warp takes its next
+// subtree from a ticket.  Right-hand sides in chunks of LF_RC.
 
-#define LF_LD 17                 // staging rows of 16 right-hand sides (+1)
+#define LF_RC 8                  // right-hand sides per chunk
+#define LF_LD 9                  // staging row length (LF_RC + 1)
 #define LF_WARPS 4               // warps per block
 
 __device__ __forceinline__ int leaf_next(int32_t *ticket)
@@ -454,13 +456,14 @@ __device__ __forceinline__ int leaf_next(int32_t *ticket)
 }
 
 template <typename T>
-__global__ void __launch_bounds__(32 * LF_WARPS)
+__global__ void __launch_bounds__(32 * LF_WARPS, 8)
 k_fwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
            const int32_t *__restrict__ blkoff, const int64_t *__restrict__ linvoff,
            const int32_t *__restrict__ ntask_f, int32_t *done, int32_t *ticket, const T *Lx,
            const T *Linv, int nrhs, T *Y, int64_t ldy, T *U)
 {
-    __shared__ T stage[LF_WARPS][2][32 * LF_LD];
+    constexpr unsigned FULL = 0xffffffffu;
+    __shared__ T stage[LF_WARPS][2][64 * LF_LD];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     T *ys = stage[warp][0], *xs = stage[warp][1];
     for (int L = leaf_next(ticket); L < nleaf; L = leaf_next(ticket)) {
@@ -473,56 +476,67 @@ k_fwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
             const T *panel = Lx + P.Px[s];
             const T *li = Linv + linvoff[blkoff[s]];
             T *us = U + P.cbvoff[s] * nrhs;
-            for (int k0 = 0; k0 < nrhs; k0 += 16) {
-                const int nk = min(16, nrhs - k0);
-                for (int k = 0; k < nk; k++)
-                    ys[lane * LF_LD + k] = lane < nscol ? Y[k1 + lane + (int64_t)(k0 + k) * ldy] : (T)0;
+            const int cb = P.child_ptr[s], nch = P.child_ptr[s + 1] - cb;
+            for (int k0 = 0; k0 < nrhs; k0 += LF_RC) {
+                const int nk = min(LF_RC, nrhs - k0);
+                for (int r = lane; r < nsrow; r += 32)
+                    for (int k = 0; k < nk; k++)
+                        ys[r * LF_LD + k] = r < nscol ? Y[k1 + r + (int64_t)(k0 + k) * ldy] : (T)0;
                 __syncwarp();
-                for (int ci = P.child_ptr[s]; ci < P.child_ptr[s + 1]; ci++) {
-                    const int c = P.child_list[ci];
-                    const int ncc = (int)(P.Super[c + 1] - P.Super[c]);
-                    const int64_t pic = P.Pi[c];
-                    const int mc = (int)(P.Pi[c + 1] - pic) - ncc;
-                    if (lane < mc) {
-                        const int t = P.relmap[pic + ncc + lane];
-                        const T *uc = U + P.cbvoff[c] * nrhs;
-                        const T sg = t < nscol ? (T)-1 : (T)1;
-                        for (int k = 0; k < nk; k++)
-                            ys[t * LF_LD + k] += sg * uc[lane + (int64_t)(k0 + k) * mc];
+                for (int j0 = 0; j0 < nch; j0 += 32) {
+                    int mc = 0;
+                    int64_t roff = 0, uoff = 0;
+                    if (j0 + lane < nch) {
+                        const int c = P.child_list[cb + j0 + lane];
+                        const int ncc = (int)(P.Super[c + 1] - P.Super[c]);
+                        const int64_t pic = P.Pi[c];
+                        mc = (int)(P.Pi[c + 1] - pic) - ncc;
+                        roff = pic + ncc;
+                        uoff = P.cbvoff[c] * nrhs;
                     }
-                    __syncwarp();
+                    const int nj = min(32, nch - j0);
+                    for (int j = 0; j < nj; j++) {
+                        const int mcj = __shfl_sync(FULL, mc, j);
+                        const int64_t rj = __shfl_sync(FULL, roff, j);
+                        const int64_t uj = __shfl_sync(FULL, uoff, j);
+                        for (int i = lane; i < mcj; i += 32) {
+                            const int t = P.relmap[rj + i];
+                            const T sg = t < nscol ? (T)-1 : (T)1;
+                            for (int k = 0; k < nk; k++)
+                                ys[t * LF_LD + k] += sg * U[uj + i + (int64_t)(k0 + k) * mcj];
+                        }
+                        __syncwarp();
+                    }
                 }
-                T x[16];
+                for (int r = lane; r < nscol; r += 32) {
+                    T x[LF_RC];
 #pragma unroll
-                for (int k = 0; k < 16; k++) x[k] = (T)0;
-                if (lane < nscol) {
-                    for (int c = 0; c <= lane; c++) {
-                        const T l = li[lane + c * nscol];
+                    for (int k = 0; k < LF_RC; k++) x[k] = (T)0;
+                    for (int c = 0; c <= r; c++) {
+                        const T l = li[r + c * nscol];
 #pragma unroll
-                        for (int k = 0; k < 16; k++)
-                            if (k < nk) x[k] += l * ys[c * LF_LD + k];
+                        for (int k = 0; k < LF_RC; k++) x[k] += l * ys[c * LF_LD + k];
                     }
 #pragma unroll
-                    for (int k = 0; k < 16; k++)
+                    for (int k = 0; k < LF_RC; k++)
                         if (k < nk) {
-                            Y[k1 + lane + (int64_t)(k0 + k) * ldy] = x[k];
-                            xs[lane * LF_LD + k] = x[k];
+                            Y[k1 + r + (int64_t)(k0 + k) * ldy] = x[k];
+                            xs[r * LF_LD + k] = x[k];
                         }
                 }
                 __syncwarp();
-                if (lane >= nscol && lane < nsrow) {
-                    T u[16];
+                for (int r = nscol + lane; r < nsrow; r += 32) {
+                    T u[LF_RC];
 #pragma unroll
-                    for (int k = 0; k < 16; k++) u[k] = k < nk ? ys[lane * LF_LD + k] : (T)0;
+                    for (int k = 0; k < LF_RC; k++) u[k] = ys[r * LF_LD + k];
                     for (int c = 0; c < nscol; c++) {
-                        const T l = panel[lane + c * nsrow];
+                        const T l = panel[r + (int64_t)c * nsrow];
 #pragma unroll
-                        for (int k = 0; k < 16; k++)
-                            if (k < nk) u[k] += l * xs[c * LF_LD + k];
+                        for (int k = 0; k < LF_RC; k++) u[k] += l * xs[c * LF_LD + k];
                     }
 #pragma unroll
-                    for (int k = 0; k < 16; k++)
-                        if (k < nk) us[(lane - nscol) + (int64_t)(k0 + k) * m] = u[k];
+                    for (int k = 0; k < LF_RC; k++)
+                        if (k < nk) us[(r - nscol) + (int64_t)(k0 + k) * m] = u[k];
                 }
                 __syncwarp();
             }
@@ -532,12 +546,12 @@ k_fwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
 }
 
 template <typename T>
-__global__ void __launch_bounds__(32 * LF_WARPS)
+__global__ void __launch_bounds__(32 * LF_WARPS, 8)
 k_bwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
            const int32_t *__restrict__ blkoff, const int64_t *__restrict__ linvoff,
            int32_t *ticket, const T *Lx, const T *Linv, int nrhs, T *Y, int64_t ldy)
 {
-    __shared__ T stage[LF_WARPS][2][32 * LF_LD];
+    __shared__ T stage[LF_WARPS][2][64 * LF_LD];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     T *ys = stage[warp][0], *xs = stage[warp][1];
     for (int L = leaf_next(ticket); L < nleaf; L = leaf_next(ticket)) {
@@ -550,41 +564,40 @@ k_bwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
             const int m = nsrow - nscol;
             const T *panel = Lx + P.Px[s];
             const T *li = Linv + linvoff[blkoff[s]];
-            for (int k0 = 0; k0 < nrhs; k0 += 16) {
-                const int nk = min(16, nrhs - k0);
-                if (lane < m) {
-                    const int64_t g = P.Ls[psi + nscol + lane];
-                    for (int k = 0; k < nk; k++) xs[lane * LF_LD + k] = Y[g + (int64_t)(k0 + k) * ldy];
+            for (int k0 = 0; k0 < nrhs; k0 += LF_RC) {
+                const int nk = min(LF_RC, nrhs - k0);
+                for (int q = lane; q < m; q += 32) {
+                    const int64_t g = P.Ls[psi + nscol + q];
+#pragma unroll
+                    for (int k = 0; k < LF_RC; k++)
+                        xs[q * LF_LD + k] = k < nk ? Y[g + (int64_t)(k0 + k) * ldy] : (T)0;
                 }
                 __syncwarp();
-                if (lane < nscol) {
-                    T y[16];
+                for (int r = lane; r < nscol; r += 32) {
+                    T y[LF_RC];
 #pragma unroll
-                    for (int k = 0; k < 16; k++) y[k] = k < nk ? Y[k1 + lane + (int64_t)(k0 + k) * ldy] : (T)0;
+                    for (int k = 0; k < LF_RC; k++) y[k] = k < nk ? Y[k1 + r + (int64_t)(k0 + k) * ldy] : (T)0;
                     for (int q = 0; q < m; q++) {
-                        const T l = panel[nscol + q + (int64_t)lane * nsrow];
+                        const T l = panel[nscol + q + (int64_t)r * nsrow];
 #pragma unroll
-                        for (int k = 0; k < 16; k++)
-                            if (k < nk) y[k] -= l * xs[q * LF_LD + k];
+                        for (int k = 0; k < LF_RC; k++) y[k] -= l * xs[q * LF_LD + k];
                     }
 #pragma unroll
-                    for (int k = 0; k < 16; k++)
-                        if (k < nk) ys[lane * LF_LD + k] = y[k];
+                    for (int k = 0; k < LF_RC; k++) ys[r * LF_LD + k] = y[k];
                 }
                 __syncwarp();
-                if (lane < nscol) {
-                    T x[16];
+                for (int r = lane; r < nscol; r += 32) {
+                    T x[LF_RC];
 #pragma unroll
-                    for (int k = 0; k < 16; k++) x[k] = (T)0;
-                    for (int c = lane; c < nscol; c++) {
-                        const T l = li[c + lane * nscol];
+                    for (int k = 0; k < LF_RC; k++) x[k] = (T)0;
+                    for (int c = r; c < nscol; c++) {
+                        const T l = li[c + r * nscol];
 #pragma unroll
-                        for (int k = 0; k < 16; k++)
-                            if (k < nk) x[k] += l * ys[c * LF_LD + k];
+                        for (int k = 0; k < LF_RC; k++) x[k] += l * ys[c * LF_LD + k];
                     }
 #pragma unroll
-                    for (int k = 0; k < 16; k++)
-                        if (k < nk) Y[k1 + lane + (int64_t)(k0 + k) * ldy] = x[k];
+                    for (int k = 0; k < LF_RC; k++)
+                        if (k < nk) Y[k1 + r + (int64_t)(k0 + k) * ldy] = x[k];
                 }
                 __syncwarp();
             }

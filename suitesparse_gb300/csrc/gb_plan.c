@@ -906,7 +906,8 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
         }
     }
     /* leaf subtrees of the sweeps: maximal subtrees whose fronts all have at
-     * most warp_rows rows, at most GB_LEAF_MEMBERS supernodes each.  One warp
+     * most GB_LEAF_ROWS rows, at most GB_LEAF_MEMBERS supernodes each (none
+     * when the one-warp fronts are off, warp_rows = 0).  One warp
      * sweeps a whole one (children first forward, parents first backward) in
      * a launch of its own, before the forward sweep's other tasks (a leaf
      * subtree depends on nothing) and after the backward sweep's (it depends
@@ -915,7 +916,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
     int32_t *lcnt = calloc(nsuper + 1, sizeof(int32_t));
     char *lel = malloc(nsuper + 1), *lmem = calloc(nsuper + 1, 1);
     if (!lcnt || !lel || !lmem) ok = 0;
-    for (Int s = 0; s < nsuper && ok; s++) lel[s] = Pi[s + 1] - Pi[s] <= P->warp_rows;
+    for (Int s = 0; s < nsuper && ok; s++) lel[s] = P->warp_rows > 0 && Pi[s + 1] - Pi[s] <= GB_LEAF_ROWS;
     for (Int s = 0; s < nsuper && ok; s++) {          /* children before parents */
         lcnt[s] += 1;
         if (parent[s] != EMPTY) {

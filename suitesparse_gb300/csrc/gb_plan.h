@@ -92,7 +92,8 @@ typedef struct {
 
 /* right-hand-side columns per single-launch sweep pass */
 #define GB_SWEEP_COLS 16
-#define GB_LEAF_MEMBERS 64         /* supernodes of a sweep leaf subtree */
+#define GB_LEAF_MEMBERS 256        /* supernodes of a sweep leaf subtree */
+#define GB_LEAF_ROWS 64            /* rows of a front in a sweep leaf subtree */
 
 /* a chunk of rows of one segment, for segmented reductions */
 typedef struct { int64_t lo, hi; int32_t seg, pad; } gb_seg_chunk;
