@@ -460,7 +460,9 @@ int gb300_get_factor_trace (cholmod_common *Common, unsigned long long *out,
     int64_t nmax) ;
 
 /* The factorization task graph of L's plan, 8 int32 per task: type, s, b,
- * r, c, priority, level, 0 (task types as in the trace).  Returns the count. */
+ * r, c, priority, level, 0 (task types as in the trace).  With the one-launch
+ * factorization (GB300_OPT_FACTOR = 1) the whole graph in the trace's order
+ * (level 0); otherwise the per-level graphs.  Returns the count. */
 int gb300_plan_tasks (cholmod_factor *L, cholmod_common *Common, int32_t *out, int64_t nmax) ;
 
 /* Facts of the GPU plan of L (built if needed): [0] algorithmic flops of the

@@ -13,6 +13,30 @@
 // relative-map scatter)
 // ---------------------------------------------------------------------------
 
+// dst[rm[i]] += src[i] for i = i0, i0 + 32, ... < mc (one lane's share of a
+// column; rm is injective, so each target takes one addition): eight rows
+// at a time with every load issued before the adds, so that a long column
+// costs few memory round trips
+template <typename TL>
+__device__ __forceinline__ void scatter_add_col(TL *__restrict__ dst, const TL *__restrict__ src,
+                                                const int32_t *__restrict__ rm, int i0, int mc)
+{
+    int i = i0;
+    for (; i + 7 * 32 < mc; i += 8 * 32) {
+        int r[8];
+        TL v[8], d[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) r[u] = rm[i + 32 * u];
+#pragma unroll
+        for (int u = 0; u < 8; u++) v[u] = src[i + 32 * u];
+#pragma unroll
+        for (int u = 0; u < 8; u++) d[u] = dst[r[u]];
+#pragma unroll
+        for (int u = 0; u < 8; u++) dst[r[u]] = d[u] + v[u];
+    }
+    for (; i < mc; i += 32) dst[rm[i]] += src[i];
+}
+
 template <typename TA, typename TL>
 __device__ void assemble_body(const gb_dev_pattern &P, const gb_asm_task tk,
                               const int64_t *__restrict__ Sp, const int64_t *__restrict__ Si,
@@ -94,13 +118,8 @@ __device__ void assemble_body(const gb_dev_pattern &P, const gb_asm_task tk,
         for (int j = j0 + warp; j < j1; j += nwarps) {
             const int t = rm[j];
             const TL *src = cbc + (int64_t)j * mc;
-            if (t < nscol) {
-                TL *dst = panel + (int64_t)t * nsrow;
-                for (int i = j + lane; i < mc; i += 32) dst[rm[i]] += src[i];
-            } else {
-                TL *dst = cb + (int64_t)(t - nscol) * m - nscol;
-                for (int i = j + lane; i < mc; i += 32) dst[rm[i]] += src[i];
-            }
+            TL *dst = t < nscol ? panel + (int64_t)t * nsrow : cb + (int64_t)(t - nscol) * m - nscol;
+            scatter_add_col<TL>(dst, src, rm, j + lane, mc);
         }
         __syncthreads();
     }

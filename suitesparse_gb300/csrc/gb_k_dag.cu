@@ -94,14 +94,16 @@ __device__ int dag_take(const gb_dq &D, const int32_t *slots, int h)
 __device__ int dag_pop(const gb_dq &D, int poller)
 {
     int32_t *ctrl = D.ctrl;
-    const int total0 = ctrl[6], total1 = ctrl[7];
     if (!poller) {
         const int h = atomicAdd(ctrl + 2, 1);
-        if (h >= total1) return -1;
+        if (h >= ctrl[7]) return -1;
         return dag_take(D, D.q1, h);
     }
     for (int it = 0; it < GB_DAG_SPIN; it++) {
         if (dag_ld_acquire(ctrl + 5)) return -2;
+        // the critical total shrinks when a block keeps a critical task it
+        // made ready (k_fdag) instead of queueing it
+        const int total0 = dag_ld_acquire(ctrl + 6);
         int h0 = dag_ld_acquire(ctrl + 0);
         if (h0 < total0 && h0 < dag_ld_acquire(ctrl + 1)) {
             if (atomicCAS(ctrl + 0, h0, h0 + 1) == h0) return dag_take(D, D.q0, h0);
@@ -167,6 +169,84 @@ __host__ __device__ constexpr size_t dag_smem()
     return sizeof(T) * (3 * 64 * 65);
 }
 
+// The POTRF and TRSM tile tasks, each with a register allocation of its own
+// (their tile loads hold 16-32 registers per thread; inlined, they would
+// push the tile products of the executor loop into spills).
+template <typename T>
+static __device__ __noinline__ void potrf_task(const gb_dev_pattern &P, const gb_dtask &tk, T *panel,
+                                               int nscol, int nsrow, int f, T *Linv,
+                                               unsigned char *smem_raw, int &sfail)
+{
+    T (*A)[65] = (T (*)[65])smem_raw;
+    T *S1 = (T *)smem_raw + 64 * 65, *S2 = S1 + 64 * 65;
+    const int s = tk.s;
+    const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
+    if (f < 0) {
+        T *blk = panel + c0 + (int64_t)c0 * nsrow;
+        // every load of the tile in flight before the shared stores
+        // (256 threads, 16 elements each)
+        T v[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int idx = threadIdx.x + 256 * q, i = idx & 63, j = idx >> 6;
+            v[q] = (i < nb && j < nb && i >= j) ? blk[i + (int64_t)j * nsrow] : (T)0;
+        }
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int idx = threadIdx.x + 256 * q;
+            A[idx & 63][idx >> 6] = v[q];
+        }
+        __syncthreads();
+        const int fl = potrf_inv64<T>(A, S1, S2, nb, &sfail);
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+            const int i = idx % nb, j = idx / nb;
+            if (i >= j) blk[i + (int64_t)j * nsrow] = A[i][j];
+        }
+        if (fl >= 0 && threadIdx.x == 0) {
+            P.fail[s] = c0 + fl;
+            atomicExch(P.anyfail, 1);
+        }
+        T *li = Linv + P.linvoff[P.blkoff[s] + tk.b];
+        for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+            const int i = idx % nb, j = idx / nb;
+            li[i + (int64_t)j * nb] = S1[j * 65 + i];
+        }
+    }
+}
+
+template <typename T>
+static __device__ __noinline__ void trsm_task(const gb_dev_pattern &P, const gb_dtask &tk, T *panel,
+                                              int nscol, int nsrow, int f, const T *Linv,
+                                              unsigned char *smem_raw)
+{
+    T *S1 = (T *)smem_raw + 64 * 65, *S2 = S1 + 64 * 65;
+    const int s = tk.s;
+    const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
+    if (!(f >= 0 && f < c0)) {
+        const int ncols = (f >= 0) ? f - c0 : nb;
+        const int r0 = max(64 * tk.r, c0 + nb), r1 = min(64 * tk.r + 64, nsrow);
+        const int nr = r1 - r0;
+        const T *li = Linv + P.linvoff[P.blkoff[s] + tk.b];
+        // both tiles' loads in flight before the shared stores
+        T v[16], w[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int idx = threadIdx.x + 256 * q, cc = idx & 63, k = idx >> 6;
+            v[q] = (cc < nb && k < nb) ? li[cc + (int64_t)k * nb] : (T)0;
+            w[q] = (cc < nr && k < nb) ? panel[r0 + cc + (int64_t)(c0 + k) * nsrow] : (T)0;
+        }
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int idx = threadIdx.x + 256 * q, cc = idx & 63, k = idx >> 6;
+            S2[k * 65 + cc] = v[q];
+            S1[k * 65 + cc] = w[q];
+        }
+        __syncthreads();
+        trsm_tile<T>(S1, S2, 65, nr, nb, ncols, panel + r0 + (int64_t)c0 * nsrow, nsrow);
+    }
+}
+
 // The work of one tile task (POTRF, TRSM, UPD or CB) of supernode tk.s.
 // smem_raw: dag_smem<T>() bytes.
 template <typename T>
@@ -181,45 +261,9 @@ __device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx
     T *panel = Lx + P.Px[s];
     const int f = P.fail[s];
     if (tk.type == GB_DT_POTRF) {
-        const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
-        if (f < 0) {
-            T *blk = panel + c0 + (int64_t)c0 * nsrow;
-            for (int idx = threadIdx.x; idx < 64 * 64; idx += blockDim.x) {
-                const int i = idx & 63, j = idx >> 6;
-                A[i][j] = (i < nb && j < nb && i >= j) ? blk[i + (int64_t)j * nsrow] : (T)0;
-            }
-            __syncthreads();
-            const int fl = potrf_inv64<T>(A, S1, S2, nb, &sfail);
-            __syncthreads();
-            for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
-                const int i = idx % nb, j = idx / nb;
-                if (i >= j) blk[i + (int64_t)j * nsrow] = A[i][j];
-            }
-            if (fl >= 0 && threadIdx.x == 0) {
-                P.fail[s] = c0 + fl;
-                atomicExch(P.anyfail, 1);
-            }
-            T *li = Linv + P.linvoff[P.blkoff[s] + tk.b];
-            for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
-                const int i = idx % nb, j = idx / nb;
-                li[i + (int64_t)j * nb] = S1[j * 65 + i];
-            }
-        }
+        potrf_task<T>(P, tk, panel, nscol, nsrow, f, Linv, smem_raw, sfail);
     } else if (tk.type == GB_DT_TRSM) {
-        const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
-        if (!(f >= 0 && f < c0)) {
-            const int ncols = (f >= 0) ? f - c0 : nb;
-            const int r0 = max(64 * tk.r, c0 + nb), r1 = min(64 * tk.r + 64, nsrow);
-            const int nr = r1 - r0;
-            const T *li = Linv + P.linvoff[P.blkoff[s] + tk.b];
-            for (int idx = threadIdx.x; idx < 64 * 64; idx += blockDim.x) {
-                const int cc = idx & 63, k = idx >> 6;
-                S2[k * 65 + cc] = (cc < nb && k < nb) ? li[cc + (int64_t)k * nb] : (T)0;
-                S1[k * 65 + cc] = (cc < nr && k < nb) ? panel[r0 + cc + (int64_t)(c0 + k) * nsrow] : (T)0;
-            }
-            __syncthreads();
-            trsm_tile<T>(S1, S2, 65, nr, nb, ncols, panel + r0 + (int64_t)c0 * nsrow, nsrow);
-        }
+        trsm_task<T>(P, tk, panel, nscol, nsrow, f, Linv, smem_raw);
     } else if (tk.type == GB_DT_UPD) {
         if (f < 0) {
             const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
@@ -337,10 +381,13 @@ __global__ void __launch_bounds__(256, 2)
 k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __shared__ int sid, sinst, sfail, spoll;
+    __shared__ int sid, sinst, sfail, spoll, snext;
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
-    if (threadIdx.x == 0) spoll = dag_role(D.Q);
+    if (threadIdx.x == 0) {
+        spoll = dag_role(D.Q);
+        snext = -1;
+    }
     __syncthreads();
     if (spoll == 2) return;
     const int poller = spoll;
@@ -369,7 +416,14 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
     }
     for (;;) {
         if (threadIdx.x == 0) {
-            sid = dag_pop(D.Q, poller);
+            // a critical task this block (a poller) made ready runs here
+            // next, without a trip through the queue
+            if (snext >= 0) {
+                sid = snext;
+                snext = -1;
+            } else {
+                sid = dag_pop(D.Q, poller);
+            }
             if (sid >= 0) sinst = fdag_instance(D, sid);
         }
         __syncthreads();
@@ -482,7 +536,12 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                 const int g = (int)(I.base + v);
                 if (dag_add_acq_rel(D.cnt + g, -1) != 1) continue;
                 if (PP.tasks[v].type != GB_DT_JOIN) {
-                    dag_push(D.Q, g, PP.tasks[v].prio);
+                    const int prio = PP.tasks[v].prio;
+                    if (prio == 0 && poller && atomicCAS(&snext, -1, g) == -1) {
+                        atomicSub(D.Q.ctrl + 6, 1);     // kept: one less to queue
+                        continue;
+                    }
+                    dag_push(D.Q, g, prio);
                     continue;
                 }
                 // a join (no work, never queued): release its successors here;
@@ -493,6 +552,7 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                     if (dag_add_acq_rel(D.cnt + gw, -1) == 1) dag_push(D.Q, gw, PP.tasks[w].prio);
                 }
             }
+            __syncwarp();      // snext, set by any lane, is read by thread 0
         }
     }
     if (TC && tc) {

@@ -920,6 +920,17 @@ int gb300_plan_tasks(cholmod_factor *L, cholmod_common *Common, int32_t *out, in
     if (!ctx || !gb_ctx_ready(ctx)) return -1;
     gb_plan *P = gb_plan_get(L, Common, ctx, 1);
     if (!P) return -1;
+    if (ctx->factor_mode == 1) {
+        /* the whole-factorization graph, local ids as in the trace */
+        const gb_dtask *f = P->fd_t.p;
+        int64_t nf = (int64_t)P->fd_t.n;
+        for (int64_t i = 0; out && i < nf && i < nmax; i++) {
+            out[8 * i + 0] = f[i].type; out[8 * i + 1] = f[i].s; out[8 * i + 2] = f[i].b;
+            out[8 * i + 3] = f[i].r; out[8 * i + 4] = f[i].c; out[8 * i + 5] = f[i].prio;
+            out[8 * i + 6] = 0; out[8 * i + 7] = 0;
+        }
+        return (int)nf;
+    }
     const gb_dtask *t = P->dag_t.p;
     const gb_dag_level *lv = P->dag_lv.p;
     int64_t n = (int64_t)P->dag_t.n;
