@@ -270,13 +270,9 @@ __device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx
             const int cs = 64 * tk.c, ce = min(cs + 64, nscol);
             const int rs = max(64 * tk.r, cs), re = min(64 * tk.r + 64, nsrow);
             if constexpr (sizeof(T) == 4) {
-                if (tc)
-                    gemm_tile_tc(panel + rs + (int64_t)c0 * nsrow, nsrow,
-                                 panel + cs + (int64_t)c0 * nsrow, nsrow,
-                                 panel + rs + (int64_t)cs * nsrow, nsrow,
-                                 re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, smem_raw, *tc);
-                else
-                    gemm_tile_f32(panel + rs + (int64_t)c0 * nsrow, nsrow,
+                // k = 64: the CUDA cores (the tensor-core tile's fixed costs
+                // make it slower at this depth)
+                gemm_tile_f32(panel + rs + (int64_t)c0 * nsrow, nsrow,
                                   panel + cs + (int64_t)c0 * nsrow, nsrow,
                                   panel + rs + (int64_t)cs * nsrow, nsrow,
                                   re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, (float *)smem_raw);
@@ -292,7 +288,7 @@ __device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx
             const int m = nsrow - nscol;
             const int I = 64 * tk.r, J = 64 * tk.c;
             if constexpr (sizeof(T) == 4) {
-                if (tc)
+                if (tc && nscol >= GB_TC_MIN_K)
                     gemm_tile_tc(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
                                  CB + P.cboff[s] + I + (int64_t)J * m, m,
                                  min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
@@ -374,6 +370,13 @@ __device__ __forceinline__ int fdag_instance(const gb_fdag_dev &D, int id)
 }
 
 static_assert(8 * warp_front_smem<float>() <= dag_smem<float>(), "one-warp fronts: shared memory");
+
+// shared memory of the tensor-core executor: the tile tasks' space and the
+// two operand stages of gemm_tile_tc, and more than a third of the SM's
+// 228 KB so that at most 2 blocks (2 x GB_TC_COLS TMEM columns) share an SM
+#define GB_FDAG_TC_SMEM (80 * 1024)
+static_assert(GB_FDAG_TC_SMEM >= GB_TC_SMEM && GB_FDAG_TC_SMEM >= (int)dag_smem<float>()
+              && 3 * GB_FDAG_TC_SMEM > 228 * 1024, "tensor-core executor: shared memory");
 static_assert(8 * warp_front_smem<double>() <= dag_smem<double>(), "one-warp fronts: shared memory");
 
 template <typename T, bool TC>
@@ -382,7 +385,7 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ int sid, sinst, sfail, spoll, snext;
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
     if (threadIdx.x == 0) {
         spoll = dag_role(D.Q);
@@ -391,26 +394,28 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
     __syncthreads();
     if (spoll == 2) return;
     const int poller = spoll;
-    // FP32: tile products on the tensor cores; a TMEM accumulator of 64
-    // columns for the block's lifetime (at most 2 blocks per SM: 128 of 512)
+    // FP32: tile products on the tensor cores; two TMEM accumulators of 128
+    // columns for the block's lifetime (GB_TC_COLS; the launch's shared
+    // memory keeps at most 2 blocks per SM: 512 of 512 columns)
     gb_tc_ctx tcx = {0u, 0u, 0u, 1};
     gb_tc_ctx *tc = nullptr;
     if constexpr (TC && sizeof(T) == 4) {
         {
             if (threadIdx.x == 0) {
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(gb_su32(&mbar)), "r"(1));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(gb_su32(&mbar[0])), "r"(1));
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(gb_su32(&mbar[1])), "r"(1));
                 asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             }
             if (threadIdx.x < 32) {
                 asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                             :: "r"(gb_su32(&tmem_base)), "r"(64));
+                             :: "r"(gb_su32(&tmem_base)), "r"(GB_TC_COLS));
                 asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             tcx.taddr = tmem_base;
-            tcx.mbar = gb_su32(&mbar);
+            tcx.mbar = gb_su32(&mbar[0]);
             tc = &tcx;
         }
     }
@@ -557,14 +562,15 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
     }
     if (TC && tc) {
         if (!tcx.ok) {
-            // MMAs may still be in flight: wait once more (bounded) before
-            // the accumulator is released
-            gb_mbar_wait(tcx.mbar, tcx.phase);
+            // MMAs may still be in flight: wait once more on each stage
+            // (bounded) before the accumulators are released
+            gb_mbar_wait(tcx.mbar, tcx.phase & 1u);
+            gb_mbar_wait(tcx.mbar + 8, (tcx.phase >> 1) & 1u);
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
         if (threadIdx.x < 32)
-            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tcx.taddr), "r"(64));
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tcx.taddr), "r"(GB_TC_COLS));
     }
 }
 
@@ -585,7 +591,7 @@ int gb_launch_fdag(const gb_fdag_args *a, void *Lx, void *CB, void *Linv, int dt
     if (!configured) {
         cudaFuncSetAttribute(k_fdag<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<double>());
         cudaFuncSetAttribute(k_fdag<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<float>());
-        cudaFuncSetAttribute(k_fdag<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<float>());
+        cudaFuncSetAttribute(k_fdag<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_FDAG_TC_SMEM);
         configured = 1;
     }
     if (grid > a->ntotal + GB_DAG_POLLERS) grid = (int)(a->ntotal + GB_DAG_POLLERS);
@@ -593,7 +599,7 @@ int gb_launch_fdag(const gb_fdag_args *a, void *Lx, void *CB, void *Linv, int dt
     if (dtype == 0)
         k_fdag<double, false><<<grid, 256, dag_smem<double>(), st>>>(D, (double *)Lx, (double *)CB, (double *)Linv);
     else if (D.use_tc)
-        k_fdag<float, true><<<grid, 256, dag_smem<float>(), st>>>(D, (float *)Lx, (float *)CB, (float *)Linv);
+        k_fdag<float, true><<<grid, 256, GB_FDAG_TC_SMEM, st>>>(D, (float *)Lx, (float *)CB, (float *)Linv);
     else
         k_fdag<float, false><<<grid, 256, dag_smem<float>(), st>>>(D, (float *)Lx, (float *)CB, (float *)Linv);
     return (int)cudaGetLastError();
