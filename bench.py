@@ -308,6 +308,26 @@ def run_gpu(args):
         solves[str(k)] = {"solves_per_s": k / (statistics.mean(ts) * 1e-3),
                           "iterations": rk["iterations"], "berr": rk["berr"]}
 
+    # the same step with the update-block tiles on the tensor cores
+    # (GB300_OPT_TENSOR; opt-in: its factor error costs a refinement step)
+    c.set_option(CH.GB300_OPT_TENSOR, 1)
+    tc_fac, tc_sol, tc_it, tc_be = [], [], [], []
+    for i in range(4):
+        f_ms, s_ms, _, Xt, rt_ = step_mixed()
+        if i > 0:
+            tc_fac.append(f_ms)
+            tc_sol.append(s_ms)
+            tc_it.append(rt_["iterations"])
+    tc_be = float(O.backward_error(n, Ap, Ai, Ax, Xt, B).max())
+    c.set_option(CH.GB300_OPT_TENSOR, 0)
+    tensor = {"factor_ms": statistics.mean(tc_fac),
+              "factor_tflops": fl / (statistics.mean(tc_fac) * 1e-3) / 1e12,
+              "refine_ms": statistics.mean(tc_sol), "refine_iterations": tc_it[-1],
+              "solves_per_s": 1e3 / (statistics.mean(tc_fac) + statistics.mean(tc_sol)),
+              "backward_error": tc_be,
+              "note": "update-block tiles of depth >= 128 as tcgen05 kind::tf32 MMAs "
+                      "(hi/lo split, 4 products); default off"}
+
     # roofline of the dominant kernel (tile update) from a profiled factorization
     c.set_option(CH.GB300_OPT_PROFILE, 1)
     CH.factorize_mixed(A, L, c)
@@ -354,6 +374,7 @@ def run_gpu(args):
         "speedup_solves_vs_fp64": (1e3 / statistics.mean(t_step)) /
                                   (1e3 / (statistics.mean(fp64_fac) + statistics.mean(fp64_sol))),
         "resident_factor_solves": solves,
+        "tensor_cores": tensor,
         "e2e": {"value": e2e_val, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "solves_per_s": 1.0 / statistics.mean(e2e_s) * ws},

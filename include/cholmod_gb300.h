@@ -354,6 +354,11 @@ int gb300_finish (cholmod_common *Common) ;
  *      subtree), several one-warp fronts at once.  The factor is the same
  *      bit for bit with every value.  0 = never.  A change applies from the
  *      next factorization (the plan is rebuilt).
+ *  GB300_OPT_GRAPH [1]: 1 = gb300_solve_refined replays its refinement
+ *      step (permutation, both sweeps, residual, backward error) from a
+ *      CUDA graph captured once per pattern, right-hand-side count and
+ *      factor precision (the first step of a solve with new buffers runs
+ *      directly); 0 = every step launches its kernels one by one.
  *  GB300_OPT_PROFILE [0]: 1 = time every kernel launch of the factorization
  *      with CUDA events (summed per kernel kind, see gb300_get_profile); also
  *      clears the accumulated profile.
@@ -381,6 +386,7 @@ int gb300_finish (cholmod_common *Common) ;
 #define GB300_OPT_TENSOR         7
 #define GB300_OPT_SUBTREE_WORK   8
 #define GB300_OPT_WARP_ROWS      9
+#define GB300_OPT_GRAPH          10
 int gb300_set_option (cholmod_common *Common, int option, int64_t value) ;
 
 /* Supernodal symbolic analysis of A (stype < 0, lower) with a given final

@@ -195,6 +195,80 @@ int gb300_factorize_mixed(cholmod_sparse *A, cholmod_factor *L, cholmod_common *
     return TRUE;
 }
 
+/* The device work of one refinement step on the context's stream: the
+ * correction x += D P' L^-T L^-1 P D r, the residual r = b - A x, and the
+ * per-segment, per-column backward-error terms in d_bred. */
+static int refine_step_launch(gb_plan *P, gb_ctx *ctx, int nrhs, int single)
+{
+    cudaStream_t st = ctx->stream;
+    const Int n = P->n;
+    const int ydt = single ? 4 : 0;
+    const double *scale = single ? P->d_scale : NULL;
+    return gb_launch_perm_in(n, nrhs, P->d_Perm, scale, P->d_R, 0, n, P->d_Y, ydt, n, st) == 0
+           && gb_run_sweep(P, ctx, single ? CHOLMOD_SINGLE : CHOLMOD_DOUBLE, nrhs, P->d_Y, 1)
+           && gb_run_sweep(P, ctx, single ? CHOLMOD_SINGLE : CHOLMOD_DOUBLE, nrhs, P->d_Y, 0)
+           && gb_launch_perm_out(n, nrhs, P->d_Perm, scale, P->d_Y, ydt, n, P->d_X, 0, n, 1, st) == 0
+           && gb_launch_residual(n, nrhs, P->d_Rp, P->d_Rj, P->d_Rx, P->d_X, n, P->d_bx, n,
+                                 P->d_R, n, st) == 0
+           && gb_launch_colmax3_seg(P->nchunk, P->d_chunk, P->nseg, nrhs, P->d_R, n, P->d_X, n,
+                                    P->d_bx, n, P->d_bred, st) == 0;
+}
+
+void gb_graph_free(gb_plan *P)
+{
+    if (P->g_exec) cudaGraphExecDestroy((cudaGraphExec_t)P->g_exec);
+    P->g_exec = NULL;
+}
+
+/* the buffers a captured step reads and writes (a reallocation of any of
+ * them invalidates the graph) */
+static void graph_bufs(gb_plan *P, int single, const void **b)
+{
+    b[0] = P->d_Y; b[1] = P->d_R; b[2] = P->d_X; b[3] = P->d_bx; b[4] = P->d_bred;
+    b[5] = P->d_U; b[6] = P->d_Lx[single ? 1 : 0]; b[7] = P->d_Linv[single ? 1 : 0];
+}
+
+/* One refinement step: from the plan's CUDA graph when it matches, else
+ * captured into one (when allowed) and replayed, else launched directly. */
+static int refine_step(gb_plan *P, gb_ctx *ctx, int nrhs, int single, int may_capture)
+{
+    cudaStream_t st = ctx->stream;
+    if (!ctx->graph_mode || ctx->sweep_mode != 1 || ctx->trace_on)
+        return refine_step_launch(P, ctx, nrhs, single);
+    const void *b[8];
+    graph_bufs(P, single, b);
+    int match = P->g_exec && P->g_nrhs == nrhs && P->g_single == single
+                && memcmp(b, P->g_bufs, sizeof b) == 0;
+    if (!match) {
+        if (!may_capture) return refine_step_launch(P, ctx, nrhs, single);
+        gb_graph_free(P);
+        cudaGraph_t g = NULL;
+        cudaGraphExec_t ge = NULL;
+        const int64_t l0 = ctx->launches;
+        int ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            int launched = refine_step_launch(P, ctx, nrhs, single);
+            ok = cudaStreamEndCapture(st, &g) == cudaSuccess && launched && g
+                 && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+        }
+        if (g) cudaGraphDestroy(g);
+        if (!ok) {
+            /* capture refused: clear the error, launch directly */
+            if (ge) cudaGraphExecDestroy(ge);
+            cudaGetLastError();
+            return refine_step_launch(P, ctx, nrhs, single);
+        }
+        P->g_exec = ge;
+        P->g_launches = ctx->launches - l0;
+        ctx->launches = l0;
+        P->g_nrhs = nrhs;
+        P->g_single = single;
+        memcpy(P->g_bufs, b, sizeof b);
+    }
+    ctx->launches += P->g_launches;
+    return cudaGraphLaunch((cudaGraphExec_t)P->g_exec, st) == cudaSuccess;
+}
+
 cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod_dense *B,
                                    double tol, double *info, cholmod_common *Common)
 {
@@ -240,18 +314,12 @@ cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod
     double bmax_all = 0, berr_max = INFINITY;
     for (int64_t r = 0; r < nsg * nrhs && best; r++) best[r] = INFINITY;
     while (ok && it < GB_MAX_REFINE) {
-        /* correction with the current factor: x += D P' L^-T L^-1 P D r */
+        /* correction with the current factor, residual, backward-error
+         * terms: the first step of a solve whose buffers are new runs
+         * directly (buffers, inverses and launch settings exist after it),
+         * later ones may be captured into the pattern's graph */
         int single = (P->mixed == 1);
-        int ydt = single ? 4 : 0;
-        const double *scale = single ? P->d_scale : NULL;
-        ok = gb_launch_perm_in(n, nrhs, P->d_Perm, scale, P->d_R, 0, n, P->d_Y, ydt, n, st) == 0
-             && gb_run_sweep(P, ctx, single ? CHOLMOD_SINGLE : CHOLMOD_DOUBLE, nrhs, P->d_Y, 1)
-             && gb_run_sweep(P, ctx, single ? CHOLMOD_SINGLE : CHOLMOD_DOUBLE, nrhs, P->d_Y, 0)
-             && gb_launch_perm_out(n, nrhs, P->d_Perm, scale, P->d_Y, ydt, n, P->d_X, 0, n, 1, st) == 0
-             && gb_launch_residual(n, nrhs, P->d_Rp, P->d_Rj, P->d_Rx, P->d_X, n, P->d_bx, n,
-                                   P->d_R, n, st) == 0
-             && gb_launch_colmax3_seg(P->nchunk, P->d_chunk, nsg, nrhs, P->d_R, n, P->d_X, n,
-                                      P->d_bx, n, P->d_bred, st) == 0
+        ok = refine_step(P, ctx, nrhs, single, it > 0 || P->g_exec != NULL)
              && cudaMemcpyAsync(hred, P->d_bred, sizeof(double) * nred, cudaMemcpyDeviceToHost, st) == cudaSuccess
              && cudaMemcpyAsync(&serr, P->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, st) == cudaSuccess
              && cudaStreamSynchronize(st) == cudaSuccess && !(ctx->sweep_mode == 1 && serr);

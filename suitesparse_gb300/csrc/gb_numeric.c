@@ -30,6 +30,7 @@ gb_ctx *gb_ctx_new(void)
     c->sweep_mode = 1;
     c->factor_mode = 1;
     c->tc_mode = 0;
+    c->graph_mode = 1;
     return c;
 }
 
@@ -77,6 +78,7 @@ int gb300_set_option(cholmod_common *Common, int option, int64_t value)
     else if (option == GB300_OPT_SWEEP) c->sweep_mode = value ? 1 : 0;
     else if (option == GB300_OPT_FACTOR) c->factor_mode = value ? 1 : 0;
     else if (option == GB300_OPT_TENSOR) c->tc_mode = value ? 1 : 0;
+    else if (option == GB300_OPT_GRAPH) c->graph_mode = value ? 1 : 0;
     else if (option == GB300_OPT_TRACE) c->trace_on = value ? 1 : 0;
     else if (option == GB300_OPT_PROFILE) {
         c->prof = value ? 1 : 0;

@@ -1184,6 +1184,7 @@ void gb_plan_free(gb_plan *P)
     gb_vec_free(&P->dag_nd); gb_vec_free(&P->dag_q0); gb_vec_free(&P->dag_q1);
     gb_vec_free(&P->dag_lv);
     gb_valmap_free(P);
+    gb_graph_free(P);
     free(P->h_seg); free(P->h_chunk); free(P->h_anorm_seg);
     gb_vec_free(&P->fd_t); gb_vec_free(&P->fd_sp); gb_vec_free(&P->fd_succ);
     gb_vec_free(&P->fd_nd); gb_vec_free(&P->fd_q0); gb_vec_free(&P->fd_q1);

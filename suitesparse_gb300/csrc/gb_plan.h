@@ -224,6 +224,13 @@ typedef struct gb_plan {
     gb_seg_chunk *d_chunk;
     double *h_anorm_seg, *d_anorm_seg, *d_bred;
     size_t bred_cap;
+    /* CUDA graph of one refinement step (gb_mixed.c), per pattern: valid
+     * for the right-hand-side count, factor precision and buffers it was
+     * captured with */
+    void *g_exec;
+    int g_nrhs, g_single;
+    int64_t g_launches;               /* kernel launches one replay makes */
+    const void *g_bufs[8];
 
     struct gb_plan *next;             /* side-table chaining */
 } gb_plan;
@@ -250,6 +257,7 @@ struct gb_ctx {
     int factor_mode;             /* 1 = one whole-factorization launch (default), 0 = per level */
     int tc_mode;                 /* 1 = FP32 tile products on the tensor cores (default 0) */
     int trace_on;                /* record per-task times of the sweeps */
+    int graph_mode;              /* 1 = refinement steps replayed from a CUDA graph (default) */
     unsigned long long *d_trace; /* device trace buffer (3 x tasks) */
     size_t trace_cap;
     int64_t trace_n[2];          /* tasks traced by the last forward/backward sweep */
@@ -269,6 +277,7 @@ void gb_vec_free(gb_vec *v);
 /* Build the plan (host side) for a supernodal symbolic factor. */
 int gb_valmap_apply(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, cholmod_common *Common);
 void gb_valmap_free(gb_plan *P);
+void gb_graph_free(gb_plan *P);     /* gb_mixed.c */
 gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_work,
                        int64_t warp_rows);
 /* Upload the pattern, task arrays and launch sequences. */

@@ -90,3 +90,29 @@ def test_refined_tensor_core_tiles(golden, lib, oracle_mod):
         assert be.max() <= TOL and not info["fp64_fallback"], (name, be.max(), info)
         CH.free_factor(L, c)
         CH.free_sparse(A, c)
+
+
+def test_refinement_graph_replay_same_result(golden, lib, oracle_mod):
+    """A refinement step replayed from the pattern's CUDA graph
+    (GB300_OPT_GRAPH) gives the same solution bit for bit as the step
+    launched kernel by kernel, for repeated solves and a change of the
+    right-hand-side count (the graph is captured again)."""
+    meta, arrays = golden
+    res = {}
+    for graph in (0, 1):
+        c = CH.Common()
+        c.set_option(CH.GB300_OPT_GRAPH, graph)
+        mat, A, L = setup(meta, arrays, "c1", c)
+        assert CH.factorize_mixed(A, L, c) == 1
+        out = []
+        for k, seed in ((2, 5), (2, 6), (5, 7), (2, 8)):
+            B = M.rhs(mat[0], k, seed)
+            X, info = CH.solve_refined(A, L, B, c, tol=TOL)
+            assert oracle_mod.backward_error(*mat, X, B).max() <= TOL
+            out.append((np.array(X, copy=True), info["iterations"]))
+        res[graph] = out
+        CH.free_factor(L, c)
+        CH.free_sparse(A, c)
+    for (x0, i0), (x1, i1) in zip(res[0], res[1]):
+        assert i0 == i1
+        assert np.array_equal(x0, x1)
