@@ -92,3 +92,33 @@ def test_solves_with_and_without_warp_paths(golden, lib, oracle_mod, name, nrhs)
         CH.free_factor(L, c)
         CH.free_sparse(A, c)
     np.testing.assert_allclose(sols[1], sols[0], rtol=1e-10, atol=1e-12 * np.abs(sols[0]).max())
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_random_orderings_match_oracle(lib, oracle_mod, seed):
+    """Random permutations give irregular elimination trees (subtrees that
+    are not index ranges, fronts of every height): the one-warp fronts, the
+    subtree waves and the sweeps' leaf subtrees still give the oracle's
+    factor and accurate solves."""
+    rng = np.random.default_rng(seed)
+    n, Ap, Ai, Ax = M.laplace2d(24 + 6 * seed, seed=seed)
+    perm = rng.permutation(n).astype(np.int64)
+    c = CH.Common()
+    A = CH.sparse(n, Ap, Ai, Ax, c)
+    L = CH.analyze_perm(A, perm, c)
+    assert CH.factorize(A, L, c) == 1 and c.status == CH.CHOLMOD_OK
+    f = CH.factor_arrays(L)
+    sym = {k: f[k] for k in ("Super", "Pi", "Px", "Ls")}
+    sym["n"] = n
+    Sp, Si, Sx = oracle_mod.permute_lower(n, Ap, Ai, Ax, perm)
+    st, minor, Lref = oracle_mod.factor(sym, Sp, Si, Sx)
+    rel = np.linalg.norm(f["Lx"] - Lref) / np.linalg.norm(Lref)
+    assert rel < 1e-10, rel
+    B = M.rhs(n, 3, seed)
+    X = CH.solve(L, B, c)
+    assert oracle_mod.backward_error(n, Ap, Ai, Ax, X, B).max() <= 1e-14
+    assert CH.factorize_mixed(A, L, c) == 1
+    Xm, info = CH.solve_refined(A, L, B, c, tol=1e-12)
+    assert oracle_mod.backward_error(n, Ap, Ai, Ax, Xm, B).max() <= 1e-12
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
