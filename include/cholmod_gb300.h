@@ -471,6 +471,13 @@ int gb300_get_factor_trace (cholmod_common *Common, unsigned long long *out,
  * (level 0); otherwise the per-level graphs.  Returns the count. */
 int gb300_plan_tasks (cholmod_factor *L, cholmod_common *Common, int32_t *out, int64_t nmax) ;
 
+/* The single-launch sweep's tasks (forward = 1 or backward) of L's plan in
+ * ticket order, the order of gb300_get_trace: 5 int32 per task: s, kind
+ * (0 diagonal block, 1 off-diagonal rows), idx, r0, nr.  Supernodes of the
+ * sweeps' leaf subtrees have none.  Returns the count. */
+int gb300_plan_sweep_tasks (cholmod_factor *L, cholmod_common *Common, int forward,
+    int32_t *out, int64_t nmax) ;
+
 /* Facts of the GPU plan of L (built if needed): [0] algorithmic flops of the
  * task graphs (wide panels' LL', solves and updates, and every update block), [1] etree levels, [2] launches per factorization, [3]
  * update-block entries, [4] tile-update tasks, [5] supernodes, [6] launches

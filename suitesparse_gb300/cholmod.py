@@ -99,6 +99,7 @@ def lib():
         "gb300_get_trace": (C.c_int, [vp, C.c_int, C.POINTER(C.c_ulonglong), C.c_int64]),
         "gb300_get_factor_trace": (C.c_int, [vp, C.POINTER(C.c_ulonglong), C.c_int64]),
         "gb300_plan_tasks": (C.c_int, [FP, vp, C.POINTER(C.c_int32), C.c_int64]),
+        "gb300_plan_sweep_tasks": (C.c_int, [FP, vp, C.c_int, C.POINTER(C.c_int32), C.c_int64]),
         "gb300_batch_analyze": (FP, [C.c_int, C.POINTER(FP), C.c_int64, C.POINTER(C.c_int32), vp]),
         "cholmod_l_super_numeric": (C.c_int, [SP, SP, C.POINTER(C.c_double), FP, vp]),
         "cholmod_l_super_lsolve": (C.c_int, [FP, DP, DP, vp]),

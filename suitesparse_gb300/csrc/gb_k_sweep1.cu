@@ -172,6 +172,8 @@ struct gb_sweep_state {
     const int32_t *parent;     // supernodal etree parent (-1 root)
     int32_t *xready, *done, *ticket, *err;
     unsigned long long *trace; // optional: per task [start, dependencies met, end] (ns)
+    const int32_t *cptr;       // forward: child row ranges of each task (gb_plan.c)
+    const int32_t *crange;
 };
 
 // dynamic shared memory: tile A, tile B (64 x TLD each), xs, ys (64 x RCH)
@@ -186,6 +188,11 @@ k_fwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *tA = (T *)smem_raw, *tB = tA + SR * TLD, *xs = tB + SR * TLD, *ys = xs + SR * RCH;
     __shared__ int sg, abort_;
+    // children of the task's supernode, 32 at a time: update-vector rows
+    // [a, b) that fall in the task's rows, their count mc, the offsets of
+    // their relative map and update vector
+    __shared__ int c_a[32], c_b[32], c_mc[32];
+    __shared__ int64_t c_rm[32], c_u[32];
     T reg[16];
     for (;;) {
         if (threadIdx.x == 0) { sg = atomicAdd(S.ticket, 1); abort_ = 0; }
@@ -215,11 +222,17 @@ k_fwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
         // first L tile this task needs, fetched before any wait
         if (tk.kind == 0 && tk.idx > 0) tile_fetch(reg, panel + r0, nsrow, nr, SR);
         else if (tk.kind == 1) tile_fetch(reg, panel + r0, nsrow, nr, min(SR, nscol));
-        if (threadIdx.x == 0) {
-            for (int ci = P.child_ptr[s]; ci < P.child_ptr[s + 1] && !abort_; ci++) {
-                const int c = P.child_list[ci];
-                if (!wait_ge(S.done + c, S.ntask_s[c], S.err)) abort_ = 1;
+        const int cb0 = P.child_ptr[s], nch = P.child_ptr[s + 1] - cb0;
+        const int32_t *cr = S.crange + 2 * (int64_t)S.cptr[t];
+        // the children's update vectors: warp 0 waits for up to 32 children
+        // at once, one lane each
+        if (threadIdx.x < 32) {
+            bool ok = true;
+            for (int j = (int)threadIdx.x; j < nch && ok; j += 32) {
+                const int c = P.child_list[cb0 + j];
+                ok = wait_ge(S.done + c, S.ntask_s[c], S.err);
             }
+            if (__any_sync(0xffffffffu, !ok) && threadIdx.x == 0) abort_ = 1;
         }
         __syncthreads();
         if (abort_) return;
@@ -240,20 +253,32 @@ k_fwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
             __syncthreads();
             // gather the children's update vectors at rows [r0, r0+nr)
             const T gsign = tk.kind == 0 ? (T)-1 : (T)1;
-            for (int ci = P.child_ptr[s]; ci < P.child_ptr[s + 1]; ci++) {
-                const int c = P.child_list[ci];
-                const int ncc = (int)(P.Super[c + 1] - P.Super[c]);
-                const int64_t pic = P.Pi[c];
-                const int mc = (int)(P.Pi[c + 1] - pic) - ncc;
-                const int32_t *rm = P.relmap + pic + ncc;
-                const int a = lower_bound_i32(rm, 0, mc, r0);
-                const int b = lower_bound_i32(rm, a, mc, r0 + nr);
-                const T *uc = U + P.cbvoff[c] * nrhs;
-                for (int idx = threadIdx.x; idx < (b - a) * nk; idx += blockDim.x) {
-                    const int i = a + idx % (b - a), k = idx / (b - a);
-                    ys[(rm[i] - r0) * RCH + k] += gsign * uc[i + (int64_t)(k0 + k) * mc];
+            for (int j0 = 0; j0 < nch; j0 += 32) {
+                // offsets of the next 32 children, fetched by warp 0's
+                // lanes together
+                if (threadIdx.x < 32 && j0 + (int)threadIdx.x < nch) {
+                    const int j = j0 + (int)threadIdx.x;
+                    const int c = P.child_list[cb0 + j];
+                    const int ncc = (int)(P.Super[c + 1] - P.Super[c]);
+                    const int64_t pic = P.Pi[c];
+                    c_mc[threadIdx.x] = (int)(P.Pi[c + 1] - pic) - ncc;
+                    c_rm[threadIdx.x] = pic + ncc;
+                    c_u[threadIdx.x] = P.cbvoff[c] * nrhs;
+                    c_a[threadIdx.x] = cr[2 * j];
+                    c_b[threadIdx.x] = cr[2 * j + 1];
                 }
                 __syncthreads();
+                const int nj = min(32, nch - j0);
+                for (int jj = 0; jj < nj; jj++) {
+                    const int a = c_a[jj], b = c_b[jj], mc = c_mc[jj];
+                    const int32_t *rm = P.relmap + c_rm[jj];
+                    const T *uc = U + c_u[jj];
+                    for (int idx = threadIdx.x; idx < (b - a) * nk; idx += blockDim.x) {
+                        const int i = a + idx % (b - a), k = idx / (b - a);
+                        ys[(rm[i] - r0) * RCH + k] += gsign * uc[i + (int64_t)(k0 + k) * mc];
+                    }
+                    __syncthreads();
+                }
             }
             if (tk.kind == 0) {
                 const int i = tk.idx;
@@ -651,6 +676,8 @@ int gb_launch_sweep1(int forward, const gb_pattern_ptrs *pp, const gb_sweep1_arg
     S.ntask_s = a->ntask_s; S.parent = a->parent; S.xready = a->xready; S.done = a->done;
     S.ticket = a->ticket; S.err = a->err; S.trace = a->trace;
     S.gptr = a->gptr; S.ngroups = a->ngroups;
+    S.cptr = a->cptr; S.crange = a->crange;
+    if (forward && (!S.cptr || !S.crange)) return (int)cudaErrorInvalidValue;
     if (grid > a->ngroups) grid = a->ngroups;
     static int configured = 0;
     if (!configured) {

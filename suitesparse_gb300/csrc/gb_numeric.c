@@ -502,6 +502,8 @@ int gb_run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int fo
         a.tasks = forward ? P->d_sf : P->d_sb;
         a.ntasks = (int)(forward ? P->sf_t.n : P->sb_t.n);
         a.gptr = forward ? P->d_gf : P->d_gb;
+        a.cptr = P->d_sf_cptr;
+        a.crange = P->d_sf_crange;
         a.ngroups = (int)(forward ? P->gf.n : P->gb.n) - 1;
         a.blkoff = P->d_blkoff;
         a.linvoff = P->d_linvoff;
@@ -915,6 +917,27 @@ cholmod_dense *gb300_solve(int sys, cholmod_factor *L, cholmod_dense *B,
 /* The factorization task graph of L's plan, 8 int32 per task (type, s, b,
  * r, c, priority, level, 0), for inspecting a factorization trace.  Returns
  * the number of tasks. */
+/* The single-launch sweep's task list of L's plan in ticket order (the
+ * order of gb300_get_trace): 5 int32 per task: s, kind (0 diagonal block,
+ * 1 off-diagonal rows), idx, r0, nr.  Supernodes of leaf subtrees (swept
+ * by one warp each in their own launch) have no tasks.  Returns the count. */
+int gb300_plan_sweep_tasks(cholmod_factor *L, cholmod_common *Common, int forward, int32_t *out,
+                           int64_t nmax)
+{
+    if (!Common || !L) return -1;
+    gb_ctx *ctx = gb_ctx_get(Common, 1);
+    if (!ctx || !gb_ctx_ready(ctx)) return -1;
+    gb_plan *P = gb_plan_get(L, Common, ctx, 1);
+    if (!P) return -1;
+    const gb_vec *v = forward ? &P->sf_t : &P->sb_t;
+    const gb_stask *t = v->p;
+    for (int64_t i = 0; out && i < (int64_t)v->n && i < nmax; i++) {
+        out[5 * i + 0] = t[i].s; out[5 * i + 1] = t[i].kind; out[5 * i + 2] = t[i].idx;
+        out[5 * i + 3] = t[i].r0; out[5 * i + 4] = t[i].nr;
+    }
+    return (int)v->n;
+}
+
 int gb300_plan_tasks(cholmod_factor *L, cholmod_common *Common, int32_t *out, int64_t nmax)
 {
     if (!Common || !L) return -1;

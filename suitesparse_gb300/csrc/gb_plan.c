@@ -474,6 +474,8 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
     vec_init(&P->sb_t, sizeof(gb_stask));
     vec_init(&P->sd_t, sizeof(gb_stask));
     vec_init(&P->lf_t, 2 * sizeof(int32_t));
+    vec_init(&P->sf_cptr, sizeof(int32_t));
+    vec_init(&P->sf_crange, sizeof(int32_t));
     vec_init(&P->fact_seq, sizeof(gb_launch_rec));
     vec_init(&P->dag_t, sizeof(gb_dtask));
     vec_init(&P->dag_sp, sizeof(int32_t));
@@ -995,6 +997,31 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
             q = e;
         }
     }
+    /* forward tasks: each child's update-vector rows that fall in the
+     * task's rows [r0, r0 + nr) (the relative map is increasing), so the
+     * sweep reads a range instead of searching the map on the device */
+    {
+        const gb_stask *tt = P->sf_t.p;
+        int32_t cnt = 0;
+        ok &= gb_vec_push(&P->sf_cptr, &cnt);
+        for (size_t q = 0; ok && q < P->sf_t.n; q++) {
+            const Int s0 = tt[q].s, r0 = tt[q].r0, r1 = tt[q].r0 + tt[q].nr;
+            for (int32_t ci = child_ptr[s0]; ok && ci < child_ptr[s0 + 1]; ci++) {
+                const Int c = child_list[ci], ncc = Super[c + 1] - Super[c];
+                const int32_t *rm = relmap + Pi[c] + ncc;
+                const Int mc = Pi[c + 1] - Pi[c] - ncc;
+                Int lo = 0, hi = mc;
+                while (lo < hi) { Int mid = (lo + hi) / 2; if (rm[mid] < r0) lo = mid + 1; else hi = mid; }
+                const Int a = lo;
+                hi = mc;
+                while (lo < hi) { Int mid = (lo + hi) / 2; if (rm[mid] < r1) lo = mid + 1; else hi = mid; }
+                int32_t ab[2] = {(int32_t)a, (int32_t)lo};
+                ok &= gb_vec_push(&P->sf_crange, &ab[0]) && gb_vec_push(&P->sf_crange, &ab[1]);
+                cnt++;
+            }
+            ok &= gb_vec_push(&P->sf_cptr, &cnt);
+        }
+    }
     free(lcnt); free(lel); free(lmem);
     P->nblk_total = nblk_total;
     P->h_linvoff = malloc(sizeof(int64_t) * (nblk_total + 1));
@@ -1103,6 +1130,8 @@ int gb_plan_upload(gb_plan *P)
     UP(P->d_gb, P->gb.p, P->gb.n * P->gb.esz);
     UP(P->d_sb, P->sb_t.p, P->sb_t.n * P->sb_t.esz);
     UP(P->d_lf, P->lf_t.p, P->lf_t.n * P->lf_t.esz);
+    UP(P->d_sf_cptr, P->sf_cptr.p, P->sf_cptr.n * P->sf_cptr.esz);
+    UP(P->d_sf_crange, P->sf_crange.p, P->sf_crange.n * P->sf_crange.esz);
     UP(P->d_sd, P->sd_t.p, P->sd_t.n * P->sd_t.esz);
     UP(P->d_blkoff, P->h_blkoff, sizeof(int32_t) * (ns + 1));
     UP(P->d_ntask_f, P->h_ntask_f, sizeof(int32_t) * (ns + 1));
@@ -1179,6 +1208,7 @@ void gb_plan_free(gb_plan *P)
     free(P->h_linvoff);
     gb_vec_free(&P->sf_t); gb_vec_free(&P->sb_t); gb_vec_free(&P->sd_t);
     gb_vec_free(&P->lf_t);
+    gb_vec_free(&P->sf_cptr); gb_vec_free(&P->sf_crange);
     gb_vec_free(&P->gf); gb_vec_free(&P->gb);
     gb_vec_free(&P->dag_t); gb_vec_free(&P->dag_sp); gb_vec_free(&P->dag_succ);
     gb_vec_free(&P->dag_nd); gb_vec_free(&P->dag_q0); gb_vec_free(&P->dag_q1);
@@ -1196,7 +1226,7 @@ void gb_plan_free(gb_plan *P)
                    P->d_gemm_owner, P->d_sweep, P->d_Lx[0], P->d_Lx[1], P->d_CB[0],
                    P->d_CB[1], P->d_Sp, P->d_Si, P->d_Sx, P->d_Y, P->d_U, P->d_B,
                    P->d_Rp, P->d_Rj, P->d_Rx, P->d_scale, P->d_scale_perm, P->d_X, P->d_R,
-                   P->d_bx, P->d_red, P->d_sf, P->d_sb, P->d_sd, P->d_lf, P->d_blkoff, P->d_ntask_f,
+                   P->d_bx, P->d_red, P->d_sf, P->d_sb, P->d_sd, P->d_lf, P->d_sf_cptr, P->d_sf_crange, P->d_blkoff, P->d_ntask_f,
                    P->d_ntask_b, P->d_parent, P->d_linvoff, P->d_xready, P->d_done,
                    P->d_ticket, P->d_Linv[0], P->d_Linv[1], P->d_dag_t, P->d_dag_sp,
                    P->d_dag_succ, P->d_dag_nd, P->d_dag_q0i, P->d_dag_q1i, P->d_dag_ctrl0,

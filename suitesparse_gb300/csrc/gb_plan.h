@@ -111,6 +111,9 @@ typedef struct {
     const int32_t *parent;
     int32_t *xready, *done, *ticket, *err;
     unsigned long long *trace;
+    const int32_t *cptr;        /* forward: [ntasks+1] start of each task's child ranges */
+    const int32_t *crange;      /* forward: per task and child (child_list order) the
+                                 * child's update-vector rows [a, b) in the task's rows */
 } gb_sweep1_args;
 
 /* growable host array */
@@ -175,6 +178,8 @@ typedef struct gb_plan {
     gb_vec sf_t, sb_t, sd_t;          /* forward, backward, diagonal-block tasks */
     gb_vec lf_t;                      /* leaf subtrees of the sweeps: (first, root) */
     int32_t *d_lf;
+    gb_vec sf_cptr, sf_crange;        /* forward tasks' child row ranges (gb_sweep1_args) */
+    int32_t *d_sf_cptr, *d_sf_crange;
     int64_t nblk_total, linv_total;
     gb_stask *d_sf, *d_sb, *d_sd;
     gb_vec gf, gb;                    /* sweep task groups (forward, backward) */
