@@ -396,18 +396,30 @@ k_bwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
                 const int r = idx / RCH, k = idx % RCH;
                 ys[idx] = (r < nr && k < nk) ? Y[k1 + r0 + r + (int64_t)(k0 + k) * ldy] : (T)0;
             }
-            // ys -= L21(:, blk i)' x(rows of s), 64 rows at a time
+            // ys -= L21(:, blk i)' x(rows of s), 64 rows at a time: the next
+            // L tile and the next chunk's x (xv: this thread's 4 of the
+            // 64 x 16 entries, a gather through the row indices) are loaded
+            // while a chunk is used
+            T xv[4];
+            auto load_x = [&](int q0) {
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int idx = threadIdx.x + 256 * u, c = idx / RCH, k = idx % RCH;
+                    xv[u] = (q0 + c < m && k < nk) ? Y[rows[q0 + c] + (int64_t)(k0 + k) * ldy] : (T)0;
+                }
+            };
+            if (m > 0) load_x(0);
             for (int q0 = 0; q0 < m; q0 += SR) {
                 const int nq = min(SR, m - q0);
                 tile_park(tA, reg);
-                for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
-                    const int c = idx / RCH, k = idx % RCH;
-                    xs[idx] = (c < nq && k < nk) ? Y[rows[q0 + c] + (int64_t)(k0 + k) * ldy] : (T)0;
-                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) xs[threadIdx.x + 256 * u] = xv[u];
                 __syncthreads();
-                if (q0 + SR < m)
+                if (q0 + SR < m) {
                     tile_fetch(reg, panel + nscol + q0 + SR + (int64_t)r0 * nsrow, nsrow,
                                min(SR, m - q0 - SR), nr);
+                    load_x(q0 + SR);
+                }
                 tile_gemv<T>(tA, 1, nr, nq, xs, ys, nk, (T)-1);
             }
             // later diagonal blocks of s: ys -= L(blk j, blk i)' x_j
