@@ -57,6 +57,11 @@ __device__ __forceinline__ void st_release(int32_t *p, int v)
     asm volatile("st.release.gpu.global.b32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
 }
 
+__device__ __forceinline__ void red_release_add(int32_t *p, int v)
+{
+    asm volatile("red.release.gpu.global.add.s32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
 __device__ __forceinline__ unsigned long long gtimer()
 {
     unsigned long long t;
@@ -69,9 +74,9 @@ __device__ bool wait_ge_n(const int32_t *flag, int target, int32_t *err, long lo
 {
     if (ld_acquire(flag) >= target) return true;
     for (long long it = 0; it < limit; it++) {
-        __nanosleep(64);
+        __nanosleep(32);
         if (ld_acquire(flag) >= target) return true;
-        if (ld_acquire(err)) return false;
+        if ((it & 15) == 15 && ld_acquire(err)) return false;   // another waiter gave up
     }
     atomicExch(err, 1);
     return false;
@@ -339,9 +344,10 @@ k_fwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
             }
         }
         if (threadIdx.x == 0) {
-            __threadfence();
+            // release stores after the block barrier: the block's writes of
+            // x and u are visible to whoever acquires either word
             if (tk.kind == 0) st_release(S.xready + S.blkoff[s] + tk.idx, 1);
-            atomicAdd(S.done + s, 1);
+            red_release_add(S.done + s, 1);
             if (S.trace) S.trace[3 * (size_t)t + 2] = gtimer();
         }
         __syncthreads();
@@ -458,9 +464,8 @@ k_bwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
             __syncthreads();
         }
         if (threadIdx.x == 0) {
-            __threadfence();
             st_release(S.xready + S.blkoff[s] + i, 1);
-            atomicAdd(S.done + s, 1);
+            red_release_add(S.done + s, 1);
             if (S.trace) S.trace[3 * (size_t)t + 2] = gtimer();
         }
         __syncthreads();
