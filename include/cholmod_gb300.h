@@ -346,14 +346,15 @@ int gb300_finish (cholmod_common *Common) ;
  *      nscol nsrow^2 + 1e4 per supernode) is at most this many flops is
  *      factorized whole by one thread block; 0 = never.  A change applies
  *      from the next factorization (the plan is rebuilt).
- *  GB300_OPT_WARP_ROWS [32]: in the one-launch factorization, a supernode
+ *  GB300_OPT_WARP_ROWS [64]: in the one-launch factorization, a supernode
  *      factorized whole (a subtree member, or a small supernode on its own)
- *      whose front has at most this many rows (0-32) is assembled and
+ *      whose front has at most this many rows (0-64) is assembled and
  *      factorized by one warp instead of a whole thread block; the subtree
  *      members run wave by wave (a wave: supernodes of equal height in the
- *      subtree), several one-warp fronts at once.  The factor is the same
- *      bit for bit with every value.  0 = never.  A change applies from the
- *      next factorization (the plan is rebuilt).
+ *      subtree), several one-warp fronts at once (eight of at most 32 rows,
+ *      two of 33-64 rows).  The factor is the same bit for bit with every
+ *      value.  0 = never (and no one-warp leaf subtrees in the sweeps).  A
+ *      change applies from the next factorization (the plan is rebuilt).
  *  GB300_OPT_GRAPH [1]: 1 = gb300_solve_refined replays its refinement
  *      step (permutation, both sweeps, residual, backward error) from a
  *      CUDA graph captured once per pattern, right-hand-side count and

@@ -199,13 +199,14 @@ __device__ void factor_small_body(const gb_dev_pattern &P, int s, T *Lx, T *Linv
 #undef LDT
 
 // ---------------------------------------------------------------------------
-// a front of at most 32 rows, whole, on one warp (lane = front row): its
-// assembly, LL' of the diagonal block, the block's inverse (kept for the
-// sweeps), the panel rows below as products with that inverse, and the
-// update block.  The front stays in the warp's shared region; nothing waits
-// on another warp.  Every value is formed by the same operations in the same
-// order as the block path (assemble_body, factor_small_body and the update-
-// block tile), so the factor is the same bit for bit on either path:
+// a front of at most MAXR (32 or 64) rows, whole, on one warp (rows r = lane,
+// lane + 32): its assembly, LL' of the diagonal block, the block's inverse
+// (kept for the sweeps), the panel rows below as products with that inverse,
+// and the update block.  The front stays in the warp's shared region;
+// nothing waits on another warp.  Every value is formed by the same
+// operations in the same order as the block path (assemble_body,
+// factor_small_body and the update-block tile), so the factor is the same
+// bit for bit on either path:
 //  * the diagonal block is factorized right-looking, which subtracts the
 //    products L(i,k) L(j,k) from A(i,j) in the order k = 0, 1, ... exactly as
 //    the block path's left-looking loop does;
@@ -216,27 +217,26 @@ __device__ void factor_small_body(const gb_dev_pattern &P, int s, T *Lx, T *Linv
 // (t_cholmod_super_numeric_worker.c :1004-1058, :1152-1218, :640-720).
 // ---------------------------------------------------------------------------
 
-#define GB_WF_LD 33
-
-// bytes of one warp's shared region
-template <typename T>
+// bytes of one warp's shared region for fronts of at most MAXR rows
+template <int MAXR, typename T>
 __host__ __device__ constexpr size_t warp_front_smem()
 {
-    return sizeof(T) * (32 * GB_WF_LD + 32) + sizeof(int) * 66;
+    return sizeof(T) * (MAXR * (MAXR + 1) + MAXR) + sizeof(int) * (2 * MAXR + 2);
 }
 
-template <typename TA, typename T>
+template <int MAXR, typename TA, typename T>
 __device__ __noinline__ void warp_front(const gb_dev_pattern &P, int s, const int64_t *__restrict__ Sp,
-                           const int64_t *__restrict__ Si, const TA *__restrict__ Sx,
-                           const double *__restrict__ scale, double beta, T *Lx, T *CB, T *Linv,
-                           unsigned char *wsm)
+                                        const int64_t *__restrict__ Si, const TA *__restrict__ Sx,
+                                        const double *__restrict__ scale, double beta, T *Lx, T *CB,
+                                        T *Linv, unsigned char *wsm)
 {
-    constexpr int LD = GB_WF_LD;
+    static_assert(MAXR == 32 || MAXR == 64, "fronts of 32 or 64 rows");
+    constexpr int LD = MAXR + 1;
     constexpr unsigned FULL = 0xffffffffu;
     T *F = (T *)wsm;                       // front, column-major: F[j*LD + i]
-    T *xd = F + 32 * LD;                   // diagonal of the block inverse
-    int *rows = (int *)(xd + 32);          // front row -> row of L
-    int *spc = rows + 32;                  // A's column starts, relative to Sp[k1]
+    T *xd = F + MAXR * LD;                 // diagonal of the block inverse
+    int *rows = (int *)(xd + MAXR);        // front row -> row of L
+    int *spc = rows + MAXR;                // A's column starts, relative to Sp[k1]
     const int lane = threadIdx.x & 31;
     const int64_t k1 = P.Super[s];
     const int nscol = (int)(P.Super[s + 1] - k1);
@@ -246,8 +246,12 @@ __device__ __noinline__ void warp_front(const gb_dev_pattern &P, int s, const in
     T *panel = Lx + P.Px[s];
 
     // 1. zero the front; row indices; A's column starts
-    for (int j = 0; j < nsrow; j++) F[j * LD + lane] = (T)0;
-    rows[lane] = lane < nsrow ? P.Ls[psi + lane] : 0x7fffffff;
+    for (int j = 0; j < nsrow; j++)
+#pragma unroll
+        for (int h = 0; h < MAXR; h += 32) F[j * LD + lane + h] = (T)0;
+#pragma unroll
+    for (int h = 0; h < MAXR; h += 32)
+        rows[lane + h] = lane + h < nsrow ? P.Ls[psi + lane + h] : 0x7fffffff;
     const int64_t p0 = Sp[k1];
     for (int t = lane; t <= nscol; t += 32) spc[t] = (int)(Sp[k1 + t] - p0);
     __syncwarp();
@@ -293,7 +297,8 @@ __device__ __noinline__ void warp_front(const gb_dev_pattern &P, int s, const in
     }
 
     // 3. extend-add of each child's update block, children in a fixed order
-    // (loads of 8 columns issued before their adds)
+    // (loads of 8 columns issued before their adds; lane holds child rows
+    // lane and lane + 32)
     for (int ci = P.child_ptr[s]; ci < P.child_ptr[s + 1]; ci++) {
         const int c = P.child_list[ci];
         const int ncc = (int)(P.Super[c + 1] - P.Super[c]);
@@ -301,19 +306,31 @@ __device__ __noinline__ void warp_front(const gb_dev_pattern &P, int s, const in
         const int mc = (int)(P.Pi[c + 1] - pic) - ncc;
         const int32_t *rm = P.relmap + pic + ncc;
         const T *cbc = CB + P.cboff[c];
-        const int ri = lane < mc ? rm[lane] : 0;
+        int ri[MAXR / 32];
+#pragma unroll
+        for (int h = 0; h < MAXR / 32; h++) ri[h] = lane + 32 * h < mc ? rm[lane + 32 * h] : 0;
         for (int j0 = 0; j0 < mc; j0 += 8) {
-            T v[8];
+            T v[MAXR / 32][8];
+#pragma unroll
+            for (int h = 0; h < MAXR / 32; h++)
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int j = j0 + u, i = lane + 32 * h;
+                    v[h][u] = (j < mc && i >= j && i < mc) ? cbc[i + (int64_t)j * mc] : (T)0;
+                }
 #pragma unroll
             for (int u = 0; u < 8; u++) {
                 const int j = j0 + u;
-                v[u] = (j < mc && lane >= j && lane < mc) ? cbc[lane + (int64_t)j * mc] : (T)0;
-            }
+                int rj = __shfl_sync(FULL, ri[0], j & 31);
+                if (MAXR == 64) {
+                    const int rj2 = __shfl_sync(FULL, ri[MAXR / 32 - 1], j & 31);
+                    if (j >= 32) rj = rj2;
+                }
 #pragma unroll
-            for (int u = 0; u < 8; u++) {
-                const int j = j0 + u;
-                const int rj = __shfl_sync(FULL, ri, j & 31);
-                if (j < mc && lane >= j && lane < mc) F[rj * LD + ri] += v[u];
+                for (int h = 0; h < MAXR / 32; h++) {
+                    const int i = lane + 32 * h;
+                    if (j < mc && i >= j && i < mc) F[rj * LD + ri[h]] += v[h][u];
+                }
             }
         }
         __syncwarp();
@@ -326,59 +343,79 @@ __device__ __noinline__ void warp_front(const gb_dev_pattern &P, int s, const in
         if (!(d > (T)0)) { fail = k; break; }
         const T lkk = gb_sqrt<T>(d);
         __syncwarp();
-        if (lane == k) F[k * LD + k] = lkk;
-        else if (lane > k && lane < nscol) F[k * LD + lane] = F[k * LD + lane] / lkk;
+#pragma unroll
+        for (int h = 0; h < MAXR; h += 32) {
+            const int r = lane + h;
+            if (r == k) F[k * LD + k] = lkk;
+            else if (r > k && r < nscol) F[k * LD + r] = F[k * LD + r] / lkk;
+        }
         __syncwarp();
-        if (lane > k && lane < nscol) {
-            const T lik = F[k * LD + lane];
-            for (int j = k + 1; j <= lane; j++) F[j * LD + lane] -= lik * F[k * LD + j];
+#pragma unroll
+        for (int h = 0; h < MAXR; h += 32) {
+            const int r = lane + h;
+            if (r > k && r < nscol) {
+                const T lik = F[k * LD + r];
+                for (int j = k + 1; j <= r; j++) F[j * LD + r] -= lik * F[k * LD + j];
+            }
         }
         __syncwarp();
     }
 
-    // 5. X = inverse of the diagonal block, lane j forms column j: X(j,j)
-    // in xd[j], X(i,j) for i > j in the block's upper triangle at F[i*LD + j]
-    if (lane < nscol) {
-        const int j = lane;
-        const T xjj = (T)1 / F[j * LD + j];
-        xd[j] = xjj;
-        for (int i = j + 1; i < nscol; i++) {
-            T acc = (T)0;
-            for (int k = j; k < i; k++) acc += F[k * LD + i] * (k == j ? xjj : F[k * LD + j]);
-            F[i * LD + j] = -acc / F[i * LD + i];
+    // 5. X = inverse of the diagonal block, column j by the lane j mod 32:
+    // X(j,j) in xd[j], X(i,j) for i > j in the block's upper triangle at
+    // F[i*LD + j]
+#pragma unroll
+    for (int h = 0; h < MAXR; h += 32) {
+        const int j = lane + h;
+        if (j < nscol) {
+            const T xjj = (T)1 / F[j * LD + j];
+            xd[j] = xjj;
+            for (int i = j + 1; i < nscol; i++) {
+                T acc = (T)0;
+                for (int k = j; k < i; k++) acc += F[k * LD + i] * (k == j ? xjj : F[k * LD + j]);
+                F[i * LD + j] = -acc / F[i * LD + i];
+            }
         }
     }
     __syncwarp();
     {
         T *out = Linv + P.linvoff[P.blkoff[s]];   // column-major, ld nscol
         for (int j = 0; j < nscol; j++)
-            if (lane < nscol)
-                out[lane + (int64_t)j * nscol] =
-                    lane < j ? (T)0 : (lane == j ? xd[j] : F[lane * LD + j]);
+            for (int r = lane; r < nscol; r += 32)
+                out[r + (int64_t)j * nscol] = r < j ? (T)0 : (r == j ? xd[j] : F[r * LD + j]);
     }
 
     // 6. panel rows below: L21(r,c) = sum_{k<=c} A21(r,k) X(c,k), in place
     // from the last column (A21(r,k), k <= c, is still unchanged)
     const int ncols = fail >= 0 ? fail : nscol;
-    if (lane >= nscol && lane < nsrow) {
-        for (int c = ncols - 1; c >= 0; c--) {
-            T acc = (T)0;
-            for (int k = 0; k <= c; k++) acc += F[k * LD + lane] * (k == c ? xd[c] : F[c * LD + k]);
-            F[c * LD + lane] = acc;
+#pragma unroll
+    for (int h = 0; h < MAXR; h += 32) {
+        const int r = lane + h;
+        if (r >= nscol && r < nsrow) {
+            for (int c = ncols - 1; c >= 0; c--) {
+                T acc = (T)0;
+                for (int k = 0; k <= c; k++) acc += F[k * LD + r] * (k == c ? xd[c] : F[c * LD + k]);
+                F[c * LD + r] = acc;
+            }
         }
     }
     __syncwarp();
 
     // 7. the panel (zero above the diagonal) and the update block
     for (int t = 0; t < nscol; t++)
-        if (lane < nsrow) panel[lane + (int64_t)t * nsrow] = lane < t ? (T)0 : F[t * LD + lane];
+        for (int r = lane; r < nsrow; r += 32)
+            panel[r + (int64_t)t * nsrow] = r < t ? (T)0 : F[t * LD + r];
     T *cb = CB + P.cboff[s];
     for (int j = nscol; j < nsrow; j++) {
-        if (lane >= j && lane < nsrow) {
-            T acc = (T)0;
-            if (fail < 0)
-                for (int k = 0; k < nscol; k++) acc += F[k * LD + lane] * F[k * LD + j];
-            cb[(lane - nscol) + (int64_t)(j - nscol) * m] = F[j * LD + lane] - acc;
+#pragma unroll
+        for (int h = 0; h < MAXR; h += 32) {
+            const int r = lane + h;
+            if (r >= j && r < nsrow) {
+                T acc = (T)0;
+                if (fail < 0)
+                    for (int k = 0; k < nscol; k++) acc += F[k * LD + r] * F[k * LD + j];
+                cb[(r - nscol) + (int64_t)(j - nscol) * m] = F[j * LD + r] - acc;
+            }
         }
     }
     if (fail >= 0 && lane == 0) {
@@ -386,7 +423,5 @@ __device__ __noinline__ void warp_front(const gb_dev_pattern &P, int s, const in
         atomicExch(P.anyfail, 1);
     }
 }
-
-#undef GB_WF_LD
 
 #endif

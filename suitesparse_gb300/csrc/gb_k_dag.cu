@@ -369,7 +369,8 @@ __device__ __forceinline__ int fdag_instance(const gb_fdag_dev &D, int id)
     return lo;
 }
 
-static_assert(8 * warp_front_smem<float>() <= dag_smem<float>(), "one-warp fronts: shared memory");
+static_assert(8 * warp_front_smem<32, float>() <= dag_smem<float>()
+              && 2 * warp_front_smem<64, float>() <= dag_smem<float>(), "one-warp fronts: shared memory");
 
 // shared memory of the tensor-core executor: the tile tasks' space and the
 // two operand stages of gemm_tile_tc, and more than a third of the SM's
@@ -377,7 +378,8 @@ static_assert(8 * warp_front_smem<float>() <= dag_smem<float>(), "one-warp front
 #define GB_FDAG_TC_SMEM (80 * 1024)
 static_assert(GB_FDAG_TC_SMEM >= GB_TC_SMEM && GB_FDAG_TC_SMEM >= (int)dag_smem<float>()
               && 3 * GB_FDAG_TC_SMEM > 228 * 1024, "tensor-core executor: shared memory");
-static_assert(8 * warp_front_smem<double>() <= dag_smem<double>(), "one-warp fronts: shared memory");
+static_assert(8 * warp_front_smem<32, double>() <= dag_smem<double>()
+              && 2 * warp_front_smem<64, double>() <= dag_smem<double>(), "one-warp fronts: shared memory");
 
 template <typename T, bool TC>
 __global__ void __launch_bounds__(256, 2)
@@ -468,32 +470,51 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
             const double *scale = D.scale ? D.scale + I.scale : nullptr;
             const int warp = threadIdx.x >> 5;
             const bool node = tk.type == GB_DT_NODE;
-            int q = 0, w1 = 0, w2 = 1;
+            // a wave [q, w3): fronts of at most 32 rows [q, w1), one warp each,
+            // eight at a time; fronts of at most warp_rows rows [w1, w2), one
+            // warp each in 64-row regions (NW64 at a time); others [w2, w3)
+            constexpr int NW64 = (int)(dag_smem<T>() / warp_front_smem<64, T>());
+            int q = 0, w1 = 0, w2 = 0, w3 = 1;
             if (node) {
-                w1 = (int)(P.Pi[tk.s + 1] - P.Pi[tk.s]) <= PP.warp_rows ? 1 : 0;
+                const int nr = (int)(P.Pi[tk.s + 1] - P.Pi[tk.s]);
+                w1 = nr <= min(PP.warp_rows, 32) ? 1 : 0;
+                w2 = nr <= PP.warp_rows ? 1 : 0;
             }
             while (q < (node ? 1 : tk.r)) {
                 if (!node) {
-                    // wave [q, w2): one-warp fronts [q, w1), then the others
-                    w1 = PP.sub_meta[2 * (tk.b + q)];
-                    w2 = PP.sub_meta[2 * (tk.b + q) + 1];
-                    if (w2 <= q || w2 > tk.r || w1 < q || w1 > w2) {
+                    w1 = PP.sub_meta[3 * (tk.b + q)];
+                    w2 = PP.sub_meta[3 * (tk.b + q) + 1];
+                    w3 = PP.sub_meta[3 * (tk.b + q) + 2];
+                    if (w3 <= q || w3 > tk.r || w1 < q || w1 > w2 || w2 > w3) {
                         if (threadIdx.x == 0) atomicExch(D.Q.err, 1);
                         break;
                     }
                 }
                 for (int i = q + warp; i < w1; i += 8) {
                     const int s = node ? tk.s : PP.sub_list[tk.b + i];
-                    unsigned char *wsm = smem_raw + (size_t)warp * warp_front_smem<T>();
+                    unsigned char *wsm = smem_raw + (size_t)warp * warp_front_smem<32, T>();
                     if (D.a_dtype == 0)
-                        warp_front<double, T>(P, s, PP.Sp, PP.Si, (const double *)D.Sx + I.sx, scale,
-                                              D.beta, Lx, CB, Linv, wsm);
+                        warp_front<32, double, T>(P, s, PP.Sp, PP.Si, (const double *)D.Sx + I.sx, scale,
+                                                  D.beta, Lx, CB, Linv, wsm);
                     else
-                        warp_front<float, T>(P, s, PP.Sp, PP.Si, (const float *)D.Sx + I.sx, scale,
-                                             D.beta, Lx, CB, Linv, wsm);
+                        warp_front<32, float, T>(P, s, PP.Sp, PP.Si, (const float *)D.Sx + I.sx, scale,
+                                                 D.beta, Lx, CB, Linv, wsm);
                 }
                 if (w1 > q) __syncthreads();
-                for (int i = w1; i < w2; i++) {
+                if (warp < NW64) {
+                    for (int i = w1 + warp; i < w2; i += NW64) {
+                        const int s = node ? tk.s : PP.sub_list[tk.b + i];
+                        unsigned char *wsm = smem_raw + (size_t)warp * warp_front_smem<64, T>();
+                        if (D.a_dtype == 0)
+                            warp_front<64, double, T>(P, s, PP.Sp, PP.Si, (const double *)D.Sx + I.sx,
+                                                      scale, D.beta, Lx, CB, Linv, wsm);
+                        else
+                            warp_front<64, float, T>(P, s, PP.Sp, PP.Si, (const float *)D.Sx + I.sx,
+                                                     scale, D.beta, Lx, CB, Linv, wsm);
+                    }
+                }
+                if (w2 > w1) __syncthreads();
+                for (int i = w2; i < w3; i++) {
                     const int s = node ? tk.s : PP.sub_list[tk.b + i];
                     const int nscol = (int)(P.Super[s + 1] - P.Super[s]);
                     const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
@@ -517,7 +538,7 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                             __syncthreads();
                         }
                 }
-                q = w2;
+                q = w3;
             }
         } else {
             dag_tile_task<T>(P, tk, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr);

@@ -76,7 +76,7 @@ typedef struct { int32_t type, s, b, r, c, prio, pad0, pad1; } gb_dtask;
 #define GB_DT_SUBTREE 9
 #define GB_SUBTREE_WORK 4.0e6       /* work estimate per subtree task (flops) */
 #define GB_NODE_MAX_ROWS 256        /* small supernodes fused into NODE tasks */
-#define GB_WARP_ROWS 32             /* fronts at most this tall: one warp each */
+#define GB_WARP_ROWS 64             /* fronts at most this tall: one warp each */
 
 /* control words of one task-graph launch: [0] head0 [1] tail0 [2] head1
  * [3] tail1 [4] blocks started [5] error [6] total0 [7] total1 [8] blocks

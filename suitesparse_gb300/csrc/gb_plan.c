@@ -145,26 +145,32 @@ static int fdag_build(gb_plan *P)
     if (ok) {
         /* members wave by wave: wave h holds the members of height h in the
          * subtree (leaves 0), so every member's children are in earlier
-         * waves; within a wave the fronts of at most warp_rows rows come
-         * first (one warp each), then the others (the whole block each),
-         * each group in ascending order.  key = 2 height + (not one-warp). */
+         * waves; within a wave the fronts of at most 32 rows come first
+         * (one warp each, eight at a time), then those of at most warp_rows
+         * rows (one warp each, 64-row regions), then the others (the whole
+         * block each), each group in ascending order.  key = 3 height +
+         * group. */
         int32_t *fill = malloc(sizeof(int32_t) * (ns + 1)), *lst = malloc(sizeof(int32_t) * (ns + 1));
-        int32_t *key = malloc(sizeof(int32_t) * (ns + 1)), *meta = calloc(2 * (size_t)ns + 2, sizeof(int32_t));
+        int32_t *key = malloc(sizeof(int32_t) * (ns + 1)), *meta = calloc(3 * (size_t)ns + 3, sizeof(int32_t));
         if (!fill || !lst || !key || !meta) ok = 0;
         for (int64_t s = 0; ok && s < ns; s++) key[s] = 0;
         for (int64_t s = 0; ok && s < ns; s++) {       /* children before parents */
             if (sub_root[s] < 0) continue;
             int32_t par = P->h_parent[s];
-            if (par >= 0 && sub_root[par] == sub_root[s] && key[par] < key[s] + 2)
-                key[par] = key[s] + 2;
+            if (par >= 0 && sub_root[par] == sub_root[s] && key[par] < key[s] + 3)
+                key[par] = key[s] + 3;
         }
-        for (int64_t s = 0; ok && s < ns; s++)
-            if (sub_root[s] >= 0 && Pi[s + 1] - Pi[s] > P->warp_rows) key[s] |= 1;
+        const Int tiny = GB_MIN(P->warp_rows, 32);
+        for (int64_t s = 0; ok && s < ns; s++) {
+            if (sub_root[s] < 0) continue;
+            const Int nr = Pi[s + 1] - Pi[s];
+            key[s] += nr <= tiny ? 0 : (nr <= P->warp_rows ? 1 : 2);
+        }
         /* counting sort of each subtree's members by key (stable) */
         int32_t maxkey = 0;
         for (int64_t s = 0; ok && s < ns; s++)
             if (sub_root[s] >= 0 && key[s] > maxkey) maxkey = key[s];
-        int32_t *kcnt = ok ? calloc((size_t)maxkey + 2, sizeof(int32_t)) : NULL;
+        int32_t *kcnt = ok ? calloc((size_t)maxkey + 4, sizeof(int32_t)) : NULL;
         if (!kcnt) ok = 0;
         for (int64_t s = 0; ok && s < ns; s++) fill[s] = 0;
         for (int64_t s = 0; ok && s < ns; s++)          /* members in ascending order */
@@ -174,17 +180,19 @@ static int fdag_build(gb_plan *P)
             const int32_t b = sub_off[r], e = sub_off[r + 1];
             int32_t kmax = 0;
             for (int32_t q = b; q < e; q++) if (key[lst[q]] > kmax) kmax = key[lst[q]];
-            for (int32_t k = 0; k <= kmax + 1; k++) kcnt[k] = 0;
+            const int32_t kend = 3 * (kmax / 3) + 3;      /* keys 0 .. kend-1 */
+            for (int32_t k = 0; k <= kend; k++) kcnt[k] = 0;
             for (int32_t q = b; q < e; q++) kcnt[key[lst[q]] + 1]++;
-            for (int32_t k = 0; k <= kmax; k++) kcnt[k + 1] += kcnt[k];
-            /* wave starts: per wave (key pair 2h, 2h+1) the end of the
-             * one-warp group and the end of the wave, relative to b */
-            for (int32_t h = 0; 2 * h <= kmax; h++) {
-                const int32_t w0 = kcnt[2 * h], w1 = kcnt[2 * h + 1];
-                const int32_t w2 = 2 * h + 2 <= kmax + 1 ? kcnt[2 * h + 2] : e - b;
-                if (w2 > w0) {
-                    meta[2 * (size_t)(b + w0)] = w1;
-                    meta[2 * (size_t)(b + w0) + 1] = w2;
+            for (int32_t k = 0; k < kend; k++) kcnt[k + 1] += kcnt[k];
+            /* wave starts: per wave (keys 3h, 3h+1, 3h+2) the ends of its
+             * three groups, relative to b */
+            for (int32_t h = 0; 3 * h < kend; h++) {
+                const int32_t w0 = kcnt[3 * h], w1 = kcnt[3 * h + 1], w2 = kcnt[3 * h + 2],
+                              w3 = kcnt[3 * h + 3];
+                if (w3 > w0) {
+                    meta[3 * (size_t)(b + w0)] = w1;
+                    meta[3 * (size_t)(b + w0) + 1] = w2;
+                    meta[3 * (size_t)(b + w0) + 2] = w3;
                 }
             }
             for (int32_t q = b; q < e; q++) {
@@ -196,8 +204,7 @@ static int fdag_build(gb_plan *P)
             if (sub_root[s] >= 0) key[fill[s]] = (int32_t)s;
         for (int64_t q = 0; ok && q < sub_off[ns]; q++) {
             ok &= gb_vec_push(&P->fd_sub, &key[q]);
-            ok &= gb_vec_push(&P->fd_smeta, &meta[2 * q]);
-            ok &= gb_vec_push(&P->fd_smeta, &meta[2 * q + 1]);
+            for (int u = 0; u < 3; u++) ok &= gb_vec_push(&P->fd_smeta, &meta[3 * q + u]);
         }
         free(kcnt);
         free(fill);

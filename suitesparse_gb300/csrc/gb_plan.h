@@ -61,9 +61,10 @@ typedef struct {
     const int32_t *succ_ptr, *succ;  /* local successor CSR */
     const int64_t *Sp, *Si;          /* S = tril(PAP') column pointers/indices */
     const int32_t *sub_list;         /* supernodes of the SUBTREE tasks, wave by wave */
-    const int32_t *sub_meta;         /* [2 per sub_list entry] at a wave's first entry:
-                                      * end of its one-warp fronts, end of the wave
-                                      * (both relative to the task's first entry) */
+    const int32_t *sub_meta;         /* [3 per sub_list entry] at a wave's first entry:
+                                      * ends of its fronts of <= 32 rows, of <= warp_rows
+                                      * rows, and of the wave (relative to the task's
+                                      * first entry) */
     int32_t ntasks, warp_rows;       /* fronts with at most warp_rows rows: one warp */
 } gb_fpat;
 

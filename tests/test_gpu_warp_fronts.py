@@ -13,7 +13,8 @@ from suitesparse_gb300 import matrices as M
 
 pytestmark = pytest.mark.gpu
 
-SETTINGS = [(0, 0), (32, 0), (0, 4_000_000), (16, 4_000_000), (32, 4_000_000), (32, 10**9)]
+SETTINGS = [(0, 0), (32, 0), (64, 0), (0, 4_000_000), (16, 4_000_000), (32, 4_000_000),
+            (48, 4_000_000), (64, 4_000_000), (64, 10**9)]
 
 
 def _factor(meta, arrays, name, warp_rows, sub_work, dtype="d"):
