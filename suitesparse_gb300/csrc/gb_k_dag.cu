@@ -395,7 +395,8 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
     }
     __syncthreads();
     if (spoll == 2) return;
-    const int poller = spoll;
+    // spoll: 1 = poller (a bulk block becomes one when the bulk queue is
+    // exhausted, and serves the critical queue until it drains)
     // FP32: tile products on the tensor cores; two TMEM accumulators of 128
     // columns for the block's lifetime (GB_TC_COLS; the launch's shared
     // memory keeps at most 2 blocks per SM: 512 of 512 columns)
@@ -429,7 +430,11 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                 sid = snext;
                 snext = -1;
             } else {
-                sid = dag_pop(D.Q, poller);
+                sid = dag_pop(D.Q, spoll);
+                if (sid == -1 && !spoll) {
+                    spoll = 1;
+                    sid = dag_pop(D.Q, 1);
+                }
             }
             if (sid >= 0) sinst = fdag_instance(D, sid);
         }
@@ -563,7 +568,7 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                 if (dag_add_acq_rel(D.cnt + g, -1) != 1) continue;
                 if (PP.tasks[v].type != GB_DT_JOIN) {
                     const int prio = PP.tasks[v].prio;
-                    if (prio == 0 && poller && atomicCAS(&snext, -1, g) == -1) {
+                    if (prio == 0 && spoll && atomicCAS(&snext, -1, g) == -1) {
                         atomicSub(D.Q.ctrl + 6, 1);     // kept: one less to queue
                         continue;
                     }

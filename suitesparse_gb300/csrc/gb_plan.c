@@ -94,6 +94,16 @@ static int push_launch(gb_vec *seq, int kind, size_t count, size_t off)
  * Joins carry no work and are never queued.  Every task of s follows
  * JA(s), so the front is assembled before any tile task touches it, and the
  * parent's assembly follows every update-block tile of every child. */
+typedef struct { double w; int32_t id; } gb_ready_est;
+
+/* descending work, then ascending task id (a deterministic order) */
+static int ready_est_cmp(const void *a, const void *b)
+{
+    const gb_ready_est *x = a, *y = b;
+    if (x->w != y->w) return x->w > y->w ? -1 : 1;
+    return (x->id > y->id) - (x->id < y->id);
+}
+
 static int fdag_build(gb_plan *P)
 {
     const int64_t ns = P->nsuper;
@@ -374,6 +384,31 @@ static int fdag_build(gb_plan *P)
             }
             if (ft[t].prio == 0) P->fd_total0++; else P->fd_total1++;
             if (nd[t] == 0) ok &= gb_vec_push(ft[t].prio == 0 ? &P->fd_q0 : &P->fd_q1, &id);
+        }
+        /* the bulk tasks ready at the start, largest estimated work first:
+         * a launch whose leaves are large subtrees (a batch of systems) does
+         * not end waiting on one that started last */
+        if (ok && P->fd_q1.n > 1) {
+            const size_t nq = P->fd_q1.n;
+            int32_t *qv = P->fd_q1.p;
+            gb_ready_est *ev = malloc(sizeof(gb_ready_est) * nq);
+            if (!ev) ok = 0;
+            for (size_t q = 0; ok && q < nq; q++) {
+                const gb_dtask *ti = &ft[qv[q]];
+                const int64_t sq = ti->s;
+                const double nc = (double)(Sup[sq + 1] - Sup[sq]), nr = (double)(Pi[sq + 1] - Pi[sq]);
+                double w = 0;
+                if (ti->type == GB_DT_SUBTREE) w = work[sq];
+                else if (ti->type == GB_DT_NODE || ti->type == GB_DT_SMALL) w = nc * nr * nr;
+                else if (ti->type == GB_DT_ASM) w = nr * (double)(ti->r - ti->b);
+                ev[q].w = w;
+                ev[q].id = qv[q];
+            }
+            if (ok) {
+                qsort(ev, nq, sizeof(gb_ready_est), ready_est_cmp);
+                for (size_t q = 0; q < nq; q++) qv[q] = ev[q].id;
+            }
+            free(ev);
         }
     }
 #undef FUSED
