@@ -580,7 +580,13 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                 for (int f = PP.succ_ptr[v]; f < PP.succ_ptr[v + 1]; f++) {
                     const int w = PP.succ[f];
                     const int gw = (int)(I.base + w);
-                    if (dag_add_acq_rel(D.cnt + gw, -1) == 1) dag_push(D.Q, gw, PP.tasks[w].prio);
+                    if (dag_add_acq_rel(D.cnt + gw, -1) != 1) continue;
+                    const int pw = PP.tasks[w].prio;
+                    if (pw == 0 && spoll && atomicCAS(&snext, -1, gw) == -1) {
+                        atomicSub(D.Q.ctrl + 6, 1);     // kept: one less to queue
+                        continue;
+                    }
+                    dag_push(D.Q, gw, pw);
                 }
             }
             __syncwarp();      // snext, set by any lane, is read by thread 0

@@ -554,10 +554,15 @@ k_fwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
                     T x[LF_RC];
 #pragma unroll
                     for (int k = 0; k < LF_RC; k++) x[k] = (T)0;
-                    for (int c = 0; c <= r; c++) {
-                        const T l = li[r + c * nscol];
+                    for (int c0 = 0; c0 <= r; c0 += 8) {
+                        T lv[8];                  // eight loads in flight
 #pragma unroll
-                        for (int k = 0; k < LF_RC; k++) x[k] += l * ys[c * LF_LD + k];
+                        for (int u = 0; u < 8; u++) lv[u] = c0 + u <= r ? li[r + (c0 + u) * nscol] : (T)0;
+#pragma unroll
+                        for (int u = 0; u < 8; u++)
+                            if (c0 + u <= r)
+#pragma unroll
+                                for (int k = 0; k < LF_RC; k++) x[k] += lv[u] * ys[(c0 + u) * LF_LD + k];
                     }
 #pragma unroll
                     for (int k = 0; k < LF_RC; k++)
@@ -571,10 +576,15 @@ k_fwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
                     T u[LF_RC];
 #pragma unroll
                     for (int k = 0; k < LF_RC; k++) u[k] = ys[r * LF_LD + k];
-                    for (int c = 0; c < nscol; c++) {
-                        const T l = panel[r + (int64_t)c * nsrow];
+                    for (int c0 = 0; c0 < nscol; c0 += 8) {
+                        T lv[8];
 #pragma unroll
-                        for (int k = 0; k < LF_RC; k++) u[k] += l * xs[c * LF_LD + k];
+                        for (int q = 0; q < 8; q++) lv[q] = c0 + q < nscol ? panel[r + (int64_t)(c0 + q) * nsrow] : (T)0;
+#pragma unroll
+                        for (int q = 0; q < 8; q++)
+                            if (c0 + q < nscol)
+#pragma unroll
+                                for (int k = 0; k < LF_RC; k++) u[k] += lv[q] * xs[(c0 + q) * LF_LD + k];
                     }
 #pragma unroll
                     for (int k = 0; k < LF_RC; k++)
@@ -619,10 +629,15 @@ k_bwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
                     T y[LF_RC];
 #pragma unroll
                     for (int k = 0; k < LF_RC; k++) y[k] = k < nk ? Y[k1 + r + (int64_t)(k0 + k) * ldy] : (T)0;
-                    for (int q = 0; q < m; q++) {
-                        const T l = panel[nscol + q + (int64_t)r * nsrow];
+                    for (int q0 = 0; q0 < m; q0 += 8) {
+                        T lv[8];
 #pragma unroll
-                        for (int k = 0; k < LF_RC; k++) y[k] -= l * xs[q * LF_LD + k];
+                        for (int u = 0; u < 8; u++) lv[u] = q0 + u < m ? panel[nscol + q0 + u + (int64_t)r * nsrow] : (T)0;
+#pragma unroll
+                        for (int u = 0; u < 8; u++)
+                            if (q0 + u < m)
+#pragma unroll
+                                for (int k = 0; k < LF_RC; k++) y[k] -= lv[u] * xs[(q0 + u) * LF_LD + k];
                     }
 #pragma unroll
                     for (int k = 0; k < LF_RC; k++) ys[r * LF_LD + k] = y[k];
@@ -632,10 +647,15 @@ k_bwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
                     T x[LF_RC];
 #pragma unroll
                     for (int k = 0; k < LF_RC; k++) x[k] = (T)0;
-                    for (int c = r; c < nscol; c++) {
-                        const T l = li[c + r * nscol];
+                    for (int c0 = r; c0 < nscol; c0 += 8) {
+                        T lv[8];
 #pragma unroll
-                        for (int k = 0; k < LF_RC; k++) x[k] += l * ys[c * LF_LD + k];
+                        for (int u = 0; u < 8; u++) lv[u] = c0 + u < nscol ? li[c0 + u + r * nscol] : (T)0;
+#pragma unroll
+                        for (int u = 0; u < 8; u++)
+                            if (c0 + u < nscol)
+#pragma unroll
+                                for (int k = 0; k < LF_RC; k++) x[k] += lv[u] * ys[(c0 + u) * LF_LD + k];
                     }
 #pragma unroll
                     for (int k = 0; k < LF_RC; k++)
