@@ -39,6 +39,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CASE = "c2"
+# DRAM bytes (read + write) of one k_fdag launch on c2, measured by ncu
+# (dram__bytes_read.sum 3.280e9 + dram__bytes_write.sum 5.293e9); the command
+# is in profiles/k_fdag_c2_dram_traffic.md
+K_FDAG_C2_DRAM_BYTES = 3280453632 + 5293096704
 METRIC = "factor TFLOP/s + solves/s at 1e-12 backward err, FP32+IR vs FP64; p50/p99"
 WORKLOAD = "c2: 3D 7-point variable-coefficient Laplacian 64^3 (n=262144), METIS"
 
@@ -385,7 +389,11 @@ def run_gpu(args):
                      "peak": peak32, "unit": "TFLOP/s",
                      "frac": (achieved / peak32) if (achieved and peak32) else None,
                      "peak_source": "measured: FMA-chain probe gb300_fma_peak in this run",
-                     "traffic": None, "share_of_factor_time": g_ms / prof_total,
+                     "traffic": K_FDAG_C2_DRAM_BYTES if CASE == "c2" else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                       "k_fdag launch of this workload "
+                                       "(profiles/k_fdag_c2_dram_traffic.md)",
+                     "share_of_factor_time": g_ms / prof_total,
                      "fp64_fma_peak": peak64},
         "kernel_profile_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
         "plan": info,
