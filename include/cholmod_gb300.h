@@ -323,6 +323,14 @@ int cholmod_l_super_lsolve (cholmod_factor *L, cholmod_dense *X,
 int cholmod_l_super_ltsolve (cholmod_factor *L, cholmod_dense *X,
     cholmod_dense *E, cholmod_common *Common) ;
 
+/* Rough reciprocal condition number of a factor: (min L(j,j) / max
+ * L(j,j))^2 for LL'; 1 for n = 0; 0 when the factorization failed
+ * (L->minor < n) or a diagonal entry is NaN; EMPTY for a missing argument.
+ * Replaces CHOLMOD/Cholesky/cholmod_rcond.c:51-110 (cholmod.h, cholmod_l_rcond);
+ * a factor whose values live on the GPU (GB300_OPT_KEEP_ON_DEVICE) is
+ * reduced there without a copy back. */
+double cholmod_l_rcond (cholmod_factor *L, cholmod_common *Common) ;
+
 /* ======================================================================== *
  * 2. gb300_* extensions.                                                    *
  * ======================================================================== */

@@ -177,16 +177,19 @@ int main(int argc, char **argv)
             free(lx);
         }
     }
+    /* the reference's rough reciprocal condition number of the factor
+     * (cholmod_rcond: (min L(j,j) / max L(j,j))^2 for LL') */
+    double rcond = ok ? cholmod_l_rcond(L, &c) : -1.0;
     snprintf(path, sizeof path, "%s/out_meta.txt", dir);
     FILE *of = fopen(path, "w");
     fprintf(of, "is_super %d\nnsuper %zu\nssize %zu\nxsize %zu\nmaxcsize %zu\n"
                 "maxesize %zu\nfl %.17g\nlnz %.17g\nanz %.17g\nminor %zu\n"
                 "status %d\nfactor_ok %d\nfactor_status %d\nordering %d\n"
                 "t_analyze %.6f\nt_factor %.6f\nt_solve %.6f\nresid %.6e\n"
-                "nthreads %d\n",
+                "nthreads %d\nrcond %.17g\n",
             L->is_super, L->nsuper, L->ssize, L->xsize, L->maxcsize, L->maxesize,
             c.fl, c.lnz, c.anz, L->minor, c.status, ok, fstatus, L->ordering,
-            t_analyze, t_factor, t_solve, resid, c.nthreads_max);
+            t_analyze, t_factor, t_solve, resid, c.nthreads_max, rcond);
     fclose(of);
 
     cholmod_l_free_factor(&L, &c);

@@ -100,6 +100,7 @@ def lib():
         "gb300_get_factor_trace": (C.c_int, [vp, C.POINTER(C.c_ulonglong), C.c_int64]),
         "gb300_plan_tasks": (C.c_int, [FP, vp, C.POINTER(C.c_int32), C.c_int64]),
         "gb300_plan_sweep_tasks": (C.c_int, [FP, vp, C.c_int, C.POINTER(C.c_int32), C.c_int64]),
+        "cholmod_l_rcond": (C.c_double, [FP, vp]),
         "gb300_batch_analyze": (FP, [C.c_int, C.POINTER(FP), C.c_int64, C.POINTER(C.c_int32), vp]),
         "cholmod_l_super_numeric": (C.c_int, [SP, SP, C.POINTER(C.c_double), FP, vp]),
         "cholmod_l_super_lsolve": (C.c_int, [FP, DP, DP, vp]),
@@ -264,6 +265,11 @@ def factor_arrays(L, with_x=True):
         dt = np.float32 if f.dtype == CHOLMOD_SINGLE else np.float64
         out["Lx"] = _arr(f.x, dt, f.xsize).copy()
     return out
+
+
+def rcond(L, common):
+    """cholmod_l_rcond: (min L(j,j) / max L(j,j))^2 of an LL' factor."""
+    return lib().cholmod_l_rcond(L, common.ptr)
 
 
 def free_factor(L, common):

@@ -104,6 +104,49 @@ __global__ void k_diag_minmax(int nsuper, const int64_t *__restrict__ Super,
     }
 }
 
+// range of the factor's diagonal L(j,j) over every supernode: out[0] = min,
+// out[1] = max (bit patterns of the positive values, 64-bit atomics),
+// out[2] = nonzero when an entry is NaN.  out[0], out[1] start at +inf, 0.
+template <typename T>
+__global__ void k_diag_range(int nsuper, const int64_t *__restrict__ Super,
+                             const int64_t *__restrict__ Pi, const int64_t *__restrict__ Px,
+                             const T *__restrict__ Lx, double *out)
+{
+    __shared__ double smin[256], smax[256];
+    __shared__ int snan;
+    if (threadIdx.x == 0) snan = 0;
+    __syncthreads();
+    double lo = __longlong_as_double(0x7FF0000000000000LL), hi = 0.0;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int s = warp; s < nsuper; s += nwarps) {          // one warp per supernode
+        const int nscol = (int)(Super[s + 1] - Super[s]);
+        const int64_t nsrow = Pi[s + 1] - Pi[s];
+        const T *panel = Lx + Px[s];
+        for (int j = lane; j < nscol; j += 32) {
+            const double d = (double)panel[j + j * nsrow];
+            if (d != d) snan = 1;
+            else { lo = fmin(lo, d); hi = fmax(hi, d); }
+        }
+    }
+    smin[threadIdx.x] = lo;
+    smax[threadIdx.x] = hi;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + o]);
+            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        atomicMin((unsigned long long *)&out[0], (unsigned long long)__double_as_longlong(smin[0]));
+        atomicMax((unsigned long long *)&out[1], (unsigned long long)__double_as_longlong(smax[0]));
+        if (snan) out[2] = 1.0;
+    }
+}
+
 // per column r: out[3r] = max|R|, out[3r+1] = max|X|, out[3r+2] = max|B|
 // (out zeroed first); grid-wide, 64-bit atomics on the bit patterns of the
 // nonnegative maxima.
@@ -343,6 +386,19 @@ int gb_launch_diag_minmax(int nsuper, const int64_t *Super, const int64_t *Pi,
     const int g = gb_grid_for(nsuper);
     if (dtype == 0) k_diag_minmax<double><<<g, 256, 0, st>>>(nsuper, Super, Pi, Px, (const double *)Lx, out);
     else k_diag_minmax<float><<<g, 256, 0, st>>>(nsuper, Super, Pi, Px, (const float *)Lx, out);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_diag_range(int nsuper, const int64_t *Super, const int64_t *Pi,
+                         const int64_t *Px, const void *Lx, int dtype, double *out,
+                         cudaStream_t st)
+{
+    if (!out || !Lx || nsuper <= 0) return (int)cudaErrorInvalidValue;
+    k_minmax_init<<<1, 1, 0, st>>>(out);
+    if (cudaMemsetAsync(out + 2, 0, sizeof(double), st) != cudaSuccess) return 1;
+    const int g = gb_grid_for(nsuper);
+    if (dtype == 0) k_diag_range<double><<<g, 256, 0, st>>>(nsuper, Super, Pi, Px, (const double *)Lx, out);
+    else k_diag_range<float><<<g, 256, 0, st>>>(nsuper, Super, Pi, Px, (const float *)Lx, out);
     return (int)cudaGetLastError();
 }
 

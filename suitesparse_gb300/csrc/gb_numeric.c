@@ -972,3 +972,71 @@ int gb300_plan_tasks(cholmod_factor *L, cholmod_common *Common, int32_t *out, in
     }
     return (int)n;
 }
+
+/* Rough reciprocal condition number of a factor, as the reference defines
+ * it (CHOLMOD/Cholesky/cholmod_rcond.c:51-110 and t_cholmod_rcond_worker.c):
+ * (min L(j,j) / max L(j,j))^2 for LL' (for LDL', min |D(j,j)| / max
+ * |D(j,j)|), 1 for n = 0, 0 when the factorization failed (L->minor < n) or
+ * a diagonal entry is NaN, EMPTY for a missing argument.  A supernodal
+ * factor whose current values live on the GPU (a factorization with
+ * GB300_OPT_KEEP_ON_DEVICE) is reduced there; any other factor is read from
+ * L->x on the host, in the reference's order. */
+double cholmod_l_rcond(cholmod_factor *L, cholmod_common *Common)
+{
+    if (!Common) return EMPTY;
+    if (!L) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return EMPTY; }
+    if (L->xtype != CHOLMOD_REAL) { GB_ERROR(CHOLMOD_INVALID, "only real factors"); return EMPTY; }
+    Common->status = CHOLMOD_OK;
+    const Int n = (Int)L->n;
+    if (n == 0) return 1;
+    if ((Int)L->minor < n) return 0;
+    double lmin = 0, lmax = 0;
+    int single = L->dtype == CHOLMOD_SINGLE;
+    if (L->is_super) {
+        gb_ctx *ctx = gb_ctx_get(Common, 0);
+        gb_plan *P = ctx ? gb_plan_get(L, Common, ctx, 0) : NULL;
+        int d = dt_index(L->dtype);
+        if (P && P->dev_valid[d] && P->host_x[d] == L->x && P->d_Lx[d]) {
+            size_t cap = 0;
+            double r[3];
+            int ok = (P->d_red || gb_dev_grow((void **)&P->d_red, &cap, sizeof(double) * 64))
+                     && gb_launch_diag_range((int)P->nsuper, P->d_Super, P->d_Pi, P->d_Px, P->d_Lx[d],
+                                             single ? 4 : 0, P->d_red, ctx->stream) == 0
+                     && cudaMemcpyAsync(r, P->d_red, sizeof r, cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess
+                     && cudaStreamSynchronize(ctx->stream) == cudaSuccess;
+            if (!ok) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error"); return EMPTY; }
+            if (r[2] != 0) return 0;
+            lmin = r[0];
+            lmax = r[1];
+        } else {
+            if (!L->x) { GB_ERROR(CHOLMOD_INVALID, "L has no numerical values"); return EMPTY; }
+            const Int *Super = L->super, *Pi = L->pi, *Px = L->px;
+            for (Int s = 0; s < (Int)L->nsuper; s++) {
+                const Int nscol = Super[s + 1] - Super[s], nsrow = Pi[s + 1] - Pi[s];
+                for (Int j = 0; j < nscol; j++) {
+                    const Int q = Px[s] + j + j * nsrow;
+                    const double v = single ? (double)((const float *)L->x)[q] : ((const double *)L->x)[q];
+                    if (v != v) return 0;
+                    if (s == 0 && j == 0) { lmin = lmax = v; }
+                    else if (v < lmin) lmin = v;
+                    else if (v > lmax) lmax = v;
+                }
+            }
+        }
+    } else {
+        /* simplicial factor (produced elsewhere): diagonal at L->x[Lp[j]] */
+        const Int *Lp = L->p;
+        if (!Lp || !L->x) { GB_ERROR(CHOLMOD_INVALID, "L has no numerical values"); return EMPTY; }
+        for (Int j = 0; j < n; j++) {
+            double v = single ? (double)((const float *)L->x)[Lp[j]] : ((const double *)L->x)[Lp[j]];
+            if (!L->is_ll) v = fabs(v);
+            if (v != v) return 0;
+            if (j == 0) { lmin = lmax = v; }
+            else if (v < lmin) lmin = v;
+            else if (v > lmax) lmax = v;
+        }
+    }
+    double rcond = lmin / lmax;
+    if (L->is_ll) rcond = rcond * rcond;
+    return rcond;
+}

@@ -344,6 +344,9 @@ int gb_launch_anorm_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t nseg
 int gb_launch_colmax3_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t nseg, int nrhs,
                           const double *R, int64_t ldr, const double *X, int64_t ldx,
                           const double *B, int64_t ldb, double *out, cudaStream_t st);
+int gb_launch_diag_range(int nsuper, const int64_t *Super, const int64_t *Pi,
+                         const int64_t *Px, const void *Lx, int dtype, double *out,
+                         cudaStream_t st);
 int gb_launch_diag_minmax(int nsuper, const int64_t *Super, const int64_t *Pi,
                           const int64_t *Px, const void *Lx, int dtype, double *out,
                           cudaStream_t st);
