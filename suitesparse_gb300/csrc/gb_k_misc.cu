@@ -12,14 +12,16 @@ __global__ void k_perm_in(int64_t n, int nrhs, const int64_t *__restrict__ perm,
                           const double *__restrict__ scale, const TB *__restrict__ B,
                           int64_t ldb, TY *Y, int64_t ldy)
 {
-    const int64_t total = n * nrhs;
-    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t k = idx % n, r = idx / n;
+    // one thread per row k, every column (the index and scale read once)
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = perm ? perm[k] : k;
-        double v = (double)B[i + r * ldb];
-        if (scale) v *= scale[i];
-        Y[k + r * ldy] = (TY)v;
+        const double sc = scale ? scale[i] : 1.0;
+        for (int r = 0; r < nrhs; r++) {
+            double v = (double)B[i + r * ldb];
+            if (scale) v *= sc;
+            Y[k + r * ldy] = (TY)v;
+        }
     }
 }
 
@@ -29,33 +31,47 @@ __global__ void k_perm_out(int64_t n, int nrhs, const int64_t *__restrict__ perm
                            const double *__restrict__ scale, const TY *__restrict__ Y,
                            int64_t ldy, TX *X, int64_t ldx, int add)
 {
-    const int64_t total = n * nrhs;
-    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t k = idx % n, r = idx / n;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = perm ? perm[k] : k;
-        double v = (double)Y[k + r * ldy];
-        if (scale) v *= scale[i];
-        if (add) X[i + r * ldx] += (TX)v;
-        else X[i + r * ldx] = (TX)v;
+        const double sc = scale ? scale[i] : 1.0;
+        for (int r = 0; r < nrhs; r++) {
+            double v = (double)Y[k + r * ldy];
+            if (scale) v *= sc;
+            if (add) X[i + r * ldx] += (TX)v;
+            else X[i + r * ldx] = (TX)v;
+        }
     }
 }
 
-// R = B - A X with A in full compressed-row form (both triangles), FP64,
-// one thread per (row, column of X), sequential sum: fixed order.
+// R = B - A X with A in full compressed-row form (both triangles), FP64:
+// one thread per row, up to four columns of X per pass so that each entry
+// of A is read once per four right-hand sides; every sum runs over the row
+// in order (a fixed order, the same for any number of columns).
 __global__ void k_residual(int64_t n, int nrhs, const int64_t *__restrict__ Rp,
                            const int32_t *__restrict__ Rj, const double *__restrict__ Rx,
                            const double *__restrict__ X, int64_t ldx,
                            const double *__restrict__ B, int64_t ldb,
                            double *R, int64_t ldr)
 {
-    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < n * nrhs;
-         w += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = w % n, r = w / n;
-        const double *x = X + r * ldx;
-        double acc = 0.0;
-        for (int64_t p = Rp[i]; p < Rp[i + 1]; p++) acc += Rx[p] * x[Rj[p]];
-        R[i + r * ldr] = B[i + r * ldb] - acc;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p0 = Rp[i], p1 = Rp[i + 1];
+        for (int r0 = 0; r0 < nrhs; r0 += 4) {
+            const int nk = min(4, nrhs - r0);
+            const double *x = X + r0 * ldx;
+            double acc[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int64_t p = p0; p < p1; p++) {
+                const double a = Rx[p];
+                const int64_t j = Rj[p];
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (u < nk) acc[u] += a * x[j + u * ldx];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (u < nk) R[i + (r0 + u) * ldr] = B[i + (r0 + u) * ldb] - acc[u];
+        }
     }
 }
 
@@ -340,7 +356,7 @@ int gb_launch_perm_in(int64_t n, int nrhs, const int64_t *perm, const double *sc
                       const void *B, int b_dtype, int64_t ldb, void *Y, int y_dtype,
                       int64_t ldy, cudaStream_t st)
 {
-    int g = gb_grid_for(n * nrhs);
+    int g = gb_grid_for(n);
     if (b_dtype == 0 && y_dtype == 0)
         k_perm_in<double, double><<<g, 256, 0, st>>>(n, nrhs, perm, scale, (const double *)B, ldb, (double *)Y, ldy);
     else if (b_dtype == 0 && y_dtype == 4)
@@ -356,7 +372,7 @@ int gb_launch_perm_out(int64_t n, int nrhs, const int64_t *perm, const double *s
                        const void *Y, int y_dtype, int64_t ldy, void *X, int x_dtype,
                        int64_t ldx, int add, cudaStream_t st)
 {
-    int g = gb_grid_for(n * nrhs);
+    int g = gb_grid_for(n);
     if (y_dtype == 0 && x_dtype == 0)
         k_perm_out<double, double><<<g, 256, 0, st>>>(n, nrhs, perm, scale, (const double *)Y, ldy, (double *)X, ldx, add);
     else if (y_dtype == 4 && x_dtype == 0)
@@ -372,7 +388,7 @@ int gb_launch_residual(int64_t n, int nrhs, const int64_t *Rp, const int32_t *Rj
                        const double *Rx, const double *X, int64_t ldx, const double *B,
                        int64_t ldb, double *R, int64_t ldr, cudaStream_t st)
 {
-    int g = gb_grid_for(n * nrhs);
+    int g = gb_grid_for(n);
     k_residual<<<g, 256, 0, st>>>(n, nrhs, Rp, Rj, Rx, X, ldx, B, ldb, R, ldr);
     return (int)cudaGetLastError();
 }
