@@ -331,6 +331,20 @@ int cholmod_l_super_ltsolve (cholmod_factor *L, cholmod_dense *X,
  * reduced there without a copy back. */
 double cholmod_l_rcond (cholmod_factor *L, cholmod_common *Common) ;
 
+/* Sparse right-hand side: X = A\B (or the system sys names, as in
+ * cholmod_l_solve) for a sparse B, X returned sparse: the entries of the
+ * dense solution that are not zero (NaN kept), rows ascending, packed and
+ * sorted, nzmax = nnz(X) (at least 1); free with gb300_free_sparse.
+ * Replaces CHOLMOD/Cholesky/cholmod_spsolve.c:56-278 (cholmod.h,
+ * cholmod_l_spsolve), same argument checks (B unsymmetric, L->n ==
+ * B->nrow, equal dtypes) and result.  L must be a real supernodal LL'
+ * factor; B real, packed or not (for a row index given twice in a column
+ * the last entry counts, as in the reference); a row index outside
+ * [0, n) is CHOLMOD_INVALID.  Up to 64 columns per GPU pass, of which only
+ * the nonzero entries are copied back. */
+cholmod_sparse *cholmod_l_spsolve (int sys, cholmod_factor *L,
+    cholmod_sparse *B, cholmod_common *Common) ;
+
 /* ======================================================================== *
  * 2. gb300_* extensions.                                                    *
  * ======================================================================== */
@@ -417,7 +431,12 @@ int gb300_factorize (cholmod_sparse *A, double beta [2], cholmod_factor *L,
 
 /* X = A\B through L: Y = P*B, cholmod_l_super_lsolve, cholmod_l_super_ltsolve,
  * X = P'*Y (the supernodal branch of cholmod_l_solve2,
- * CHOLMOD/Cholesky/cholmod_solve.c:656-724).  sys must be CHOLMOD_A.
+ * CHOLMOD/Cholesky/cholmod_solve.c:656-724).  The other sys values as
+ * there: P*B and P'*B for CHOLMOD_P / CHOLMOD_Pt; the lower sweep alone
+ * for CHOLMOD_L / CHOLMOD_LD, the upper alone for CHOLMOD_Lt / CHOLMOD_DLt,
+ * both for CHOLMOD_LDLt, none for CHOLMOD_D, all of these without the
+ * permutation (the reference applies L->Perm only for A, P and Pt,
+ * cholmod_solve.c:262-267).
  * Returns a new dense X (free with gb300_free_dense) or NULL. */
 cholmod_dense *gb300_solve (int sys, cholmod_factor *L, cholmod_dense *B,
     cholmod_common *Common) ;

@@ -161,6 +161,54 @@ def solve(sym, Lx, perm, B, dtype="d", use_blas=True):
     return X
 
 
+def solve_sys(sym, Lx, perm, B, sys, natural=False, dtype="d", use_blas=True):
+    """cholmod_l_solve's sys values for a supernodal LL' factor
+    (CHOLMOD/Cholesky/cholmod_solve.c): the permutation only for sys = A (0),
+    P (7), Pt (8) and an ordering other than natural (:262-267); P: X = P*B,
+    Pt: X = P'*B (:616-650); otherwise Y = P*B, the lower sweep for A, LDLt,
+    LD, L (0, 1, 2, 4), the upper for A, LDLt, DLt, Lt (0, 1, 3, 5), and
+    X = P'*Y (:689-722); D (6) is the identity for LL'."""
+    B = np.asarray(B)
+    if B.ndim == 1:
+        B = B[:, None]
+    perm = np.asarray(perm, np.int64)
+    use = sys in (0, 7, 8) and not natural
+    Y = B[perm, :] if use and sys in (0, 7) else np.array(B, copy=True)
+    if sys in (0, 1, 2, 4):
+        Y = sweep(sym, Lx, Y, True, dtype, use_blas)
+    if sys in (0, 1, 3, 5):
+        Y = sweep(sym, Lx, Y, False, dtype, use_blas)
+    if use and sys in (0, 8):
+        X = np.empty_like(Y)
+        X[perm, :] = Y
+        return X
+    return Y
+
+
+def spsolve(sym, Lx, perm, n, Bp, Bi, Bx, sys=0, natural=False, dtype="d", use_blas=True):
+    """cholmod_l_spsolve (CHOLMOD/Cholesky/cholmod_spsolve.c:56-278): B is
+    scattered into a dense block (for a repeated row the last entry counts,
+    the scatter worker of t_cholmod_spsolve_worker.c), solved with
+    solve_sys, and each column's entries x != 0 (a NaN kept) appended in
+    row order; returns (Xp, Xi, Xx) with nnz(X) = Xp[-1]."""
+    ncol = len(Bp) - 1
+    rt = np.float32 if dtype == "s" else np.float64
+    Bd = np.zeros((n, ncol), rt)
+    for j in range(ncol):
+        for p in range(int(Bp[j]), int(Bp[j + 1])):
+            Bd[int(Bi[p]), j] = Bx[p]
+    X = solve_sys(sym, Lx, perm, Bd, sys, natural, dtype, use_blas)
+    Xp = np.zeros(ncol + 1, np.int64)
+    Xi, Xx = [], []
+    for j in range(ncol):
+        rows = np.nonzero(X[:, j] != 0)[0]
+        Xi.append(rows)
+        Xx.append(X[rows, j])
+        Xp[j + 1] = Xp[j] + len(rows)
+    cat = (lambda a, t: np.concatenate(a).astype(t) if a else np.zeros(0, t))
+    return Xp, cat(Xi, np.int64), cat(Xx, rt)
+
+
 def backward_error(n, Ap, Ai, Ax, X, B):
     """|b - A x|_inf / (|A|_inf |x|_inf + |b|_inf) per column (A lower-stored
     symmetric), the measure of CHOLMOD/Demo/cholmod_di_demo.c:614-617."""

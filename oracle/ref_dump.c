@@ -72,8 +72,8 @@ int main(int argc, char **argv)
     snprintf(path, sizeof path, "%s/meta.txt", dir);
     FILE *mf = fopen(path, "r");
     if (!mf) { perror(path); return 2; }
-    long n, nnz, nrhs = 0;
-    if (fscanf(mf, "%ld %ld %ld", &n, &nnz, &nrhs) < 2) { fclose(mf); return 2; }
+    long n, nnz, nrhs = 0, sncol = 0;
+    if (fscanf(mf, "%ld %ld %ld %ld", &n, &nnz, &nrhs, &sncol) < 2) { fclose(mf); return 2; }
     fclose(mf);
 
     int64_t *Ap = read_file(dir, "Ap.bin", NULL);
@@ -158,6 +158,39 @@ int main(int argc, char **argv)
         cholmod_l_free_dense(&B, &c);
     }
 
+    /* sparse right-hand side (SBp/SBi/SBx.bin, sncol columns, double):
+     * cholmod_l_spsolve for every sys, X written as SX<sys>{p,i,x}.bin */
+    long spnz[9] = {0};
+    int64_t *SBp = sncol > 0 ? read_file(dir, "SBp.bin", NULL) : NULL;
+    int64_t *SBi = SBp ? read_file(dir, "SBi.bin", NULL) : NULL;
+    double *SBx = SBp ? read_file(dir, "SBx.bin", NULL) : NULL;
+    if (SBp && !single && L->is_super && L->minor == (size_t)n) {
+        long bnz = SBp[sncol];
+        cholmod_sparse *SB = cholmod_l_allocate_sparse(n, sncol, bnz > 0 ? bnz : 1, 0, 1, 0,
+                                                       CHOLMOD_REAL + CHOLMOD_DOUBLE, &c);
+        memcpy(SB->p, SBp, (sncol + 1) * sizeof(int64_t));
+        if (bnz > 0) {
+            memcpy(SB->i, SBi, bnz * sizeof(int64_t));
+            memcpy(SB->x, SBx, bnz * sizeof(double));
+        }
+        for (int sys = 0; sys <= 8; sys++) {
+            cholmod_sparse *X = cholmod_l_spsolve(sys, L, SB, &c);
+            if (!X) { spnz[sys] = -1; continue; }
+            int64_t *xp = X->p;
+            char name[64];
+            snprintf(name, sizeof name, "SX%dp.bin", sys);
+            write_file(dir, name, xp, (sncol + 1) * sizeof(int64_t));
+            snprintf(name, sizeof name, "SX%di.bin", sys);
+            write_file(dir, name, X->i, xp[sncol] * sizeof(int64_t));
+            snprintf(name, sizeof name, "SX%dx.bin", sys);
+            write_file(dir, name, X->x, xp[sncol] * sizeof(double));
+            spnz[sys] = (long)X->nzmax;
+            cholmod_l_free_sparse(&X, &c);
+        }
+        cholmod_l_free_sparse(&SB, &c);
+    }
+    free(SBp); free(SBi); free(SBx);
+
     write_file(dir, "Perm.bin", L->Perm, n * sizeof(int64_t));
     write_file(dir, "ColCount.bin", L->ColCount, n * sizeof(int64_t));
     if (L->is_super) {
@@ -186,10 +219,12 @@ int main(int argc, char **argv)
                 "maxesize %zu\nfl %.17g\nlnz %.17g\nanz %.17g\nminor %zu\n"
                 "status %d\nfactor_ok %d\nfactor_status %d\nordering %d\n"
                 "t_analyze %.6f\nt_factor %.6f\nt_solve %.6f\nresid %.6e\n"
-                "nthreads %d\nrcond %.17g\n",
+                "nthreads %d\nrcond %.17g\n"
+                "spnzmax %ld,%ld,%ld,%ld,%ld,%ld,%ld,%ld,%ld\n",
             L->is_super, L->nsuper, L->ssize, L->xsize, L->maxcsize, L->maxesize,
             c.fl, c.lnz, c.anz, L->minor, c.status, ok, fstatus, L->ordering,
-            t_analyze, t_factor, t_solve, resid, c.nthreads_max, rcond);
+            t_analyze, t_factor, t_solve, resid, c.nthreads_max, rcond,
+            spnz[0], spnz[1], spnz[2], spnz[3], spnz[4], spnz[5], spnz[6], spnz[7], spnz[8]);
     fclose(of);
 
     cholmod_l_free_factor(&L, &c);

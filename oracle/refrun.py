@@ -19,12 +19,18 @@ def available():
 
 
 def run(n, Ap, Ai, Ax, ordering="amd", dtype="d", B=None, perm=None, trials=1,
-        env=None):
-    """Analyze + factorize (+ solve if B) with the reference; returns a dict."""
+        env=None, SB=None):
+    """Analyze + factorize (+ solve if B) with the reference; returns a dict.
+    SB = (Bp, Bi, Bx) of a sparse right-hand side: out["SX"][sys] =
+    (Xp, Xi, Xx, nzmax) of cholmod_l_spsolve(sys) for sys = 0..8."""
     with tempfile.TemporaryDirectory() as d:
         nrhs = 0 if B is None else (1 if B.ndim == 1 else B.shape[1])
+        sncol = 0 if SB is None else len(SB[0]) - 1
         with open(os.path.join(d, "meta.txt"), "w") as f:
-            f.write(f"{n} {len(Ai)} {nrhs}\n")
+            f.write(f"{n} {len(Ai)} {nrhs} {sncol}\n")
+        if SB is not None:
+            for name, a, dt in zip(("SBp", "SBi", "SBx"), SB, (np.int64, np.int64, np.float64)):
+                np.asarray(a, dt).tofile(os.path.join(d, name + ".bin"))
         np.asarray(Ap, np.int64).tofile(os.path.join(d, "Ap.bin"))
         np.asarray(Ai, np.int64).tofile(os.path.join(d, "Ai.bin"))
         np.asarray(Ax, np.float64).tofile(os.path.join(d, "Ax.bin"))
@@ -39,7 +45,10 @@ def run(n, Ap, Ai, Ax, ordering="amd", dtype="d", B=None, perm=None, trials=1,
         with open(os.path.join(d, "out_meta.txt")) as f:
             for line in f:
                 k, v = line.split()
-                out[k] = float(v) if any(c in v for c in ".e") else int(v)
+                if "," in v:
+                    out[k] = [int(t) for t in v.split(",")]
+                else:
+                    out[k] = float(v) if any(c in v for c in ".e") else int(v)
 
         def rd(name, dt):
             p = os.path.join(d, name)
@@ -48,6 +57,13 @@ def run(n, Ap, Ai, Ax, ordering="amd", dtype="d", B=None, perm=None, trials=1,
         for name in ("Perm", "ColCount", "Super", "Pi", "Px", "Ls"):
             out[name] = rd(name + ".bin", np.int64)
         out["Lx"] = rd("Lx.bin", np.float64)
+        if sncol:
+            out["SX"] = {}
+            for sys in range(9):
+                xp = rd(f"SX{sys}p.bin", np.int64)
+                if xp is not None:
+                    out["SX"][sys] = (xp, rd(f"SX{sys}i.bin", np.int64),
+                                      rd(f"SX{sys}x.bin", np.float64), out["spnzmax"][sys])
         X = rd("X.bin", np.float64)
         if X is not None:
             out["X"] = X.reshape(-1, n).T.copy()

@@ -20,7 +20,8 @@ CHOLMOD_DOUBLE, CHOLMOD_SINGLE = 0, 4
 CHOLMOD_OK, CHOLMOD_NOT_INSTALLED, CHOLMOD_OUT_OF_MEMORY = 0, -1, -2
 CHOLMOD_TOO_LARGE, CHOLMOD_INVALID, CHOLMOD_GPU_PROBLEM = -3, -4, -5
 CHOLMOD_NOT_POSDEF, CHOLMOD_DSMALL = 1, 2
-CHOLMOD_A = 0
+CHOLMOD_A, CHOLMOD_LDLt, CHOLMOD_LD, CHOLMOD_DLt, CHOLMOD_L = 0, 1, 2, 3, 4
+CHOLMOD_Lt, CHOLMOD_D, CHOLMOD_P, CHOLMOD_Pt = 5, 6, 7, 8
 GB300_OPT_KEEP_ON_DEVICE, GB300_OPT_SMALL_COLS, GB300_OPT_PROFILE, GB300_OPT_SWEEP = 1, 2, 3, 4
 GB300_OPT_TRACE, GB300_OPT_FACTOR, GB300_OPT_TENSOR = 5, 6, 7
 GB300_OPT_SUBTREE_WORK = 8
@@ -101,6 +102,7 @@ def lib():
         "gb300_plan_tasks": (C.c_int, [FP, vp, C.POINTER(C.c_int32), C.c_int64]),
         "gb300_plan_sweep_tasks": (C.c_int, [FP, vp, C.c_int, C.POINTER(C.c_int32), C.c_int64]),
         "cholmod_l_rcond": (C.c_double, [FP, vp]),
+        "cholmod_l_spsolve": (SP, [C.c_int, FP, SP, vp]),
         "gb300_batch_analyze": (FP, [C.c_int, C.POINTER(FP), C.c_int64, C.POINTER(C.c_int32), vp]),
         "cholmod_l_super_numeric": (C.c_int, [SP, SP, C.POINTER(C.c_double), FP, vp]),
         "cholmod_l_super_lsolve": (C.c_int, [FP, DP, DP, vp]),
@@ -286,9 +288,34 @@ def factorize(A, L, common, beta=0.0):
     return lib().gb300_factorize(A, b, L, common.ptr)
 
 
-def solve(L, B, common, dtype="d"):
+def sparse_arrays(A):
+    """numpy copies (p, i, x) of a packed cholmod_sparse."""
+    a = A.contents
+    nz = int(_arr(a.p, np.int64, a.ncol + 1)[a.ncol]) if a.ncol >= 0 else 0
+    dt = np.float32 if a.dtype == CHOLMOD_SINGLE else np.float64
+    return (_arr(a.p, np.int64, a.ncol + 1).copy(), _arr(a.i, np.int64, nz).copy(),
+            _arr(a.x, dt, nz).copy())
+
+
+def spsolve(L, n, Bp, Bi, Bx, common, sys=None, dtype="d"):
+    """cholmod_l_spsolve: X = A\\B for a sparse B given in CSC form; returns
+    (Xp, Xi, Xx, nzmax) of the sparse solution."""
+    sys = CHOLMOD_A if sys is None else sys
+    ncol = len(Bp) - 1
+    B = sparse(n, Bp, Bi, Bx, common, stype=0, dtype=dtype, ncol=ncol)
+    X = lib().cholmod_l_spsolve(sys, L, B, common.ptr)
+    free_sparse(B, common)
+    if not X:
+        raise RuntimeError(f"spsolve failed, status {common.status}")
+    out = sparse_arrays(X) + (int(X.contents.nzmax),)
+    free_sparse(X, common)
+    return out
+
+
+def solve(L, B, common, dtype="d", sys=None):
+    sys = CHOLMOD_A if sys is None else sys
     Bd = dense(B, common, dtype)
-    X = lib().gb300_solve(CHOLMOD_A, L, Bd, common.ptr)
+    X = lib().gb300_solve(sys, L, Bd, common.ptr)
     free_dense(Bd, common)
     if not X:
         raise RuntimeError(f"solve failed, status {common.status}")

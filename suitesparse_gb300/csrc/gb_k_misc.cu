@@ -329,6 +329,94 @@ __global__ void __launch_bounds__(256) k_fma_peak(int iters, T seed, T *out)
     if (s == (T)-12345.0) out[0] = s;     // keeps the chains live
 }
 
+// ---------------------------------------------------------------------------
+// sparse right-hand sides and sparse solutions (cholmod_l_spsolve)
+// ---------------------------------------------------------------------------
+
+// Y(Bi[p], j) = Bx[p] for the packed columns 0 <= j < ncol of a chunk of B
+// (Bp relative to the chunk); Y is zero on entry and the host has removed
+// duplicate row indices, so no two lanes write one entry.  One warp per
+// column; rows outside [0, n) are skipped.
+template <typename T>
+__global__ void k_sp_scatter(int64_t n, int64_t ncol, const int64_t *__restrict__ Bp,
+                             const int64_t *__restrict__ Bi, const T *__restrict__ Bx, T *Y,
+                             int64_t ldy)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t j = warp; j < ncol; j += nwarps) {
+        T *y = Y + j * ldy;
+        for (int64_t p = Bp[j] + lane; p < Bp[j + 1]; p += 32) {
+            const int64_t i = Bi[p];
+            if (i >= 0 && i < n) y[i] = Bx[p];
+        }
+    }
+}
+
+// cnt[j * nseg + s] = number of entries x != 0 (a NaN counts) in rows
+// s*GB_SP_SEG .. (s+1)*GB_SP_SEG-1 of column j of X.  Block (s, j), 256
+// threads.
+#define GB_SP_SEG 4096
+template <typename T>
+__global__ void __launch_bounds__(256) k_sp_count(int64_t n, int64_t nseg,
+                                                  const T *__restrict__ X, int64_t ldx,
+                                                  int64_t *cnt)
+{
+    __shared__ int w[8];
+    const int64_t s = blockIdx.x, j = blockIdx.y;
+    const int64_t r0 = s * GB_SP_SEG, r1 = r0 + GB_SP_SEG < n ? r0 + GB_SP_SEG : n;
+    const T *x = X + j * ldx;
+    int c = 0;
+    for (int64_t i = r0 + threadIdx.x; i < r1; i += 256) c += x[i] != (T)0;
+    c = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int k = 0; k < 8; k++) t += w[k];
+        cnt[j * nseg + s] = t;
+    }
+}
+
+// The nonzero entries of segment s of column j of X, rows ascending, to
+// Xi/Xx starting at off[j * nseg + s].  Block (s, j), 256 threads: per tile
+// of 256 rows a ballot per warp and a prefix over the 8 warp counts.
+template <typename T>
+__global__ void __launch_bounds__(256) k_sp_compact(int64_t n, int64_t nseg,
+                                                    const T *__restrict__ X, int64_t ldx,
+                                                    const int64_t *__restrict__ off,
+                                                    int64_t *Xi, T *Xx)
+{
+    __shared__ int w[8];
+    const int64_t s = blockIdx.x, j = blockIdx.y;
+    const int64_t r0 = s * GB_SP_SEG, r1 = r0 + GB_SP_SEG < n ? r0 + GB_SP_SEG : n;
+    const T *x = X + j * ldx;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int64_t base = off[j * nseg + s];
+    for (int64_t t0 = r0; t0 < r1; t0 += 256) {
+        const int64_t i = t0 + threadIdx.x;
+        const T v = i < r1 ? x[i] : (T)0;
+        const bool nz = i < r1 && v != (T)0;
+        const unsigned b = __ballot_sync(0xffffffffu, nz);
+        if (lane == 0) w[wid] = __popc(b);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int k = 0; k < 8; k++) {
+            const int c = w[k];
+            before += k < wid ? c : 0;
+            total += c;
+        }
+        if (nz) {
+            const int64_t q = base + before + __popc(b & ((1u << lane) - 1u));
+            Xi[q] = i;
+            Xx[q] = v;
+        }
+        base += total;
+        __syncthreads();
+    }
+}
+
 extern "C" {
 
 int gb_launch_fma_peak(int dtype, int iters, int blocks, float *ms, cudaStream_t st)
@@ -381,6 +469,42 @@ int gb_launch_perm_out(int64_t n, int nrhs, const int64_t *perm, const double *s
         k_perm_out<float, float><<<g, 256, 0, st>>>(n, nrhs, perm, scale, (const float *)Y, ldy, (float *)X, ldx, add);
     else
         k_perm_out<double, float><<<g, 256, 0, st>>>(n, nrhs, perm, scale, (const double *)Y, ldy, (float *)X, ldx, add);
+    return (int)cudaGetLastError();
+}
+
+// dtype: 0 double, 4 single
+int gb_launch_sp_scatter(int64_t n, int64_t ncol, const int64_t *Bp, const int64_t *Bi,
+                         const void *Bx, int dtype, void *Y, int64_t ldy, cudaStream_t st)
+{
+    int g = gb_grid_for(ncol * 32);
+    if (dtype == 4) k_sp_scatter<float><<<g, 256, 0, st>>>(n, ncol, Bp, Bi, (const float *)Bx, (float *)Y, ldy);
+    else k_sp_scatter<double><<<g, 256, 0, st>>>(n, ncol, Bp, Bi, (const double *)Bx, (double *)Y, ldy);
+    return (int)cudaGetLastError();
+}
+
+int64_t gb_sp_nseg(int64_t n) { return (n + GB_SP_SEG - 1) / GB_SP_SEG; }
+
+int gb_launch_sp_count(int64_t n, int64_t ncol, const void *X, int dtype, int64_t ldx,
+                       int64_t *cnt, cudaStream_t st)
+{
+    const int64_t nseg = gb_sp_nseg(n);
+    if (nseg == 0 || ncol == 0) return 0;
+    if (nseg > 0x7fffffff || ncol > 65535) return (int)cudaErrorInvalidValue;
+    dim3 g((unsigned)nseg, (unsigned)ncol);
+    if (dtype == 4) k_sp_count<float><<<g, 256, 0, st>>>(n, nseg, (const float *)X, ldx, cnt);
+    else k_sp_count<double><<<g, 256, 0, st>>>(n, nseg, (const double *)X, ldx, cnt);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_sp_compact(int64_t n, int64_t ncol, const void *X, int dtype, int64_t ldx,
+                         const int64_t *off, int64_t *Xi, void *Xx, cudaStream_t st)
+{
+    const int64_t nseg = gb_sp_nseg(n);
+    if (nseg == 0 || ncol == 0) return 0;
+    if (nseg > 0x7fffffff || ncol > 65535) return (int)cudaErrorInvalidValue;
+    dim3 g((unsigned)nseg, (unsigned)ncol);
+    if (dtype == 4) k_sp_compact<float><<<g, 256, 0, st>>>(n, nseg, (const float *)X, ldx, off, Xi, (float *)Xx);
+    else k_sp_compact<double><<<g, 256, 0, st>>>(n, nseg, (const double *)X, ldx, off, Xi, (double *)Xx);
     return (int)cudaGetLastError();
 }
 

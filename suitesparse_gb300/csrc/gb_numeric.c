@@ -867,12 +867,39 @@ int gb300_factorize(cholmod_sparse *A, double beta[2], cholmod_factor *L,
     return ok;
 }
 
+/* X = op(B) on the device for the sys values of cholmod_l_solve with a
+ * supernodal LL' factor: the permutation only for sys = A, P, Pt and an
+ * ordering other than natural (CHOLMOD/Cholesky/cholmod_solve.c:262-267);
+ * sys = P is X = P*B and Pt is X = P'*B (:616-650); every other sys is
+ * X = P'*(op(L) \ (P*B)) with lsolve for A, LDLt, LD, L and ltsolve for A,
+ * LDLt, DLt, Lt (:689-722), D = I.  B and X share P->d_B (n x nrhs,
+ * leading dimension n); P->d_Y is the workspace.  *swept = 1 when a sweep
+ * ran. */
+static int gb_solve_dev(int sys, cholmod_factor *L, gb_plan *P, gb_ctx *ctx, int nrhs,
+                        int *swept)
+{
+    Int n = P->n;
+    int dt = L->dtype == CHOLMOD_SINGLE ? 4 : 0;
+    cudaStream_t st = ctx->stream;
+    const int64_t *perm = L->ordering != CHOLMOD_NATURAL ? P->d_Perm : NULL;
+    const int64_t *pin = (sys == CHOLMOD_A || sys == CHOLMOD_P) ? perm : NULL;
+    const int64_t *pout = (sys == CHOLMOD_A || sys == CHOLMOD_Pt) ? perm : NULL;
+    int fwd = sys == CHOLMOD_A || sys == CHOLMOD_LDLt || sys == CHOLMOD_LD || sys == CHOLMOD_L;
+    int bwd = sys == CHOLMOD_A || sys == CHOLMOD_LDLt || sys == CHOLMOD_DLt || sys == CHOLMOD_Lt;
+    *swept = fwd || bwd;
+    int ok = gb_launch_perm_in(n, nrhs, pin, NULL, P->d_B, dt, n, P->d_Y, dt, n, st) == 0;
+    ok = ok && (!fwd || gb_run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, 1));
+    ok = ok && (!bwd || gb_run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, 0));
+    ok = ok && gb_launch_perm_out(n, nrhs, pout, NULL, P->d_Y, dt, n, P->d_B, dt, n, 0, st) == 0;
+    return ok;
+}
+
 cholmod_dense *gb300_solve(int sys, cholmod_factor *L, cholmod_dense *B,
                            cholmod_common *Common)
 {
     if (!Common) return NULL;
     if (!L || !B) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return NULL; }
-    if (sys != CHOLMOD_A) { GB_ERROR(CHOLMOD_INVALID, "only sys = CHOLMOD_A is supported"); return NULL; }
+    if (sys < CHOLMOD_A || sys > CHOLMOD_Pt) { GB_ERROR(CHOLMOD_INVALID, "invalid system"); return NULL; }
     if (L->xtype != CHOLMOD_REAL || !L->is_super || B->xtype != CHOLMOD_REAL
         || B->nrow != L->n || B->dtype != L->dtype) {
         GB_ERROR(CHOLMOD_INVALID, "invalid L or B");
@@ -886,23 +913,20 @@ cholmod_dense *gb300_solve(int sys, cholmod_factor *L, cholmod_dense *B,
     int nrhs = (int)B->ncol;
     Int n = P->n;
     size_t e = dt_size(L->dtype);
-    int dt = L->dtype == CHOLMOD_SINGLE ? 4 : 0;
     cholmod_dense *X = gb300_allocate_dense(n, nrhs, n, CHOLMOD_REAL + L->dtype, Common);
     if (!X) return NULL;
     if (n == 0 || nrhs == 0) return X;
     cudaStream_t st = ctx->stream;
+    int swept = 0;
     int ok = gb_dev_grow(&P->d_Y, &P->y_cap, e * n * nrhs) && gb_dev_grow(&P->d_B, &P->b_cap, e * n * nrhs);
     ok = ok && cudaMemcpy2DAsync(P->d_B, e * n, B->x, e * B->d, e * n, nrhs,
                                  cudaMemcpyHostToDevice, st) == cudaSuccess;
     cudaEventRecord(ctx->ev0, st);
-    ok = ok && gb_launch_perm_in(n, nrhs, P->d_Perm, NULL, P->d_B, dt, n, P->d_Y, dt, n, st) == 0;
-    ok = ok && gb_run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, 1);
-    ok = ok && gb_run_sweep(P, ctx, L->dtype, nrhs, P->d_Y, 0);
-    ok = ok && gb_launch_perm_out(n, nrhs, P->d_Perm, NULL, P->d_Y, dt, n, P->d_B, dt, n, 0, st) == 0;
+    ok = ok && gb_solve_dev(sys, L, P, ctx, nrhs, &swept);
     cudaEventRecord(ctx->ev1, st);
     ok = ok && cudaMemcpyAsync(X->x, P->d_B, e * n * nrhs, cudaMemcpyDeviceToHost, st) == cudaSuccess;
     ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
-    ok = ok && !(ctx->sweep_mode == 1 && sweep_failed(P));
+    ok = ok && !(swept && ctx->sweep_mode == 1 && sweep_failed(P));
     if (!ok) {
         gb300_free_dense(&X, Common);
         GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the solve");
@@ -911,6 +935,163 @@ cholmod_dense *gb300_solve(int sys, cholmod_factor *L, cholmod_dense *B,
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     ctx->stats[1] = ms;
+    return X;
+}
+
+/* ---- cholmod_l_spsolve ------------------------------------------------------ */
+
+#define GB_SP_CHUNK 64                /* right-hand-side columns per device pass */
+
+static size_t sp_align(size_t b) { return (b + 255) & ~(size_t)255; }
+
+/* X = A\B (or the other sys) for a sparse B, returned sparse
+ * (CHOLMOD/Cholesky/cholmod_spsolve.c:56-278): the same argument checks and
+ * result, X(:,j) holding the entries of the dense solution that are not zero
+ * (x != 0; NaN kept), rows ascending, X packed and sorted with nzmax = nnz(X)
+ * (at least 1).  Where the reference solves 4 columns at a time through
+ * cholmod_l_solve, this solves up to 64 per pass on the GPU: the host packs
+ * the chunk of B (for a duplicated row index the last entry wins, as in the
+ * reference's scatter), the device scatters it into a dense block, solves,
+ * counts the nonzeros of every 4096-row segment of every column and compacts
+ * them; only the counts and the compacted entries come back. */
+cholmod_sparse *cholmod_l_spsolve(int sys, cholmod_factor *L, cholmod_sparse *B,
+                                  cholmod_common *Common)
+{
+    if (!Common) return NULL;
+    if (!L || !B) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return NULL; }
+    if (L->xtype != CHOLMOD_REAL || B->xtype != CHOLMOD_REAL) {
+        GB_ERROR(CHOLMOD_INVALID, "L and B must be real");
+        return NULL;
+    }
+    if (L->n != B->nrow) { GB_ERROR(CHOLMOD_INVALID, "dimensions of L and B do not match"); return NULL; }
+    if (B->stype) { GB_ERROR(CHOLMOD_INVALID, "B cannot be stored in symmetric mode"); return NULL; }
+    if (L->dtype != B->dtype) { GB_ERROR(CHOLMOD_INVALID, "dtype of L and B must match"); return NULL; }
+    if (sys < CHOLMOD_A || sys > CHOLMOD_Pt) { GB_ERROR(CHOLMOD_INVALID, "invalid system"); return NULL; }
+    if (!L->is_super) { GB_ERROR(CHOLMOD_INVALID, "L must be supernodal"); return NULL; }
+    Common->status = CHOLMOD_OK;
+    const Int n = (Int)L->n, nrhs = (Int)B->ncol;
+    const Int *Bp = B->p, *Bi = B->i, *Bnz = B->nz;
+    const int packed = B->packed;
+    const size_t e = dt_size(L->dtype);
+    const int dt = L->dtype == CHOLMOD_SINGLE ? 4 : 0;
+    for (Int j = 0; j < nrhs; j++) {
+        Int p0 = Bp[j], p1 = packed ? Bp[j + 1] : p0 + Bnz[j];
+        for (Int p = p0; p < p1; p++)
+            if (Bi[p] < 0 || Bi[p] >= n) { GB_ERROR(CHOLMOD_INVALID, "B row index out of range"); return NULL; }
+    }
+    gb_ctx *ctx = gb_ctx_get(Common, 1);
+    if (!ctx || !gb_ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return NULL; }
+    gb_plan *P = factor_on_device(L, ctx, Common);
+    if (!P) return NULL;
+
+    const Int ch = GB_MIN(GB_MAX(nrhs, 1), GB_SP_CHUNK);
+    const int64_t nseg = gb_sp_nseg(n);
+    /* host staging: packed chunk of B, counts/offsets, growable X entries */
+    Int *cp = malloc(sizeof(Int) * (ch + 1)), *cnt = malloc(sizeof(Int) * (nseg * ch + 1));
+    Int *mark = malloc(sizeof(Int) * (n + 1));
+    Int *Xp = calloc(nrhs + 1, sizeof(Int));
+    size_t bcap = 1024, xcap = 1024, xnz = 0;
+    Int *ci = malloc(sizeof(Int) * bcap), *Xi = malloc(sizeof(Int) * xcap);
+    char *cx = malloc(e * bcap), *Xx = malloc(e * xcap);
+    int ok = cp && cnt && mark && Xp && ci && Xi && cx && Xx, oom = !ok;
+    for (Int i = 0; ok && i < n; i++) mark[i] = -1;
+    cudaStream_t st = ctx->stream;
+    int swept = 0;
+    for (Int j0 = 0; ok && n > 0 && j0 < nrhs; j0 += ch) {
+        const Int j1 = GB_MIN(nrhs, j0 + ch), w = j1 - j0;
+        /* pack B(:, j0:j1-1), the last of duplicated rows kept */
+        size_t bnz = 0;
+        for (Int j = j0; j < j1; j++) bnz += (size_t)(packed ? Bp[j + 1] - Bp[j] : Bnz[j]);
+        if (bnz > bcap) {
+            bcap = bnz;
+            Int *ni = realloc(ci, sizeof(Int) * bcap);
+            char *nx = ni ? realloc(cx, e * bcap) : NULL;
+            if (ni) ci = ni;
+            if (nx) cx = nx;
+            if (!ni || !nx) { ok = 0; oom = 1; break; }
+        }
+        size_t q = 0;
+        for (Int j = j0; j < j1; j++) {
+            cp[j - j0] = (Int)q;
+            Int p0 = Bp[j], p1 = packed ? Bp[j + 1] : p0 + Bnz[j];
+            for (Int p = p1 - 1; p >= p0; p--) {
+                if (mark[Bi[p]] == j) continue;
+                mark[Bi[p]] = j;
+                ci[q] = Bi[p];
+                memcpy(cx + e * q, (const char *)B->x + e * p, e);
+                q++;
+            }
+        }
+        cp[w] = (Int)q;
+        /* device scratch: cp, ci, cx, counts/offsets, X rows, X values */
+        size_t o_cp = 0, o_ci = o_cp + sp_align(sizeof(Int) * (w + 1));
+        size_t o_cx = o_ci + sp_align(sizeof(Int) * GB_MAX(q, 1));
+        size_t o_cn = o_cx + sp_align(e * GB_MAX(q, 1));
+        size_t o_xi = o_cn + sp_align(sizeof(Int) * (nseg * w + 1));
+        size_t o_xx = o_xi + sp_align(sizeof(Int) * n * w);
+        size_t tot = o_xx + sp_align(e * n * w);
+        ok = gb_dev_grow(&P->d_Y, &P->y_cap, e * n * w) && gb_dev_grow(&P->d_B, &P->b_cap, e * n * w)
+             && gb_dev_grow(&P->d_spw, &P->spw_cap, tot);
+        if (!ok) break;
+        char *base = (char *)P->d_spw;
+        Int *d_cp = (Int *)(base + o_cp), *d_ci = (Int *)(base + o_ci), *d_cn = (Int *)(base + o_cn);
+        Int *d_xi = (Int *)(base + o_xi);
+        void *d_cx = base + o_cx, *d_xx = base + o_xx;
+        ok = cudaMemcpyAsync(d_cp, cp, sizeof(Int) * (w + 1), cudaMemcpyHostToDevice, st) == cudaSuccess
+             && (q == 0 || (cudaMemcpyAsync(d_ci, ci, sizeof(Int) * q, cudaMemcpyHostToDevice, st) == cudaSuccess
+                            && cudaMemcpyAsync(d_cx, cx, e * q, cudaMemcpyHostToDevice, st) == cudaSuccess))
+             && cudaMemsetAsync(P->d_B, 0, e * n * w, st) == cudaSuccess
+             && gb_launch_sp_scatter(n, w, d_cp, d_ci, d_cx, dt, P->d_B, n, st) == 0
+             && gb_solve_dev(sys, L, P, ctx, (int)w, &swept)
+             && gb_launch_sp_count(n, w, P->d_B, dt, n, d_cn, st) == 0
+             && cudaMemcpyAsync(cnt, d_cn, sizeof(Int) * nseg * w, cudaMemcpyDeviceToHost, st) == cudaSuccess
+             && cudaStreamSynchronize(st) == cudaSuccess
+             && !(swept && ctx->sweep_mode == 1 && sweep_failed(P));
+        if (!ok) break;
+        /* offsets of every (column, segment) within the chunk, columns first */
+        size_t c = 0;
+        for (Int j = 0; j < w; j++) {
+            Xp[j0 + j] = (Int)(xnz + c);
+            for (int64_t s = 0; s < nseg; s++) {
+                size_t k = (size_t)cnt[j * nseg + s];
+                cnt[j * nseg + s] = (Int)c;
+                c += k;
+            }
+        }
+        if (xnz + c > xcap) {
+            size_t ncap = GB_MAX(xnz + c, 2 * xcap);
+            Int *ni = realloc(Xi, sizeof(Int) * ncap);
+            char *nx = ni ? realloc(Xx, e * ncap) : NULL;
+            if (ni) Xi = ni;
+            if (nx) Xx = nx;
+            if (!ni || !nx) { ok = 0; oom = 1; break; }
+            xcap = ncap;
+        }
+        ok = c == 0
+             || (cudaMemcpyAsync(d_cn, cnt, sizeof(Int) * nseg * w, cudaMemcpyHostToDevice, st) == cudaSuccess
+                 && gb_launch_sp_compact(n, w, P->d_B, dt, n, d_cn, d_xi, d_xx, st) == 0
+                 && cudaMemcpyAsync(Xi + xnz, d_xi, sizeof(Int) * c, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                 && cudaMemcpyAsync(Xx + e * xnz, d_xx, e * c, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                 && cudaStreamSynchronize(st) == cudaSuccess);
+        xnz += c;
+    }
+    cholmod_sparse *X = NULL;
+    if (ok) {
+        Xp[nrhs] = (Int)xnz;
+        X = gb300_allocate_sparse(n, nrhs, GB_MAX(xnz, 1), TRUE, TRUE, 0, CHOLMOD_REAL + L->dtype, Common);
+        if (X) {
+            memcpy(X->p, Xp, sizeof(Int) * (nrhs + 1));
+            if (xnz) {
+                memcpy(X->i, Xi, sizeof(Int) * xnz);
+                memcpy(X->x, Xx, e * xnz);
+            }
+        }
+    } else if (oom) {
+        GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "out of memory");
+    } else {
+        GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the sparse solve");
+    }
+    free(cp); free(cnt); free(mark); free(Xp); free(ci); free(Xi); free(cx); free(Xx);
     return X;
 }
 

@@ -204,6 +204,8 @@ typedef struct gb_plan {
     size_t sx_cap, si_cap, sp_cap;
     void *d_Y, *d_U, *d_B;
     size_t y_cap, u_cap, b_cap;
+    void *d_spw;                      /* cholmod_l_spsolve: B chunk, counts, X chunk */
+    size_t spw_cap;
 
     /* full (both triangles) FP64 copy of A for residuals, plus scaling */
     int64_t *d_Rp;
@@ -330,6 +332,13 @@ int gb_launch_perm_in(int64_t n, int nrhs, const int64_t *perm, const double *sc
 int gb_launch_perm_out(int64_t n, int nrhs, const int64_t *perm, const double *scale,
                        const void *Y, int y_dtype, int64_t ldy, void *X, int x_dtype,
                        int64_t ldx, int add, cudaStream_t st);
+int gb_launch_sp_scatter(int64_t n, int64_t ncol, const int64_t *Bp, const int64_t *Bi,
+                         const void *Bx, int dtype, void *Y, int64_t ldy, cudaStream_t st);
+int64_t gb_sp_nseg(int64_t n);
+int gb_launch_sp_count(int64_t n, int64_t ncol, const void *X, int dtype, int64_t ldx,
+                       int64_t *cnt, cudaStream_t st);
+int gb_launch_sp_compact(int64_t n, int64_t ncol, const void *X, int dtype, int64_t ldx,
+                         const int64_t *off, int64_t *Xi, void *Xx, cudaStream_t st);
 int gb_launch_residual(int64_t n, int nrhs, const int64_t *Rp, const int32_t *Rj,
                        const double *Rx, const double *X, int64_t ldx, const double *B,
                        int64_t ldb, double *R, int64_t ldr, cudaStream_t st);
