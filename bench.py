@@ -567,6 +567,140 @@ def run_serve(args):
     return 0
 
 
+def measured_hbm_peak():
+    """The measured copy bandwidth of the GB300s (GB/s), else the
+    fallback figure of one earlier GB300 measurement."""
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
+
+
+def run_spsolve(args):
+    """sp: cholmod_l_spsolve on the c2 FP64 factor kept on the GPU.  A step is
+    one call with 64 sparse right-hand sides (unit vectors e_k at seeded
+    distinct rows: 64 columns of inv(A)), B and X sparse in host memory, so
+    the one measured form is the C-ABI call itself (host in, host out).
+    Roofline: with 64 columns the FP64 sweeps are bound by the FP64 FMA pipe
+    (2 x sum over supernodes of nscol^2 + 2 (nsrow - nscol) nscol flops per
+    column, over the device time of the call's pass).  CPU baseline: the oracle's spsolve (the
+    reference's 4-column dense blocks through its supernodal sweeps over
+    OpenBLAS) on 8 of the same columns, also the parity check."""
+    ws, rank, dist = dist_setup()
+    from suitesparse_gb300 import cholmod as CH
+    from oracle import oracle as O
+    gold, mat, perm = load_case("c2")
+    n, Ap, Ai, Ax = mat
+    c = CH.Common()
+    c.set_option(CH.GB300_OPT_KEEP_ON_DEVICE, 1)
+    A = CH.sparse(n, Ap, Ai, Ax, c)
+    L = CH.analyze_perm(A, perm, c)
+    assert CH.factorize(A, L, c) == 1 and c.status == CH.CHOLMOD_OK
+    xsize = int(L.contents.xsize)
+    ncol = 64
+    nsteps = args.warmup + args.steps
+    rng = np.random.default_rng(3)
+    rows = rng.choice(n, ncol * nsteps, replace=False).astype(np.int64)
+    Bp = np.arange(ncol + 1, dtype=np.int64)
+    Bs = [CH.sparse(n, Bp, rows[k * ncol:(k + 1) * ncol], np.ones(ncol), c, stype=0, ncol=ncol)
+          for k in range(nsteps)]
+    lib = CH.lib()
+    wall, dev, nnzx, first = [], [], [], None
+    l0 = None
+    with Clocks(0) as clk:
+        for k in range(nsteps):
+            if k == args.warmup:
+                barrier(dist)
+                l0 = c.stats()[5]
+            t0 = time.perf_counter()
+            X = lib.cholmod_l_spsolve(CH.CHOLMOD_A, L, Bs[k], c.ptr)
+            t1 = time.perf_counter()
+            assert X, c.status
+            if k >= args.warmup:
+                wall.append(t1 - t0)
+                dev.append(c.stats()[1])
+                nnzx.append(int(CH.sparse_arrays(X)[0][-1]))
+                if first is None:
+                    first = CH.sparse_arrays(X)
+            CH.free_sparse(X, c)
+    launches = int(c.stats()[5] - l0)
+    barrier(dist)
+    t_call = max_over_ranks(dist, statistics.mean(wall))
+    value = ncol / t_call * ws
+    f = CH.factor_arrays(L, with_x=False)
+    # CPU baseline and parity: the oracle on 8 of the first timed step's columns
+    O.build()
+    O.lib(use_blas=True)
+    threads = os.cpu_count() or 1
+    O.blas_threads(threads)
+    sym = {k: f[k] for k in ("Super", "Pi", "Px", "Ls")}
+    sym["n"] = n
+    Sp, Si, Sx = O.permute_lower(n, Ap, Ai, Ax, perm)
+    st, minor, Lx = O.factor(sym, Sp, Si, Sx, use_blas=True)
+    sample = rows[args.warmup * ncol:args.warmup * ncol + 8]
+    t0 = time.perf_counter()
+    outs = [O.spsolve(sym, Lx, perm, n, np.arange(5, dtype=np.int64), sample[b:b + 4],
+                      np.ones(4), 0) for b in (0, 4)]
+    t_cpu = time.perf_counter() - t0
+    Xp, Xi, Xx = first
+    err = 0.0
+    same_pattern = True
+    for b, (op, oi, ox) in enumerate(outs):
+        for j in range(4):
+            jj = 4 * b + j
+            gi, gx = Xi[Xp[jj]:Xp[jj + 1]], Xx[Xp[jj]:Xp[jj + 1]]
+            wi, wx = oi[op[j]:op[j + 1]], ox[op[j]:op[j + 1]]
+            same_pattern &= bool(np.array_equal(gi, wi))
+            if len(gi) == len(wi):
+                err = max(err, float(np.abs(gx - wx).max() / np.abs(wx).max()))
+    dev_ms = statistics.mean(dev)
+    # per column and sweep: the diagonal triangle (nscol^2 flops) and the
+    # off-diagonal rows (2 (nsrow - nscol) nscol) of every supernode
+    nscol = np.diff(f["Super"]).astype(np.float64)
+    nsrow = np.diff(f["Pi"]).astype(np.float64)
+    fl_col = float(np.sum(nscol * nscol + 2.0 * (nsrow - nscol) * nscol))
+    alg_flops = 2 * fl_col * ncol
+    peak64 = CH.fma_peak("d")
+    achieved = alg_flops / (dev_ms * 1e-3) / 1e12
+    alg_bytes = 2 * 8 * xsize * -(-ncol // 16)
+    line = {
+        "metric": "spsolve columns/s (sparse B and X, c2 FP64 factor on the GPU); p50/p99",
+        "value": value, "unit": "columns/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_call, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "sp: c2 64^3 variable-coefficient Laplacian (n=262144, METIS), "
+                               "FP64 factor resident; 64 unit-vector columns per call",
+                   "columns_per_call": ncol, "l2": "factor (1.1 GB) larger than L2"},
+        "p50_ms": 1e3 * statistics.median(wall),
+        "p99_ms": 1e3 * float(np.percentile(wall, 99)),
+        "device_ms_per_call": dev_ms, "nnz_x_per_column": statistics.mean(nnzx) / ncol,
+        "parity_vs_oracle": {"columns": 8, "same_pattern": same_pattern,
+                             "max_rel_diff": err},
+        "e2e": {"value": value, "unit": "columns/s",
+                "h2d_bytes_per_step": 8 * (ncol + 1) + 16 * ncol,
+                "d2h_bytes_per_step": int(16 * statistics.mean(nnzx)),
+                "note": "the API takes and returns host buffers: value is this call"},
+        "roofline": {"kernel": "k_fwd_sweep + k_bwd_sweep + leaf sweeps (one pass of 64 "
+                               "columns: 2 sweeps x 4 groups of 16 columns)",
+                     "bound": "compute (FP64 FMA pipe)", "achieved": achieved, "peak": peak64,
+                     "unit": "TFLOP/s", "frac": achieved / peak64 if peak64 else None,
+                     "peak_source": "measured: FMA-chain probe gb300_fma_peak in this run",
+                     "algorithmic_flops": alg_flops, "traffic": None,
+                     "hbm_gbs": alg_bytes / (dev_ms * 1e-3) / 1e9,
+                     "hbm_note": "the factor is read once per 16-column group per sweep "
+                                 "(algorithmic bytes 2 x 8 x xsize x 4); hbm_gbs of the "
+                                 "measured %.0f GB/s" % measured_hbm_peak()},
+        "gpu_launches": launches, "clocks": clk.summary(),
+        "cpu_baseline": {"value": 8 / t_cpu, "unit": "columns/s", "cores": threads,
+                         "kind": "port",
+                         "sample": "8 of the same columns in two 4-column blocks (the "
+                                   "reference's block), oracle sweeps over OpenBLAS"},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -575,7 +709,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--case", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "p40"],
+    ap.add_argument("--case", default="c2",
+                    choices=["c1", "c2", "c3", "c4", "c5", "p40", "sp"],
                     help="workload (c2 is the benchmark configuration; c1/c3 for profiling)")
     ap.add_argument("--quick", action="store_true",
                     help="mixed-form steps only (no FP64 form, solve sweep, roofline, CPU leg)")
@@ -592,6 +727,8 @@ def main():
         return run_batch(args)
     if CASE == "c5":
         return run_serve(args)
+    if CASE == "sp":
+        return run_spsolve(args)
     return run_gpu(args)
 
 

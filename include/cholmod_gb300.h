@@ -518,7 +518,8 @@ int gb300_factor_info (cholmod_factor *L, cholmod_common *Common, double *out, i
 int gb300_fma_peak (int dtype, double *tflops) ;
 
 /* Last device-side timings of this library for Common (milliseconds, CUDA
- * events on the library's stream): [0] factor, [1] last solve sweep pair,
+ * events on the library's stream): [0] factor, [1] last solve sweep pair
+ * (for cholmod_l_spsolve: its passes' scatter, solve and count, summed),
  * [2] refined solve total, [3] assembly, [4] kernel launches of the last
  * factorization (count), [5] kernel launches issued through Common so far. */
 int gb300_get_stats (cholmod_common *Common, double *out, int nout) ;

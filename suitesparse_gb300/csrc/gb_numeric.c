@@ -997,6 +997,7 @@ cholmod_sparse *cholmod_l_spsolve(int sys, cholmod_factor *L, cholmod_sparse *B,
     for (Int i = 0; ok && i < n; i++) mark[i] = -1;
     cudaStream_t st = ctx->stream;
     int swept = 0;
+    double dev_ms = 0;                /* device time of the passes (events) */
     for (Int j0 = 0; ok && n > 0 && j0 < nrhs; j0 += ch) {
         const Int j1 = GB_MIN(nrhs, j0 + ch), w = j1 - j0;
         /* pack B(:, j0:j1-1), the last of duplicated rows kept */
@@ -1040,14 +1041,19 @@ cholmod_sparse *cholmod_l_spsolve(int sys, cholmod_factor *L, cholmod_sparse *B,
         ok = cudaMemcpyAsync(d_cp, cp, sizeof(Int) * (w + 1), cudaMemcpyHostToDevice, st) == cudaSuccess
              && (q == 0 || (cudaMemcpyAsync(d_ci, ci, sizeof(Int) * q, cudaMemcpyHostToDevice, st) == cudaSuccess
                             && cudaMemcpyAsync(d_cx, cx, e * q, cudaMemcpyHostToDevice, st) == cudaSuccess))
+             && cudaEventRecord(ctx->ev0, st) == cudaSuccess
              && cudaMemsetAsync(P->d_B, 0, e * n * w, st) == cudaSuccess
              && gb_launch_sp_scatter(n, w, d_cp, d_ci, d_cx, dt, P->d_B, n, st) == 0
              && gb_solve_dev(sys, L, P, ctx, (int)w, &swept)
              && gb_launch_sp_count(n, w, P->d_B, dt, n, d_cn, st) == 0
+             && cudaEventRecord(ctx->ev1, st) == cudaSuccess
              && cudaMemcpyAsync(cnt, d_cn, sizeof(Int) * nseg * w, cudaMemcpyDeviceToHost, st) == cudaSuccess
              && cudaStreamSynchronize(st) == cudaSuccess
              && !(swept && ctx->sweep_mode == 1 && sweep_failed(P));
         if (!ok) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        dev_ms += ms;
         /* offsets of every (column, segment) within the chunk, columns first */
         size_t c = 0;
         for (Int j = 0; j < w; j++) {
@@ -1074,7 +1080,9 @@ cholmod_sparse *cholmod_l_spsolve(int sys, cholmod_factor *L, cholmod_sparse *B,
                  && cudaMemcpyAsync(Xx + e * xnz, d_xx, e * c, cudaMemcpyDeviceToHost, st) == cudaSuccess
                  && cudaStreamSynchronize(st) == cudaSuccess);
         xnz += c;
+        ctx->launches += 4 + (c > 0);   /* scatter, two permutations, count, compact */
     }
+    ctx->stats[1] = dev_ms;
     cholmod_sparse *X = NULL;
     if (ok) {
         Xp[nrhs] = (Int)xnz;
