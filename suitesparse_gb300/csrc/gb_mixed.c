@@ -156,7 +156,9 @@ int gb300_factorize_mixed(cholmod_sparse *A, cholmod_factor *L, cholmod_common *
         GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "device allocation failed");
         return FALSE;
     }
-    if (gb_valmap_apply(P, ctx, A, Common)) {
+    int deferred = 0, via_maps = 0;
+    if (gb_valmap_apply(P, ctx, A, Common, &deferred)) {
+        via_maps = 1;
         ok = gb_ensure_numeric(P, CHOLMOD_SINGLE);
     } else {
         cholmod_sparse *S = gb_permute_lower(A, L->Perm, Common);
@@ -178,12 +180,22 @@ int gb300_factorize_mixed(cholmod_sparse *A, cholmod_factor *L, cholmod_common *
          && gb_launch_diag_minmax((int)P->nsuper, P->d_Super, P->d_Pi, P->d_Px, P->d_Lx[1], 4,
                                   P->d_red, st) == 0;
     cudaEventRecord(ctx->ev1, st);
+    /* A's pattern, compared while the device factorizes (the values went
+     * through the maps of the pattern they were built for) */
+    const int changed = ok && deferred && !gb_valmap_verify(P, A);
     int32_t dagerr = 0;
     ok = ok && cudaMemcpyAsync(&anyfail, P->d_anyfail, sizeof(int32_t), cudaMemcpyDeviceToHost, st) == cudaSuccess
          && cudaMemcpyAsync(mm, P->d_red, 2 * sizeof(double), cudaMemcpyDeviceToHost, st) == cudaSuccess
          && cudaMemcpyAsync(&dagerr, P->d_ticket + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, st) == cudaSuccess
          && cudaStreamSynchronize(st) == cudaSuccess && !dagerr;
     if (!ok) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the FP32 factorization"); return FALSE; }
+    if (changed) {
+        /* the pattern differs from the maps': rebuild them and factorize
+         * again (the comparison is not deferred the second time) */
+        P->vm_valid = 0;
+        return gb300_factorize_mixed(A, L, Common);
+    }
+    if (via_maps) gb_valmap_anorm(P);
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     ctx->stats[0] = ms;

@@ -472,7 +472,15 @@ static int segments_build(gb_plan *P)
                 lo += GB_SEG_CHUNK;
             } while (lo < hi);
         }
-        P->h_anorm_seg = calloc(P->nseg, sizeof(double));
+        /* pinned, so that its copy from the device does not wait for the
+         * stream (plain memory when no device is present) */
+        if (cudaMallocHost((void **)&P->h_anorm_seg, sizeof(double) * P->nseg) == cudaSuccess) {
+            P->anorm_pinned = 1;
+            memset(P->h_anorm_seg, 0, sizeof(double) * P->nseg);
+        } else {
+            cudaGetLastError();
+            P->h_anorm_seg = calloc(P->nseg, sizeof(double));
+        }
         if (!P->h_anorm_seg) ok = 0;
     }
     free(root);
@@ -1257,7 +1265,9 @@ void gb_plan_free(gb_plan *P)
     gb_vec_free(&P->dag_lv);
     gb_valmap_free(P);
     gb_graph_free(P);
-    free(P->h_seg); free(P->h_chunk); free(P->h_anorm_seg);
+    free(P->h_seg); free(P->h_chunk);
+    if (P->anorm_pinned) cudaFreeHost(P->h_anorm_seg);
+    else free(P->h_anorm_seg);
     gb_vec_free(&P->fd_t); gb_vec_free(&P->fd_sp); gb_vec_free(&P->fd_succ);
     gb_vec_free(&P->fd_nd); gb_vec_free(&P->fd_q0); gb_vec_free(&P->fd_q1);
     gb_vec_free(&P->fd_sub);

@@ -231,6 +231,7 @@ typedef struct gb_plan {
     gb_seg_chunk *h_chunk;            /* row chunks of at most GB_SEG_CHUNK rows */
     gb_seg_chunk *d_chunk;
     double *h_anorm_seg, *d_anorm_seg, *d_bred;
+    int anorm_pinned;                 /* h_anorm_seg from cudaMallocHost */
     size_t bred_cap;
     /* CUDA graph of one refinement step (gb_mixed.c), per pattern: valid
      * for the right-hand-side count, factor precision and buffers it was
@@ -283,7 +284,16 @@ int gb_vec_push(gb_vec *v, const void *e);
 void gb_vec_free(gb_vec *v);
 
 /* Build the plan (host side) for a supernodal symbolic factor. */
-int gb_valmap_apply(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, cholmod_common *Common);
+/* Values of the caller's A to the device through the pattern's maps (built
+ * on first use or pattern change; FALSE: use the host path).  With
+ * deferred != NULL, a packed A of the maps' shape skips the comparison of
+ * its pattern (*deferred = 1): the caller runs gb_valmap_verify while the
+ * device works and redoes the work if it fails.  gb_valmap_anorm forms
+ * P->anorm once the stream has been synchronized. */
+int gb_valmap_apply(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, cholmod_common *Common,
+                    int *deferred);
+int gb_valmap_verify(const gb_plan *P, const cholmod_sparse *A);
+void gb_valmap_anorm(gb_plan *P);
 void gb_valmap_free(gb_plan *P);
 void gb_graph_free(gb_plan *P);     /* gb_mixed.c */
 gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_work,

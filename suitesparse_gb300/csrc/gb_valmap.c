@@ -43,6 +43,18 @@ static Int value_extent(const cholmod_sparse *A)
     return e;
 }
 
+/* The part of the pattern check that costs nothing: maps built for this n
+ * and packing, and a packed A with as many entries, so that the value copy
+ * and the gathers stay inside A->x and the device arrays.  The comparison
+ * of Ap and Ai (gb_valmap_verify) can then run while the factorization
+ * does. */
+static int same_shape(const gb_plan *P, const cholmod_sparse *A)
+{
+    Int n = (Int)A->ncol;
+    return P->vm_valid && P->vm_n == n && P->vm_packed == A->packed && A->packed
+           && ((const Int *)A->p)[n] == P->vm_xlen;
+}
+
 static int same_pattern(const gb_plan *P, const cholmod_sparse *A)
 {
     Int n = (Int)A->ncol;
@@ -162,10 +174,18 @@ static int build(gb_plan *P, cholmod_sparse *A, cholmod_common *Common)
 /* Device copies of S = tril(PAP') (FP64 values), of A's rows and of the
  * scaling for the mixed factorization, from A's values.  FALSE: use the
  * host path. */
-int gb_valmap_apply(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, cholmod_common *Common)
+int gb_valmap_verify(const gb_plan *P, const cholmod_sparse *A) { return same_pattern(P, A); }
+
+int gb_valmap_apply(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, cholmod_common *Common,
+                    int *deferred)
 {
     if (A->xtype != CHOLMOD_REAL || A->dtype != CHOLMOD_DOUBLE || A->itype != CHOLMOD_LONG) return FALSE;
-    if (!same_pattern(P, A) && !build(P, A, Common)) return FALSE;
+    if (deferred && same_shape(P, A)) {
+        *deferred = 1;
+    } else {
+        if (deferred) *deferred = 0;
+        if (!same_pattern(P, A) && !build(P, A, Common)) return FALSE;
+    }
     cudaStream_t st = ctx->stream;
     Int n = P->vm_n;
     size_t cap = 0;
@@ -192,11 +212,16 @@ int gb_valmap_apply(gb_plan *P, gb_ctx *ctx, cholmod_sparse *A, cholmod_common *
          && gb_launch_diag_scale(n, P->d_dmap, P->d_Ax, P->d_Perm, P->d_scale, P->d_scale_perm, st) == 0
          && gb_launch_anorm_seg(P->nchunk, P->d_chunk, P->nseg, P->d_Rp, P->d_Rx, P->d_anorm_seg, st) == 0
          && cudaMemcpyAsync(P->h_anorm_seg, P->d_anorm_seg, sizeof(double) * P->nseg,
-                            cudaMemcpyDeviceToHost, st) == cudaSuccess
-         && cudaStreamSynchronize(st) == cudaSuccess;
+                            cudaMemcpyDeviceToHost, st) == cudaSuccess;
     if (!ok) return FALSE;
-    P->anorm = 0;
-    for (int64_t g = 0; g < P->nseg; g++) P->anorm = fmax(P->anorm, P->h_anorm_seg[g]);
+    /* h_anorm_seg (pinned) is complete at the caller's next synchronization
+     * of the stream; P->anorm is formed there (gb_valmap_anorm) */
     ctx->launches += 4;
     return TRUE;
+}
+
+void gb_valmap_anorm(gb_plan *P)
+{
+    P->anorm = 0;
+    for (int64_t g = 0; g < P->nseg; g++) P->anorm = fmax(P->anorm, P->h_anorm_seg[g]);
 }

@@ -116,3 +116,42 @@ def test_refinement_graph_replay_same_result(golden, lib, oracle_mod):
     for (x0, i0), (x1, i1) in zip(res[0], res[1]):
         assert i0 == i1
         assert np.array_equal(x0, x1)
+
+
+def test_value_maps_follow_a_pattern_change(golden, lib, oracle_mod):
+    """Refactorizations gather A's values on the device through maps built
+    for A's pattern; a packed A with as many entries is compared with that
+    pattern while the device factorizes.  Two entries of a column swapped in
+    place (the same matrix, another pattern) must be detected: the maps are
+    rebuilt and the result equals the first one bit for bit (stale maps
+    would swap the two values)."""
+    meta, arrays = golden
+    c = CH.Common()
+    mat, A, L = setup(meta, arrays, "g3", c)
+    n = mat[0]
+    B = M.rhs(n, 2, 4)
+    assert CH.factorize_mixed(A, L, c) == 1
+    X1, _ = CH.solve_refined(A, L, B, c, tol=TOL)
+    a = A.contents
+    nz = int(mat[1][-1])
+    Ap = CH._arr(a.p, np.int64, n + 1)
+    Ai = CH._arr(a.i, np.int64, nz)
+    Ax = CH._arr(a.x, np.float64, nz)
+    j = next(j for j in range(n) if Ap[j + 1] - Ap[j] >= 3)
+    p, q = int(Ap[j]) + 1, int(Ap[j]) + 2          # two off-diagonal entries
+    assert Ax[p] != Ax[q]
+    Ai[p], Ai[q] = Ai[q], Ai[p]
+    Ax[p], Ax[q] = Ax[q], Ax[p]
+    a.sorted = 0
+    assert CH.factorize_mixed(A, L, c) == 1 and c.status == CH.CHOLMOD_OK
+    X2, _ = CH.solve_refined(A, L, B, c, tol=TOL)
+    np.testing.assert_array_equal(X1, X2)
+    # and the values of the new positions are used from now on
+    Ax[p] *= 0.5                                  # still diagonally dominant
+    assert CH.factorize_mixed(A, L, c) == 1
+    X3, _ = CH.solve_refined(A, L, B, c, tol=TOL)
+    Ai2, Ax2 = np.array(Ai), np.array(Ax)
+    be = oracle_mod.backward_error(n, np.array(Ap), Ai2, Ax2, X3, B)
+    assert be.max() <= TOL
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
