@@ -10,10 +10,10 @@ A step is one factorization of the matrix (numeric values re-assembled from
 A) followed by one refined solve to 1e-12 with one right-hand side.
   value       = fl / device time of the factorization, inputs resident on the
                 GPU (CUDA events on the library's stream)
-  e2e         = the same through the C ABI from host buffers
-                (gb300_factorize_mixed + gb300_solve_refined: the copy of A's
-                values, their permutation on the GPU, the copy of B and the
-                read of X inside the timed region)
+  e2e         = the same through the C ABI from pinned host buffers
+                (gb300_factorize_mixed + gb300_solve_refined2 into a reused X:
+                the copy of A's values, their permutation on the GPU, the copy
+                of B and the read of X inside the timed region)
   --impl reference  times the CPU oracle (the reference's left-looking
                 supernodal algorithm over OpenBLAS, all host cores) on the same
                 matrix in FP64, the form the reference CPU path computes.
@@ -134,6 +134,25 @@ def pin_ptr(rt, ptr, nbytes):
         rt.cudaHostRegister(ctypes.c_void_p(ptr), ctypes.c_size_t(nbytes), 0)
 
 
+def solve_refined_raw(A, L, Bd, Xh, c, tol=1e-12):
+    """gb300_solve_refined2 with caller-owned (pinned) cholmod_dense B and X
+    (Xh: a pointer to the X handle, reused from step to step): the C call a
+    user makes.  Returns the info record."""
+    from suitesparse_gb300 import cholmod as CH
+    info = (ctypes.c_double * 4)()
+    assert CH.lib().gb300_solve_refined2(A, L, Bd, tol, info, Xh, c.ptr), c.status
+    return {"iterations": int(info[0]), "berr": info[1], "fp64_fallback": bool(info[2])}
+
+
+def pinned_x(rt, c, n, nrhs):
+    """A cholmod_dense X (n x nrhs, real double) in pinned memory and a
+    handle to it for gb300_solve_refined2."""
+    from suitesparse_gb300 import cholmod as CH
+    Xd = CH.dense(np.zeros((n, nrhs)), c)
+    pin_ptr(rt, Xd.contents.x, 8 * n * nrhs)
+    return Xd, ctypes.pointer(Xd)
+
+
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -251,15 +270,21 @@ def run_gpu(args):
                  "table_ms": {f"{k[0]}/{k[1]}": v for k, v in table.items()}}
     info = CH.factor_info(L, c)
 
+    # B and X in caller-owned cholmod_dense objects in pinned memory, as
+    # A's arrays
+    Bd = CH.dense(B, c)
+    pin_ptr(rt, Bd.contents.x, 8 * n)
+    Xd, Xh = pinned_x(rt, c, n, 1)
+
     def step_mixed():
         t0 = time.perf_counter()
         ok = CH.factorize_mixed(A, L, c)
         st = c.stats()
-        X, rinfo = CH.solve_refined(A, L, B, c, tol=1e-12)
+        rinfo = solve_refined_raw(A, L, Bd, Xh, c)
         t1 = time.perf_counter()
         st2 = c.stats()
         assert ok, c.status
-        return st[0], st2[2], t1 - t0, X, rinfo
+        return st[0], st2[2], t1 - t0, CH.dense_array(Xh.contents), rinfo
 
     for _ in range(args.warmup):
         step_mixed()
@@ -440,12 +465,23 @@ def run_batch(args):
     tuned = {"small_cols": best[0], "subtree_work": best[1],
              "table_ms": {f"{k[0]}/{k[1]}": v for k, v in table.items()}}
 
+    # A's arrays, B and X (caller-owned cholmod_dense objects) in pinned memory
+    rt = cudart()
+    a = b.A.contents
+    pin_ptr(rt, a.p, 8 * (b.n + 1))
+    pin_ptr(rt, a.i, 8 * int(a.nzmax))
+    pin_ptr(rt, a.x, 8 * int(a.nzmax))
+    Bd = CH.dense(B, c)
+    pin_ptr(rt, Bd.contents.x, 8 * b.n * nrhs)
+    Xd, Xh = pinned_x(rt, c, b.n, nrhs)
+
     def step():
         t0 = time.perf_counter()
         assert CH.factorize_mixed(b.A, b.L, c)
         f_ms = c.stats()[0]
-        X, info = CH.solve_refined(b.A, b.L, B, c, tol=1e-12)
-        return f_ms, c.stats()[2], time.perf_counter() - t0, X, info
+        info = solve_refined_raw(b.A, b.L, Bd, Xh, c)
+        t1 = time.perf_counter()
+        return f_ms, c.stats()[2], t1 - t0, CH.dense_array(Xh.contents), info
 
     for _ in range(args.warmup):
         step()
@@ -500,6 +536,11 @@ def run_batch(args):
                 "d2h_bytes_per_step": int(8 * b.n * nrhs)},
         "plan": info_plan, "autotune": tuned, "gpu_launches": launches, "clocks": clk.summary(),
     }
+    if rt is not None:
+        for ptr in (a.p, a.i, a.x, Bd.contents.x, Xh.contents.contents.x):
+            rt.cudaHostUnregister(ctypes.c_void_p(ptr))
+    CH.free_dense(Bd, c)
+    CH.free_dense(Xh.contents, c)
     b.free()
     c.finish()
     if rank == 0:

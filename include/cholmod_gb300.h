@@ -456,7 +456,19 @@ int gb300_factorize_mixed (cholmod_sparse *A, cholmod_factor *L,
 cholmod_dense *gb300_solve_refined (cholmod_sparse *A, cholmod_factor *L,
     cholmod_dense *B, double tol, double *info, cholmod_common *Common) ;
 
-/* Release the GPU state attached to L (device factor, plans, graphs). */
+/* gb300_solve_refined writing into *X_Handle, as cholmod_l_solve2 reuses
+ * its X (CHOLMOD/Cholesky/cholmod_solve.c:298, ensure_dense): an X of n
+ * rows, B->ncol columns, d >= n, real double, is overwritten in place (it
+ * may be page-locked by the caller, so that the result's copy back is a
+ * plain DMA); any other X is freed and replaced, a NULL one allocated.
+ * Returns TRUE, or FALSE with Common->status set. */
+int gb300_solve_refined2 (cholmod_sparse *A, cholmod_factor *L, cholmod_dense *B,
+    double tol, double *info, cholmod_dense **X_Handle, cholmod_common *Common) ;
+
+/* Release the GPU state attached to L (device factor, plans, graphs).  The
+ * plan of a factor is found again by the factor's address, sizes, pattern
+ * array addresses and a fingerprint of sampled pattern entries; a caller
+ * that rewrites L's pattern arrays in place calls this first. */
 int gb300_release_factor (cholmod_factor *L, cholmod_common *Common) ;
 
 /* Object helpers for programs without the reference library.  Memory comes

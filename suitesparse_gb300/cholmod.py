@@ -93,6 +93,8 @@ def lib():
         "gb300_solve": (DP, [C.c_int, FP, DP, vp]),
         "gb300_factorize_mixed": (C.c_int, [SP, FP, vp]),
         "gb300_solve_refined": (DP, [SP, FP, DP, C.c_double, C.POINTER(C.c_double), vp]),
+        "gb300_solve_refined2": (C.c_int, [SP, FP, DP, C.c_double, C.POINTER(C.c_double),
+                                           C.POINTER(DP), vp]),
         "gb300_release_factor": (C.c_int, [FP, vp]),
         "gb300_get_profile": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]),
         "gb300_factor_info": (C.c_int, [FP, vp, C.POINTER(C.c_double), C.c_int]),

@@ -281,8 +281,12 @@ static int refine_step(gb_plan *P, gb_ctx *ctx, int nrhs, int single, int may_ca
     return cudaGraphLaunch((cudaGraphExec_t)P->g_exec, st) == cudaSuccess;
 }
 
-cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod_dense *B,
-                                   double tol, double *info, cholmod_common *Common)
+/* The refined solve into X: a caller's X of the right shape (n x nrhs,
+ * real double, d >= n) is written in place, else a new one is allocated;
+ * on failure an X allocated here is freed and NULL returned. */
+static cholmod_dense *solve_refined_into(cholmod_sparse *A, cholmod_factor *L, cholmod_dense *B,
+                                         double tol, double *info, cholmod_dense *Xin,
+                                         cholmod_common *Common)
 {
     if (!Common) return NULL;
     if (!A || !L || !B) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return NULL; }
@@ -301,7 +305,8 @@ cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod
     }
     Int n = P->n;
     int nrhs = (int)B->ncol;
-    cholmod_dense *X = gb300_allocate_dense(n, nrhs, n, CHOLMOD_REAL + CHOLMOD_DOUBLE, Common);
+    cholmod_dense *X = Xin;
+    if (!X) X = gb300_allocate_dense(n, nrhs, n, CHOLMOD_REAL + CHOLMOD_DOUBLE, Common);
     if (!X) return NULL;
     if (info) { info[0] = 0; info[1] = 0; info[2] = P->mixed == 2; info[3] = 0; }
     if (n == 0 || nrhs == 0) return X;
@@ -364,7 +369,7 @@ cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod
     free(hred);
     free(best);
     if (!ok) {
-        gb300_free_dense(&X, Common);
+        if (X != Xin) gb300_free_dense(&X, Common);
         if (Common->status == CHOLMOD_OK) GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in refinement");
         return NULL;
     }
@@ -374,4 +379,28 @@ cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod
     if (info) { info[0] = it; info[1] = berr_max; info[3] = berr_max; info[2] = P->mixed == 2; }
     if (berr_max > tol) GB_ERROR(CHOLMOD_DSMALL, "refinement did not reach the requested tolerance");
     return X;
+}
+
+cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod_dense *B,
+                                   double tol, double *info, cholmod_common *Common)
+{
+    return solve_refined_into(A, L, B, tol, info, NULL, Common);
+}
+
+int gb300_solve_refined2(cholmod_sparse *A, cholmod_factor *L, cholmod_dense *B, double tol,
+                         double *info, cholmod_dense **X_Handle, cholmod_common *Common)
+{
+    if (!Common) return FALSE;
+    if (!X_Handle) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return FALSE; }
+    cholmod_dense *X = *X_Handle;
+    if (X && B && L
+        && !(X->nrow == L->n && X->ncol == B->ncol && X->d >= X->nrow && X->xtype == CHOLMOD_REAL
+             && X->dtype == CHOLMOD_DOUBLE && X->x)) {
+        gb300_free_dense(X_Handle, Common);          /* wrong shape: replaced */
+        X = NULL;
+    }
+    cholmod_dense *R = solve_refined_into(A, L, B, tol, info, X, Common);
+    if (!R) return FALSE;
+    *X_Handle = R;
+    return TRUE;
 }

@@ -43,8 +43,13 @@ static uint64_t mix64(uint64_t h, uint64_t x)
     return h ^ (h >> 31);
 }
 
-/* fingerprint of the supernodal pattern: all of super/pi, every 16th row
- * index of s, and the sizes */
+/* A fingerprint of L's supernodal pattern, checked on every use of the plan
+ * (with the sizes and array addresses): the sizes, every supernode's
+ * boundaries and row count at up to 4096 evenly spaced supernodes, and up to
+ * 4096 evenly spaced row indices, so that its cost does not grow with the
+ * factor (a batch of 4096 systems has 1.7M supernodes).  A caller that
+ * rewrites L's pattern arrays in place must release the factor's GPU state
+ * (gb300_release_factor) first. */
 uint64_t gb_pattern_hash(const cholmod_factor *L)
 {
     uint64_t h = mix64(0, L->n);
@@ -52,9 +57,12 @@ uint64_t gb_pattern_hash(const cholmod_factor *L)
     h = mix64(h, L->ssize);
     h = mix64(h, L->xsize);
     const Int *Super = L->super, *Pi = L->pi, *Ls = L->s;
-    for (size_t s = 0; s <= L->nsuper; s++) h = mix64(mix64(h, Super[s]), Pi[s]);
+    const size_t ss = L->nsuper / 4096 + 1;
+    for (size_t s = 0; s <= L->nsuper; s += ss) h = mix64(mix64(h, Super[s]), Pi[s]);
+    h = mix64(mix64(h, Super[L->nsuper]), Pi[L->nsuper]);
     size_t ns = (size_t)Pi[L->nsuper];
-    for (size_t p = 0; p < ns; p += 16) h = mix64(h, Ls[p]);
+    const size_t sp = ns / 4096 + 1;
+    for (size_t p = 0; p < ns; p += sp) h = mix64(h, Ls[p]);
     if (ns) h = mix64(h, Ls[ns - 1]);
     return h;
 }

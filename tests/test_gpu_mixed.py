@@ -155,3 +155,39 @@ def test_value_maps_follow_a_pattern_change(golden, lib, oracle_mod):
     assert be.max() <= TOL
     CH.free_factor(L, c)
     CH.free_sparse(A, c)
+
+
+def test_solve_refined2_reuses_x(golden, lib, oracle_mod):
+    """gb300_solve_refined2: a caller's X of the right shape is written in
+    place (the same pointer, the same result as gb300_solve_refined); a
+    NULL handle gets a new X, one of the wrong shape is replaced."""
+    import ctypes as C
+    meta, arrays = golden
+    c = CH.Common()
+    mat, A, L = setup(meta, arrays, "g3", c)
+    n = mat[0]
+    B = M.rhs(n, 3, 8)
+    assert CH.factorize_mixed(A, L, c) == 1
+    X0, _ = CH.solve_refined(A, L, B, c, tol=TOL)
+    Bd = CH.dense(B, c)
+    info = (C.c_double * 4)()
+    Xd = CH.dense(np.zeros((n, 3)), c)
+    addr = C.addressof(Xd.contents)
+    h = C.pointer(Xd)
+    assert lib.gb300_solve_refined2(A, L, Bd, TOL, info, h, c.ptr) == 1
+    assert C.addressof(h.contents.contents) == addr
+    np.testing.assert_array_equal(CH.dense_array(h.contents), X0)
+    assert info[1] <= TOL
+    wrong = CH.dense(np.zeros((n, 2)), c)
+    h2 = C.pointer(wrong)
+    assert lib.gb300_solve_refined2(A, L, Bd, TOL, info, h2, c.ptr) == 1
+    assert h2.contents.contents.ncol == 3
+    np.testing.assert_array_equal(CH.dense_array(h2.contents), X0)
+    h3 = C.pointer(CH.DP())
+    assert lib.gb300_solve_refined2(A, L, Bd, TOL, info, h3, c.ptr) == 1
+    np.testing.assert_array_equal(CH.dense_array(h3.contents), X0)
+    for hh in (h, h2, h3):
+        CH.free_dense(hh.contents, c)
+    CH.free_dense(Bd, c)
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
