@@ -238,6 +238,7 @@ static void graph_bufs(gb_plan *P, int single, const void **b)
 {
     b[0] = P->d_Y; b[1] = P->d_R; b[2] = P->d_X; b[3] = P->d_bx; b[4] = P->d_bred;
     b[5] = P->d_U; b[6] = P->d_Lx[single ? 1 : 0]; b[7] = P->d_Linv[single ? 1 : 0];
+    b[8] = P->d_sws;
 }
 
 /* One refinement step: from the plan's CUDA graph when it matches, else
@@ -247,7 +248,7 @@ static int refine_step(gb_plan *P, gb_ctx *ctx, int nrhs, int single, int may_ca
     cudaStream_t st = ctx->stream;
     if (!ctx->graph_mode || ctx->sweep_mode != 1 || ctx->trace_on)
         return refine_step_launch(P, ctx, nrhs, single);
-    const void *b[8];
+    const void *b[9];
     graph_bufs(P, single, b);
     int match = P->g_exec && P->g_nrhs == nrhs && P->g_single == single
                 && memcmp(b, P->g_bufs, sizeof b) == 0;

@@ -41,6 +41,11 @@ void gb_ctx_delete(gb_ctx *c)
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (int i = 0; i < c->npev; i++) cudaEventDestroy(c->pev[i]);
+    for (int i = 0; i < GB_SWEEP_STREAMS - 1; i++) {
+        if (c->side[i]) cudaStreamDestroy(c->side[i]);
+        if (c->ev_join[i]) cudaEventDestroy(c->ev_join[i]);
+    }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->d_trace) cudaFree(c->d_trace);
     if (c->d_ftrace) cudaFree(c->d_ftrace);
     free(c->pev);
@@ -479,6 +484,87 @@ static int sweep_failed(gb_plan *P)
 }
 
 /* Replay one sweep on Y (device, n x nrhs, ld n) with the device factor. */
+/* One single-launch sweep pass over nrhs <= GB_SWEEP_COLS columns on
+ * stream st, with its own dependency words (xready, done, ticket[0..1]) and
+ * update vectors U (cbv_total x nrhs): the leaf subtrees (one warp each,
+ * before the other tasks forward, after them backward) and the
+ * dependency-driven launch. */
+static int sweep_pass(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int forward,
+                      cudaStream_t st, int32_t *xready, int32_t *done, int32_t *ticket, void *U,
+                      int allow_trace)
+{
+    int d = dt_index(l_dtype);
+    int ldt = l_dtype == CHOLMOD_SINGLE ? 4 : 0;
+    const void *Lx = P->d_Lx[d];
+    gb_sweep1_args a;
+    a.tasks = forward ? P->d_sf : P->d_sb;
+    a.ntasks = (int)(forward ? P->sf_t.n : P->sb_t.n);
+    a.gptr = forward ? P->d_gf : P->d_gb;
+    a.cptr = P->d_sf_cptr;
+    a.crange = P->d_sf_crange;
+    a.ngroups = (int)(forward ? P->gf.n : P->gb.n) - 1;
+    a.blkoff = P->d_blkoff;
+    a.linvoff = P->d_linvoff;
+    a.ntask_s = forward ? P->d_ntask_f : P->d_ntask_b;
+    a.parent = P->d_parent;
+    a.xready = xready;
+    a.done = done;
+    a.ticket = ticket;
+    a.err = P->d_err;
+    a.trace = NULL;
+    if (allow_trace && ctx->trace_on) {
+        size_t need = 3 * (size_t)(P->sf_t.n + P->sb_t.n + 2) * sizeof(unsigned long long);
+        if (gb_dev_grow((void **)&ctx->d_trace, &ctx->trace_cap, need)) {
+            int64_t off = forward ? 0 : 3 * (int64_t)(P->sf_t.n + 1);
+            a.trace = ctx->d_trace + off;
+            ctx->trace_off[forward ? 0 : 1] = off;
+            ctx->trace_n[forward ? 0 : 1] = a.ntasks;
+        }
+    }
+    if (cudaMemsetAsync(xready, 0, sizeof(int32_t) * (P->nblk_total + 1), st) != cudaSuccess
+        || cudaMemsetAsync(done, 0, sizeof(int32_t) * (P->nsuper + 1), st) != cudaSuccess
+        || cudaMemsetAsync(ticket, 0, sizeof(int32_t) * 2, st) != cudaSuccess)
+        return FALSE;
+    int grid = GB_MAX(1, ctx->sms) * 4;
+    const int nleaf = (int)P->lf_t.n;
+    const int lgrid = GB_MAX(1, ctx->sms) * 16;
+    if (forward && nleaf > 0) {
+        if (gb_launch_sweep_leaf(1, &P->ptrs, P->d_lf, nleaf, P->d_blkoff, P->d_linvoff,
+                                 P->d_ntask_f, done, ticket + 1, Lx, P->d_Linv[d],
+                                 ldt, nrhs, Y, P->n, U, lgrid, st) != 0)
+            return FALSE;
+        ctx->launches += 1;
+    }
+    if (a.ntasks > 0) {
+        if (gb_launch_sweep1(forward, &P->ptrs, &a, Lx, P->d_Linv[d], ldt, nrhs, Y, P->n,
+                             U, grid, st) != 0)
+            return FALSE;
+        ctx->launches += 1;
+    }
+    if (!forward && nleaf > 0) {
+        if (gb_launch_sweep_leaf(0, &P->ptrs, P->d_lf, nleaf, P->d_blkoff, P->d_linvoff,
+                                 P->d_ntask_b, done, ticket + 1, Lx, P->d_Linv[d],
+                                 ldt, nrhs, Y, P->n, U, lgrid, st) != 0)
+            return FALSE;
+        ctx->launches += 1;
+    }
+    return TRUE;
+}
+
+/* side streams and fork/join events of the concurrent sweep passes */
+static int sweep_streams(gb_ctx *ctx)
+{
+    if (ctx->side_ok) return ctx->side_ok > 0;
+    ctx->side_ok = -1;
+    if (cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess) return FALSE;
+    for (int c = 0; c < GB_SWEEP_STREAMS - 1; c++)
+        if (cudaStreamCreateWithFlags(&ctx->side[c], cudaStreamNonBlocking) != cudaSuccess
+            || cudaEventCreateWithFlags(&ctx->ev_join[c], cudaEventDisableTiming) != cudaSuccess)
+            return FALSE;
+    ctx->side_ok = 1;
+    return TRUE;
+}
+
 int gb_run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int forward)
 {
     cudaStream_t st = ctx->stream;
@@ -486,74 +572,53 @@ int gb_run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int fo
     int ldt = l_dtype == CHOLMOD_SINGLE ? 4 : 0;
     size_t e = dt_size(l_dtype);
     const void *Lx = P->d_Lx[d];
-    if (ctx->sweep_mode == 1 && nrhs > GB_SWEEP_COLS) {
-        /* passes of GB_SWEEP_COLS columns: each pass's update vectors
-         * (cbv_total x GB_SWEEP_COLS entries) stay resident in L2 */
+    if (ctx->sweep_mode == 1) {
+        if (!P->linv_valid[d] && !gb_run_inverse(P, ctx, l_dtype)) return FALSE;
+        /* the sweep's error word, shared by its passes */
+        if (cudaMemsetAsync(P->d_err, 0, sizeof(int32_t), st) != cudaSuccess) return FALSE;
+        const int npass = (nrhs + GB_SWEEP_COLS - 1) / GB_SWEEP_COLS;
+        const int ns = GB_MIN(npass, GB_SWEEP_STREAMS);
+        const size_t ureg = e * (size_t)GB_MAX(P->cbv_total, 1) * GB_SWEEP_COLS;
+        const size_t words = (size_t)(P->nblk_total + 1) + (size_t)(P->nsuper + 1) + 4;
+        if (npass > 1 && sweep_streams(ctx) && gb_dev_grow(&P->d_U, &P->u_cap, ureg * ns)
+            && gb_dev_grow((void **)&P->d_sws, &P->sws_cap, sizeof(int32_t) * words * ns)) {
+            /* passes of GB_SWEEP_COLS columns, up to GB_SWEEP_STREAMS of them
+             * at once on their own streams, each with its own dependency
+             * words and update vectors: the passes' dependency chains
+             * through the top separators overlap instead of following one
+             * another */
+            int ok = cudaEventRecord(ctx->ev_fork, st) == cudaSuccess;
+            for (int c = 1; c < ns; c++)
+                ok = ok && cudaStreamWaitEvent(ctx->side[c - 1], ctx->ev_fork, 0) == cudaSuccess;
+            for (int p = 0; ok && p < npass; p++) {
+                const int c = p % ns;
+                cudaStream_t sc = c ? ctx->side[c - 1] : st;
+                int32_t *xr = P->d_sws + words * c;
+                int32_t *dn = xr + P->nblk_total + 1;
+                int32_t *tk = dn + P->nsuper + 1;
+                ok = sweep_pass(P, ctx, l_dtype, GB_MIN(GB_SWEEP_COLS, nrhs - p * GB_SWEEP_COLS),
+                                (char *)Y + e * (size_t)p * GB_SWEEP_COLS * (size_t)P->n, forward,
+                                sc, xr, dn, tk, (char *)P->d_U + ureg * c, 0);
+            }
+            /* the side streams join the main stream whatever happened */
+            for (int c = 1; c < ns; c++) {
+                int j = cudaEventRecord(ctx->ev_join[c - 1], ctx->side[c - 1]) == cudaSuccess
+                        && cudaStreamWaitEvent(st, ctx->ev_join[c - 1], 0) == cudaSuccess;
+                ok = ok && j;
+            }
+            return ok;
+        }
+        /* one pass after the other on the main stream */
+        const int w = GB_MIN(nrhs, GB_SWEEP_COLS);
+        if (!gb_dev_grow(&P->d_U, &P->u_cap, e * GB_MAX(P->cbv_total, 1) * w)) return FALSE;
         for (int k0 = 0; k0 < nrhs; k0 += GB_SWEEP_COLS)
-            if (!gb_run_sweep(P, ctx, l_dtype, GB_MIN(GB_SWEEP_COLS, nrhs - k0),
-                              (char *)Y + e * (size_t)k0 * (size_t)P->n, forward))
+            if (!sweep_pass(P, ctx, l_dtype, GB_MIN(GB_SWEEP_COLS, nrhs - k0),
+                            (char *)Y + e * (size_t)k0 * (size_t)P->n, forward, st, P->d_xready,
+                            P->d_done, P->d_ticket, P->d_U, npass == 1))
                 return FALSE;
         return TRUE;
     }
     if (!gb_dev_grow(&P->d_U, &P->u_cap, e * GB_MAX(P->cbv_total, 1) * nrhs)) return FALSE;
-    if (ctx->sweep_mode == 1) {
-        if (!P->linv_valid[d] && !gb_run_inverse(P, ctx, l_dtype)) return FALSE;
-        gb_sweep1_args a;
-        a.tasks = forward ? P->d_sf : P->d_sb;
-        a.ntasks = (int)(forward ? P->sf_t.n : P->sb_t.n);
-        a.gptr = forward ? P->d_gf : P->d_gb;
-        a.cptr = P->d_sf_cptr;
-        a.crange = P->d_sf_crange;
-        a.ngroups = (int)(forward ? P->gf.n : P->gb.n) - 1;
-        a.blkoff = P->d_blkoff;
-        a.linvoff = P->d_linvoff;
-        a.ntask_s = forward ? P->d_ntask_f : P->d_ntask_b;
-        a.parent = P->d_parent;
-        a.xready = P->d_xready;
-        a.done = P->d_done;
-        a.ticket = P->d_ticket;
-        a.err = P->d_err;
-        a.trace = NULL;
-        if (ctx->trace_on) {
-            size_t need = 3 * (size_t)(P->sf_t.n + P->sb_t.n + 2) * sizeof(unsigned long long);
-            if (gb_dev_grow((void **)&ctx->d_trace, &ctx->trace_cap, need)) {
-                int64_t off = forward ? 0 : 3 * (int64_t)(P->sf_t.n + 1);
-                a.trace = ctx->d_trace + off;
-                ctx->trace_off[forward ? 0 : 1] = off;
-                ctx->trace_n[forward ? 0 : 1] = a.ntasks;
-            }
-        }
-        if (cudaMemsetAsync(P->d_xready, 0, sizeof(int32_t) * (P->nblk_total + 1), st) != cudaSuccess
-            || cudaMemsetAsync(P->d_done, 0, sizeof(int32_t) * (P->nsuper + 1), st) != cudaSuccess
-            || cudaMemsetAsync(P->d_ticket, 0, sizeof(int32_t) * 4, st) != cudaSuccess)
-            return FALSE;
-        int grid = GB_MAX(1, ctx->sms) * 4;
-        /* leaf subtrees (one warp each): before the other tasks forward,
-         * after them backward */
-        const int nleaf = (int)P->lf_t.n;
-        const int lgrid = GB_MAX(1, ctx->sms) * 16;
-        if (forward && nleaf > 0) {
-            if (gb_launch_sweep_leaf(1, &P->ptrs, P->d_lf, nleaf, P->d_blkoff, P->d_linvoff,
-                                     P->d_ntask_f, P->d_done, P->d_ticket + 1, Lx, P->d_Linv[d],
-                                     ldt, nrhs, Y, P->n, P->d_U, lgrid, st) != 0)
-                return FALSE;
-            ctx->launches += 1;
-        }
-        if (a.ntasks > 0) {
-            if (gb_launch_sweep1(forward, &P->ptrs, &a, Lx, P->d_Linv[d], ldt, nrhs, Y, P->n,
-                                 P->d_U, grid, st) != 0)
-                return FALSE;
-            ctx->launches += 1;
-        }
-        if (!forward && nleaf > 0) {
-            if (gb_launch_sweep_leaf(0, &P->ptrs, P->d_lf, nleaf, P->d_blkoff, P->d_linvoff,
-                                     P->d_ntask_b, P->d_done, P->d_ticket + 1, Lx, P->d_Linv[d],
-                                     ldt, nrhs, Y, P->n, P->d_U, lgrid, st) != 0)
-                return FALSE;
-            ctx->launches += 1;
-        }
-        return TRUE;
-    }
     gb_vec *seqv = forward ? &P->fwd_seq : &P->bwd_seq;
     const gb_launch_rec *seq = seqv->p;
     for (size_t i = 0; i < seqv->n; i++) {

@@ -1284,7 +1284,7 @@ void gb_plan_free(gb_plan *P)
                    P->d_Ls, P->d_relmap, P->d_child_ptr, P->d_child_list, P->d_fail,
                    P->d_anyfail, P->d_asm, P->d_node, P->d_potrf, P->d_trsm, P->d_gemm,
                    P->d_gemm_owner, P->d_sweep, P->d_Lx[0], P->d_Lx[1], P->d_CB[0],
-                   P->d_CB[1], P->d_Sp, P->d_Si, P->d_Sx, P->d_Y, P->d_U, P->d_B, P->d_spw,
+                   P->d_CB[1], P->d_Sp, P->d_Si, P->d_Sx, P->d_Y, P->d_U, P->d_B, P->d_spw, P->d_sws,
                    P->d_Rp, P->d_Rj, P->d_Rx, P->d_scale, P->d_scale_perm, P->d_X, P->d_R,
                    P->d_bx, P->d_red, P->d_sf, P->d_sb, P->d_sd, P->d_lf, P->d_sf_cptr, P->d_sf_crange, P->d_blkoff, P->d_ntask_f,
                    P->d_ntask_b, P->d_parent, P->d_linvoff, P->d_xready, P->d_done,

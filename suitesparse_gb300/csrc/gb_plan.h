@@ -91,8 +91,10 @@ typedef struct {
     int use_tc;                      /* FP32 tile products on the tensor cores */
 } gb_fdag_args;
 
-/* right-hand-side columns per single-launch sweep pass */
+/* right-hand-side columns per single-launch sweep pass, and passes that run
+ * at once on their own streams */
 #define GB_SWEEP_COLS 16
+#define GB_SWEEP_STREAMS 4
 #define GB_LEAF_MEMBERS 256        /* supernodes of a sweep leaf subtree */
 #define GB_LEAF_ROWS 64            /* rows of a front in a sweep leaf subtree */
 
@@ -206,6 +208,8 @@ typedef struct gb_plan {
     size_t y_cap, u_cap, b_cap;
     void *d_spw;                      /* cholmod_l_spsolve: B chunk, counts, X chunk */
     size_t spw_cap;
+    int32_t *d_sws;                   /* dependency words of concurrent sweep passes */
+    size_t sws_cap;
 
     /* full (both triangles) FP64 copy of A for residuals, plus scaling */
     int64_t *d_Rp;
@@ -239,7 +243,7 @@ typedef struct gb_plan {
     void *g_exec;
     int g_nrhs, g_single;
     int64_t g_launches;               /* kernel launches one replay makes */
-    const void *g_bufs[8];
+    const void *g_bufs[9];
 
     struct gb_plan *next;             /* side-table chaining */
 } gb_plan;
@@ -277,6 +281,11 @@ struct gb_ctx {
     int sms;
     cudaEvent_t *pev;
     int npev;
+    /* concurrent sweep passes (more than GB_SWEEP_COLS right-hand sides):
+     * side streams, fork and join events; side_ok 1 ready, -1 failed */
+    cudaStream_t side[GB_SWEEP_STREAMS - 1];
+    cudaEvent_t ev_fork, ev_join[GB_SWEEP_STREAMS - 1];
+    int side_ok;
     double kind_ms[16], kind_n[16];
 };
 

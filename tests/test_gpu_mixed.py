@@ -191,3 +191,29 @@ def test_solve_refined2_reuses_x(golden, lib, oracle_mod):
     CH.free_dense(Bd, c)
     CH.free_factor(L, c)
     CH.free_sparse(A, c)
+
+
+def test_concurrent_sweep_passes(golden, lib, oracle_mod):
+    """More than 16 right-hand sides: passes of 16 columns run at once on
+    their own streams, each with its own dependency words and update
+    vectors.  Each pass computes what a 16-column solve computes (bit for
+    bit); the refined solve with 70 columns (5 passes on 4 streams) meets
+    the tolerance, directly and replayed from the pattern's graph."""
+    meta, arrays = golden
+    c = CH.Common()
+    mat, A, L = setup(meta, arrays, "c1", c)
+    n = mat[0]
+    B = M.rhs(n, 70, 12)
+    assert CH.factorize(A, L, c) == 1
+    X = CH.solve(L, B, c)
+    for k0 in range(0, 70, 16):
+        Xk = CH.solve(L, B[:, k0:k0 + 16], c)
+        np.testing.assert_array_equal(X[:, k0:k0 + 16], Xk)
+    assert oracle_mod.backward_error(*mat, X, B).max() <= 1e-14
+    assert CH.factorize_mixed(A, L, c) == 1
+    X1, i1 = CH.solve_refined(A, L, B, c, tol=TOL)
+    X2, i2 = CH.solve_refined(A, L, B, c, tol=TOL)
+    np.testing.assert_array_equal(X1, X2)
+    assert oracle_mod.backward_error(*mat, X2, B).max() <= TOL
+    CH.free_factor(L, c)
+    CH.free_sparse(A, c)
