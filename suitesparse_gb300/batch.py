@@ -25,13 +25,35 @@ def golden_perms(sides):
     return [arrays[f"c4_{s}_Perm"].astype(np.int64) for s in sides]
 
 
-def c4_workload(nsys=4096, seed=3):
+def c4_workload(nsys=4096, seed=3, systems=None):
     """sides (8 distinct), sys_pat (side index of each system), perms, and
-    the systems' lower-triangular CSC matrices."""
+    the systems' lower-triangular CSC matrices (only those of the indices in
+    ``systems`` when given; ``pat`` still covers every system)."""
     sides, pat = M.batch_layout(nsys, seed)
     perms = golden_perms(sides)
-    mats = [M.batch_system(i, sides[pat[i]]) for i in range(nsys)]
+    idx = range(nsys) if systems is None else systems
+    mats = [M.batch_system(i, sides[pat[i]]) for i in idx]
     return sides, pat, perms, mats
+
+
+def shard_systems(weights, world_size):
+    """Split independent systems across ranks by weight (for a batch, the
+    bytes of each system's factor), with no communication: every rank
+    computes the same split from the same inputs.  Largest first, each to
+    the least-loaded rank (ties: lower system index first, lower rank
+    first).  Returns, per rank, its system indices in increasing order; the
+    largest load exceeds the mean by at most one system's weight."""
+    import heapq
+    w = [float(x) for x in weights]
+    if world_size < 1:
+        raise ValueError("world_size must be >= 1")
+    heap = [(0.0, r) for r in range(world_size)]
+    out = [[] for _ in range(world_size)]
+    for i in sorted(range(len(w)), key=lambda i: (-w[i], i)):
+        load, r = heapq.heappop(heap)
+        out[r].append(i)
+        heapq.heappush(heap, (load + w[i], r))
+    return [sorted(o) for o in out]
 
 
 class Batch:
