@@ -178,6 +178,15 @@ def max_over_ranks(dist, v):
     return float(t.item())
 
 
+def sum_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def cpu_oracle_run(mat, perm, fl, steps=1, threads=None):
     """FP64 factor + solve with the CPU oracle over OpenBLAS; seconds per step."""
     from oracle import oracle as O
@@ -576,9 +585,14 @@ def run_serve(args):
     nreq = 300 if not args.quick else 60
     sweep = []
     for rate in (25.0, 100.0, 400.0):
-        stream = SV.make_stream(nreq=nreq, seed=5, rate=rate, sides2d=(32, 256),
+        # with N ranks: N times the requests at N times the rate, each rank
+        # serving the share of factor ids serve.shard_stream gives it (weak
+        # scaling, no collective on the data path)
+        stream = SV.make_stream(nreq=nreq * ws, seed=5, rate=rate * ws, sides2d=(32, 256),
                                 sides3d=(16, 48), ncached=16, p_reuse=0.6, p_solve=0.2,
                                 max_rhs=32)
+        if ws > 1:
+            stream = SV.shard_stream(stream, ws, rank)
         S = SV.Server(nslots=4, budget_bytes=150 << 30, max_rhs=64)
         with Clocks(0) as clk:
             recs, wall = SV.run_stream(S, stream, realtime=True)
@@ -599,11 +613,22 @@ def run_serve(args):
             mat, _ = SV.request_inputs(f)
             be_o = max(be_o, float(O.backward_error(*mat, recs[q["req"]]["X"],
                                                     SV.request_inputs(byreq[q["req"]])).max()))
-        sweep.append({"rate_per_s": rate, "requests": nreq, "wall_s": wall, "all_ok": ok,
-                      "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                      "solve_p50_ms": float(np.percentile(lat_s, 50)) if len(lat_s) else None,
-                      "solve_p99_ms": float(np.percentile(lat_s, 99)) if len(lat_s) else None,
-                      "requests_per_s": nreq / wall, "solves_per_s": cols / wall,
+        # whole job over ranks: requests and columns summed, wall time,
+        # latencies and errors the worst rank's
+        nrq = sum_over_ranks(dist, len(stream))
+        cols = sum_over_ranks(dist, cols)
+        wall = max_over_ranks(dist, wall)
+        ok = max_over_ranks(dist, 0.0 if ok else 1.0) == 0.0
+        berr = max_over_ranks(dist, berr)
+        be_o = max_over_ranks(dist, be_o)
+        def worst(a, q):
+            # every rank joins each reduction (-1: no such requests here)
+            r = max_over_ranks(dist, float(np.percentile(a, q)) if len(a) else -1.0)
+            return r if r >= 0 else None
+        pct = {"p50_ms": worst(lat, 50), "p99_ms": worst(lat, 99),
+               "solve_p50_ms": worst(lat_s, 50), "solve_p99_ms": worst(lat_s, 99)}
+        sweep.append({"rate_per_s": rate * ws, "requests": int(nrq), "wall_s": wall, "all_ok": ok,
+                      **pct, "requests_per_s": nrq / wall, "solves_per_s": cols / wall,
                       "max_backward_error": berr, "oracle_sample_backward_error": be_o,
                       "server": st, "clocks": clk.summary()})
     top = sweep[-1]

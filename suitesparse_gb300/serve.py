@@ -164,6 +164,30 @@ def request_inputs(rq, _cache={}):
     return M.rhs(n, rq["nrhs"], rq["seed"] % 1000003)
 
 
+def factor_weight(pat):
+    """Estimated factor bytes of a request's pattern, for splitting streams
+    across GPUs: nnz(L) of a nested-dissection factor grows as n log n on a
+    2D grid and as n^(4/3) on a 3D grid."""
+    n = float(np.prod(pat["dims"]))
+    return n * np.log2(max(n, 2.0)) if len(pat["dims"]) == 2 else n ** (4.0 / 3.0)
+
+
+def shard_stream(stream, world_size, rank):
+    """This rank's requests of a stream split across world_size GPUs with no
+    communication: factor ids are split by estimated factor bytes
+    (batch.shard_systems, the same split on every rank) and every request
+    follows its factor id, so a solve runs where its factor lives."""
+    from .batch import shard_systems
+    w = {}
+    for q in stream:
+        if q["kind"] == "factor":
+            w[q["fid"]] = factor_weight(q["pat"])
+    fids = sorted(w)
+    part = shard_systems([w[f] for f in fids], world_size)[rank]
+    mine = {fids[i] for i in part}
+    return [q for q in stream if q["fid"] in mine]
+
+
 def run_stream(server, stream, realtime=True):
     """Submit the stream (at its arrival times when realtime) from one
     thread, collect every request's result in another.  Returns the

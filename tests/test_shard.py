@@ -77,3 +77,29 @@ def test_two_gloo_ranks_agree_without_exchange():
         s.bind(("127.0.0.1", 0))
         port = s.getsockname()[1]
     mp.spawn(_rank_main, args=(2, port, 4096 * 2), nprocs=2, join=True)
+
+
+@pytest.mark.parametrize("ws", [2, 3])
+def test_request_stream_split(ws):
+    """Request streams split by factor id: the ranks' shares partition the
+    stream, every solve lands on the rank of its factor, and the estimated
+    factor bytes are balanced."""
+    from suitesparse_gb300 import serve as SV
+    stream = SV.make_stream(nreq=300 * ws, seed=5, rate=100.0 * ws, sides2d=(32, 256),
+                            sides3d=(16, 48), ncached=16, p_reuse=0.6, p_solve=0.2,
+                            max_rhs=32)
+    shares = [SV.shard_stream(stream, ws, r) for r in range(ws)]
+    reqs = sorted(q["req"] for sh in shares for q in sh)
+    assert reqs == sorted(q["req"] for q in stream)
+    home = {}
+    for r, sh in enumerate(shares):
+        for q in sh:
+            if q["kind"] == "factor":
+                home[q["fid"]] = r
+    for r, sh in enumerate(shares):
+        for q in sh:
+            assert home[q["fid"]] == r
+    w = [sum(SV.factor_weight(q["pat"]) for q in sh if q["kind"] == "factor") for sh in shares]
+    wmax = max(SV.factor_weight(q["pat"]) for q in stream if q["kind"] == "factor")
+    assert max(w) - np.mean(w) <= wmax
+    assert SV.shard_stream(stream, ws, 1) == shares[1]
