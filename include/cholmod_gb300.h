@@ -382,6 +382,10 @@ int gb300_finish (cholmod_common *Common) ;
  *      CUDA graph captured once per pattern, right-hand-side count and
  *      factor precision (the first step of a solve with new buffers runs
  *      directly); 0 = every step launches its kernels one by one.
+ *  GB300_OPT_SWEEP_STREAMS [2]: with more than 16 right-hand sides the
+ *      sweeps run in passes of 16 columns; up to this many passes (1-4) run
+ *      at once, each on its own stream with its own dependency words and
+ *      update vectors.  The result is the same bit for bit with every value.
  *  GB300_OPT_PROFILE [0]: 1 = time every kernel launch of the factorization
  *      with CUDA events (summed per kernel kind, see gb300_get_profile); also
  *      clears the accumulated profile.
@@ -410,6 +414,7 @@ int gb300_finish (cholmod_common *Common) ;
 #define GB300_OPT_SUBTREE_WORK   8
 #define GB300_OPT_WARP_ROWS      9
 #define GB300_OPT_GRAPH          10
+#define GB300_OPT_SWEEP_STREAMS  11
 int gb300_set_option (cholmod_common *Common, int option, int64_t value) ;
 
 /* Supernodal symbolic analysis of A (stype < 0, lower) with a given final

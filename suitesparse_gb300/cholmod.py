@@ -27,6 +27,7 @@ GB300_OPT_TRACE, GB300_OPT_FACTOR, GB300_OPT_TENSOR = 5, 6, 7
 GB300_OPT_SUBTREE_WORK = 8
 GB300_OPT_WARP_ROWS = 9
 GB300_OPT_GRAPH = 10
+GB300_OPT_SWEEP_STREAMS = 11
 KIND_NAMES = {1: "assemble", 2: "factor_small", 3: "potrf_diag", 4: "trsm_rows", 5: "gemm_tile",
               6: "task_graph", 15: "whole_graph"}
 

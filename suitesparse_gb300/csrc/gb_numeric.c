@@ -31,6 +31,7 @@ gb_ctx *gb_ctx_new(void)
     c->factor_mode = 1;
     c->tc_mode = 0;
     c->graph_mode = 1;
+    c->sweep_streams = 2;
     return c;
 }
 
@@ -84,6 +85,8 @@ int gb300_set_option(cholmod_common *Common, int option, int64_t value)
     else if (option == GB300_OPT_FACTOR) c->factor_mode = value ? 1 : 0;
     else if (option == GB300_OPT_TENSOR) c->tc_mode = value ? 1 : 0;
     else if (option == GB300_OPT_GRAPH) c->graph_mode = value ? 1 : 0;
+    else if (option == GB300_OPT_SWEEP_STREAMS)
+        c->sweep_streams = (int)GB_MAX(1, GB_MIN(GB_SWEEP_STREAMS, value));
     else if (option == GB300_OPT_TRACE) c->trace_on = value ? 1 : 0;
     else if (option == GB300_OPT_PROFILE) {
         c->prof = value ? 1 : 0;
@@ -577,10 +580,10 @@ int gb_run_sweep(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, int fo
         /* the sweep's error word, shared by its passes */
         if (cudaMemsetAsync(P->d_err, 0, sizeof(int32_t), st) != cudaSuccess) return FALSE;
         const int npass = (nrhs + GB_SWEEP_COLS - 1) / GB_SWEEP_COLS;
-        const int ns = GB_MIN(npass, GB_SWEEP_STREAMS);
+        const int ns = GB_MIN(npass, ctx->sweep_streams);
         const size_t ureg = e * (size_t)GB_MAX(P->cbv_total, 1) * GB_SWEEP_COLS;
         const size_t words = (size_t)(P->nblk_total + 1) + (size_t)(P->nsuper + 1) + 4;
-        if (npass > 1 && sweep_streams(ctx) && gb_dev_grow(&P->d_U, &P->u_cap, ureg * ns)
+        if (ns > 1 && sweep_streams(ctx) && gb_dev_grow(&P->d_U, &P->u_cap, ureg * ns)
             && gb_dev_grow((void **)&P->d_sws, &P->sws_cap, sizeof(int32_t) * words * ns)) {
             /* passes of GB_SWEEP_COLS columns, up to GB_SWEEP_STREAMS of them
              * at once on their own streams, each with its own dependency

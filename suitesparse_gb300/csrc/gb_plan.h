@@ -271,6 +271,7 @@ struct gb_ctx {
     int tc_mode;                 /* 1 = FP32 tile products on the tensor cores (default 0) */
     int trace_on;                /* record per-task times of the sweeps */
     int graph_mode;              /* 1 = refinement steps replayed from a CUDA graph (default) */
+    int sweep_streams;           /* passes of 16 columns run at once (1..GB_SWEEP_STREAMS) */
     unsigned long long *d_trace; /* device trace buffer (3 x tasks) */
     size_t trace_cap;
     int64_t trace_n[2];          /* tasks traced by the last forward/backward sweep */

@@ -210,6 +210,10 @@ def test_concurrent_sweep_passes(golden, lib, oracle_mod):
         Xk = CH.solve(L, B[:, k0:k0 + 16], c)
         np.testing.assert_array_equal(X[:, k0:k0 + 16], Xk)
     assert oracle_mod.backward_error(*mat, X, B).max() <= 1e-14
+    for k in (1, 2):                                  # passes one after another
+        c.set_option(CH.GB300_OPT_SWEEP_STREAMS, k)
+        np.testing.assert_array_equal(CH.solve(L, B, c), X)
+    c.set_option(CH.GB300_OPT_SWEEP_STREAMS, 4)
     assert CH.factorize_mixed(A, L, c) == 1
     X1, i1 = CH.solve_refined(A, L, B, c, tol=TOL)
     X2, i2 = CH.solve_refined(A, L, B, c, tol=TOL)
