@@ -47,18 +47,37 @@ METRIC = "factor TFLOP/s + solves/s at 1e-12 backward err, FP32+IR vs FP64; p50/
 WORKLOAD = "c2: 3D 7-point variable-coefficient Laplacian 64^3 (n=262144), METIS"
 
 
+def measured_peaks():
+    """Roofline denominators: MEASURED_PEAKS.json (copy bandwidth and cuBLAS
+    bf16 GEMM rate measured on the GB300s) when present, else the
+    fallback figures of one earlier GB300 measurement."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]),
+                "bf16_tflops_sustained": float(d.get("bf16_tflops_sustained",
+                                                     d["bf16_tflops"])),
+                "source": "measured (MEASURED_PEAKS.json)"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+                "source": "fallback (no MEASURED_PEAKS.json on this machine)"}
+
+
 def load_case(name=None):
+    """(reference analysis record, matrix, permutation); the record carries
+    the reference's supernode partition as "Super" (None for p40)."""
     name = name or CASE
     from suitesparse_gb300 import matrices as M
     if name == "p40":
         # profiling case: 3D 7-point variable-coefficient Laplacian 40^3,
         # geometric nested dissection (factor > L2, device footprint < 1 GB)
         mat = M.laplace3d(40, seed=1, lo=1e-2, hi=1e2)
-        return {"fl": None}, mat, M.grid_nd_perm((40, 40, 40))
+        return {"fl": None, "Super": None}, mat, M.grid_nd_perm((40, 40, 40))
     gold = json.load(open(os.path.join(ROOT, "tests", "golden", "golden.json")))[name]
     arrays = np.load(os.path.join(ROOT, "tests", "golden", "golden_arrays.npz"))
     n, Ap, Ai, Ax = M.config_matrix(name)
     perm = arrays[name + "_Perm"].astype(np.int64)
+    gold["Super"] = arrays[name + "_Super"].astype(np.int64)
     return gold, (n, Ap, Ai, Ax), perm
 
 
@@ -70,13 +89,15 @@ class Clocks:
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu=0):
-        self.gpu = gpu
+        # nvidia-smi numbers GPUs physically and ignores CUDA_VISIBLE_DEVICES:
+        # name the device this process runs on by its PCI bus id
+        self.gpu = device_bus_id(gpu) or str(gpu)
         self.proc = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                ["nvidia-smi", "-i", self.gpu, "--query-gpu=" + self.Q,
                  "--format=csv,noheader,nounits", "-lms", "200"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
@@ -121,6 +142,18 @@ def cudart():
         except OSError:
             continue
     return None
+
+
+def device_bus_id(ordinal):
+    """PCI bus id of CUDA device `ordinal` of this process (after
+    CUDA_VISIBLE_DEVICES), or None."""
+    rt = cudart()
+    if rt is None:
+        return None
+    buf = ctypes.create_string_buffer(64)
+    if rt.cudaDeviceGetPCIBusId(buf, ctypes.c_int(64), ctypes.c_int(ordinal)) != 0:
+        return None
+    return buf.value.decode() or None
 
 
 def pin(rt, arr):
@@ -187,25 +220,20 @@ def sum_over_ranks(dist, v):
     return float(t.item())
 
 
-def cpu_oracle_run(mat, perm, fl, steps=1, threads=None):
-    """FP64 factor + solve with the CPU oracle over OpenBLAS; seconds per step."""
+def cpu_oracle_run(mat, perm, Super, steps=1, threads=None):
+    """FP64 factor + solve with the CPU oracle over OpenBLAS; seconds per step.
+    The symbolic factor is the reference's, rebuilt by the oracle from the
+    reference's permutation and supernode partition (fixtures): this path
+    loads no product library."""
     from oracle import oracle as O
-    from suitesparse_gb300 import cholmod as CH
     from suitesparse_gb300 import matrices as M
     n, Ap, Ai, Ax = mat
     O.build()
     O.lib(use_blas=True)
     threads = threads or os.cpu_count() or 1
     O.blas_threads(threads)
-    c = CH.Common()
-    A = CH.sparse(n, Ap, Ai, Ax, c)
-    L = CH.analyze_perm(A, perm, c)
-    f = CH.factor_arrays(L, with_x=False)
-    CH.free_factor(L, c)
-    CH.free_sparse(A, c)
-    sym = {k: f[k] for k in ("Super", "Pi", "Px", "Ls")}
-    sym["n"] = n
     Sp, Si, Sx = O.permute_lower(n, Ap, Ai, Ax, perm)
+    sym = O.symbolic(n, Sp, Si, Super)
     B = M.rhs(n, 1, 1)
     tf, ts, be = [], [], None
     for _ in range(steps):
@@ -226,7 +254,7 @@ def run_reference(args):
         return 0
     gold, mat, perm = load_case()
     fl = gold["fl"]
-    tf, ts, be, threads = cpu_oracle_run(mat, perm, fl, steps=args.warmup + args.steps)
+    tf, ts, be, threads = cpu_oracle_run(mat, perm, gold["Super"], steps=args.warmup + args.steps)
     tf, ts = tf[args.warmup:], ts[args.warmup:]
     t_step = [a + b for a, b in zip(tf, ts)]
     value = fl / statistics.mean(tf) / 1e12
@@ -300,7 +328,7 @@ def run_gpu(args):
     barrier(dist)
     l0 = c.stats()[5]
     fac_ms, sol_ms, e2e_s, infos = [], [], [], []
-    with Clocks(int(os.environ.get("LOCAL_RANK", "0")) if ws == 1 else 0) as clk:
+    with Clocks(0) as clk:
         t_all = time.perf_counter()
         for _ in range(args.steps):
             f_ms, s_ms, w_s, X, rinfo = step_mixed()
@@ -373,6 +401,7 @@ def run_gpu(args):
     c.set_option(CH.GB300_OPT_PROFILE, 0)
     peak32 = CH.fma_peak("s")
     peak64 = CH.fma_peak("d")
+    peaks = measured_peaks()
     g_ms, g_n = prof.get("whole_graph", prof.get("task_graph", (0.0, 0)))
     achieved = info["fl_taskgraph"] / (g_ms * 1e-3) / 1e12 if g_ms else None
     prof_total = sum(v[0] for v in prof.values()) or 1.0
@@ -419,10 +448,13 @@ def run_gpu(args):
         "roofline": {"kernel": "k_fdag<float> (whole-factorization task graph: assembly, "
                                "small supernodes, tile LL', panel solves, tile and "
                                "update-block products; achieved = tile-task flops / launch time)",
-                     "bound": "compute (FP32 FMA pipe, SIMT)", "achieved": achieved,
-                     "peak": peak32, "unit": "TFLOP/s",
-                     "frac": (achieved / peak32) if (achieved and peak32) else None,
-                     "peak_source": "measured: FMA-chain probe gb300_fma_peak in this run",
+                     "bound": "tensor", "achieved": achieved,
+                     "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                     "frac": (achieved / peaks["bf16_tflops"]) if achieved else None,
+                     "peak_source": peaks["source"] + ": dense bf16 tensor rate, burst",
+                     "fp32_fma_peak": peak32,
+                     "frac_of_fp32_fma_peak": (achieved / peak32) if (achieved and peak32) else None,
+                     "fp32_fma_peak_source": "measured: FMA-chain probe gb300_fma_peak in this run",
                      "traffic": K_FDAG_C2_DRAM_BYTES if CASE == "c2" else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
                                        "k_fdag launch of this workload "
@@ -437,12 +469,21 @@ def run_gpu(args):
         "clocks": clk.summary(),
     }
     if args.cpu_baseline and rank == 0:
-        tf, ts, bec, threads = cpu_oracle_run(mat, perm, fl, steps=1)
+        Super = gold["Super"] if gold.get("Super") is not None else \
+            CH.factor_arrays(L, with_x=False)["Super"]
+        tf, ts, bec, threads = cpu_oracle_run(mat, perm, Super, steps=1)
         line["cpu_baseline"] = {"value": fl / tf[0] / 1e12, "unit": "TFLOP/s", "cores": threads,
                                 "kind": "port",
-                                "sample": "one full c2 FP64 factorization (oracle over "
+                                "sample": f"one full {CASE} FP64 factorization (oracle over "
                                           "OpenBLAS, the reference's left-looking algorithm)",
                                 "solve_s": ts[0]}
+        # same precision on both sides: the GPU's plain FP64 factorization
+        # against the CPU's FP64 factorization of the same matrix
+        line["fp64_vs_reference"] = {
+            "factor": line["fp64"]["factor_tflops"] / line["cpu_baseline"]["value"],
+            "solves_per_s": line["fp64"]["solves_per_s"] / (1.0 / (tf[0] + ts[0])),
+            "note": "GPU FP64 factor + solve vs the CPU FP64 factor + solve (oracle over "
+                    "OpenBLAS, all host cores), both on this box"}
     CH.free_factor(L, c)
     CH.free_sparse(A, c)
     c.finish()
@@ -653,10 +694,7 @@ def run_serve(args):
 def measured_hbm_peak():
     """The measured copy bandwidth of the GB300s (GB/s), else the
     fallback figure of one earlier GB300 measurement."""
-    try:
-        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
-    except (OSError, KeyError, ValueError):
-        return 6800.0
+    return measured_peaks()["hbm_gbs"]
 
 
 def run_spsolve(args):

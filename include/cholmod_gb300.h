@@ -386,6 +386,10 @@ int gb300_finish (cholmod_common *Common) ;
  *      sweeps run in passes of 16 columns; up to this many passes (1-4) run
  *      at once, each on its own stream with its own dependency words and
  *      update vectors.  The result is the same bit for bit with every value.
+ *  GB300_OPT_PIVOT_LOG2 [23]: gb300_factorize_mixed switches to the FP64
+ *      factor when the smallest pivot of the FP32 factor satisfies
+ *      min L(k,k)^2 <= 2^-value * max L(k,k)^2 (23: the single-precision
+ *      epsilon; 0 makes every FP32 factor take the FP64 path).
  *  GB300_OPT_PROFILE [0]: 1 = time every kernel launch of the factorization
  *      with CUDA events (summed per kernel kind, see gb300_get_profile); also
  *      clears the accumulated profile.
@@ -415,6 +419,7 @@ int gb300_finish (cholmod_common *Common) ;
 #define GB300_OPT_WARP_ROWS      9
 #define GB300_OPT_GRAPH          10
 #define GB300_OPT_SWEEP_STREAMS  11
+#define GB300_OPT_PIVOT_LOG2     12
 int gb300_set_option (cholmod_common *Common, int option, int64_t value) ;
 
 /* Supernodal symbolic analysis of A (stype < 0, lower) with a given final
@@ -455,11 +460,26 @@ cholmod_dense *gb300_solve (int sys, cholmod_factor *L, cholmod_dense *B,
  * stalls (no residual reduction in 2 steps, or a pivot <= eps*max diagonal
  * in the FP32 factor) it refactors in FP64 and finishes with that factor.
  * info (optional, 4 doubles): [0] iterations, [1] final backward error,
- * [2] 1 if the FP64 fallback ran, [3] max backward error over columns. */
+ * [2] 1 if the FP64 fallback ran, [3] max backward error over columns.
+ * A NaN or infinity in the residual, x, b or A makes a column's backward
+ * error NaN, which never meets tol: refinement goes on to the FP64
+ * fallback (or stops at once when b itself is not finite) and the call
+ * ends with Common->status = CHOLMOD_DSMALL and info[1] = NaN. */
 int gb300_factorize_mixed (cholmod_sparse *A, cholmod_factor *L,
     cholmod_common *Common) ;
 cholmod_dense *gb300_solve_refined (cholmod_sparse *A, cholmod_factor *L,
     cholmod_dense *B, double tol, double *info, cholmod_common *Common) ;
+
+/* Why the mixed factor of L is in FP64: 0 = it is not (the FP32 factor is
+ * in use), 1 = the FP32 factorization failed (a pivot was not positive),
+ * 2 = an FP32 pivot was small (GB300_OPT_PIVOT_LOG2), 3 = refinement
+ * stalled (the backward error did not halve in 2 steps).  -1 when L has no
+ * mixed factor. */
+#define GB300_REASON_NONE        0
+#define GB300_REASON_FP32_FAILED 1
+#define GB300_REASON_SMALL_PIVOT 2
+#define GB300_REASON_STALLED     3
+int gb300_mixed_reason (cholmod_factor *L, cholmod_common *Common) ;
 
 /* gb300_solve_refined writing into *X_Handle, as cholmod_l_solve2 reuses
  * its X (CHOLMOD/Cholesky/cholmod_solve.c:298, ensure_dense): an X of n
@@ -606,7 +626,9 @@ int gb300_wait_probe (int64_t polls, int32_t *out) ;
  *         serves as row i of the residual;
  *   X, B: n x nrhs, column-major, leading dimensions ldx, ldb >= n;
  *   berr: nrhs doubles, receives |b - A x|_inf / (|A|_inf |x|_inf + |b|_inf)
- *         per column -- the measure gb300_solve_refined reports in info.
+ *         per column -- the measure gb300_solve_refined reports in info; a
+ *         NaN or infinite entry in that column of x or b, or in A, gives
+ *         NaN, so a non-finite solution never passes a tolerance test.
  * The work is queued on stream (a cudaStream_t, NULL for the default
  * stream) and the call returns without waiting.  The reduction scratch is a
  * fixed device array inside this library, sized for GB300_BERR_MAX_RHS

@@ -15,7 +15,8 @@ the scipy wheel, whose exported names carry a ``scipy_`` prefix, so every
 undefined BLAS/LAPACK symbol ``xyz_`` of the compiled objects is renamed to
 ``scipy_xyz_`` with objcopy before linking against that library.
 
-Usage: python oracle/build_ref.py [REFERENCE_ROOT]   (default /root/reference)
+Usage: python oracle/build_ref.py [REFERENCE_ROOT]
+(default: $CHOLMOD_REFERENCE_ROOT, else /root/reference)
 Outputs: oracle/_ref/libcholmod_ref.so, oracle/_ref/ref_dump (driver).
 """
 import glob
@@ -26,6 +27,12 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+
+
+def reference_root():
+    """Where the reference sources are read from (only this recipe, the
+    fixture generators and the header-layout test read them)."""
+    return os.environ.get("CHOLMOD_REFERENCE_ROOT", "/root/reference")
 
 
 def openblas_path():
@@ -68,7 +75,7 @@ def run(cmd):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else reference_root()
     if not os.path.isdir(os.path.join(ref, "CHOLMOD")):
         print("reference sources not present; oracle/_ref not built")
         return 1

@@ -128,3 +128,90 @@ int oracle_super_solve(int dtype, int lower, Int n, Int nsuper, const Int *Super
     if (dtype == 4) return sweep_s(lower, n, nsuper, Super, Pi, Px, Ls, Lx, nrhs, X, ldx);
     return sweep_d(lower, n, nsuper, Super, Pi, Px, Ls, Lx, nrhs, X, ldx);
 }
+
+/* Row pattern of a supernodal factor from its column partition.
+ *
+ * Given S = tril(P A P') (sorted lower CSC, n columns) and the supernode
+ * partition Super [nsuper+1] that the reference's analysis chose, the rows
+ * of supernode s are its own columns k1..k2-1 followed by every row i >= k2
+ * that is nonzero in some column of s of S or in the pattern of a child
+ * supernode (the supernodal form of the column-pattern recurrence
+ * struct(L(:,j)) = struct(S(j:n,j)) U struct(L(:,c)) \ {c} over the etree
+ * children c of j), in ascending order, as cholmod_super_symbolic stores
+ * L->s (CHOLMOD/Supernodal/cholmod_super_symbolic.c:760-900 build the same
+ * sets by row subtrees).  Children precede their parent in the postordered
+ * numbering.  Output: Pi [nsuper+1], Px [nsuper+1] and *Ls_out (malloc'd,
+ * *ssize entries; free with oracle_free).  Returns 0, or -1 (bad input or
+ * out of memory).  Test infrastructure: lets the reference arm of the
+ * benchmark and the CPU checks rebuild the reference's symbolic factor from
+ * a fixture of Super alone, without the product library. */
+static int cmp_int(const void *a, const void *b)
+{
+    Int x = *(const Int *)a, y = *(const Int *)b;
+    return x < y ? -1 : x > y;
+}
+
+int oracle_super_pattern(Int n, const Int *Sp, const Int *Si, Int nsuper, const Int *Super,
+                         Int *Pi, Int *Px, Int **Ls_out, Int *ssize)
+{
+    *Ls_out = NULL;
+    *ssize = 0;
+    if (n < 0 || nsuper < 0 || Super[0] != 0 || Super[nsuper] != n) return -1;
+    Int *smap = malloc(sizeof(Int) * (n + 1));
+    Int *mark = malloc(sizeof(Int) * (n + 1));
+    Int *head = malloc(sizeof(Int) * (nsuper + 1));   /* children lists */
+    Int *next = malloc(sizeof(Int) * (nsuper + 1));
+    Int cap = 4 * (n + 16), len = 0;
+    Int *Ls = malloc(sizeof(Int) * cap);
+    int ok = smap && mark && head && next && Ls;
+    for (Int s = 0; ok && s < nsuper; s++) {
+        if (Super[s + 1] <= Super[s]) { ok = 0; break; }
+        for (Int j = Super[s]; j < Super[s + 1]; j++) smap[j] = s;
+        head[s] = -1;
+    }
+    for (Int i = 0; ok && i < n; i++) mark[i] = -1;
+    Pi[0] = 0;
+    Px[0] = 0;
+    for (Int s = 0; ok && s < nsuper; s++) {
+        const Int k1 = Super[s], k2 = Super[s + 1];
+        const Int p0 = len;
+        /* worst case: every row of the matrix */
+        if (cap - len < n) {
+            cap = 2 * cap + n;
+            Int *t = realloc(Ls, sizeof(Int) * cap);
+            if (!t) { ok = 0; break; }
+            Ls = t;
+        }
+        for (Int k = k1; k < k2; k++) { Ls[len++] = k; mark[k] = s; }
+        for (Int k = k1; k < k2; k++)
+            for (Int p = Sp[k]; p < Sp[k + 1]; p++) {
+                const Int i = Si[p];
+                if (i < k || i >= n) { if (i < k) continue; ok = 0; break; }
+                if (mark[i] != s) { mark[i] = s; Ls[len++] = i; }
+            }
+        for (Int c = head[s]; ok && c >= 0; c = next[c]) {
+            const Int nscol_c = Super[c + 1] - Super[c];
+            for (Int p = Pi[c] + nscol_c; p < Pi[c + 1]; p++) {
+                const Int i = Ls[p];
+                if (i >= k2 && mark[i] != s) { mark[i] = s; Ls[len++] = i; }
+            }
+        }
+        if (!ok) break;
+        qsort(Ls + p0 + (k2 - k1), len - p0 - (k2 - k1), sizeof(Int), cmp_int);
+        Pi[s + 1] = len;
+        Px[s + 1] = Px[s] + (k2 - k1) * (len - p0);
+        /* parent: the supernode of the first row below the diagonal block */
+        if (len - p0 > k2 - k1) {
+            const Int par = smap[Ls[p0 + (k2 - k1)]];
+            next[s] = head[par];
+            head[par] = s;
+        }
+    }
+    free(smap); free(mark); free(head); free(next);
+    if (!ok) { free(Ls); return -1; }
+    *Ls_out = Ls;
+    *ssize = len;
+    return 0;
+}
+
+void oracle_free(void *p) { free(p); }

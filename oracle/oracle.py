@@ -57,6 +57,8 @@ def lib(use_blas=True):
         _lib.oracle_super_numeric.restype = C.c_int
         _lib.oracle_super_solve.restype = C.c_int
         _lib.oracle_has_blas.restype = C.c_int
+        _lib.oracle_super_pattern.restype = C.c_int
+        _lib.oracle_free.argtypes = [C.c_void_p]
     set_blas(use_blas)
     return _lib
 
@@ -130,6 +132,30 @@ def sweep(sym, Lx, X, lower, dtype="d", use_blas=True):
     if st != 0:
         raise RuntimeError("oracle sweep failed")
     return X
+
+
+def symbolic(n, Sp, Si, Super):
+    """The reference's supernodal symbolic factor (dict with n, Super, Pi, Px,
+    Ls) rebuilt from S = tril(PAP')'s pattern and the reference's supernode
+    partition Super (a fixture), without the product library."""
+    L = _lib if _lib is not None else lib()
+    Sp = np.ascontiguousarray(Sp, np.int64)
+    Si = np.ascontiguousarray(Si, np.int64)
+    Super = np.ascontiguousarray(Super, np.int64)
+    nsuper = len(Super) - 1
+    Pi = np.zeros(nsuper + 1, np.int64)
+    Px = np.zeros(nsuper + 1, np.int64)
+    ls = C.POINTER(C.c_int64)()
+    ssize = C.c_int64(0)
+    st = L.oracle_super_pattern(C.c_int64(n), _p(Sp, C.c_int64), _p(Si, C.c_int64),
+                                C.c_int64(nsuper), _p(Super, C.c_int64), _p(Pi, C.c_int64),
+                                _p(Px, C.c_int64), C.byref(ls), C.byref(ssize))
+    if st != 0:
+        raise RuntimeError("oracle symbolic failed")
+    Ls = np.ctypeslib.as_array(ls, shape=(ssize.value,)).copy() if ssize.value else \
+        np.zeros(0, np.int64)
+    L.oracle_free(ls)
+    return {"n": n, "Super": Super, "Pi": Pi, "Px": Px, "Ls": Ls}
 
 
 def permute_lower(n, Ap, Ai, Ax, perm):

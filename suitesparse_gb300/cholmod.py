@@ -28,6 +28,9 @@ GB300_OPT_SUBTREE_WORK = 8
 GB300_OPT_WARP_ROWS = 9
 GB300_OPT_GRAPH = 10
 GB300_OPT_SWEEP_STREAMS = 11
+GB300_OPT_PIVOT_LOG2 = 12
+GB300_REASON_NONE, GB300_REASON_FP32_FAILED = 0, 1
+GB300_REASON_SMALL_PIVOT, GB300_REASON_STALLED = 2, 3
 KIND_NAMES = {1: "assemble", 2: "factor_small", 3: "potrf_diag", 4: "trsm_rows", 5: "gemm_tile",
               6: "task_graph", 15: "whole_graph"}
 
@@ -97,6 +100,7 @@ def lib():
         "gb300_solve_refined2": (C.c_int, [SP, FP, DP, C.c_double, C.POINTER(C.c_double),
                                            C.POINTER(DP), vp]),
         "gb300_release_factor": (C.c_int, [FP, vp]),
+        "gb300_mixed_reason": (C.c_int, [FP, vp]),
         "gb300_get_profile": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]),
         "gb300_factor_info": (C.c_int, [FP, vp, C.POINTER(C.c_double), C.c_int]),
         "gb300_fma_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
@@ -367,4 +371,10 @@ def solve_refined(A, L, B, common, tol=1e-12):
         raise RuntimeError(f"refined solve failed, status {common.status}")
     out = dense_array(X)
     free_dense(X, common)
-    return out, {"iterations": int(info[0]), "berr": info[1], "fp64_fallback": bool(info[2])}
+    return out, {"iterations": int(info[0]), "berr": info[1], "fp64_fallback": bool(info[2]),
+                 "status": common.status}
+
+
+def mixed_reason(L, common):
+    """Why the mixed factor is in FP64 (GB300_REASON_*), -1 without one."""
+    return lib().gb300_mixed_reason(L, common.ptr)

@@ -26,6 +26,22 @@ __device__ __forceinline__ int lower_bound_i32(const int32_t *a, int lo, int hi,
     return lo;
 }
 
+// Maximum that keeps NaN: fmax(a, NaN) returns a, which would let a
+// solution holding NaN pass a backward-error test.  Operands are >= 0 or
+// NaN.
+__device__ __forceinline__ double gb_maxnan(double a, double b)
+{
+    return (b > a || b != b) ? b : a;
+}
+
+// Bit pattern for the 64-bit atomicMax of a maximum that is >= 0 or NaN:
+// any NaN becomes the positive quiet NaN, which orders above +inf as an
+// unsigned integer, so it survives every later atomicMax.
+__device__ __forceinline__ unsigned long long gb_maxbits(double v)
+{
+    return v != v ? 0x7FF8000000000000ull : (unsigned long long)__double_as_longlong(v);
+}
+
 template <typename T> __device__ __forceinline__ T gb_sqrt(T x);
 template <> __device__ __forceinline__ double gb_sqrt<double>(double x) { return sqrt(x); }
 template <> __device__ __forceinline__ float gb_sqrt<float>(float x) { return sqrtf(x); }

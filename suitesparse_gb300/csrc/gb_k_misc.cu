@@ -100,8 +100,8 @@ __global__ void k_diag_minmax(int nsuper, const int64_t *__restrict__ Super,
         const T *panel = Lx + Px[s];
         for (int j = lane; j < nscol; j += 32) {
             const double d = (double)panel[j + j * nsrow];
-            lo = fmin(lo, d * d);
-            hi = fmax(hi, d * d);
+            if (d != d) lo = 0.0;                       // NaN pivot: as small as can be
+            else { lo = fmin(lo, d * d); hi = fmax(hi, d * d); }
         }
     }
     smin[threadIdx.x] = lo;
@@ -165,7 +165,8 @@ __global__ void k_diag_range(int nsuper, const int64_t *__restrict__ Super,
 
 // per column r: out[3r] = max|R|, out[3r+1] = max|X|, out[3r+2] = max|B|
 // (out zeroed first); grid-wide, 64-bit atomics on the bit patterns of the
-// nonnegative maxima.
+// nonnegative maxima.  A NaN anywhere makes its maximum NaN (gb_maxnan,
+// gb_maxbits), so a non-finite solution can never pass the test.
 __global__ void k_colmax3(int64_t n, const double *__restrict__ R, int64_t ldr,
                           const double *__restrict__ X, int64_t ldx,
                           const double *__restrict__ B, int64_t ldb, double *out)
@@ -175,9 +176,9 @@ __global__ void k_colmax3(int64_t n, const double *__restrict__ R, int64_t ldr,
     double a = 0, b = 0, c = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        a = fmax(a, fabs(R[i + r * ldr]));
-        b = fmax(b, fabs(X[i + r * ldx]));
-        c = fmax(c, fabs(B[i + r * ldb]));
+        a = gb_maxnan(a, fabs(R[i + r * ldr]));
+        b = gb_maxnan(b, fabs(X[i + r * ldx]));
+        c = gb_maxnan(c, fabs(B[i + r * ldb]));
     }
     sm[0][threadIdx.x] = a;
     sm[1][threadIdx.x] = b;
@@ -186,13 +187,12 @@ __global__ void k_colmax3(int64_t n, const double *__restrict__ R, int64_t ldr,
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
         if (threadIdx.x < o)
             for (int q = 0; q < 3; q++)
-                sm[q][threadIdx.x] = fmax(sm[q][threadIdx.x], sm[q][threadIdx.x + o]);
+                sm[q][threadIdx.x] = gb_maxnan(sm[q][threadIdx.x], sm[q][threadIdx.x + o]);
         __syncthreads();
     }
     if (threadIdx.x == 0)
         for (int q = 0; q < 3; q++)
-            atomicMax((unsigned long long *)&out[3 * r + q],
-                      (unsigned long long)__double_as_longlong(sm[q][0]));
+            atomicMax((unsigned long long *)&out[3 * r + q], gb_maxbits(sm[q][0]));
 }
 
 // max over rows of sum |A(i,:)| (for the backward error denominator)
@@ -205,16 +205,16 @@ __global__ void k_anorm_inf(int64_t n, const int64_t *__restrict__ Rp,
          i += (int64_t)gridDim.x * blockDim.x) {
         double acc = 0;
         for (int64_t p = Rp[i]; p < Rp[i + 1]; p++) acc += fabs(Rx[p]);
-        best = fmax(best, acc);
+        best = gb_maxnan(best, acc);
     }
     sm[threadIdx.x] = best;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + o]);
+        if (threadIdx.x < o) sm[threadIdx.x] = gb_maxnan(sm[threadIdx.x], sm[threadIdx.x + o]);
         __syncthreads();
     }
     if (threadIdx.x == 0)
-        atomicMax((unsigned long long *)out, (unsigned long long)__double_as_longlong(sm[0]));
+        atomicMax((unsigned long long *)out, gb_maxbits(sm[0]));
 }
 
 // Segmented forms (one segment per independent block of A): block
@@ -231,9 +231,9 @@ __global__ void k_colmax3_seg(const gb_seg_chunk *__restrict__ chunks, int nrhs,
     const int r = blockIdx.y;
     double a = 0, b = 0, c = 0;
     for (int64_t i = ch.lo + threadIdx.x; i < ch.hi; i += blockDim.x) {
-        a = fmax(a, fabs(R[i + r * ldr]));
-        b = fmax(b, fabs(X[i + r * ldx]));
-        c = fmax(c, fabs(B[i + r * ldb]));
+        a = gb_maxnan(a, fabs(R[i + r * ldr]));
+        b = gb_maxnan(b, fabs(X[i + r * ldx]));
+        c = gb_maxnan(c, fabs(B[i + r * ldb]));
     }
     sm[0][threadIdx.x] = a;
     sm[1][threadIdx.x] = b;
@@ -242,13 +242,13 @@ __global__ void k_colmax3_seg(const gb_seg_chunk *__restrict__ chunks, int nrhs,
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
         if (threadIdx.x < o)
             for (int q = 0; q < 3; q++)
-                sm[q][threadIdx.x] = fmax(sm[q][threadIdx.x], sm[q][threadIdx.x + o]);
+                sm[q][threadIdx.x] = gb_maxnan(sm[q][threadIdx.x], sm[q][threadIdx.x + o]);
         __syncthreads();
     }
     if (threadIdx.x == 0)
         for (int q = 0; q < 3; q++)
             atomicMax((unsigned long long *)&out[3 * ((int64_t)ch.seg * nrhs + r) + q],
-                      (unsigned long long)__double_as_longlong(sm[q][0]));
+                      gb_maxbits(sm[q][0]));
 }
 
 __global__ void k_anorm_seg(const gb_seg_chunk *__restrict__ chunks, const int64_t *__restrict__ Rp,
@@ -260,16 +260,16 @@ __global__ void k_anorm_seg(const gb_seg_chunk *__restrict__ chunks, const int64
     for (int64_t i = ch.lo + threadIdx.x; i < ch.hi; i += blockDim.x) {
         double acc = 0;
         for (int64_t p = Rp[i]; p < Rp[i + 1]; p++) acc += fabs(Rx[p]);
-        best = fmax(best, acc);
+        best = gb_maxnan(best, acc);
     }
     sm[threadIdx.x] = best;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + o]);
+        if (threadIdx.x < o) sm[threadIdx.x] = gb_maxnan(sm[threadIdx.x], sm[threadIdx.x + o]);
         __syncthreads();
     }
     if (threadIdx.x == 0)
-        atomicMax((unsigned long long *)&out[ch.seg], (unsigned long long)__double_as_longlong(sm[0]));
+        atomicMax((unsigned long long *)&out[ch.seg], gb_maxbits(sm[0]));
 }
 
 // dst[q] = src[map[q]] (device-side value permutation)

@@ -10,7 +10,8 @@
 
 // Reduction scratch: per column the bit patterns of max|b - A x|, max|x|,
 // max|b| (nonnegative doubles, for which IEEE order equals unsigned
-// order), the bit pattern of |A|_inf, and the count of finished blocks.
+// order; a NaN is stored as the positive quiet NaN, above +inf), the bit
+// pattern of |A|_inf, and the count of finished blocks.
 // All zero when a call starts: zero at module load, and the last block of
 // every call zeroes what the call used.
 struct gb_berr_scratch {
@@ -21,6 +22,16 @@ struct gb_berr_scratch {
 };
 
 static __device__ __align__(256) gb_berr_scratch gb_berr_scr;
+
+// Maximum that keeps NaN (fmax(a, NaN) returns a); operands are >= 0 or NaN.
+__device__ __forceinline__ double maxnan(double a, double b) { return (b > a || b != b) ? b : a; }
+
+// Bit pattern for atomicMax: a NaN becomes the positive quiet NaN, which
+// orders above +inf as an unsigned integer and so survives the reduction.
+__device__ __forceinline__ unsigned long long maxbits(double v)
+{
+    return v != v ? 0x7FF8000000000000ull : (unsigned long long)__double_as_longlong(v);
+}
 
 // Block (bx, r): rows bx, bx + gridDim.x, ... of column r.  A holds both
 // triangles in compressed-column form; by symmetry column i is row i, so
@@ -44,10 +55,10 @@ k_berr_noalloc(int64_t n, const int64_t *__restrict__ Ap, const int64_t *__restr
             acc += Ax[p] * x[Ai[p]];
             rs += fabs(Ax[p]);
         }
-        mr = fmax(mr, fabs(b[i] - acc));
-        mx = fmax(mx, fabs(x[i]));
-        mb = fmax(mb, fabs(b[i]));
-        an = fmax(an, rs);
+        mr = maxnan(mr, fabs(b[i] - acc));
+        mx = maxnan(mx, fabs(x[i]));
+        mb = maxnan(mb, fabs(b[i]));
+        an = maxnan(an, rs);
     }
     sm[0][threadIdx.x] = mr;
     sm[1][threadIdx.x] = mx;
@@ -56,13 +67,13 @@ k_berr_noalloc(int64_t n, const int64_t *__restrict__ Ap, const int64_t *__restr
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
         if (threadIdx.x < o)
-            for (int q = 0; q < 4; q++) sm[q][threadIdx.x] = fmax(sm[q][threadIdx.x], sm[q][threadIdx.x + o]);
+            for (int q = 0; q < 4; q++) sm[q][threadIdx.x] = maxnan(sm[q][threadIdx.x], sm[q][threadIdx.x + o]);
         __syncthreads();
     }
     if (threadIdx.x == 0) {
         for (int q = 0; q < 3; q++)
-            atomicMax(&S->colmax[3 * r + q], (unsigned long long)__double_as_longlong(sm[q][0]));
-        if (r == 0) atomicMax(&S->anorm, (unsigned long long)__double_as_longlong(sm[3][0]));
+            atomicMax(&S->colmax[3 * r + q], maxbits(sm[q][0]));
+        if (r == 0) atomicMax(&S->anorm, maxbits(sm[3][0]));
         __threadfence();
         const unsigned int total = gridDim.x * gridDim.y;
         last = atomicAdd(&S->done, 1u) == total - 1;
@@ -78,7 +89,10 @@ k_berr_noalloc(int64_t n, const int64_t *__restrict__ Ap, const int64_t *__restr
         const double xmax = __longlong_as_double((long long)cm[3 * c + 1]);
         const double bmax = __longlong_as_double((long long)cm[3 * c + 2]);
         const double den = anorm * xmax + bmax;
-        berr[c] = den > 0 ? rmax / den : 0.0;
+        // a NaN or infinite term (in x, b or A) gives NaN: never converged
+        const bool finite = isfinite(rmax) && isfinite(xmax) && isfinite(bmax) && isfinite(anorm)
+                            && isfinite(den);
+        berr[c] = !finite ? __longlong_as_double(0x7FF8000000000000ll) : den > 0 ? rmax / den : 0.0;
     }
     __syncthreads();
     for (int q = threadIdx.x; q < 3 * nrhs; q += blockDim.x) S->colmax[q] = 0ull;

@@ -22,11 +22,10 @@
 #include <stdlib.h>
 #include <string.h>
 
-#define GB_EPS_SINGLE 1.1920928955078125e-07
 #define GB_MAX_REFINE 30
 
-enum { GB_REASON_NONE = 0, GB_REASON_FP32_FAILED = 1, GB_REASON_SMALL_PIVOT = 2,
-       GB_REASON_STALLED = 3 };
+enum { GB_REASON_NONE = GB300_REASON_NONE, GB_REASON_FP32_FAILED = GB300_REASON_FP32_FAILED,
+       GB_REASON_SMALL_PIVOT = GB300_REASON_SMALL_PIVOT, GB_REASON_STALLED = GB300_REASON_STALLED };
 
 /* Full (both triangles) compressed-row copy of the lower-stored A: row i of
  * the result is column i of the full symmetric matrix. */
@@ -203,7 +202,9 @@ int gb300_factorize_mixed(cholmod_sparse *A, cholmod_factor *L, cholmod_common *
     P->mixed_reason = GB_REASON_NONE;
     P->dev_valid[1] = 0;                 /* the FP32 factor is of D A D, not of L->x */
     if (anyfail) return factor_fp64(P, ctx, GB_REASON_FP32_FAILED, Common);
-    if (mm[0] <= GB_EPS_SINGLE * mm[1]) return factor_fp64(P, ctx, GB_REASON_SMALL_PIVOT, Common);
+    /* small pivot: min L(k,k)^2 <= 2^-pivot_log2 max L(k,k)^2 (by default
+     * 2^-23, the single-precision epsilon) */
+    if (mm[0] <= ldexp(mm[1], -ctx->pivot_log2)) return factor_fp64(P, ctx, GB_REASON_SMALL_PIVOT, Common);
     return TRUE;
 }
 
@@ -345,16 +346,24 @@ static cholmod_dense *solve_refined_into(cholmod_sparse *A, cholmod_factor *L, c
         if (!ok) break;
         it++;
         berr_max = 0;
-        int improved = 0;
+        int improved = 0, b_bad = 0;
         for (int64_t q = 0; q < nsg * nrhs; q++) {
             const double *h = hred + 3 * q;
-            double den = P->h_anorm_seg[q / nrhs] * h[1] + h[2];
-            double be = den > 0 ? h[0] / den : 0;
+            const double an = P->h_anorm_seg[q / nrhs];
+            double den = an * h[1] + h[2];
+            /* a NaN or infinity in r, x, b or A (the device maxima keep
+             * NaN) makes the column's backward error NaN: not converged */
+            double be = (isfinite(h[0]) && isfinite(h[1]) && isfinite(h[2]) && isfinite(an)
+                         && isfinite(den)) ? (den > 0 ? h[0] / den : 0) : NAN;
             if (be < best[q]) { if (be < 0.5 * best[q]) improved = 1; best[q] = be; }
-            berr_max = fmax(berr_max, be);
+            if (!(be <= berr_max)) berr_max = be;       /* keeps NaN */
+            if (!isfinite(h[2])) b_bad = 1;
             bmax_all = fmax(bmax_all, h[2]);
         }
         if (berr_max <= tol) break;
+        /* a right-hand side that is not finite cannot be refined by any
+         * factor: stop with its NaN backward error */
+        if (b_bad) break;
         stall = improved ? 0 : stall + 1;
         if (stall >= 2) {
             if (P->mixed == 2) break;           /* FP64 factor cannot do better */
@@ -380,6 +389,16 @@ static cholmod_dense *solve_refined_into(cholmod_sparse *A, cholmod_factor *L, c
     if (info) { info[0] = it; info[1] = berr_max; info[3] = berr_max; info[2] = P->mixed == 2; }
     if (berr_max > tol) GB_ERROR(CHOLMOD_DSMALL, "refinement did not reach the requested tolerance");
     return X;
+}
+
+int gb300_mixed_reason(cholmod_factor *L, cholmod_common *Common)
+{
+    if (!Common || !L) return -1;
+    gb_ctx *ctx = gb_ctx_get(Common, 0);
+    if (!ctx) return -1;
+    gb_plan *P = gb_plan_get(L, Common, ctx, 0);
+    if (!P || !P->mixed) return -1;
+    return P->mixed == 1 ? GB_REASON_NONE : P->mixed_reason;
 }
 
 cholmod_dense *gb300_solve_refined(cholmod_sparse *A, cholmod_factor *L, cholmod_dense *B,

@@ -30,6 +30,7 @@ gb_ctx *gb_ctx_new(void)
     c->sweep_mode = 1;
     c->factor_mode = 1;
     c->tc_mode = 0;
+    c->pivot_log2 = 23;
     c->graph_mode = 1;
     c->sweep_streams = 2;
     return c;
@@ -85,6 +86,7 @@ int gb300_set_option(cholmod_common *Common, int option, int64_t value)
     else if (option == GB300_OPT_FACTOR) c->factor_mode = value ? 1 : 0;
     else if (option == GB300_OPT_TENSOR) c->tc_mode = value ? 1 : 0;
     else if (option == GB300_OPT_GRAPH) c->graph_mode = value ? 1 : 0;
+    else if (option == GB300_OPT_PIVOT_LOG2) c->pivot_log2 = (int)GB_MAX(0, GB_MIN(60, value));
     else if (option == GB300_OPT_SWEEP_STREAMS)
         c->sweep_streams = (int)GB_MAX(1, GB_MIN(GB_SWEEP_STREAMS, value));
     else if (option == GB300_OPT_TRACE) c->trace_on = value ? 1 : 0;

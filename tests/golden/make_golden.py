@@ -1,7 +1,8 @@
 """Generate the golden fixtures from the reference CHOLMOD (run here only).
 
 Needs oracle/_ref (python oracle/build_ref.py, which compiles the reference
-sources under /root/reference).  For every case it records what the
+sources found by oracle/build_ref.py reference_root()).  For every case it
+records what the
 reference's cholmod_l_analyze / cholmod_l_factorize / cholmod_l_solve
 produce on the seeded matrix of suitesparse_gb300.matrices:
 
@@ -10,8 +11,9 @@ produce on the seeded matrix of suitesparse_gb300.matrices:
                      nsuper, xsize, maxcsize, maxesize, minor, status,
                      SHA-256 of the supernodal pattern (super, pi, px, s),
                      Frobenius norm of L, backward error of the solve
-  golden_arrays.npz  the final permutation of every case (int32); for the
-                     small cases also L->x (double and single) and X
+  golden_arrays.npz  the final permutation and the supernode partition
+                     L->super of every case (int32); for the small cases
+                     also L->x (double and single) and X
 
 Usage: python tests/golden/make_golden.py
 """
@@ -78,6 +80,7 @@ def main(only=None):
             rec[k] = float(r[k])
         rec["L_fro"] = float(np.linalg.norm(r["Lx"]))
         arrays[name + "_Perm"] = r["Perm"].astype(np.int32)
+        arrays[name + "_Super"] = r["Super"].astype(np.int32)
         if full:
             arrays[name + "_Lx"] = r["Lx"]
             rs = refrun.run(n, Ap, Ai, Ax, ordering, "s", B=B)

@@ -10,7 +10,10 @@ import pytest
 
 from conftest import ROOT
 
-REF_INC = "/root/reference/CHOLMOD/Include"
+from oracle.build_ref import reference_root
+
+REF_ROOT = reference_root()
+REF_INC = os.path.join(REF_ROOT, "CHOLMOD", "Include")
 OBJ = {"cholmod_common": 0, "cholmod_sparse": 1, "cholmod_factor": 2, "cholmod_dense": 3}
 
 
@@ -49,7 +52,7 @@ def test_layout_matches_reference_header(lib):
     with tempfile.TemporaryDirectory() as d:
         exe = os.path.join(d, "probe")
         subprocess.run(["gcc", "-o", exe, os.path.join(ROOT, "tests", "abi_probe.c"),
-                        "-I" + REF_INC, "-I/root/reference/SuiteSparse_config",
+                        "-I" + REF_INC, "-I" + os.path.join(REF_ROOT, "SuiteSparse_config"),
                         "-I" + os.path.join(ROOT, "suitesparse_gb300", "csrc")], check=True)
         out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
     checked = 0

@@ -181,18 +181,30 @@ def test_keep_factor_on_device(golden, lib):
     CH.free_sparse(A, c)
 
 
-def test_c2_full_size_fp64(golden, lib, oracle_mod):
-    """64^3 variable-coefficient Laplacian at full size: L norm against the
-    reference's and the solve's backward error (size-independent checks)."""
+@pytest.mark.parametrize("name", ["c2", "c3"])
+def test_full_size_fp64(golden, lib, oracle_mod, name):
+    """Full-size configurations, FP64: c2 (64^3 variable-coefficient
+    Laplacian, METIS, supernodes up to 6,072 wide) and c3 (27-point 40^3
+    x 3-dof elasticity, METIS, supernodes up to 6,720 wide).  L element by
+    element against the oracle's factor of the same S = tril(PAP') (the
+    reference's algorithm over OpenBLAS), its norm against the reference's
+    own, and the solve's backward error at 1 and 8 right-hand sides."""
     meta, arrays = golden
-    rec = meta["c2"]
+    rec = meta[name]
     c = CH.Common()
-    mat, A, L, perm = setup(meta, arrays, "c2", c)
+    mat, A, L, perm = setup(meta, arrays, name, c)
     assert CH.factorize(A, L, c) == 1 and c.status == CH.CHOLMOD_OK
     f = CH.factor_arrays(L)
+    assert f["nsuper"] == rec["nsuper"] and f["xsize"] == rec["xsize"]
     assert abs(np.linalg.norm(f["Lx"]) - rec["L_fro"]) <= 1e-10 * rec["L_fro"]
-    B = M.rhs(mat[0], 1, rec["rhs_seed"])
-    X = CH.solve(L, B, c)
-    assert oracle_mod.backward_error(*mat, X, B).max() <= 1e-12
+    sym, st, minor, Lx = oracle_factor(oracle_mod, mat, perm, f)
+    assert st == 0
+    err = relerr(f["Lx"], Lx)
+    del Lx
+    assert err <= L_TOL, err
+    for nrhs in (1, 8):
+        B = M.rhs(mat[0], nrhs, rec["rhs_seed"] + nrhs - 1)
+        X = CH.solve(L, B, c)
+        assert oracle_mod.backward_error(*mat, X, B).max() <= 1e-12
     CH.free_factor(L, c)
     CH.free_sparse(A, c)

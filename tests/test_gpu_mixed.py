@@ -35,11 +35,14 @@ def test_refined_reaches_tolerance(golden, lib, oracle_mod, name, nrhs):
     CH.free_sparse(A, c)
 
 
-def test_refined_c2_full_size(golden, lib, oracle_mod):
-    """64^3 variable-coefficient Laplacian (condition ~1e8) at full size."""
+@pytest.mark.parametrize("name", ["c2", "c3"])
+def test_refined_full_size(golden, lib, oracle_mod, name):
+    """Full size: c2 (64^3 variable-coefficient Laplacian, condition ~1e8)
+    and c3 (27-point 40^3 x 3-dof elasticity), 1, 8 and 64 right-hand
+    sides, each column to 1e-12 against the oracle's FP64 evaluation."""
     meta, arrays = golden
     c = CH.Common()
-    mat, A, L = setup(meta, arrays, "c2", c)
+    mat, A, L = setup(meta, arrays, name, c)
     assert CH.factorize_mixed(A, L, c) == 1
     for nrhs in (1, 8, 64):
         B = M.rhs(mat[0], nrhs, 5 + nrhs)

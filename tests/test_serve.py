@@ -74,7 +74,7 @@ def test_same_result_alone_and_in_the_mix(lib, oracle_mod):
         coalesced = S.stats()["coalesced"]
     finally:
         S.close()
-    nsolve = 0
+    nsolve = nexact = 0
     for rq in stream:
         st_a, X_a, info_a = alone[rq["req"]]
         rec = mix[rq["req"]]
@@ -91,8 +91,17 @@ def test_same_result_alone_and_in_the_mix(lib, oracle_mod):
         for X in (X_a, rec["X"]):
             be = oracle_mod.backward_error(*mat, X, B)
             assert be.max() <= 1e-12, (rq["req"], be.max())
-        # both solutions meet the backward-error target; they agree to the
-        # forward error that target allows for these condition numbers
-        rel = np.abs(X_a - rec["X"]).max() / np.abs(X_a).max()
-        assert rel <= 1e-6, (rq["req"], rel)
-    assert nsolve >= 4
+        if rec["batch_cols"] == B.shape[1]:
+            # not coalesced: the factorization (owner-computes, no atomics)
+            # and the refined solve do the same arithmetic in the same order
+            # alone and in the mix, so the solution is the same bit for bit
+            assert np.array_equal(X_a, rec["X"]), rq["req"]
+            nexact += 1
+        else:
+            # coalesced with other solves of the factor: the refinement ran
+            # until every column converged, so this one may have taken an
+            # extra step; both meet the target and agree to the forward
+            # error it allows for these condition numbers
+            rel = np.abs(X_a - rec["X"]).max() / np.abs(X_a).max()
+            assert rel <= 1e-6, (rq["req"], rel)
+    assert nsolve >= 4 and nexact >= 1

@@ -134,3 +134,32 @@ def test_rejects_sizes_beyond_the_scratch(golden, lib):
     rc, be = _call(f, torch, n, t, 3)
     assert rc == 0
     np.testing.assert_allclose(be, _numpy_berr(n, Fp, Fi, Fx, X[:, :3], B[:, :3]), rtol=REL_TOL)
+
+
+def test_non_finite_solutions_give_nan(golden, lib):
+    """A NaN or an infinity in x or b must not vanish from the maxima (a plain
+    fmax drops NaN and would report such a column as converged)."""
+    torch = pytest.importorskip("torch")
+    meta, arrays = golden
+    f = _fn(lib)
+    n, Ap, Ai, Ax = make_case(meta, "g3")
+    Fp, Fi, Fx = M.full_from_lower(n, Ap, Ai, Ax)
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((n, 5))
+    B = rng.standard_normal((n, 5))
+    X[:, 0] = np.nan                 # all of x NaN
+    X[n // 2, 1] = np.nan            # one entry of x NaN
+    X[3, 2] = np.inf                 # one entry of x infinite
+    B[n - 1, 3] = np.nan             # one entry of b NaN; column 4 clean
+    t = _device(torch, n, Fp, Fi, Fx, X, B)
+    for _ in range(2):
+        rc, be = _call(f, torch, n, t, 5)
+        assert rc == 0
+        assert np.all(np.isnan(be[:4])), be
+        np.testing.assert_allclose(be[4], _numpy_berr(n, Fp, Fi, Fx, X[:, 4:], B[:, 4:])[0],
+                                   rtol=REL_TOL)
+    # the NaN maxima were cleared: a clean call afterwards is exact again
+    t1 = _device(torch, n, Fp, Fi, Fx, X[:, 4:], B[:, 4:])
+    rc, be = _call(f, torch, n, t1, 1)
+    assert rc == 0 and np.isfinite(be[0])
+    np.testing.assert_allclose(be, _numpy_berr(n, Fp, Fi, Fx, X[:, 4:], B[:, 4:]), rtol=REL_TOL)
