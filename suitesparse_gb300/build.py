@@ -79,7 +79,9 @@ def build(verbose=False):
         objs = list(ex.map(one, jobs))
     tmp = LIB + ".tmp"
     _run([nvcc, "-shared"] + ARCH + ["-o", tmp] + objs +
-         ["-Xlinker", "-rpath," + os.path.join(cuda, "lib64"), "-lcudart", "-lpthread"])
+         ["-Xlinker", "-rpath," + os.path.join(cuda, "lib64"),
+          "-Xlinker", "--version-script=" + os.path.join(CSRC, "exports.map"),
+          "-lcudart", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

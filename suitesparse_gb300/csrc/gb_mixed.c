@@ -387,7 +387,8 @@ static cholmod_dense *solve_refined_into(cholmod_sparse *A, cholmod_factor *L, c
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     ctx->stats[2] = ms;
     if (info) { info[0] = it; info[1] = berr_max; info[3] = berr_max; info[2] = P->mixed == 2; }
-    if (berr_max > tol) GB_ERROR(CHOLMOD_DSMALL, "refinement did not reach the requested tolerance");
+    if (!(berr_max <= tol))              /* NaN included */
+        GB_ERROR(CHOLMOD_DSMALL, "refinement did not reach the requested tolerance");
     return X;
 }
 
