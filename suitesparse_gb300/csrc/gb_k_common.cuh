@@ -10,6 +10,7 @@
 
 struct gb_dev_pattern {
     const int64_t *Super, *Pi, *Px, *cboff, *cbvoff;
+    const int64_t *imgbase;    // first operand image of s (tensor-core tiles), -1 if none
     const int32_t *Ls, *relmap, *child_ptr, *child_list;
     const int32_t *blkoff;     // first 64-column diagonal block id of s
     const int64_t *linvoff;    // offset of each diagonal block's inverse
@@ -98,13 +99,19 @@ __device__ void tri_inverse(const T (*A)[NB + 1], int nb, T *out, int ldo)
     }
 }
 
+__device__ __forceinline__ void gb_img_store(const float (&acc)[4][4], int nr, int ncols, int m0,
+                                             float *S, float *Imgdst);
+
 // Panel triangular solve as a product with the block inverse:
 // X(nr x nc) = B * Linv', with Bt[k*ldt + r] = B(r, k) and
 // Lt[k*ldt + c] = Linv(c, k) in shared memory (256 threads, 4x4 each);
-// only columns c < ncols are written to dst (column-major, ld).
+// only columns c < ncols are written to dst (column-major, ld).  FP32 with
+// img: the block is also written as the split operand image of the
+// tensor-core tile products (rows from m0; Bt and Lt, contiguous, serve as
+// its 32 KB of staging space once the product is formed).
 template <typename T>
 __device__ void trsm_tile(const T *Bt, const T *Lt, int ldt, int nr, int nc, int ncols,
-                          T *dst, int64_t ld)
+                          T *dst, int64_t ld, float *img = nullptr, int m0 = 0)
 {
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     T acc[4][4];
@@ -130,6 +137,12 @@ __device__ void trsm_tile(const T *Bt, const T *Lt, int ldt, int nr, int nc, int
         for (int b = 0; b < 4; b++) {
             const int cc = tx + 16 * b;
             if (r < nr && cc < ncols) dst[r + (int64_t)cc * ld] = acc[a][b];
+        }
+    }
+    if constexpr (sizeof(T) == 4) {
+        if (img) {
+            __syncthreads();
+            gb_img_store(acc, nr, ncols, m0, (float *)Bt, img);
         }
     }
 }
@@ -622,23 +635,39 @@ __device__ __forceinline__ void gemm_tile_f32(const float *A, int64_t lda, const
 }
 
 // ---------------------------------------------------------------------------
-// tensor-core tile update (tcgen05, kind::tf32, accumulator in TMEM)
+// tensor-core tile products (tcgen05, kind::tf32, accumulators in TMEM) with
+// operands staged by bulk asynchronous copies from split panel images
 // ---------------------------------------------------------------------------
 
 #define GB_TC_SPIN (1 << 22)
 
-// per block: TMEM accumulator (64 columns), the mbarrier the MMAs commit to,
-// and its phase; ok = 0 after a wait gave up
+// TMEM columns per block: two accumulators of 128 columns (the executor's
+// shared memory keeps at most 2 blocks per SM: 512 of 512 columns)
+#define GB_TC_COLS 256
+// operand stages in shared memory, 32 KB each (A' and B' of one K chunk)
+#define GB_IMG_NS 3
+#define GB_TC_SMEM (GB_IMG_NS * 32768)
+// K chunks (32 deep) accumulated in one TMEM accumulator before it is
+// drained into FP32 registers
+#define GB_IMG_GROUP 8
+// one image: a 64-row block of one 64-column panel, split x = hi + lo
+// (hi = x rounded to TF32), as two K chunks of 32, each [hi rows 0-63;
+// lo rows 64-127] x 32 in the canonical K-major no-swizzle layout of
+// gb_img_off: 2 x 16 KB
+#define GB_IMG_FLOATS GB_IMG_FLOATS_HOST
+
+// per block: TMEM accumulators, mbarriers and their phases; ok = 0 after a
+// wait gave up.  Barriers (8 bytes each from mbar): full[s] = s (operand
+// stage s landed), empty[s] = GB_IMG_NS + s (the MMAs reading stage s are
+// done), accd = 2 GB_IMG_NS (an accumulator's MMAs are done).  phase bit i
+// is the parity of barrier i's next completion.
 struct gb_tc_ctx {
-    uint32_t taddr;    // TMEM: two accumulators of 128 columns
-    uint32_t mbar;     // two mbarriers (one per operand stage) at mbar, mbar + 8
-    uint32_t phase;    // phase bit of each stage's mbarrier
+    uint32_t taddr;
+    uint32_t mbar;
+    uint32_t phase;
     int ok;
 };
-
-#define GB_TC_COLS 256          // TMEM columns per block
-#define GB_TC_SMEM (2 * 32768)  // two operand stages of 32 KB
-#define GB_TC_MIN_K 128         // depth from which a tile runs on the tensor cores
+#define GB_TC_NBAR (2 * GB_IMG_NS + 1)
 
 __device__ __forceinline__ uint32_t gb_su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -658,11 +687,21 @@ __device__ __forceinline__ float gb_tf32_rna(float x)
     return __uint_as_float(r);
 }
 
-// element (m, k) of a K-major tile with a K chunk of 32 (4-byte elements):
-// lbo = 128 bytes, sbo = 1024 bytes
-__device__ __forceinline__ uint32_t gb_tc_off(int m, int k)
+// byte offset of element (m, k) (m < 128: rows 64-127 are the lo parts;
+// k < 64) in an image: chunk k / 32 of 16 KB, then core matrices of 8 rows
+// x 4 k (lbo = 128 bytes along K, sbo = 1024 bytes along M)
+__device__ __forceinline__ uint32_t gb_img_off(int m, int k)
 {
-    return (uint32_t)((m >> 3) * 1024 + (k >> 2) * 128 + (m & 7) * 16 + (k & 3) * 4);
+    return (uint32_t)((k >> 5) * 16384 + (m >> 3) * 1024 + ((k & 31) >> 2) * 128 + (m & 7) * 16
+                      + (k & 3) * 4);
+}
+
+// image of 64-row block r of panel b of a supernode whose images start at
+// image ibase, with R row blocks (only blocks r >= b are stored)
+__device__ __forceinline__ const float *gb_img_ptr(const float *Img, int64_t ibase, int R, int b, int r)
+{
+    return Img + ((int64_t)ibase + (int64_t)b * R - ((int64_t)b * (b - 1)) / 2 + (r - b))
+                 * (int64_t)GB_IMG_FLOATS;
 }
 
 __device__ __forceinline__ bool gb_mbar_wait(uint32_t mbar, uint32_t phase)
@@ -676,7 +715,15 @@ __device__ __forceinline__ bool gb_mbar_wait(uint32_t mbar, uint32_t phase)
     return false;
 }
 
-// 32 lanes x 16 columns of 32-bit accumulator (warp w: TMEM lanes 32 w ..)
+// thread: wait for barrier i's next completion (bounded), track its parity
+__device__ __forceinline__ bool gb_tc_wait(gb_tc_ctx &tc, int i)
+{
+    const bool ok = gb_mbar_wait(tc.mbar + 8u * (uint32_t)i, (tc.phase >> i) & 1u);
+    tc.phase ^= 1u << i;
+    return ok;
+}
+
+// 32 lanes x 16 columns of 32-bit accumulator (warp w: TMEM lanes 32 (w % 4) ..)
 __device__ __forceinline__ void gb_tmem_ld16(uint32_t (&r)[16], uint32_t taddr)
 {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
@@ -695,148 +742,197 @@ __device__ __forceinline__ void gb_tc_mma(uint32_t taddr, uint64_t a, uint64_t b
                  :: "r"(taddr), "l"(a), "l"(b), "r"(idesc), "r"(accumulate) : "memory");
 }
 
-// One K chunk (32) of both operands into a stage: A' = [A_hi; A_lo] (128
-// rows) and B' = [B_hi; B_lo] (128 rows), x_hi = x rounded to TF32, x_lo =
-// x - x_hi, in the canonical K-major no-swizzle layout (gb_tc_off).  Element
-// q of a thread: core matrix cm = 8 warp + q (rows 8 (cm & 7).., k 4 (cm >> 3)..),
-// row 8 (cm & 7) + lane / 4, k 4 (cm >> 3) + lane % 4: a warp's store fills
-// one 128-byte core matrix (no bank conflicts), its load reads 8 rows x 4
-// columns (four 32-byte sectors).
-__device__ __forceinline__ void gb_tc_stage(unsigned char *stage, int lane, int warp, const float (&xa)[8],
-                                            const float (&xb)[8])
+// Write the 64 x 64 panel block held by a trsm_tile thread layout (acc
+// rows ty + 16 a, columns tx + 16 b; rows rr >= nr or columns >= ncols are
+// zero) as an image at Imgdst: image row m0 + rr (rows 0..m0-1 zero), split
+// into TF32 hi and FP32 lo parts.  Staged through S (32 KB of shared
+// memory, free when called) so that the global stores are whole 16-byte
+// vectors; all 256 threads.  The image is read later by the bulk-copy
+// (async) proxy of another block, hence the proxy fence after the stores.
+__device__ __forceinline__ void gb_img_store(const float (&acc)[4][4], int nr, int ncols, int m0,
+                                             float *S, float *Imgdst)
 {
-    unsigned char *Ap = stage, *Bp = stage + 16384;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    unsigned char *Sb = (unsigned char *)S;
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-        const int cm = warp * 8 + q;
-        const uint32_t off = (uint32_t)((cm & 7) * 1024 + (cm >> 3) * 128 + lane * 4);
-        const float ah = gb_tf32_rna(xa[q]), bh = gb_tf32_rna(xb[q]);
-        *(float *)(Ap + off) = ah;
-        *(float *)(Ap + off + 8192) = xa[q] - ah;
-        *(float *)(Bp + off) = bh;
-        *(float *)(Bp + off + 8192) = xb[q] - bh;
+    for (int a = 0; a < 4; a++) {
+        const int rr = ty + 16 * a, m = m0 + rr;
+        if (m >= 64) continue;
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const int k = tx + 16 * b;
+            const float v = (rr < nr && k < ncols) ? acc[a][b] : 0.0f;
+            const float h = gb_tf32_rna(v);
+            const uint32_t off = gb_img_off(m, k);
+            *(float *)(Sb + off) = h;
+            *(float *)(Sb + off + 8192) = v - h;
+        }
     }
+    for (int idx = threadIdx.x; idx < m0 * 64; idx += blockDim.x) {
+        const uint32_t off = gb_img_off(idx >> 6, idx & 63);
+        *(float *)(Sb + off) = 0.0f;
+        *(float *)(Sb + off + 8192) = 0.0f;
+    }
+    __syncthreads();
+    const float4 *src = (const float4 *)S;
+    float4 *dst = (float4 *)Imgdst;
+    for (int q = threadIdx.x; q < GB_IMG_FLOATS / 4; q += blockDim.x) dst[q] = src[q];
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    __syncthreads();
 }
 
-// C[0:m, 0:n] -= A[0:m, 0:k] B[0:n, 0:k]' (m, n <= 64, column-major; lower:
-// only entries with row - col >= diag_off) on the tensor cores with 256
-// threads.  FP32 operands are split x = hi + lo (hi = x rounded to TF32) and
-// packed as A' = [A_hi; A_lo], B' = [B_hi; B_lo]; one MMA of
-// tcgen05.mma.cta_group::1.kind::tf32, M = 128, N = 128, per K step of 8
-// yields all four products hi*hi, hi*lo, lo*hi, lo*lo in the four quarters
-// of the accumulator.  Consecutive K chunks of 32 alternate between two
-// accumulators (TMEM columns 0-127 and 128-255), which halves the error of
-// the tensor core's FP32 accumulation; the epilogue adds the quarters and
-// the two accumulators in FP32 (max error near that of a sequential FP32
-// sum: 3.7e-5 vs 2.7e-5 for 64 x 64 x 2048 of values in [-0.5, 0.5]).
-// Pipeline: two operand stages in shared memory (GB_TC_SMEM), each with an
-// mbarrier the MMAs commit to; the loads of chunk c + 2 are in flight while
-// chunk c's MMAs run and chunk c + 1 is staged.  Every wait is bounded;
-// returns false when one gave up (tc.ok = 0).
-static __device__ __noinline__ bool gemm_tile_tc(const float *A, int64_t lda, const float *B, int64_t ldb,
-                                                 float *C, int64_t ldc, int m, int n, int k, bool lower,
-                                                 int diag_off, unsigned char *smem, gb_tc_ctx &tc)
+// C[i, j] -= sum over K chunks c = 0..nch-1 of A(i, k) B(j, k) for the 64 x
+// 64 output of rows i in [i0, i1), columns j in [j0, j1) (lower: only i >=
+// j), C[c_off + i + j ldc] in global memory.  Chunk c is K chunk c & 1 of
+// panel b0 + c / 2; A's operand is the image of row block ra, B's of row
+// block rb (gb_img_ptr).  One MMA of tcgen05.mma.cta_group::1.kind::tf32,
+// M = 128, N = 128, per K step of 8 multiplies A' = [A_hi; A_lo] by B' =
+// [B_hi; B_lo]: the four quarters of the accumulator hold hi*hi, hi*lo,
+// lo*hi, lo*lo.  Thread 0 issues the bulk copies of each chunk's two
+// images into one of GB_IMG_NS stages (mbarrier with transaction count)
+// and the MMAs (committed to the stage's empty barrier), GB_IMG_NS - 1
+// chunks ahead.  Every GB_IMG_GROUP chunks the accumulator alternates, and
+// the one just finished is drained by all threads into FP32 registers (sums
+// over at most 256 of K, then summed with round-to-nearest adds: the
+// tensor core's FP32 accumulation truncates, and its error would otherwise
+// grow linearly with K).  The epilogue adds the hi and lo rows' sums
+// through shared memory and updates C, whose values were loaded while the
+// operands were in flight.  Every wait is bounded; returns false when one
+// gave up (tc.ok = 0), after waiting (bounded) for the copies and MMAs in
+// flight.
+static __device__ __noinline__ bool gemm_img_tc(const float *Img, int64_t ibase, int R, int ra, int rb,
+                                                int b0, int nch, float *C, int64_t c_off, int64_t ldc,
+                                                int i0, int i1, int j0, int j1, bool lower,
+                                                unsigned char *smem, gb_tc_ctx &tc)
 {
-    if (k <= 0) return true;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(128 >> 3) << 17)
                            | ((uint32_t)(128 >> 4) << 24);
-    auto load = [&](float (&xa)[8], float (&xb)[8], int k0) {
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-            const int cm = warp * 8 + q;
-            const int r = (cm & 7) * 8 + (lane >> 2), kg = k0 + (cm >> 3) * 4 + (lane & 3);
-            xa[q] = (r < m && kg < k) ? A[r + (int64_t)kg * lda] : 0.0f;
-            xb[q] = (r < n && kg < k) ? B[r + (int64_t)kg * ldb] : 0.0f;
-        }
-    };
-    const int nch = (k + 31) / 32;
+    const int NS = GB_IMG_NS;
     bool ok = true;
-    auto step = [&](int c, const float (&xa)[8], const float (&xb)[8]) {
-        const int st = c & 1;
-        unsigned char *stage = smem + st * 32768;
-        if (c >= 2) {
-            // the MMAs of chunk c - 2 read this stage
-            if (!gb_mbar_wait(tc.mbar + 8 * st, (tc.phase >> st) & 1u)) ok = false;
-            tc.phase ^= 1u << st;
+    auto issue = [&](int c) {
+        const int st = c % NS, b = b0 + (c >> 1), h = c & 1;
+        const float *pa = gb_img_ptr(Img, ibase, R, b, ra) + h * 4096;
+        const float *pb = gb_img_ptr(Img, ibase, R, b, rb) + h * 4096;
+        const uint32_t fb = tc.mbar + 8u * (uint32_t)st;
+        const uint32_t dst = gb_su32(smem + st * 32768);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                     :: "r"(fb), "r"(32768) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     :: "r"(dst), "l"(pa), "r"(16384), "r"(fb) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     :: "r"(dst + 16384u), "l"(pb), "r"(16384), "r"(fb) : "memory");
+    };
+    // the images were written by other blocks through the generic proxy
+    // (ordered by the executor's release/acquire); make them visible to the
+    // async proxy before the copies
+    int issued = 0, nmma = 0;     // thread 0: chunks loaded, chunks multiplied
+    if (tid == 0) {
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        for (; issued < nch && issued < NS; issued++) issue(issued);
+    }
+    // C's values, in flight with the operands
+    float cval[16];
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const int idx = tid + 256 * q, i = idx & 63, j = idx >> 6;
+        const bool in = i >= i0 && i < i1 && j >= j0 && j < j1 && !(lower && i < j);
+        cval[q] = in ? C[c_off + i + (int64_t)j * ldc] : 0.0f;
+    }
+    float sum[32];
+#pragma unroll
+    for (int q = 0; q < 32; q++) sum[q] = 0.0f;
+    // drain accumulator sel: this thread's TMEM lane 32 (warp % 4) + lane,
+    // output columns 32 (warp / 4) .. + 31 (products with B_hi at those
+    // columns, with B_lo at 64 + those columns)
+    auto drain = [&](int sel) {
+        const uint32_t base = tc.taddr + ((uint32_t)(32 * (warp & 3)) << 16)
+                              + (uint32_t)(sel * 128 + 32 * (warp >> 2));
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+        for (int hf = 0; hf < 2; hf++) {
+            uint32_t x[16], y[16];
+            gb_tmem_ld16(x, base + 16u * hf);
+            gb_tmem_ld16(y, base + 64u + 16u * hf);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 16; q++) sum[16 * hf + q] += __uint_as_float(x[q]) + __uint_as_float(y[q]);
         }
-        gb_tc_stage(stage, lane, warp, xa, xb);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    };
+    for (int c = 0; c < nch; c++) {
+        const int g = c / GB_IMG_GROUP, gs = g * GB_IMG_GROUP;
+        if (tid == 0 && ok) {
+            const int st = c % NS;
+            if (!gb_tc_wait(tc, st)) ok = false;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a0 = gb_su32(stage), b0 = gb_su32(stage + 16384);
+            const uint32_t a0 = gb_su32(smem + st * 32768), bb0 = a0 + 16384u;
+            const uint32_t acc = tc.taddr + (uint32_t)((g & 1) * 128);
 #pragma unroll
             for (int j = 0; j < 4; j++)
-                gb_tc_mma(tc.taddr + (uint32_t)(st * 128), gb_tc_desc(a0 + j * 256, 128, 1024),
-                          gb_tc_desc(b0 + j * 256, 128, 1024), idesc, (c > 1 || j > 0) ? 1u : 0u);
+                gb_tc_mma(acc, gb_tc_desc(a0 + j * 256, 128, 1024), gb_tc_desc(bb0 + j * 256, 128, 1024),
+                          idesc, (c > gs || j > 0) ? 1u : 0u);
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                         :: "r"(tc.mbar + 8 * st) : "memory");
-        }
-    };
-    float pa[2][8], pb[2][8];
-#pragma unroll
-    for (int u = 0; u < 2; u++)
-        if (u < nch) load(pa[u], pb[u], u * 32);
-    int issued = 0;
-    for (int c = 0; c < nch && ok; c += 2) {
-#pragma unroll
-        for (int u = 0; u < 2; u++) {
-            if (c + u < nch) {
-                step(c + u, pa[u], pb[u]);
-                issued = c + u + 1;
-                if (c + u + 2 < nch) load(pa[u], pb[u], (c + u + 2) * 32);
+                         :: "r"(tc.mbar + 8u * (uint32_t)(NS + st)) : "memory");
+            nmma = c + 1;
+            // the group's last chunk, with more groups to come: signal the
+            // accumulator's completion for its drain
+            if (c == gs + GB_IMG_GROUP - 1 && c + 1 < nch)
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                             :: "r"(tc.mbar + 8u * (uint32_t)(2 * NS)) : "memory");
+            // refill the stage of chunk c - 1 (its MMAs are done or nearly)
+            if (c >= 1 && issued < nch) {
+                if (!gb_tc_wait(tc, NS + (c - 1) % NS)) ok = false;
+                issue(issued++);
             }
         }
-        ok = __syncthreads_and(ok);
+        // a new group's first MMAs are issued: drain the previous group's
+        // accumulator meanwhile
+        if (c == gs && c > 0) {
+            if (!gb_tc_wait(tc, 2 * NS)) ok = false;
+            if (ok) drain((g - 1) & 1);
+            ok = __syncthreads_and(ok);
+        }
     }
-    // the chunks whose MMAs were not waited for yet
-    for (int c = issued >= 2 ? issued - 2 : 0; c < issued; c++) {
-        const int st = c & 1;
-        if (!gb_mbar_wait(tc.mbar + 8 * st, (tc.phase >> st) & 1u)) ok = false;
-        tc.phase ^= 1u << st;
+    // the MMAs whose stages were not refilled: their completion also
+    // covers every earlier MMA
+    if (tid == 0 && ok) {
+        const int first = issued - NS > 0 ? issued - NS : 0;
+        for (int c = first; c < issued; c++)
+            if (!gb_tc_wait(tc, NS + c % NS)) ok = false;
     }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (!__syncthreads_and(ok)) {
+    ok = __syncthreads_and(ok);
+    if (!ok) {
+        // a wait gave up: before the block moves on (and releases its
+        // TMEM), wait once more, bounded, for the copies no MMA consumed
+        // and for every MMA issued (one more commit covers them all)
+        if (tid == 0) {
+            for (int c = nmma; c < issued; c++) gb_mbar_wait(tc.mbar + 8u * (uint32_t)(c % NS), 0u),
+                                                 gb_mbar_wait(tc.mbar + 8u * (uint32_t)(c % NS), 1u);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         :: "r"(tc.mbar + 8u * (uint32_t)(2 * NS)) : "memory");
+            gb_mbar_wait(tc.mbar + 8u * (uint32_t)(2 * NS), 0u);
+            gb_mbar_wait(tc.mbar + 8u * (uint32_t)(2 * NS), 1u);
+        }
+        __syncthreads();
         tc.ok = 0;
         return false;
     }
-    // epilogue: warps 0-1 hold the rows of A_hi (TMEM lanes 0-63), warps 2-3
-    // those of A_lo (lanes 64-127); columns j and 64 + j of an accumulator
-    // are the products with B_hi and B_lo.  Each sums its quarters into a
-    // 64 x 64 shared tile (T1: hi rows, T2: lo rows); then all threads
-    // update C.
-    float *T1 = (float *)smem, *T2 = T1 + 64 * 65;
-    const bool two = nch > 1;
-    if (warp < 4) {
-        const int r = (warp & 1) * 32 + lane;
-        float *T = warp < 2 ? T1 : T2;
-        for (int c0 = 0; c0 < 64; c0 += 16) {
-            uint32_t x[16], y[16];
-            const uint32_t a = tc.taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-            gb_tmem_ld16(x, a);
-            gb_tmem_ld16(y, a + 64u);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            float v[16];
-#pragma unroll
-            for (int q = 0; q < 16; q++) v[q] = __uint_as_float(x[q]) + __uint_as_float(y[q]);
-            if (two) {
-                gb_tmem_ld16(x, a + 128u);
-                gb_tmem_ld16(y, a + 192u);
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-                for (int q = 0; q < 16; q++) v[q] += __uint_as_float(x[q]) + __uint_as_float(y[q]);
-            }
-#pragma unroll
-            for (int q = 0; q < 16; q++) T[(c0 + q) * 65 + r] = v[q];
-        }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    if (nch > 0) drain(((nch - 1) / GB_IMG_GROUP) & 1);
+    // hi rows (TMEM lanes 0-63) and lo rows (64-127) of each output row
+    float *T = (float *)smem;
     __syncthreads();
-    for (int idx = tid; idx < 64 * 64; idx += blockDim.x) {
-        const int r = idx & 63, col = idx >> 6;
-        if (r < m && col < n && !(lower && r - col < diag_off))
-            C[r + (int64_t)col * ldc] -= T1[col * 65 + r] + T2[col * 65 + r];
+    {
+        const int row = 32 * (warp & 3) + lane, col = 32 * (warp >> 2);
+#pragma unroll
+        for (int q = 0; q < 32; q++) T[row * 65 + col + q] = sum[q];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const int idx = tid + 256 * q, i = idx & 63, j = idx >> 6;
+        if (i >= i0 && i < i1 && j >= j0 && j < j1 && !(lower && i < j))
+            C[c_off + i + (int64_t)j * ldc] = cval[q] - (T[i * 65 + j] + T[(64 + i) * 65 + j]);
     }
     // the next task reuses shared memory and the accumulators
     __syncthreads();
@@ -852,6 +948,7 @@ static inline __host__ __device__ gb_dev_pattern gb_to_dev(const gb_pattern_ptrs
     d.child_ptr = p->child_ptr; d.child_list = p->child_list;
     d.fail = p->fail; d.anyfail = p->anyfail;
     d.blkoff = p->blkoff; d.linvoff = p->linvoff;
+    d.imgbase = p->imgbase;
     return d;
 }
 

@@ -218,7 +218,7 @@ static __device__ __noinline__ void potrf_task(const gb_dev_pattern &P, const gb
 template <typename T>
 static __device__ __noinline__ void trsm_task(const gb_dev_pattern &P, const gb_dtask &tk, T *panel,
                                               int nscol, int nsrow, int f, const T *Linv,
-                                              unsigned char *smem_raw)
+                                              unsigned char *smem_raw, float *Img)
 {
     T *S1 = (T *)smem_raw + 64 * 65, *S2 = S1 + 64 * 65;
     const int s = tk.s;
@@ -243,15 +243,28 @@ static __device__ __noinline__ void trsm_task(const gb_dev_pattern &P, const gb_
             S1[k * 65 + cc] = w[q];
         }
         __syncthreads();
-        trsm_tile<T>(S1, S2, 65, nr, nb, ncols, panel + r0 + (int64_t)c0 * nsrow, nsrow);
+        // FP32 on the tensor cores: the block is also the operand image of
+        // the tile products that read it (UPD, CB)
+        float *img = nullptr;
+        if (Img && P.imgbase[s] >= 0)
+            img = (float *)gb_img_ptr(Img, P.imgbase[s], (nsrow + 63) / 64, tk.b, tk.r);
+        trsm_tile<T>(S1, S2, 65, nr, nb, ncols, panel + r0 + (int64_t)c0 * nsrow, nsrow, img,
+                     r0 - 64 * tk.r);
     }
 }
 
 // The work of one tile task (POTRF, TRSM, UPD or CB) of supernode tk.s.
-// smem_raw: dag_smem<T>() bytes.
+// smem_raw: dag_smem<T>() bytes (GB_TC_SMEM with tc).  With tc and Img
+// (FP32 on the tensor cores), TRSM also writes the split operand images and
+// UPD / CB tiles read them (gemm_img_tc).  CB tiles with tk.b = 1 lie on the
+// 64-row grid of the supernode's rows (tile (r, c): rows [max(64 r, nscol),
+// min(64 r + 64, nsrow)) and likewise the columns, in update-block
+// coordinates minus nscol), those with tk.b = 0 on the grid of the update
+// block itself.
 template <typename T>
 __device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx, T *CB, T *Linv,
-                              unsigned char *smem_raw, int &sfail, gb_tc_ctx *tc = nullptr)
+                              unsigned char *smem_raw, int &sfail, gb_tc_ctx *tc = nullptr,
+                              float *Img = nullptr)
 {
     T (*A)[65] = (T (*)[65])smem_raw;
     T *S1 = (T *)smem_raw + 64 * 65, *S2 = S1 + 64 * 65;
@@ -260,16 +273,25 @@ __device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx
     const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
     T *panel = Lx + P.Px[s];
     const int f = P.fail[s];
+    const bool img = tc && Img && P.imgbase[s] >= 0;
     if (tk.type == GB_DT_POTRF) {
         potrf_task<T>(P, tk, panel, nscol, nsrow, f, Linv, smem_raw, sfail);
     } else if (tk.type == GB_DT_TRSM) {
-        trsm_task<T>(P, tk, panel, nscol, nsrow, f, Linv, smem_raw);
+        trsm_task<T>(P, tk, panel, nscol, nsrow, f, Linv, smem_raw, img ? Img : nullptr);
     } else if (tk.type == GB_DT_UPD) {
         if (f < 0) {
             const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
             const int cs = 64 * tk.c, ce = min(cs + 64, nscol);
             const int rs = max(64 * tk.r, cs), re = min(64 * tk.r + 64, nsrow);
             if constexpr (sizeof(T) == 4) {
+                if (img) {
+                    // rows 64 r.. of the images of row blocks r and c of
+                    // panel b (rs = 64 r: r >= c)
+                    gemm_img_tc(Img, P.imgbase[s], (nsrow + 63) / 64, tk.r, tk.c, tk.b,
+                                nb > 32 ? 2 : 1, (float *)Lx, P.Px[s] + rs + (int64_t)cs * nsrow, nsrow,
+                                0, re - rs, 0, ce - cs, tk.r == tk.c, smem_raw, *tc);
+                    return;
+                }
                 // k = 64: the CUDA cores (the tensor-core tile's fixed costs
                 // make it slower at this depth)
                 gemm_tile_f32(panel + rs + (int64_t)c0 * nsrow, nsrow,
@@ -286,24 +308,36 @@ __device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx
     } else {  // GB_DT_CB
         if (f < 0) {
             const int m = nsrow - nscol;
-            const int I = 64 * tk.r, J = 64 * tk.c;
-            if constexpr (sizeof(T) == 4) {
-                if (tc && nscol >= GB_TC_MIN_K)
-                    gemm_tile_tc(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
-                                 CB + P.cboff[s] + I + (int64_t)J * m, m,
-                                 min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
-                                 smem_raw, *tc);
-                else
-                    gemm_tile_f32(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
-                                  CB + P.cboff[s] + I + (int64_t)J * m, m,
-                                  min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
-                                  (float *)smem_raw);
+            int I = 64 * tk.r, J = 64 * tk.c, mt = min(64, m - I), nt = min(64, m - J);
+            if (tk.b == 1) {
+                // 64-row grid of the supernode's rows
+                const int ri = max(64 * tk.r, nscol), ci = max(64 * tk.c, nscol);
+                mt = min(64 * tk.r + 64, nsrow) - ri;
+                nt = min(64 * tk.c + 64, nsrow) - ci;
+                I = ri - nscol;
+                J = ci - nscol;
+                if constexpr (sizeof(T) == 4) {
+                    if (img) {
+                        // output (i, j) = rows 64 r + i, 64 c + j of the
+                        // images; those below nscol are skipped
+                        const int i0 = ri - 64 * tk.r, j0 = ci - 64 * tk.c;
+                        const int nb_last = nscol - 64 * ((nscol - 1) / 64);
+                        const int nch = 2 * ((nscol + 63) / 64) - (nb_last > 32 ? 0 : 1);
+                        gemm_img_tc(Img, P.imgbase[s], (nsrow + 63) / 64, tk.r, tk.c, 0, nch,
+                                    (float *)CB, P.cboff[s] + (int64_t)(I - i0) + (int64_t)(J - j0) * m,
+                                    m, i0, i0 + mt, j0, j0 + nt, tk.r == tk.c, smem_raw, *tc);
+                        return;
+                    }
+                }
             }
+            if constexpr (sizeof(T) == 4)
+                gemm_tile_f32(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
+                              CB + P.cboff[s] + I + (int64_t)J * m, m,
+                              mt, nt, nscol, tk.r == tk.c, 0, (float *)smem_raw);
             else
                 gemm_tile_nt<T>(panel + nscol + I, nsrow, panel + nscol + J, nsrow,
                                 CB + P.cboff[s] + I + (int64_t)J * m, m,
-                                min(64, m - I), min(64, m - J), nscol, tk.r == tk.c, 0,
-                                S1, S2);
+                                mt, nt, nscol, tk.r == tk.c, 0, S1, S2);
         }
     }
 }
@@ -346,6 +380,7 @@ k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
 struct gb_fdag_dev {
     gb_dq Q;
     int use_tc;              // FP32 tile products on the tensor cores
+    float *img;              // their split operand images (gb_img_ptr)
     const gb_fpat *pats;
     const gb_finst *inst;
     const int64_t *ibase;
@@ -373,9 +408,9 @@ static_assert(8 * warp_front_smem<32, float>() <= dag_smem<float>()
               && 2 * warp_front_smem<64, float>() <= dag_smem<float>(), "one-warp fronts: shared memory");
 
 // shared memory of the tensor-core executor: the tile tasks' space and the
-// two operand stages of gemm_tile_tc, and more than a third of the SM's
-// 228 KB so that at most 2 blocks (2 x GB_TC_COLS TMEM columns) share an SM
-#define GB_FDAG_TC_SMEM (80 * 1024)
+// operand stages of gemm_img_tc, and more than a third of the SM's 228 KB
+// so that at most 2 blocks (2 x GB_TC_COLS TMEM columns) share an SM
+#define GB_FDAG_TC_SMEM (100 * 1024)
 static_assert(GB_FDAG_TC_SMEM >= GB_TC_SMEM && GB_FDAG_TC_SMEM >= (int)dag_smem<float>()
               && 3 * GB_FDAG_TC_SMEM > 228 * 1024, "tensor-core executor: shared memory");
 static_assert(8 * warp_front_smem<32, double>() <= dag_smem<double>()
@@ -387,7 +422,7 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ int sid, sinst, sfail, spoll, snext;
-    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ __align__(8) uint64_t mbar[GB_TC_NBAR];
     __shared__ uint32_t tmem_base;
     if (threadIdx.x == 0) {
         spoll = dag_role(D.Q);
@@ -405,8 +440,8 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
     if constexpr (TC && sizeof(T) == 4) {
         {
             if (threadIdx.x == 0) {
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(gb_su32(&mbar[0])), "r"(1));
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(gb_su32(&mbar[1])), "r"(1));
+                for (int i = 0; i < GB_TC_NBAR; i++)
+                    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(gb_su32(&mbar[i])), "r"(1));
                 asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             }
             if (threadIdx.x < 32) {
@@ -546,7 +581,8 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                 q = w3;
             }
         } else {
-            dag_tile_task<T>(P, tk, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr);
+            dag_tile_task<T>(P, tk, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr,
+                             TC ? D.img : nullptr);
             if (TC && tc && !tcx.ok) {
                 // a tensor-core wait gave up: stop the executor (every block
                 // returns on the error word)
@@ -593,12 +629,8 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
         }
     }
     if (TC && tc) {
-        if (!tcx.ok) {
-            // MMAs may still be in flight: wait once more on each stage
-            // (bounded) before the accumulators are released
-            gb_mbar_wait(tcx.mbar, tcx.phase & 1u);
-            gb_mbar_wait(tcx.mbar + 8, (tcx.phase >> 1) & 1u);
-        }
+        // (a tile product whose wait gave up has already waited, bounded,
+        // for its copies and MMAs in flight)
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
         if (threadIdx.x < 32)
@@ -618,7 +650,8 @@ int gb_launch_fdag(const gb_fdag_args *a, void *Lx, void *CB, void *Linv, int dt
     D.pats = a->pats; D.inst = a->inst; D.ibase = a->inst_base; D.ninst = a->ninst;
     D.cnt = a->cnt; D.trace = a->trace;
     D.Sx = a->Sx; D.a_dtype = a->a_dtype; D.scale = a->scale; D.beta = a->beta;
-    D.use_tc = a->use_tc;
+    D.use_tc = a->use_tc && a->img;
+    D.img = a->img;
     static int configured = 0;
     if (!configured) {
         cudaFuncSetAttribute(k_fdag<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<double>());

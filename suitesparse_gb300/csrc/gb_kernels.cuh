@@ -85,6 +85,9 @@ typedef struct { int32_t type, s, b, r, c, prio, pad0, pad1; } gb_dtask;
 #define GB_DAG_NSMF 1024    /* per-SM poller marks (indexed by %smid) */
 
 #define GB_NB 64            /* block size of the blocked paths */
+/* floats of one tensor-core operand image (a 64-row block of a 64-column
+ * panel, split into TF32 hi and FP32 lo parts): GB_IMG_FLOATS on the device */
+#define GB_IMG_FLOATS_HOST 8192
 #define GB_TILE 64          /* output tile edge of the update kernel */
 #define GB_TRSM_ROWS 64     /* rows per triangular-solve task */
 #define GB_SMALL_MAX 64     /* widest supernode factored by one block */

@@ -355,7 +355,16 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
         a.a_dtype = adt;
         a.scale = scale;
         a.beta = beta;
-        a.use_tc = ctx->tc_mode;
+        a.use_tc = ctx->tc_mode && l_dtype == CHOLMOD_SINGLE && P->img_total > 0;
+        if (a.use_tc && !P->d_img
+            && cudaMalloc((void **)&P->d_img, sizeof(float) * GB_IMG_FLOATS_HOST * (size_t)P->img_total)
+                   != cudaSuccess) {
+            /* no room for the operand images: the CUDA cores take the tiles */
+            P->d_img = NULL;
+            cudaGetLastError();
+            a.use_tc = 0;
+        }
+        a.img = a.use_tc ? P->d_img : NULL;
         if (ctx->trace_on) {
             size_t need = 3 * (N + 1) * sizeof(unsigned long long);
             if (gb_dev_grow((void **)&ctx->d_ftrace, &ctx->ftrace_cap, need)) {

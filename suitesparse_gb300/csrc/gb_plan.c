@@ -746,29 +746,34 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
                 double mm = (double)m;
                 P->fl_dag += mm * (mm + 1) / 2.0 * 2.0 * (double)nscol;     /* update block */
             }
-            /* update-block tiles (k = nscol) */
-            for (Int J = 0; J < m && ok; J += NB) {
+            /* update-block tiles (k = nscol).  A supernode with panel tasks
+             * tiles its update block on the 64-row grid of its own rows
+             * (tk.b = 1), so that a tile's operand rows are exactly the
+             * row blocks the panel solves produce (and write as the
+             * tensor-core operand images); tile (r, c) needs the last
+             * panel's solves of row blocks r and c. */
+            if (Pid && m > 0) {
+                const Int lastb = Cp - 1;
+                for (Int cc = nscol / NB; cc < R && ok; cc++) {
+                    for (Int r = cc; r < R && ok; r++) {
+                        gb_dtask ct = {GB_DT_CB, (int32_t)s, 1, (int32_t)r, (int32_t)cc, 1, 0, 0};
+                        int32_t cid = base + (int32_t)(P->dag_t.n - t0g);
+                        ok &= gb_vec_push(&P->dag_t, &ct);
+                        int32_t t1 = Tid[lastb * R + r], t2 = Tid[lastb * R + cc];
+                        if (t1 < 0 || t2 < 0) { ok = 0; break; }
+                        int32_t e[2] = {t1, cid};
+                        ok &= gb_vec_push(&edges, e);
+                        if (t2 != t1) { e[0] = t2; ok &= gb_vec_push(&edges, e); }
+                    }
+                }
+            }
+            /* a narrow supernode (factored whole by one SMALL task, which
+             * precedes these tiles through its join): the update block's
+             * own 64-grid */
+            for (Int J = 0; !Pid && J < m && ok; J += NB) {
                 for (Int I = J; I < m; I += NB) {
                     gb_dtask ct = {GB_DT_CB, (int32_t)s, 0, (int32_t)(I / NB), (int32_t)(J / NB), 1, 0, 0};
-                    int32_t cid = base + (int32_t)(P->dag_t.n - t0g);
                     ok &= gb_vec_push(&P->dag_t, &ct);
-                    if (Pid) {
-                        /* rows of L21 tiles I and J final: last panel solves */
-                        Int lastb = Cp - 1;
-                        Int rows[2] = {nscol + I, nscol + J};
-                        int32_t prev = -1;
-                        for (int w = 0; w < 2; w++) {
-                            Int rlo = rows[w] / NB, rhi = GB_MIN(rows[w] + NB, nsrow) - 1;
-                            rhi /= NB;
-                            for (Int r = rlo; r <= rhi; r++) {
-                                int32_t t = Tid[lastb * R + r];
-                                if (t < 0 || t == prev) continue;
-                                int32_t e[2] = {t, cid};
-                                ok &= gb_vec_push(&edges, e);
-                                prev = t;
-                            }
-                        }
-                    }
                 }
             }
             free(Pid); free(Tid); free(Uid);
@@ -1094,6 +1099,23 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
         P->h_linvoff[nblk_total] = off;
         P->linv_total = off;
     }
+    /* tensor-core operand images: a supernode with panel tasks (wider than
+     * small_cols) has one per panel b < Cp and row block b <= r < R */
+    P->h_imgbase = malloc(sizeof(int64_t) * (P->nsuper + 1));
+    if (!P->h_imgbase) ok = 0;
+    if (ok) {
+        int64_t tot = 0;
+        for (Int s = 0; s < P->nsuper; s++) {
+            const Int nscol = Super[s + 1] - Super[s], nsrow = Pi[s + 1] - Pi[s];
+            P->h_imgbase[s] = -1;
+            if (nscol <= small_cols) continue;
+            const int64_t Cp = (nscol + GB_NB - 1) / GB_NB, R = (nsrow + GB_NB - 1) / GB_NB;
+            P->h_imgbase[s] = tot;
+            tot += Cp * R - Cp * (Cp - 1) / 2;
+        }
+        P->h_imgbase[P->nsuper] = tot;
+        P->img_total = tot;
+    }
     if (!ok) goto fail;
 
     P->h_child_ptr = child_ptr;
@@ -1196,6 +1218,7 @@ int gb_plan_upload(gb_plan *P)
     UP(P->d_ntask_b, P->h_ntask_b, sizeof(int32_t) * (ns + 1));
     UP(P->d_parent, P->h_parent, sizeof(int32_t) * (ns + 1));
     UP(P->d_linvoff, P->h_linvoff, sizeof(int64_t) * (P->nblk_total + 1));
+    UP(P->d_imgbase, P->h_imgbase, sizeof(int64_t) * (ns + 1));
     if (cudaMalloc((void **)&P->d_xready, sizeof(int32_t) * (P->nblk_total + 1)) != cudaSuccess) goto fail;
     if (cudaMalloc((void **)&P->d_done, sizeof(int32_t) * (ns + 1)) != cudaSuccess) goto fail;
     if (cudaMalloc((void **)&P->d_ticket, sizeof(int32_t) * 4) != cudaSuccess) goto fail;
@@ -1213,6 +1236,7 @@ int gb_plan_upload(gb_plan *P)
     P->ptrs.anyfail = P->d_anyfail;
     P->ptrs.blkoff = P->d_blkoff;
     P->ptrs.linvoff = P->d_linvoff;
+    P->ptrs.imgbase = P->d_imgbase;
     UP(P->d_chunk, P->h_chunk, sizeof(gb_seg_chunk) * P->nchunk);
     if (cudaMalloc((void **)&P->d_anorm_seg, sizeof(double) * (P->nseg + 1)) != cudaSuccess) goto fail;
     /* whole-factorization task graph, one instance */
@@ -1264,6 +1288,7 @@ void gb_plan_free(gb_plan *P)
     free(P->h_cboff); free(P->h_cbvoff);
     free(P->h_blkoff); free(P->h_ntask_f); free(P->h_ntask_b); free(P->h_parent);
     free(P->h_linvoff);
+    free(P->h_imgbase);
     gb_vec_free(&P->sf_t); gb_vec_free(&P->sb_t); gb_vec_free(&P->sd_t);
     gb_vec_free(&P->lf_t);
     gb_vec_free(&P->sf_cptr); gb_vec_free(&P->sf_crange);
@@ -1293,7 +1318,7 @@ void gb_plan_free(gb_plan *P)
                    P->d_dag_cnt, P->d_dag_q, P->d_dag_ctrl, P->d_dag_smf, P->d_fd_t,
                    P->d_fd_sp, P->d_fd_succ, P->d_fd_nd, P->d_fd_qi, P->d_fd_ctrl0,
                    P->d_fd_cnt, P->d_fd_q, P->d_fd_pat, P->d_fd_inst, P->d_fd_ibase, P->d_fd_sub,
-                   P->d_fd_smeta,
+                   P->d_fd_smeta, P->d_imgbase, P->d_img,
                    P->d_chunk, P->d_anorm_seg, P->d_bred, P->d_gf, P->d_gb};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++)
         if (dev[i]) cudaFree(dev[i]);

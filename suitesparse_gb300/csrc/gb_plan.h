@@ -23,6 +23,7 @@ typedef struct {
     int32_t *fail, *anyfail;
     const int32_t *blkoff;
     const int64_t *linvoff;
+    const int64_t *imgbase;          /* first tensor-core operand image of s, -1 if none */
 } gb_pattern_ptrs;
 
 enum {
@@ -89,6 +90,7 @@ typedef struct {
     const double *scale;             /* optional D A D scaling */
     double beta;
     int use_tc;                      /* FP32 tile products on the tensor cores */
+    float *img;                      /* their operand images (GB_IMG_FLOATS each) */
 } gb_fdag_args;
 
 /* right-hand-side columns per single-launch sweep pass, and passes that run
@@ -194,6 +196,13 @@ typedef struct gb_plan {
     int64_t *h_linvoff;
     void *d_Linv[2];
     int linv_valid[2];
+
+    /* split operand images of the tensor-core tile products (FP32): per
+     * supernode with tile tasks, one per panel b and 64-row block r >= b
+     * (written by the panel solves, read by bulk copies) */
+    int64_t *h_imgbase, *d_imgbase;
+    int64_t img_total;                /* images (GB_IMG_FLOATS floats each) */
+    float *d_img;
 
     /* numeric buffers, [0] double, [1] single */
     void *d_Lx[2], *d_CB[2];
