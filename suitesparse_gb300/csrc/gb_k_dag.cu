@@ -280,30 +280,38 @@ __device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx
         trsm_task<T>(P, tk, panel, nscol, nsrow, f, Linv, smem_raw, img ? Img : nullptr);
     } else if (tk.type == GB_DT_UPD) {
         if (f < 0) {
-            const int c0 = 64 * tk.b, nb = min(64, nscol - c0);
+            // panels b .. b + nbk - 1 at once: k = their columns
+            const int nbk = max(1, tk.nbk);
+            const int c0 = 64 * tk.b, kk = min(64 * (tk.b + nbk), nscol) - c0;
             const int cs = 64 * tk.c, ce = min(cs + 64, nscol);
             const int rs = max(64 * tk.r, cs), re = min(64 * tk.r + 64, nsrow);
             if constexpr (sizeof(T) == 4) {
                 if (img) {
                     // rows 64 r.. of the images of row blocks r and c of
-                    // panel b (rs = 64 r: r >= c)
+                    // those panels (rs = 64 r: r >= c); the last panel's
+                    // second K chunk is empty when it is at most 32 wide
+                    const int nb_last = kk - 64 * (nbk - 1);
                     gemm_img_tc(Img, P.imgbase[s], (nsrow + 63) / 64, tk.r, tk.c, tk.b,
-                                nb > 32 ? 2 : 1, (float *)Lx, P.Px[s] + rs + (int64_t)cs * nsrow, nsrow,
+                                2 * nbk - (nb_last > 32 ? 0 : 1), (float *)Lx,
+                                P.Px[s] + rs + (int64_t)cs * nsrow, nsrow,
                                 0, re - rs, 0, ce - cs, tk.r == tk.c, smem_raw, *tc);
                     return;
                 }
-                // k = 64: the CUDA cores (the tensor-core tile's fixed costs
-                // make it slower at this depth)
                 gemm_tile_f32(panel + rs + (int64_t)c0 * nsrow, nsrow,
-                                  panel + cs + (int64_t)c0 * nsrow, nsrow,
-                                  panel + rs + (int64_t)cs * nsrow, nsrow,
-                                  re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, (float *)smem_raw);
+                              panel + cs + (int64_t)c0 * nsrow, nsrow,
+                              panel + rs + (int64_t)cs * nsrow, nsrow,
+                              re - rs, ce - cs, kk, tk.r == tk.c, cs - rs, (float *)smem_raw);
             }
-            else
+            else if (kk <= 64)
                 gemm_tile_k64<T>(panel + rs + (int64_t)c0 * nsrow, nsrow,
                                  panel + cs + (int64_t)c0 * nsrow, nsrow,
                                  panel + rs + (int64_t)cs * nsrow, nsrow,
-                                 re - rs, ce - cs, nb, tk.r == tk.c, cs - rs, S1, S2);
+                                 re - rs, ce - cs, kk, tk.r == tk.c, cs - rs, S1, S2);
+            else
+                gemm_tile_nt<T>(panel + rs + (int64_t)c0 * nsrow, nsrow,
+                                panel + cs + (int64_t)c0 * nsrow, nsrow,
+                                panel + rs + (int64_t)cs * nsrow, nsrow,
+                                re - rs, ce - cs, kk, tk.r == tk.c, cs - rs, S1, S2);
         }
     } else {  // GB_DT_CB
         if (f < 0) {
@@ -346,7 +354,7 @@ template <typename T>
 __global__ void __launch_bounds__(256, 2)
 k_dag(gb_dev_pattern P, gb_dag_dev D, T *Lx, T *CB, T *Linv)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ int sid, sfail, spoll;
     if (threadIdx.x == 0) spoll = dag_role(D.Q);
     __syncthreads();

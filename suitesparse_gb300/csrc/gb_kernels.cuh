@@ -47,12 +47,16 @@ typedef struct { int32_t s, kind, idx, r0, nr, pad0, pad1, pad2; } gb_stask;
  * tiles of the panel of s; c0 = 64 b):
  *   POTRF (s, b)       LL' + inverse of the diagonal block of column block b
  *   TRSM  (s, b, r)    panel rows of row tile r below that block
- *   UPD   (s, b, r, c) tile (r, c) of the panel -= L(r, blk b) L(c, blk b)'
+ *   UPD   (s, b, r, c) tile (r, c) of the panel -= L(r, blks b..b+nbk-1)
+ *                      L(c, blks b..b+nbk-1)' (nbk panels at once, k up
+ *                      to 64 nbk)
  *   CB    (s, r, c)    update-block tile (r, c) -= L21(r) L21(c)', k = nscol
  * prio 0 = the tasks near the diagonal that the next steps wait on
- * (POTRF; TRSM of row tiles <= b+3; UPD of tiles r <= b+3, c <= b+2),
- * 1 = bulk. */
-typedef struct { int32_t type, s, b, r, c, prio, pad0, pad1; } gb_dtask;
+ * (POTRF; TRSM of row tiles <= b+3; UPD of tiles r <= b+3, c <= b+2, and
+ * the grouped updates of the next group's first column), 1 = bulk. */
+typedef struct { int32_t type, s, b, r, c, prio, nbk, pad1; } gb_dtask;
+/* panels whose trailing updates are applied at once (GB_DT_UPD nbk) */
+#define GB_UPD_GROUP 4
 #define GB_DT_POTRF 1
 #define GB_DT_TRSM  2
 #define GB_DT_UPD   3

@@ -668,12 +668,26 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
             Int nscol = Super[s + 1] - Super[s], nsrow = Pi[s + 1] - Pi[s];
             Int m = nsrow - nscol;
             Int Cp = (nscol + NB - 1) / NB, R = (nsrow + NB - 1) / NB;
-            int32_t *Pid = NULL, *Tid = NULL, *Uid = NULL;
+            int32_t *Pid = NULL, *Tid = NULL, *Uid = NULL, *Aid = NULL;
             if (nscol > small_cols) {
+                /* Blocked right-looking LL' in 64-column panels, grouped by
+                 * GB_UPD_GROUP panels: a tile (r, c) takes the update of
+                 * each earlier panel of c's own group separately (UPD with
+                 * one panel: the lookahead that the next diagonal steps
+                 * wait on) and the updates of each earlier group at once
+                 * (UPD with GB_UPD_GROUP panels, k up to 256), so that the
+                 * bulk of the trailing update runs as deeper, fewer tile
+                 * products.  Updates of one tile run in panel order. */
+                const Int G = GB_UPD_GROUP, Q = (Cp + G - 1) / G;
                 Pid = malloc(sizeof(int32_t) * Cp);
                 Tid = malloc(sizeof(int32_t) * Cp * R);
                 Uid = malloc(sizeof(int32_t) * Cp * R * Cp);
-                if (!Pid || !Tid || !Uid) { free(Pid); free(Tid); free(Uid); ok = 0; break; }
+                Aid = malloc(sizeof(int32_t) * Q * R * Cp);
+                if (!Pid || !Tid || !Uid || !Aid) {
+                    free(Pid); free(Tid); free(Uid); free(Aid);
+                    ok = 0;
+                    break;
+                }
                 for (Int b = 0; b < Cp; b++) {
                     Int c0 = b * NB, nb = GB_MIN(NB, nscol - c0);
                     gb_dtask pt = {GB_DT_POTRF, (int32_t)s, (int32_t)b, 0, 0, 0, 0, 0};
@@ -689,22 +703,42 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
                         Tid[b * R + r] = base + (int32_t)(P->dag_t.n - t0g);
                         ok &= gb_vec_push(&P->dag_t, &tt);
                     }
+                    /* single-panel updates of the tiles in b's own group */
                     for (Int cc = 0; cc < Cp; cc++) {
                         for (Int r = 0; r < R; r++) {
                             Uid[(b * R + r) * Cp + cc] = -1;
-                            if (cc <= b || r < cc) continue;
+                            if (cc <= b || r < cc || cc / G != b / G) continue;
                             gb_dtask ut = {GB_DT_UPD, (int32_t)s, (int32_t)b, (int32_t)r, (int32_t)cc,
-                                           (cc <= b + 2 && r <= b + 3) ? 0 : 1, 0, 0};
+                                           (cc <= b + 2 && r <= b + 3) ? 0 : 1, 1, 0};
                             Uid[(b * R + r) * Cp + cc] = base + (int32_t)(P->dag_t.n - t0g);
                             ok &= gb_vec_push(&P->dag_t, &ut);
                         }
                     }
+                    /* after the group's last panel: its update of every tile
+                     * right of the group */
+                    if (b % G == G - 1 || b == Cp - 1) {
+                        const Int q = b / G, bq = q * G;
+                        for (Int cc = 0; cc < Cp; cc++) {
+                            for (Int r = 0; r < R; r++) {
+                                Aid[(q * R + r) * Cp + cc] = -1;
+                                if (cc < G * (q + 1) || r < cc) continue;
+                                gb_dtask at = {GB_DT_UPD, (int32_t)s, (int32_t)bq, (int32_t)r, (int32_t)cc,
+                                               (cc == G * (q + 1) && r <= cc + 3) ? 0 : 1,
+                                               (int32_t)(b + 1 - bq), 0};
+                                Aid[(q * R + r) * Cp + cc] = base + (int32_t)(P->dag_t.n - t0g);
+                                ok &= gb_vec_push(&P->dag_t, &at);
+                            }
+                        }
+                    }
                 }
+                /* the last update task of tile (r, c), r >= c, or -1 */
+#define LASTU(r, c) (((c) % G) ? Uid[(((c) - 1) * R + (r)) * Cp + (c)]             \
+                     : ((c) > 0 ? Aid[(((c) / G - 1) * R + (r)) * Cp + (c)] : -1))
                 /* edges of the blocked right-looking factorization */
                 for (Int b = 0; b < Cp && ok; b++) {
                     int32_t e[2];
-                    if (b > 0) {
-                        e[0] = Uid[((b - 1) * R + b) * Cp + b]; e[1] = Pid[b];
+                    if (LASTU(b, b) >= 0) {
+                        e[0] = LASTU(b, b); e[1] = Pid[b];
                         ok &= gb_vec_push(&edges, e);
                     }
                     for (Int r = b; r < R; r++) {
@@ -712,24 +746,45 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
                         if (t < 0) continue;
                         e[0] = Pid[b]; e[1] = t;
                         ok &= gb_vec_push(&edges, e);
-                        if (b > 0) {
-                            e[0] = Uid[((b - 1) * R + r) * Cp + b]; e[1] = t;
+                        if (LASTU(r, b) >= 0) {
+                            e[0] = LASTU(r, b); e[1] = t;
                             ok &= gb_vec_push(&edges, e);
                         }
                     }
                     for (Int cc = b + 1; cc < Cp; cc++) {
+                        if (cc / G != b / G) continue;
                         for (Int r = cc; r < R; r++) {
                             int32_t u = Uid[(b * R + r) * Cp + cc];
                             e[1] = u;
                             e[0] = Tid[b * R + r]; ok &= gb_vec_push(&edges, e);
                             if (r != cc) { e[0] = Tid[b * R + cc]; ok &= gb_vec_push(&edges, e); }
-                            if (b > 0) {
-                                e[0] = Uid[((b - 1) * R + r) * Cp + cc];
-                                ok &= gb_vec_push(&edges, e);
+                            /* the previous update of the tile: this group's
+                             * previous panel, or the previous group at once */
+                            int32_t pv = (b % G) ? Uid[((b - 1) * R + r) * Cp + cc]
+                                         : (b > 0 ? Aid[((b / G - 1) * R + r) * Cp + cc] : -1);
+                            if (pv >= 0) { e[0] = pv; ok &= gb_vec_push(&edges, e); }
+                        }
+                    }
+                    if (b % G == G - 1 || b == Cp - 1) {
+                        /* the group's panel solves of rows r and cc: the last
+                         * panel's (each earlier one precedes it through the
+                         * tile (r, b) updates) */
+                        const Int q = b / G;
+                        for (Int cc = G * (q + 1); cc < Cp; cc++) {
+                            for (Int r = cc; r < R; r++) {
+                                int32_t u = Aid[(q * R + r) * Cp + cc];
+                                e[1] = u;
+                                e[0] = Tid[b * R + r]; ok &= gb_vec_push(&edges, e);
+                                if (r != cc) { e[0] = Tid[b * R + cc]; ok &= gb_vec_push(&edges, e); }
+                                if (q > 0) {
+                                    e[0] = Aid[((q - 1) * R + r) * Cp + cc];
+                                    ok &= gb_vec_push(&edges, e);
+                                }
                             }
                         }
                     }
                 }
+#undef LASTU
             }
             if (Pid) {
                 /* algorithmic flops of the panel tasks (2 per multiply-add) */
@@ -776,7 +831,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
                     ok &= gb_vec_push(&P->dag_t, &ct);
                 }
             }
-            free(Pid); free(Tid); free(Uid);
+            free(Pid); free(Tid); free(Uid); free(Aid);
         }
         if (!ok) break;
         /* CSR of successors, dependency counts, initial ready lists */
