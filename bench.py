@@ -374,9 +374,9 @@ def run_gpu(args):
         solves[str(k)] = {"solves_per_s": k / (statistics.mean(ts) * 1e-3),
                           "iterations": rk["iterations"], "berr": rk["berr"]}
 
-    # the same step with the update-block tiles on the tensor cores
-    # (GB300_OPT_TENSOR; opt-in: its factor error costs a refinement step)
-    c.set_option(CH.GB300_OPT_TENSOR, 1)
+    # the same step with the tile products on the CUDA cores instead of the
+    # tensor cores (GB300_OPT_TENSOR = 0), for comparison
+    c.set_option(CH.GB300_OPT_TENSOR, 0)
     tc_fac, tc_sol, tc_it, tc_be = [], [], [], []
     for i in range(4):
         f_ms, s_ms, _, Xt, rt_ = step_mixed()
@@ -385,14 +385,14 @@ def run_gpu(args):
             tc_sol.append(s_ms)
             tc_it.append(rt_["iterations"])
     tc_be = float(O.backward_error(n, Ap, Ai, Ax, Xt, B).max())
-    c.set_option(CH.GB300_OPT_TENSOR, 0)
-    tensor = {"factor_ms": statistics.mean(tc_fac),
-              "factor_tflops": fl / (statistics.mean(tc_fac) * 1e-3) / 1e12,
-              "refine_ms": statistics.mean(tc_sol), "refine_iterations": tc_it[-1],
-              "solves_per_s": 1e3 / (statistics.mean(tc_fac) + statistics.mean(tc_sol)),
-              "backward_error": tc_be,
-              "note": "update-block tiles of depth >= 128 as tcgen05 kind::tf32 MMAs "
-                      "(hi/lo split, 4 products); default off"}
+    c.set_option(CH.GB300_OPT_TENSOR, 1)
+    cuda_cores = {"factor_ms": statistics.mean(tc_fac),
+                  "factor_tflops": fl / (statistics.mean(tc_fac) * 1e-3) / 1e12,
+                  "refine_ms": statistics.mean(tc_sol), "refine_iterations": tc_it[-1],
+                  "solves_per_s": 1e3 / (statistics.mean(tc_fac) + statistics.mean(tc_sol)),
+                  "backward_error": tc_be,
+                  "note": "GB300_OPT_TENSOR = 0: the tile products as FP32 multiply-adds on "
+                          "the CUDA cores (the headline uses the tensor cores)"}
 
     # roofline of the dominant kernel (tile update) from a profiled factorization
     c.set_option(CH.GB300_OPT_PROFILE, 1)
@@ -441,13 +441,14 @@ def run_gpu(args):
         "speedup_solves_vs_fp64": (1e3 / statistics.mean(t_step)) /
                                   (1e3 / (statistics.mean(fp64_fac) + statistics.mean(fp64_sol))),
         "resident_factor_solves": solves,
-        "tensor_cores": tensor,
+        "cuda_cores_variant": cuda_cores,
         "e2e": {"value": e2e_val, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "solves_per_s": 1.0 / statistics.mean(e2e_s) * ws},
-        "roofline": {"kernel": "k_fdag<float> (whole-factorization task graph: assembly, "
+        "roofline": {"kernel": "k_fdag<float, true> (whole-factorization task graph: assembly, "
                                "small supernodes, tile LL', panel solves, tile and "
-                               "update-block products; achieved = tile-task flops / launch time)",
+                               "update-block products on the tensor cores; achieved = "
+                               "tile-task flops / launch time)",
                      "bound": "tensor", "achieved": achieved,
                      "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": (achieved / peaks["bf16_tflops"]) if achieved else None,

@@ -404,10 +404,15 @@ int gb300_finish (cholmod_common *Common) ;
  *      supernodes, tiles of the wide supernodes, update blocks; a supernode
  *      starts when its children's update blocks are done); 0 = one launch
  *      of each kind per etree level, levels in sequence.
- *  GB300_OPT_TENSOR [0]: 1 = in the FP32 factorization the tile and
- *      update-block products run on the tensor cores (tcgen05, operands
- *      split into two TF32 parts, three products, FP32 accumulation);
- *      0 = FP32 multiply-adds on the CUDA cores. */
+ *  GB300_OPT_TENSOR [1]: 1 = in the FP32 factorization the tile and
+ *      update-block products of the supernodes wider than the small
+ *      cutoff run on the tensor cores (tcgen05 kind::tf32; the panel solves
+ *      write each 64 x 64 block of L split into TF32 hi and FP32 lo parts,
+ *      the products stage these by bulk asynchronous copies and form all
+ *      four hi/lo products, draining the accumulator into FP32 sums every
+ *      64 of K); 0 = FP32 multiply-adds on the CUDA cores.  The operand
+ *      images take twice the FP32 factor's memory; when they cannot be
+ *      allocated the CUDA cores take the products. */
 #define GB300_OPT_KEEP_ON_DEVICE 1
 #define GB300_OPT_SMALL_COLS     2
 #define GB300_OPT_PROFILE        3

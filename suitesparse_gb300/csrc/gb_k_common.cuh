@@ -648,8 +648,11 @@ __device__ __forceinline__ void gemm_tile_f32(const float *A, int64_t lda, const
 #define GB_IMG_NS 3
 #define GB_TC_SMEM (GB_IMG_NS * 32768)
 // K chunks (32 deep) accumulated in one TMEM accumulator before it is
-// drained into FP32 registers
-#define GB_IMG_GROUP 8
+// drained into FP32 registers: 2 (8 MMA steps) keeps the factor's error
+// near that of FP32 sums on the CUDA cores (1.37e-7 vs 1.24e-7 relative to
+// the FP64 factor on a 40^3 Laplacian; with 8 chunks 1.67e-7, and the
+// 64^3 case's refinement sometimes needed a third step)
+#define GB_IMG_GROUP 2
 // one image: a 64-row block of one 64-column panel, split x = hi + lo
 // (hi = x rounded to TF32), as two K chunks of 32, each [hi rows 0-63;
 // lo rows 64-127] x 32 in the canonical K-major no-swizzle layout of
@@ -793,9 +796,9 @@ __device__ __forceinline__ void gb_img_store(const float (&acc)[4][4], int nr, i
 // and the MMAs (committed to the stage's empty barrier), GB_IMG_NS - 1
 // chunks ahead.  Every GB_IMG_GROUP chunks the accumulator alternates, and
 // the one just finished is drained by all threads into FP32 registers (sums
-// over at most 256 of K, then summed with round-to-nearest adds: the
-// tensor core's FP32 accumulation truncates, and its error would otherwise
-// grow linearly with K).  The epilogue adds the hi and lo rows' sums
+// over at most 64 of K, then summed with round-to-nearest adds: the tensor
+// core's FP32 accumulation truncates, and its error would otherwise grow
+// linearly with K).  The epilogue adds the hi and lo rows' sums
 // through shared memory and updates C, whose values were loaded while the
 // operands were in flight.  Every wait is bounded; returns false when one
 // gave up (tc.ok = 0), after waiting (bounded) for the copies and MMAs in

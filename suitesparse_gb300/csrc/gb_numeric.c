@@ -29,7 +29,7 @@ gb_ctx *gb_ctx_new(void)
     c->device = -1;
     c->sweep_mode = 1;
     c->factor_mode = 1;
-    c->tc_mode = 0;
+    c->tc_mode = 1;
     c->pivot_log2 = 23;
     c->graph_mode = 1;
     c->sweep_streams = 2;

@@ -277,7 +277,7 @@ struct gb_ctx {
     int prof;
     int sweep_mode;              /* 1 = single-launch sweeps (default), 0 = per level */
     int factor_mode;             /* 1 = one whole-factorization launch (default), 0 = per level */
-    int tc_mode;                 /* 1 = FP32 tile products on the tensor cores (default 0) */
+    int tc_mode;                 /* 1 = FP32 tile products on the tensor cores (default) */
     int pivot_log2;              /* small-pivot threshold of the FP32 factor: 2^-pivot_log2 */
     int trace_on;                /* record per-task times of the sweeps */
     int graph_mode;              /* 1 = refinement steps replayed from a CUDA graph (default) */
