@@ -147,124 +147,6 @@ __device__ void trsm_tile(const T *Bt, const T *Lt, int ldt, int nr, int nc, int
     }
 }
 
-// LL' of a 64 x 64 (nb <= 64) lower block in shared memory A (leading
-// dimension 65) with 256 threads, blocked by 16 columns: warp 0 factors the
-// 16 x 16 diagonal block in registers (lane = row, columns exchanged by
-// shuffles), the rows below solve against it in registers, and the trailing
-// lower part takes the rank-16 update.  Returns the first column whose
-// pivot is not positive (earlier columns are final), or -1.
-template <typename T>
-__device__ int potrf64(T (*A)[65], int nb, int *sfail)
-{
-    const int tid = threadIdx.x;
-    if (tid == 0) *sfail = -1;
-    __syncthreads();
-    for (int p0 = 0; p0 < nb; p0 += 16) {
-        const int pw = min(16, nb - p0);
-        if (tid < 32) {
-            const int i = tid;
-            T row[16];
-#pragma unroll
-            for (int k = 0; k < 16; k++) row[k] = (i < pw && k <= i) ? A[p0 + i][p0 + k] : (T)0;
-            int bad = -1;
-#pragma unroll
-            for (int j = 0; j < 16; j++) {
-                if (j < pw && bad < 0) {
-                    const T d = __shfl_sync(0xffffffffu, row[j], j);
-                    if (!(d > (T)0)) {
-                        bad = j;
-                    } else {
-                        const T sd = gb_sqrt<T>(d);
-                        if (i == j) row[j] = sd;
-                        else if (i > j) row[j] /= sd;
-#pragma unroll
-                        for (int k = j + 1; k < 16; k++) {
-                            const T lkj = __shfl_sync(0xffffffffu, row[j], k);
-                            if (i >= k && k < pw) row[k] -= row[j] * lkj;
-                        }
-                    }
-                }
-            }
-            if (i < pw) {
-#pragma unroll
-                for (int k = 0; k < 16; k++)
-                    if (k <= i) A[p0 + i][p0 + k] = row[k];
-            }
-            if (i == 0 && bad >= 0) *sfail = p0 + bad;
-        }
-        __syncthreads();
-        if (*sfail >= 0) return *sfail;
-        // rows below the diagonal block: forward substitution in registers
-        for (int r = p0 + pw + tid; r < nb; r += blockDim.x) {
-            T x[16];
-#pragma unroll
-            for (int k = 0; k < 16; k++) x[k] = (k < pw) ? A[r][p0 + k] : (T)0;
-#pragma unroll
-            for (int j = 0; j < 16; j++) {
-                if (j < pw) {
-                    T v = x[j];
-#pragma unroll
-                    for (int k = 0; k < j; k++) v -= x[k] * A[p0 + j][p0 + k];
-                    x[j] = v / A[p0 + j][p0 + j];
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < 16; k++)
-                if (k < pw) A[r][p0 + k] = x[k];
-        }
-        __syncthreads();
-        // trailing lower part: rank-pw update, one (row, 8-column group) each
-        const int t0 = p0 + pw, nt = nb - t0;
-        const int ngroups = (nt + 7) / 8;
-        for (int w = tid; w < nt * ngroups; w += blockDim.x) {
-            const int r = t0 + w / ngroups, cb = t0 + 8 * (w % ngroups);
-            if (cb > r) continue;
-            T a[16];
-#pragma unroll
-            for (int k = 0; k < 16; k++) a[k] = (k < pw) ? A[r][p0 + k] : (T)0;
-            for (int cc = cb; cc < cb + 8 && cc <= r; cc++) {
-                T acc = A[r][cc];
-#pragma unroll
-                for (int k = 0; k < 16; k++) acc -= a[k] * A[cc][p0 + k];
-                A[r][cc] = acc;
-            }
-        }
-        __syncthreads();
-    }
-    return -1;
-}
-
-// X = L^-1 of the factored lower block A (leading dimension 65), formed in
-// shared memory X (column j at X + j*65 by thread j < nb, four partial sums
-// per entry) and then stored to out (column-major, leading dimension nb).
-template <typename T>
-__device__ void tri_inverse64(const T (*A)[65], int nb, T *X, T *out)
-{
-    const int j = threadIdx.x;
-    if (j < nb) {
-        T *x = X + j * 65;
-        for (int i = 0; i < j; i++) x[i] = (T)0;
-        x[j] = (T)1 / A[j][j];
-        for (int i = j + 1; i < nb; i++) {
-            T a0 = (T)0, a1 = (T)0, a2 = (T)0, a3 = (T)0;
-            int k = j;
-            for (; k + 3 < i; k += 4) {
-                a0 += A[i][k] * x[k];
-                a1 += A[i][k + 1] * x[k + 1];
-                a2 += A[i][k + 2] * x[k + 2];
-                a3 += A[i][k + 3] * x[k + 3];
-            }
-            for (; k < i; k++) a0 += A[i][k] * x[k];
-            x[i] = -((a0 + a1) + (a2 + a3)) / A[i][i];
-        }
-    }
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
-        const int i = idx % nb, jj = idx / nb;
-        out[i + (int64_t)jj * nb] = X[jj * 65 + i];
-    }
-}
-
 // C(m x n) -= A(m x 64) B(n x 64)' with both operands staged whole in
 // shared memory (As[k*65 + i], Bs[k*65 + i]); 256 threads, 4x4 each; store
 // only r - c >= diag_off when lower.  k <= 64.
@@ -314,19 +196,22 @@ template <typename T> __device__ __forceinline__ T gb_rsqrt(T x);
 template <> __device__ __forceinline__ double gb_rsqrt<double>(double x) { return rsqrt(x); }
 template <> __device__ __forceinline__ float gb_rsqrt<float>(float x) { return rsqrtf(x); }
 
-// One warp, lane i = row i of a 16 x 16 lower block held in registers
-// (row[k] = A(i, k), k <= i; rows >= pw are zero): LL' in place, pivots by
-// reciprocal square root (L(j,j) = d rsqrt(d), column j scaled by rsqrt(d)).
-// rinv receives 1 / L(i,i) in lane i.  Returns the first column whose pivot
-// is not positive (the same in every lane), or -1.
+// One warp, lane i = row i of the lower n x n (n <= 32) block held in
+// registers (row[k] = A(i, k) for k <= i, zero elsewhere and in rows >= n):
+// right-looking LL' in place, column j's pivot broadcast by shuffle, L(j,j)
+// = d rsqrt(d), the column scaled by rsqrt(d), the trailing rows updated
+// with L(k, j) from lane k.  rinv receives 1 / L(i,i) in lane i (0 from the
+// failing column on).  Returns the first column whose pivot is not positive
+// (the same in every lane; earlier columns are final), or -1.
 template <typename T>
-__device__ __forceinline__ int warp_potrf16(T (&row)[16], T &rinv, int pw)
+__device__ __forceinline__ int warp_chol32(T (&row)[32], T &rinv, int n)
 {
     const int i = threadIdx.x & 31;
     int bad = -1;
+    rinv = (T)0;
 #pragma unroll
-    for (int j = 0; j < 16; j++) {
-        if (j < pw && bad < 0) {
+    for (int j = 0; j < 32; j++) {
+        if (j < n && bad < 0) {
             const T d = __shfl_sync(0xffffffffu, row[j], j);
             if (!(d > (T)0)) {
                 bad = j;
@@ -335,9 +220,9 @@ __device__ __forceinline__ int warp_potrf16(T (&row)[16], T &rinv, int pw)
                 if (i == j) { row[j] = d * r; rinv = r; }
                 else if (i > j) row[j] *= r;
 #pragma unroll
-                for (int k = j + 1; k < 16; k++) {
+                for (int k = j + 1; k < 32; k++) {
                     const T lkj = __shfl_sync(0xffffffffu, row[j], k);
-                    if (i >= k && k < pw) row[k] -= row[j] * lkj;
+                    if (i >= k && k < n) row[k] -= row[j] * lkj;
                 }
             }
         }
@@ -345,161 +230,129 @@ __device__ __forceinline__ int warp_potrf16(T (&row)[16], T &rinv, int pw)
     return bad;
 }
 
-// One warp: lane c (< pv) forms column c of the inverse of the 16 x 16
-// lower factor stored in A[p1.., p1..] (leading pv x pv block; zero
-// elsewhere): x[r] = -(1 / L(r,r)) sum_{k<r} L(r, k) x[k] for r > c, with
-// the factor read from shared memory (the same address in every lane) and
-// 1 / L(r,r) taken from lane r's rinv.
+// One warp: X = L^-1 of the lower n x n factor stored at A[o + i][o + k]
+// (shared memory, leading dimension 65), lane j forming column j in
+// registers: X(j, j) = 1 / L(j, j) (rinv of lane j), then row by row
+// X(i, j) = -(1 / L(i, i)) sum_{m = j}^{i-1} L(i, m) X(m, j), the factor read
+// by broadcast (every lane the same address).  Column j goes to
+// X[(o + j) 65 + o + i] (rows i < j zero; rows >= n zero).
 template <typename T>
-__device__ __forceinline__ void warp_trinv16(T (*A)[65], int p1, T rinv, T (&x)[16], int pv)
+__device__ __forceinline__ void warp_inv32(const T (*A)[65], int o, T rinv, int n, T *X)
 {
-    const int c = threadIdx.x & 31;
-    T rv[16];
+    const int j = threadIdx.x & 31;
+    T x[32];
 #pragma unroll
-    for (int r = 0; r < 16; r++) rv[r] = __shfl_sync(0xffffffffu, rinv, r);
+    for (int i = 0; i < 32; i++) {
+        const T ri = __shfl_sync(0xffffffffu, rinv, i);
+        T v0 = (T)0, v1 = (T)0;
 #pragma unroll
-    for (int r = 0; r < 16; r++) {
-        T v = (T)0;
-#pragma unroll
-        for (int k = 0; k < r; k++) v += A[p1 + r][p1 + k] * x[k];
-        x[r] = (r < pv && r >= c) ? ((r == c) ? rv[r] : -rv[r] * v) : (T)0;
-    }
-}
-
-// Warp 0: diagonal 16 x 16 block of panel p1 (width pw1): take the rank-pwp
-// update from the previous panel p0 (if p0 >= 0), factor, invert, store L
-// into A and the inverse into X; on a non-positive pivot write its column
-// to *sfail.
-template <typename T>
-__device__ __forceinline__ void diag_block16(T (*A)[65], T *X, int p1, int pw1, int p0, int pwp, int *sfail)
-{
-    const int i = threadIdx.x & 31;
-    T row[16];
-#pragma unroll
-    for (int k = 0; k < 16; k++) row[k] = (i < pw1 && k <= i) ? A[p1 + i][p1 + k] : (T)0;
-    if (p0 >= 0) {
-        T a[16];
-#pragma unroll
-        for (int q = 0; q < 16; q++) a[q] = (i < pw1 && q < pwp) ? A[p1 + i][p0 + q] : (T)0;
-#pragma unroll
-        for (int k = 0; k < 16; k++) {
-            if (k < pw1) {
-                T s = (T)0;
-#pragma unroll
-                for (int q = 0; q < 16; q++) s += a[q] * A[p1 + k][p0 + q];
-                if (k <= i) row[k] -= s;
-            }
+        for (int m = 0; m + 1 < i; m += 2) {
+            v0 += A[o + i][o + m] * x[m];
+            v1 += A[o + i][o + m + 1] * x[m + 1];
         }
+        if (i & 1) v0 += A[o + i][o + i - 1] * x[i - 1];
+        x[i] = (i >= n) ? (T)0 : (i == j ? ri : (i > j ? -ri * (v0 + v1) : (T)0));
     }
-    T rinv = (T)0, x[16];
-    const int bad = warp_potrf16<T>(row, rinv, pw1);
-    const int pv = bad >= 0 ? bad : pw1;
-    if (i < pw1) {
 #pragma unroll
-        for (int k = 0; k < 16; k++)
-            if (k <= i) A[p1 + i][p1 + k] = row[k];
-    }
-    __syncwarp();
-    warp_trinv16<T>(A, p1, rinv, x, pv);
-    if (i < pv) {
-#pragma unroll
-        for (int r = 0; r < 16; r++)
-            if (r >= i) X[(p1 + i) * 65 + p1 + r] = x[r];
-    }
-    if (bad >= 0 && i == 0) *sfail = p1 + bad;
+    for (int i = 0; i < 32; i++) X[(o + j) * 65 + o + i] = x[i];
 }
 
 // LL' and inverse of a 64 x 64 (nb <= 64) lower block in shared memory with
-// 256 threads.  A (leading dimension 65) is overwritten by L; X receives
-// L^-1 (X[c*65 + r] = Linv(r, c), zeros above the diagonal); Tm is scratch
-// of 3*256 entries.  In 16-column panels: warp 0 factors and inverts the
-// panel's diagonal block in registers; the rows below become A * inv(D)'
-// (a half warp per row, operands by shuffle); then warp 0 applies the
-// panel's update to the next diagonal block and factors it while the other
-// warps update the rest of the trailing lower part.  The off-diagonal
-// 16 x 16 blocks of the inverse follow in three waves, X_ij = -X_ii
-// sum_{k=j}^{i-1} L_ik X_kj.  Returns the first column whose pivot is not
-// positive, or -1; on failure the columns before it (of L and of the
+// 256 threads, in 2 x 2 blocks of 32: A = [A11; A21 A22] (leading dimension
+// 65) is overwritten by L; X receives L^-1 (X[c*65 + r] = Linv(r, c), zeros
+// above the diagonal); Tm is scratch of 32 x 33 entries.
+//   L11 = chol(A11), X11 = L11^-1     (one warp, registers and broadcasts)
+//   L21 = A21 X11'                    (all threads)
+//   S = A22 - L21 L21', L22 = chol(S), X22 = L22^-1   (all, then one warp)
+//   X21 = -X22 (L21 X11)              (all threads, two products)
+// Returns the first column whose pivot is not positive, or -1; on failure
+// the columns before it (of L, its rows below included, and of the
 // inverse) are final.
 template <typename T>
 __device__ int potrf_inv64(T (*A)[65], T *X, T *Tm, int nb, int *sfail)
 {
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n1 = min(32, nb), n2 = nb - n1;
     for (int idx = tid; idx < 64 * 65; idx += blockDim.x) X[idx] = (T)0;
     if (tid == 0) *sfail = -1;
     __syncthreads();
-    if (warp == 0) diag_block16<T>(A, X, 0, min(16, nb), -1, 0, sfail);
-    __syncthreads();
-    int nv = nb;
-    for (int p0 = 0; p0 < nb; p0 += 16) {
-        const int pw = min(16, nb - p0);
-        const int f = *sfail;
-        const int pv = (f >= 0) ? f - p0 : pw;
-        // rows below the diagonal block: L(r, panel) = A(r, panel) inv(D)'
-        const int rb = p0 + pw, nrows = nb - rb;
-        for (int base = 0; base < nrows; base += 16) {
-            const int rr = base + (tid >> 4), cc = tid & 15;
-            const bool ok = rr < nrows;
-            const T a = (ok && cc < pw) ? A[rb + rr][p0 + cc] : (T)0;
-            T acc = (T)0;
+    if (warp == 0) {
+        T row[32], rinv;
 #pragma unroll
-            for (int q = 0; q < 16; q++) acc += __shfl_sync(0xffffffffu, a, q, 16) * X[(p0 + q) * 65 + p0 + cc];
-            if (ok && cc < pv) A[rb + rr][p0 + cc] = acc;
+        for (int k = 0; k < 32; k++) row[k] = (lane < n1 && k <= lane) ? A[lane][k] : (T)0;
+        const int bad = warp_chol32<T>(row, rinv, n1);
+        if (lane < n1) {
+#pragma unroll
+            for (int k = 0; k < 32; k++)
+                if (k <= lane) A[lane][k] = row[k];
         }
-        if (f >= 0) { nv = f; break; }
-        __syncthreads();
-        if (rb < nb) {
-            const int pw1 = min(16, nb - rb);
-            if (warp == 0) {
-                diag_block16<T>(A, X, rb, pw1, p0, pw, sfail);
-            } else {
-                // rows below the next diagonal block, columns rb..r
-                const int t0 = rb + pw1, nt = nb - t0, ng = (nb - rb + 7) / 8;
-                for (int w = tid - 32; w < nt * ng; w += blockDim.x - 32) {
-                    const int r = t0 + w / ng, cb = rb + 8 * (w % ng);
-                    if (cb > r) continue;
-                    T a[16];
-#pragma unroll
-                    for (int q = 0; q < 16; q++) a[q] = (q < pw) ? A[r][p0 + q] : (T)0;
-                    const int ce = min(cb + 8, r + 1);
-                    for (int cc = cb; cc < ce; cc++) {
-                        T s = (T)0;
-#pragma unroll
-                        for (int q = 0; q < 16; q++) s += a[q] * A[cc][p0 + q];
-                        A[r][cc] -= s;
-                    }
-                }
-            }
-        }
-        __syncthreads();
+        __syncwarp();
+        warp_inv32<T>(A, 0, rinv, bad >= 0 ? bad : n1, X);
+        if (lane == 0 && bad >= 0) *sfail = bad;
     }
     __syncthreads();
-    // off-diagonal 16 x 16 blocks of the inverse, by distance d = i - j
-    const int nbk = (nv + 15) / 16;
-    for (int d = 1; d < nbk; d++) {
-        const int nblk = nbk - d;          // blocks (j + d, j), j = 0..nblk-1
-        for (int e = tid; e < nblk * 256; e += blockDim.x) {
-            const int j = e / 256, rc = e % 256, r = rc / 16, cc = rc % 16, i = j + d;
-            T acc = (T)0;
-            for (int k = j; k < i; k++) {
-#pragma unroll
-                for (int q = 0; q < 16; q++)
-                    acc += A[16 * i + r][16 * k + q] * X[(16 * j + cc) * 65 + 16 * k + q];
-            }
-            Tm[e] = acc;
-        }
-        __syncthreads();
-        for (int e = tid; e < nblk * 256; e += blockDim.x) {
-            const int j = e / 256, rc = e % 256, r = rc / 16, cc = rc % 16, i = j + d;
-            T acc = (T)0;
-#pragma unroll
-            for (int q = 0; q < 16; q++)
-                acc += X[(16 * i + q) * 65 + 16 * i + r] * Tm[j * 256 + q * 16 + cc];
-            X[(16 * j + cc) * 65 + 16 * i + r] = -acc;
-        }
-        __syncthreads();
+    const int f1 = *sfail, v1 = f1 >= 0 ? f1 : n1;
+    if (n2 <= 0) return f1;
+    // L21(i, c) = sum_{k <= c} A21(i, k) X11(c, k), columns c < v1
+    for (int o = tid; o < n2 * 32; o += blockDim.x) {
+        const int i = o >> 5, c = o & 31;
+        T acc = (T)0;
+        if (c < v1)
+            for (int k = 0; k <= c; k++) acc += A[32 + i][k] * X[k * 65 + c];
+        Tm[i * 33 + c] = acc;
     }
-    return nv < nb ? nv : -1;
+    __syncthreads();
+    for (int o = tid; o < n2 * 32; o += blockDim.x) {
+        const int i = o >> 5, c = o & 31;
+        if (c < v1) A[32 + i][c] = Tm[i * 33 + c];
+    }
+    __syncthreads();
+    if (f1 >= 0) return f1;
+    // S = A22 - L21 L21' (lower)
+    for (int o = tid; o < n2 * n2; o += blockDim.x) {
+        const int i = o / n2, j = o - i * n2;
+        if (j > i) continue;
+        T a0 = (T)0, a1 = (T)0;
+#pragma unroll 8
+        for (int k = 0; k < 32; k += 2) {
+            a0 += A[32 + i][k] * A[32 + j][k];
+            a1 += A[32 + i][k + 1] * A[32 + j][k + 1];
+        }
+        A[32 + i][32 + j] -= a0 + a1;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        T row[32], rinv;
+#pragma unroll
+        for (int k = 0; k < 32; k++) row[k] = (lane < n2 && k <= lane) ? A[32 + lane][32 + k] : (T)0;
+        const int bad = warp_chol32<T>(row, rinv, n2);
+        if (lane < n2) {
+#pragma unroll
+            for (int k = 0; k < 32; k++)
+                if (k <= lane) A[32 + lane][32 + k] = row[k];
+        }
+        __syncwarp();
+        warp_inv32<T>(A, 32, rinv, bad >= 0 ? bad : n2, X);
+        if (lane == 0 && bad >= 0) *sfail = 32 + bad;
+    }
+    __syncthreads();
+    // T = L21 X11: T(i, c) = sum_{k >= c} L21(i, k) X11(k, c)
+    for (int o = tid; o < n2 * 32; o += blockDim.x) {
+        const int i = o >> 5, c = o & 31;
+        T acc = (T)0;
+        for (int k = c; k < n1; k++) acc += A[32 + i][k] * X[c * 65 + k];
+        Tm[i * 33 + c] = acc;
+    }
+    __syncthreads();
+    // X21(i, c) = -sum_{k <= i} X22(i, k) T(k, c)
+    for (int o = tid; o < n2 * 32; o += blockDim.x) {
+        const int i = o >> 5, c = o & 31;
+        T acc = (T)0;
+        for (int k = 0; k <= i; k++) acc += X[(32 + k) * 65 + 32 + i] * Tm[k * 33 + c];
+        X[c * 65 + 32 + i] = -acc;
+    }
+    __syncthreads();
+    return *sfail;
 }
 
 // One 64 x 64 output tile of C -= A B' (SIMT): A is m x k (lda), B is n x k
