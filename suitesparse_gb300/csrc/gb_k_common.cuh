@@ -200,34 +200,35 @@ template <> __device__ __forceinline__ float gb_rsqrt<float>(float x) { return r
 // registers (row[k] = A(i, k) for k <= i, zero elsewhere and in rows >= n):
 // right-looking LL' in place, column j's pivot broadcast by shuffle, L(j,j)
 // = d rsqrt(d), the column scaled by rsqrt(d), the trailing rows updated
-// with L(k, j) from lane k.  rinv receives 1 / L(i,i) in lane i (0 from the
-// failing column on).  Returns the first column whose pivot is not positive
-// (the same in every lane; earlier columns are final), or -1.
+// with L(k, j) from lane k.  No shuffle sits under a data-dependent branch
+// (a full-warp shuffle there makes the compiler reconverge the warp before
+// each one, which made this loop 2.5 times slower): from the first pivot
+// that is not positive on, the columns are formed from a unit pivot
+// (finite, never read).  rinv receives 1 / L(i,i) in lane i (0 from the
+// failing column on).  Returns the first column whose pivot is not
+// positive (earlier columns are final), or -1.
 template <typename T>
 __device__ __forceinline__ int warp_chol32(T (&row)[32], T &rinv, int n)
 {
     const int i = threadIdx.x & 31;
-    int bad = -1;
+    int bad = n;
     rinv = (T)0;
 #pragma unroll
     for (int j = 0; j < 32; j++) {
-        if (j < n && bad < 0) {
-            const T d = __shfl_sync(0xffffffffu, row[j], j);
-            if (!(d > (T)0)) {
-                bad = j;
-            } else {
-                const T r = gb_rsqrt<T>(d);
-                if (i == j) { row[j] = d * r; rinv = r; }
-                else if (i > j) row[j] *= r;
+        const T d = __shfl_sync(0xffffffffu, row[j], j);
+        if (j < n && !(d > (T)0) && bad == n) bad = j;
+        const T dd = j < bad ? d : (T)1;
+        const T r = gb_rsqrt<T>(dd);
+        const T lj = i == j ? dd * r : (i > j ? row[j] * r : row[j]);
+        row[j] = lj;
+        if (i == j) rinv = j < bad ? r : (T)0;
 #pragma unroll
-                for (int k = j + 1; k < 32; k++) {
-                    const T lkj = __shfl_sync(0xffffffffu, row[j], k);
-                    if (i >= k && k < n) row[k] -= row[j] * lkj;
-                }
-            }
+        for (int k = j + 1; k < 32; k++) {
+            const T lkj = __shfl_sync(0xffffffffu, lj, k);
+            row[k] = i >= k ? row[k] - lj * lkj : row[k];
         }
     }
-    return bad;
+    return bad < n ? bad : -1;
 }
 
 // One warp: X = L^-1 of the lower n x n factor stored at A[o + i][o + k]
@@ -293,13 +294,17 @@ __device__ int potrf_inv64(T (*A)[65], T *X, T *Tm, int nb, int *sfail)
     __syncthreads();
     const int f1 = *sfail, v1 = f1 >= 0 ? f1 : n1;
     if (n2 <= 0) return f1;
-    // L21(i, c) = sum_{k <= c} A21(i, k) X11(c, k), columns c < v1
+    // L21(i, c) = sum_k A21(i, k) X11(c, k), columns c < v1 (X11 is zero
+    // above its diagonal, so all 32 terms are summed)
     for (int o = tid; o < n2 * 32; o += blockDim.x) {
         const int i = o >> 5, c = o & 31;
-        T acc = (T)0;
-        if (c < v1)
-            for (int k = 0; k <= c; k++) acc += A[32 + i][k] * X[k * 65 + c];
-        Tm[i * 33 + c] = acc;
+        T a0 = (T)0, a1 = (T)0;
+#pragma unroll
+        for (int k = 0; k < 32; k += 2) {
+            a0 += A[32 + i][k] * X[k * 65 + c];
+            a1 += A[32 + i][k + 1] * X[(k + 1) * 65 + c];
+        }
+        Tm[i * 33 + c] = c < v1 ? a0 + a1 : (T)0;
     }
     __syncthreads();
     for (int o = tid; o < n2 * 32; o += blockDim.x) {
@@ -313,7 +318,7 @@ __device__ int potrf_inv64(T (*A)[65], T *X, T *Tm, int nb, int *sfail)
         const int i = o / n2, j = o - i * n2;
         if (j > i) continue;
         T a0 = (T)0, a1 = (T)0;
-#pragma unroll 8
+#pragma unroll
         for (int k = 0; k < 32; k += 2) {
             a0 += A[32 + i][k] * A[32 + j][k];
             a1 += A[32 + i][k + 1] * A[32 + j][k + 1];
@@ -336,20 +341,31 @@ __device__ int potrf_inv64(T (*A)[65], T *X, T *Tm, int nb, int *sfail)
         if (lane == 0 && bad >= 0) *sfail = 32 + bad;
     }
     __syncthreads();
-    // T = L21 X11: T(i, c) = sum_{k >= c} L21(i, k) X11(k, c)
-    for (int o = tid; o < n2 * 32; o += blockDim.x) {
+    // T = L21 X11: T(i, c) = sum_k L21(i, k) X11(k, c) (X11 zero above its
+    // diagonal; rows i >= n2 of T zero)
+    for (int o = tid; o < 32 * 32; o += blockDim.x) {
         const int i = o >> 5, c = o & 31;
-        T acc = (T)0;
-        for (int k = c; k < n1; k++) acc += A[32 + i][k] * X[c * 65 + k];
-        Tm[i * 33 + c] = acc;
+        T a0 = (T)0, a1 = (T)0;
+        if (i < n2) {
+#pragma unroll
+            for (int k = 0; k < 32; k += 2) {
+                a0 += A[32 + i][k] * X[c * 65 + k];
+                a1 += A[32 + i][k + 1] * X[c * 65 + k + 1];
+            }
+        }
+        Tm[i * 33 + c] = a0 + a1;
     }
     __syncthreads();
-    // X21(i, c) = -sum_{k <= i} X22(i, k) T(k, c)
+    // X21(i, c) = -sum_k X22(i, k) T(k, c) (X22 zero above its diagonal)
     for (int o = tid; o < n2 * 32; o += blockDim.x) {
         const int i = o >> 5, c = o & 31;
-        T acc = (T)0;
-        for (int k = 0; k <= i; k++) acc += X[(32 + k) * 65 + 32 + i] * Tm[k * 33 + c];
-        X[c * 65 + 32 + i] = -acc;
+        T a0 = (T)0, a1 = (T)0;
+#pragma unroll
+        for (int k = 0; k < 32; k += 2) {
+            a0 += X[(32 + k) * 65 + 32 + i] * Tm[k * 33 + c];
+            a1 += X[(32 + k + 1) * 65 + 32 + i] * Tm[(k + 1) * 33 + c];
+        }
+        X[c * 65 + 32 + i] = -(a0 + a1);
     }
     __syncthreads();
     return *sfail;
