@@ -323,6 +323,23 @@ int cholmod_l_super_lsolve (cholmod_factor *L, cholmod_dense *X,
 int cholmod_l_super_ltsolve (cholmod_factor *L, cholmod_dense *X,
     cholmod_dense *E, cholmod_common *Common) ;
 
+/* The int32 forms of the three entry points above, for programs of the
+ * int32 CHOLMOD API (cholmod_start, cholmod_factorize, cholmod_solve):
+ * cholmod_super_numeric (cholmod.h:4016), cholmod_super_lsolve (4037),
+ * cholmod_super_ltsolve (4058); called by the int32 cholmod_factorize_p
+ * (CHOLMOD/Cholesky/cholmod_factorize.c:260) and cholmod_solve2
+ * (cholmod_solve.c:698-707).  Common->itype must be CHOLMOD_INT and A, F, L
+ * int32 objects (otherwise CHOLMOD_INVALID, as in the reference).  The GPU
+ * path runs on an int64 shadow of L's index arrays, kept per factor (its
+ * device state stays attached between calls; gb300_release_factor(L) drops
+ * it); L->x is L's own.  Results are those of the int64 entry points. */
+int cholmod_super_numeric (cholmod_sparse *A, cholmod_sparse *F, double beta [2],
+    cholmod_factor *L, cholmod_common *Common) ;
+int cholmod_super_lsolve (cholmod_factor *L, cholmod_dense *X,
+    cholmod_dense *E, cholmod_common *Common) ;
+int cholmod_super_ltsolve (cholmod_factor *L, cholmod_dense *X,
+    cholmod_dense *E, cholmod_common *Common) ;
+
 /* Rough reciprocal condition number of a factor: (min L(j,j) / max
  * L(j,j))^2 for LL'; 1 for n = 0; 0 when the factorization failed
  * (L->minor < n) or a diagonal entry is NaN; EMPTY for a missing argument.

@@ -114,6 +114,9 @@ def lib():
         "cholmod_l_super_numeric": (C.c_int, [SP, SP, C.POINTER(C.c_double), FP, vp]),
         "cholmod_l_super_lsolve": (C.c_int, [FP, DP, DP, vp]),
         "cholmod_l_super_ltsolve": (C.c_int, [FP, DP, DP, vp]),
+        "cholmod_super_numeric": (C.c_int, [SP, SP, C.POINTER(C.c_double), FP, vp]),
+        "cholmod_super_lsolve": (C.c_int, [FP, DP, DP, vp]),
+        "cholmod_super_ltsolve": (C.c_int, [FP, DP, DP, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -127,7 +130,7 @@ _COMMON_FIELDS = {
     "status": C.c_int, "print": C.c_int, "try_catch": C.c_int,
     "quick_return_if_not_posdef": C.c_int, "fl": C.c_double, "lnz": C.c_double,
     "anz": C.c_double, "malloc_count": C.c_size_t, "memory_inuse": C.c_size_t,
-    "supernodal": C.c_int, "useGPU": C.c_int,
+    "supernodal": C.c_int, "useGPU": C.c_int, "itype": C.c_int,
 }
 
 

@@ -48,6 +48,19 @@ cholmod_factor *gb_analyze_perm(cholmod_sparse *A, const Int *Perm,
 cholmod_sparse *gb_permute_lower(cholmod_sparse *A, const Int *Perm,
                                  cholmod_common *Common);
 
+/* ---- gb_numeric.c: the bodies of the int64 entry points ------------------ */
+int gb_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2], cholmod_factor *L,
+                     cholmod_common *Common);
+int gb_super_solve(cholmod_factor *L, cholmod_dense *X, cholmod_dense *E, cholmod_common *Common,
+                   int forward);
+
+/* drop the device state (plan, device factor) attached to L */
+int gb_release_factor_state(cholmod_factor *L);
+
+/* ---- gb_int32.c ---------------------------------------------------------- */
+/* drop the int64 shadow (and its device state) of an int32 factor */
+int gb_release_int32_shadow(const cholmod_factor *L);
+
 /* ---- kernel launchers (gb_kernels.cu) ------------------------------------ */
 /* Every launcher enqueues on `stream` and returns a cudaError_t as int. */
 

@@ -213,6 +213,7 @@ int gb300_release_factor(cholmod_factor *L, cholmod_common *Common)
 {
     (void)Common;
     if (!L) return FALSE;
+    if (L->itype == CHOLMOD_INT) return gb_release_int32_shadow(L);
     return gb_release_factor_state(L);
 }
 
@@ -717,6 +718,19 @@ int cholmod_l_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2]
                             cholmod_factor *L, cholmod_common *Common)
 {
     if (!Common) return FALSE;
+    if (Common->itype != CHOLMOD_LONG) {      /* as the reference's RETURN_IF_NULL_COMMON */
+        Common->status = CHOLMOD_INVALID;
+        return FALSE;
+    }
+    return gb_super_numeric(A, F, beta, L, Common);
+}
+
+/* The body of cholmod_l_super_numeric on int64 objects (also reached from
+ * the int32 entry point through int64 shadow objects, gb_int32.c). */
+int gb_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2],
+                     cholmod_factor *L, cholmod_common *Common)
+{
+    if (!Common) return FALSE;
     if (!L || !A) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return FALSE; }
     if (A->xtype < CHOLMOD_REAL || A->xtype > CHOLMOD_ZOMPLEX || !A->x) {
         GB_ERROR(CHOLMOD_INVALID, "invalid xtype");
@@ -915,15 +929,23 @@ static int super_solve(cholmod_factor *L, cholmod_dense *X, cholmod_dense *E,
     return TRUE;
 }
 
+int gb_super_solve(cholmod_factor *L, cholmod_dense *X, cholmod_dense *E, cholmod_common *Common,
+                   int forward)
+{
+    return super_solve(L, X, E, Common, forward);
+}
+
 int cholmod_l_super_lsolve(cholmod_factor *L, cholmod_dense *X, cholmod_dense *E,
                            cholmod_common *Common)
 {
+    if (Common && Common->itype != CHOLMOD_LONG) { Common->status = CHOLMOD_INVALID; return FALSE; }
     return super_solve(L, X, E, Common, 1);
 }
 
 int cholmod_l_super_ltsolve(cholmod_factor *L, cholmod_dense *X, cholmod_dense *E,
                             cholmod_common *Common)
 {
+    if (Common && Common->itype != CHOLMOD_LONG) { Common->status = CHOLMOD_INVALID; return FALSE; }
     return super_solve(L, X, E, Common, 0);
 }
 

@@ -281,7 +281,7 @@ int gb300_free_dense(cholmod_dense **Xh, cholmod_common *Common)
     return TRUE;
 }
 
-extern int gb_release_factor_state(cholmod_factor *L);
+
 
 int gb300_free_factor(cholmod_factor **Lh, cholmod_common *Common)
 {

@@ -44,35 +44,38 @@ def _build(d, libs):
     return exe
 
 
-def _run(exe, env=None):
-    out = subprocess.run([exe, "20"], capture_output=True, text=True, check=True,
+def _run(exe, env=None, width="64"):
+    out = subprocess.run([exe, "20", width], capture_output=True, text=True, check=True,
                          env=env, timeout=120).stdout.split()
     return {out[i]: float(out[i + 1]) for i in range(0, len(out), 2)}
 
 
-def test_reference_alone_factors_on_the_cpu(lib):
+@pytest.mark.parametrize("width", ["64", "32"])
+def test_reference_alone_factors_on_the_cpu(lib, width):
     with tempfile.TemporaryDirectory() as d:
-        r = _run(_build(d, ["-L" + os.path.dirname(REF_LIB), "-lcholmod_ref"]))
+        r = _run(_build(d, ["-L" + os.path.dirname(REF_LIB), "-lcholmod_ref"]), width=width)
     assert r["factorize_ok"] == 1 and r["status"] == 0 and r["is_super"] == 1
     assert r["minor"] == r["n"] and 0 <= r["resid"] < 1e-14
 
 
 @pytest.mark.skipif(not _no_gpu(), reason="the proof by status needs a machine without a GPU")
-def test_link_order_interposes_super_numeric(lib):
+@pytest.mark.parametrize("width", ["64", "32"])
+def test_link_order_interposes_super_numeric(lib, width):
     with tempfile.TemporaryDirectory() as d:
         # --no-as-needed: the program names no symbol of this library itself,
         # and an as-needed link would drop it from the needed list
         exe = _build(d, ["-Wl,--no-as-needed", "-L" + GB_DIR, "-lcholmod_gb300",
                          "-L" + os.path.dirname(REF_LIB), "-lcholmod_ref"])
-        r = _run(exe)
+        r = _run(exe, width=width)
     assert r["status"] == -5 and r["factorize_ok"] == 0, r     # CHOLMOD_GPU_PROBLEM
 
 
 @pytest.mark.skipif(not _no_gpu(), reason="the proof by status needs a machine without a GPU")
-def test_ld_preload_interposes_super_numeric(lib):
+@pytest.mark.parametrize("width", ["64", "32"])
+def test_ld_preload_interposes_super_numeric(lib, width):
     from suitesparse_gb300 import cholmod as CH
     with tempfile.TemporaryDirectory() as d:
         exe = _build(d, ["-L" + os.path.dirname(REF_LIB), "-lcholmod_ref"])
         env = dict(os.environ, LD_PRELOAD=CH.LIB_PATH)
-        r = _run(exe, env=env)
+        r = _run(exe, env=env, width=width)
     assert r["status"] == -5 and r["factorize_ok"] == 0, r
