@@ -323,6 +323,27 @@ int cholmod_l_super_lsolve (cholmod_factor *L, cholmod_dense *X,
 int cholmod_l_super_ltsolve (cholmod_factor *L, cholmod_dense *X,
     cholmod_dense *E, cholmod_common *Common) ;
 
+/* Simplicial numeric LL' or LDL' factorization on the GPU.  Replaces
+ * CHOLMOD/Cholesky/cholmod_rowfac.c:588-604 (cholmod_l_rowfac); called by
+ * cholmod_l_factorize_p for the simplicial method at
+ * CHOLMOD/Cholesky/cholmod_factorize.c:393.  A is triu(S) in column form
+ * (stype > 0), L a simplicial symbolic or numeric factor of the same
+ * pattern.  The factor is computed by the GPU supernodal LL' on an
+ * exact-pattern supernodal shadow of L (kept per factor) and written into
+ * L's simplicial layout: a symbolic L gets the reference's unpacked layout
+ * (Lp from ColCount with the grow0/grow1/grow2 slack, next/prev in column
+ * order), Li/Lnz the exact rows, Lx L (LL') or D on the diagonal and the
+ * unit factor below (LDL', L->is_ll = FALSE).  Not positive definite:
+ * returns TRUE with CHOLMOD_NOT_POSDEF, L->minor the failing column, the
+ * columns from it on zero, as the reference.  On the GPU path: stype > 0,
+ * real double or single, kstart = 0 and kend = n, dbound = sbound = 0;
+ * otherwise CHOLMOD_INVALID with a message.  LDL' is formed from LL', so an
+ * indefinite matrix stops at its first non-positive pivot (the reference's
+ * LDL' continues through negative pivots).  Sets Common->rowfacfl as the
+ * reference counts it. */
+int cholmod_l_rowfac (cholmod_sparse *A, cholmod_sparse *F, double beta [2],
+    size_t kstart, size_t kend, cholmod_factor *L, cholmod_common *Common) ;
+
 /* The int32 forms of the three entry points above, for programs of the
  * int32 CHOLMOD API (cholmod_start, cholmod_factorize, cholmod_solve):
  * cholmod_super_numeric (cholmod.h:4016), cholmod_super_lsolve (4037),

@@ -86,6 +86,13 @@ int main(int argc, char **argv)
     cholmod_common c;
     cholmod_l_start(&c);
     c.supernodal = CHOLMOD_SUPERNODAL;
+    /* REF_SIMPLICIAL=ll|ldl: the simplicial factorization instead (final_ll
+     * as given); L->p, L->i, L->x, L->nz are dumped */
+    const char *simp = getenv("REF_SIMPLICIAL");
+    if (simp && (!strcmp(simp, "ll") || !strcmp(simp, "ldl"))) {
+        c.supernodal = CHOLMOD_SIMPLICIAL;
+        c.final_ll = !strcmp(simp, "ll");
+    }
     c.nmethods = 1;
     c.postorder = 1;
     if (!strcmp(ord, "amd")) c.method[0].ordering = CHOLMOD_AMD;
@@ -191,6 +198,18 @@ int main(int argc, char **argv)
     }
     free(SBp); free(SBi); free(SBx);
 
+    if (!L->is_super && L->xtype != CHOLMOD_PATTERN) {
+        int64_t *lp = L->p;
+        write_file(dir, "Lp.bin", L->p, (n + 1) * sizeof(int64_t));
+        write_file(dir, "Lnz.bin", L->nz, n * sizeof(int64_t));
+        write_file(dir, "Li.bin", L->i, L->nzmax * sizeof(int64_t));
+        double *lx = malloc(L->nzmax * sizeof(double));
+        for (size_t p = 0; p < L->nzmax; p++)
+            lx[p] = single ? ((float *)L->x)[p] : ((double *)L->x)[p];
+        write_file(dir, "SLx.bin", lx, L->nzmax * sizeof(double));
+        free(lx);
+        (void)lp;
+    }
     write_file(dir, "Perm.bin", L->Perm, n * sizeof(int64_t));
     write_file(dir, "ColCount.bin", L->ColCount, n * sizeof(int64_t));
     if (L->is_super) {
@@ -215,6 +234,7 @@ int main(int argc, char **argv)
     double rcond = ok ? cholmod_l_rcond(L, &c) : -1.0;
     snprintf(path, sizeof path, "%s/out_meta.txt", dir);
     FILE *of = fopen(path, "w");
+    fprintf(of, "nzmax %zu\nis_ll %d\n", L->nzmax, L->is_ll);
     fprintf(of, "is_super %d\nnsuper %zu\nssize %zu\nxsize %zu\nmaxcsize %zu\n"
                 "maxesize %zu\nfl %.17g\nlnz %.17g\nanz %.17g\nminor %zu\n"
                 "status %d\nfactor_ok %d\nfactor_status %d\nordering %d\n"

@@ -54,8 +54,9 @@ def run(n, Ap, Ai, Ax, ordering="amd", dtype="d", B=None, perm=None, trials=1,
             p = os.path.join(d, name)
             return np.fromfile(p, dtype=dt) if os.path.exists(p) else None
 
-        for name in ("Perm", "ColCount", "Super", "Pi", "Px", "Ls"):
+        for name in ("Perm", "ColCount", "Super", "Pi", "Px", "Ls", "Lp", "Lnz", "Li"):
             out[name] = rd(name + ".bin", np.int64)
+        out["SLx"] = rd("SLx.bin", np.float64)
         out["Lx"] = rd("Lx.bin", np.float64)
         if sncol:
             out["SX"] = {}

@@ -115,6 +115,8 @@ def lib():
         "cholmod_l_super_lsolve": (C.c_int, [FP, DP, DP, vp]),
         "cholmod_l_super_ltsolve": (C.c_int, [FP, DP, DP, vp]),
         "cholmod_super_numeric": (C.c_int, [SP, SP, C.POINTER(C.c_double), FP, vp]),
+        "cholmod_l_rowfac": (C.c_int, [SP, SP, C.POINTER(C.c_double), C.c_size_t, C.c_size_t,
+                                       FP, vp]),
         "cholmod_super_lsolve": (C.c_int, [FP, DP, DP, vp]),
         "cholmod_super_ltsolve": (C.c_int, [FP, DP, DP, vp]),
     }
@@ -130,7 +132,8 @@ _COMMON_FIELDS = {
     "status": C.c_int, "print": C.c_int, "try_catch": C.c_int,
     "quick_return_if_not_posdef": C.c_int, "fl": C.c_double, "lnz": C.c_double,
     "anz": C.c_double, "malloc_count": C.c_size_t, "memory_inuse": C.c_size_t,
-    "supernodal": C.c_int, "useGPU": C.c_int, "itype": C.c_int,
+    "supernodal": C.c_int, "useGPU": C.c_int, "itype": C.c_int, "grow2": C.c_size_t,
+    "final_ll": C.c_int, "rowfacfl": C.c_double,
 }
 
 

@@ -60,6 +60,8 @@ int gb_release_factor_state(cholmod_factor *L);
 /* ---- gb_int32.c ---------------------------------------------------------- */
 /* drop the int64 shadow (and its device state) of an int32 factor */
 int gb_release_int32_shadow(const cholmod_factor *L);
+/* ---- gb_simplicial.c ----------------------------------------------------- */
+int gb_release_simplicial_shadow(const cholmod_factor *L);
 
 /* ---- kernel launchers (gb_kernels.cu) ------------------------------------ */
 /* Every launcher enqueues on `stream` and returns a cudaError_t as int. */

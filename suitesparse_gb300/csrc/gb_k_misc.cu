@@ -301,6 +301,31 @@ __global__ void k_permute_vec(int64_t n, const int64_t *__restrict__ Perm, const
         out[k] = v[Perm[k]];
 }
 
+// Simplicial layout of a factor computed on a supernodal pattern without
+// explicit zeros: column j of L is the contiguous run Fx[src[j] ..
+// src[j] + len[j]) (the supernode's column from its diagonal down), written
+// to Lx[dst[j] ..].  ldl: D(j,j) = L(j,j)^2 on the diagonal and L(i,j) /
+// L(j,j) below (the unit lower factor of L D L').  Columns j >= minor are
+// zero (the factorization broke down at column minor).  One warp per column.
+template <typename T>
+__global__ void k_simplicial_gather(int64_t n, const int64_t *__restrict__ src,
+                                    const int64_t *__restrict__ dst, const int64_t *__restrict__ len,
+                                    int64_t minor, int ldl, const T *__restrict__ Fx, T *__restrict__ Lx)
+{
+    const int lane = threadIdx.x & 31;
+    for (int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; j < n;
+         j += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const int64_t s0 = src[j], d0 = dst[j], m = len[j];
+        const bool zero = j >= minor;
+        const T d = zero ? (T)0 : Fx[s0];
+        for (int64_t t = lane; t < m; t += 32) {
+            T v = zero ? (T)0 : Fx[s0 + t];
+            if (ldl && !zero) v = (t == 0) ? d * d : v / d;
+            Lx[d0 + t] = v;
+        }
+    }
+}
+
 // zero factor entries [from, to) (not-positive-definite clean-up)
 template <typename T>
 __global__ void k_zero_range(T *x, int64_t from, int64_t to)
@@ -599,6 +624,21 @@ int gb_launch_diag_scale(int64_t n, const int64_t *dmap, const double *Ax, const
     if (!dmap || !Ax || !Perm || !scale || !scale_perm) return (int)cudaErrorInvalidValue;
     k_diag_scale<<<gb_grid_for(n), 256, 0, st>>>(n, dmap, Ax, scale);
     k_permute_vec<<<gb_grid_for(n), 256, 0, st>>>(n, Perm, scale, scale_perm);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_simplicial_gather(int64_t n, const int64_t *src, const int64_t *dst,
+                                const int64_t *len, int64_t minor, int ldl, const void *Fx,
+                                void *Lx, int dtype, cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    int g = gb_grid_for(32 * n);
+    if (dtype == 0)
+        k_simplicial_gather<double><<<g, 256, 0, st>>>(n, src, dst, len, minor, ldl,
+                                                        (const double *)Fx, (double *)Lx);
+    else
+        k_simplicial_gather<float><<<g, 256, 0, st>>>(n, src, dst, len, minor, ldl,
+                                                       (const float *)Fx, (float *)Lx);
     return (int)cudaGetLastError();
 }
 

@@ -214,6 +214,7 @@ int gb300_release_factor(cholmod_factor *L, cholmod_common *Common)
     (void)Common;
     if (!L) return FALSE;
     if (L->itype == CHOLMOD_INT) return gb_release_int32_shadow(L);
+    if (!L->is_super) return gb_release_simplicial_shadow(L);
     return gb_release_factor_state(L);
 }
 
@@ -859,6 +860,54 @@ int gb_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2],
     }
     if (Apk != A) gb300_free_sparse(&Apk, Common);
     return Common->status >= CHOLMOD_OK;
+}
+
+/* Factorize S (lower, in FS's column order, dtype; beta added to the
+ * diagonal) into the device factor of the supernodal symbolic factor FS,
+ * without the supernodal not-positive-definite clean-up and without host
+ * values.  *minor = the first column whose pivot was not positive (FS->n
+ * when none); every column before it is complete.  Returns the plan (its
+ * d_Lx[dtype] holds the factor) or NULL with Common->status set. */
+gb_plan *gb_factor_device_only(cholmod_sparse *S, double beta, cholmod_factor *FS, int dtype,
+                               int64_t *minor, cholmod_common *Common)
+{
+    gb_ctx *ctx = gb_ctx_get(Common, 1);
+    if (!ctx || !gb_ctx_ready(ctx)) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device"); return NULL; }
+    gb_plan *P = gb_plan_get(FS, Common, ctx, 1);
+    if (!P) return NULL;
+    if (!gb_ensure_numeric(P, dtype) || !gb_upload_input(P, ctx, S, dtype)) {
+        GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed");
+        return NULL;
+    }
+    cudaEventRecord(ctx->ev0, ctx->stream);
+    int ok = gb_run_factor(P, ctx, P->d_Sx, dtype, dtype, NULL, beta);
+    cudaEventRecord(ctx->ev1, ctx->stream);
+    int32_t anyfail = 0, dagerr = 0;
+    if (ok) ok = cudaMemcpyAsync(&anyfail, P->d_anyfail, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess
+                 && cudaMemcpyAsync(&dagerr, P->d_ticket + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess
+                 && cudaStreamSynchronize(ctx->stream) == cudaSuccess && !dagerr;
+    if (!ok) { GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the factorization"); return NULL; }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats[0] = ms;
+    int d = dt_index(dtype);
+    P->dev_valid[d] = 0;                 /* no host values mirror it */
+    P->dev_valid[1 - d] = 0;
+    *minor = (int64_t)FS->n;
+    if (anyfail) {
+        int32_t *fail = malloc(sizeof(int32_t) * (P->nsuper + 1));
+        if (!fail || cudaMemcpy(fail, P->d_fail, sizeof(int32_t) * P->nsuper,
+                                cudaMemcpyDeviceToHost) != cudaSuccess) {
+            free(fail);
+            GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error");
+            return NULL;
+        }
+        const Int *Super = FS->super;
+        for (Int s = 0; s < P->nsuper; s++)
+            if (fail[s] >= 0) { *minor = Super[s] + fail[s]; break; }
+        free(fail);
+    }
+    return P;
 }
 
 /* device factor of L in dtype, uploading L->x when this library did not

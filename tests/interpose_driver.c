@@ -2,7 +2,8 @@
  * (cholmod.h of the reference), as an unmodified user of the library would
  * write it: analyze -> factorize -> solve of a 2D 5-point Laplacian with
  * the supernodal method forced, through the int64 API (cholmod_l_*) or, with
- * a second argument "32", the int32 API (cholmod_*).
+ * a second argument "32", the int32 API (cholmod_*); a third argument
+ * "simplicial" selects the simplicial method (cholmod_l_rowfac).
  *
  * Test infrastructure (tests/test_interpose.py): linked against the
  * reference library built from its sources (oracle/_ref/libcholmod_ref.so),
@@ -17,6 +18,8 @@
 #include <string.h>
 #include "cholmod.h"
 
+static int simplicial;     /* third argument "simplicial": the simplicial method */
+
 /* the same program for both index widths: ITYPE_T, P (function prefix) */
 #define DRIVER(NAME, ITYPE_T, P)                                                          \
 static void NAME(int64_t m)                                                              \
@@ -24,7 +27,7 @@ static void NAME(int64_t m)                                                     
     const int64_t n = m * m;                                                             \
     cholmod_common c;                                                                     \
     P##start(&c);                                                                         \
-    c.supernodal = CHOLMOD_SUPERNODAL;                                                    \
+    c.supernodal = simplicial ? CHOLMOD_SIMPLICIAL : CHOLMOD_SUPERNODAL;                   \
     c.print = 0;                                                                          \
     c.error_handler = NULL;                                                               \
     cholmod_sparse *A = P##allocate_sparse(n, n, 3 * n, 1, 1, -1, CHOLMOD_REAL, &c);      \
@@ -68,6 +71,7 @@ DRIVER(run32, int32_t, cholmod_)
 int main(int argc, char **argv)
 {
     const int64_t m = argc > 1 ? atol(argv[1]) : 20;
+    simplicial = argc > 3 && strcmp(argv[3], "simplicial") == 0;
     if (argc > 2 && strcmp(argv[2], "32") == 0) run32(m);
     else run64(m);
     return 0;

@@ -44,8 +44,8 @@ def _build(d, libs):
     return exe
 
 
-def _run(exe, env=None, width="64"):
-    out = subprocess.run([exe, "20", width], capture_output=True, text=True, check=True,
+def _run(exe, env=None, width="64", method="supernodal"):
+    out = subprocess.run([exe, "20", width, method], capture_output=True, text=True, check=True,
                          env=env, timeout=120).stdout.split()
     return {out[i]: float(out[i + 1]) for i in range(0, len(out), 2)}
 
@@ -79,3 +79,17 @@ def test_ld_preload_interposes_super_numeric(lib, width):
         env = dict(os.environ, LD_PRELOAD=CH.LIB_PATH)
         r = _run(exe, env=env, width=width)
     assert r["status"] == -5 and r["factorize_ok"] == 0, r
+
+
+@pytest.mark.skipif(not _no_gpu(), reason="the proof by status needs a machine without a GPU")
+def test_link_order_interposes_rowfac(lib):
+    """The simplicial method: the reference's cholmod_l_factorize reaches
+    cholmod_l_rowfac (Cholesky/cholmod_factorize.c:393) through its PLT."""
+    with tempfile.TemporaryDirectory() as d:
+        ref_alone = _run(_build(d, ["-L" + os.path.dirname(REF_LIB), "-lcholmod_ref"]),
+                         method="simplicial")
+        exe = _build(d, ["-Wl,--no-as-needed", "-L" + GB_DIR, "-lcholmod_gb300",
+                         "-L" + os.path.dirname(REF_LIB), "-lcholmod_ref"])
+        r = _run(exe, method="simplicial")
+    assert ref_alone["status"] == 0 and ref_alone["is_super"] == 0 and ref_alone["resid"] < 1e-14
+    assert r["status"] == -5 and r["factorize_ok"] == 0 and r["is_super"] == 0, r
