@@ -305,7 +305,13 @@ typedef struct cholmod_dense_struct
  * supernode factorized only up to the failing column and all later
  * supernodes zero (quick_return_if_not_posdef: the failing supernode is
  * left zero).  Real double and real single are supported; complex/zomplex
- * input and the unsymmetric A*F form return FALSE with CHOLMOD_INVALID. */
+ * input returns FALSE with CHOLMOD_INVALID.  The unsymmetric form (A with
+ * stype 0, n x k, and F = A' or A(:,f)', k x n; the matrix
+ * cholmod_factorize_p passes for an unsymmetric A) factorizes beta I + A F:
+ * the pattern of tril(A F) and, per entry, its list of products are formed
+ * on the host, the products summed on the device in the reference's order
+ * (t_cholmod_super_numeric_worker.c:471-506), then the factorization runs
+ * as for a symmetric-lower input. */
 int cholmod_l_super_numeric (cholmod_sparse *A, cholmod_sparse *F,
     double beta [2], cholmod_factor *L, cholmod_common *Common) ;
 

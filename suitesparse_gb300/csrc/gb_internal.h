@@ -60,6 +60,10 @@ int gb_release_factor_state(cholmod_factor *L);
 /* ---- gb_int32.c ---------------------------------------------------------- */
 /* drop the int64 shadow (and its device state) of an int32 factor */
 int gb_release_int32_shadow(const cholmod_factor *L);
+/* ---- gb_aft.c ------------------------------------------------------------ */
+cholmod_sparse *gb_aft_pattern(cholmod_sparse *A, cholmod_sparse *F, int64_t **pptr_out,
+                               int64_t **pairs_out, cholmod_common *Common);
+
 /* ---- gb_simplicial.c ----------------------------------------------------- */
 int gb_release_simplicial_shadow(const cholmod_factor *L);
 

@@ -326,6 +326,22 @@ __global__ void k_simplicial_gather(int64_t n, const int64_t *__restrict__ src,
     }
 }
 
+// values of C = tril(A F): entry e = sum over its products q of
+// Ax[pairs[2q]] Fx[pairs[2q+1]], from zero, in list order (the reference's
+// order of multiply-adds)
+template <typename T>
+__global__ void k_pair_sum(int64_t nent, const int64_t *__restrict__ pptr,
+                           const int64_t *__restrict__ pairs, const T *__restrict__ Ax,
+                           const T *__restrict__ Fx, T *__restrict__ Cx)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nent;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        T acc = (T)0;
+        for (int64_t q = pptr[e]; q < pptr[e + 1]; q++) acc += Ax[pairs[2 * q]] * Fx[pairs[2 * q + 1]];
+        Cx[e] = acc;
+    }
+}
+
 // zero factor entries [from, to) (not-positive-definite clean-up)
 template <typename T>
 __global__ void k_zero_range(T *x, int64_t from, int64_t to)
@@ -639,6 +655,20 @@ int gb_launch_simplicial_gather(int64_t n, const int64_t *src, const int64_t *ds
     else
         k_simplicial_gather<float><<<g, 256, 0, st>>>(n, src, dst, len, minor, ldl,
                                                        (const float *)Fx, (float *)Lx);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_pair_sum(int64_t nent, const int64_t *pptr, const int64_t *pairs, const void *Ax,
+                       const void *Fx, void *Cx, int dtype, cudaStream_t st)
+{
+    if (nent <= 0) return 0;
+    int g = gb_grid_for(nent);
+    if (dtype == 0)
+        k_pair_sum<double><<<g, 256, 0, st>>>(nent, pptr, pairs, (const double *)Ax,
+                                              (const double *)Fx, (double *)Cx);
+    else
+        k_pair_sum<float><<<g, 256, 0, st>>>(nent, pptr, pairs, (const float *)Ax,
+                                             (const float *)Fx, (float *)Cx);
     return (int)cudaGetLastError();
 }
 

@@ -747,10 +747,26 @@ int gb_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2],
             return FALSE;
         }
     } else if (A->stype == 0) {
+        /* beta I + A F, F = A' or A(:,f)' (the reference's checks,
+         * Supernodal/cholmod_super_numeric.c:135-156) */
         if (A->nrow != L->n) { GB_ERROR(CHOLMOD_INVALID, "invalid dimensions"); return FALSE; }
-        (void)F;
-        GB_ERROR(CHOLMOD_INVALID, "unsymmetric A*F' form not supported on the GPU path");
-        return FALSE;
+        if (!F) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return FALSE; }
+        if (F->xtype < CHOLMOD_REAL || F->xtype > CHOLMOD_ZOMPLEX || !F->x) {
+            GB_ERROR(CHOLMOD_INVALID, "invalid xtype");
+            return FALSE;
+        }
+        if (A->nrow != F->ncol || A->ncol != F->nrow || F->stype != 0) {
+            GB_ERROR(CHOLMOD_INVALID, "F invalid");
+            return FALSE;
+        }
+        if (A->xtype != F->xtype || A->dtype != F->dtype) {
+            GB_ERROR(CHOLMOD_INVALID, "A and F must have same xtype and dtype");
+            return FALSE;
+        }
+        if (F->itype != CHOLMOD_LONG) {
+            GB_ERROR(CHOLMOD_INVALID, "int64 (cholmod_l_) objects required");
+            return FALSE;
+        }
     } else {
         GB_ERROR(CHOLMOD_INVALID, "symmetric upper case not supported");
         return FALSE;
@@ -778,7 +794,13 @@ int gb_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2],
     Common->status = CHOLMOD_OK;
     int dtype = A->dtype;
     cholmod_sparse *Apk = A;
-    if (!A->packed) {
+    /* the A F form: C = tril(A F), pattern and product lists on the host,
+     * values on the device after the upload (gb_aft.c) */
+    int64_t *aft_ptr = NULL, *aft_pairs = NULL;
+    if (A->stype == 0) {
+        Apk = gb_aft_pattern(A, F, &aft_ptr, &aft_pairs, Common);
+        if (!Apk) return FALSE;
+    } else if (!A->packed) {
         /* pack the columns (unpacked input) on the host */
         Int n = (Int)A->ncol, nz = 0;
         const Int *Ap = A->p, *Anz = A->nz;
@@ -806,11 +828,49 @@ int gb_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2],
     }
     int symbolic = (L->xtype == CHOLMOD_PATTERN);
     gb_plan *P = gb_plan_get(L, Common, ctx, 1);
-    if (!P) { if (Apk != A) gb300_free_sparse(&Apk, Common); return FALSE; }
+    if (!P) {
+        if (Apk != A) gb300_free_sparse(&Apk, Common);
+        free(aft_ptr); free(aft_pairs);
+        return FALSE;
+    }
     if (!gb_ensure_numeric(P, dtype) || !gb_upload_input(P, ctx, Apk, dtype)) {
         if (Apk != A) gb300_free_sparse(&Apk, Common);
+        free(aft_ptr); free(aft_pairs);
         GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed");
         return FALSE;
+    }
+    if (aft_ptr) {
+        /* values of C = tril(A F): each entry's products summed on the device */
+        const Int nent = ((const Int *)Apk->p)[Apk->ncol];
+        const Int *Ap0 = A->p, *Fp0 = F->p;
+        const Int anz = A->packed ? Ap0[A->ncol] : A->nzmax, fnz = F->packed ? Fp0[F->ncol] : F->nzmax;
+        const size_t e = dt_size(dtype);
+        void *dA = NULL, *dF = NULL;
+        int64_t *dptr = NULL, *dpairs = NULL;
+        int okp = cudaMalloc(&dA, e * GB_MAX(anz, 1)) == cudaSuccess
+                  && cudaMalloc(&dF, e * GB_MAX(fnz, 1)) == cudaSuccess
+                  && cudaMalloc((void **)&dptr, sizeof(int64_t) * (nent + 1)) == cudaSuccess
+                  && cudaMalloc((void **)&dpairs, sizeof(int64_t) * 2 * GB_MAX(aft_ptr[nent], 1)) == cudaSuccess
+                  && cudaMemcpyAsync(dA, A->x, e * anz, cudaMemcpyHostToDevice, ctx->stream) == cudaSuccess
+                  && cudaMemcpyAsync(dF, F->x, e * fnz, cudaMemcpyHostToDevice, ctx->stream) == cudaSuccess
+                  && cudaMemcpyAsync(dptr, aft_ptr, sizeof(int64_t) * (nent + 1), cudaMemcpyHostToDevice, ctx->stream) == cudaSuccess
+                  && cudaMemcpyAsync(dpairs, aft_pairs, sizeof(int64_t) * 2 * aft_ptr[nent], cudaMemcpyHostToDevice, ctx->stream) == cudaSuccess
+                  && gb_launch_pair_sum(nent, dptr, dpairs, dA, dF, P->d_Sx, dtype == CHOLMOD_SINGLE ? 4 : 0,
+                                        ctx->stream) == 0
+                  && cudaStreamSynchronize(ctx->stream) == cudaSuccess;
+        if (dA) cudaFree(dA);
+        if (dF) cudaFree(dF);
+        if (dptr) cudaFree(dptr);
+        if (dpairs) cudaFree(dpairs);
+        free(aft_ptr);
+        free(aft_pairs);
+        aft_ptr = aft_pairs = NULL;
+        if (!okp) {
+            gb300_free_sparse(&Apk, Common);
+            cudaGetLastError();
+            GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error forming A*F'");
+            return FALSE;
+        }
     }
     if (symbolic) {
         /* supernodal symbolic -> numeric: allocate L->x (change_factor) */

@@ -408,6 +408,8 @@ int gb_launch_diag_inverse(const gb_pattern_ptrs *pp, const gb_stask *dtasks, in
 int gb_launch_zero_range(void *x, int dtype, int64_t from, int64_t to, cudaStream_t st);
 gb_plan *gb_factor_device_only(cholmod_sparse *S, double beta, cholmod_factor *FS, int dtype,
                                int64_t *minor, cholmod_common *Common);
+int gb_launch_pair_sum(int64_t nent, const int64_t *pptr, const int64_t *pairs, const void *Ax,
+                       const void *Fx, void *Cx, int dtype, cudaStream_t st);
 int gb_launch_simplicial_gather(int64_t n, const int64_t *src, const int64_t *dst,
                                 const int64_t *len, int64_t minor, int ldl, const void *Fx,
                                 void *Lx, int dtype, cudaStream_t st);

@@ -208,3 +208,46 @@ def test_full_size_fp64(golden, lib, oracle_mod, name):
         assert oracle_mod.backward_error(*mat, X, B).max() <= 1e-12
     CH.free_factor(L, c)
     CH.free_sparse(A, c)
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_super_numeric_unsymmetric_a_ft(lib, oracle_mod, seed):
+    """The unsymmetric form: A is m x k (stype 0), F = A' (k x m), L the
+    supernodal factor of A A' + beta I; against the oracle's factor of the
+    symmetric matrix tril(A A') (+ beta) formed in float64 by numpy."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(20 + seed)
+    m, k = 300, 420
+    Ad = sp.random(m, k, density=0.02, random_state=rng, format="csc")
+    Ad = (Ad + sp.eye(m, k, format="csc")).tocsc()
+    Ad.sort_indices()
+    Ft = Ad.T.tocsc()
+    Ft.sort_indices()
+    beta = 0.5
+    AAt = (Ad @ Ft).tocsc() + beta * sp.eye(m, format="csc")
+    low = sp.tril(AAt).tocsc()
+    low.sort_indices()
+    n = m
+    c = CH.Common()
+    Al = CH.sparse(n, low.indptr.astype(np.int64), low.indices.astype(np.int64), low.data, c)
+    L = CH.analyze_perm(Al, np.arange(n, dtype=np.int64), c)   # pattern of A A'
+    f = CH.factor_arrays(L, with_x=False)
+    A = CH.sparse(m, Ad.indptr.astype(np.int64), Ad.indices.astype(np.int64), Ad.data, c,
+                  stype=0, ncol=k)
+    F = CH.sparse(k, Ft.indptr.astype(np.int64), Ft.indices.astype(np.int64), Ft.data, c,
+                  stype=0, ncol=m)
+    b = (C.c_double * 2)(beta, 0.0)
+    assert lib.cholmod_l_super_numeric(A, F, b, L, c.ptr) == 1 and c.status == CH.CHOLMOD_OK
+    Lx = CH.factor_arrays(L)["Lx"]
+    sym = {kk: f[kk] for kk in ("Super", "Pi", "Px", "Ls")}
+    sym["n"] = n
+    st, minor, Lref = oracle_mod.factor(sym, low.indptr.astype(np.int64),
+                                        low.indices.astype(np.int64), low.data)
+    assert st == 0
+    assert relerr(Lx, Lref) < L_TOL
+    # F missing: the reference's argument check
+    assert lib.cholmod_l_super_numeric(A, None, b, L, c.ptr) == 0
+    assert c.status == CH.CHOLMOD_INVALID
+    for obj in (A, F, Al):
+        CH.free_sparse(obj, c)
+    CH.free_factor(L, c)
