@@ -653,6 +653,11 @@ int gb300_server_solve (gb300_server *S, int64_t req, int64_t factor_id, int64_t
     int nrhs, const double *B, double arrival) ;
 int gb300_server_wait (gb300_server *S, int64_t req, double *X, int64_t ldx, double *out) ;
 int gb300_server_stats (gb300_server *S, double *out, int nout) ;
+/* gb300_set_option on every worker's Common (before requests are
+ * submitted); e.g. GB300_OPT_PIVOT_LOG2 = 0 makes every factorization take
+ * the FP64 factor (the plain FP64 form of the stream).  TRUE when every
+ * worker accepted it. */
+int gb300_server_set_option (gb300_server *S, int option, int64_t value) ;
 int gb300_server_destroy (gb300_server *S) ;
 double gb300_server_now (void) ;
 

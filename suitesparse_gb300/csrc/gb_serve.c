@@ -367,6 +367,16 @@ static void *worker(void *arg)
     return NULL;
 }
 
+int gb300_server_set_option(gb300_server *S, int option, int64_t value)
+{
+    if (!S) return FALSE;
+    int ok = TRUE;
+    pthread_mutex_lock(&S->mu);
+    for (int i = 0; i < S->ncommons; i++) ok &= gb300_set_option(&S->commons[i], option, value);
+    pthread_mutex_unlock(&S->mu);
+    return ok;
+}
+
 gb300_server *gb300_server_create(int nslots, int64_t budget_bytes, int max_rhs)
 {
     if (nslots < 1 || nslots > 64 || budget_bytes <= 0 || max_rhs < 1) return NULL;

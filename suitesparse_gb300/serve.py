@@ -4,11 +4,17 @@ request server (gb300_server_* in include/cholmod_gb300.h).
 The stream restates the serving workload: requests arrive as a Poisson
 process; matrices are 2D 5-point and 3D 7-point grid Laplacians with
 log-uniform coefficients; a share of the factor requests reuses one of a
-few cached patterns with new values (the server reuses the symbolic analysis
-and, for a resident factor id, the device factor), a share are solve-only
-requests against a resident factor with 1-32 right-hand sides, the rest are
-factor requests of new patterns.  Orderings are geometric nested dissection
-of the grids (matrices.grid_nd_perm) given with a pattern's first request.
+few cached patterns with new values (each cached pattern owns one factor
+id, refactorized in place: the server reuses the symbolic analysis, the plan
+and the device factor), a share are solve-only requests against a resident
+factor of a cached pattern with 1-32 right-hand sides (queued solves of one
+factor are coalesced), the rest are factor requests of new patterns (a
+factor id each, evicted least recently used under the byte budget).
+Orderings are geometric nested dissection of the grids
+(matrices.grid_nd_perm) given with a pattern's first request.  Matrix
+values come from grid_matrix: new coefficients gathered into a pattern
+cached per grid shape, so that a long stream's inputs are made as fast as
+they arrive.
 """
 import ctypes as C
 import threading
@@ -33,6 +39,7 @@ def _lib():
             "gb300_server_stats": (C.c_int, [vp, dp, C.c_int]),
             "gb300_server_destroy": (C.c_int, [vp]),
             "gb300_server_now": (C.c_double, []),
+            "gb300_server_set_option": (C.c_int, [vp, C.c_int, i64]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -103,17 +110,103 @@ class Server:
                 "evictions", "coalesced", "served")
         return dict(zip(keys, list(out)))
 
+    def set_option(self, option, value):
+        """gb300_set_option on every worker's Common (e.g. GB300_OPT_PIVOT_LOG2
+        = 0: every factorization takes the FP64 factor, the plain FP64 form)."""
+        if not self.L.gb300_server_set_option(self.h, option, int(value)):
+            raise RuntimeError(f"server option {option} refused")
+
     def close(self):
         if self.h:
             self.L.gb300_server_destroy(self.h)
             self.h = None
 
 
+_grids = {}
+
+
+def _grid_struct(dims):
+    """Per grid shape: the lower CSC pattern of the Dirichlet grid Laplacian
+    (column v: the diagonal, then the neighbours v + 1, v + nx, v + nx ny
+    that exist, rows ascending) and the edge indices that form each stored
+    value (diagonal: the 2 d incident edges, the ghost ones included;
+    off-diagonal: minus the edge between the two nodes)."""
+    key = tuple(int(d) for d in dims)
+    if key in _grids:
+        return _grids[key]
+    nd = len(key)
+    n = int(np.prod(key))
+    coord = np.indices(key[::-1]).reshape(nd, -1)[::-1]     # coord[d][v], x fastest
+    strides = np.cumprod((1,) + key[:-1])
+    # flat edge index of direction d at node coordinate c (coordinate d in 0..dims[d])
+    eoff, eshape = [], []
+    tot = 0
+    for d in range(nd):
+        shp = list(key)
+        shp[d] += 1
+        eoff.append(tot)
+        eshape.append(shp)
+        tot += int(np.prod(shp))
+
+    def edge(d, c):
+        shp = eshape[d]
+        flat = np.zeros(c.shape[1], dtype=np.int64)
+        mul = 1
+        for a in range(nd):
+            flat += c[a] * mul
+            mul *= shp[a]
+        return eoff[d] + flat
+
+    # entries per column: diagonal + one per existing forward neighbour
+    has = [coord[d] < key[d] - 1 for d in range(nd)]
+    cnt = 1 + sum(h.astype(np.int64) for h in has)
+    Ap = np.zeros(n + 1, dtype=np.int64)
+    Ap[1:] = np.cumsum(cnt)
+    Ai = np.empty(int(Ap[-1]), dtype=np.int64)
+    pos = Ap[:-1].copy()
+    v = np.arange(n, dtype=np.int64)
+    diag_pos = pos.copy()
+    Ai[diag_pos] = v
+    pos += 1
+    lo_e, hi_e, off_pos, off_e = [], [], [], []
+    for d in range(nd):
+        lo_e.append(edge(d, coord))                       # edge before the node
+        c2 = coord.copy()
+        c2[d] += 1
+        hi_e.append(edge(d, c2))                          # edge after the node
+        m = has[d]
+        off_pos.append(pos[m].copy())
+        off_e.append(hi_e[d][m])
+        Ai[pos[m]] = v[m] + strides[d]
+        pos[m] += 1
+    st = dict(n=n, Ap=Ap, Ai=Ai, E=tot, diag_pos=diag_pos, lo_e=lo_e, hi_e=hi_e,
+              off_pos=off_pos, off_e=off_e)
+    _grids[key] = st
+    return st
+
+
+def grid_matrix(dims, seed, lo=1e-2, hi=1e2, shift=0.0):
+    """(n, Ap, Ai, Ax): the grid Laplacian of shape dims with edge
+    conductivities log-uniform in [lo, hi] from seed (one uniform stream
+    over every edge, ghost edges to the Dirichlet boundary included)."""
+    st = _grid_struct(dims)
+    c = M.log_uniform(lo, hi, M.uniform01(seed, st["E"]))
+    x = np.empty(len(st["Ai"]), dtype=np.float64)
+    dg = np.full(st["n"], float(shift))
+    for d in range(len(st["lo_e"])):
+        dg += c[st["lo_e"][d]] + c[st["hi_e"][d]]
+        x[st["off_pos"][d]] = -c[st["off_e"][d]]
+    x[st["diag_pos"]] = dg
+    return st["n"], st["Ap"], st["Ai"], x
+
+
 def make_stream(nreq=200, seed=5, rate=200.0, sides2d=(32, 160), sides3d=(16, 40),
                 ncached=16, p_reuse=0.6, p_solve=0.2, max_rhs=32):
     """A request stream: list of dicts with kind, arrival offset (s), ids and
-    inputs.  Patterns are grids; pattern ids 0..ncached-1 are the cached set,
-    new patterns get fresh ids."""
+    inputs' seeds.  Pattern ids 0..ncached-1 are the cached set, and cached
+    pattern p is factor id p (refactorized in place by its reuse requests);
+    solves go to a cached factor already requested; a new pattern gets a
+    fresh pattern id and factor id."""
     rng = np.random.default_rng(seed)
 
     def new_pattern(pid):
@@ -124,28 +217,30 @@ def make_stream(nreq=200, seed=5, rate=200.0, sides2d=(32, 160), sides3d=(16, 40
         return dict(pid=pid, dims=(s, s, s))
 
     cached = [new_pattern(p) for p in range(ncached)]
-    next_pid, next_fid = ncached, 0
-    resident = []                        # factor ids known to be factored, with their pattern
+    next_pid, next_fid = ncached, ncached
+    resident = []                        # cached factor ids already requested
     t = 0.0
     out = []
     for r in range(nreq):
         t += rng.exponential(1.0 / rate)
         u = rng.random()
         if u < p_solve and resident:
-            fid, pat = resident[int(rng.integers(len(resident)))]
-            out.append(dict(kind="solve", req=r, t=t, fid=fid, pat=pat,
+            fid = resident[int(rng.integers(len(resident)))]
+            out.append(dict(kind="solve", req=r, t=t, fid=fid, pat=cached[fid],
                             nrhs=int(rng.integers(1, max_rhs + 1)), seed=int(rng.integers(1 << 30))))
             continue
         if u < p_solve + p_reuse:
             pat = cached[int(rng.integers(ncached))]
+            fid = pat["pid"]
+            if fid not in resident:
+                resident.append(fid)
         else:
             pat = new_pattern(next_pid)
             next_pid += 1
-        fid = next_fid
-        next_fid += 1
+            fid = next_fid
+            next_fid += 1
         out.append(dict(kind="factor", req=r, t=t, fid=fid, pat=pat,
                         seed=int(rng.integers(1 << 30))))
-        resident.append((fid, pat))
     return out
 
 
@@ -154,8 +249,7 @@ def request_inputs(rq, _cache={}):
     pat = rq["pat"]
     dims = pat["dims"]
     if rq["kind"] == "factor":
-        gen = M.laplace2d if len(dims) == 2 else M.laplace3d
-        mat = gen(*dims, seed=rq["seed"], lo=1e-2, hi=1e2)
+        mat = grid_matrix(dims, rq["seed"], lo=1e-2, hi=1e2)
         key = dims
         if key not in _cache:
             _cache[key] = M.grid_nd_perm(dims)
@@ -174,25 +268,44 @@ def factor_weight(pat):
 
 def shard_stream(stream, world_size, rank):
     """This rank's requests of a stream split across world_size GPUs with no
-    communication: factor ids are split by estimated factor bytes
-    (batch.shard_systems, the same split on every rank) and every request
-    follows its factor id, so a solve runs where its factor lives."""
+    communication: factor ids are split by the estimated factor bytes of
+    all their factor requests (a cached pattern's id is refactorized many
+    times; batch.shard_systems, the same split on every rank) and every
+    request follows its factor id, so a solve runs where its factor lives."""
     from .batch import shard_systems
     w = {}
     for q in stream:
         if q["kind"] == "factor":
-            w[q["fid"]] = factor_weight(q["pat"])
+            w[q["fid"]] = w.get(q["fid"], 0.0) + factor_weight(q["pat"])
     fids = sorted(w)
     part = shard_systems([w[f] for f in fids], world_size)[rank]
     mine = {fids[i] for i in part}
     return [q for q in stream if q["fid"] in mine]
 
 
-def run_stream(server, stream, realtime=True):
+def nd_orderings(stream, workers=0):
+    """The nested-dissection ordering of every grid shape in the stream
+    (computed once per shape; workers > 1: in a spawned process pool, so it
+    may run after CUDA was initialized).  Fills request_inputs' cache."""
+    shapes = sorted({tuple(q["pat"]["dims"]) for q in stream if q["kind"] == "factor"})
+    cache = request_inputs.__defaults__[0]
+    todo = [d for d in shapes if d not in cache]
+    if workers > 1 and len(todo) > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(workers) as pool:
+            for d, perm in zip(todo, pool.map(M.grid_nd_perm, todo)):
+                cache[d] = perm
+    else:
+        for d in todo:
+            cache[d] = M.grid_nd_perm(d)
+
+
+def run_stream(server, stream, realtime=True, keep_x=None):
     """Submit the stream (at its arrival times when realtime) from one
-    thread, collect every request's result in another.  Returns the
-    per-request records and the wall time."""
-    inputs = {rq["req"]: request_inputs(rq) for rq in stream}
+    thread, collect every request's result in another.  A request's inputs
+    are made when it is submitted (its arrival time is taken after that).
+    keep_x: request ids whose solution is kept in the records (all when
+    None).  Returns the per-request records and the wall time."""
     seen = set()
     t0 = server.now()
     records = {}
@@ -203,15 +316,16 @@ def run_stream(server, stream, realtime=True):
                 delay = t0 + rq["t"] - server.now()
                 if delay > 0:
                     time.sleep(delay)
+            inp = request_inputs(rq)
             arr = server.now()
             if rq["kind"] == "factor":
-                mat, perm = inputs[rq["req"]]
+                mat, perm = inp
                 pid = rq["pat"]["pid"]
                 server.factor(rq["req"], rq["fid"], pid, mat, perm if pid not in seen else None,
                               arrival=arr)
                 seen.add(pid)
             else:
-                server.solve(rq["req"], rq["fid"], inputs[rq["req"]], arrival=arr)
+                server.solve(rq["req"], rq["fid"], inp, arrival=arr)
 
     th = threading.Thread(target=submitter)
     th.start()
@@ -220,6 +334,8 @@ def run_stream(server, stream, realtime=True):
             time.sleep(1e-4)
         st, X, info = server.wait(rq["req"])
         info["status"] = st
+        if keep_x is not None and rq["req"] not in keep_x:
+            X = None if X is None else X.shape
         records[rq["req"]] = dict(kind=rq["kind"], X=X, **info)
     th.join()
     return records, server.now() - t0
