@@ -694,7 +694,7 @@ def run_serve(args):
                 "coalesced": st["coalesced"], "evictions": st["evictions"], "server": st,
                 "clocks": clk.summary()}
 
-    sweep = [run(rate * ws, len(base), False) for rate in (100.0, 400.0)]
+    sweep = [run(rate * ws, len(base), False) for rate in (200.0, 800.0)]
     fp64 = run(100.0 * ws, min(n64 * ws, len(base)), True)
     top = sweep[-1]
     line = {

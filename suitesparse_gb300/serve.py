@@ -188,9 +188,11 @@ def _grid_struct(dims):
 def grid_matrix(dims, seed, lo=1e-2, hi=1e2, shift=0.0):
     """(n, Ap, Ai, Ax): the grid Laplacian of shape dims with edge
     conductivities log-uniform in [lo, hi] from seed (one uniform stream
-    over every edge, ghost edges to the Dirichlet boundary included)."""
+    over every edge, ghost edges to the Dirichlet boundary included; numpy's
+    PCG64 and exp, fast enough to make a stream's inputs as they arrive)."""
     st = _grid_struct(dims)
-    c = M.log_uniform(lo, hi, M.uniform01(seed, st["E"]))
+    u = np.random.default_rng(seed).random(st["E"])
+    c = np.exp(np.log(lo) + u * (np.log(hi) - np.log(lo)))
     x = np.empty(len(st["Ai"]), dtype=np.float64)
     dg = np.full(st["n"], float(shift))
     for d in range(len(st["lo_e"])):
@@ -302,21 +304,31 @@ def nd_orderings(stream, workers=0):
 
 def run_stream(server, stream, realtime=True, keep_x=None):
     """Submit the stream (at its arrival times when realtime) from one
-    thread, collect every request's result in another.  A request's inputs
-    are made when it is submitted (its arrival time is taken after that).
+    thread, collect every request's result in another.  A third thread makes
+    the requests' inputs ahead of their arrival (up to 64); a request whose
+    inputs are late arrives when they are ready.
     keep_x: request ids whose solution is kept in the records (all when
     None).  Returns the per-request records and the wall time."""
+    import queue
     seen = set()
+    ready = queue.Queue(maxsize=64)       # inputs made ahead of their arrival
+
+    def producer():
+        for rq in stream:
+            ready.put(request_inputs(rq))
+
+    pt = threading.Thread(target=producer, daemon=True)
+    pt.start()
     t0 = server.now()
     records = {}
 
     def submitter():
         for rq in stream:
+            inp = ready.get()
             if realtime:
                 delay = t0 + rq["t"] - server.now()
                 if delay > 0:
                     time.sleep(delay)
-            inp = request_inputs(rq)
             arr = server.now()
             if rq["kind"] == "factor":
                 mat, perm = inp
