@@ -298,13 +298,14 @@ def run_gpu(args):
     B = M.rhs(n, 1, 1)
     if gold.get("fl") is None:
         fl = c["fl"]
-    # schedule parameters (small/large cutoff, subtree size) by the autotuner
+    # plan options (small/large cutoff, subtree size, update group) by the
+    # library's autotuner
     tuned = None
     if not args.quick:
         from suitesparse_gb300 import autotune as AT
         best, table = AT.autotune(A, L, c, reps=2, mixed=True)
-        tuned = {"small_cols": best[0], "subtree_work": best[1],
-                 "table_ms": {f"{k[0]}/{k[1]}": v for k, v in table.items()}}
+        tuned = {"small_cols": best[0], "subtree_work": best[1], "upd_group": best[2],
+                 "table_ms": {"/".join(map(str, k)): v for k, v in table.items()}}
     info = CH.factor_info(L, c)
 
     # B and X in caller-owned cholmod_dense objects in pinned memory, as
@@ -522,8 +523,8 @@ def run_batch(args):
     best, table = AT.autotune(b.A, b.L, c, reps=1, mixed=True,
                               candidates=((64, 4_000_000), (64, 16_000_000), (64, 64_000_000),
                                           (32, 16_000_000)))
-    tuned = {"small_cols": best[0], "subtree_work": best[1],
-             "table_ms": {f"{k[0]}/{k[1]}": v for k, v in table.items()}}
+    tuned = {"small_cols": best[0], "subtree_work": best[1], "upd_group": best[2],
+             "table_ms": {"/".join(map(str, k)): v for k, v in table.items()}}
 
     # A's arrays, B and X (caller-owned cholmod_dense objects) in pinned memory
     rt = cudart()

@@ -456,7 +456,18 @@ int gb300_finish (cholmod_common *Common) ;
  *      four hi/lo products, draining the accumulator into FP32 sums every
  *      64 of K); 0 = FP32 multiply-adds on the CUDA cores.  The operand
  *      images take twice the FP32 factor's memory; when they cannot be
- *      allocated the CUDA cores take the products. */
+ *      allocated the CUDA cores take the products.
+ *  GB300_OPT_UPD_GROUP [4]: in a supernode wider than the small cutoff the
+ *      trailing updates of this many 64-column panels (1-4) run as one tile
+ *      product of depth 64 x value; the updates within a group stay one
+ *      panel deep (the diagonal chain waits on them).  A change applies
+ *      from the next factorization (the plan is rebuilt).
+ *  GB300_OPT_AUTOTUNE [0]: 1 = the first cholmod_l_super_numeric (or
+ *      cholmod_super_numeric) on this Common runs gb300_autotune's default
+ *      candidates on its own input (one timed factorization each after a
+ *      warm-up), leaves the fastest set on the Common, then factorizes; a
+ *      program that only calls the CHOLMOD API gets tuned plan options this
+ *      way.  Setting the option again arms another tuning. */
 #define GB300_OPT_KEEP_ON_DEVICE 1
 #define GB300_OPT_SMALL_COLS     2
 #define GB300_OPT_PROFILE        3
@@ -469,7 +480,37 @@ int gb300_finish (cholmod_common *Common) ;
 #define GB300_OPT_GRAPH          10
 #define GB300_OPT_SWEEP_STREAMS  11
 #define GB300_OPT_PIVOT_LOG2     12
+#define GB300_OPT_UPD_GROUP      13
+#define GB300_OPT_AUTOTUNE       14
 int gb300_set_option (cholmod_common *Common, int option, int64_t value) ;
+/* The current value of an option with a numeric setting (SMALL_COLS,
+ * SUBTREE_WORK, WARP_ROWS, UPD_GROUP, KEEP_ON_DEVICE, AUTOTUNE), the
+ * default when none was set; 0 for the others. */
+int64_t gb300_get_option (cholmod_common *Common, int option) ;
+
+/* Autotuner of the plan options (small cutoff, subtree work limit, update
+ * group).  cand: ncand rows of 3 values (GB300_OPT_SMALL_COLS,
+ * GB300_OPT_SUBTREE_WORK, GB300_OPT_UPD_GROUP), or NULL for the default
+ * list (gb300_autotune_candidates).  Each candidate is set on Common, one
+ * factorization builds its plan, then reps (1-15) factorizations are timed
+ * (the library's device time of the factorization launch, as
+ * gb300_get_stats()[0]) and their median goes to ms[i] (ms may be NULL).
+ * mixed: 1 = gb300_factorize_mixed, 0 = gb300_factorize of A (FP64).
+ * Returns the index of the fastest candidate and leaves it set on Common;
+ * -1 when a factorization failed (the options are then restored; Common->
+ * status tells why).  L holds the last candidate's factor afterwards:
+ * factorize again for the tuned one. */
+int gb300_autotune (cholmod_sparse *A, cholmod_factor *L, int mixed, int reps,
+    const int64_t *cand, int ncand, double *ms, cholmod_common *Common) ;
+/* The default candidates: writes up to ncand rows of 3 values into cand
+ * (may be NULL) and returns how many there are. */
+int gb300_autotune_candidates (int64_t *cand, int ncand) ;
+/* gb300_autotune with the timing supplied by the caller: timer(Common, ud)
+ * performs one run under the options currently set on Common and returns
+ * its milliseconds (negative: failed). */
+typedef double (*gb300_tune_timer) (cholmod_common *Common, void *ud) ;
+int gb300_autotune_with (const int64_t *cand, int ncand, int reps, double *ms,
+    gb300_tune_timer timer, void *ud, cholmod_common *Common) ;
 
 /* Supernodal symbolic analysis of A (stype < 0, lower) with a given final
  * (already postordered) permutation Perm: elimination tree, column counts,

@@ -29,6 +29,9 @@ GB300_OPT_WARP_ROWS = 9
 GB300_OPT_GRAPH = 10
 GB300_OPT_SWEEP_STREAMS = 11
 GB300_OPT_PIVOT_LOG2 = 12
+GB300_OPT_UPD_GROUP = 13
+GB300_OPT_AUTOTUNE = 14
+TUNE_TIMER = C.CFUNCTYPE(C.c_double, C.c_void_p, C.c_void_p)
 GB300_REASON_NONE, GB300_REASON_FP32_FAILED = 0, 1
 GB300_REASON_SMALL_PIVOT, GB300_REASON_STALLED = 2, 3
 KIND_NAMES = {1: "assemble", 2: "factor_small", 3: "potrf_diag", 4: "trsm_rows", 5: "gemm_tile",
@@ -83,6 +86,12 @@ def lib():
         "gb300_start": (C.c_int, [vp]),
         "gb300_finish": (C.c_int, [vp]),
         "gb300_set_option": (C.c_int, [vp, C.c_int, C.c_int64]),
+        "gb300_get_option": (C.c_int64, [vp, C.c_int]),
+        "gb300_autotune": (C.c_int, [vp, vp, C.c_int, C.c_int, C.POINTER(C.c_int64), C.c_int,
+                                     C.POINTER(C.c_double), vp]),
+        "gb300_autotune_candidates": (C.c_int, [C.POINTER(C.c_int64), C.c_int]),
+        "gb300_autotune_with": (C.c_int, [C.POINTER(C.c_int64), C.c_int, C.c_int,
+                                          C.POINTER(C.c_double), TUNE_TIMER, vp, vp]),
         "gb300_get_stats": (C.c_int, [vp, C.POINTER(C.c_double), C.c_int]),
         "gb300_abi_offset": (C.c_long, [C.c_int, C.c_char_p]),
         "gb300_abi_sizeof": (C.c_long, [C.c_int]),
@@ -165,6 +174,9 @@ class Common:
 
     def set_option(self, option, value):
         return lib().gb300_set_option(self.ptr, option, int(value))
+
+    def get_option(self, option):
+        return lib().gb300_get_option(self.ptr, option)
 
     def stats(self):
         out = (C.c_double * 8)()

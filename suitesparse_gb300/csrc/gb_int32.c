@@ -166,6 +166,7 @@ int cholmod_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2], 
         GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "out of memory");
         return FALSE;
     }
+    gb_autotune_first(a, f, beta, S, Common);
     int ok = gb_super_numeric(a, f, beta, S, Common);
     shadow_put(L, S);
     free_widened(a);

@@ -39,6 +39,8 @@ void gb_error(int status, const char *file, int line, const char *msg,
 typedef struct gb_ctx gb_ctx;
 gb_ctx *gb_ctx_get(cholmod_common *Common, int create);
 int64_t gb_option(cholmod_common *Common, int option);
+void gb_autotune_first(cholmod_sparse *A, cholmod_sparse *F, double beta[2],
+                       cholmod_factor *L, cholmod_common *Common);
 
 /* ---- gb_symbolic.c ------------------------------------------------------- */
 /* Supernodal symbolic analysis of the lower-stored A permuted by Perm. */

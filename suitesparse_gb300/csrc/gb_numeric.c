@@ -26,6 +26,7 @@ gb_ctx *gb_ctx_new(void)
     c->opt_small = GB_SMALL_MAX;
     c->opt_subwork = GB_SUBTREE_WORK;
     c->opt_warprows = GB_WARP_ROWS;
+    c->opt_updgroup = GB_UPD_GROUP;
     c->device = -1;
     c->sweep_mode = 1;
     c->factor_mode = 1;
@@ -73,6 +74,8 @@ int64_t gb_option(cholmod_common *Common, int option)
     if (option == GB300_OPT_SMALL_COLS) return c ? c->opt_small : GB_SMALL_MAX;
     if (option == GB300_OPT_SUBTREE_WORK) return c ? (int64_t)c->opt_subwork : (int64_t)GB_SUBTREE_WORK;
     if (option == GB300_OPT_WARP_ROWS) return c ? c->opt_warprows : GB_WARP_ROWS;
+    if (option == GB300_OPT_UPD_GROUP) return c ? c->opt_updgroup : GB_UPD_GROUP;
+    if (option == GB300_OPT_AUTOTUNE) return c ? c->opt_autotune : 0;
     return 0;
 }
 
@@ -97,6 +100,8 @@ int gb300_set_option(cholmod_common *Common, int option, int64_t value)
     else if (option == GB300_OPT_SMALL_COLS) c->opt_small = GB_MAX(1, GB_MIN(GB_SMALL_MAX, value));
     else if (option == GB300_OPT_SUBTREE_WORK) c->opt_subwork = value < 0 ? 0.0 : (double)value;
     else if (option == GB300_OPT_WARP_ROWS) c->opt_warprows = GB_MAX(0, GB_MIN(GB_WARP_ROWS, value));
+    else if (option == GB300_OPT_UPD_GROUP) c->opt_updgroup = GB_MAX(1, GB_MIN(GB_UPD_GROUP, value));
+    else if (option == GB300_OPT_AUTOTUNE) { c->opt_autotune = value ? 1 : 0; c->tuned = 0; }
     else { GB_ERROR(CHOLMOD_INVALID, "unknown option"); return FALSE; }
     return TRUE;
 }
@@ -228,7 +233,8 @@ gb_plan *gb_plan_get(cholmod_factor *L, cholmod_common *Common, gb_ctx *ctx, int
         if (q->L == L) { P = q; break; }
     if (P && (!plan_matches(P, L) || P->hash != gb_pattern_hash(L)
               || (create && (P->small_cols != ctx->opt_small || P->sub_work != ctx->opt_subwork
-                             || P->warp_rows != ctx->opt_warprows)))) {
+                             || P->warp_rows != ctx->opt_warprows
+                             || P->upd_group != ctx->opt_updgroup)))) {
         plan_unlink(P);
         pthread_mutex_unlock(&plan_lock);
         cudaStreamSynchronize(ctx->stream);
@@ -238,7 +244,7 @@ gb_plan *gb_plan_get(cholmod_factor *L, cholmod_common *Common, gb_ctx *ctx, int
     }
     pthread_mutex_unlock(&plan_lock);
     if (P || !create) return P;
-    P = gb_plan_build(L, ctx->opt_small, ctx->opt_subwork, ctx->opt_warprows);
+    P = gb_plan_build(L, ctx->opt_small, ctx->opt_subwork, ctx->opt_warprows, ctx->opt_updgroup);
     if (!P) { GB_ERROR(CHOLMOD_OUT_OF_MEMORY, "plan construction failed"); return NULL; }
     if (!gb_plan_upload(P)) {
         gb_plan_free(P);
@@ -723,6 +729,7 @@ int cholmod_l_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2]
         Common->status = CHOLMOD_INVALID;
         return FALSE;
     }
+    gb_autotune_first(A, F, beta, L, Common);
     return gb_super_numeric(A, F, beta, L, Common);
 }
 

@@ -497,7 +497,7 @@ static int segments_build(gb_plan *P)
 }
 
 gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_work,
-                       int64_t warp_rows)
+                       int64_t warp_rows, int64_t upd_group)
 {
     if (small_cols < 1) small_cols = 1;
     if (small_cols > GB_SMALL_MAX) small_cols = GB_SMALL_MAX;
@@ -511,6 +511,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
     P->small_cols = small_cols;
     P->sub_work = sub_work;
     P->warp_rows = warp_rows < 0 ? 0 : (warp_rows > GB_WARP_ROWS ? GB_WARP_ROWS : warp_rows);
+    P->upd_group = upd_group < 1 ? 1 : (upd_group > GB_UPD_GROUP ? GB_UPD_GROUP : upd_group);
     P->super_ptr = L->super;
     P->s_ptr = L->s;
     P->pi_ptr = L->pi;
@@ -671,14 +672,14 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
             int32_t *Pid = NULL, *Tid = NULL, *Uid = NULL, *Aid = NULL;
             if (nscol > small_cols) {
                 /* Blocked right-looking LL' in 64-column panels, grouped by
-                 * GB_UPD_GROUP panels: a tile (r, c) takes the update of
+                 * G = upd_group panels: a tile (r, c) takes the update of
                  * each earlier panel of c's own group separately (UPD with
                  * one panel: the lookahead that the next diagonal steps
                  * wait on) and the updates of each earlier group at once
-                 * (UPD with GB_UPD_GROUP panels, k up to 256), so that the
-                 * bulk of the trailing update runs as deeper, fewer tile
-                 * products.  Updates of one tile run in panel order. */
-                const Int G = GB_UPD_GROUP, Q = (Cp + G - 1) / G;
+                 * (UPD with G panels, k up to 64 G), so that the bulk of
+                 * the trailing update runs as deeper, fewer tile products.
+                 * Updates of one tile run in panel order. */
+                const Int G = P->upd_group, Q = (Cp + G - 1) / G;
                 Pid = malloc(sizeof(int32_t) * Cp);
                 Tid = malloc(sizeof(int32_t) * Cp * R);
                 Uid = malloc(sizeof(int32_t) * Cp * R * Cp);

@@ -132,6 +132,7 @@ typedef struct gb_plan {
     Int small_cols;                   /* widest supernode factored whole by one block */
     double sub_work;                  /* work limit of a SUBTREE task (0: none) */
     Int warp_rows;                    /* fronts this tall or less run on one warp (0: none) */
+    Int upd_group;                    /* panels whose trailing updates run at once (1..GB_UPD_GROUP) */
     uint64_t hash;
 
     /* host arrays derived from the pattern (kept for the plan's lifetime) */
@@ -269,6 +270,9 @@ struct gb_ctx {
     int64_t opt_keep, opt_small;
     double opt_subwork;                /* SUBTREE task work limit for new plans */
     int64_t opt_warprows;              /* one-warp front height limit for new plans */
+    int64_t opt_updgroup;              /* grouped trailing updates of new plans */
+    int opt_autotune;                  /* 1 = the first super_numeric tunes the plan options */
+    int tuned;                         /* the automatic tuning ran on this Common */
     double stats[8];
     int64_t launches;            /* kernel launches issued since creation */
     cudaEvent_t ev0, ev1;
@@ -317,7 +321,7 @@ void gb_valmap_anorm(gb_plan *P);
 void gb_valmap_free(gb_plan *P);
 void gb_graph_free(gb_plan *P);     /* gb_mixed.c */
 gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_work,
-                       int64_t warp_rows);
+                       int64_t warp_rows, int64_t upd_group);
 /* Upload the pattern, task arrays and launch sequences. */
 int gb_plan_upload(gb_plan *P);
 void gb_plan_free(gb_plan *P);
