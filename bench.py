@@ -663,6 +663,11 @@ def run_serve(args):
         cols = sum((r["X"].shape if hasattr(r["X"], "shape") else r["X"])[1]
                    for r in recs.values() if r["kind"] == "solve" and r["X"] is not None)
         ok = all(r["status"] == 0 for r in recs.values())
+        bad = {}
+        for r in recs.values():
+            if r["status"] != 0:
+                k = f'{r["kind"]}:{r["status"]}'
+                bad[k] = bad.get(k, 0) + 1
         berr = max([r["berr"] for r in recs.values() if r["kind"] == "solve"] or [0.0])
         # the oracle's backward error of a sample of solutions (the factor a
         # solve used: the latest factor request of its id before it)
@@ -688,11 +693,12 @@ def run_serve(args):
             return r if r >= 0 else None
         return {"form": "FP64 factor" if fp64 else "FP32 factor + FP64 refinement",
                 "offered_rate_per_s": rate * ws, "requests": int(nrq), "wall_s": wall,
-                "all_ok": ok, "p50_ms": worst(lat, 50), "p99_ms": worst(lat, 99),
+                "all_ok": ok, "failed": bad, "p50_ms": worst(lat, 50), "p99_ms": worst(lat, 99),
                 "solve_p50_ms": worst(lat_s, 50), "solve_p99_ms": worst(lat_s, 99),
                 "requests_per_s": nrq / wall, "solves_per_s": cols / wall,
                 "max_backward_error": berr, "oracle_sample_backward_error": be_o,
-                "coalesced": st["coalesced"], "evictions": st["evictions"], "server": st,
+                "coalesced": st["coalesced"], "evictions": st["evictions"],
+                "readmissions": st["readmissions"], "server": st,
                 "clocks": clk.summary()}
 
     sweep = [run(rate * ws, len(base), False) for rate in (200.0, 800.0)]

@@ -585,6 +585,16 @@ int gb300_solve_refined2 (cholmod_sparse *A, cholmod_factor *L, cholmod_dense *B
  * array addresses and a fingerprint of sampled pattern entries; a caller
  * that rewrites L's pattern arrays in place calls this first. */
 int gb300_release_factor (cholmod_factor *L, cholmod_common *Common) ;
+/* Device bytes held by L's device state on Common's device (0 when it has
+ * none): plan structures, factors, update blocks, inverses, operand images,
+ * value maps and work buffers. */
+int64_t gb300_factor_device_bytes (cholmod_factor *L, cholmod_common *Common) ;
+/* Frees what only a factorization uses, keeping what the solves use: the
+ * update blocks, the tensor-core operand images and, after
+ * gb300_factorize_mixed, the factor of the precision the refined solves do
+ * not read (the FP64 one when the FP32 factor is used, else the FP32 one).
+ * The next factorization allocates them again.  Returns the bytes freed. */
+int64_t gb300_trim_factor (cholmod_factor *L, cholmod_common *Common) ;
 
 /* Object helpers for programs without the reference library.  Memory comes
  * from malloc and is counted in Common->malloc_count / memory_inuse the way
@@ -674,6 +684,12 @@ cholmod_factor *gb300_batch_analyze (int npat, cholmod_factor *const *Lpat,
  * factor request for a resident factor refactorizes it in place); a factor
  * request is admitted when its device-memory estimate (from nnz(L)) fits
  * under budget_bytes, evicting idle factors least recently used first;
+ * after each factorization a factor keeps only what its solves use
+ * (gb300_trim_factor) and is charged its measured device bytes
+ * (gb300_factor_device_bytes), also after each refined solve; an evicted
+ * factor keeps the copy of its A on the host (up to 32 GB of evicted A's,
+ * the oldest dropped first), so that a later solve against it factorizes
+ * it again first (a readmission) instead of failing;
  * requests of one factor run in order, and queued solves of one factor are
  * coalesced into one refined solve of up to max_rhs columns.  Every solve is
  * the FP32 factor + FP64 refinement to backward error 1e-12.  A, perm and B
@@ -684,7 +700,8 @@ cholmod_factor *gb300_batch_analyze (int npat, cholmod_factor *const *Lpat,
  * iterations, status, columns of the coalesced solve.  Returns the
  * request's CHOLMOD status.  gb300_server_stats: [0] resident bytes, [1]
  * budget, [2] resident factors, [3] cached patterns, [4] evictions, [5]
- * solves merged into another, [6] requests served. */
+ * solves merged into another, [6] requests served, [7] readmissions, [8]
+ * evicted factors whose A is kept, [9] host bytes of those A's. */
 typedef struct gb300_server gb300_server ;
 gb300_server *gb300_server_create (int nslots, int64_t budget_bytes, int max_rhs) ;
 int gb300_server_factor (gb300_server *S, int64_t req, int64_t factor_id,

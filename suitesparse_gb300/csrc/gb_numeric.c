@@ -288,6 +288,65 @@ int gb_ensure_numeric(gb_plan *P, int dtype)
     return TRUE;
 }
 
+/* device bytes held by a plan: its structures, factors, update blocks,
+ * inverses, operand images, value maps and the grown work buffers */
+size_t gb_plan_device_bytes(const gb_plan *P)
+{
+    size_t b = P->struct_bytes + P->vm_bytes;
+    for (int d = 0; d < 2; d++) {
+        const size_t e = d ? sizeof(float) : sizeof(double);
+        if (P->d_Lx[d]) b += e * (size_t)GB_MAX(P->xsize, 1);
+        if (P->d_CB[d]) b += e * (size_t)GB_MAX(P->cb_total, 1);
+        if (P->d_Linv[d]) b += e * (size_t)GB_MAX(P->linv_total, 1);
+    }
+    if (P->d_img) b += sizeof(float) * GB_IMG_FLOATS_HOST * (size_t)P->img_total;
+    b += P->sx_cap + P->si_cap + P->sp_cap + P->y_cap + P->u_cap + P->b_cap + P->spw_cap
+         + P->sws_cap + P->ax_cap + P->rp_cap + P->rj_cap + P->rx_cap + P->x_cap + P->r_cap
+         + P->bx_cap + P->bred_cap;
+    if (P->d_scale) b += sizeof(double) * (size_t)(P->n + 1);
+    if (P->d_scale_perm) b += sizeof(double) * (size_t)(P->n + 1);
+    return b;
+}
+
+int64_t gb300_factor_device_bytes(cholmod_factor *L, cholmod_common *Common)
+{
+    if (!Common || !L) return -1;
+    gb_ctx *ctx = gb_ctx_get(Common, 0);
+    gb_plan *P = ctx ? gb_plan_get(L, Common, ctx, 0) : NULL;
+    return P ? (int64_t)gb_plan_device_bytes(P) : 0;
+}
+
+int64_t gb300_trim_factor(cholmod_factor *L, cholmod_common *Common)
+{
+    if (!Common || !L) return -1;
+    gb_ctx *ctx = gb_ctx_get(Common, 0);
+    gb_plan *P = ctx ? gb_plan_get(L, Common, ctx, 0) : NULL;
+    if (!P) return 0;
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error");
+        return -1;
+    }
+    const size_t before = gb_plan_device_bytes(P);
+    /* a captured refinement step names these buffers: capture again */
+    gb_graph_free(P);
+    for (int d = 0; d < 2; d++) {
+        if (P->d_CB[d]) cudaFree(P->d_CB[d]);
+        P->d_CB[d] = NULL;
+    }
+    if (P->d_img) cudaFree(P->d_img);
+    P->d_img = NULL;
+    /* the precision the refined solves do not use */
+    const int unused = P->mixed == 1 ? 0 : (P->mixed == 2 ? 1 : -1);
+    if (unused >= 0) {
+        if (P->d_Lx[unused]) cudaFree(P->d_Lx[unused]);
+        if (P->d_Linv[unused]) cudaFree(P->d_Linv[unused]);
+        P->d_Lx[unused] = P->d_Linv[unused] = NULL;
+        P->dev_valid[unused] = 0;
+        P->linv_valid[unused] = 0;
+    }
+    return (int64_t)(before - gb_plan_device_bytes(P));
+}
+
 #define CU(call) do { if ((call) != cudaSuccess) goto cuda_fail; } while (0)
 #define LK(call) do { if ((call) != 0) goto cuda_fail; } while (0)
 

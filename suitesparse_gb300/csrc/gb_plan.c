@@ -1198,6 +1198,7 @@ fail:
     do {                                                                       \
         size_t b_ = (bytes) ? (bytes) : 16;                                    \
         if (cudaMalloc((void **)&(dst), b_) != cudaSuccess) goto fail;         \
+        P->struct_bytes += b_;                                                 \
         if ((bytes) && cudaMemcpy((dst), (src), (bytes), cudaMemcpyHostToDevice) != cudaSuccess) goto fail; \
     } while (0)
 
@@ -1257,6 +1258,7 @@ int gb_plan_upload(gb_plan *P)
         size_t mx = (size_t)GB_MAX(P->dag_max, 1);
         if (cudaMalloc((void **)&P->d_dag_cnt, sizeof(int32_t) * mx) != cudaSuccess) goto fail;
         if (cudaMalloc((void **)&P->d_dag_q, sizeof(int32_t) * 2 * mx) != cudaSuccess) goto fail;
+        P->struct_bytes += sizeof(int32_t) * 3 * mx;
         if (cudaMalloc((void **)&P->d_dag_ctrl, sizeof(int32_t) * GB_DAG_NCTRL) != cudaSuccess) goto fail;
         if (cudaMalloc((void **)&P->d_dag_smf, sizeof(int32_t) * GB_DAG_NSMF) != cudaSuccess) goto fail;
         if (cudaMemset(P->d_dag_smf, 0, sizeof(int32_t) * GB_DAG_NSMF) != cudaSuccess) goto fail;
@@ -1277,6 +1279,7 @@ int gb_plan_upload(gb_plan *P)
     UP(P->d_imgbase, P->h_imgbase, sizeof(int64_t) * (ns + 1));
     if (cudaMalloc((void **)&P->d_xready, sizeof(int32_t) * (P->nblk_total + 1)) != cudaSuccess) goto fail;
     if (cudaMalloc((void **)&P->d_done, sizeof(int32_t) * (ns + 1)) != cudaSuccess) goto fail;
+    P->struct_bytes += sizeof(int32_t) * (P->nblk_total + ns + 2);
     if (cudaMalloc((void **)&P->d_ticket, sizeof(int32_t) * 4) != cudaSuccess) goto fail;
     P->d_err = P->d_ticket + 2;
     P->ptrs.Super = P->d_Super;
@@ -1321,6 +1324,7 @@ int gb_plan_upload(gb_plan *P)
         UP(P->d_fd_ctrl0, ctrl0, sizeof ctrl0);
         if (cudaMalloc((void **)&P->d_fd_cnt, sizeof(int32_t) * (N + 1)) != cudaSuccess) goto fail;
         if (cudaMalloc((void **)&P->d_fd_q, sizeof(int32_t) * 2 * (N + 1)) != cudaSuccess) goto fail;
+        P->struct_bytes += sizeof(int32_t) * (n0 + n1 + 3 * (N + 1));
         gb_finst inst;
         memset(&inst, 0, sizeof inst);
         inst.fail = P->d_fail;

@@ -213,6 +213,8 @@ typedef struct gb_plan {
     /* inputs and sweep workspace */
     int64_t *d_Sp, *d_Si;
     void *d_Sx;
+    size_t struct_bytes;               /* device bytes of the uploaded plan structures */
+    size_t vm_bytes;                   /* device bytes of the value maps */
     size_t sx_cap, si_cap, sp_cap;
     void *d_Y, *d_U, *d_B;
     size_t y_cap, u_cap, b_cap;
@@ -322,6 +324,7 @@ void gb_valmap_free(gb_plan *P);
 void gb_graph_free(gb_plan *P);     /* gb_mixed.c */
 gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_work,
                        int64_t warp_rows, int64_t upd_group);
+size_t gb_plan_device_bytes(const gb_plan *P);
 /* Upload the pattern, task arrays and launch sequences. */
 int gb_plan_upload(gb_plan *P);
 void gb_plan_free(gb_plan *P);

@@ -11,7 +11,15 @@
  *     plan and device buffers are reused);
  *   - admission: a factor request starts only when its device-memory
  *     estimate fits under the budget; idle resident factors without queued
- *     work are evicted least recently used first to make room;
+ *     work are evicted least recently used first to make room.  After each
+ *     factorization the factor drops what only a factorization uses
+ *     (gb300_trim_factor: update blocks, tensor-core operand images, the
+ *     unused precision) and is charged its measured device bytes
+ *     (gb300_factor_device_bytes), also after each refined solve;
+ *   - an evicted factor keeps the host copy of its A (within a host budget,
+ *     oldest dropped first): a later solve against it factorizes it again
+ *     before solving (a readmission), a later factor request refactorizes
+ *     it as usual;
  *   - requests of one factor run in arrival order and never concurrently;
  *     queued solve requests of one factor are coalesced into one refined
  *     solve with all their right-hand sides (up to max_rhs columns);
@@ -47,6 +55,8 @@ typedef struct gb_sfactor {
     cholmod_factor *L;            /* NULL until its first factorization succeeds */
     cholmod_sparse *A;
     int busy;
+    int evicted;                  /* device state released; A kept on the host */
+    int64_t est;                  /* device bytes when last resident */
     double last_use;
     struct gb_sfactor *next;
 } gb_sfactor;
@@ -68,7 +78,8 @@ struct gb300_server {
     gb_sfactor *factors;
     gb_spattern *patterns;
     int nslots, ncommons, max_rhs, stop;
-    int64_t budget, in_use, evictions, coalesced, served;
+    int64_t budget, in_use, evictions, coalesced, served, readmissions;
+    int64_t host_budget, host_kept;   /* host bytes of the evicted factors' A */
     pthread_t *th;
     cholmod_common *commons;
 };
@@ -112,12 +123,32 @@ static void req_free_payload(gb_sreq *r, cholmod_common *c)
     r->B = NULL;
 }
 
-/* device bytes of a resident factor: FP32 factor, update blocks and
- * inverses (about 2.5 xsize entries), FP64 copy of A and refinement vectors */
+/* admission estimate of a factor's resident device bytes before it was
+ * measured: FP32 factor and diagonal-block inverses (about 1.5 xsize
+ * entries), the FP64 copy of A in both triangles with its maps (~60 bytes
+ * per stored entry of the lower part) and the refinement vectors */
 static int64_t estimate_bytes(const cholmod_factor *L, const cholmod_sparse *A)
 {
     int64_t nz = A ? (int64_t)((const int64_t *)A->p)[A->ncol] : 0;
-    return (int64_t)(10.0 * (double)L->xsize) + 24 * nz + 64 * (int64_t)L->n;
+    if (!L) return 100 * nz;
+    return (int64_t)(6.0 * (double)L->xsize) + 60 * nz + 256 * (int64_t)L->n;
+}
+
+static int64_t host_bytes(const cholmod_sparse *A)
+{
+    return A ? (int64_t)(24 * ((const int64_t *)A->p)[A->ncol] + 8 * (A->ncol + 1)) : 0;
+}
+
+static void factor_unlink_free(gb300_server *S, gb_sfactor *victim, cholmod_common *c)
+{
+    for (gb_sfactor **pp = &S->factors; *pp; pp = &(*pp)->next)
+        if (*pp == victim) { *pp = victim->next; break; }
+    if (victim->L) {
+        gb300_release_factor(victim->L, c);
+        gb300_free_factor(&victim->L, c);
+    }
+    gb300_free_sparse(&victim->A, c);
+    free(victim);
 }
 
 static int pending_for(gb300_server *S, int64_t factor_id)
@@ -127,26 +158,53 @@ static int pending_for(gb300_server *S, int64_t factor_id)
     return 0;
 }
 
-/* under S->mu: release idle factors (least recently used first) until need
- * bytes fit; returns whether they fit */
+/* under S->mu: release the device state of idle factors (least recently
+ * used first) until need bytes fit; returns whether they fit.  An evicted
+ * factor keeps its A on the host while the host budget allows (the oldest
+ * evicted factors are dropped whole beyond it). */
 static int make_room(gb300_server *S, int64_t need, cholmod_common *c)
 {
     while (S->in_use + need > S->budget) {
-        gb_sfactor *victim = NULL, **vp = NULL;
-        for (gb_sfactor **pp = &S->factors; *pp; pp = &(*pp)->next) {
-            gb_sfactor *f = *pp;
-            if (f->busy || pending_for(S, f->id)) continue;
-            if (!victim || f->last_use < victim->last_use) { victim = f; vp = pp; }
+        gb_sfactor *victim = NULL;
+        for (gb_sfactor *f = S->factors; f; f = f->next) {
+            if (f->busy || f->evicted || pending_for(S, f->id)) continue;
+            if (!victim || f->last_use < victim->last_use) victim = f;
         }
         if (!victim) return S->in_use + need <= S->budget || S->in_use == 0;
-        *vp = victim->next;
         S->in_use -= victim->bytes;
         S->evictions++;
-        gb300_release_factor(victim->L, c);
-        gb300_free_factor(&victim->L, c);
-        gb300_free_sparse(&victim->A, c);
-        free(victim);
+        if (victim->L) {
+            gb300_release_factor(victim->L, c);
+            gb300_free_factor(&victim->L, c);
+        }
+        victim->est = victim->bytes;
+        victim->bytes = 0;
+        if (!victim->A) { factor_unlink_free(S, victim, c); continue; }
+        victim->evicted = 1;
+        S->host_kept += host_bytes(victim->A);
+        while (S->host_kept > S->host_budget) {
+            gb_sfactor *old = NULL;
+            for (gb_sfactor *f = S->factors; f; f = f->next)
+                if (f->evicted && !f->busy && !pending_for(S, f->id)
+                    && (!old || f->last_use < old->last_use)) old = f;
+            if (!old) break;
+            S->host_kept -= host_bytes(old->A);
+            factor_unlink_free(S, old, c);
+        }
     }
+    return 1;
+}
+
+/* under S->mu: bring an evicted factor back under the budget (its device
+ * state is rebuilt by the worker that takes it) */
+static int readmit(gb300_server *S, gb_sfactor *F, cholmod_common *c)
+{
+    int64_t need = F->est > 0 ? F->est : estimate_bytes(F->L ? F->L : NULL, F->A);
+    if (!make_room(S, need, c)) return 0;
+    S->host_kept -= host_bytes(F->A);
+    F->evicted = 0;
+    F->bytes = need;
+    S->in_use += need;
     return 1;
 }
 
@@ -172,7 +230,7 @@ static gb_sreq *take_work(gb300_server *S, gb_sreq **group, int *ngroup, cholmod
         /* an earlier queued request of the same factor goes first */
         for (gb_sreq *q = S->qhead; q != r; q = q->next_q)
             if (q->factor_id == r->factor_id) { blocked = 1; break; }
-        if (!blocked && r->kind == REQ_SOLVE && !F) {
+        if (!blocked && r->kind == REQ_SOLVE && (!F || (F->evicted && !F->A))) {
             unlink_req(S, pp, r, prev);
             r->status = CHOLMOD_INVALID;
             r->start = r->finish = gb300_server_now();
@@ -185,7 +243,14 @@ static gb_sreq *take_work(gb300_server *S, gb_sreq **group, int *ngroup, cholmod
         gb_spattern *pat = NULL;
         int64_t need = 0;
         int runnable = !blocked && !(F && F->busy);
-        if (runnable && r->kind == REQ_FACTOR && !F) {
+        if (runnable && F && F->evicted) {
+            /* a request of an evicted factor: a factor request replaces its
+             * A, a solve refactorizes the kept one */
+            gb_spattern *fp = pattern_find(S, F->pattern_id);
+            if (r->kind == REQ_SOLVE && !(fp && fp->state == 1)) runnable = 0;
+            else runnable = readmit(S, F, c);
+            if (runnable && r->kind == REQ_SOLVE) S->readmissions++;
+        } else if (runnable && r->kind == REQ_FACTOR && !F) {
             pat = pattern_find(S, r->pattern_id);
             if (pat && pat->state == 2) runnable = 0;   /* being analysed by a worker */
             else {
@@ -246,6 +311,20 @@ static gb_sreq *take_work(gb300_server *S, gb_sreq **group, int *ngroup, cholmod
     return NULL;
 }
 
+/* the factor's measured device bytes replace its charge (after a
+ * factorization, first without what only the factorization used) */
+static void charge(gb300_server *S, gb_sfactor *F, cholmod_common *c, int trim)
+{
+    if (!F->L) return;
+    if (trim) gb300_trim_factor(F->L, c);
+    int64_t bytes = gb300_factor_device_bytes(F->L, c);
+    if (bytes <= 0) return;
+    pthread_mutex_lock(&S->mu);
+    S->in_use += bytes - F->bytes;
+    F->bytes = bytes;
+    pthread_mutex_unlock(&S->mu);
+}
+
 static void run_factor(gb300_server *S, gb_sreq *r, cholmod_common *c)
 {
     pthread_mutex_lock(&S->mu);
@@ -278,11 +357,24 @@ static void run_factor(gb300_server *S, gb_sreq *r, cholmod_common *c)
     r->A = NULL;
     int ok = gb300_factorize_mixed(F->A, F->L, c);
     r->status = ok ? c->status : (c->status ? c->status : CHOLMOD_GPU_PROBLEM);
-    int64_t bytes = estimate_bytes(F->L, F->A);
+    charge(S, F, c, 1);
+}
+
+/* a readmitted factor: its pattern copied again and its kept A factorized */
+static int refactor_kept(gb300_server *S, gb_sfactor *F, cholmod_common *c)
+{
     pthread_mutex_lock(&S->mu);
-    S->in_use += bytes - F->bytes;
-    F->bytes = bytes;
+    gb_spattern *p = pattern_find(S, F->pattern_id);
     pthread_mutex_unlock(&S->mu);
+    if (!p || p->state != 1 || !p->L || !F->A) return CHOLMOD_INVALID;
+    cholmod_factor *Lp = p->L;
+    int32_t zero = 0;
+    F->L = gb300_batch_analyze(1, &Lp, 1, &zero, c);
+    if (!F->L) return CHOLMOD_OUT_OF_MEMORY;
+    int ok = gb300_factorize_mixed(F->A, F->L, c);
+    int st = ok ? c->status : (c->status ? c->status : CHOLMOD_GPU_PROBLEM);
+    charge(S, F, c, 1);
+    return st;
 }
 
 static void run_solves(gb300_server *S, gb_sreq **g, int ng, cholmod_common *c)
@@ -290,6 +382,13 @@ static void run_solves(gb300_server *S, gb_sreq **g, int ng, cholmod_common *c)
     pthread_mutex_lock(&S->mu);
     gb_sfactor *F = factor_find(S, g[0]->factor_id);
     pthread_mutex_unlock(&S->mu);
+    if (F && !F->L && F->A) {
+        int st = refactor_kept(S, F, c);
+        if (st != CHOLMOD_OK) {
+            for (int k = 0; k < ng; k++) g[k]->status = st;
+            return;
+        }
+    }
     if (!F || !F->L || !F->A) {
         for (int k = 0; k < ng; k++) g[k]->status = CHOLMOD_INVALID;
         return;
@@ -329,6 +428,7 @@ static void run_solves(gb300_server *S, gb_sreq **g, int ng, cholmod_common *c)
     }
     gb300_free_dense(&X, c);
     gb300_free_dense(&B, c);
+    charge(S, F, c, 0);           /* the solves' work buffers */
 }
 
 typedef struct { gb300_server *S; int slot; } gb_warg;
@@ -384,6 +484,7 @@ gb300_server *gb300_server_create(int nslots, int64_t budget_bytes, int max_rhs)
     if (!S) return NULL;
     S->nslots = nslots;
     S->budget = budget_bytes;
+    S->host_budget = (int64_t)32 << 30;
     S->max_rhs = max_rhs;
     S->th = calloc(nslots, sizeof(pthread_t));
     S->commons = calloc(nslots, sizeof(cholmod_common));
@@ -504,10 +605,13 @@ int gb300_server_stats(gb300_server *S, double *out, int nout)
     int64_t nf = 0, np = 0;
     for (gb_sfactor *f = S->factors; f; f = f->next) nf++;
     for (gb_spattern *p = S->patterns; p; p = p->next) np++;
-    double v[7] = {(double)S->in_use, (double)S->budget, (double)nf, (double)np,
-                   (double)S->evictions, (double)S->coalesced, (double)S->served};
+    int64_t ne = 0;
+    for (gb_sfactor *f = S->factors; f; f = f->next) ne += f->evicted;
+    double v[10] = {(double)S->in_use, (double)S->budget, (double)(nf - ne), (double)np,
+                    (double)S->evictions, (double)S->coalesced, (double)S->served,
+                    (double)S->readmissions, (double)ne, (double)S->host_kept};
     pthread_mutex_unlock(&S->mu);
-    for (int i = 0; i < nout && i < 7; i++) out[i] = v[i];
+    for (int i = 0; i < nout && i < 10; i++) out[i] = v[i];
     return TRUE;
 }
 

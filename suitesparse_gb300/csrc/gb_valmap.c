@@ -30,6 +30,7 @@ void gb_valmap_free(gb_plan *P)
     P->d_Ax = NULL;
     P->ax_cap = 0;
     P->vm_valid = 0;
+    P->vm_bytes = 0;
 }
 
 /* length of A's value array that entries can occupy */
@@ -143,6 +144,7 @@ static int build(gb_plan *P, cholmod_sparse *A, cholmod_common *Common)
          && UPLOAD(P->d_smap, smap, sizeof(int64_t) * snz)
          && UPLOAD(P->d_rmap, rmap, sizeof(int64_t) * rnz)
          && UPLOAD(P->d_dmap, dmap, sizeof(int64_t) * n);
+    if (ok) P->vm_bytes = sizeof(int64_t) * (size_t)(snz + rnz + n);
     if (ok) {
         P->h_vm_Ap = malloc(sizeof(Int) * (n + 1));
         P->h_vm_Ai = malloc(sizeof(Int) * GB_MAX(xlen, 1));

@@ -104,10 +104,11 @@ class Server:
         return st, X, info
 
     def stats(self):
-        out = (C.c_double * 7)()
-        self.L.gb300_server_stats(self.h, out, 7)
+        out = (C.c_double * 10)()
+        self.L.gb300_server_stats(self.h, out, 10)
         keys = ("resident_bytes", "budget_bytes", "resident_factors", "cached_patterns",
-                "evictions", "coalesced", "served")
+                "evictions", "coalesced", "served", "readmissions", "evicted_kept",
+                "evicted_host_bytes")
         return dict(zip(keys, list(out)))
 
     def set_option(self, option, value):

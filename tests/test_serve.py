@@ -105,3 +105,43 @@ def test_same_result_alone_and_in_the_mix(lib, oracle_mod):
             rel = np.abs(X_a - rec["X"]).max() / np.abs(X_a).max()
             assert rel <= 1e-6, (rq["req"], rel)
     assert nsolve >= 4 and nexact >= 1
+
+
+@pytest.mark.gpu
+def test_evicted_factor_is_readmitted_for_its_solves(lib, oracle_mod):
+    """A budget that holds about one factor: each new factor evicts the
+    previous one (its A stays on the host); a solve against an evicted
+    factor factorizes it again and gives the same solution, bit for bit,
+    as the solve against the resident factor did; the charge of a resident
+    factor is its measured device bytes."""
+    mats = {}
+    for fid, dims in enumerate(((40, 40), (36, 44), (12, 12, 12))):
+        mats[fid] = (M.laplace2d(*dims, seed=fid) if len(dims) == 2
+                     else M.laplace3d(dims[0], seed=fid)), M.grid_nd_perm(dims)
+    S = SV.Server(nslots=1, budget_bytes=1 << 20, max_rhs=8)
+    try:
+        first = {}
+        req = 0
+        for fid, (mat, perm) in mats.items():
+            S.factor(req, fid, fid, mat, perm)
+            assert S.wait(req)[0] == 0
+            st = S.stats()
+            assert st["resident_factors"] == 1 and 0 < st["resident_bytes"]
+            B = M.rhs(mat[0], 2, 10 + fid)
+            S.solve(req + 1, fid, B)
+            first[fid] = (B, S.wait(req + 1))
+            assert first[fid][1][0] == 0
+            req += 2
+        st = S.stats()
+        assert st["evictions"] >= 2 and st["evicted_kept"] == 2
+        for fid, (mat, _) in mats.items():
+            B, (_, X0, _) = first[fid]
+            S.solve(req, fid, B)
+            s1, X1, info = S.wait(req)
+            req += 1
+            assert s1 == 0, s1
+            assert oracle_mod.backward_error(*mat, X1, B).max() <= 1e-12
+            assert np.array_equal(X0, X1), fid
+        assert S.stats()["readmissions"] >= 2
+    finally:
+        S.close()
