@@ -598,7 +598,9 @@ int64_t gb300_trim_factor (cholmod_factor *L, cholmod_common *Common) ;
 
 /* Object helpers for programs without the reference library.  Memory comes
  * from malloc and is counted in Common->malloc_count / memory_inuse the way
- * CHOLMOD counts it, so CHOLMOD's own cholmod_l_free_* can free it too. */
+ * CHOLMOD counts it, so CHOLMOD's own cholmod_l_free_* can free it too.
+ * xdtype = xtype + dtype: real, complex ((re, im) pairs in x) or zomplex
+ * (re in x, im in z); pattern for a sparse matrix only. */
 cholmod_sparse *gb300_allocate_sparse (size_t nrow, size_t ncol, size_t nzmax,
     int sorted, int packed, int stype, int xdtype, cholmod_common *Common) ;
 cholmod_dense *gb300_allocate_dense (size_t nrow, size_t ncol, size_t d,

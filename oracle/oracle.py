@@ -253,3 +253,78 @@ def backward_error(n, Ap, Ai, Ax, X, B):
     anorm = rowsum.max() if n else 0.0
     R = B - AX
     return np.abs(R).max(axis=0) / (anorm * np.abs(X).max(axis=0) + np.abs(B).max(axis=0))
+
+
+def complex_hermitian(n, Ap, Ai, Ax, perm=None):
+    """Dense P A P^H of a Hermitian A given by its lower triangle (complex
+    Ax); the imaginary part of the diagonal is dropped, as the reference's
+    complex factorization ignores it (LAPACK's zpotrf reads the real part of
+    a diagonal entry only)."""
+    cols = np.repeat(np.arange(n, dtype=np.int64), np.diff(Ap))
+    low = Ai >= cols
+    i, j, v = Ai[low], cols[low], np.asarray(Ax)[low]
+    H = np.zeros((n, n), dtype=np.complex128)
+    d = i == j
+    H[i[d], j[d]] = v[d].real
+    H[i[~d], j[~d]] = v[~d]
+    H[j[~d], i[~d]] = np.conj(v[~d])
+    if perm is not None:
+        p = np.asarray(perm, np.int64)
+        H = H[np.ix_(p, p)]
+    return H
+
+
+def complex_factor(sym, H, quick_return=False):
+    """Complex supernodal LL^H of the dense Hermitian H (already permuted) on
+    the supernodal pattern sym (Super, Pi, Px, Ls), restated for small
+    orders: column-by-column left-looking Cholesky, L(j,j) = sqrt(H(j,j) -
+    sum |L(j,k)|^2) real, L(i,j) = (H(i,j) - sum L(i,k) conj(L(j,k))) /
+    L(j,j) -- the factor the reference's complex workers compute with
+    zherk / zgemm / zpotrf / ztrsm (Supernodal/t_cholmod_super_numeric_worker.c
+    with L_ENTRY 2).  A non-positive pivot in column f stops it: L->minor =
+    f and the failing supernode is cleaned up as in the real worker (its
+    columns from f on, the whole supernode with quick_return, and every
+    later entry zero).  Returns (status 0/1, minor, Lx complex)."""
+    n = H.shape[0]
+    L = np.zeros((n, n), dtype=np.complex128)
+    minor = n
+    for j in range(n):
+        dj = H[j, j].real - np.sum(np.abs(L[j, :j]) ** 2)
+        if not dj > 0:
+            minor = j
+            break
+        ljj = np.sqrt(dj)
+        L[j, j] = ljj
+        L[j + 1:, j] = (H[j + 1:, j] - L[j + 1:, :j] @ np.conj(L[j, :j])) / ljj
+    Super, Pi, Px, Ls = (np.asarray(sym[k], np.int64) for k in ("Super", "Pi", "Px", "Ls"))
+    ns = len(Super) - 1
+    Lx = np.zeros(int(Px[ns]), dtype=np.complex128)
+    zero_from = len(Lx)
+    for s in range(ns):
+        k1, k2 = int(Super[s]), int(Super[s + 1])
+        rows = Ls[Pi[s]:Pi[s + 1]]
+        blk = L[np.ix_(rows, np.arange(k1, k2))]
+        Lx[Px[s]:Px[s] + blk.size] = blk.ravel(order="F")
+        if k1 <= minor < k2:
+            info = minor - k1 + 1
+            keep = 0 if (info == 1 or quick_return) else info - 1
+            zero_from = int(Px[s]) + keep * len(rows)
+    Lx[zero_from:] = 0
+    return (0 if minor == n else 1), minor, Lx
+
+
+def complex_solve(H, B):
+    """x = H \\ b for the dense Hermitian positive definite H (numpy)."""
+    return np.linalg.solve(H, np.asarray(B, np.complex128))
+
+
+def complex_backward_error(H, X, B):
+    """|b - H x|_inf / (|H|_inf |x|_inf + |b|_inf) per column, complex
+    moduli (the measure of backward_error for a dense Hermitian H)."""
+    X = np.asarray(X, np.complex128)
+    B = np.asarray(B, np.complex128)
+    if X.ndim == 1:
+        X, B = X[:, None], B[:, None]
+    R = B - H @ X
+    an = np.abs(H).sum(axis=1).max()
+    return np.abs(R).max(axis=0) / (an * np.abs(X).max(axis=0) + np.abs(B).max(axis=0))

@@ -18,6 +18,9 @@
 //   TRIALS   number of timed factorizations (median reported), default 1
 // outputs in DIR: out_meta.txt, Perm.bin, ColCount.bin, Super.bin, Pi.bin,
 //   Px.bin, Ls.bin (int64), Lx.bin (double, widened when DTYPE=s), X.bin.
+// REF_COMPLEX=1: A is complex (Hermitian, lower), its imaginary parts in
+//   Az.bin and B's in Bz.bin (double); L->x and X are written as (re, im)
+//   pairs of doubles in Lx.bin and X.bin.
 
 #include <stdio.h>
 #include <stdlib.h>
@@ -82,6 +85,12 @@ int main(int argc, char **argv)
     double *Bx = nrhs > 0 ? read_file(dir, "B.bin", NULL) : NULL;
     int64_t *UserPerm = read_file(dir, "UserPerm.bin", NULL);
     if (!Ap || !Ai || !Ax) { fprintf(stderr, "missing matrix files\n"); return 2; }
+    const char *cx_env = getenv("REF_COMPLEX");
+    const int cx = cx_env && cx_env[0] == '1';
+    double *Az = cx ? read_file(dir, "Az.bin", NULL) : NULL;
+    double *Bz = cx && nrhs > 0 ? read_file(dir, "Bz.bin", NULL) : NULL;
+    if (cx && (!Az || (nrhs > 0 && !Bz))) { fprintf(stderr, "missing imaginary parts\n"); return 2; }
+    const int xt = cx ? CHOLMOD_COMPLEX : CHOLMOD_REAL, ne = cx ? 2 : 1;
 
     cholmod_common c;
     cholmod_l_start(&c);
@@ -101,15 +110,15 @@ int main(int argc, char **argv)
     else c.method[0].ordering = CHOLMOD_NATURAL;
 
     int dt = single ? CHOLMOD_SINGLE : CHOLMOD_DOUBLE;
-    cholmod_sparse *A = cholmod_l_allocate_sparse(n, n, nnz, 1, 1, -1,
-                                                  CHOLMOD_REAL + dt, &c);
+    cholmod_sparse *A = cholmod_l_allocate_sparse(n, n, nnz, 1, 1, -1, xt + dt, &c);
     memcpy(A->p, Ap, (n + 1) * sizeof(int64_t));
     memcpy(A->i, Ai, nnz * sizeof(int64_t));
-    if (single) {
-        float *x = A->x;
-        for (long p = 0; p < nnz; p++) x[p] = (float)Ax[p];
-    } else {
-        memcpy(A->x, Ax, nnz * sizeof(double));
+    for (long p = 0; p < nnz; p++) {
+        for (int k = 0; k < ne; k++) {
+            double v = k ? Az[p] : Ax[p];
+            if (single) ((float *)A->x)[ne * p + k] = (float)v;
+            else ((double *)A->x)[ne * p + k] = v;
+        }
     }
 
     double t0 = SuiteSparse_time();
@@ -132,24 +141,21 @@ int main(int argc, char **argv)
 
     double t_solve = 0, resid = -1;
     if (Bx && nrhs > 0 && L->is_super && L->minor == (size_t)n) {
-        cholmod_dense *B = cholmod_l_allocate_dense(n, nrhs, n, CHOLMOD_REAL + dt, &c);
-        if (single) {
-            float *b = B->x;
-            for (long p = 0; p < n * nrhs; p++) b[p] = (float)Bx[p];
-        } else {
-            memcpy(B->x, Bx, n * nrhs * sizeof(double));
+        cholmod_dense *B = cholmod_l_allocate_dense(n, nrhs, n, xt + dt, &c);
+        for (long p = 0; p < n * nrhs; p++) {
+            for (int k = 0; k < ne; k++) {
+                double v = k ? Bz[p] : Bx[p];
+                if (single) ((float *)B->x)[ne * p + k] = (float)v;
+                else ((double *)B->x)[ne * p + k] = v;
+            }
         }
         t0 = SuiteSparse_time();
         cholmod_dense *X = cholmod_l_solve(CHOLMOD_A, L, B, &c);
         t_solve = SuiteSparse_time() - t0;
-        double *xo = malloc(n * nrhs * sizeof(double));
-        if (single) {
-            float *x = X->x;
-            for (long p = 0; p < n * nrhs; p++) xo[p] = x[p];
-        } else {
-            memcpy(xo, X->x, n * nrhs * sizeof(double));
-        }
-        write_file(dir, "X.bin", xo, n * nrhs * sizeof(double));
+        double *xo = malloc(ne * n * nrhs * sizeof(double));
+        for (long p = 0; p < ne * n * nrhs; p++)
+            xo[p] = single ? ((float *)X->x)[p] : ((double *)X->x)[p];
+        write_file(dir, "X.bin", xo, ne * n * nrhs * sizeof(double));
         // backward error |b-Ax|/(|A||x|+|b|), inf-norms, column 0 (demo :614-617)
         double one[2] = {1, 0}, m1[2] = {-1, 0};
         cholmod_dense *R = cholmod_l_copy_dense(B, &c);
@@ -171,7 +177,7 @@ int main(int argc, char **argv)
     int64_t *SBp = sncol > 0 ? read_file(dir, "SBp.bin", NULL) : NULL;
     int64_t *SBi = SBp ? read_file(dir, "SBi.bin", NULL) : NULL;
     double *SBx = SBp ? read_file(dir, "SBx.bin", NULL) : NULL;
-    if (SBp && !single && L->is_super && L->minor == (size_t)n) {
+    if (SBp && !single && !cx && L->is_super && L->minor == (size_t)n) {
         long bnz = SBp[sncol];
         cholmod_sparse *SB = cholmod_l_allocate_sparse(n, sncol, bnz > 0 ? bnz : 1, 0, 1, 0,
                                                        CHOLMOD_REAL + CHOLMOD_DOUBLE, &c);
@@ -218,14 +224,11 @@ int main(int argc, char **argv)
         write_file(dir, "Px.bin", L->px, (L->nsuper + 1) * sizeof(int64_t));
         write_file(dir, "Ls.bin", L->s, L->ssize * sizeof(int64_t));
         if (L->x) {
-            double *lx = malloc(L->xsize * sizeof(double));
-            if (single) {
-                float *x = L->x;
-                for (size_t p = 0; p < L->xsize; p++) lx[p] = x[p];
-            } else {
-                memcpy(lx, L->x, L->xsize * sizeof(double));
-            }
-            write_file(dir, "Lx.bin", lx, L->xsize * sizeof(double));
+            const size_t nx = (L->xtype == CHOLMOD_COMPLEX ? 2 : 1) * L->xsize;
+            double *lx = malloc(nx * sizeof(double));
+            for (size_t p = 0; p < nx; p++)
+                lx[p] = single ? ((float *)L->x)[p] : ((double *)L->x)[p];
+            write_file(dir, "Lx.bin", lx, nx * sizeof(double));
             free(lx);
         }
     }

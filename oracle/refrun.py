@@ -22,7 +22,12 @@ def run(n, Ap, Ai, Ax, ordering="amd", dtype="d", B=None, perm=None, trials=1,
         env=None, SB=None):
     """Analyze + factorize (+ solve if B) with the reference; returns a dict.
     SB = (Bp, Bi, Bx) of a sparse right-hand side: out["SX"][sys] =
-    (Xp, Xi, Xx, nzmax) of cholmod_l_spsolve(sys) for sys = 0..8."""
+    (Xp, Xi, Xx, nzmax) of cholmod_l_spsolve(sys) for sys = 0..8.  A complex
+    Ax (and B) runs the complex factorization: out["Lx"] and out["X"] are
+    complex then."""
+    cx = np.iscomplexobj(Ax)
+    if cx:
+        env = dict(env if env is not None else os.environ, REF_COMPLEX="1")
     with tempfile.TemporaryDirectory() as d:
         nrhs = 0 if B is None else (1 if B.ndim == 1 else B.shape[1])
         sncol = 0 if SB is None else len(SB[0]) - 1
@@ -33,10 +38,14 @@ def run(n, Ap, Ai, Ax, ordering="amd", dtype="d", B=None, perm=None, trials=1,
                 np.asarray(a, dt).tofile(os.path.join(d, name + ".bin"))
         np.asarray(Ap, np.int64).tofile(os.path.join(d, "Ap.bin"))
         np.asarray(Ai, np.int64).tofile(os.path.join(d, "Ai.bin"))
-        np.asarray(Ax, np.float64).tofile(os.path.join(d, "Ax.bin"))
+        np.asarray(np.real(Ax), np.float64).tofile(os.path.join(d, "Ax.bin"))
+        if cx:
+            np.asarray(np.imag(Ax), np.float64).tofile(os.path.join(d, "Az.bin"))
         if B is not None:
-            np.asarray(B, np.float64).reshape(n, -1).T.copy().tofile(
-                os.path.join(d, "B.bin"))
+            Bm = np.asarray(B).reshape(n, -1)
+            np.asarray(np.real(Bm), np.float64).T.copy().tofile(os.path.join(d, "B.bin"))
+            if cx:
+                np.asarray(np.imag(Bm), np.float64).T.copy().tofile(os.path.join(d, "Bz.bin"))
         if perm is not None:
             np.asarray(perm, np.int64).tofile(os.path.join(d, "UserPerm.bin"))
         subprocess.run([REF_DUMP, d, ordering, dtype, str(trials)], check=True,
@@ -66,6 +75,11 @@ def run(n, Ap, Ai, Ax, ordering="amd", dtype="d", B=None, perm=None, trials=1,
                     out["SX"][sys] = (xp, rd(f"SX{sys}i.bin", np.int64),
                                       rd(f"SX{sys}x.bin", np.float64), out["spnzmax"][sys])
         X = rd("X.bin", np.float64)
+        if cx:
+            if out["Lx"] is not None:
+                out["Lx"] = out["Lx"][0::2] + 1j * out["Lx"][1::2]
+            if X is not None:
+                X = X[0::2] + 1j * X[1::2]
         if X is not None:
             out["X"] = X.reshape(-1, n).T.copy()
         return out

@@ -15,7 +15,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libcholmod_gb300.so")
 
-CHOLMOD_PATTERN, CHOLMOD_REAL = 0, 1
+CHOLMOD_PATTERN, CHOLMOD_REAL, CHOLMOD_COMPLEX, CHOLMOD_ZOMPLEX = 0, 1, 2, 3
 CHOLMOD_DOUBLE, CHOLMOD_SINGLE = 0, 4
 CHOLMOD_OK, CHOLMOD_NOT_INSTALLED, CHOLMOD_OUT_OF_MEMORY = 0, -1, -2
 CHOLMOD_TOO_LARGE, CHOLMOD_INVALID, CHOLMOD_GPU_PROBLEM = -3, -4, -5
@@ -236,6 +236,75 @@ def sparse(n, Ap, Ai, Ax, common, stype=-1, dtype="d", ncol=None):
     return A
 
 
+def csparse(n, Ap, Ai, Ax, common, stype=-1, dtype="d", ncol=None, zomplex=False):
+    """A complex cholmod_sparse ((re, im) pairs; separate re and im arrays
+    when zomplex) from CSC arrays with complex values."""
+    ncol = n if ncol is None else ncol
+    nz = int(Ap[-1])
+    dt = CHOLMOD_SINGLE if dtype == "s" else CHOLMOD_DOUBLE
+    xt = CHOLMOD_ZOMPLEX if zomplex else CHOLMOD_COMPLEX
+    A = lib().gb300_allocate_sparse(n, ncol, nz, 1, 1, stype, xt + dt, common.ptr)
+    if not A:
+        raise RuntimeError(f"allocate_sparse failed, status {common.status}")
+    a = A.contents
+    _arr(a.p, np.int64, ncol + 1)[:] = Ap
+    _arr(a.i, np.int64, max(nz, 1))[:nz] = Ai
+    rdt = np.float32 if dtype == "s" else np.float64
+    Ax = np.asarray(Ax)
+    if zomplex:
+        _arr(a.x, rdt, max(nz, 1))[:nz] = Ax.real
+        _arr(a.z, rdt, max(nz, 1))[:nz] = Ax.imag
+    else:
+        v = _arr(a.x, rdt, 2 * max(nz, 1))
+        v[0:2 * nz:2] = Ax.real
+        v[1:2 * nz:2] = Ax.imag
+    return A
+
+
+def cdense(X, common, dtype="d"):
+    """A complex cholmod_dense ((re, im) pairs) holding X (n x k)."""
+    X = np.asarray(X)
+    if X.ndim == 1:
+        X = X[:, None]
+    n, k = X.shape
+    dt = CHOLMOD_SINGLE if dtype == "s" else CHOLMOD_DOUBLE
+    D = lib().gb300_allocate_dense(n, k, n, CHOLMOD_COMPLEX + dt, common.ptr)
+    if not D:
+        raise RuntimeError(f"allocate_dense failed, status {common.status}")
+    v = _arr(D.contents.x, np.float32 if dtype == "s" else np.float64, 2 * max(n * k, 1))
+    flat = X.T.ravel()
+    v[0:2 * n * k:2] = flat.real
+    v[1:2 * n * k:2] = flat.imag
+    return D
+
+
+def cdense_array(D):
+    d = D.contents
+    dt = np.float32 if d.dtype == CHOLMOD_SINGLE else np.float64
+    v = _arr(d.x, dt, 2 * d.d * d.ncol)
+    z = (v[0::2] + 1j * v[1::2]).reshape(d.ncol, d.d)[:, :d.nrow].T.copy()
+    return z
+
+
+def super_solve(L, X, common, forward, dtype="d"):
+    """cholmod_l_super_lsolve (forward) or _ltsolve on a copy of X (real or
+    complex, n x k); returns (ok, solution)."""
+    X = np.asarray(X)
+    cx = np.iscomplexobj(X)
+    k = 1 if X.ndim == 1 else X.shape[1]
+    D = cdense(X, common, dtype) if cx else dense(X, common, dtype)
+    dt = CHOLMOD_SINGLE if dtype == "s" else CHOLMOD_DOUBLE
+    me = max(int(L.contents.maxesize), 1)
+    E = lib().gb300_allocate_dense(me, k, me, (CHOLMOD_COMPLEX if cx else CHOLMOD_REAL) + dt,
+                                   common.ptr)
+    fn = lib().cholmod_l_super_lsolve if forward else lib().cholmod_l_super_ltsolve
+    ok = fn(L, D, E, common.ptr)
+    out = cdense_array(D) if cx else dense_array(D)
+    free_dense(D, common)
+    free_dense(E, common)
+    return ok, out
+
+
 def free_sparse(A, common):
     lib().gb300_free_sparse(C.byref(A), common.ptr)
 
@@ -290,7 +359,12 @@ def factor_arrays(L, with_x=True):
     }
     if with_x and f.x:
         dt = np.float32 if f.dtype == CHOLMOD_SINGLE else np.float64
-        out["Lx"] = _arr(f.x, dt, f.xsize).copy()
+        if f.xtype == CHOLMOD_COMPLEX:
+            v = _arr(f.x, dt, 2 * f.xsize)
+            out["Lx"] = (v[0::2] + 1j * v[1::2]).astype(np.complex64 if dt == np.float32
+                                                        else np.complex128)
+        else:
+            out["Lx"] = _arr(f.x, dt, f.xsize).copy()
     return out
 
 
@@ -303,9 +377,9 @@ def free_factor(L, common):
     lib().gb300_free_factor(C.byref(L), common.ptr)
 
 
-def super_numeric(S, L, common, beta=0.0):
-    b = (C.c_double * 2)(beta, 0.0)
-    return lib().cholmod_l_super_numeric(S, None, b, L, common.ptr)
+def super_numeric(S, L, common, beta=0.0, F=None, beta_im=0.0):
+    b = (C.c_double * 2)(beta, beta_im)
+    return lib().cholmod_l_super_numeric(S, F, b, L, common.ptr)
 
 
 def factorize(A, L, common, beta=0.0):

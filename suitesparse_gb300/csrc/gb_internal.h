@@ -69,6 +69,15 @@ cholmod_sparse *gb_aft_pattern(cholmod_sparse *A, cholmod_sparse *F, int64_t **p
 /* ---- gb_simplicial.c ----------------------------------------------------- */
 int gb_release_simplicial_shadow(const cholmod_factor *L);
 
+/* ---- gb_complex.c -------------------------------------------------------- */
+/* complex (or zomplex input) supernodal LL' and sweeps through the real
+ * embedding of the factor */
+int gb_super_numeric_complex(cholmod_sparse *A, cholmod_sparse *F, double beta[2],
+                             cholmod_factor *L, cholmod_common *Common);
+int gb_super_solve_complex(cholmod_factor *L, cholmod_dense *X, cholmod_dense *E,
+                           cholmod_common *Common, int forward);
+int gb_release_complex_shadow(const cholmod_factor *L);
+
 /* ---- kernel launchers (gb_kernels.cu) ------------------------------------ */
 /* Every launcher enqueues on `stream` and returns a cudaError_t as int. */
 

@@ -342,6 +342,58 @@ __global__ void k_pair_sum(int64_t nent, const int64_t *__restrict__ pptr,
     }
 }
 
+// A complex supernodal factor and its real embedding: each complex entry
+// l = re + i im is the 2 x 2 block [re -im; im re], so that supernode s of
+// the embedding has twice the columns and rows of the complex supernode and
+// starts at 4 px[s] (its index arrays are those of the embedding: Super_e,
+// Pi_e, Px_e).  Complex entry (i, c) of s is at px[s] + c nsrow + i (pairs
+// of reals); its block starts at row 2i of column 2c of the embedding.
+// Gather: the first column of each block (re, im), the imaginary part of a
+// diagonal entry zero, and every complex entry from zero_from on zero.
+template <typename T>
+__global__ void k_cx_gather(int64_t nsuper, const int64_t *__restrict__ Super_e,
+                            const int64_t *__restrict__ Pi_e, const int64_t *__restrict__ Px_e,
+                            const T *__restrict__ E, T *__restrict__ Lx, int64_t zero_from)
+{
+    for (int64_t s = blockIdx.x; s < nsuper; s += gridDim.x) {
+        const int64_t nscol = (Super_e[s + 1] - Super_e[s]) / 2, nsrow = (Pi_e[s + 1] - Pi_e[s]) / 2;
+        const int64_t pe = Px_e[s], pc = pe / 4, cnt = nscol * nsrow;
+        for (int64_t t = threadIdx.x; t < cnt; t += blockDim.x) {
+            const int64_t c = t / nsrow, i = t - c * nsrow, q = pc + t;
+            T re = (T)0, im = (T)0;
+            if (q < zero_from) {
+                const int64_t src = pe + 2 * c * (2 * nsrow) + 2 * i;
+                re = E[src];
+                im = i == c ? (T)0 : E[src + 1];
+            }
+            Lx[2 * q] = re;
+            Lx[2 * q + 1] = im;
+        }
+    }
+}
+
+// Scatter: the whole 2 x 2 block of every complex entry (a diagonal entry
+// taken as real, so that the embedding stays lower triangular).
+template <typename T>
+__global__ void k_cx_scatter(int64_t nsuper, const int64_t *__restrict__ Super_e,
+                             const int64_t *__restrict__ Pi_e, const int64_t *__restrict__ Px_e,
+                             const T *__restrict__ Lx, T *__restrict__ E)
+{
+    for (int64_t s = blockIdx.x; s < nsuper; s += gridDim.x) {
+        const int64_t nscol = (Super_e[s + 1] - Super_e[s]) / 2, nsrow = (Pi_e[s + 1] - Pi_e[s]) / 2;
+        const int64_t pe = Px_e[s], pc = pe / 4, cnt = nscol * nsrow, lde = 2 * nsrow;
+        for (int64_t t = threadIdx.x; t < cnt; t += blockDim.x) {
+            const int64_t c = t / nsrow, i = t - c * nsrow, q = pc + t;
+            const T re = Lx[2 * q], im = i == c ? (T)0 : Lx[2 * q + 1];
+            const int64_t b0 = pe + 2 * c * lde + 2 * i, b1 = b0 + lde;
+            E[b0] = re;
+            E[b0 + 1] = im;
+            E[b1] = -im;
+            E[b1 + 1] = re;
+        }
+    }
+}
+
 // zero factor entries [from, to) (not-positive-definite clean-up)
 template <typename T>
 __global__ void k_zero_range(T *x, int64_t from, int64_t to)
@@ -669,6 +721,35 @@ int gb_launch_pair_sum(int64_t nent, const int64_t *pptr, const int64_t *pairs, 
     else
         k_pair_sum<float><<<g, 256, 0, st>>>(nent, pptr, pairs, (const float *)Ax,
                                              (const float *)Fx, (float *)Cx);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_cx_gather(int64_t nsuper, const int64_t *Super_e, const int64_t *Pi_e,
+                        const int64_t *Px_e, const void *E, void *Lx, int64_t zero_from, int dtype,
+                        cudaStream_t st)
+{
+    if (nsuper <= 0) return 0;
+    const int g = (int)(nsuper < 65535 ? nsuper : 65535);
+    if (dtype == 0)
+        k_cx_gather<double><<<g, 256, 0, st>>>(nsuper, Super_e, Pi_e, Px_e, (const double *)E,
+                                               (double *)Lx, zero_from);
+    else
+        k_cx_gather<float><<<g, 256, 0, st>>>(nsuper, Super_e, Pi_e, Px_e, (const float *)E,
+                                              (float *)Lx, zero_from);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_cx_scatter(int64_t nsuper, const int64_t *Super_e, const int64_t *Pi_e,
+                         const int64_t *Px_e, const void *Lx, void *E, int dtype, cudaStream_t st)
+{
+    if (nsuper <= 0) return 0;
+    const int g = (int)(nsuper < 65535 ? nsuper : 65535);
+    if (dtype == 0)
+        k_cx_scatter<double><<<g, 256, 0, st>>>(nsuper, Super_e, Pi_e, Px_e, (const double *)Lx,
+                                                (double *)E);
+    else
+        k_cx_scatter<float><<<g, 256, 0, st>>>(nsuper, Super_e, Pi_e, Px_e, (const float *)Lx,
+                                               (float *)E);
     return (int)cudaGetLastError();
 }
 

@@ -187,6 +187,7 @@ static void plan_unlink(gb_plan *P)
 
 int gb_release_factor_state(cholmod_factor *L)
 {
+    gb_release_complex_shadow(L);
     pthread_mutex_lock(&plan_lock);
     gb_plan *found = NULL;
     for (gb_plan *P = plan_head; P; P = P->next)
@@ -849,23 +850,82 @@ int gb_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2],
             return FALSE;
         }
     }
-    if (A->xtype != CHOLMOD_REAL) {
-        GB_ERROR(CHOLMOD_INVALID, "complex factorization not supported on the GPU path");
-        return FALSE;
-    }
     if (A->itype != CHOLMOD_LONG || L->itype != CHOLMOD_LONG) {
         GB_ERROR(CHOLMOD_INVALID, "int64 (cholmod_l_) objects required");
         return FALSE;
     }
+    if (A->xtype != CHOLMOD_REAL) return gb_super_numeric_complex(A, F, beta, L, Common);
     Common->status = CHOLMOD_OK;
-    int dtype = A->dtype;
+    const int dtype = A->dtype;
+    gb_ctx *ctx = NULL;
+    int32_t anyfail = 0;
+    gb_plan *P = gb_numeric_core(A, F, beta ? beta[0] : 0.0, L, dtype, 0, &anyfail, &ctx, Common);
+    if (!P) return FALSE;
+    if (L->xtype == CHOLMOD_PATTERN) {
+        /* supernodal symbolic -> numeric: allocate L->x (change_factor) */
+        L->x = gb_malloc(L->xsize, dt_size(dtype), Common);
+        if (!L->x) return FALSE;
+        L->dtype = dtype;
+        L->xtype = CHOLMOD_REAL;
+    }
+    L->is_ll = TRUE;
+    L->minor = L->n;
+    if (anyfail && !gb_fix_not_posdef(P, ctx, L, dtype, Common)) return FALSE;
+    int d = dt_index(dtype);
+    P->dev_valid[d] = 1;
+    P->dev_valid[1 - d] = 0;
+    P->host_x[d] = L->x;
+    if (!ctx->opt_keep) {
+        if (cudaMemcpyAsync(L->x, P->d_Lx[d], dt_size(dtype) * L->xsize, cudaMemcpyDeviceToHost,
+                            ctx->stream) != cudaSuccess
+            || cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+            GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error copying L");
+            return FALSE;
+        }
+    } else {
+        cudaStreamSynchronize(ctx->stream);
+    }
+    return Common->status >= CHOLMOD_OK;
+}
+
+/* The device factorization behind cholmod_l_super_numeric: the input (S
+ * lower, or beta I + A F in the A F form, packed on the host when it is
+ * not), uploaded and factorized into the device factor of FL's plan in
+ * dtype.  cx_diag: in the A F form the entries (2k+1, 2k) of the product
+ * stay zero (the imaginary parts of a complex diagonal, in the real
+ * embedding of a complex matrix, which the reference's complex
+ * factorization ignores).  *anyfail: a pivot was not positive.  Returns the
+ * plan, or NULL with Common->status set; FL's host values are untouched. */
+gb_plan *gb_numeric_core(cholmod_sparse *A, cholmod_sparse *F, double beta, cholmod_factor *FL,
+                         int dtype, int cx_diag, int32_t *anyfail, gb_ctx **pctx,
+                         cholmod_common *Common)
+{
     cholmod_sparse *Apk = A;
     /* the A F form: C = tril(A F), pattern and product lists on the host,
      * values on the device after the upload (gb_aft.c) */
     int64_t *aft_ptr = NULL, *aft_pairs = NULL;
     if (A->stype == 0) {
         Apk = gb_aft_pattern(A, F, &aft_ptr, &aft_pairs, Common);
-        if (!Apk) return FALSE;
+        if (!Apk) return NULL;
+        if (cx_diag) {
+            /* drop the products of the entries (2k+1, 2k) */
+            const Int nc = (Int)Apk->ncol, *Cp = Apk->p, *Ci = Apk->i;
+            int64_t w = 0, start = 0;
+            for (Int c = 0; c < nc; c++) {
+                for (Int e = Cp[c]; e < Cp[c + 1]; e++) {
+                    const int64_t p0 = start, p1 = aft_ptr[e + 1];
+                    start = p1;
+                    aft_ptr[e] = w;
+                    if (c % 2 == 0 && Ci[e] == c + 1) continue;
+                    for (int64_t q = p0; q < p1; q++) {
+                        aft_pairs[2 * w] = aft_pairs[2 * q];
+                        aft_pairs[2 * w + 1] = aft_pairs[2 * q + 1];
+                        w++;
+                    }
+                }
+            }
+            aft_ptr[Cp[nc]] = w;
+        }
     } else if (!A->packed) {
         /* pack the columns (unpacked input) on the host */
         Int n = (Int)A->ncol, nz = 0;
@@ -873,7 +933,7 @@ int gb_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2],
         for (Int j = 0; j < n; j++) nz += Anz[j];
         Apk = gb300_allocate_sparse(A->nrow, n, nz, A->sorted, TRUE, A->stype,
                                     CHOLMOD_REAL + dtype, Common);
-        if (!Apk) return FALSE;
+        if (!Apk) return NULL;
         Int *Bp = Apk->p, *Bi = Apk->i;
         size_t e = dt_size(dtype);
         Int q = 0;
@@ -885,25 +945,19 @@ int gb_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2],
         }
         Bp[n] = q;
     }
-
+    gb_plan *P = NULL;
     gb_ctx *ctx = gb_ctx_get(Common, 1);
     if (!ctx || !gb_ctx_ready(ctx)) {
-        if (Apk != A) gb300_free_sparse(&Apk, Common);
         GB_ERROR(CHOLMOD_GPU_PROBLEM, "no CUDA device");
-        return FALSE;
+        goto done;
     }
-    int symbolic = (L->xtype == CHOLMOD_PATTERN);
-    gb_plan *P = gb_plan_get(L, Common, ctx, 1);
-    if (!P) {
-        if (Apk != A) gb300_free_sparse(&Apk, Common);
-        free(aft_ptr); free(aft_pairs);
-        return FALSE;
-    }
+    *pctx = ctx;
+    P = gb_plan_get(FL, Common, ctx, 1);
+    if (!P) goto done;
     if (!gb_ensure_numeric(P, dtype) || !gb_upload_input(P, ctx, Apk, dtype)) {
-        if (Apk != A) gb300_free_sparse(&Apk, Common);
-        free(aft_ptr); free(aft_pairs);
         GB_ERROR(CHOLMOD_GPU_PROBLEM, "device allocation failed");
-        return FALSE;
+        P = NULL;
+        goto done;
     }
     if (aft_ptr) {
         /* values of C = tril(A F): each entry's products summed on the device */
@@ -928,64 +982,36 @@ int gb_super_numeric(cholmod_sparse *A, cholmod_sparse *F, double beta[2],
         if (dF) cudaFree(dF);
         if (dptr) cudaFree(dptr);
         if (dpairs) cudaFree(dpairs);
-        free(aft_ptr);
-        free(aft_pairs);
-        aft_ptr = aft_pairs = NULL;
         if (!okp) {
-            gb300_free_sparse(&Apk, Common);
             cudaGetLastError();
             GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error forming A*F'");
-            return FALSE;
+            P = NULL;
+            goto done;
         }
     }
-    if (symbolic) {
-        /* supernodal symbolic -> numeric: allocate L->x (change_factor) */
-        L->dtype = dtype;
-        L->x = gb_malloc(L->xsize, dt_size(dtype), Common);
-        if (!L->x) { if (Apk != A) gb300_free_sparse(&Apk, Common); return FALSE; }
-        memset(L->x, 0, GB_MIN(2 * sizeof(double), L->xsize * dt_size(dtype)));
-        L->xtype = CHOLMOD_REAL;
-    }
-    L->is_ll = TRUE;
-
-    int ok = TRUE;
-    cudaEventRecord(ctx->ev0, ctx->stream);
-    ok = gb_run_factor(P, ctx, P->d_Sx, dtype, dtype, NULL, beta ? beta[0] : 0.0);
-    cudaEventRecord(ctx->ev1, ctx->stream);
-    int32_t anyfail = 0, dagerr = 0;
-    if (ok) ok = cudaMemcpyAsync(&anyfail, P->d_anyfail, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess
-                 && cudaMemcpyAsync(&dagerr, P->d_ticket + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess
-                 && cudaStreamSynchronize(ctx->stream) == cudaSuccess && !dagerr;
-    if (!ok) {
-        if (Apk != A) gb300_free_sparse(&Apk, Common);
-        GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the factorization");
-        return FALSE;
-    }
-    float ms = 0;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-    ctx->stats[0] = ms;
-    L->minor = L->n;
-    if (anyfail && !gb_fix_not_posdef(P, ctx, L, dtype, Common)) {
-        if (Apk != A) gb300_free_sparse(&Apk, Common);
-        return FALSE;
-    }
-    int d = dt_index(dtype);
-    P->dev_valid[d] = 1;
-    P->dev_valid[1 - d] = 0;
-    P->host_x[d] = L->x;
-    if (!ctx->opt_keep) {
-        if (cudaMemcpyAsync(L->x, P->d_Lx[d], dt_size(dtype) * L->xsize, cudaMemcpyDeviceToHost,
-                            ctx->stream) != cudaSuccess
-            || cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
-            if (Apk != A) gb300_free_sparse(&Apk, Common);
-            GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error copying L");
-            return FALSE;
+    {
+        cudaEventRecord(ctx->ev0, ctx->stream);
+        int ok = gb_run_factor(P, ctx, P->d_Sx, dtype, dtype, NULL, beta);
+        cudaEventRecord(ctx->ev1, ctx->stream);
+        int32_t dagerr = 0;
+        *anyfail = 0;
+        if (ok) ok = cudaMemcpyAsync(anyfail, P->d_anyfail, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess
+                     && cudaMemcpyAsync(&dagerr, P->d_ticket + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess
+                     && cudaStreamSynchronize(ctx->stream) == cudaSuccess && !dagerr;
+        if (!ok) {
+            GB_ERROR(CHOLMOD_GPU_PROBLEM, "CUDA error in the factorization");
+            P = NULL;
+            goto done;
         }
-    } else {
-        cudaStreamSynchronize(ctx->stream);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        ctx->stats[0] = ms;
     }
+done:
     if (Apk != A) gb300_free_sparse(&Apk, Common);
-    return Common->status >= CHOLMOD_OK;
+    free(aft_ptr);
+    free(aft_pairs);
+    return P;
 }
 
 /* Factorize S (lower, in FS's column order, dtype; beta added to the
@@ -1062,6 +1088,7 @@ static int super_solve(cholmod_factor *L, cholmod_dense *X, cholmod_dense *E,
 {
     if (!Common) return FALSE;
     if (!L || !X || !E) { GB_ERROR(CHOLMOD_INVALID, "argument missing"); return FALSE; }
+    if (L->xtype == CHOLMOD_COMPLEX) return gb_super_solve_complex(L, X, E, Common, forward);
     if (L->xtype != CHOLMOD_REAL || X->xtype != CHOLMOD_REAL || E->xtype != CHOLMOD_REAL) {
         GB_ERROR(CHOLMOD_INVALID, "real factor and matrices required");
         return FALSE;

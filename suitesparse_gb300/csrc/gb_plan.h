@@ -420,6 +420,14 @@ int gb_launch_pair_sum(int64_t nent, const int64_t *pptr, const int64_t *pairs, 
 int gb_launch_simplicial_gather(int64_t n, const int64_t *src, const int64_t *dst,
                                 const int64_t *len, int64_t minor, int ldl, const void *Fx,
                                 void *Lx, int dtype, cudaStream_t st);
+int gb_launch_cx_gather(int64_t nsuper, const int64_t *Super_e, const int64_t *Pi_e,
+                        const int64_t *Px_e, const void *E, void *Lx, int64_t zero_from, int dtype,
+                        cudaStream_t st);
+int gb_launch_cx_scatter(int64_t nsuper, const int64_t *Super_e, const int64_t *Pi_e,
+                         const int64_t *Px_e, const void *Lx, void *E, int dtype, cudaStream_t st);
+gb_plan *gb_numeric_core(cholmod_sparse *A, cholmod_sparse *F, double beta, cholmod_factor *FL,
+                         int dtype, int cx_diag, int32_t *anyfail, gb_ctx **pctx,
+                         cholmod_common *Common);
 
 #ifdef __cplusplus
 }

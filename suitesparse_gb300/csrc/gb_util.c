@@ -206,10 +206,6 @@ cholmod_sparse *gb300_allocate_sparse(size_t nrow, size_t ncol, size_t nzmax,
     if (!Common) return NULL;
     Common->status = CHOLMOD_OK;
     int xtype = xdtype & 3;
-    if (xtype != CHOLMOD_REAL && xtype != CHOLMOD_PATTERN) {
-        GB_ERROR(CHOLMOD_INVALID, "only real or pattern sparse matrices");
-        return NULL;
-    }
     cholmod_sparse *A = gb_calloc(1, sizeof(cholmod_sparse), Common);
     if (!A) return NULL;
     A->nrow = nrow;
@@ -224,8 +220,12 @@ cholmod_sparse *gb300_allocate_sparse(size_t nrow, size_t ncol, size_t nzmax,
     A->p = gb_calloc(ncol + 1, sizeof(Int), Common);
     A->i = gb_malloc(A->nzmax, sizeof(Int), Common);
     if (!packed) A->nz = gb_calloc(ncol, sizeof(Int), Common);
-    if (xtype == CHOLMOD_REAL) A->x = gb_malloc(A->nzmax, xsize_of(xdtype), Common);
-    if (!A->p || !A->i || (!packed && !A->nz) || (xtype == CHOLMOD_REAL && !A->x)) {
+    /* complex: (re, im) pairs in x; zomplex: re in x, im in z */
+    if (xtype != CHOLMOD_PATTERN)
+        A->x = gb_malloc(A->nzmax, xsize_of(xdtype) * (xtype == CHOLMOD_COMPLEX ? 2 : 1), Common);
+    if (xtype == CHOLMOD_ZOMPLEX) A->z = gb_malloc(A->nzmax, xsize_of(xdtype), Common);
+    if (!A->p || !A->i || (!packed && !A->nz) || (xtype != CHOLMOD_PATTERN && !A->x)
+        || (xtype == CHOLMOD_ZOMPLEX && !A->z)) {
         gb300_free_sparse(&A, Common);
         return NULL;
     }
@@ -240,7 +240,7 @@ int gb300_free_sparse(cholmod_sparse **Ah, cholmod_common *Common)
     gb_free(A->ncol + 1, sizeof(Int), A->p, Common);
     gb_free(A->nzmax, sizeof(Int), A->i, Common);
     gb_free(A->ncol, sizeof(Int), A->nz, Common);
-    gb_free(A->nzmax, e * (A->xtype == CHOLMOD_REAL ? 1 : 2), A->x, Common);
+    gb_free(A->nzmax, e * (A->xtype == CHOLMOD_COMPLEX ? 2 : 1), A->x, Common);
     gb_free(A->nzmax, e, A->z, Common);
     gb_free(1, sizeof(cholmod_sparse), A, Common);
     *Ah = NULL;
@@ -252,8 +252,9 @@ cholmod_dense *gb300_allocate_dense(size_t nrow, size_t ncol, size_t d,
 {
     if (!Common) return NULL;
     Common->status = CHOLMOD_OK;
-    if ((xdtype & 3) != CHOLMOD_REAL) {
-        GB_ERROR(CHOLMOD_INVALID, "only real dense matrices");
+    const int xtype = xdtype & 3;
+    if (xtype == CHOLMOD_PATTERN) {
+        GB_ERROR(CHOLMOD_INVALID, "a dense matrix has values");
         return NULL;
     }
     if (d < nrow) d = nrow;
@@ -263,10 +264,11 @@ cholmod_dense *gb300_allocate_dense(size_t nrow, size_t ncol, size_t d,
     X->ncol = ncol;
     X->d = d;
     X->nzmax = GB_MAX(d * ncol, 1);
-    X->xtype = CHOLMOD_REAL;
+    X->xtype = xtype;
     X->dtype = xdtype & 4;
-    X->x = gb_calloc(X->nzmax, xsize_of(xdtype), Common);
-    if (!X->x) { gb300_free_dense(&X, Common); return NULL; }
+    X->x = gb_calloc(X->nzmax, xsize_of(xdtype) * (xtype == CHOLMOD_COMPLEX ? 2 : 1), Common);
+    if (xtype == CHOLMOD_ZOMPLEX) X->z = gb_calloc(X->nzmax, xsize_of(xdtype), Common);
+    if (!X->x || (xtype == CHOLMOD_ZOMPLEX && !X->z)) { gb300_free_dense(&X, Common); return NULL; }
     return X;
 }
 
@@ -275,7 +277,8 @@ int gb300_free_dense(cholmod_dense **Xh, cholmod_common *Common)
     if (!Xh || !*Xh) return TRUE;
     cholmod_dense *X = *Xh;
     size_t e = X->dtype == CHOLMOD_SINGLE ? sizeof(float) : sizeof(double);
-    gb_free(X->nzmax, e, X->x, Common);
+    gb_free(X->nzmax, e * (X->xtype == CHOLMOD_COMPLEX ? 2 : 1), X->x, Common);
+    gb_free(X->nzmax, e, X->z, Common);
     gb_free(1, sizeof(cholmod_dense), X, Common);
     *Xh = NULL;
     return TRUE;

@@ -166,6 +166,29 @@ def laplace3d(nx, ny=None, nz=None, seed=None, lo=1e-2, hi=1e2, shift=0.0):
     return _grid_laplacian(dims, coef, shift)
 
 
+def magnetic_laplacian(dims, seed=11, lo=1e-1, hi=1e1, shift=1e-2, diag_imag=0.0):
+    """Hermitian positive definite test matrix: the graph Laplacian of a box
+    grid (5- or 7-point, Dirichlet, log-uniform conductivities) whose
+    off-diagonal entries carry unit phases -- the discrete magnetic
+    Laplacian -- plus shift on the diagonal.  A phase is the unit complex
+    number ((1 - t^2) + 2 t i) / (1 + t^2), t uniform in [-1, 1), so that
+    only correctly rounded arithmetic is used and the values are the same on
+    every platform.  diag_imag puts that imaginary part on every diagonal
+    entry (the factorization ignores it).  Returns (n, Ap, Ai, Ax) of the
+    lower triangle with complex Ax."""
+    dims = tuple(int(v) for v in dims)
+    n, Ap, Ai, Ax = _grid_laplacian(dims, _edge_coefs(dims, seed, lo, hi), shift)
+    col = np.repeat(np.arange(n, dtype=np.int64), np.diff(Ap))
+    off = Ai != col
+    t = 2.0 * uniform01(seed + 101, int(off.sum())) - 1.0
+    den = 1.0 + t * t
+    z = np.ones(len(Ax), dtype=np.complex128)
+    z[off] = (1.0 - t * t) / den + 1j * (2.0 * t / den)
+    Axc = Ax * z
+    Axc[~off] += 1j * diag_imag
+    return n, Ap, Ai, Axc
+
+
 def _rotations(u):
     """Rotation matrices from unit quaternions built from 4 uniforms each."""
     q = 2.0 * u.reshape(-1, 4) - 1.0
