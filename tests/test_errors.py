@@ -38,11 +38,13 @@ def test_super_numeric_rejects_bad_inputs(lib):
     assert lib.cholmod_l_super_numeric(A, None, beta, L, c.ptr) == 0
     assert c.status == CH.CHOLMOD_INVALID
     A.contents.nrow = n
-    # complex values are not supported on the GPU path
-    A.contents.xtype = 2
+    # complex A with a real numeric L: the reference's complex type mismatch
+    A.contents.xtype = CH.CHOLMOD_COMPLEX
+    L.contents.xtype = CH.CHOLMOD_REAL
     assert lib.cholmod_l_super_numeric(A, None, beta, L, c.ptr) == 0
     assert c.status == CH.CHOLMOD_INVALID
-    A.contents.xtype = 1
+    A.contents.xtype = CH.CHOLMOD_REAL
+    L.contents.xtype = CH.CHOLMOD_PATTERN
     # numeric L of another dtype
     L.contents.xtype = CH.CHOLMOD_REAL
     L.contents.dtype = CH.CHOLMOD_SINGLE
