@@ -250,3 +250,42 @@ def test_a_times_f_form(lib, oracle_mod):
     CH.free_sparse(F, c)
     CH.free_factor(L, c)
     c.finish()
+
+
+@pytest.mark.gpu
+def test_int32_entry_points_take_complex_factors(cgold, lib):
+    """cholmod_super_numeric / cholmod_super_lsolve on int32 copies of a
+    complex problem give the int64 path's factor and solution bit for bit."""
+    import ctypes as C
+    from test_gpu_int32 import CHOLMOD_INT, Int32Objects
+    meta, arrays = cgold
+    n, Ap, Ai, Ax = _case(meta, "cx2")
+    perm = arrays["cx2_Perm"]
+    c = CH.Common()
+    A = CH.sparse(n, Ap, Ai, np.abs(Ax), c)
+    L = CH.analyze_perm(A, perm, c)
+    CH.free_sparse(A, c)
+    S = CH.csparse(*_permuted_lower(n, Ap, Ai, Ax, perm), c)
+    o32 = Int32Objects(S, L)
+    assert CH.super_numeric(S, L, c) == 1
+    Lx64 = CH.factor_arrays(L)["Lx"]
+    B = _rhs(meta, "cx2", n)[perm]
+    _, Y64 = CH.super_solve(L, B, c, True)
+    c32 = CH.Common()
+    c32["itype"] = CHOLMOD_INT
+    L32, A32 = C.pointer(o32.L), C.pointer(o32.A)
+    beta = (C.c_double * 2)(0.0, 0.0)
+    assert lib.cholmod_super_numeric(A32, None, beta, L32, c32.ptr) == 1, c32.status
+    assert o32.L.xtype == CH.CHOLMOD_COMPLEX and o32.L.minor == n
+    v = np.ctypeslib.as_array(C.cast(o32.L.x, C.POINTER(C.c_double)), shape=(2 * o32.L.xsize,))
+    assert np.array_equal(v[0::2] + 1j * v[1::2], Lx64)
+    X = CH.cdense(B, c32)
+    me = max(int(o32.L.maxesize), 1)
+    E = lib.gb300_allocate_dense(me, B.shape[1], me, CH.CHOLMOD_COMPLEX + CH.CHOLMOD_DOUBLE, c32.ptr)
+    assert lib.cholmod_super_lsolve(L32, X, E, c32.ptr) == 1
+    assert np.array_equal(CH.cdense_array(X), Y64)
+    CH.free_dense(X, c32)
+    CH.free_dense(E, c32)
+    lib.gb300_release_factor(L32, c32.ptr)
+    CH.free_sparse(S, c)
+    CH.free_factor(L, c)
