@@ -586,14 +586,15 @@ int gb300_solve_refined2 (cholmod_sparse *A, cholmod_factor *L, cholmod_dense *B
  * that rewrites L's pattern arrays in place calls this first. */
 int gb300_release_factor (cholmod_factor *L, cholmod_common *Common) ;
 /* Device bytes held by L's device state on Common's device (0 when it has
- * none): plan structures, factors, update blocks, inverses, operand images,
- * value maps and work buffers. */
+ * none): plan structures, factors, diagonal-block inverses, value maps and
+ * work buffers.  The update blocks and tensor-core operand images of a
+ * factorization are scratch of the Common, grown to the largest pattern it
+ * factorized and shared by all its factors; gb300_finish frees them. */
 int64_t gb300_factor_device_bytes (cholmod_factor *L, cholmod_common *Common) ;
-/* Frees what only a factorization uses, keeping what the solves use: the
- * update blocks, the tensor-core operand images and, after
- * gb300_factorize_mixed, the factor of the precision the refined solves do
- * not read (the FP64 one when the FP32 factor is used, else the FP32 one).
- * The next factorization allocates them again.  Returns the bytes freed. */
+/* After gb300_factorize_mixed: frees the factor of the precision the
+ * refined solves do not read (the FP64 one when the FP32 factor is used,
+ * else the FP32 one); a later factorization allocates it again.  Returns
+ * the bytes freed. */
 int64_t gb300_trim_factor (cholmod_factor *L, cholmod_common *Common) ;
 
 /* Object helpers for programs without the reference library.  Memory comes
@@ -687,7 +688,8 @@ cholmod_factor *gb300_batch_analyze (int npat, cholmod_factor *const *Lpat,
  * request is admitted when its device-memory estimate (from nnz(L)) fits
  * under budget_bytes, evicting idle factors least recently used first;
  * after each factorization a factor keeps only what its solves use
- * (gb300_trim_factor) and is charged its measured device bytes
+ * (gb300_trim_factor; update blocks and operand images are per-worker
+ * scratch) and is charged its measured device bytes
  * (gb300_factor_device_bytes), also after each refined solve; an evicted
  * factor keeps the copy of its A on the host (up to 32 GB of evicted A's,
  * the oldest dropped first), so that a later solve against it factorizes

@@ -261,19 +261,23 @@ __device__ __forceinline__ void warp_inv32(const T (*A)[65], int o, T rinv, int 
 // LL' and inverse of a 64 x 64 (nb <= 64) lower block in shared memory with
 // 256 threads, in 2 x 2 blocks of 32: A = [A11; A21 A22] (leading dimension
 // 65) is overwritten by L; X receives L^-1 (X[c*65 + r] = Linv(r, c), zeros
-// above the diagonal); Tm is scratch of 32 x 33 entries.
-//   L11 = chol(A11), X11 = L11^-1     (one warp, registers and broadcasts)
-//   L21 = A21 X11'                    (all threads)
-//   S = A22 - L21 L21', L22 = chol(S), X22 = L22^-1   (all, then one warp)
-//   X21 = -X22 (L21 X11)              (all threads, two products)
-// Returns the first column whose pivot is not positive, or -1; on failure
-// the columns before it (of L, its rows below included, and of the
-// inverse) are final.
+// above the diagonal); Tm is scratch of 32 x 33 + 32 entries.
+//   L11 = chol(A11)                          (warp 0, registers)
+//   X11 = L11^-1                             (warp 1, meanwhile:)
+//   L21 = A21 L11^-T by substitution         (warp 2)
+//   S = A22 - L21 L21', L22 = chol(S), X22 = L22^-1   (warps 0, 2-7; warp 0)
+//   X21 = -X22 (L21 X11)                     (all threads, two products)
+// The inverse of the first diagonal block is off the dependency chain: the
+// warps that form L21, S and L22 synchronize on a named barrier of their
+// own (224 threads) while warp 1 inverts.  Returns the first column whose
+// pivot is not positive, or -1; on failure the columns before it (of L,
+// its rows below included, and of the inverse) are final.
 template <typename T>
 __device__ int potrf_inv64(T (*A)[65], T *X, T *Tm, int nb, int *sfail)
 {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n1 = min(32, nb), n2 = nb - n1;
+    T *rinv11 = Tm + 32 * 33;                   // 1 / L11(c, c)
     for (int idx = tid; idx < 64 * 65; idx += blockDim.x) X[idx] = (T)0;
     if (tid == 0) *sfail = -1;
     __syncthreads();
@@ -287,60 +291,67 @@ __device__ int potrf_inv64(T (*A)[65], T *X, T *Tm, int nb, int *sfail)
             for (int k = 0; k < 32; k++)
                 if (k <= lane) A[lane][k] = row[k];
         }
-        __syncwarp();
-        warp_inv32<T>(A, 0, rinv, bad >= 0 ? bad : n1, X);
+        rinv11[lane] = rinv;
         if (lane == 0 && bad >= 0) *sfail = bad;
     }
     __syncthreads();
     const int f1 = *sfail, v1 = f1 >= 0 ? f1 : n1;
-    if (n2 <= 0) return f1;
-    // L21(i, c) = sum_k A21(i, k) X11(c, k), columns c < v1 (X11 is zero
-    // above its diagonal, so all 32 terms are summed)
-    for (int o = tid; o < n2 * 32; o += blockDim.x) {
-        const int i = o >> 5, c = o & 31;
-        T a0 = (T)0, a1 = (T)0;
+    if (warp == 1) {
+        warp_inv32<T>(A, 0, rinv11[lane], v1, X);
+    } else if (n2 > 0) {
+        // warps 0 and 2-7 (224 threads, named barrier 1)
+        const int t7 = warp == 0 ? lane : tid - 32;
+        if (warp == 2 && lane < n2) {
+            // row 32 + lane of L21: L11 L21(i, :)' = A21(i, :)', columns < v1
+            T a[32];
 #pragma unroll
-        for (int k = 0; k < 32; k += 2) {
-            a0 += A[32 + i][k] * X[k * 65 + c];
-            a1 += A[32 + i][k + 1] * X[(k + 1) * 65 + c];
-        }
-        Tm[i * 33 + c] = c < v1 ? a0 + a1 : (T)0;
-    }
-    __syncthreads();
-    for (int o = tid; o < n2 * 32; o += blockDim.x) {
-        const int i = o >> 5, c = o & 31;
-        if (c < v1) A[32 + i][c] = Tm[i * 33 + c];
-    }
-    __syncthreads();
-    if (f1 >= 0) return f1;
-    // S = A22 - L21 L21' (lower)
-    for (int o = tid; o < n2 * n2; o += blockDim.x) {
-        const int i = o / n2, j = o - i * n2;
-        if (j > i) continue;
-        T a0 = (T)0, a1 = (T)0;
+            for (int k = 0; k < 32; k++) a[k] = A[32 + lane][k];
 #pragma unroll
-        for (int k = 0; k < 32; k += 2) {
-            a0 += A[32 + i][k] * A[32 + j][k];
-            a1 += A[32 + i][k + 1] * A[32 + j][k + 1];
-        }
-        A[32 + i][32 + j] -= a0 + a1;
-    }
-    __syncthreads();
-    if (warp == 0) {
-        T row[32], rinv;
+            for (int c = 0; c < 32; c++) {
+                if (c < v1) {
+                    const T x = a[c] * rinv11[c];
+                    a[c] = x;
 #pragma unroll
-        for (int k = 0; k < 32; k++) row[k] = (lane < n2 && k <= lane) ? A[32 + lane][32 + k] : (T)0;
-        const int bad = warp_chol32<T>(row, rinv, n2);
-        if (lane < n2) {
+                    for (int k = c + 1; k < 32; k++) a[k] -= x * A[k][c];
+                }
+            }
 #pragma unroll
             for (int k = 0; k < 32; k++)
-                if (k <= lane) A[32 + lane][32 + k] = row[k];
+                if (k < v1) A[32 + lane][k] = a[k];
         }
-        __syncwarp();
-        warp_inv32<T>(A, 32, rinv, bad >= 0 ? bad : n2, X);
-        if (lane == 0 && bad >= 0) *sfail = 32 + bad;
+        asm volatile("bar.sync 1, 224;" ::: "memory");
+        if (f1 < 0) {
+            // S = A22 - L21 L21' (lower)
+            for (int o = t7; o < n2 * n2; o += 224) {
+                const int i = o / n2, j = o - i * n2;
+                if (j > i) continue;
+                T a0 = (T)0, a1 = (T)0;
+#pragma unroll
+                for (int k = 0; k < 32; k += 2) {
+                    a0 += A[32 + i][k] * A[32 + j][k];
+                    a1 += A[32 + i][k + 1] * A[32 + j][k + 1];
+                }
+                A[32 + i][32 + j] -= a0 + a1;
+            }
+            asm volatile("bar.sync 1, 224;" ::: "memory");
+            if (warp == 0) {
+                T row[32], rinv;
+#pragma unroll
+                for (int k = 0; k < 32; k++) row[k] = (lane < n2 && k <= lane) ? A[32 + lane][32 + k] : (T)0;
+                const int bad = warp_chol32<T>(row, rinv, n2);
+                if (lane < n2) {
+#pragma unroll
+                    for (int k = 0; k < 32; k++)
+                        if (k <= lane) A[32 + lane][32 + k] = row[k];
+                }
+                __syncwarp();
+                warp_inv32<T>(A, 32, rinv, bad >= 0 ? bad : n2, X);
+                if (lane == 0 && bad >= 0) *sfail = 32 + bad;
+            }
+        }
     }
     __syncthreads();
+    if (f1 >= 0 || n2 <= 0) return f1;
     // T = L21 X11: T(i, c) = sum_k L21(i, k) X11(k, c) (X11 zero above its
     // diagonal; rows i >= n2 of T zero)
     for (int o = tid; o < 32 * 32; o += blockDim.x) {

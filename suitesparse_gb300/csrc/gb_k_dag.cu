@@ -602,11 +602,14 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
             }
         }
         __syncthreads();
-        if (threadIdx.x < 32) {
+        {
+            // every thread releases successors (a diagonal step's task has
+            // up to ~100: one round of counter atomics instead of several
+            // on one warp, which the dependency chain would wait for)
             if (D.trace && threadIdx.x == 0) D.trace[3 * (size_t)id + 1] = dag_timer();
-            __threadfence();
             const int e0 = PP.succ_ptr[local], e1 = PP.succ_ptr[local + 1];
-            for (int e = e0 + (int)threadIdx.x; e < e1; e += 32) {
+            if (e0 + (int)threadIdx.x < e1) __threadfence();
+            for (int e = e0 + (int)threadIdx.x; e < e1; e += (int)blockDim.x) {
                 const int v = PP.succ[e];
                 const int g = (int)(I.base + v);
                 if (dag_add_acq_rel(D.cnt + g, -1) != 1) continue;
@@ -633,7 +636,7 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                     dag_push(D.Q, gw, pw);
                 }
             }
-            __syncwarp();      // snext, set by any lane, is read by thread 0
+            __syncthreads();   // snext, set by any thread, is read by thread 0
         }
     }
     if (TC && tc) {

@@ -49,6 +49,9 @@ void gb_ctx_delete(gb_ctx *c)
         if (c->ev_join[i]) cudaEventDestroy(c->ev_join[i]);
     }
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    for (int d = 0; d < 2; d++)
+        if (c->d_cbs[d]) cudaFree(c->d_cbs[d]);
+    if (c->d_imgs) cudaFree(c->d_imgs);
     if (c->d_trace) cudaFree(c->d_trace);
     if (c->d_ftrace) cudaFree(c->d_ftrace);
     free(c->pev);
@@ -273,17 +276,13 @@ int gb_dev_grow(void **p, size_t *cap, size_t bytes)
 static int dt_index(int dtype) { return dtype == CHOLMOD_SINGLE ? 1 : 0; }
 static size_t dt_size(int dtype) { return dtype == CHOLMOD_SINGLE ? sizeof(float) : sizeof(double); }
 
-/* device factor and update-block buffers of one precision */
+/* the device factor of one precision */
 int gb_ensure_numeric(gb_plan *P, int dtype)
 {
     int d = dt_index(dtype);
     size_t e = dt_size(dtype);
     if (!P->d_Lx[d] && cudaMalloc(&P->d_Lx[d], e * GB_MAX(P->xsize, 1)) != cudaSuccess) {
         P->d_Lx[d] = NULL;
-        return FALSE;
-    }
-    if (!P->d_CB[d] && cudaMalloc(&P->d_CB[d], e * GB_MAX(P->cb_total, 1)) != cudaSuccess) {
-        P->d_CB[d] = NULL;
         return FALSE;
     }
     return TRUE;
@@ -297,10 +296,8 @@ size_t gb_plan_device_bytes(const gb_plan *P)
     for (int d = 0; d < 2; d++) {
         const size_t e = d ? sizeof(float) : sizeof(double);
         if (P->d_Lx[d]) b += e * (size_t)GB_MAX(P->xsize, 1);
-        if (P->d_CB[d]) b += e * (size_t)GB_MAX(P->cb_total, 1);
         if (P->d_Linv[d]) b += e * (size_t)GB_MAX(P->linv_total, 1);
     }
-    if (P->d_img) b += sizeof(float) * GB_IMG_FLOATS_HOST * (size_t)P->img_total;
     b += P->sx_cap + P->si_cap + P->sp_cap + P->y_cap + P->u_cap + P->b_cap + P->spw_cap
          + P->sws_cap + P->ax_cap + P->rp_cap + P->rj_cap + P->rx_cap + P->x_cap + P->r_cap
          + P->bx_cap + P->bred_cap;
@@ -328,17 +325,11 @@ int64_t gb300_trim_factor(cholmod_factor *L, cholmod_common *Common)
         return -1;
     }
     const size_t before = gb_plan_device_bytes(P);
-    /* a captured refinement step names these buffers: capture again */
-    gb_graph_free(P);
-    for (int d = 0; d < 2; d++) {
-        if (P->d_CB[d]) cudaFree(P->d_CB[d]);
-        P->d_CB[d] = NULL;
-    }
-    if (P->d_img) cudaFree(P->d_img);
-    P->d_img = NULL;
     /* the precision the refined solves do not use */
     const int unused = P->mixed == 1 ? 0 : (P->mixed == 2 ? 1 : -1);
-    if (unused >= 0) {
+    if (unused >= 0 && (P->d_Lx[unused] || P->d_Linv[unused])) {
+        /* a captured refinement step may name these buffers: capture again */
+        gb_graph_free(P);
         if (P->d_Lx[unused]) cudaFree(P->d_Lx[unused]);
         if (P->d_Linv[unused]) cudaFree(P->d_Linv[unused]);
         P->d_Lx[unused] = P->d_Linv[unused] = NULL;
@@ -360,7 +351,9 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
     int d = dt_index(l_dtype);
     int ldt = l_dtype == CHOLMOD_SINGLE ? 4 : 0;
     int adt = a_dtype == CHOLMOD_SINGLE ? 4 : 0;
-    void *Lx = P->d_Lx[d], *CB = P->d_CB[d];
+    if (!gb_dev_grow(&ctx->d_cbs[d], &ctx->cbs_cap[d], dt_size(l_dtype) * GB_MAX(P->cb_total, 1)))
+        return FALSE;
+    void *Lx = P->d_Lx[d], *CB = ctx->d_cbs[d];
     const gb_launch_rec *seq = P->fact_seq.p;
     int launches = 0;
     if (!P->d_Linv[d] && cudaMalloc(&P->d_Linv[d], dt_size(l_dtype) * GB_MAX(P->linv_total, 1))
@@ -424,15 +417,13 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
         a.scale = scale;
         a.beta = beta;
         a.use_tc = ctx->tc_mode && l_dtype == CHOLMOD_SINGLE && P->img_total > 0;
-        if (a.use_tc && !P->d_img
-            && cudaMalloc((void **)&P->d_img, sizeof(float) * GB_IMG_FLOATS_HOST * (size_t)P->img_total)
-                   != cudaSuccess) {
+        if (a.use_tc && !gb_dev_grow(&ctx->d_imgs, &ctx->imgs_cap,
+                                     sizeof(float) * GB_IMG_FLOATS_HOST * (size_t)P->img_total)) {
             /* no room for the operand images: the CUDA cores take the tiles */
-            P->d_img = NULL;
             cudaGetLastError();
             a.use_tc = 0;
         }
-        a.img = a.use_tc ? P->d_img : NULL;
+        a.img = a.use_tc ? (float *)ctx->d_imgs : NULL;
         if (ctx->trace_on) {
             size_t need = 3 * (N + 1) * sizeof(unsigned long long);
             if (gb_dev_grow((void **)&ctx->d_ftrace, &ctx->ftrace_cap, need)) {

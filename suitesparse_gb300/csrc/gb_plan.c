@@ -1368,8 +1368,8 @@ void gb_plan_free(gb_plan *P)
     void *dev[] = {P->d_Super, P->d_Pi, P->d_Px, P->d_cboff, P->d_cbvoff, P->d_Perm,
                    P->d_Ls, P->d_relmap, P->d_child_ptr, P->d_child_list, P->d_fail,
                    P->d_anyfail, P->d_asm, P->d_node, P->d_potrf, P->d_trsm, P->d_gemm,
-                   P->d_gemm_owner, P->d_sweep, P->d_Lx[0], P->d_Lx[1], P->d_CB[0],
-                   P->d_CB[1], P->d_Sp, P->d_Si, P->d_Sx, P->d_Y, P->d_U, P->d_B, P->d_spw, P->d_sws,
+                   P->d_gemm_owner, P->d_sweep, P->d_Lx[0], P->d_Lx[1],
+                   P->d_Sp, P->d_Si, P->d_Sx, P->d_Y, P->d_U, P->d_B, P->d_spw, P->d_sws,
                    P->d_Rp, P->d_Rj, P->d_Rx, P->d_scale, P->d_scale_perm, P->d_X, P->d_R,
                    P->d_bx, P->d_red, P->d_sf, P->d_sb, P->d_sd, P->d_lf, P->d_sf_cptr, P->d_sf_crange, P->d_blkoff, P->d_ntask_f,
                    P->d_ntask_b, P->d_parent, P->d_linvoff, P->d_xready, P->d_done,
@@ -1378,7 +1378,7 @@ void gb_plan_free(gb_plan *P)
                    P->d_dag_cnt, P->d_dag_q, P->d_dag_ctrl, P->d_dag_smf, P->d_fd_t,
                    P->d_fd_sp, P->d_fd_succ, P->d_fd_nd, P->d_fd_qi, P->d_fd_ctrl0,
                    P->d_fd_cnt, P->d_fd_q, P->d_fd_pat, P->d_fd_inst, P->d_fd_ibase, P->d_fd_sub,
-                   P->d_fd_smeta, P->d_imgbase, P->d_img,
+                   P->d_fd_smeta, P->d_imgbase,
                    P->d_chunk, P->d_anorm_seg, P->d_bred, P->d_gf, P->d_gb};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++)
         if (dev[i]) cudaFree(dev[i]);

@@ -203,10 +203,9 @@ typedef struct gb_plan {
      * (written by the panel solves, read by bulk copies) */
     int64_t *h_imgbase, *d_imgbase;
     int64_t img_total;                /* images (GB_IMG_FLOATS floats each) */
-    float *d_img;
 
     /* numeric buffers, [0] double, [1] single */
-    void *d_Lx[2], *d_CB[2];
+    void *d_Lx[2];
     int dev_valid[2];                 /* device factor holds the last result */
     const void *host_x[2];            /* L->x that the device factor mirrors */
 
@@ -273,6 +272,13 @@ struct gb_ctx {
     double opt_subwork;                /* SUBTREE task work limit for new plans */
     int64_t opt_warprows;              /* one-warp front height limit for new plans */
     int64_t opt_updgroup;              /* grouped trailing updates of new plans */
+    /* scratch of a factorization, grown as needed and reused by every
+     * factor this Common factorizes (resident factors do not hold it):
+     * update blocks per precision and the tensor-core operand images */
+    void *d_cbs[2];
+    size_t cbs_cap[2];
+    void *d_imgs;
+    size_t imgs_cap;
     int opt_autotune;                  /* 1 = the first super_numeric tunes the plan options */
     int tuned;                         /* the automatic tuning ran on this Common */
     double stats[8];

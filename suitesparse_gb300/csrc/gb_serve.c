@@ -11,11 +11,12 @@
  *     plan and device buffers are reused);
  *   - admission: a factor request starts only when its device-memory
  *     estimate fits under the budget; idle resident factors without queued
- *     work are evicted least recently used first to make room.  After each
- *     factorization the factor drops what only a factorization uses
- *     (gb300_trim_factor: update blocks, tensor-core operand images, the
- *     unused precision) and is charged its measured device bytes
- *     (gb300_factor_device_bytes), also after each refined solve;
+ *     work are evicted least recently used first to make room.  A resident
+ *     factor holds only what its solves use: the update blocks and operand
+ *     images of a factorization are scratch of the worker's Common, and
+ *     after each factorization the precision the solves do not read is
+ *     dropped (gb300_trim_factor); each factor is charged its measured
+ *     device bytes (gb300_factor_device_bytes), also after each solve;
  *   - an evicted factor keeps the host copy of its A (within a host budget,
  *     oldest dropped first): a later solve against it factorizes it again
  *     before solving (a readmission), a later factor request refactorizes
