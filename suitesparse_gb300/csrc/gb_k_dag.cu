@@ -262,9 +262,8 @@ static __device__ __noinline__ void trsm_task(const gb_dev_pattern &P, const gb_
 // coordinates minus nscol), those with tk.b = 0 on the grid of the update
 // block itself.
 template <typename T>
-__device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx, T *CB, T *Linv,
-                              unsigned char *smem_raw, int &sfail, gb_tc_ctx *tc = nullptr,
-                              float *Img = nullptr)
+__device__ void tile_body(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx, T *CB, T *Linv,
+                          unsigned char *smem_raw, int &sfail, gb_tc_ctx *tc, float *Img)
 {
     T (*A)[65] = (T (*)[65])smem_raw;
     T *S1 = (T *)smem_raw + 64 * 65, *S2 = S1 + 64 * 65;
@@ -348,6 +347,33 @@ __device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx
                                 mt, nt, nscol, tk.r == tk.c, 0, S1, S2);
         }
     }
+}
+
+// The work of one task of the tile graph: POTRF, TRSM, UPD or CB as
+// above, or DIAG (s, b, r, nbk), the diagonal chain of panel b as one task:
+// the panel solve of row block b by panel b - 1, the update of tile (b, b)
+// by panels r .. r + nbk - 1, then POTRF of panel b, in that order on this
+// block (each step reads what the previous one wrote, after a barrier; the
+// operand images written by the solve are fenced for the bulk copies).
+template <typename T>
+__device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx, T *CB, T *Linv,
+                              unsigned char *smem_raw, int &sfail, gb_tc_ctx *tc = nullptr,
+                              float *Img = nullptr)
+{
+    if (tk.type != GB_DT_DIAG) {
+        tile_body<T>(P, tk, Lx, CB, Linv, smem_raw, sfail, tc, Img);
+        return;
+    }
+    const gb_dtask t1 = {GB_DT_TRSM, tk.s, tk.b - 1, tk.b, 0, 0, 0, 0};
+    tile_body<T>(P, t1, Lx, CB, Linv, smem_raw, sfail, tc, Img);
+    __syncthreads();
+    if (tc && !tc->ok) return;
+    const gb_dtask t2 = {GB_DT_UPD, tk.s, tk.r, tk.b, tk.b, 0, tk.nbk, 0};
+    tile_body<T>(P, t2, Lx, CB, Linv, smem_raw, sfail, tc, Img);
+    __syncthreads();
+    if (tc && !tc->ok) return;
+    const gb_dtask t3 = {GB_DT_POTRF, tk.s, tk.b, 0, 0, 0, 0, 0};
+    tile_body<T>(P, t3, Lx, CB, Linv, smem_raw, sfail, tc, Img);
 }
 
 template <typename T>

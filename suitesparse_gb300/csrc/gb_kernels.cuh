@@ -78,6 +78,11 @@ typedef struct { int32_t type, s, b, r, c, prio, nbk, pad1; } gb_dtask;
  *                              subtree list, children first), each as NODE,
  *                              in one task: no queue traffic inside it */
 #define GB_DT_SUBTREE 9
+/* DIAG (s, b, r, nbk): the diagonal chain of panel b >= 1 of a wide
+ * supernode as one task: the panel solve of row block b by panel b - 1,
+ * the update of tile (b, b) by panels r .. r + nbk - 1 (the last update of
+ * that tile), then POTRF of panel b */
+#define GB_DT_DIAG 10
 #define GB_SUBTREE_WORK 4.0e6       /* work estimate per subtree task (flops) */
 #define GB_NODE_MAX_ROWS 256        /* small supernodes fused into NODE tasks */
 #define GB_WARP_ROWS 64             /* fronts at most this tall: one warp each */

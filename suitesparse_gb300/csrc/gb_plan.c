@@ -496,6 +496,76 @@ static int segments_build(gb_plan *P)
     return ok;
 }
 
+static int cmp_edge(const void *a, const void *b)
+{
+    const int32_t *x = a, *y = b;
+    if (x[0] != y[0]) return x[0] < y[0] ? -1 : 1;
+    return (x[1] > y[1]) - (x[1] < y[1]);
+}
+
+/* Contract each chain (panel solve T of row block b by panel b - 1, the
+ * update U of tile (b, b) that follows it, LL' P of panel b) of the level's
+ * task graph into one DIAG task in P's place, which one block runs as the
+ * three steps in order: the diagonal chain of a wide supernode then costs
+ * one task hand-over per panel instead of three.  Edges into or out of T
+ * and U move to the DIAG task (edges between the three vanish), T and U
+ * leave the task list, and the local task ids are renumbered.  No cycle
+ * arises: every path out of T or U that leaves the triple reaches tasks of
+ * later panels only, and P's only predecessor is U. */
+static int contract_diag(gb_plan *P, size_t t0g, gb_vec *edges, gb_vec *fuse)
+{
+    const int32_t ntl = (int32_t)(P->dag_t.n - t0g);
+    gb_dtask *dt = (gb_dtask *)P->dag_t.p + t0g;
+    int32_t *rep = malloc(sizeof(int32_t) * (ntl + 1));
+    int32_t *nid = malloc(sizeof(int32_t) * (ntl + 1));
+    if (!rep || !nid) { free(rep); free(nid); return 0; }
+    for (int32_t t = 0; t < ntl; t++) rep[t] = t;
+    const int32_t *F = fuse->p;
+    for (size_t q = 0; q < fuse->n; q++) {
+        const int32_t T = F[3 * q], U = F[3 * q + 1], Pt = F[3 * q + 2];
+        rep[T] = rep[U] = Pt;
+        /* DIAG (s, b): b = P's panel; r, nbk = U's first panel and count */
+        dt[Pt].type = GB_DT_DIAG;
+        dt[Pt].r = dt[U].b;
+        dt[Pt].nbk = GB_MAX(1, dt[U].nbk);
+        dt[Pt].prio = 0;
+    }
+    /* edges through rep, without self-loops and duplicates */
+    int32_t *E = edges->p;
+    size_t w = 0;
+    for (size_t q = 0; q < edges->n; q++) {
+        const int32_t a = rep[E[2 * q]], b = rep[E[2 * q + 1]];
+        if (a == b) continue;
+        E[2 * w] = a;
+        E[2 * w + 1] = b;
+        w++;
+    }
+    qsort(E, w, 2 * sizeof(int32_t), cmp_edge);
+    size_t u = 0;
+    for (size_t q = 0; q < w; q++) {
+        if (u && E[2 * (u - 1)] == E[2 * q] && E[2 * (u - 1) + 1] == E[2 * q + 1]) continue;
+        E[2 * u] = E[2 * q];
+        E[2 * u + 1] = E[2 * q + 1];
+        u++;
+    }
+    edges->n = u;
+    /* drop the contracted tasks, renumber the rest */
+    int32_t k = 0;
+    for (int32_t t = 0; t < ntl; t++) {
+        if (rep[t] != t) { nid[t] = -1; continue; }
+        nid[t] = k;
+        dt[k++] = dt[t];
+    }
+    P->dag_t.n = t0g + (size_t)k;
+    for (size_t q = 0; q < edges->n; q++) {
+        E[2 * q] = nid[E[2 * q]];
+        E[2 * q + 1] = nid[E[2 * q + 1]];
+    }
+    free(rep);
+    free(nid);
+    return 1;
+}
+
 gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_work,
                        int64_t warp_rows, int64_t upd_group)
 {
@@ -636,8 +706,9 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
 
     /* ---- factorization sequence: per level ASM, SMALL, DAG ---- */
     const int NB = GB_NB;
-    gb_vec edges;
+    gb_vec edges, fuse;
     vec_init(&edges, 2 * sizeof(int32_t));
+    vec_init(&fuse, 3 * sizeof(int32_t));
     for (int l = 0; l < nlevels && ok; l++) {
         size_t a0 = P->asm_t.n;
         for (Int q = lev_ptr[l]; q < lev_ptr[l + 1]; q++) {
@@ -664,6 +735,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
         int32_t base = 0;
         size_t t0g = P->dag_t.n;
         edges.n = 0;
+        fuse.n = 0;
         for (Int q = lev_ptr[l]; q < lev_ptr[l + 1] && ok; q++) {
             Int s = lev_list[q];
             Int nscol = Super[s + 1] - Super[s], nsrow = Pi[s + 1] - Pi[s];
@@ -785,6 +857,14 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
                         }
                     }
                 }
+                /* the diagonal chain: panel solve of row block b by panel
+                 * b - 1, the update of tile (b, b) that follows it, LL' of
+                 * panel b -- contracted into one DIAG task below */
+                for (Int b = 1; b < Cp && ok; b++) {
+                    int32_t tri[3] = {Tid[(b - 1) * R + b], LASTU(b, b), Pid[b]};
+                    if (tri[0] < 0 || tri[1] < 0) continue;
+                    ok &= gb_vec_push(&fuse, tri);
+                }
 #undef LASTU
             }
             if (Pid) {
@@ -834,6 +914,8 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
             }
             free(Pid); free(Tid); free(Uid); free(Aid);
         }
+        if (!ok) break;
+        if (fuse.n) ok = contract_diag(P, t0g, &edges, &fuse);
         if (!ok) break;
         /* CSR of successors, dependency counts, initial ready lists */
         int32_t ntl = (int32_t)(P->dag_t.n - t0g);
@@ -893,6 +975,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
         }
     }
     gb_vec_free(&edges);
+    gb_vec_free(&fuse);
 
     /* ---- forward sweep sequence ---- */
     for (int l = 0; l < nlevels && ok; l++) {
