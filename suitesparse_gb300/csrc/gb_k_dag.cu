@@ -450,6 +450,47 @@ static_assert(GB_FDAG_TC_SMEM >= GB_TC_SMEM && GB_FDAG_TC_SMEM >= (int)dag_smem<
 static_assert(8 * warp_front_smem<32, double>() <= dag_smem<double>()
               && 2 * warp_front_smem<64, double>() <= dag_smem<double>(), "one-warp fronts: shared memory");
 
+// All threads of the block, after a barrier that follows the work whose
+// results the successors read: release the block's writes, decrement the
+// dependency counters of successors succ[ea, eb) of the task (one round of
+// atomics for up to blockDim.x successors) and queue those that became
+// ready.  A join (no work, never queued) releases its own successors here.
+// keep: a critical successor that becomes ready may be kept in *snext for
+// this block to run next (a poller, at the end of its task); otherwise
+// every ready successor is queued.  Ends with a barrier (snext, set by any
+// thread, is read by thread 0).
+__device__ void fdag_release(const gb_fdag_dev &D, const gb_fpat &PP, const gb_finst &I, int ea,
+                             int eb, bool keep, int *snext)
+{
+    if (ea + (int)threadIdx.x < eb) __threadfence();
+    for (int e = ea + (int)threadIdx.x; e < eb; e += (int)blockDim.x) {
+        const int v = PP.succ[e];
+        const int g = (int)(I.base + v);
+        if (dag_add_acq_rel(D.cnt + g, -1) != 1) continue;
+        if (PP.tasks[v].type != GB_DT_JOIN) {
+            const int prio = PP.tasks[v].prio;
+            if (prio == 0 && keep && atomicCAS(snext, -1, g) == -1) {
+                atomicSub(D.Q.ctrl + 6, 1);     // kept: one less to queue
+                continue;
+            }
+            dag_push(D.Q, g, prio);
+            continue;
+        }
+        for (int f = PP.succ_ptr[v]; f < PP.succ_ptr[v + 1]; f++) {
+            const int w = PP.succ[f];
+            const int gw = (int)(I.base + w);
+            if (dag_add_acq_rel(D.cnt + gw, -1) != 1) continue;
+            const int pw = PP.tasks[w].prio;
+            if (pw == 0 && keep && atomicCAS(snext, -1, gw) == -1) {
+                atomicSub(D.Q.ctrl + 6, 1);     // kept: one less to queue
+                continue;
+            }
+            dag_push(D.Q, gw, pw);
+        }
+    }
+    __syncthreads();
+}
+
 template <typename T, bool TC>
 __global__ void __launch_bounds__(256, 2)
 k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
@@ -615,8 +656,32 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                 q = w3;
             }
         } else {
-            dag_tile_task<T>(P, tk, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr,
+            if (tk.type == GB_DT_DIAG) {
+                // the diagonal chain of panel tk.b: the panel solve of row
+                // block b, then the updates that read it may start (early
+                // successors) while this block updates tile (b, b) and
+                // factors panel b
+                const gb_dtask t1 = {GB_DT_TRSM, tk.s, tk.b - 1, tk.b, 0, 0, 0, 0};
+                tile_body<T>(P, t1, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr,
                              TC ? D.img : nullptr);
+                __syncthreads();
+                fdag_release(D, PP, I, PP.succ_ptr[local], PP.succ_ptr[local] + tk.pad1, false,
+                             &snext);
+                if (!TC || !tc || tcx.ok) {
+                    const gb_dtask t2 = {GB_DT_UPD, tk.s, tk.r, tk.b, tk.b, 0, tk.nbk, 0};
+                    tile_body<T>(P, t2, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr,
+                                 TC ? D.img : nullptr);
+                    __syncthreads();
+                }
+                if (!TC || !tc || tcx.ok) {
+                    const gb_dtask t3 = {GB_DT_POTRF, tk.s, tk.b, 0, 0, 0, 0, 0};
+                    tile_body<T>(P, t3, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr,
+                                 TC ? D.img : nullptr);
+                }
+            } else {
+                dag_tile_task<T>(P, tk, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr,
+                                 TC ? D.img : nullptr);
+            }
             if (TC && tc && !tcx.ok) {
                 // a tensor-core wait gave up: stop the executor (every block
                 // returns on the error word)
@@ -628,42 +693,11 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
             }
         }
         __syncthreads();
-        {
-            // every thread releases successors (a diagonal step's task has
-            // up to ~100: one round of counter atomics instead of several
-            // on one warp, which the dependency chain would wait for)
-            if (D.trace && threadIdx.x == 0) D.trace[3 * (size_t)id + 1] = dag_timer();
-            const int e0 = PP.succ_ptr[local], e1 = PP.succ_ptr[local + 1];
-            if (e0 + (int)threadIdx.x < e1) __threadfence();
-            for (int e = e0 + (int)threadIdx.x; e < e1; e += (int)blockDim.x) {
-                const int v = PP.succ[e];
-                const int g = (int)(I.base + v);
-                if (dag_add_acq_rel(D.cnt + g, -1) != 1) continue;
-                if (PP.tasks[v].type != GB_DT_JOIN) {
-                    const int prio = PP.tasks[v].prio;
-                    if (prio == 0 && spoll && atomicCAS(&snext, -1, g) == -1) {
-                        atomicSub(D.Q.ctrl + 6, 1);     // kept: one less to queue
-                        continue;
-                    }
-                    dag_push(D.Q, g, prio);
-                    continue;
-                }
-                // a join (no work, never queued): release its successors here;
-                // they are never joins themselves
-                for (int f = PP.succ_ptr[v]; f < PP.succ_ptr[v + 1]; f++) {
-                    const int w = PP.succ[f];
-                    const int gw = (int)(I.base + w);
-                    if (dag_add_acq_rel(D.cnt + gw, -1) != 1) continue;
-                    const int pw = PP.tasks[w].prio;
-                    if (pw == 0 && spoll && atomicCAS(&snext, -1, gw) == -1) {
-                        atomicSub(D.Q.ctrl + 6, 1);     // kept: one less to queue
-                        continue;
-                    }
-                    dag_push(D.Q, gw, pw);
-                }
-            }
-            __syncthreads();   // snext, set by any thread, is read by thread 0
-        }
+        // the successors not released early (a DIAG task released its
+        // first tk.pad1 after its panel solve)
+        if (D.trace && threadIdx.x == 0) D.trace[3 * (size_t)id + 1] = dag_timer();
+        fdag_release(D, PP, I, PP.succ_ptr[local] + (tk.type == GB_DT_DIAG ? tk.pad1 : 0),
+                     PP.succ_ptr[local + 1], spoll != 0, &snext);
     }
     if (TC && tc) {
         // (a tile product whose wait gave up has already waited, bounded,

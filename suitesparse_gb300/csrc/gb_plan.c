@@ -102,6 +102,9 @@ static int push_launch(gb_vec *seq, int kind, size_t count, size_t off)
  * Joins carry no work and are never queued.  Every task of s follows
  * JA(s), so the front is assembled before any tile task touches it, and the
  * parent's assembly follows every update-block tile of every child. */
+static void gb_order_succ(const gb_dtask *tasks, int32_t early, int32_t *succ, int32_t lo,
+                          int32_t hi, int32_t *tmp);
+
 typedef struct { double w; int32_t id; } gb_ready_est;
 
 /* descending work, then ascending task id (a deterministic order) */
@@ -371,13 +374,9 @@ static int fdag_build(gb_plan *P)
         for (size_t t = 0; t < N; t++) deg[t + 1] += deg[t];
         memcpy(pos, deg, sizeof(int32_t) * (N + 1));
         for (size_t q = 0; q < E.n; q++) succ[pos[ed[2 * q]]++] = ed[2 * q + 1];
-        for (size_t t = 0; t < N; t++) {
-            int32_t w = deg[t];
-            for (int pass = 0; pass < 2; pass++)
-                for (int32_t e = deg[t]; e < deg[t + 1]; e++)
-                    if ((ft[succ[e]].prio == 0) == (pass == 0)) tmp[w++] = succ[e];
-            memcpy(succ + deg[t], tmp + deg[t], sizeof(int32_t) * (deg[t + 1] - deg[t]));
-        }
+        for (size_t t = 0; t < N; t++)
+            gb_order_succ(ft, ft[t].type == GB_DT_DIAG ? ft[t].pad1 : 0, succ, deg[t], deg[t + 1],
+                          tmp);
         for (size_t t = 0; ok && t <= N; t++) ok &= gb_vec_push(&P->fd_sp, &deg[t]);
         for (size_t q = 0; ok && q < E.n; q++) ok &= gb_vec_push(&P->fd_succ, &succ[q]);
         /* joins are never queued: the block that finishes a join's last
@@ -496,11 +495,29 @@ static int segments_build(gb_plan *P)
     return ok;
 }
 
-static int cmp_edge(const void *a, const void *b)
+static int cmp_edge3(const void *a, const void *b)
 {
     const int32_t *x = a, *y = b;
-    if (x[0] != y[0]) return x[0] < y[0] ? -1 : 1;
-    return (x[1] > y[1]) - (x[1] < y[1]);
+    for (int k = 0; k < 3; k++)
+        if (x[k] != y[k]) return x[k] < y[k] ? -1 : 1;
+    return 0;
+}
+
+/* Order the successors succ[lo, hi) of a task critical (prio 0) first;
+ * a DIAG task's first `early` successors stay ahead of the others (its
+ * executor releases them when its panel solve is done). */
+static void gb_order_succ(const gb_dtask *tasks, int32_t early, int32_t *succ, int32_t lo,
+                          int32_t hi, int32_t *tmp)
+{
+    const int32_t mid = lo + early < hi ? lo + early : hi;
+    int32_t w = lo;
+    for (int part = 0; part < 2; part++) {
+        const int32_t a = part ? mid : lo, b = part ? hi : mid;
+        for (int pass = 0; pass < 2; pass++)
+            for (int32_t e = a; e < b; e++)
+                if ((tasks[succ[e]].prio == 0) == (pass == 0)) tmp[w++] = succ[e];
+    }
+    memcpy(succ + lo, tmp + lo, sizeof(int32_t) * (size_t)(hi - lo));
 }
 
 /* Contract each chain (panel solve T of row block b by panel b - 1, the
@@ -509,46 +526,67 @@ static int cmp_edge(const void *a, const void *b)
  * three steps in order: the diagonal chain of a wide supernode then costs
  * one task hand-over per panel instead of three.  Edges into or out of T
  * and U move to the DIAG task (edges between the three vanish), T and U
- * leave the task list, and the local task ids are renumbered.  No cycle
- * arises: every path out of T or U that leaves the triple reaches tasks of
- * later panels only, and P's only predecessor is U. */
+ * leave the task list, and the local task ids are renumbered.  The
+ * successors that only T had (the updates that read the block T solves)
+ * are the DIAG task's "early" successors, listed first and counted in its
+ * pad1: the executor releases them as soon as the solve is done, so that
+ * they run beside the rest of the chain as they did beside U and P.  No
+ * cycle arises: every path out of T or U that leaves the triple reaches
+ * tasks of later panels only, and P's only predecessor is U. */
 static int contract_diag(gb_plan *P, size_t t0g, gb_vec *edges, gb_vec *fuse)
 {
     const int32_t ntl = (int32_t)(P->dag_t.n - t0g);
     gb_dtask *dt = (gb_dtask *)P->dag_t.p + t0g;
     int32_t *rep = malloc(sizeof(int32_t) * (ntl + 1));
     int32_t *nid = malloc(sizeof(int32_t) * (ntl + 1));
-    if (!rep || !nid) { free(rep); free(nid); return 0; }
+    unsigned char *isT = calloc(ntl + 1, 1);
+    int32_t *E3 = malloc(sizeof(int32_t) * 3 * (edges->n + 1));
+    if (!rep || !nid || !isT || !E3) { free(rep); free(nid); free(isT); free(E3); return 0; }
     for (int32_t t = 0; t < ntl; t++) rep[t] = t;
     const int32_t *F = fuse->p;
     for (size_t q = 0; q < fuse->n; q++) {
         const int32_t T = F[3 * q], U = F[3 * q + 1], Pt = F[3 * q + 2];
         rep[T] = rep[U] = Pt;
+        isT[T] = 1;
         /* DIAG (s, b): b = P's panel; r, nbk = U's first panel and count */
         dt[Pt].type = GB_DT_DIAG;
         dt[Pt].r = dt[U].b;
         dt[Pt].nbk = GB_MAX(1, dt[U].nbk);
         dt[Pt].prio = 0;
+        dt[Pt].pad1 = 0;
     }
-    /* edges through rep, without self-loops and duplicates */
-    int32_t *E = edges->p;
+    /* edges through rep, without self-loops; late = 0 for an edge out of a
+     * T (an early successor unless another edge makes it wait) */
+    const int32_t *E = edges->p;
     size_t w = 0;
     for (size_t q = 0; q < edges->n; q++) {
         const int32_t a = rep[E[2 * q]], b = rep[E[2 * q + 1]];
         if (a == b) continue;
-        E[2 * w] = a;
-        E[2 * w + 1] = b;
+        E3[3 * w] = a;
+        E3[3 * w + 1] = b;
+        E3[3 * w + 2] = isT[E[2 * q]] ? 0 : 1;
         w++;
     }
-    qsort(E, w, 2 * sizeof(int32_t), cmp_edge);
+    /* duplicates: one edge, late if any copy is */
+    qsort(E3, w, 3 * sizeof(int32_t), cmp_edge3);
     size_t u = 0;
     for (size_t q = 0; q < w; q++) {
-        if (u && E[2 * (u - 1)] == E[2 * q] && E[2 * (u - 1) + 1] == E[2 * q + 1]) continue;
-        E[2 * u] = E[2 * q];
-        E[2 * u + 1] = E[2 * q + 1];
+        if (u && E3[3 * (u - 1)] == E3[3 * q] && E3[3 * (u - 1) + 1] == E3[3 * q + 1]) {
+            E3[3 * (u - 1) + 2] |= E3[3 * q + 2];
+            continue;
+        }
+        memmove(E3 + 3 * u, E3 + 3 * q, 3 * sizeof(int32_t));
         u++;
     }
-    edges->n = u;
+    /* per source: early edges first (only DIAG sources have any) */
+    for (size_t q = 0; q < u; q++) {
+        const int32_t tmp = E3[3 * q + 1];
+        E3[3 * q + 1] = E3[3 * q + 2];
+        E3[3 * q + 2] = tmp;
+    }
+    qsort(E3, u, 3 * sizeof(int32_t), cmp_edge3);
+    for (size_t q = 0; q < u; q++)
+        if (E3[3 * q + 1] == 0 && dt[E3[3 * q]].type == GB_DT_DIAG) dt[E3[3 * q]].pad1++;
     /* drop the contracted tasks, renumber the rest */
     int32_t k = 0;
     for (int32_t t = 0; t < ntl; t++) {
@@ -557,12 +595,16 @@ static int contract_diag(gb_plan *P, size_t t0g, gb_vec *edges, gb_vec *fuse)
         dt[k++] = dt[t];
     }
     P->dag_t.n = t0g + (size_t)k;
-    for (size_t q = 0; q < edges->n; q++) {
-        E[2 * q] = nid[E[2 * q]];
-        E[2 * q + 1] = nid[E[2 * q + 1]];
+    int32_t *Eo = edges->p;
+    for (size_t q = 0; q < u; q++) {
+        Eo[2 * q] = nid[E3[3 * q]];
+        Eo[2 * q + 1] = nid[E3[3 * q + 2]];
     }
+    edges->n = u;
     free(rep);
     free(nid);
+    free(isT);
+    free(E3);
     return 1;
 }
 
@@ -943,13 +985,9 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
              * successors 32 at a time, in list order */
             int32_t *tmp = ok ? malloc(sizeof(int32_t) * (edges.n + 1)) : NULL;
             if (!tmp) ok = 0;
-            for (int32_t t = 0; ok && t < ntl; t++) {
-                int32_t w = deg[t];
-                for (int pass = 0; pass < 2; pass++)
-                    for (int32_t e = deg[t]; e < deg[t + 1]; e++)
-                        if ((dt[succ[e]].prio == 0) == (pass == 0)) tmp[w++] = succ[e];
-                memcpy(succ + deg[t], tmp + deg[t], sizeof(int32_t) * (deg[t + 1] - deg[t]));
-            }
+            for (int32_t t = 0; ok && t < ntl; t++)
+                gb_order_succ(dt, dt[t].type == GB_DT_DIAG ? dt[t].pad1 : 0, succ, deg[t],
+                              deg[t + 1], tmp);
             free(tmp);
             for (int32_t t = 0; ok && t <= ntl; t++) ok &= gb_vec_push(&P->dag_sp, &deg[t]);
             for (size_t q2 = 0; ok && q2 < edges.n; q2++) ok &= gb_vec_push(&P->dag_succ, &succ[q2]);

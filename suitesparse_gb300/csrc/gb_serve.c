@@ -32,6 +32,7 @@
  */
 #include <math.h>
 #include <pthread.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
@@ -47,9 +48,18 @@ typedef struct gb_sreq {
     int64_t *perm;                /* factor: owned copy or NULL */
     double *B, *X;                /* solve: owned n x nrhs */
     double arrival, start, finish, berr;
-    struct gb_sreq *next_q;       /* pending queue */
+    struct gb_sreq *next_q, *prev_q;  /* pending queue (arrival order) */
+    struct gb_sreq *next_f;       /* the pending requests of the same factor id */
     struct gb_sreq *next_h;       /* hash chain */
 } gb_sreq;
+
+/* the pending requests of one factor id, in arrival order */
+typedef struct gb_sfq {
+    int64_t fid;
+    int count;
+    gb_sreq *head, *tail;
+    struct gb_sfq *next_h;
+} gb_sfq;
 
 typedef struct gb_sfactor {
     int64_t id, pattern_id, bytes;
@@ -59,14 +69,14 @@ typedef struct gb_sfactor {
     int evicted;                  /* device state released; A kept on the host */
     int64_t est;                  /* device bytes when last resident */
     double last_use;
-    struct gb_sfactor *next;
+    struct gb_sfactor *next, *next_h;
 } gb_sfactor;
 
 typedef struct gb_spattern {
     int64_t id;
     cholmod_factor *L;            /* symbolic; NULL while being analysed */
     int state;                    /* 0 new, 2 being analysed, 1 ready, -1 failed */
-    struct gb_spattern *next;
+    struct gb_spattern *next, *next_h;
 } gb_spattern;
 
 #define GB_SHASH 65536
@@ -76,8 +86,9 @@ struct gb300_server {
     pthread_cond_t cv;            /* work, completion, pattern ready */
     gb_sreq *qhead, *qtail;
     gb_sreq *hash[GB_SHASH];
-    gb_sfactor *factors;
-    gb_spattern *patterns;
+    gb_sfactor *factors, *fhash[GB_SHASH];
+    gb_spattern *patterns, *phash[GB_SHASH];
+    gb_sfq *qhash[GB_SHASH];
     int nslots, ncommons, max_rhs, stop;
     int64_t budget, in_use, evictions, coalesced, served, readmissions;
     int64_t host_budget, host_kept;   /* host bytes of the evicted factors' A */
@@ -103,14 +114,47 @@ static gb_sreq *req_find(gb300_server *S, int64_t id)
 
 static gb_sfactor *factor_find(gb300_server *S, int64_t id)
 {
-    for (gb_sfactor *f = S->factors; f; f = f->next)
+    for (gb_sfactor *f = S->fhash[hslot(id)]; f; f = f->next_h)
         if (f->id == id) return f;
     return NULL;
 }
 
+static void factor_add(gb300_server *S, gb_sfactor *F)
+{
+    F->next = S->factors;
+    S->factors = F;
+    const unsigned h = hslot(F->id);
+    F->next_h = S->fhash[h];
+    S->fhash[h] = F;
+}
+
+static void pattern_add(gb300_server *S, gb_spattern *p)
+{
+    p->next = S->patterns;
+    S->patterns = p;
+    const unsigned h = hslot(p->id);
+    p->next_h = S->phash[h];
+    S->phash[h] = p;
+}
+
+/* the pending-request list of a factor id (created when create) */
+static gb_sfq *fq_get(gb300_server *S, int64_t fid, int create)
+{
+    const unsigned h = hslot(fid);
+    for (gb_sfq *q = S->qhash[h]; q; q = q->next_h)
+        if (q->fid == fid) return q;
+    if (!create) return NULL;
+    gb_sfq *q = calloc(1, sizeof *q);
+    if (!q) return NULL;
+    q->fid = fid;
+    q->next_h = S->qhash[h];
+    S->qhash[h] = q;
+    return q;
+}
+
 static gb_spattern *pattern_find(gb300_server *S, int64_t id)
 {
-    for (gb_spattern *p = S->patterns; p; p = p->next)
+    for (gb_spattern *p = S->phash[hslot(id)]; p; p = p->next_h)
         if (p->id == id) return p;
     return NULL;
 }
@@ -144,6 +188,8 @@ static void factor_unlink_free(gb300_server *S, gb_sfactor *victim, cholmod_comm
 {
     for (gb_sfactor **pp = &S->factors; *pp; pp = &(*pp)->next)
         if (*pp == victim) { *pp = victim->next; break; }
+    for (gb_sfactor **pp = &S->fhash[hslot(victim->id)]; *pp; pp = &(*pp)->next_h)
+        if (*pp == victim) { *pp = victim->next_h; break; }
     if (victim->L) {
         gb300_release_factor(victim->L, c);
         gb300_free_factor(&victim->L, c);
@@ -154,9 +200,8 @@ static void factor_unlink_free(gb300_server *S, gb_sfactor *victim, cholmod_comm
 
 static int pending_for(gb300_server *S, int64_t factor_id)
 {
-    for (gb_sreq *r = S->qhead; r; r = r->next_q)
-        if (r->factor_id == factor_id) return 1;
-    return 0;
+    const gb_sfq *q = fq_get(S, factor_id, 0);
+    return q && q->count > 0;
 }
 
 /* under S->mu: release the device state of idle factors (least recently
@@ -209,47 +254,63 @@ static int readmit(gb300_server *S, gb_sfactor *F, cholmod_common *c)
     return 1;
 }
 
-/* under S->mu: unlink r (whose predecessor in the queue is prev) */
-static void unlink_req(gb300_server *S, gb_sreq **pp, gb_sreq *r, gb_sreq *prev)
+/* under S->mu: take r off the pending queue and off its factor id's list,
+ * whose first request it is */
+static void unlink_req(gb300_server *S, gb_sreq *r)
 {
-    *pp = r->next_q;
-    if (S->qtail == r) S->qtail = prev;
-    r->next_q = NULL;
+    if (r->prev_q) r->prev_q->next_q = r->next_q; else S->qhead = r->next_q;
+    if (r->next_q) r->next_q->prev_q = r->prev_q; else S->qtail = r->prev_q;
+    r->next_q = r->prev_q = NULL;
+    gb_sfq *q = fq_get(S, r->factor_id, 0);
+    if (q && q->head == r) {
+        q->head = r->next_f;
+        if (!q->head) q->tail = NULL;
+        q->count--;
+    }
+    r->next_f = NULL;
 }
 
 /* under S->mu: the next runnable request (and, for a solve, the queued
  * solves of the same factor coalesced behind it), unlinked from the queue.
- * A solve whose factor neither exists nor has a factor request queued
- * before it (never factored, or evicted) fails here. */
+ * Only the first pending request of a factor id can run (its id's list);
+ * lookups of factors, patterns and lists are hashed, so one scan costs
+ * O(1) per pending request.  A solve whose factor neither exists nor has
+ * a factor request queued before it (never factored, or evicted and
+ * dropped) fails here. */
 static gb_sreq *take_work(gb300_server *S, gb_sreq **group, int *ngroup, cholmod_common *c)
 {
-    gb_sreq *prev = NULL;
-    for (gb_sreq **pp = &S->qhead; *pp;) {
-        gb_sreq *r = *pp;
-        gb_sfactor *F = factor_find(S, r->factor_id);
-        int blocked = 0;
+    /* the smallest need that found no room in this scan: a larger one will
+     * not find any either (nothing is freed during the scan) */
+    int64_t no_room = INT64_MAX;
+    for (gb_sreq *r = S->qhead, *nx; r; r = nx) {
+        nx = r->next_q;
         /* an earlier queued request of the same factor goes first */
-        for (gb_sreq *q = S->qhead; q != r; q = q->next_q)
-            if (q->factor_id == r->factor_id) { blocked = 1; break; }
-        if (!blocked && r->kind == REQ_SOLVE && (!F || (F->evicted && !F->A))) {
-            unlink_req(S, pp, r, prev);
+        const gb_sfq *fq = fq_get(S, r->factor_id, 0);
+        if (fq && fq->head != r) continue;
+        gb_sfactor *F = factor_find(S, r->factor_id);
+        if (r->kind == REQ_SOLVE && (!F || (F->evicted && !F->A))) {
+            unlink_req(S, r);
             r->status = CHOLMOD_INVALID;
             r->start = r->finish = gb300_server_now();
             r->done = 1;
             S->served++;
             req_free_payload(r, c);
             pthread_cond_broadcast(&S->cv);
-            continue;                                  /* *pp is the next request */
+            continue;
         }
         gb_spattern *pat = NULL;
         int64_t need = 0;
-        int runnable = !blocked && !(F && F->busy);
+        int runnable = !(F && F->busy);
         if (runnable && F && F->evicted) {
             /* a request of an evicted factor: a factor request replaces its
              * A, a solve refactorizes the kept one */
             gb_spattern *fp = pattern_find(S, F->pattern_id);
             if (r->kind == REQ_SOLVE && !(fp && fp->state == 1)) runnable = 0;
-            else runnable = readmit(S, F, c);
+            else if (F->est >= no_room) runnable = 0;
+            else {
+                runnable = readmit(S, F, c);
+                if (!runnable) no_room = F->est;
+            }
             if (runnable && r->kind == REQ_SOLVE) S->readmissions++;
         } else if (runnable && r->kind == REQ_FACTOR && !F) {
             pat = pattern_find(S, r->pattern_id);
@@ -257,29 +318,25 @@ static gb_sreq *take_work(gb300_server *S, gb_sreq **group, int *ngroup, cholmod
             else {
                 need = pat && pat->L ? estimate_bytes(pat->L, r->A)
                                      : (int64_t)40 * ((const int64_t *)r->A->p)[r->A->ncol];
-                runnable = make_room(S, need, c);
+                runnable = need < no_room && make_room(S, need, c);
+                if (!runnable && need < no_room) no_room = need;
             }
         }
-        if (!runnable) {
-            prev = r;
-            pp = &r->next_q;
-            continue;
-        }
-        unlink_req(S, pp, r, prev);
+        if (!runnable) continue;
+        gb_sreq *follow = r->next_f;
+        unlink_req(S, r);
         *ngroup = 0;
         group[(*ngroup)++] = r;
         if (r->kind == REQ_SOLVE) {
             /* coalesce the queued solves of the same factor that follow, up
              * to a refactorization of it or max_rhs columns */
             int cols = r->nrhs;
-            gb_sreq *p2 = prev;
-            for (gb_sreq **qq = pp; *qq;) {
-                gb_sreq *q = *qq;
-                if (q->factor_id != r->factor_id) { p2 = q; qq = &q->next_q; continue; }
+            for (gb_sreq *q = follow, *qn; q; q = qn) {
+                qn = q->next_f;
                 if (q->kind != REQ_SOLVE || q->n != r->n || cols + q->nrhs > S->max_rhs
                     || *ngroup >= 64)
                     break;
-                unlink_req(S, qq, q, p2);
+                unlink_req(S, q);
                 group[(*ngroup)++] = q;
                 cols += q->nrhs;
             }
@@ -293,16 +350,14 @@ static gb_sreq *take_work(gb300_server *S, gb_sreq **group, int *ngroup, cholmod
                 if (pat) {
                     pat->id = r->pattern_id;
                     pat->state = 0;
-                    pat->next = S->patterns;
-                    S->patterns = pat;
+                    pattern_add(S, pat);
                 }
             }
             if (F) {
                 F->id = r->factor_id;
                 F->pattern_id = r->pattern_id;
                 F->bytes = need;
-                F->next = S->factors;
-                S->factors = F;
+                factor_add(S, F);
                 S->in_use += need;
             }
         }
@@ -513,11 +568,19 @@ static int submit(gb300_server *S, gb_sreq *r)
 {
     pthread_mutex_lock(&S->mu);
     if (req_find(S, r->id)) { pthread_mutex_unlock(&S->mu); return CHOLMOD_INVALID; }
+    gb_sfq *fq = fq_get(S, r->factor_id, 1);
+    if (!fq) { pthread_mutex_unlock(&S->mu); return CHOLMOD_OUT_OF_MEMORY; }
     unsigned h = hslot(r->id);
     r->next_h = S->hash[h];
     S->hash[h] = r;
+    r->prev_q = S->qtail;
+    r->next_q = NULL;
     if (S->qtail) S->qtail->next_q = r; else S->qhead = r;
     S->qtail = r;
+    r->next_f = NULL;
+    if (fq->tail) fq->tail->next_f = r; else fq->head = r;
+    fq->tail = r;
+    fq->count++;
     pthread_cond_broadcast(&S->cv);
     pthread_mutex_unlock(&S->mu);
     return CHOLMOD_OK;
@@ -648,6 +711,14 @@ int gb300_server_destroy(gb300_server *S)
         S->patterns = p->next;
         if (p->L) gb300_free_factor(&p->L, c);
         free(p);
+    }
+    for (int h = 0; h < GB_SHASH; h++) {
+        gb_sfq *q = S->qhash[h];
+        while (q) {
+            gb_sfq *nx = q->next_h;
+            free(q);
+            q = nx;
+        }
     }
     for (int i = 0; i < S->ncommons; i++) gb300_finish(&S->commons[i]);
     pthread_mutex_destroy(&S->mu);

@@ -5,9 +5,10 @@
  * and executing the tile tasks of every wide supernode (POTRF, TRSM, UPD,
  * DIAG, CB on its own 64-row grid) in random topological orders of that
  * graph on a dense SPD front gives the front's blocked Cholesky: L and the
- * Schur complement of the update block, to rounding.  A missing dependency
- * lets some order read a tile before its last update, which shows as an
- * error far above rounding.
+ * Schur complement of the update block, to rounding.  A DIAG task runs in
+ * two parts with its early successors released in between, as on the GPU.
+ * A missing dependency lets some order read a tile before its last update,
+ * which shows as an error far above rounding.
  *
  * usage: plan_dag_check Ap.bin Ai.bin perm.bin  (int64 arrays of the lower
  * pattern of A and a postordered fill-reducing permutation) */
@@ -172,7 +173,12 @@ int main(int argc, char **argv)
                         update(ref[s], m, c0 + nb, m, c0 + nb, m, c0, c0 + nb, 1);
                     }
                 }
-                int *cnt = calloc(nt, sizeof(int)), *ready = malloc(sizeof(int) * nt), nr = 0, done = 0;
+                /* a DIAG task runs in two parts, as the executor runs it:
+                 * its panel solve, then (after its early successors were
+                 * released, so that they may run first) the update of the
+                 * diagonal tile and the LL'; ready entries >= nt are the
+                 * second parts of DIAG tasks k - nt */
+                int *cnt = calloc(nt, sizeof(int)), *ready = malloc(sizeof(int) * 2 * nt), nr = 0, done = 0;
                 for (int k = 0; k < nt; k++)
                     for (int e = lsp[k]; e < lsp[k + 1]; e++) cnt[ls[e]]++;
                 for (int k = 0; k < nt; k++)
@@ -180,9 +186,29 @@ int main(int argc, char **argv)
                 while (nr) {
                     const int pick = (int)(next_rand() % (uint64_t)nr), k = ready[pick];
                     ready[pick] = ready[--nr];
-                    run_task(&t[k], front, Super, Pi);
-                    done++;
-                    for (int e = lsp[k]; e < lsp[k + 1]; e++)
+                    int e0 = 0, e1 = 0;
+                    if (k < nt && t[k].type == GB_DT_DIAG) {
+                        const gb_dtask a = {GB_DT_TRSM, t[k].s, t[k].b - 1, t[k].b, 0, 0, 0, 0};
+                        run_task(&a, front, Super, Pi);
+                        e0 = lsp[k];
+                        e1 = lsp[k] + t[k].pad1;
+                        ready[nr++] = nt + k;
+                    } else if (k >= nt) {
+                        const int d = k - nt;
+                        const gb_dtask b = {GB_DT_UPD, t[d].s, t[d].r, t[d].b, t[d].b, 0, t[d].nbk, 0};
+                        const gb_dtask c = {GB_DT_POTRF, t[d].s, t[d].b, 0, 0, 0, 0, 0};
+                        run_task(&b, front, Super, Pi);
+                        run_task(&c, front, Super, Pi);
+                        e0 = lsp[d] + t[d].pad1;
+                        e1 = lsp[d + 1];
+                        done++;
+                    } else {
+                        run_task(&t[k], front, Super, Pi);
+                        e0 = lsp[k];
+                        e1 = lsp[k + 1];
+                        done++;
+                    }
+                    for (int e = e0; e < e1; e++)
                         if (--cnt[ls[e]] == 0) ready[nr++] = ls[e];
                 }
                 if (done != nt) {
