@@ -39,10 +39,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CASE = "c2"
-# DRAM bytes (read + write) of one k_fdag launch on c2, measured by ncu
-# (dram__bytes_read.sum 3.280e9 + dram__bytes_write.sum 5.293e9); the command
-# is in profiles/k_fdag_c2_dram_traffic.md
-K_FDAG_C2_DRAM_BYTES = 3280453632 + 5293096704
+# DRAM bytes (read + write) of one k_fdag<float, true> launch on c2, measured
+# by ncu (dram__bytes_read.sum 4.49e9 + dram__bytes_write.sum 6.15e9); the
+# command is in profiles/k_fdag_c2_dram_traffic.md
+K_FDAG_C2_DRAM_BYTES = 4.49e9 + 6.15e9
 METRIC = "factor TFLOP/s + solves/s at 1e-12 backward err, FP32+IR vs FP64; p50/p99"
 WORKLOAD = "c2: 3D 7-point variable-coefficient Laplacian 64^3 (n=262144), METIS"
 
