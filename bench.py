@@ -624,9 +624,10 @@ def run_serve(args):
     2D 5-point grids of side 32-512 and 3D 7-point grids of side 16-64,
     log-uniform coefficients in [1e-2, 1e2], 60% refactorizations of 16
     cached patterns, 20% solves with 1-32 right-hand sides against their
-    resident factors, 20% new patterns; the mixed form at two arrival rates
-    and the plain FP64 form (every factorization in FP64) on the first 2,000
-    requests.  p50/p99 latency (finish - arrival), requests/s and solved
+    resident factors, 20% new patterns; the mixed form at three arrival
+    rates (below, near and far above what the GPU serves) and the plain FP64
+    form (every factorization in FP64) on the first 2,000 requests at a rate
+    it sustains.  p50/p99 latency (finish - arrival), requests/s and solved
     columns/s per rate; a sample of solutions checked against the oracle."""
     ws, rank, dist = dist_setup()
     from suitesparse_gb300 import cholmod as CH
@@ -701,8 +702,8 @@ def run_serve(args):
                 "readmissions": st["readmissions"], "server": st,
                 "clocks": clk.summary()}
 
-    sweep = [run(rate * ws, len(base), False) for rate in (200.0, 800.0)]
-    fp64 = run(100.0 * ws, min(n64 * ws, len(base)), True)
+    sweep = [run(rate * ws, len(base), False) for rate in (100.0, 200.0, 800.0)]
+    fp64 = run(20.0 * ws, min(n64 * ws, len(base)), True)
     top = sweep[-1]
     line = {
         "metric": METRIC, "value": top["solves_per_s"], "unit": "solves/s", "n_gpus": ws,
