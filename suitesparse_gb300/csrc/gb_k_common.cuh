@@ -207,7 +207,7 @@ template <> __device__ __forceinline__ float gb_rsqrt<float>(float x) { return r
 // through shared memory; L(j,j) = d rsqrt(d), the column scaled by
 // rsqrt(d), and every lane stores its L(i, j) into S[i][j].  Only two warp
 // barriers and no shuffles per column: the loads of a column's dot
-// products are independent and overlap (4.3 us for 32 columns against
+// products are independent and overlap (3.3 us for 32 columns against
 // 11.4 us for the right-looking form with a shuffle per update, measured
 // alone on a GB300).  From the first pivot that is not positive on, the
 // columns are formed from a unit pivot (finite, never read).  rinv
@@ -267,10 +267,41 @@ __device__ __forceinline__ void warp_inv32(const T (*A)[65], int o, T rinv, int 
     for (int i = 0; i < 32; i++) X[(o + j) * 65 + o + i] = x[i];
 }
 
+// One copy each of the unrolled 32 x 32 routines, called for both
+// diagonal sub-blocks of a 64 x 64 block: the executor runs them cold (one
+// diagonal step between many other tasks), and fetching a second inlined
+// copy of ~1,100 instructions cost more than the call.  chol32_block loads
+// lane i's row of the block at A[o + i][o + k] (k <= i, rows < n) into
+// registers, factors it (warp_chol32, S and Pv its scratch), stores it back
+// and leaves 1 / L(i,i) in rinv[i]; inv32_block forms the inverse from the
+// factor and rinv (warp_inv32).
+template <typename T>
+__device__ __noinline__ int chol32_block(T (*A)[65], int o, int n, T *rinv, T (*S)[33], T *Pv)
+{
+    const int lane = threadIdx.x & 31;
+    T row[32], r;
+#pragma unroll
+    for (int k = 0; k < 32; k++) row[k] = (lane < n && k <= lane) ? A[o + lane][o + k] : (T)0;
+    const int bad = warp_chol32<T>(row, r, n, S, Pv);
+    if (lane < n) {
+#pragma unroll
+        for (int k = 0; k < 32; k++)
+            if (k <= lane) A[o + lane][o + k] = row[k];
+    }
+    rinv[lane] = r;
+    return bad;
+}
+
+template <typename T>
+__device__ __noinline__ void inv32_block(const T (*A)[65], int o, const T *rinv, int n, T *X)
+{
+    warp_inv32<T>(A, o, rinv[threadIdx.x & 31], n, X);
+}
+
 // LL' and inverse of a 64 x 64 (nb <= 64) lower block in shared memory with
 // 256 threads, in 2 x 2 blocks of 32: A = [A11; A21 A22] (leading dimension
 // 65) is overwritten by L; X receives L^-1 (X[c*65 + r] = Linv(r, c), zeros
-// above the diagonal); Tm is scratch of 32 x 33 + 34 entries.
+// above the diagonal); Tm is scratch of 32 x 33 + 66 entries.
 //   L11 = chol(A11)                          (warp 0, registers)
 //   X11 = L11^-1                             (warp 1, meanwhile:)
 //   L21 = A21 L11^-T by substitution         (warp 2)
@@ -286,27 +317,18 @@ __device__ int potrf_inv64(T (*A)[65], T *X, T *Tm, int nb, int *sfail)
 {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n1 = min(32, nb), n2 = nb - n1;
-    T *rinv11 = Tm + 32 * 33;                   // 1 / L11(c, c)
+    T *rinv11 = Tm + 32 * 33, *rinv22 = rinv11 + 32, *Pv = rinv22 + 32;
     for (int idx = tid; idx < 64 * 65; idx += blockDim.x) X[idx] = (T)0;
     if (tid == 0) *sfail = -1;
     __syncthreads();
     if (warp == 0) {
-        T row[32], rinv;
-#pragma unroll
-        for (int k = 0; k < 32; k++) row[k] = (lane < n1 && k <= lane) ? A[lane][k] : (T)0;
-        const int bad = warp_chol32<T>(row, rinv, n1, (T (*)[33])Tm, Tm + 32 * 33 + 32);
-        if (lane < n1) {
-#pragma unroll
-            for (int k = 0; k < 32; k++)
-                if (k <= lane) A[lane][k] = row[k];
-        }
-        rinv11[lane] = rinv;
+        const int bad = chol32_block<T>(A, 0, n1, rinv11, (T (*)[33])Tm, Pv);
         if (lane == 0 && bad >= 0) *sfail = bad;
     }
     __syncthreads();
     const int f1 = *sfail, v1 = f1 >= 0 ? f1 : n1;
     if (warp == 1) {
-        warp_inv32<T>(A, 0, rinv11[lane], v1, X);
+        inv32_block<T>(A, 0, rinv11, v1, X);
     } else if (n2 > 0) {
         // warps 0 and 2-7 (224 threads, named barrier 1)
         const int t7 = warp == 0 ? lane : tid - 32;
@@ -344,17 +366,9 @@ __device__ int potrf_inv64(T (*A)[65], T *X, T *Tm, int nb, int *sfail)
             }
             asm volatile("bar.sync 1, 224;" ::: "memory");
             if (warp == 0) {
-                T row[32], rinv;
-#pragma unroll
-                for (int k = 0; k < 32; k++) row[k] = (lane < n2 && k <= lane) ? A[32 + lane][32 + k] : (T)0;
-                const int bad = warp_chol32<T>(row, rinv, n2, (T (*)[33])Tm, Tm + 32 * 33 + 32);
-                if (lane < n2) {
-#pragma unroll
-                    for (int k = 0; k < 32; k++)
-                        if (k <= lane) A[32 + lane][32 + k] = row[k];
-                }
+                const int bad = chol32_block<T>(A, 32, n2, rinv22, (T (*)[33])Tm, Pv);
                 __syncwarp();
-                warp_inv32<T>(A, 32, rinv, bad >= 0 ? bad : n2, X);
+                inv32_block<T>(A, 32, rinv22, bad >= 0 ? bad : n2, X);
                 if (lane == 0 && bad >= 0) *sfail = 32 + bad;
             }
         }
