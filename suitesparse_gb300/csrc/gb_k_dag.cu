@@ -438,17 +438,49 @@ __device__ __forceinline__ int fdag_instance(const gb_fdag_dev &D, int id)
     return lo;
 }
 
-static_assert(8 * warp_front_smem<32, float>() <= dag_smem<float>()
-              && 2 * warp_front_smem<64, float>() <= dag_smem<float>(), "one-warp fronts: shared memory");
+// One-warp fronts of a subtree wave: fdag_nw64 warps own a region for
+// fronts of up to 64 rows.  FP32: the other warps own regions for fronts of
+// up to 32 rows and both kinds run in one phase (fdag_merged); FP64: the
+// 32-row fronts (every warp) and the 64-row fronts run in two phases over
+// the same space.
+template <typename T>
+__host__ __device__ constexpr int fdag_nw64()
+{
+    return sizeof(T) == 4 ? 6 : 3;
+}
 
-// shared memory of the tensor-core executor: the tile tasks' space and the
-// operand stages of gemm_img_tc, and more than a third of the SM's 228 KB
-// so that at most 2 blocks (2 x GB_TC_COLS TMEM columns) share an SM
-#define GB_FDAG_TC_SMEM (100 * 1024)
-static_assert(GB_FDAG_TC_SMEM >= GB_TC_SMEM && GB_FDAG_TC_SMEM >= (int)dag_smem<float>()
-              && 3 * GB_FDAG_TC_SMEM > 228 * 1024, "tensor-core executor: shared memory");
-static_assert(8 * warp_front_smem<32, double>() <= dag_smem<double>()
-              && 2 * warp_front_smem<64, double>() <= dag_smem<double>(), "one-warp fronts: shared memory");
+template <typename T>
+__host__ __device__ constexpr bool fdag_merged()
+{
+    return sizeof(T) == 4;
+}
+
+template <typename T>
+__host__ __device__ constexpr size_t fdag_front_smem()
+{
+    return fdag_merged<T>()
+        ? fdag_nw64<T>() * warp_front_smem<64, T>() + (8 - fdag_nw64<T>()) * warp_front_smem<32, T>()
+        : (fdag_nw64<T>() * warp_front_smem<64, T>() > 8 * warp_front_smem<32, T>()
+               ? fdag_nw64<T>() * warp_front_smem<64, T>() : 8 * warp_front_smem<32, T>());
+}
+
+// dynamic shared memory of the executor: the tile tasks' space, the fronts'
+// regions and (FP32) the operand stages of gemm_img_tc
+template <typename T>
+__host__ __device__ constexpr size_t fdag_smem()
+{
+    return (sizeof(T) == 4 && (size_t)GB_TC_SMEM > fdag_front_smem<T>() && (size_t)GB_TC_SMEM > dag_smem<T>())
+        ? (size_t)GB_TC_SMEM
+        : (fdag_front_smem<T>() > dag_smem<T>() ? fdag_front_smem<T>() : dag_smem<T>());
+}
+
+// two blocks share an SM (228 KB, 1 KB reserved per block, the kernel's
+// static shared variables under 1 KB); with the tensor cores more than a
+// third of the SM's shared memory, so that no third block (2 x GB_TC_COLS
+// TMEM columns each) is resident
+static_assert(2 * (fdag_smem<float>() + 2048) <= 228 * 1024
+              && 2 * (fdag_smem<double>() + 2048) <= 228 * 1024, "executor: two blocks per SM");
+static_assert(3 * fdag_smem<float>() > 228 * 1024, "tensor-core executor: at most two blocks per SM");
 
 // All threads of the block, after a barrier that follows the work whose
 // results the successors read: release the block's writes, decrement the
@@ -491,12 +523,28 @@ __device__ void fdag_release(const gb_fdag_dev &D, const gb_fpat &PP, const gb_f
     __syncthreads();
 }
 
+// one front of at most MAXR rows on the calling warp, A's values in the
+// launch's precision
+template <int MAXR, typename T>
+__device__ __forceinline__ void fdag_warp_front(const gb_fdag_dev &D, const gb_finst &I, const gb_fpat &PP,
+                                                const gb_dev_pattern &P, int s, const double *scale, T *Lx,
+                                                T *CB, T *Linv, unsigned char *wsm)
+{
+    if (D.a_dtype == 0)
+        warp_front<MAXR, double, T>(P, s, PP.Sp, PP.Si, (const double *)D.Sx + I.sx, scale, D.beta, Lx,
+                                    CB, Linv, wsm);
+    else
+        warp_front<MAXR, float, T>(P, s, PP.Sp, PP.Si, (const float *)D.Sx + I.sx, scale, D.beta, Lx, CB,
+                                   Linv, wsm);
+}
+
 template <typename T, bool TC>
 __global__ void __launch_bounds__(256, 2)
 k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ int sid, sinst, sfail, spoll, snext;
+    __shared__ int sclaim[4];          // claim counters of subtree waves (two pairs)
     __shared__ __align__(8) uint64_t mbar[GB_TC_NBAR];
     __shared__ uint32_t tmem_base;
     if (threadIdx.x == 0) {
@@ -585,15 +633,23 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
             const double *scale = D.scale ? D.scale + I.scale : nullptr;
             const int warp = threadIdx.x >> 5;
             const bool node = tk.type == GB_DT_NODE;
-            // a wave [q, w3): fronts of at most 32 rows [q, w1), one warp each,
-            // eight at a time; fronts of at most warp_rows rows [w1, w2), one
-            // warp each in 64-row regions (NW64 at a time); others [w2, w3)
-            constexpr int NW64 = (int)(dag_smem<T>() / warp_front_smem<64, T>());
-            int q = 0, w1 = 0, w2 = 0, w3 = 1;
+            // a wave [q, w3): fronts of at most 32 rows [q, w1) and of at most
+            // warp_rows rows [w1, w2), one warp each; others [w2, w3).  FP32:
+            // one phase in which warps 0 .. NW64-1 take the 64-row fronts and
+            // then, like every other warp, the 32-row ones, each warp claiming
+            // the next front of a list; FP64: the 32-row fronts (eight at a
+            // time), a barrier, the 64-row fronts (NW64 at a time).
+            constexpr int NW64 = fdag_nw64<T>();
+            constexpr size_t WF64 = warp_front_smem<64, T>(), WF32 = warp_front_smem<32, T>();
+            int q = 0, w1 = 0, w2 = 0, w3 = 1, wave = 0;
             if (node) {
                 const int nr = (int)(P.Pi[tk.s + 1] - P.Pi[tk.s]);
                 w1 = nr <= min(PP.warp_rows, 32) ? 1 : 0;
                 w2 = nr <= PP.warp_rows ? 1 : 0;
+            }
+            if constexpr (fdag_merged<T>()) {
+                if (threadIdx.x == 0) sclaim[0] = sclaim[1] = 0;
+                __syncthreads();
             }
             while (q < (node ? 1 : tk.r)) {
                 if (!node) {
@@ -605,30 +661,52 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                         break;
                     }
                 }
-                for (int i = q + warp; i < w1; i += 8) {
-                    const int s = node ? tk.s : PP.sub_list[tk.b + i];
-                    unsigned char *wsm = smem_raw + (size_t)warp * warp_front_smem<32, T>();
-                    if (D.a_dtype == 0)
-                        warp_front<32, double, T>(P, s, PP.Sp, PP.Si, (const double *)D.Sx + I.sx, scale,
-                                                  D.beta, Lx, CB, Linv, wsm);
-                    else
-                        warp_front<32, float, T>(P, s, PP.Sp, PP.Si, (const float *)D.Sx + I.sx, scale,
-                                                 D.beta, Lx, CB, Linv, wsm);
-                }
-                if (w1 > q) __syncthreads();
-                if (warp < NW64) {
-                    for (int i = w1 + warp; i < w2; i += NW64) {
-                        const int s = node ? tk.s : PP.sub_list[tk.b + i];
-                        unsigned char *wsm = smem_raw + (size_t)warp * warp_front_smem<64, T>();
-                        if (D.a_dtype == 0)
-                            warp_front<64, double, T>(P, s, PP.Sp, PP.Si, (const double *)D.Sx + I.sx,
-                                                      scale, D.beta, Lx, CB, Linv, wsm);
-                        else
-                            warp_front<64, float, T>(P, s, PP.Sp, PP.Si, (const float *)D.Sx + I.sx,
-                                                     scale, D.beta, Lx, CB, Linv, wsm);
+                if constexpr (fdag_merged<T>()) {
+                    // claim counters of this wave: sclaim[2 (wave & 1) ..];
+                    // thread 0 clears the next wave's pair, which no warp
+                    // touches before this wave's barrier (a wave always has
+                    // one: the phase's, or the block fronts')
+                    int *c64 = sclaim + 2 * (wave & 1), *c32 = c64 + 1;
+                    if (threadIdx.x == 0) {
+                        sclaim[2 * ((wave + 1) & 1)] = 0;
+                        sclaim[2 * ((wave + 1) & 1) + 1] = 0;
                     }
+                    const int lane = threadIdx.x & 31;
+                    unsigned char *wsm = warp < NW64 ? smem_raw + (size_t)warp * WF64
+                                                     : smem_raw + NW64 * WF64 + (size_t)(warp - NW64) * WF32;
+                    if (warp < NW64 && w2 > w1) {
+                        for (;;) {
+                            int i = 0;
+                            if (lane == 0) i = atomicAdd(c64, 1);
+                            i = w1 + __shfl_sync(0xffffffffu, i, 0);
+                            if (i >= w2) break;
+                            fdag_warp_front<64, T>(D, I, PP, P, node ? tk.s : PP.sub_list[tk.b + i], scale,
+                                                   Lx, CB, Linv, wsm);
+                        }
+                    }
+                    if (w1 > q) {
+                        for (;;) {
+                            int i = 0;
+                            if (lane == 0) i = atomicAdd(c32, 1);
+                            i = q + __shfl_sync(0xffffffffu, i, 0);
+                            if (i >= w1) break;
+                            fdag_warp_front<32, T>(D, I, PP, P, node ? tk.s : PP.sub_list[tk.b + i], scale,
+                                                   Lx, CB, Linv, wsm);
+                        }
+                    }
+                    if (w2 > q) __syncthreads();
+                } else {
+                    for (int i = q + warp; i < w1; i += 8)
+                        fdag_warp_front<32, T>(D, I, PP, P, node ? tk.s : PP.sub_list[tk.b + i], scale, Lx,
+                                               CB, Linv, smem_raw + (size_t)warp * WF32);
+                    if (w1 > q) __syncthreads();
+                    if (warp < NW64) {
+                        for (int i = w1 + warp; i < w2; i += NW64)
+                            fdag_warp_front<64, T>(D, I, PP, P, node ? tk.s : PP.sub_list[tk.b + i], scale,
+                                                   Lx, CB, Linv, smem_raw + (size_t)warp * WF64);
+                    }
+                    if (w2 > w1) __syncthreads();
                 }
-                if (w2 > w1) __syncthreads();
                 for (int i = w2; i < w3; i++) {
                     const int s = node ? tk.s : PP.sub_list[tk.b + i];
                     const int nscol = (int)(P.Super[s + 1] - P.Super[s]);
@@ -654,6 +732,7 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                         }
                 }
                 q = w3;
+                wave++;
             }
         } else {
             if (tk.type == GB_DT_DIAG) {
@@ -725,19 +804,26 @@ int gb_launch_fdag(const gb_fdag_args *a, void *Lx, void *CB, void *Linv, int dt
     D.img = a->img;
     static int configured = 0;
     if (!configured) {
-        cudaFuncSetAttribute(k_fdag<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<double>());
-        cudaFuncSetAttribute(k_fdag<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<float>());
-        cudaFuncSetAttribute(k_fdag<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_FDAG_TC_SMEM);
+        cudaFuncSetAttribute(k_fdag<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fdag_smem<double>());
+        cudaFuncSetAttribute(k_fdag<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fdag_smem<float>());
+        cudaFuncSetAttribute(k_fdag<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fdag_smem<float>());
+        // the whole shared-memory carveout, so that two blocks fit an SM
+        cudaFuncSetAttribute(k_fdag<double, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+        cudaFuncSetAttribute(k_fdag<float, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+        cudaFuncSetAttribute(k_fdag<float, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
         configured = 1;
     }
     if (grid > a->ntotal + GB_DAG_POLLERS) grid = (int)(a->ntotal + GB_DAG_POLLERS);
     if (grid < GB_DAG_POLLERS + 1) grid = GB_DAG_POLLERS + 1;
     if (dtype == 0)
-        k_fdag<double, false><<<grid, 256, dag_smem<double>(), st>>>(D, (double *)Lx, (double *)CB, (double *)Linv);
+        k_fdag<double, false><<<grid, 256, fdag_smem<double>(), st>>>(D, (double *)Lx, (double *)CB, (double *)Linv);
     else if (D.use_tc)
-        k_fdag<float, true><<<grid, 256, GB_FDAG_TC_SMEM, st>>>(D, (float *)Lx, (float *)CB, (float *)Linv);
+        k_fdag<float, true><<<grid, 256, fdag_smem<float>(), st>>>(D, (float *)Lx, (float *)CB, (float *)Linv);
     else
-        k_fdag<float, false><<<grid, 256, dag_smem<float>(), st>>>(D, (float *)Lx, (float *)CB, (float *)Linv);
+        k_fdag<float, false><<<grid, 256, fdag_smem<float>(), st>>>(D, (float *)Lx, (float *)CB, (float *)Linv);
     return (int)cudaGetLastError();
 }
 
