@@ -386,16 +386,37 @@ __device__ __noinline__ void warp_front(const gb_dev_pattern &P, int s, const in
     }
 
     // 6. panel rows below: L21(r,c) = sum_{k<=c} A21(r,k) X(c,k), in place
-    // from the last column (A21(r,k), k <= c, is still unchanged)
+    // from the last column, four columns at a time (A21(r,k), k <= c, is
+    // still unchanged until the group's stores); each sum is formed from
+    // zero in k order, the four and the lane's rows side by side
     const int ncols = fail >= 0 ? fail : nscol;
+    for (int c0 = ncols - 1; c0 >= 0; c0 -= 4) {
+        T acc[MAXR / 32][4];
 #pragma unroll
-    for (int h = 0; h < MAXR; h += 32) {
-        const int r = lane + h;
-        if (r >= nscol && r < nsrow) {
-            for (int c = ncols - 1; c >= 0; c--) {
-                T acc = (T)0;
-                for (int k = 0; k <= c; k++) acc += F[k * LD + r] * (k == c ? xd[c] : F[c * LD + k]);
-                F[c * LD + r] = acc;
+        for (int h = 0; h < MAXR / 32; h++)
+#pragma unroll
+            for (int u = 0; u < 4; u++) acc[h][u] = (T)0;
+        for (int k = 0; k <= c0; k++) {
+            T a[MAXR / 32];
+#pragma unroll
+            for (int h = 0; h < MAXR / 32; h++) a[h] = F[k * LD + lane + 32 * h];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int c = c0 - u;
+                if (c >= 0 && k <= c) {
+                    const T x = k == c ? xd[c] : F[c * LD + k];
+#pragma unroll
+                    for (int h = 0; h < MAXR / 32; h++) acc[h][u] += a[h] * x;
+                }
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < MAXR / 32; h++) {
+            const int r = lane + 32 * h;
+            if (r >= nscol && r < nsrow) {
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (c0 - u >= 0) F[(c0 - u) * LD + r] = acc[h][u];
             }
         }
     }
@@ -405,16 +426,36 @@ __device__ __noinline__ void warp_front(const gb_dev_pattern &P, int s, const in
     for (int t = 0; t < nscol; t++)
         for (int r = lane; r < nsrow; r += 32)
             panel[r + (int64_t)t * nsrow] = r < t ? (T)0 : F[t * LD + r];
+    // update block C - L21 L21', four columns at a time; each sum formed
+    // from zero in k order
     T *cb = CB + P.cboff[s];
-    for (int j = nscol; j < nsrow; j++) {
+    for (int j0 = nscol; j0 < nsrow; j0 += 4) {
+        T acc[MAXR / 32][4];
 #pragma unroll
-        for (int h = 0; h < MAXR; h += 32) {
-            const int r = lane + h;
-            if (r >= j && r < nsrow) {
-                T acc = (T)0;
-                if (fail < 0)
-                    for (int k = 0; k < nscol; k++) acc += F[k * LD + r] * F[k * LD + j];
-                cb[(r - nscol) + (int64_t)(j - nscol) * m] = F[j * LD + r] - acc;
+        for (int h = 0; h < MAXR / 32; h++)
+#pragma unroll
+            for (int u = 0; u < 4; u++) acc[h][u] = (T)0;
+        if (fail < 0) {
+            for (int k = 0; k < nscol; k++) {
+                T a[MAXR / 32], b[4];
+#pragma unroll
+                for (int h = 0; h < MAXR / 32; h++) a[h] = F[k * LD + lane + 32 * h];
+#pragma unroll
+                for (int u = 0; u < 4; u++) b[u] = F[k * LD + min(j0 + u, MAXR)];
+#pragma unroll
+                for (int h = 0; h < MAXR / 32; h++)
+#pragma unroll
+                    for (int u = 0; u < 4; u++) acc[h][u] += a[h] * b[u];
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < MAXR / 32; h++) {
+            const int r = lane + 32 * h;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int j = j0 + u;
+                if (j < nsrow && r >= j && r < nsrow)
+                    cb[(r - nscol) + (int64_t)(j - nscol) * m] = F[j * LD + r] - acc[h][u];
             }
         }
     }
