@@ -28,6 +28,7 @@ struct gb_dq {
     int32_t *err;            // error word kept across launches
     int32_t *smflag;         // per SM: epoch of the launch whose poller runs there
     int32_t epoch;
+    int32_t npoll;           // blocks that serve only the critical queue
 };
 
 struct gb_dag_dev {
@@ -65,8 +66,6 @@ __device__ __forceinline__ int dag_add_acq_rel(int32_t *p, int v)
     return old;
 }
 
-#define GB_DAG_POLLERS 16   // blocks that serve only the critical-path queue
-
 // thread 0: claim slot h of a queue (the pusher reserved it with tail and
 // writes it right away, or will once the task is ready)
 __device__ int dag_take(const gb_dq &D, const int32_t *slots, int h)
@@ -83,7 +82,7 @@ __device__ int dag_take(const gb_dq &D, const int32_t *slots, int h)
 }
 
 // Thread 0: the next task id, -1 when its queue is exhausted, -2 on error.
-// The first GB_DAG_POLLERS blocks to start serve the critical-path queue:
+// The first D.npoll blocks to start serve the critical-path queue:
 // they claim a slot only when it is already reserved (compare-and-swap on
 // the head, no waiting for future tasks).  All other blocks claim bulk-queue
 // slots in order with atomicAdd and wait for their slot to be filled.
@@ -117,6 +116,38 @@ __device__ int dag_pop(const gb_dq &D, int poller)
     return -2;
 }
 
+// Thread 0 of a bulk block when no block is a dedicated poller
+// (D.npoll = 0): like dag_pop for a bulk block, but while its bulk slot is
+// empty the block takes any ready critical task instead, keeping the slot's
+// ticket (*ticket, -1 for none) for its next call.  Deadlock-free as
+// dag_pop: a ready critical task is taken by any waiting bulk block, and a
+// block whose bulk queue is exhausted serves the critical queue.
+__device__ int dag_pop_bulk(const gb_dq &D, int *ticket)
+{
+    int32_t *ctrl = D.ctrl;
+    if (*ticket < 0) {
+        const int h = atomicAdd(ctrl + 2, 1);
+        if (h >= ctrl[7]) return -1;
+        *ticket = h;
+    }
+    for (int k = 0; k < GB_DAG_SPIN; k++) {
+        const int v = dag_ld_acquire(D.q1 + *ticket);
+        if (v >= 0) {
+            *ticket = -1;
+            return v;
+        }
+        if (dag_ld_acquire(ctrl + 5)) return -2;
+        const int h0 = dag_ld_acquire(ctrl + 0);
+        if (h0 < dag_ld_acquire(ctrl + 6) && h0 < dag_ld_acquire(ctrl + 1)
+            && atomicCAS(ctrl + 0, h0, h0 + 1) == h0)
+            return dag_take(D, D.q0, h0);
+        __nanosleep(k < 64 ? 32 : 256);
+    }
+    atomicExch(ctrl + 5, 1);
+    atomicExch(D.err, 1);
+    return -2;
+}
+
 // warp 0: queue task v (its last dependency just finished) on the queue of
 // its priority
 __device__ __forceinline__ void dag_push(const gb_dq &D, int v, int prio)
@@ -141,21 +172,20 @@ __device__ void dag_complete(const gb_dag_dev &D, int id)
 }
 
 // thread 0 at the start of an executor block: 1 = poller, 0 = bulk block,
-// 2 = leave.  The first GB_DAG_POLLERS blocks to start serve the critical
-// queue and mark their SM.  The critical path is a chain of latency-bound
-// tasks, so a bulk block that finds itself on a marked SM leaves (at most
-// 2 GB_DAG_POLLERS of them, and only in a large grid, so that plenty of bulk
-// blocks remain).
+// 2 = leave.  The first D.npoll blocks to start serve the critical queue
+// and mark their SM.  The critical path is a chain of latency-bound tasks,
+// so a bulk block that finds itself on a marked SM leaves (at most 2 npoll
+// of them, and only in a large grid, so that plenty of bulk blocks remain).
 __device__ int dag_role(const gb_dq &D)
 {
-    int role = atomicAdd(D.ctrl + 4, 1) < GB_DAG_POLLERS;
+    int role = atomicAdd(D.ctrl + 4, 1) < D.npoll;
     unsigned smid;
     asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
     smid %= GB_DAG_NSMF;
     if (role) {
         atomicExch(D.smflag + smid, D.epoch);
-    } else if (gridDim.x >= 4 * GB_DAG_POLLERS && dag_ld_acquire(D.smflag + smid) == D.epoch
-               && atomicAdd(D.ctrl + 8, 1) < 2 * GB_DAG_POLLERS) {
+    } else if (D.npoll > 0 && gridDim.x >= 4 * D.npoll && dag_ld_acquire(D.smflag + smid) == D.epoch
+               && atomicAdd(D.ctrl + 8, 1) < 2 * D.npoll) {
         role = 2;
     }
     return role;
@@ -545,11 +575,13 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ int sid, sinst, sfail, spoll, snext;
     __shared__ int sclaim[4];          // claim counters of subtree waves (two pairs)
+    __shared__ int sticket;            // bulk slot held while serving critical tasks (npoll = 0)
     __shared__ __align__(8) uint64_t mbar[GB_TC_NBAR];
     __shared__ uint32_t tmem_base;
     if (threadIdx.x == 0) {
         spoll = dag_role(D.Q);
         snext = -1;
+        sticket = -1;
     }
     __syncthreads();
     if (spoll == 2) return;
@@ -588,7 +620,7 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                 sid = snext;
                 snext = -1;
             } else {
-                sid = dag_pop(D.Q, spoll);
+                sid = spoll || D.Q.npoll ? dag_pop(D.Q, spoll) : dag_pop_bulk(D.Q, &sticket);
                 if (sid == -1 && !spoll) {
                     spoll = 1;
                     sid = dag_pop(D.Q, 1);
@@ -796,7 +828,7 @@ int gb_launch_fdag(const gb_fdag_args *a, void *Lx, void *CB, void *Linv, int dt
     if (a->ntotal <= 0) return 0;
     gb_fdag_dev D;
     D.Q.q0 = a->q0; D.Q.q1 = a->q1; D.Q.ctrl = a->ctrl; D.Q.err = a->err;
-    D.Q.smflag = a->smflag; D.Q.epoch = a->epoch;
+    D.Q.smflag = a->smflag; D.Q.epoch = a->epoch; D.Q.npoll = a->npoll;
     D.pats = a->pats; D.inst = a->inst; D.ibase = a->inst_base; D.ninst = a->ninst;
     D.cnt = a->cnt; D.trace = a->trace;
     D.Sx = a->Sx; D.a_dtype = a->a_dtype; D.scale = a->scale; D.beta = a->beta;
@@ -836,7 +868,7 @@ int gb_launch_dag(const gb_pattern_ptrs *pp, const gb_dag_args *a, void *Lx, voi
     D.tasks = a->tasks; D.ntasks = a->ntasks; D.succ_ptr = a->succ_ptr; D.succ = a->succ;
     D.cnt = a->cnt; D.trace = a->trace;
     D.Q.q0 = a->q0; D.Q.q1 = a->q1; D.Q.ctrl = a->ctrl; D.Q.err = a->err;
-    D.Q.smflag = a->smflag; D.Q.epoch = a->epoch;
+    D.Q.smflag = a->smflag; D.Q.epoch = a->epoch; D.Q.npoll = GB_DAG_POLLERS;
     static int configured = 0;
     if (!configured) {
         cudaFuncSetAttribute(k_dag<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dag_smem<double>());

@@ -92,6 +92,7 @@ typedef struct { int32_t type, s, b, r, c, prio, nbk, pad1; } gb_dtask;
  * that left a poller's SM */
 #define GB_DAG_NCTRL 16
 #define GB_DAG_NSMF 1024    /* per-SM poller marks (indexed by %smid) */
+#define GB_DAG_POLLERS 16   /* blocks that serve only the critical-path queue */
 
 #define GB_NB 64            /* block size of the blocked paths */
 /* floats of one tensor-core operand image (a 64-row block of a 64-column

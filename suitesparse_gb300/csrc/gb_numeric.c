@@ -424,6 +424,7 @@ int gb_run_factor(gb_plan *P, gb_ctx *ctx, const void *Sx, int a_dtype, int l_dt
             a.use_tc = 0;
         }
         a.img = a.use_tc ? (float *)ctx->d_imgs : NULL;
+        a.npoll = P->fd_spread ? 0 : GB_DAG_POLLERS;
         if (ctx->trace_on) {
             size_t need = 3 * (N + 1) * sizeof(unsigned long long);
             if (gb_dev_grow((void **)&ctx->d_ftrace, &ctx->ftrace_cap, need)) {

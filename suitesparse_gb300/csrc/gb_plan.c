@@ -151,6 +151,18 @@ static int fdag_build(gb_plan *P)
             if (!elig[s]) elig[par] = 0;
         }
     }
+    /* work of each elimination tree (at its root): a forest in which no
+     * tree holds 5 % of the work (a batch of independent systems) has no
+     * long critical chain to keep blocks waiting for */
+    {
+        double wtot = 0, wmax = 0;
+        for (int64_t s = 0; ok && s < ns; s++)
+            if (P->h_parent[s] < 0) {
+                wtot += work[s];
+                if (work[s] > wmax) wmax = work[s];
+            }
+        P->fd_spread = ok && wmax < 0.05 * wtot;
+    }
 #define SUB_OK(s) (elig[s] && work[s] <= P->sub_work)
     for (int64_t s = ns - 1; ok && s >= 0; s--) {      /* parents before children */
         int32_t par = P->h_parent[s];

@@ -91,6 +91,8 @@ typedef struct {
     double beta;
     int use_tc;                      /* FP32 tile products on the tensor cores */
     float *img;                      /* their operand images (GB_IMG_FLOATS each) */
+    int npoll;                       /* blocks that serve only the critical queue (0: every
+                                      * block serves it while it waits for bulk work) */
 } gb_fdag_args;
 
 /* right-hand-side columns per single-launch sweep pass, and passes that run
@@ -172,6 +174,8 @@ typedef struct gb_plan {
      * assembly chunks, small supernodes, and two joins per supernode) */
     gb_vec fd_t, fd_sp, fd_succ, fd_nd, fd_q0, fd_q1, fd_sub, fd_smeta;
     int32_t fd_total0, fd_total1;
+    int fd_spread;                   /* no elimination tree holds 5 % of the work (a batch):
+                                      * no dedicated pollers (gb_fdag_args.npoll = 0) */
     gb_dtask *d_fd_t;
     int32_t *d_fd_sp, *d_fd_succ, *d_fd_nd, *d_fd_qi, *d_fd_ctrl0;
     int32_t *d_fd_cnt, *d_fd_q, *d_fd_sub, *d_fd_smeta;
