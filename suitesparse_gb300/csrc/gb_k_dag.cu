@@ -659,7 +659,7 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
             // wave by wave, children in earlier waves (SUBTREE).  A front of
             // at most warp_rows rows runs on one warp (a wave's such fronts
             // side by side, a warp each); any other runs on the whole block:
-            // assembly chunk by chunk, LL', then every update-block tile.  A
+            // assembly, LL', then every update-block tile.  A
             // parent reads its children's update blocks, written by this
             // block, after a barrier.
             const double *scale = D.scale ? D.scale + I.scale : nullptr;
@@ -744,8 +744,10 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                     const int nscol = (int)(P.Super[s + 1] - P.Super[s]);
                     const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
                     const int m = nsrow - nscol;
-                    for (int t0 = 0; t0 < nsrow; t0 += 64) {
-                        const gb_asm_task a = {s, t0, min(t0 + 64, nsrow), 0};
+                    {
+                        // every column at once (each entry still set from A,
+                        // then added to by the children in their order)
+                        const gb_asm_task a = {s, 0, nsrow, 0};
                         if (D.a_dtype == 0)
                             assemble_body<double, T>(P, a, PP.Sp, PP.Si, (const double *)D.Sx + I.sx,
                                                      scale, D.beta, Lx, CB);
