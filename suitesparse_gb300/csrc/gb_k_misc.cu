@@ -272,6 +272,17 @@ __global__ void k_anorm_seg(const gb_seg_chunk *__restrict__ chunks, const int64
         atomicMax((unsigned long long *)&out[ch.seg], gb_maxbits(sm[0]));
 }
 
+// R(rows of the chunk, every column) = 0 when the chunk's segment is marked
+// converged (act[seg] == 0): its correction is then zero
+__global__ void k_zero_inactive(const gb_seg_chunk *__restrict__ chunks, const unsigned char *__restrict__ act,
+                                double *R, int64_t ldr, int nrhs)
+{
+    const gb_seg_chunk ch = chunks[blockIdx.x];
+    if (act[ch.seg]) return;
+    for (int r = 0; r < nrhs; r++)
+        for (int64_t i = ch.lo + threadIdx.x; i < ch.hi; i += blockDim.x) R[i + r * ldr] = 0.0;
+}
+
 // dst[q] = src[map[q]] (device-side value permutation)
 __global__ void k_gather(int64_t n, const int64_t *__restrict__ map, const double *__restrict__ src,
                          double *__restrict__ dst)
@@ -664,6 +675,15 @@ int gb_launch_colmax3_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t ns
     if (nchunk <= 0 || nrhs <= 0) return 0;
     dim3 grid((unsigned)nchunk, (unsigned)nrhs);
     k_colmax3_seg<<<grid, 256, 0, st>>>(chunks, nrhs, R, ldr, X, ldx, B, ldb, out);
+    return (int)cudaGetLastError();
+}
+
+int gb_launch_zero_inactive(int64_t nchunk, const gb_seg_chunk *chunks, const unsigned char *act,
+                            double *R, int64_t ldr, int nrhs, cudaStream_t st)
+{
+    if (nchunk <= 0 || nrhs <= 0) return 0;
+    if (!chunks || !act || !R) return (int)cudaErrorInvalidValue;
+    k_zero_inactive<<<(unsigned)nchunk, 256, 0, st>>>(chunks, act, R, ldr, nrhs);
     return (int)cudaGetLastError();
 }
 

@@ -179,6 +179,9 @@ struct gb_sweep_state {
     unsigned long long *trace; // optional: per task [start, dependencies met, end] (ns)
     const int32_t *cptr;       // forward: child row ranges of each task (gb_plan.c)
     const int32_t *crange;
+    const unsigned char *act;  // optional: act[sseg[s]] == 0 skips supernode s's tasks
+    const int32_t *sseg;       // (independent systems already converged: no task of
+                               // another segment waits for them)
 };
 
 // dynamic shared memory: tile A, tile B (64 x TLD each), xs, ys (64 x RCH)
@@ -207,6 +210,7 @@ k_fwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
         const int tend = S.gptr[g + 1];
         for (int t = S.gptr[g]; t < tend; t++) {
         const gb_stask tk = S.tasks[t];
+        if (S.act && !S.act[S.sseg[tk.s]]) continue;
         if (S.trace && threadIdx.x == 0) S.trace[3 * (size_t)t] = gtimer();
         const int s = tk.s;
         const int64_t k1 = P.Super[s];
@@ -372,6 +376,7 @@ k_bwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
         const int tend = S.gptr[g + 1];
         for (int t = S.gptr[g]; t < tend; t++) {
         const gb_stask tk = S.tasks[t];
+        if (S.act && !S.act[S.sseg[tk.s]]) continue;
         if (S.trace && threadIdx.x == 0) S.trace[3 * (size_t)t] = gtimer();
         const int s = tk.s;
         const int64_t k1 = P.Super[s];
@@ -502,7 +507,8 @@ __global__ void __launch_bounds__(32 * LF_WARPS, 8)
 k_fwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
            const int32_t *__restrict__ blkoff, const int64_t *__restrict__ linvoff,
            const int32_t *__restrict__ ntask_f, int32_t *done, int32_t *ticket, const T *Lx,
-           const T *Linv, int nrhs, T *Y, int64_t ldy, T *U)
+           const T *Linv, int nrhs, T *Y, int64_t ldy, T *U, const unsigned char *act,
+           const int32_t *sseg)
 {
     constexpr unsigned FULL = 0xffffffffu;
     __shared__ T stage[LF_WARPS][2][64 * LF_LD];
@@ -510,6 +516,7 @@ k_fwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
     T *ys = stage[warp][0], *xs = stage[warp][1];
     for (int L = leaf_next(ticket); L < nleaf; L = leaf_next(ticket)) {
         const int s0 = leaf[2 * L], root = leaf[2 * L + 1];
+        if (act && !act[sseg[s0]]) continue;   // a converged system's subtree
         for (int s = s0; s <= root; s++) {
             const int64_t k1 = P.Super[s];
             const int nscol = (int)(P.Super[s + 1] - k1);
@@ -601,13 +608,15 @@ template <typename T>
 __global__ void __launch_bounds__(32 * LF_WARPS, 8)
 k_bwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
            const int32_t *__restrict__ blkoff, const int64_t *__restrict__ linvoff,
-           int32_t *ticket, const T *Lx, const T *Linv, int nrhs, T *Y, int64_t ldy)
+           int32_t *ticket, const T *Lx, const T *Linv, int nrhs, T *Y, int64_t ldy,
+           const unsigned char *act, const int32_t *sseg)
 {
     __shared__ T stage[LF_WARPS][2][64 * LF_LD];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     T *ys = stage[warp][0], *xs = stage[warp][1];
     for (int L = leaf_next(ticket); L < nleaf; L = leaf_next(ticket)) {
         const int s0 = leaf[2 * L], root = leaf[2 * L + 1];
+        if (act && !act[sseg[s0]]) continue;   // a converged system's subtree
         for (int s = root; s >= s0; s--) {
             const int64_t k1 = P.Super[s];
             const int nscol = (int)(P.Super[s + 1] - k1);
@@ -714,7 +723,9 @@ int gb_launch_sweep1(int forward, const gb_pattern_ptrs *pp, const gb_sweep1_arg
     S.ticket = a->ticket; S.err = a->err; S.trace = a->trace;
     S.gptr = a->gptr; S.ngroups = a->ngroups;
     S.cptr = a->cptr; S.crange = a->crange;
+    S.act = a->act; S.sseg = a->sseg;
     if (forward && (!S.cptr || !S.crange)) return (int)cudaErrorInvalidValue;
+    if (S.act && !S.sseg) return (int)cudaErrorInvalidValue;
     if (grid > a->ngroups) grid = a->ngroups;
     static int configured = 0;
     if (!configured) {
@@ -740,8 +751,9 @@ int gb_launch_sweep_leaf(int forward, const gb_pattern_ptrs *pp, const int32_t *
                          const int32_t *blkoff, const int64_t *linvoff, const int32_t *ntask_f,
                          int32_t *done, int32_t *ticket, const void *Lx, const void *Linv,
                          int dtype, int nrhs, void *Y, int64_t ldy, void *U, int grid,
-                         cudaStream_t st)
+                         const unsigned char *act, const int32_t *sseg, cudaStream_t st)
 {
+    if (act && !sseg) return (int)cudaErrorInvalidValue;
     if (nleaf <= 0) return 0;
     if (!leaf || !blkoff || !linvoff || !done || !ticket || !Lx || !Linv || !Y
         || (forward && (!ntask_f || !U)))
@@ -753,17 +765,21 @@ int gb_launch_sweep_leaf(int forward, const gb_pattern_ptrs *pp, const int32_t *
     if (dtype == 0) {
         if (forward)
             k_fwd_leaf<double><<<grid, 32 * LF_WARPS, 0, st>>>(P, leaf, nleaf, blkoff, linvoff, ntask_f, done, ticket,
-                                                               (const double *)Lx, (const double *)Linv, nrhs, (double *)Y, ldy, (double *)U);
+                                                               (const double *)Lx, (const double *)Linv, nrhs, (double *)Y, ldy, (double *)U,
+                                                               act, sseg);
         else
             k_bwd_leaf<double><<<grid, 32 * LF_WARPS, 0, st>>>(P, leaf, nleaf, blkoff, linvoff, ticket,
-                                                               (const double *)Lx, (const double *)Linv, nrhs, (double *)Y, ldy);
+                                                               (const double *)Lx, (const double *)Linv, nrhs, (double *)Y, ldy,
+                                                               act, sseg);
     } else {
         if (forward)
             k_fwd_leaf<float><<<grid, 32 * LF_WARPS, 0, st>>>(P, leaf, nleaf, blkoff, linvoff, ntask_f, done, ticket,
-                                                              (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy, (float *)U);
+                                                              (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy, (float *)U,
+                                                              act, sseg);
         else
             k_bwd_leaf<float><<<grid, 32 * LF_WARPS, 0, st>>>(P, leaf, nleaf, blkoff, linvoff, ticket,
-                                                              (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy);
+                                                              (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy,
+                                                              act, sseg);
     }
     return (int)cudaGetLastError();
 }

@@ -217,14 +217,31 @@ static int refine_step_launch(gb_plan *P, gb_ctx *ctx, int nrhs, int single)
     const Int n = P->n;
     const int ydt = single ? 4 : 0;
     const double *scale = single ? P->d_scale : NULL;
-    return gb_launch_perm_in(n, nrhs, P->d_Perm, scale, P->d_R, 0, n, P->d_Y, ydt, n, st) == 0
-           && gb_run_sweep(P, ctx, single ? CHOLMOD_SINGLE : CHOLMOD_DOUBLE, nrhs, P->d_Y, 1)
-           && gb_run_sweep(P, ctx, single ? CHOLMOD_SINGLE : CHOLMOD_DOUBLE, nrhs, P->d_Y, 0)
-           && gb_launch_perm_out(n, nrhs, P->d_Perm, scale, P->d_Y, ydt, n, P->d_X, 0, n, 1, st) == 0
+    /* a batch: the segments (independent systems) already at the tolerance
+     * (P->d_segact 0) get a zero correction, and the single-launch sweeps
+     * skip their tasks */
+    const int mask = P->d_segact != NULL;
+    int ok = !mask || gb_launch_zero_inactive(P->nchunk, P->d_chunk, P->d_segact, P->d_R, n, nrhs,
+                                              st) == 0;
+    P->sweep_act = mask ? P->d_segact : NULL;
+    ok = ok && gb_launch_perm_in(n, nrhs, P->d_Perm, scale, P->d_R, 0, n, P->d_Y, ydt, n, st) == 0
+         && gb_run_sweep(P, ctx, single ? CHOLMOD_SINGLE : CHOLMOD_DOUBLE, nrhs, P->d_Y, 1)
+         && gb_run_sweep(P, ctx, single ? CHOLMOD_SINGLE : CHOLMOD_DOUBLE, nrhs, P->d_Y, 0);
+    P->sweep_act = NULL;
+    return ok && gb_launch_perm_out(n, nrhs, P->d_Perm, scale, P->d_Y, ydt, n, P->d_X, 0, n, 1, st) == 0
            && gb_launch_residual(n, nrhs, P->d_Rp, P->d_Rj, P->d_Rx, P->d_X, n, P->d_bx, n,
                                  P->d_R, n, st) == 0
            && gb_launch_colmax3_seg(P->nchunk, P->d_chunk, P->nseg, nrhs, P->d_R, n, P->d_X, n,
                                     P->d_bx, n, P->d_bred, st) == 0;
+}
+
+/* every segment to be refined (the first step, and after an FP64 refactor) */
+static int segact_all(gb_plan *P, cudaStream_t st)
+{
+    if (!P->d_segact) return TRUE;
+    memset(P->h_segact, 1, (size_t)P->nseg);
+    return cudaMemcpyAsync(P->d_segact, P->h_segact, (size_t)P->nseg, cudaMemcpyHostToDevice, st)
+           == cudaSuccess;
 }
 
 void gb_graph_free(gb_plan *P)
@@ -326,7 +343,8 @@ static cholmod_dense *solve_refined_into(cholmod_sparse *A, cholmod_factor *L, c
     ok = ok && cudaMemcpy2DAsync(P->d_bx, sizeof(double) * n, B->x, sizeof(double) * B->d,
                                  sizeof(double) * n, nrhs, cudaMemcpyHostToDevice, st) == cudaSuccess
          && cudaMemsetAsync(P->d_X, 0, nb, st) == cudaSuccess
-         && cudaMemcpyAsync(P->d_R, P->d_bx, nb, cudaMemcpyDeviceToDevice, st) == cudaSuccess;
+         && cudaMemcpyAsync(P->d_R, P->d_bx, nb, cudaMemcpyDeviceToDevice, st) == cudaSuccess
+         && segact_all(P, st);
     cudaEventRecord(ctx->ev0, st);
     int it = 0, stall = 0;
     int32_t serr = 0;
@@ -347,6 +365,7 @@ static cholmod_dense *solve_refined_into(cholmod_sparse *A, cholmod_factor *L, c
         it++;
         berr_max = 0;
         int improved = 0, b_bad = 0;
+        if (P->h_segact) memset(P->h_segact, 0, (size_t)nsg);
         for (int64_t q = 0; q < nsg * nrhs; q++) {
             const double *h = hred + 3 * q;
             const double an = P->h_anorm_seg[q / nrhs];
@@ -357,6 +376,7 @@ static cholmod_dense *solve_refined_into(cholmod_sparse *A, cholmod_factor *L, c
                          && isfinite(den)) ? (den > 0 ? h[0] / den : 0) : NAN;
             if (be < best[q]) { if (be < 0.5 * best[q]) improved = 1; best[q] = be; }
             if (!(be <= berr_max)) berr_max = be;       /* keeps NaN */
+            if (P->h_segact && !(be <= tol)) P->h_segact[q / nrhs] = 1;
             if (!isfinite(h[2])) b_bad = 1;
             bmax_all = fmax(bmax_all, h[2]);
         }
@@ -367,9 +387,13 @@ static cholmod_dense *solve_refined_into(cholmod_sparse *A, cholmod_factor *L, c
         stall = improved ? 0 : stall + 1;
         if (stall >= 2) {
             if (P->mixed == 2) break;           /* FP64 factor cannot do better */
-            ok = factor_fp64(P, ctx, GB_REASON_STALLED, Common);
+            ok = factor_fp64(P, ctx, GB_REASON_STALLED, Common) && segact_all(P, st);
             stall = 0;
             if (info) info[2] = 1;
+        } else if (P->d_segact) {
+            /* the next step refines only the segments above the tolerance */
+            ok = cudaMemcpyAsync(P->d_segact, P->h_segact, (size_t)nsg, cudaMemcpyHostToDevice, st)
+                 == cudaSuccess;
         }
     }
     cudaEventRecord(ctx->ev1, st);

@@ -586,6 +586,8 @@ static int sweep_pass(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, i
     a.ticket = ticket;
     a.err = P->d_err;
     a.trace = NULL;
+    a.act = P->sweep_act;
+    a.sseg = P->d_sseg;
     if (allow_trace && ctx->trace_on) {
         size_t need = 3 * (size_t)(P->sf_t.n + P->sb_t.n + 2) * sizeof(unsigned long long);
         if (gb_dev_grow((void **)&ctx->d_trace, &ctx->trace_cap, need)) {
@@ -605,7 +607,7 @@ static int sweep_pass(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, i
     if (forward && nleaf > 0) {
         if (gb_launch_sweep_leaf(1, &P->ptrs, P->d_lf, nleaf, P->d_blkoff, P->d_linvoff,
                                  P->d_ntask_f, done, ticket + 1, Lx, P->d_Linv[d],
-                                 ldt, nrhs, Y, P->n, U, lgrid, st) != 0)
+                                 ldt, nrhs, Y, P->n, U, lgrid, P->sweep_act, P->d_sseg, st) != 0)
             return FALSE;
         ctx->launches += 1;
     }
@@ -618,7 +620,7 @@ static int sweep_pass(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, i
     if (!forward && nleaf > 0) {
         if (gb_launch_sweep_leaf(0, &P->ptrs, P->d_lf, nleaf, P->d_blkoff, P->d_linvoff,
                                  P->d_ntask_b, done, ticket + 1, Lx, P->d_Linv[d],
-                                 ldt, nrhs, Y, P->n, U, lgrid, st) != 0)
+                                 ldt, nrhs, Y, P->n, U, lgrid, P->sweep_act, P->d_sseg, st) != 0)
             return FALSE;
         ctx->launches += 1;
     }

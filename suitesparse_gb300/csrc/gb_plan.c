@@ -491,6 +491,22 @@ static int segments_build(gb_plan *P)
                 lo += GB_SEG_CHUNK;
             } while (lo < hi);
         }
+        /* the segment of each supernode (its first column's row of A), for
+         * refinement steps that skip converged segments */
+        if (P->nseg > 1) {
+            P->h_sseg = malloc(sizeof(int32_t) * (ns + 1));
+            P->h_segact = malloc((size_t)P->nseg);
+            if (!P->h_sseg || !P->h_segact) ok = 0;
+            for (Int s = 0; ok && s < ns; s++) {
+                const Int i = Perm ? Perm[Super[s]] : Super[s];
+                int64_t lo = 0, hi = P->nseg - 1;          /* last g with h_seg[g] <= i */
+                while (lo < hi) {
+                    const int64_t mid = (lo + hi + 1) / 2;
+                    if (P->h_seg[mid] <= i) lo = mid; else hi = mid - 1;
+                }
+                P->h_sseg[s] = (int32_t)lo;
+            }
+        }
         /* pinned, so that its copy from the device does not wait for the
          * stream (plain memory when no device is present) */
         if (cudaMallocHost((void **)&P->h_anorm_seg, sizeof(double) * P->nseg) == cudaSuccess) {
@@ -1430,6 +1446,11 @@ int gb_plan_upload(gb_plan *P)
     P->ptrs.linvoff = P->d_linvoff;
     P->ptrs.imgbase = P->d_imgbase;
     UP(P->d_chunk, P->h_chunk, sizeof(gb_seg_chunk) * P->nchunk);
+    if (P->h_sseg) {
+        UP(P->d_sseg, P->h_sseg, sizeof(int32_t) * P->nsuper);
+        if (cudaMalloc((void **)&P->d_segact, (size_t)P->nseg + 16) != cudaSuccess) goto fail;
+        P->struct_bytes += (size_t)P->nseg + 16;
+    }
     if (cudaMalloc((void **)&P->d_anorm_seg, sizeof(double) * (P->nseg + 1)) != cudaSuccess) goto fail;
     /* whole-factorization task graph, one instance */
     UP(P->d_fd_t, P->fd_t.p, P->fd_t.n * P->fd_t.esz);
@@ -1491,7 +1512,7 @@ void gb_plan_free(gb_plan *P)
     gb_vec_free(&P->dag_lv);
     gb_valmap_free(P);
     gb_graph_free(P);
-    free(P->h_seg); free(P->h_chunk);
+    free(P->h_seg); free(P->h_chunk); free(P->h_sseg); free(P->h_segact);
     if (P->anorm_pinned) cudaFreeHost(P->h_anorm_seg);
     else free(P->h_anorm_seg);
     gb_vec_free(&P->fd_t); gb_vec_free(&P->fd_sp); gb_vec_free(&P->fd_succ);
@@ -1512,7 +1533,8 @@ void gb_plan_free(gb_plan *P)
                    P->d_fd_sp, P->d_fd_succ, P->d_fd_nd, P->d_fd_qi, P->d_fd_ctrl0,
                    P->d_fd_cnt, P->d_fd_q, P->d_fd_pat, P->d_fd_inst, P->d_fd_ibase, P->d_fd_sub,
                    P->d_fd_smeta, P->d_imgbase,
-                   P->d_chunk, P->d_anorm_seg, P->d_bred, P->d_gf, P->d_gb};
+                   P->d_chunk, P->d_anorm_seg, P->d_bred, P->d_gf, P->d_gb, P->d_sseg,
+                   P->d_segact};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++)
         if (dev[i]) cudaFree(dev[i]);
     gb_vec_free(&P->asm_t); gb_vec_free(&P->node_t); gb_vec_free(&P->potrf_t);

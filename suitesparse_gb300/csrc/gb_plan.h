@@ -121,6 +121,8 @@ typedef struct {
     const int32_t *cptr;        /* forward: [ntasks+1] start of each task's child ranges */
     const int32_t *crange;      /* forward: per task and child (child_list order) the
                                  * child's update-vector rows [a, b) in the task's rows */
+    const unsigned char *act;   /* optional [nseg]: 0 = skip the segment's tasks */
+    const int32_t *sseg;        /* [nsuper] segment of each supernode (with act) */
 } gb_sweep1_args;
 
 /* growable host array */
@@ -250,6 +252,10 @@ typedef struct gb_plan {
     gb_seg_chunk *h_chunk;            /* row chunks of at most GB_SEG_CHUNK rows */
     gb_seg_chunk *d_chunk;
     double *h_anorm_seg, *d_anorm_seg, *d_bred;
+    int32_t *h_sseg, *d_sseg;         /* nseg > 1: [nsuper] segment of each supernode */
+    unsigned char *h_segact, *d_segact; /* [nseg] refinement: segment not yet converged */
+    const unsigned char *sweep_act;   /* set during refinement steps: sweeps skip the
+                                       * segments it marks 0 */
     int anorm_pinned;                 /* h_anorm_seg from cudaMallocHost */
     size_t bred_cap;
     /* CUDA graph of one refinement step (gb_mixed.c), per pattern: valid
@@ -397,6 +403,9 @@ int gb_launch_diag_scale(int64_t n, const int64_t *dmap, const double *Ax, const
                          double *scale, double *scale_perm, cudaStream_t st);
 int gb_launch_anorm_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t nseg, const int64_t *Rp,
                         const double *Rx, double *out, cudaStream_t st);
+/* R(rows of the segments act marks 0, every column) = 0 */
+int gb_launch_zero_inactive(int64_t nchunk, const gb_seg_chunk *chunks, const unsigned char *act,
+                            double *R, int64_t ldr, int nrhs, cudaStream_t st);
 int gb_launch_colmax3_seg(int64_t nchunk, const gb_seg_chunk *chunks, int64_t nseg, int nrhs,
                           const double *R, int64_t ldr, const double *X, int64_t ldx,
                           const double *B, int64_t ldb, double *out, cudaStream_t st);
@@ -418,7 +427,7 @@ int gb_launch_sweep_leaf(int forward, const gb_pattern_ptrs *pp, const int32_t *
                          const int32_t *blkoff, const int64_t *linvoff, const int32_t *ntask_f,
                          int32_t *done, int32_t *ticket, const void *Lx, const void *Linv,
                          int dtype, int nrhs, void *Y, int64_t ldy, void *U, int grid,
-                         cudaStream_t st);
+                         const unsigned char *act, const int32_t *sseg, cudaStream_t st);
 int gb_launch_diag_inverse(const gb_pattern_ptrs *pp, const gb_stask *dtasks, int ndiag,
                            const int32_t *blkoff, const int64_t *linvoff, const void *Lx,
                            void *Linv, int dtype, cudaStream_t st);

@@ -130,3 +130,48 @@ def test_batch_factor_solve_per_system(lib, oracle_mod, mixed):
     for L in Lpats + [Lb]:
         CH.free_factor(L, c)
     CH.free_sparse(Ab, c)
+
+
+@pytest.mark.gpu
+def test_batch_refinement_freezes_converged_systems(lib, oracle_mod):
+    """The refined solve of a batch refines only the systems still above the
+    tolerance: a system whose backward error is reached stops (its sweep
+    tasks are skipped, its correction is zero), so every system's solution
+    is the one its own refined solve gives, even beside a system that needs
+    more steps."""
+    nx = 24
+    mats = [M.laplace2d(nx, seed=31, lo=0.5, hi=2.0), M.laplace2d(nx, seed=32, lo=1e-5, hi=1e5, shift=0.0),
+            M.laplace2d(nx, seed=33, lo=0.5, hi=2.0), M.laplace2d(nx, seed=34, lo=1e-3, hi=1e3)]
+    n, Ap, Ai, _ = mats[0]
+    perm = _perm_rcm(n, Ap, Ai)
+    c = CH.Common()
+    alone, iters = [], []
+    for i, (n, p, ii, x) in enumerate(mats):
+        A = CH.sparse(n, p, ii, x, c)
+        L = CH.analyze_perm(A, perm, c)
+        assert CH.factorize_mixed(A, L, c) == 1
+        X, info = CH.solve_refined(A, L, M.rhs(n, 2, 40 + i), c, tol=1e-12)
+        assert info["berr"] <= 1e-12 and not info["fp64_fallback"]
+        alone.append(np.array(X, copy=True))
+        iters.append(info["iterations"])
+        CH.free_factor(L, c)
+        CH.free_sparse(A, c)
+    assert len(set(iters)) > 1, iters            # the systems need different step counts
+    A0 = CH.sparse(n, Ap, Ai, mats[0][3], c)
+    Lpat = CH.analyze_perm(A0, perm, c)
+    CH.free_sparse(A0, c)
+    Lb = CH.batch_analyze([Lpat], np.zeros(len(mats), dtype=np.int32), c)
+    nb, bp, bi, bx = M.block_diag_lower(mats)
+    Ab = CH.sparse(nb, bp, bi, bx, c)
+    B = np.vstack([M.rhs(n, 2, 40 + i) for i in range(len(mats))])
+    assert CH.factorize_mixed(Ab, Lb, c) == 1
+    X, info = CH.solve_refined(Ab, Lb, B, c, tol=1e-12)
+    assert info["iterations"] == max(iters) and info["berr"] <= 1e-12
+    for i, (n, p, ii, x) in enumerate(mats):
+        Xi = X[i * n:(i + 1) * n]
+        assert oracle_mod.backward_error(n, p, ii, x, Xi, B[i * n:(i + 1) * n]).max() <= 1e-12
+        # the batch's arithmetic for system i is its own: the same solution
+        assert np.array_equal(Xi, alone[i]), (i, iters, np.abs(Xi - alone[i]).max())
+    for L in (Lpat, Lb):
+        CH.free_factor(L, c)
+    CH.free_sparse(Ab, c)
