@@ -179,6 +179,8 @@ struct gb_sweep_state {
     unsigned long long *trace; // optional: per task [start, dependencies met, end] (ns)
     const int32_t *cptr;       // forward: child row ranges of each task (gb_plan.c)
     const int32_t *crange;
+    const int32_t *bchunk_ptr; // backward: per supernode and 64-row chunk of its rows
+    const int32_t *bchunk;     // below the diagonal block, the block of the chunk's first row
     const unsigned char *act;  // optional: act[sseg[s]] == 0 skips supernode s's tasks
     const int32_t *sseg;       // (independent systems already converged: no task of
                                // another segment waits for them)
@@ -386,51 +388,54 @@ k_bwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
         const int m = nsrow - nscol;
         const T *panel = Lx + P.Px[s];
         const int32_t *rows = P.Ls + psi + nscol;
-        const int par = S.parent[s];
         const int i = tk.idx, r0 = tk.r0, nr = tk.nr;
         const int nblk = (nscol + SR - 1) / SR;
+        const int nch = (m + SR - 1) / SR;
+        const int32_t *cblk = S.bchunk + S.bchunk_ptr[s];
         // the diagonal block's inverse, parked in tB before any wait
         tile_fetch(reg, Linv + S.linvoff[S.blkoff[s] + i], nr, nr, nr);
         tile_park(tB, reg);
-        // first L21 tile: rows nscol.., columns of block i
-        if (m > 0) tile_fetch(reg, panel + nscol + (int64_t)r0 * nsrow, nsrow, min(SR, m), nr);
-        if (threadIdx.x == 0 && par >= 0) {
-            if (!wait_ge(S.done + par, S.ntask_s[par], S.err)) abort_ = 1;
-        }
+        // the last L21 tile: rows of the farthest ancestors, final first
+        if (m > 0)
+            tile_fetch(reg, panel + nscol + (int64_t)(nch - 1) * SR + (int64_t)r0 * nsrow, nsrow,
+                       m - (nch - 1) * SR, nr);
         __syncthreads();
-        if (abort_) return;
         if (S.trace && threadIdx.x == 0) S.trace[3 * (size_t)t + 1] = gtimer();
         for (int k0 = 0; k0 < nrhs; k0 += RCH) {
             const int nk = min(RCH, nrhs - k0);
-            if (k0 > 0 && m > 0) tile_fetch(reg, panel + nscol + (int64_t)r0 * nsrow, nsrow, min(SR, m), nr);
+            if (k0 > 0 && m > 0)
+                tile_fetch(reg, panel + nscol + (int64_t)(nch - 1) * SR + (int64_t)r0 * nsrow, nsrow,
+                           m - (nch - 1) * SR, nr);
             for (int idx = threadIdx.x; idx < SR * RCH; idx += blockDim.x) {
                 const int r = idx / RCH, k = idx % RCH;
                 ys[idx] = (r < nr && k < nk) ? Y[k1 + r0 + r + (int64_t)(k0 + k) * ldy] : (T)0;
             }
-            // ys -= L21(:, blk i)' x(rows of s), 64 rows at a time: the next
-            // L tile and the next chunk's x (xv: this thread's 4 of the
-            // 64 x 16 entries, a gather through the row indices) are loaded
-            // while a chunk is used
+            // ys -= L21(:, blk i)' x(rows of s), 64 rows at a time from the
+            // last.  A chunk waits only for the diagonal block holding its
+            // first row: the chunk's other rows lie in later blocks of that
+            // supernode (final before it) or in its ancestors' blocks (rows
+            // of its own below its diagonal, final before any of its
+            // blocks), so the chunks of far ancestors are used while the
+            // nearer ones are still being solved.  The next L tile is loaded
+            // while a chunk is used; the chunk's x (xv: this thread's 4 of
+            // the 64 x 16 entries, a gather through the row indices) after
+            // its wait.
             T xv[4];
-            auto load_x = [&](int q0) {
+            for (int qc = nch - 1; qc >= 0; qc--) {
+                const int q0 = qc * SR, nq = min(SR, m - q0);
+                if (k0 == 0 && threadIdx.x == 0 && !wait_ge(S.xready + cblk[qc], 1, S.err)) abort_ = 1;
+                __syncthreads();
+                if (abort_) return;
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
                     const int idx = threadIdx.x + 256 * u, c = idx / RCH, k = idx % RCH;
                     xv[u] = (q0 + c < m && k < nk) ? Y[rows[q0 + c] + (int64_t)(k0 + k) * ldy] : (T)0;
                 }
-            };
-            if (m > 0) load_x(0);
-            for (int q0 = 0; q0 < m; q0 += SR) {
-                const int nq = min(SR, m - q0);
                 tile_park(tA, reg);
 #pragma unroll
                 for (int u = 0; u < 4; u++) xs[threadIdx.x + 256 * u] = xv[u];
                 __syncthreads();
-                if (q0 + SR < m) {
-                    tile_fetch(reg, panel + nscol + q0 + SR + (int64_t)r0 * nsrow, nsrow,
-                               min(SR, m - q0 - SR), nr);
-                    load_x(q0 + SR);
-                }
+                if (qc > 0) tile_fetch(reg, panel + nscol + q0 - SR + (int64_t)r0 * nsrow, nsrow, SR, nr);
                 tile_gemv<T>(tA, 1, nr, nq, xs, ys, nk, (T)-1);
             }
             // later diagonal blocks of s: ys -= L(blk j, blk i)' x_j
@@ -724,6 +729,8 @@ int gb_launch_sweep1(int forward, const gb_pattern_ptrs *pp, const gb_sweep1_arg
     S.gptr = a->gptr; S.ngroups = a->ngroups;
     S.cptr = a->cptr; S.crange = a->crange;
     S.act = a->act; S.sseg = a->sseg;
+    S.bchunk_ptr = a->bchunk_ptr; S.bchunk = a->bchunk;
+    if (!forward && (!S.bchunk_ptr || !S.bchunk)) return (int)cudaErrorInvalidValue;
     if (forward && (!S.cptr || !S.crange)) return (int)cudaErrorInvalidValue;
     if (S.act && !S.sseg) return (int)cudaErrorInvalidValue;
     if (grid > a->ngroups) grid = a->ngroups;

@@ -588,6 +588,8 @@ static int sweep_pass(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, i
     a.trace = NULL;
     a.act = P->sweep_act;
     a.sseg = P->d_sseg;
+    a.bchunk_ptr = P->d_bchunk_ptr;
+    a.bchunk = P->d_bchunk;
     if (allow_trace && ctx->trace_on) {
         size_t need = 3 * (size_t)(P->sf_t.n + P->sb_t.n + 2) * sizeof(unsigned long long);
         if (gb_dev_grow((void **)&ctx->d_trace, &ctx->trace_cap, need)) {

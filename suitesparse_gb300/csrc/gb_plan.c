@@ -1175,6 +1175,26 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
             ok &= gb_vec_push(&P->sd_t, &t);
         }
     }
+    /* backward sweep: per supernode, the global diagonal block holding the
+     * first row of each 64-row chunk of its rows below the diagonal block
+     * (the chunk's x is final when that block is) */
+    P->h_bchunk_ptr = ok ? malloc(sizeof(int32_t) * (nsuper + 1)) : NULL;
+    if (!P->h_bchunk_ptr) ok = 0;
+    int64_t nbchunk = 0;
+    for (Int s = 0; s < nsuper && ok; s++) {
+        P->h_bchunk_ptr[s] = (int32_t)nbchunk;
+        nbchunk += (Pi[s + 1] - Pi[s] - (Super[s + 1] - Super[s]) + 63) / 64;
+    }
+    if (ok) P->h_bchunk_ptr[nsuper] = (int32_t)nbchunk;
+    P->h_bchunk = ok ? malloc(sizeof(int32_t) * (nbchunk + 1)) : NULL;
+    if (!P->h_bchunk || nbchunk >= INT32_MAX) ok = 0;
+    for (Int s = 0; s < nsuper && ok; s++) {
+        Int nscol = Super[s + 1] - Super[s], m = Pi[s + 1] - Pi[s] - nscol;
+        for (Int q = 0; q < (m + 63) / 64; q++) {
+            const Int g = Ls[Pi[s] + nscol + 64 * q], a = SuperMap[g];
+            P->h_bchunk[P->h_bchunk_ptr[s] + q] = P->h_blkoff[a] + (int32_t)((g - Super[a]) / 64);
+        }
+    }
     /* leaf subtrees of the sweeps: maximal subtrees whose fronts all have at
      * most GB_LEAF_ROWS rows, at most GB_LEAF_MEMBERS supernodes each (none
      * when the one-warp fronts are off, warp_rows = 0).  One warp
@@ -1423,6 +1443,8 @@ int gb_plan_upload(gb_plan *P)
     UP(P->d_blkoff, P->h_blkoff, sizeof(int32_t) * (ns + 1));
     UP(P->d_ntask_f, P->h_ntask_f, sizeof(int32_t) * (ns + 1));
     UP(P->d_ntask_b, P->h_ntask_b, sizeof(int32_t) * (ns + 1));
+    UP(P->d_bchunk_ptr, P->h_bchunk_ptr, sizeof(int32_t) * (ns + 1));
+    UP(P->d_bchunk, P->h_bchunk, sizeof(int32_t) * (size_t)P->h_bchunk_ptr[ns]);
     UP(P->d_parent, P->h_parent, sizeof(int32_t) * (ns + 1));
     UP(P->d_linvoff, P->h_linvoff, sizeof(int64_t) * (P->nblk_total + 1));
     UP(P->d_imgbase, P->h_imgbase, sizeof(int64_t) * (ns + 1));
@@ -1501,6 +1523,7 @@ void gb_plan_free(gb_plan *P)
     free(P->h_child_ptr); free(P->h_child_list); free(P->h_relmap);
     free(P->h_cboff); free(P->h_cbvoff);
     free(P->h_blkoff); free(P->h_ntask_f); free(P->h_ntask_b); free(P->h_parent);
+    free(P->h_bchunk_ptr); free(P->h_bchunk);
     free(P->h_linvoff);
     free(P->h_imgbase);
     gb_vec_free(&P->sf_t); gb_vec_free(&P->sb_t); gb_vec_free(&P->sd_t);
@@ -1526,7 +1549,7 @@ void gb_plan_free(gb_plan *P)
                    P->d_Sp, P->d_Si, P->d_Sx, P->d_Y, P->d_U, P->d_B, P->d_spw, P->d_sws,
                    P->d_Rp, P->d_Rj, P->d_Rx, P->d_scale, P->d_scale_perm, P->d_X, P->d_R,
                    P->d_bx, P->d_red, P->d_sf, P->d_sb, P->d_sd, P->d_lf, P->d_sf_cptr, P->d_sf_crange, P->d_blkoff, P->d_ntask_f,
-                   P->d_ntask_b, P->d_parent, P->d_linvoff, P->d_xready, P->d_done,
+                   P->d_ntask_b, P->d_parent, P->d_bchunk_ptr, P->d_bchunk, P->d_linvoff, P->d_xready, P->d_done,
                    P->d_ticket, P->d_Linv[0], P->d_Linv[1], P->d_dag_t, P->d_dag_sp,
                    P->d_dag_succ, P->d_dag_nd, P->d_dag_q0i, P->d_dag_q1i, P->d_dag_ctrl0,
                    P->d_dag_cnt, P->d_dag_q, P->d_dag_ctrl, P->d_dag_smf, P->d_fd_t,

@@ -121,6 +121,7 @@ typedef struct {
     const int32_t *cptr;        /* forward: [ntasks+1] start of each task's child ranges */
     const int32_t *crange;      /* forward: per task and child (child_list order) the
                                  * child's update-vector rows [a, b) in the task's rows */
+    const int32_t *bchunk_ptr, *bchunk; /* backward: the block each row chunk waits for */
     const unsigned char *act;   /* optional [nseg]: 0 = skip the segment's tasks */
     const int32_t *sseg;        /* [nsuper] segment of each supernode (with act) */
 } gb_sweep1_args;
@@ -197,6 +198,9 @@ typedef struct gb_plan {
     gb_vec gf, gb;                    /* sweep task groups (forward, backward) */
     int32_t *d_gf, *d_gb;
     int32_t *d_blkoff, *d_ntask_f, *d_ntask_b, *d_parent;
+    int32_t *h_bchunk_ptr, *h_bchunk, *d_bchunk_ptr, *d_bchunk; /* backward sweep: per supernode
+                                      * and 64-row chunk below its diagonal, the block of the
+                                      * chunk's first row */
     int64_t *d_linvoff;
     int32_t *d_xready, *d_done, *d_ticket, *d_err;
     int32_t *h_blkoff, *h_ntask_f, *h_ntask_b, *h_parent;
