@@ -485,7 +485,8 @@ k_bwd_sweep(gb_dev_pattern P, gb_sweep_state S, const T *Lx, const T *Linv, int 
 
 // ---- leaf subtrees: one warp each ------------------------------------------
 // A leaf subtree (supernodes s0..root, contiguous in postorder, every front
-// at most 64 rows) is swept by one warp, rows r = lane and lane + 32, with no
+// at most GB_LEAF_ROWS rows and one diagonal block) is swept by one warp,
+// rows r = lane, lane + 32, ..., the front staged in shared memory, with no
 // waits: the forward sweep runs these before its other tasks (they depend on
 // nothing), the backward sweep after them (they depend only on their
 // ancestors' x, final by then).  Per supernode, forward:
@@ -513,12 +514,12 @@ k_fwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
            const int32_t *__restrict__ blkoff, const int64_t *__restrict__ linvoff,
            const int32_t *__restrict__ ntask_f, int32_t *done, int32_t *ticket, const T *Lx,
            const T *Linv, int nrhs, T *Y, int64_t ldy, T *U, const unsigned char *act,
-           const int32_t *sseg)
+           const int32_t *sseg, int lrows)
 {
     constexpr unsigned FULL = 0xffffffffu;
-    __shared__ T stage[LF_WARPS][2][64 * LF_LD];
+    extern __shared__ __align__(16) unsigned char lf_smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    T *ys = stage[warp][0], *xs = stage[warp][1];
+    T *ys = (T *)lf_smem + (size_t)(2 * warp) * lrows * LF_LD, *xs = ys + (size_t)lrows * LF_LD;
     for (int L = leaf_next(ticket); L < nleaf; L = leaf_next(ticket)) {
         const int s0 = leaf[2 * L], root = leaf[2 * L + 1];
         if (act && !act[sseg[s0]]) continue;   // a converged system's subtree
@@ -614,11 +615,11 @@ __global__ void __launch_bounds__(32 * LF_WARPS, 8)
 k_bwd_leaf(gb_dev_pattern P, const int32_t *__restrict__ leaf, int nleaf,
            const int32_t *__restrict__ blkoff, const int64_t *__restrict__ linvoff,
            int32_t *ticket, const T *Lx, const T *Linv, int nrhs, T *Y, int64_t ldy,
-           const unsigned char *act, const int32_t *sseg)
+           const unsigned char *act, const int32_t *sseg, int lrows)
 {
-    __shared__ T stage[LF_WARPS][2][64 * LF_LD];
+    extern __shared__ __align__(16) unsigned char lf_smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    T *ys = stage[warp][0], *xs = stage[warp][1];
+    T *ys = (T *)lf_smem + (size_t)(2 * warp) * lrows * LF_LD, *xs = ys + (size_t)lrows * LF_LD;
     for (int L = leaf_next(ticket); L < nleaf; L = leaf_next(ticket)) {
         const int s0 = leaf[2 * L], root = leaf[2 * L + 1];
         if (act && !act[sseg[s0]]) continue;   // a converged system's subtree
@@ -757,9 +758,21 @@ int gb_launch_sweep1(int forward, const gb_pattern_ptrs *pp, const gb_sweep1_arg
 int gb_launch_sweep_leaf(int forward, const gb_pattern_ptrs *pp, const int32_t *leaf, int nleaf,
                          const int32_t *blkoff, const int64_t *linvoff, const int32_t *ntask_f,
                          int32_t *done, int32_t *ticket, const void *Lx, const void *Linv,
-                         int dtype, int nrhs, void *Y, int64_t ldy, void *U, int grid,
+                         int dtype, int nrhs, void *Y, int64_t ldy, void *U, int grid, int lrows,
                          const unsigned char *act, const int32_t *sseg, cudaStream_t st)
 {
+    // staging of each warp's front (ys, xs: lrows x LF_LD each)
+    if (lrows < 1 || lrows > GB_LEAF_ROWS) return (int)cudaErrorInvalidValue;
+    static int configured = 0;
+    if (!configured) {
+        const int mx = (int)(LF_WARPS * 2 * GB_LEAF_ROWS * LF_LD * sizeof(double));
+        cudaFuncSetAttribute(k_fwd_leaf<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        cudaFuncSetAttribute(k_bwd_leaf<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        cudaFuncSetAttribute(k_fwd_leaf<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx / 2);
+        cudaFuncSetAttribute(k_bwd_leaf<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx / 2);
+        configured = 1;
+    }
+    const size_t lsm = (size_t)LF_WARPS * 2 * lrows * LF_LD * (dtype == 0 ? sizeof(double) : sizeof(float));
     if (act && !sseg) return (int)cudaErrorInvalidValue;
     if (nleaf <= 0) return 0;
     if (!leaf || !blkoff || !linvoff || !done || !ticket || !Lx || !Linv || !Y
@@ -771,22 +784,22 @@ int gb_launch_sweep_leaf(int forward, const gb_pattern_ptrs *pp, const int32_t *
     if (grid < 1) grid = 1;
     if (dtype == 0) {
         if (forward)
-            k_fwd_leaf<double><<<grid, 32 * LF_WARPS, 0, st>>>(P, leaf, nleaf, blkoff, linvoff, ntask_f, done, ticket,
+            k_fwd_leaf<double><<<grid, 32 * LF_WARPS, lsm, st>>>(P, leaf, nleaf, blkoff, linvoff, ntask_f, done, ticket,
                                                                (const double *)Lx, (const double *)Linv, nrhs, (double *)Y, ldy, (double *)U,
-                                                               act, sseg);
+                                                               act, sseg, lrows);
         else
-            k_bwd_leaf<double><<<grid, 32 * LF_WARPS, 0, st>>>(P, leaf, nleaf, blkoff, linvoff, ticket,
+            k_bwd_leaf<double><<<grid, 32 * LF_WARPS, lsm, st>>>(P, leaf, nleaf, blkoff, linvoff, ticket,
                                                                (const double *)Lx, (const double *)Linv, nrhs, (double *)Y, ldy,
-                                                               act, sseg);
+                                                               act, sseg, lrows);
     } else {
         if (forward)
-            k_fwd_leaf<float><<<grid, 32 * LF_WARPS, 0, st>>>(P, leaf, nleaf, blkoff, linvoff, ntask_f, done, ticket,
+            k_fwd_leaf<float><<<grid, 32 * LF_WARPS, lsm, st>>>(P, leaf, nleaf, blkoff, linvoff, ntask_f, done, ticket,
                                                               (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy, (float *)U,
-                                                              act, sseg);
+                                                              act, sseg, lrows);
         else
-            k_bwd_leaf<float><<<grid, 32 * LF_WARPS, 0, st>>>(P, leaf, nleaf, blkoff, linvoff, ticket,
+            k_bwd_leaf<float><<<grid, 32 * LF_WARPS, lsm, st>>>(P, leaf, nleaf, blkoff, linvoff, ticket,
                                                               (const float *)Lx, (const float *)Linv, nrhs, (float *)Y, ldy,
-                                                              act, sseg);
+                                                              act, sseg, lrows);
     }
     return (int)cudaGetLastError();
 }

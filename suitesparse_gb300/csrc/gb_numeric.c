@@ -609,7 +609,7 @@ static int sweep_pass(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, i
     if (forward && nleaf > 0) {
         if (gb_launch_sweep_leaf(1, &P->ptrs, P->d_lf, nleaf, P->d_blkoff, P->d_linvoff,
                                  P->d_ntask_f, done, ticket + 1, Lx, P->d_Linv[d],
-                                 ldt, nrhs, Y, P->n, U, lgrid, P->sweep_act, P->d_sseg, st) != 0)
+                                 ldt, nrhs, Y, P->n, U, lgrid, P->leaf_rows, P->sweep_act, P->d_sseg, st) != 0)
             return FALSE;
         ctx->launches += 1;
     }
@@ -622,7 +622,7 @@ static int sweep_pass(gb_plan *P, gb_ctx *ctx, int l_dtype, int nrhs, void *Y, i
     if (!forward && nleaf > 0) {
         if (gb_launch_sweep_leaf(0, &P->ptrs, P->d_lf, nleaf, P->d_blkoff, P->d_linvoff,
                                  P->d_ntask_b, done, ticket + 1, Lx, P->d_Linv[d],
-                                 ldt, nrhs, Y, P->n, U, lgrid, P->sweep_act, P->d_sseg, st) != 0)
+                                 ldt, nrhs, Y, P->n, U, lgrid, P->leaf_rows, P->sweep_act, P->d_sseg, st) != 0)
             return FALSE;
         ctx->launches += 1;
     }

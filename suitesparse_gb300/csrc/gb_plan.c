@@ -1196,7 +1196,8 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
         }
     }
     /* leaf subtrees of the sweeps: maximal subtrees whose fronts all have at
-     * most GB_LEAF_ROWS rows, at most GB_LEAF_MEMBERS supernodes each (none
+     * most GB_LEAF_ROWS rows and one diagonal block (at most 64 columns), at
+     * most GB_LEAF_MEMBERS supernodes each (none
      * when the one-warp fronts are off, warp_rows = 0).  One warp
      * sweeps a whole one (children first forward, parents first backward) in
      * a launch of its own, before the forward sweep's other tasks (a leaf
@@ -1206,7 +1207,8 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
     int32_t *lcnt = calloc(nsuper + 1, sizeof(int32_t));
     char *lel = malloc(nsuper + 1), *lmem = calloc(nsuper + 1, 1);
     if (!lcnt || !lel || !lmem) ok = 0;
-    for (Int s = 0; s < nsuper && ok; s++) lel[s] = P->warp_rows > 0 && Pi[s + 1] - Pi[s] <= GB_LEAF_ROWS;
+    for (Int s = 0; s < nsuper && ok; s++)
+        lel[s] = P->warp_rows > 0 && Pi[s + 1] - Pi[s] <= GB_LEAF_ROWS && Super[s + 1] - Super[s] <= 64;
     for (Int s = 0; s < nsuper && ok; s++) {          /* children before parents */
         lcnt[s] += 1;
         if (parent[s] != EMPTY) {
@@ -1224,7 +1226,10 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
         if (!contiguous) continue;
         int32_t pr[2] = {(int32_t)s0, (int32_t)s};
         ok &= gb_vec_push(&P->lf_t, pr);
-        for (Int q = s0; q <= s; q++) lmem[q] = 1;
+        for (Int q = s0; q <= s; q++) {
+            lmem[q] = 1;
+            P->leaf_rows = (int)GB_MAX(P->leaf_rows, Pi[q + 1] - Pi[q]);
+        }
     }
 #undef LEAF_OK
     /* forward: levels ascending; backward: levels descending, so that a task

@@ -100,7 +100,8 @@ typedef struct {
 #define GB_SWEEP_COLS 16
 #define GB_SWEEP_STREAMS 4
 #define GB_LEAF_MEMBERS 256        /* supernodes of a sweep leaf subtree */
-#define GB_LEAF_ROWS 64            /* rows of a front in a sweep leaf subtree */
+#define GB_LEAF_ROWS 128           /* rows of a front in a sweep leaf subtree (one
+                                    * diagonal block: at most 64 columns) */
 
 /* a chunk of rows of one segment, for segmented reductions */
 typedef struct { int64_t lo, hi; int32_t seg, pad; } gb_seg_chunk;
@@ -190,6 +191,7 @@ typedef struct gb_plan {
     /* single-launch sweeps: tasks, diagonal-block inverses, flags */
     gb_vec sf_t, sb_t, sd_t;          /* forward, backward, diagonal-block tasks */
     gb_vec lf_t;                      /* leaf subtrees of the sweeps: (first, root) */
+    int leaf_rows;                    /* most rows of a front in a leaf subtree */
     int32_t *d_lf;
     gb_vec sf_cptr, sf_crange;        /* forward tasks' child row ranges (gb_sweep1_args) */
     int32_t *d_sf_cptr, *d_sf_crange;
@@ -430,7 +432,7 @@ int gb_launch_sweep1(int forward, const gb_pattern_ptrs *pp, const gb_sweep1_arg
 int gb_launch_sweep_leaf(int forward, const gb_pattern_ptrs *pp, const int32_t *leaf, int nleaf,
                          const int32_t *blkoff, const int64_t *linvoff, const int32_t *ntask_f,
                          int32_t *done, int32_t *ticket, const void *Lx, const void *Linv,
-                         int dtype, int nrhs, void *Y, int64_t ldy, void *U, int grid,
+                         int dtype, int nrhs, void *Y, int64_t ldy, void *U, int grid, int lrows,
                          const unsigned char *act, const int32_t *sseg, cudaStream_t st);
 int gb_launch_diag_inverse(const gb_pattern_ptrs *pp, const gb_stask *dtasks, int ndiag,
                            const int32_t *blkoff, const int64_t *linvoff, const void *Lx,
