@@ -303,29 +303,47 @@ def nd_orderings(stream, workers=0):
             cache[d] = M.grid_nd_perm(d)
 
 
-def run_stream(server, stream, realtime=True, keep_x=None):
+def run_stream(server, stream, realtime=True, keep_x=None, producers=None):
     """Submit the stream (at its arrival times when realtime) from one
-    thread, collect every request's result in another.  A third thread makes
-    the requests' inputs ahead of their arrival (up to 64); a request whose
-    inputs are late arrives when they are ready.
+    thread, collect every request's result in another.  Producer threads
+    (``producers``, default half the host's cores, 2 to 8) make the
+    requests' inputs ahead of their arrival (at most 64 ahead; request i by
+    producer i mod producers; numpy releases the interpreter lock in the
+    array work, so they run side by side); a request whose inputs are late
+    arrives when they are ready.
     keep_x: request ids whose solution is kept in the records (all when
     None).  Returns the per-request records and the wall time."""
-    import queue
+    import os
     seen = set()
-    ready = queue.Queue(maxsize=64)       # inputs made ahead of their arrival
+    nprod = producers or min(8, max(2, (os.cpu_count() or 2) // 2))
+    made = {}                             # request index -> inputs
+    cond = threading.Condition()
+    next_i = [0]                          # the submitter's next request
 
-    def producer():
-        for rq in stream:
-            ready.put(request_inputs(rq))
+    def producer(t):
+        for i in range(t, len(stream), nprod):
+            with cond:
+                while i - next_i[0] >= 64:
+                    cond.wait()
+            inp = request_inputs(stream[i])
+            with cond:
+                made[i] = inp
+                cond.notify_all()
 
-    pt = threading.Thread(target=producer, daemon=True)
-    pt.start()
+    pts = [threading.Thread(target=producer, args=(t,), daemon=True) for t in range(nprod)]
+    for pt in pts:
+        pt.start()
     t0 = server.now()
     records = {}
 
     def submitter():
-        for rq in stream:
-            inp = ready.get()
+        for i, rq in enumerate(stream):
+            with cond:
+                while i not in made:
+                    cond.wait()
+                inp = made.pop(i)
+                next_i[0] = i + 1
+                cond.notify_all()
             if realtime:
                 delay = t0 + rq["t"] - server.now()
                 if delay > 0:
