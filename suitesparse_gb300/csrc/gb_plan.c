@@ -1197,7 +1197,7 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
     }
     /* leaf subtrees of the sweeps: maximal subtrees whose fronts all have at
      * most GB_LEAF_ROWS rows and one diagonal block (at most 64 columns), at
-     * most GB_LEAF_MEMBERS supernodes each (none
+     * most leaf_cap supernodes each (below; none
      * when the one-warp fronts are off, warp_rows = 0).  One warp
      * sweeps a whole one (children first forward, parents first backward) in
      * a launch of its own, before the forward sweep's other tasks (a leaf
@@ -1216,7 +1216,12 @@ gb_plan *gb_plan_build(const cholmod_factor *L, int64_t small_cols, double sub_w
             if (!lel[s]) lel[parent[s]] = 0;
         }
     }
-#define LEAF_OK(s) (lel[s] && lcnt[s] <= GB_LEAF_MEMBERS)
+    /* members per leaf subtree: up to GB_LEAF_MEMBERS in a large forest (a
+     * batch: many subtrees side by side, throughput), fewer in a small one
+     * (one warp sweeps a subtree serially: its length is the leaf phase's
+     * latency when there are few of them) */
+    const Int leaf_cap = GB_MAX(16, GB_MIN(GB_LEAF_MEMBERS, nsuper / 1024));
+#define LEAF_OK(s) (lel[s] && lcnt[s] <= leaf_cap)
     for (Int s = 0; s < nsuper && ok; s++) {
         if (!LEAF_OK(s) || (parent[s] != EMPTY && LEAF_OK(parent[s]))) continue;
         Int s0 = s - lcnt[s] + 1;
