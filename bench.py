@@ -42,7 +42,7 @@ CASE = "c2"
 # DRAM bytes (read + write) of one k_fdag<float, true> launch on c2, measured
 # by ncu (dram__bytes_read.sum 4.49e9 + dram__bytes_write.sum 6.15e9); the
 # command is in profiles/k_fdag_c2_dram_traffic.md
-K_FDAG_C2_DRAM_BYTES = 4.52e9 + 6.57e9
+K_FDAG_C2_DRAM_BYTES = 4.70e9 + 6.66e9
 METRIC = "factor TFLOP/s + solves/s at 1e-12 backward err, FP32+IR vs FP64; p50/p99"
 WORKLOAD = "c2: 3D 7-point variable-coefficient Laplacian 64^3 (n=262144), METIS"
 
