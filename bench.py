@@ -25,6 +25,7 @@ flush is needed between steps.
 """
 import argparse
 import ctypes
+import faulthandler
 import json
 import os
 import statistics
@@ -888,4 +889,6 @@ def main():
 
 
 if __name__ == "__main__":
+    # a fault in the library or a worker thread prints every thread's stack
+    faulthandler.enable(all_threads=True)
     sys.exit(main())
