@@ -283,6 +283,101 @@ static __device__ __noinline__ void trsm_task(const gb_dev_pattern &P, const gb_
     }
 }
 
+// The diagonal step's last update of tile (b, b) and its LL' and inverse in
+// one pass: C = A(b, b) - sum over the panels p of the update (tk.r ..
+// tk.r + tk.nbk - 1) of L(b, p) L(b, p)', formed on the CUDA cores (each
+// thread 4 x 4 entries of the tile, one 64-column panel staged in shared
+// memory at a time) straight into the shared tile that potrf_inv64
+// factors, so the tile makes no round trip through global memory between
+// the update and the factorization.  The products are summed from zero and
+// subtracted from A(b, b) once (subtracting each product in turn loses
+// accuracy in the pivots).  The tile is the whole 64-row row block
+// b: when panel b is narrower than 64, its rows below the diagonal block
+// (read later by that row block's panel solve) are updated too and stored
+// back.  Stores L(b, b) and its inverse as potrf_task does.  Skipped for a
+// supernode that already failed.
+template <typename T>
+static __device__ __noinline__ void diag_update_potrf(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx,
+                                                      T *Linv, unsigned char *smem_raw, int &sfail)
+{
+    T (*A)[65] = (T (*)[65])smem_raw;
+    T *S1 = (T *)smem_raw + 64 * 65, *S2 = S1 + 64 * 65;
+    const int s = tk.s, b = tk.b;
+    const int nscol = (int)(P.Super[s + 1] - P.Super[s]);
+    const int nsrow = (int)(P.Pi[s + 1] - P.Pi[s]);
+    if (P.fail[s] >= 0) return;
+    T *panel = Lx + P.Px[s];
+    const int c0 = 64 * b, nb = min(64, nscol - c0), mr = min(64, nsrow - c0);
+    const int p0 = tk.r, nbk = max(1, tk.nbk);
+    T *blk = panel + c0 + (int64_t)c0 * nsrow;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    T acc[4][4], cv[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int i = ty + 16 * a, j = tx + 16 * q;
+            cv[a][q] = (i < mr && j < nb && i >= j) ? blk[i + (int64_t)j * nsrow] : (T)0;
+            acc[a][q] = (T)0;
+        }
+    for (int p = p0; p < p0 + nbk; p++) {
+        const int kc = min(64, nscol - 64 * p);
+        // S1[k * 65 + i] = L(c0 + i, 64 p + k); every load in flight first
+        T v[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int idx = threadIdx.x + 256 * q, i = idx & 63, k = idx >> 6;
+            v[q] = (i < mr && k < kc) ? panel[c0 + i + (int64_t)(64 * p + k) * nsrow] : (T)0;
+        }
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int idx = threadIdx.x + 256 * q;
+            S1[(idx >> 6) * 65 + (idx & 63)] = v[q];
+        }
+        __syncthreads();
+        for (int k = 0; k < kc; k++) {
+            T x[4], y[4];
+#pragma unroll
+            for (int a = 0; a < 4; a++) x[a] = S1[k * 65 + ty + 16 * a];
+#pragma unroll
+            for (int q = 0; q < 4; q++) y[q] = S1[k * 65 + tx + 16 * q];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) acc[a][q] += x[a] * y[q];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[a][q] = cv[a][q] - acc[a][q];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int i = ty + 16 * a, j = tx + 16 * q;
+            A[i][j] = (i < nb && j < nb && i >= j) ? acc[a][q] : (T)0;
+            if (i >= nb && i < mr && j < nb) blk[i + (int64_t)j * nsrow] = acc[a][q];
+        }
+    __syncthreads();
+    const int fl = potrf_inv64<T>(A, S1, S2, nb, &sfail);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+        const int i = idx % nb, j = idx / nb;
+        if (i >= j) blk[i + (int64_t)j * nsrow] = A[i][j];
+    }
+    if (fl >= 0 && threadIdx.x == 0) {
+        P.fail[s] = c0 + fl;
+        atomicExch(P.anyfail, 1);
+    }
+    T *li = Linv + P.linvoff[P.blkoff[s] + b];
+    for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+        const int i = idx % nb, j = idx / nb;
+        li[i + (int64_t)j * nb] = S1[j * 65 + i];
+    }
+}
+
 // The work of one tile task (POTRF, TRSM, UPD or CB) of supernode tk.s.
 // smem_raw: dag_smem<T>() bytes (GB_TC_SMEM with tc).  With tc and Img
 // (FP32 on the tensor cores), TRSM also writes the split operand images and
@@ -398,12 +493,7 @@ __device__ void dag_tile_task(const gb_dev_pattern &P, const gb_dtask &tk, T *Lx
     tile_body<T>(P, t1, Lx, CB, Linv, smem_raw, sfail, tc, Img);
     __syncthreads();
     if (tc && !tc->ok) return;
-    const gb_dtask t2 = {GB_DT_UPD, tk.s, tk.r, tk.b, tk.b, 0, tk.nbk, 0};
-    tile_body<T>(P, t2, Lx, CB, Linv, smem_raw, sfail, tc, Img);
-    __syncthreads();
-    if (tc && !tc->ok) return;
-    const gb_dtask t3 = {GB_DT_POTRF, tk.s, tk.b, 0, 0, 0, 0, 0};
-    tile_body<T>(P, t3, Lx, CB, Linv, smem_raw, sfail, tc, Img);
+    diag_update_potrf<T>(P, tk, Lx, Linv, smem_raw, sfail);
 }
 
 template <typename T>
@@ -780,17 +870,7 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
                 __syncthreads();
                 fdag_release(D, PP, I, PP.succ_ptr[local], PP.succ_ptr[local] + tk.pad1, false,
                              &snext);
-                if (!TC || !tc || tcx.ok) {
-                    const gb_dtask t2 = {GB_DT_UPD, tk.s, tk.r, tk.b, tk.b, 0, tk.nbk, 0};
-                    tile_body<T>(P, t2, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr,
-                                 TC ? D.img : nullptr);
-                    __syncthreads();
-                }
-                if (!TC || !tc || tcx.ok) {
-                    const gb_dtask t3 = {GB_DT_POTRF, tk.s, tk.b, 0, 0, 0, 0, 0};
-                    tile_body<T>(P, t3, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr,
-                                 TC ? D.img : nullptr);
-                }
+                if (!TC || !tc || tcx.ok) diag_update_potrf<T>(P, tk, Lx, Linv, smem_raw, sfail);
             } else {
                 dag_tile_task<T>(P, tk, Lx, CB, Linv, smem_raw, sfail, TC ? tc : nullptr,
                                  TC ? D.img : nullptr);
