@@ -614,13 +614,25 @@ static_assert(3 * fdag_smem<float>() > 228 * 1024, "tensor-core executor: at mos
 __device__ void fdag_release(const gb_fdag_dev &D, const gb_fpat &PP, const gb_finst &I, int ea,
                              int eb, bool keep, int *snext)
 {
-    if (ea + (int)threadIdx.x < eb) __threadfence();
-    for (int e = ea + (int)threadIdx.x; e < eb; e += (int)blockDim.x) {
-        const int v = PP.succ[e];
+    // the successor lists and the successors' type and priority are plan
+    // data, never written by the launch: a thread's first successor is
+    // read before the fence, so those loads overlap the fence instead of
+    // adding two round trips after it
+    const int e0 = ea + (int)threadIdx.x;
+    int v0 = -1, ty0 = 0, pr0 = 0;
+    if (e0 < eb) {
+        v0 = PP.succ[e0];
+        ty0 = PP.tasks[v0].type;
+        pr0 = PP.tasks[v0].prio;
+        __threadfence();
+    }
+    for (int e = e0; e < eb; e += (int)blockDim.x) {
+        const bool first = e == e0;
+        const int v = first ? v0 : PP.succ[e];
         const int g = (int)(I.base + v);
         if (dag_add_acq_rel(D.cnt + g, -1) != 1) continue;
-        if (PP.tasks[v].type != GB_DT_JOIN) {
-            const int prio = PP.tasks[v].prio;
+        if ((first ? ty0 : PP.tasks[v].type) != GB_DT_JOIN) {
+            const int prio = first ? pr0 : PP.tasks[v].prio;
             if (prio == 0 && keep && atomicCAS(snext, -1, g) == -1) {
                 atomicSub(D.Q.ctrl + 6, 1);     // kept: one less to queue
                 continue;
