@@ -629,7 +629,9 @@ int gb300_get_trace (cholmod_common *Common, int forward, unsigned long long *ou
     int64_t nmax) ;
 
 /* Per-task trace of the last traced factorization's task graphs (all
- * levels, plan order): out[3t..3t+2] = claimed, finished (ns), block. */
+ * levels, plan order): out[3t..3t+2] = claimed, finished (ns), block
+ * (with the one-launch factorization: the SM id in the high 32 bits, the
+ * block index in the low 32). */
 int gb300_get_factor_trace (cholmod_common *Common, unsigned long long *out,
     int64_t nmax) ;
 

@@ -734,8 +734,10 @@ k_fdag(gb_fdag_dev D, T *LxB, T *CBB, T *LinvB)
         const int id = sid;
         if (id < 0) break;
         if (D.trace && threadIdx.x == 0) {
+            unsigned smid;
+            asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
             D.trace[3 * (size_t)id] = dag_timer();
-            D.trace[3 * (size_t)id + 2] = blockIdx.x;
+            D.trace[3 * (size_t)id + 2] = ((unsigned long long)smid << 32) | blockIdx.x;
         }
         const gb_finst I = D.inst[sinst];
         const gb_fpat &PP = D.pats[I.pat];
